@@ -1,0 +1,240 @@
+"""Benchmark: cell-updates/s of the full FP64 time step on one GB300.
+
+Workload (the 256x128x128 case the metric is quoted on): two-phase Couette flow
+with contact lines, density and viscosity ratio 10, perturbed x-stripe
+interface, 60 deg walls, dt=2e-5 -- in reference axis order (ni, nj_wall, nk) =
+(256, 128, 128).  One "step" is one full time step (main.f90:473-697).
+value = interior cells x timed steps / device time (CUDA events on the
+library's stream, device-resident state).  e2e = the same through the C-ABI with
+host buffers: every step uploads the 12 state fields from pinned host memory,
+steps, and downloads them.
+
+`--impl reference` times the CPU restatement of the reference's algorithm
+(oracle/, the reference Fortran cannot be built here: no Fortran compiler) on
+the host cores, same workload and metric.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(REPO, "fel-multi-phase-flow_gb300"))
+sys.path.insert(0, os.path.join(REPO, "oracle"))
+
+WORKLOAD = "couette256"
+METRIC = "cell-updates/s/step plain FP64 vs mixed at stated error; adjoint/forward cost"
+UNIT = "cell-updates/s"
+
+
+def _peaks():
+    try:
+        with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as f:
+            return json.load(f), "measured"
+    except Exception:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region (clocks, throttle reasons)."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self):
+        self.p = None
+        self.path = os.path.join(REPO, "gpurun_out", "clocks_bench.csv")
+
+    def start(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.f = open(self.path, "w")
+            self.p = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                                       "-lms", "200", "-i", os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0]],
+                                      stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.p = None
+
+    def stop(self):
+        if not self.p:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        self.p.wait()
+        self.f.close()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, val in zip(names, parts[5:9]):
+                if val.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_baseline_sample(cfg, steps=1):
+    """The oracle (C++/OpenMP restatement, all host threads) on a bounded sample."""
+    import oracle
+    from fmf import config as C
+    s = oracle.Solver(cfg)
+    st = s.initial_state()
+    s.step(st, 1)  # warm
+    t0 = time.perf_counter()
+    s.step(st, steps)
+    dt = time.perf_counter() - t0
+    return cfg.cells * steps / dt, dt
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    from fmf import config as C
+    cfg = C.get(WORKLOAD)
+    import oracle
+    s = oracle.Solver(cfg)
+    st = s.initial_state()
+    s.step(st, args.warmup)
+    t0 = time.perf_counter()
+    s.step(st, args.steps)
+    dt = time.perf_counter() - t0
+    v = cfg.cells * args.steps / dt
+    cores = os.cpu_count()
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic",
+            "config": {"workload": f"{WORKLOAD} 256x128x128 (ni,nj_wall,nk)", "precision": "fp64"},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": f"{args.steps} full steps of {WORKLOAD} after {args.warmup} warm-up "
+                                       "steps; the reference Fortran cannot be built here (no Fortran "
+                                       "compiler), so its C++/OpenMP restatement oracle/fmf_oracle.cpp runs"},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="fmf", choices=["fmf", "reference"])
+    ap.add_argument("--workload", default=WORKLOAD)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+
+    import numpy as np
+    import torch
+
+    from fmf import build as fbuild
+    from fmf import capi
+    from fmf import config as C
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    fbuild.build()
+    L = capi.load()
+    cfg = C.get(args.workload)
+    stream = torch.cuda.Stream()
+    g = capi.Stepper(cfg, stream=stream.cuda_stream)
+    st = g.initial_state()
+    g.step(args.warmup)
+    g.sync()
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+
+    clocks = Clocks()
+    barrier()
+    clocks.start()
+    l0 = L.fmf_kernel_launches()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    g.step(args.steps)
+    e1.record(stream)
+    e1.synchronize()
+    launches = L.fmf_kernel_launches() - l0
+    ms = e0.elapsed_time(e1)
+    barrier()
+    clk = clocks.stop()
+    iters = g.sor_iterations()
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * cfg.cells * args.steps / (ms * 1e-3)
+
+    # e2e: host buffers through the C-ABI, upload + step + download every step
+    pinned = torch.empty((12,) + cfg.shape, dtype=torch.float64, pin_memory=True)
+    host = pinned.numpy()
+    host[:] = g.get_state()
+    bytes_field = cfg.shape[0] * cfg.shape[1] * cfg.shape[2] * 8
+    e2e_steps = max(1, min(args.steps, 5))
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        g.upload(host)
+        g.step(1)
+        g.download(host)
+        g.sync()
+    e2e_dt = time.perf_counter() - t0
+    e2e_value = world * cfg.cells * e2e_steps / e2e_dt
+
+    # dominant-stage roofline: WENO5 advection (stage 0), algorithmic bytes 6 words per cell
+    ms_stage = ctypes.c_float()
+    capi.check(L.fmf_ctx_time_stage(g.h, 0, 5, ctypes.byref(ms_stage)), "time_stage")
+    peaks, peak_kind = _peaks()
+    weno_bytes = 6 * 8 * cfg.cells
+    achieved = weno_bytes / (ms_stage.value * 1e-3) / 1e9
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                "frac": achieved / peaks["hbm_gbs"], "traffic": None,
+                "kernel": "cal_advu_weno5 (one call: u,v,w -> adv_u,adv_v,adv_w)",
+                "kernel_ms": ms_stage.value, "peak_source": peak_kind}
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        v, dt = cpu_baseline_sample(cfg, 1)
+        cpu = {"value": v, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+               "sample": f"1 full step of {args.workload} after 1 warm-up step ({dt:.1f} s), oracle/fmf_oracle.cpp "
+                         "C++/OpenMP restatement, all host threads"}
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                "config": {"workload": f"{args.workload} {cfg.ni}x{cfg.nj}x{cfg.nk} (ni,nj_wall,nk)",
+                           "precision": "fp64", "l2": "inputs larger than L2 (state + work arrays ~GBs/step)",
+                           "sor_iterations_mean": float(np.mean(iters)) if iters else None,
+                           "parallelism": "replicas" if world > 1 else "single"},
+                "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 12 * bytes_field,
+                        "d2h_bytes_per_step": 12 * bytes_field},
+                "gpu_launches": int(launches), "clocks": clk, "roofline": roofline, "cpu_baseline": cpu}
+        print(json.dumps(line), flush=True)
+    g.close()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,575 @@
+// capi.cu -- the drop-in C-ABI (include/fmf_capi.h, parts 1 and 2).
+#include <cmath>
+#include <cstring>
+
+#include "../../include/fmf_capi.h"
+#include "ops.cuh"
+#include "runtime.cuh"
+
+using namespace fmf;
+
+namespace {
+inline long n3(int ni, int nj, int nk) { return (long)(ni + 6) * (nj + 6) * (nk + 6); }
+bool check_grid(int ni, int nj, int nk) {
+  auto p2 = [](int n) { return n >= 4 && (n & (n - 1)) == 0; };
+  if (!p2(ni) || !p2(nj) || !p2(nk)) {
+    set_status(FMF_ERR_ARG);
+    return false;
+  }
+  return true;
+}
+bool one_rank(const int* ipara) {
+  if (ipara && *ipara != 0) {
+    set_status(FMF_ERR_UNSUPPORTED);
+    return false;
+  }
+  return true;
+}
+bool walls_only(const int* nID) {
+  // one GPU holds the whole domain: both wall neighbours must be absent
+  if (nID && (nID[1] >= 0 || nID[4] >= 0)) {
+    set_status(FMF_ERR_UNSUPPORTED);
+    return false;
+  }
+  return true;
+}
+// dyinv_array(dis), dis = j + nj*ID for j in -2..nj+2 (cal_grad_p2a.f:34-36): the device
+// kernels take one dy; a non-uniform array is reported as unsupported.
+bool uniform_dy(const double* a, int ID, int nj, double* out) {
+  const double* base = a + 2 + (long)nj * ID;
+  const double v = base[-2];
+  for (int j = -2; j <= nj + 2; ++j)
+    if (base[j] != v) {
+      set_status(FMF_ERR_UNSUPPORTED);
+      return false;
+    }
+  *out = v;
+  return true;
+}
+int g_last_sor_iters = 0;
+double g_last_sor_ratio = 0.0;
+}  // namespace
+
+#define GRID3 \
+  if (!check_grid(*ni, *nj, *nk)) return; \
+  const Grid g(*ni, *nj, *nk);            \
+  const long N3 = g.n;                    \
+  cudaStream_t s = stream();              \
+  Call call;
+
+extern "C" {
+
+int fmf_last_error(void) { return take_status(); }
+const char* fmf_error_string(int code) {
+  switch (code) {
+    case FMF_OK: return "ok";
+    case FMF_ERR_CUDA: return "CUDA runtime error";
+    case FMF_ERR_ARG: return "invalid argument";
+    case FMF_ERR_NONFINITE: return "non-finite value in a reduction";
+    case FMF_ERR_ITER_CAP: return "SOR iteration cap reached";
+    case FMF_ERR_NOMEM: return "device allocation failed";
+    case FMF_ERR_UNSUPPORTED: return "unsupported on the one-GPU build";
+    default: return "unknown error";
+  }
+}
+int fmf_set_mode(int m) {
+  if (m != FMF_RESIDENT && m != FMF_COHERENT) return FMF_ERR_ARG;
+  set_mode(m);
+  return 0;
+}
+int fmf_set_stream(void* st) {
+  set_stream((cudaStream_t)st);
+  return 0;
+}
+int fmf_sync_to_host(void* p) { return sync_to_host(p, 0); }
+int fmf_sync_to_device(void* p) { return sync_to_device(p, 0); }
+int fmf_sync_all_to_host(void) { return sync_all_to_host(); }
+int fmf_forget(void* p) { return forget(p); }
+int fmf_reset(void) { return reset_registry(); }
+int fmf_device_synchronize(void) {
+  FMF_CUDA(cudaStreamSynchronize(stream()));
+  return take_status();
+}
+long long fmf_kernel_launches(void) { return launches(); }
+int fmf_last_sor_iterations(void) { return g_last_sor_iters; }
+double fmf_last_sor_ratio(void) { return g_last_sor_ratio; }
+
+// ---------------------------------------------------------------- C1
+void cal_grad_p2a_(int* ID, int* svall, int* ni, int* nj, int* nk, double* dxinv, double* dyinv_array,
+                   double* dzinv, double* q, double* qx, double* qy, double* qz) {
+  (void)svall;
+  GRID3;
+  double dy;
+  if (!uniform_dy(dyinv_array, *ID, *nj, &dy)) return;
+  op::cal_grad_p2a(s, g, *dxinv, dy, *dzinv, call.in(q, N3), call.out(qx, N3), call.out(qy, N3), call.out(qz, N3));
+  call.finish();
+}
+void solphi_mthinc1_(int* ni, int* nj, int* nk, double* dxinv, double* dyinv, double* dzinv, double* dt,
+                     double* bet, double* phi, double* phix, double* phiy, double* phiz, double* u, double* v,
+                     double* w, double* flx, double* fly, double* flz) {
+  GRID3;
+  op::solphi_mthinc1(s, g, *dxinv, *dyinv, *dzinv, *dt, *bet, call.in(phi, N3), call.in(phix, N3),
+                     call.in(phiy, N3), call.in(phiz, N3), call.in(u, N3), call.in(v, N3), call.in(w, N3),
+                     call.out(flx, N3), call.out(fly, N3), call.out(flz, N3));
+  call.finish();
+}
+void solphi_mthinc2_(int* ni, int* nj, int* nk, double* dxinv, double* dyinv, double* dzinv, double* dt,
+                     double* u, double* v, double* w, double* flx, double* fly, double* flz, double* phi,
+                     double* phin) {
+  GRID3;
+  op::solphi_mthinc2(s, g, *dxinv, *dyinv, *dzinv, *dt, call.in(u, N3), call.in(v, N3), call.in(w, N3),
+                     call.in(flx, N3), call.in(fly, N3), call.in(flz, N3), call.in(phi, N3), call.out(phin, N3));
+  call.finish();
+}
+void solphi_mthinc3_(int* ipara, int* ni, int* nj, int* nk, double* dxinv, double* dyinv, double* dzinv,
+                     double* bet, double* phix, double* phiy, double* phiz, double* phi, double* phin) {
+  if (!one_rank(ipara)) return;
+  GRID3;
+  double* sums = (double*)scratch(sizeof(double) * 4, 2);
+  op::solphi_mthinc3(s, g, *dxinv, *dyinv, *dzinv, *bet, call.in(phix, N3), call.in(phiy, N3),
+                     call.in(phiz, N3), call.in(phi, N3), call.out(phin, N3), sums);
+  call.finish();
+}
+void summation_(int* ni, int* nj, int* nk, double* qk, int* nbub) {
+  GRID3;
+  if (*nbub != 1) {
+    set_status(FMF_ERR_UNSUPPORTED);
+    return;
+  }
+  double* d = call.out(qk, 2 * N3);
+  op::summation(s, g, d, d + N3);
+  call.finish();
+}
+
+// ---------------------------------------------------------------- C5
+void gnbc_(int* nID, int* ni, int* nj, int* nk, double* uk, double* wk, double* uwall, double* theta0,
+           double* sigma, double* zeta, double* theta) {
+  if (!walls_only(nID)) return;
+  GRID3;
+  op::gnbc(s, g, call.in(uk, N3), call.in(wk, N3), *uwall, call.in(theta0, N3), *sigma, call.in(zeta, N3),
+           call.out(theta, N3));
+  call.finish();
+}
+void bnd_contact_angle_(int* nID, int* ni, int* nj, int* nk, double* qk, double* theta, double* dx, double* dy,
+                        double* dz) {
+  if (!walls_only(nID)) return;
+  GRID3;
+  op::bnd_contact_angle(s, g, call.out(qk, N3), call.in(theta, N3), *dx, *dy, *dz);
+  call.finish();
+}
+void bndu_(int* nID, int* ni, int* nj, int* nk, double* uk, double* vk, double* wk, double* uwall, double* dy,
+           double* l1, double* l2, double* phi) {
+  if (!walls_only(nID)) return;
+  GRID3;
+  op::bndu(s, g, call.out(uk, N3), call.out(vk, N3), call.out(wk, N3), *uwall, *dy, call.in(l1, N3),
+           call.in(l2, N3), call.in(phi, N3));
+  call.finish();
+}
+void bnd_periodic_(int* ni, int* nj, int* nk, double* qk) {
+  GRID3;
+  op::bnd_periodic(s, g, call.out(qk, N3));
+  call.finish();
+}
+void bnd_neumann_(int* nID, int* ni, int* nj, int* nk, double* qk) {
+  if (!walls_only(nID)) return;
+  GRID3;
+  op::bnd_neumann(s, g, call.out(qk, N3));
+  call.finish();
+}
+void bnd_comm_(int* ipara, int*, int*, int*, int*, int*, double*, double*, double*) { one_rank(ipara); }
+
+// ---------------------------------------------------------------- C2
+void cal_advu_weno5_(int* ni, int* nj, int* nk, double* dxinv, double* dyinv, double* dzinv, double* u,
+                     double* v, double* w, double* au, double* av, double* aw) {
+  GRID3;
+  op::cal_advu_weno5(s, g, *dxinv, *dyinv, *dzinv, call.in(u, N3), call.in(v, N3), call.in(w, N3),
+                     call.out(au, N3), call.out(av, N3), call.out(aw, N3));
+  call.finish();
+}
+
+// ---------------------------------------------------------------- C6
+void cal_arith_mean_(int* ni, int* nj, int* nk, double* phik, double* ql, double* qg, double* qk) {
+  GRID3;
+  op::cal_arith_mean(s, g, call.in(phik, N3), *ql, *qg, call.out(qk, N3));
+  call.finish();
+}
+void cal_harm_mean_(int* ni, int* nj, int* nk, double* phik, double* ql, double* qg, double* qk) {
+  GRID3;
+  op::cal_harm_mean(s, g, call.in(phik, N3), *ql, *qg, call.out(qk, N3));
+  call.finish();
+}
+void calphat_(int* ni, int* nj, int* nk, double* p, double* po, double* phat) {
+  GRID3;
+  op::calphat(s, g, call.in(p, N3), call.in(po, N3), call.out(phat, N3));
+  call.finish();
+}
+void cal_grad_prs_(int* ni, int* nj, int* nk, double* dxinv, double* dyinv, double* dzinv, double* q,
+                   double* qx, double* qy, double* qz) {
+  GRID3;
+  op::cal_grad_prs(s, g, *dxinv, *dyinv, *dzinv, call.in(q, N3), call.out(qx, N3), call.out(qy, N3),
+                   call.out(qz, N3));
+  call.finish();
+}
+void calsij_(int* ni, int* nj, int* nk, double* dxinv, double* dyinv, double* dzinv, double* uk, double* vk,
+             double* wk, double* sk) {
+  GRID3;
+  op::calsij(s, g, *dxinv, *dyinv, *dzinv, call.in(uk, N3), call.in(vk, N3), call.in(wk, N3),
+             call.out(sk, 6 * N3));
+  call.finish();
+}
+void cal_arith_tau_(int* ni, int* nj, int* nk, double* sk, double* rmu, double* tau) {
+  GRID3;
+  op::cal_tau(s, g, call.in(sk, 6 * N3), call.in(rmu, N3), call.out(tau, 6 * N3), false);
+  call.finish();
+}
+void cal_harm_tau_(int* ni, int* nj, int* nk, double* sk, double* rmu, double* tau) {
+  GRID3;
+  op::cal_tau(s, g, call.in(sk, 6 * N3), call.in(rmu, N3), call.out(tau, 6 * N3), true);
+  call.finish();
+}
+void cal_div_tensor_(int* ni, int* nj, int* nk, double* dxinv, double* dyinv, double* dzinv, double* tau,
+                     double* uk, double* vk, double* wk) {
+  GRID3;
+  op::cal_div_tensor(s, g, *dxinv, *dyinv, *dzinv, call.in(tau, 6 * N3), call.out(uk, N3), call.out(vk, N3),
+                     call.out(wk, N3));
+  call.finish();
+}
+void calrn_(int* ni, int* nj, int* nk, double* dxinv, double* dyinv, double* dzinv, int* ip, int* jp, int* kp,
+            double* phix, double* phiy, double* phiz, double* rn) {
+  GRID3;
+  if (*ip < 0 || *ip > 1 || *jp < 0 || *jp > 1 || *kp < 0 || *kp > 1) {
+    set_status(FMF_ERR_ARG);
+    return;
+  }
+  op::calrn(s, g, *dxinv, *dyinv, *dzinv, *ip, *jp, *kp, call.in(phix, N3), call.in(phiy, N3),
+            call.in(phiz, N3), call.out(rn, 3 * N3));
+  call.finish();
+}
+void calrkap_(int* ni, int* nj, int* nk, double* dxinv, double* dyinv, double* dzinv, double* rpp,
+              double* r12, double* r13, double* r23, double* rkap) {
+  GRID3;
+  op::calrkap(s, g, *dxinv, *dyinv, *dzinv, call.in(rpp, 3 * N3), call.in(r12, 3 * N3), call.in(r13, 3 * N3),
+              call.in(r23, 3 * N3), call.out(rkap, 3 * N3));
+  call.finish();
+}
+void cal_grad_p2uvw_(int* ID, int* svall, int* ni, int* nj, int* nk, double* dxinv, double* dyinv_array,
+                     double* dzinv, double* q, double* qx, double* qy, double* qz) {
+  (void)svall;
+  GRID3;
+  double dy;
+  if (!uniform_dy(dyinv_array, *ID, *nj, &dy)) return;
+  op::cal_grad_prs(s, g, *dxinv, dy, *dzinv, call.in(q, N3), call.out(qx, N3), call.out(qy, N3),
+                   call.out(qz, N3));
+  call.finish();
+}
+void calfst_(int* ni, int* nj, int* nk, double* rhol, double* rhog, double* sigma, double* gx, double* gy,
+             double* gz, double* rkap, double* fu, double* fv, double* fw) {
+  GRID3;
+  op::calfst(s, g, *rhol, *rhog, *sigma, call.in(gx, N3), call.in(gy, N3), call.in(gz, N3),
+             call.in(rkap, 3 * N3), call.out(fu, N3), call.out(fv, N3), call.out(fw, N3));
+  call.finish();
+}
+void sum_fst_(int* ni, int* nj, int* nk, double* fu, double* fv, double* fw, double* su, double* sv,
+              double* sw) {
+  GRID3;
+  op::sum_fst(s, g, call.in(fu, N3), call.in(fv, N3), call.in(fw, N3), call.out(su, N3), call.out(sv, N3),
+              call.out(sw, N3));
+  call.finish();
+}
+void init_q_(int* ni, int* nj, int* nk, double* q1, double* q2, double* q3) {
+  GRID3;
+  op::fill(s, N3, call.out(q1, N3), 0.0);
+  op::fill(s, N3, call.out(q2, N3), 0.0);
+  op::fill(s, N3, call.out(q3, N3), 0.0);
+  call.finish();
+}
+void cal_av_(int* ipara, int* ndiv, int* ni, int* nj, int* nk, double* q, double* av) {
+  if (!one_rank(ipara)) return;
+  (void)ndiv;
+  GRID3;
+  double* d = (double*)scratch(sizeof(double) * 2, 3);
+  op::cal_av(s, g, call.in(q, N3), d);
+  FMF_CUDA(cudaMemcpyAsync(av, d, sizeof(double), cudaMemcpyDeviceToHost, s));
+  FMF_CUDA(cudaStreamSynchronize(s));
+  if (!std::isfinite(*av)) set_status(FMF_ERR_NONFINITE);
+  call.finish();
+}
+void cal_srcu_(int* nID, int* ni, int* nj, int* nk, double* rho_av, double* dt, double* grvb, double* grvp,
+               double* u, double* v, double* w, double* rho, double* rhon, double* adv_u, double* adv_v,
+               double* adv_w, double* adv_uo, double* adv_vo, double* adv_wo, double* prs_u, double* prs_v,
+               double* prs_w, double* vis_u, double* vis_v, double* vis_w, double* fst_u, double* fst_v,
+               double* fst_w, double* fst_un, double* fst_vn, double* fst_wn, double* src_u, double* src_v,
+               double* src_w) {
+  (void)rho_av;
+  if (!walls_only(nID)) return;
+  GRID3;
+  const double* adv[3] = {call.in(adv_u, N3), call.in(adv_v, N3), call.in(adv_w, N3)};
+  const double* advo[3] = {call.in(adv_uo, N3), call.in(adv_vo, N3), call.in(adv_wo, N3)};
+  const double* prs[3] = {call.in(prs_u, N3), call.in(prs_v, N3), call.in(prs_w, N3)};
+  const double* vis[3] = {call.in(vis_u, N3), call.in(vis_v, N3), call.in(vis_w, N3)};
+  const double* fst[3] = {call.in(fst_u, N3), call.in(fst_v, N3), call.in(fst_w, N3)};
+  const double* fstn[3] = {call.in(fst_un, N3), call.in(fst_vn, N3), call.in(fst_wn, N3)};
+  double* src[3] = {call.out(src_u, N3), call.out(src_v, N3), call.out(src_w, N3)};
+  op::cal_srcu(s, g, *dt, *grvb, *grvp, call.in(u, N3), call.in(v, N3), call.in(w, N3), call.in(rho, N3),
+               call.in(rhon, N3), adv, advo, prs, vis, fst, fstn, src);
+  call.finish();
+}
+void cpy_(int* ni, int* nj, int* nk, double* q1, double* q2) {
+  GRID3;
+  op::copy(s, N3, call.in(q1, N3), call.out(q2, N3));
+  call.finish();
+}
+
+// ---------------------------------------------------------------- C3
+static void coef_vis_impl(int* ni, int* nj, int* nk, double* dxinv, double* dyinv, double* dzinv, double* rmu,
+                          double** c45, bool harmonic) {
+  GRID3;
+  double* d[45];
+  for (int q = 0; q < 45; ++q) d[q] = call.out(c45[q], N3);
+  op::cal_coef_vis(s, g, *dxinv, *dyinv, *dzinv, call.in(rmu, N3), d, harmonic);
+  call.finish();
+}
+#define C45_PARAMS                                                                                        \
+  double *a0, double *a1, double *a2, double *a3, double *a4, double *a5, double *a6, double *a7,          \
+      double *a8, double *a9, double *a10, double *a11, double *a12, double *a13, double *a14, double *a15, \
+      double *a16, double *a17, double *a18, double *a19, double *a20, double *a21, double *a22,            \
+      double *a23, double *a24, double *a25, double *a26, double *a27, double *a28, double *a29,            \
+      double *a30, double *a31, double *a32, double *a33, double *a34, double *a35, double *a36,            \
+      double *a37, double *a38, double *a39, double *a40, double *a41, double *a42, double *a43, double *a44
+#define C45_ARRAY                                                                                         \
+  {a0,  a1,  a2,  a3,  a4,  a5,  a6,  a7,  a8,  a9,  a10, a11, a12, a13, a14, a15, a16, a17, a18, a19, a20, a21, \
+   a22, a23, a24, a25, a26, a27, a28, a29, a30, a31, a32, a33, a34, a35, a36, a37, a38, a39, a40, a41, a42, a43, a44}
+void cal_arith_coef_vis_(int* ni, int* nj, int* nk, double* dxinv, double* dyinv, double* dzinv, double* rmu,
+                         C45_PARAMS) {
+  double* c[45] = C45_ARRAY;
+  coef_vis_impl(ni, nj, nk, dxinv, dyinv, dzinv, rmu, c, false);
+}
+void cal_harm_coef_vis_(int* ni, int* nj, int* nk, double* dxinv, double* dyinv, double* dzinv, double* rmu,
+                        C45_PARAMS) {
+  double* c[45] = C45_ARRAY;
+  coef_vis_impl(ni, nj, nk, dxinv, dyinv, dzinv, rmu, c, true);
+}
+void solu_sor4_(int* ipara, int* ID, int* nID, int* ndiv, int* ni, int* nj, int* nk, int* key, double* sendjb,
+                double* recvjb, int* nstep, int* imon_t, double* dt, double* rho, double* rhon, C45_PARAMS,
+                double* src_u, double* src_v, double* src_w, double* un, double* vn, double* wn, double* uwall,
+                double* dy, double* l1, double* l2, double* phi) {
+  (void)key;
+  (void)sendjb;
+  (void)recvjb;
+  (void)ndiv;
+  if (!one_rank(ipara) || !walls_only(nID)) return;
+  GRID3;
+  double* hc[45] = C45_ARRAY;
+  const double* c[45];
+  for (int q = 0; q < 45; ++q) c[q] = call.in(hc[q], N3);
+  const double* src[3] = {call.in(src_u, N3), call.in(src_v, N3), call.in(src_w, N3)};
+  double* du = call.out(un, N3);
+  double* dv = call.out(vn, N3);
+  double* dw = call.out(wn, N3);
+  const double* dr = call.in(rho, N3);
+  const double* drn = call.in(rhon, N3);
+  const double* dl1 = call.in(l1, N3);
+  const double* dl2 = call.in(l2, N3);
+  const double* dphi = call.in(phi, N3);
+  double* es = (double*)scratch(sizeof(double) * 2, 1);
+  double err = 0.0, err0 = 0.0;
+  int lp;
+  for (lp = 0; lp <= 20; ++lp) {
+    op::sor_iteration(s, g, *dt, dr, drn, c, src, du, dv, dw, *uwall, *dy, dl1, dl2, dphi, es);
+    double e = 0.0;
+    FMF_CUDA(cudaMemcpyAsync(&e, es, sizeof(double), cudaMemcpyDeviceToHost, s));
+    FMF_CUDA(cudaStreamSynchronize(s));
+    if (!std::isfinite(e)) {
+      set_status(FMF_ERR_NONFINITE);
+      break;
+    }
+    err = std::sqrt(e / (double)g.cells()) + 1.0e-99;
+    if (lp == 0) err0 = err;
+    if (err / err0 <= 1.0e-3) break;
+  }
+  g_last_sor_iters = (lp <= 20 ? lp : 20) + 1;
+  g_last_sor_ratio = err0 > 0.0 ? err / err0 : 0.0;
+  if (*ID == 0 && *imon_t > 0 && (*nstep % *imon_t) == 0)
+    std::printf("Err_solu %10d%10d%20.10E%20.10E%20.10E\n", *nstep, lp, err / err0, err, err0);
+  call.finish();
+}
+
+// ---------------------------------------------------------------- C4
+void caldiv_(int* ipara, int* ndiv, int* ni, int* nj, int* nk, double* dxinv, double* dyinv, double* dzinv,
+             double* dt, double* uk, double* vk, double* wk, double* div, double* err_div) {
+  if (!one_rank(ipara)) return;
+  (void)ndiv;
+  GRID3;
+  double* e = (double*)scratch(sizeof(double) * 2, 3);
+  op::caldiv(s, g, *dxinv, *dyinv, *dzinv, *dt, call.in(uk, N3), call.in(vk, N3), call.in(wk, N3),
+             call.out(div, N3), e);
+  FMF_CUDA(cudaMemcpyAsync(err_div, e, sizeof(double), cudaMemcpyDeviceToHost, s));
+  FMF_CUDA(cudaStreamSynchronize(s));
+  call.finish();
+}
+void cal_coef_prs_(int* nj, double* rho, double* dxinv, double* dyinv, double* dzinv, double* aw, double* ae,
+                   double* as, double* an, double* ab, double* at, double* ap) {
+  // 1-D, computed once before the time loop (main.f90:467): host arithmetic as the reference.
+  const int NJ = *nj;
+  const double r = *rho;
+  for (int j = 1; j <= NJ; ++j) {
+    const int t = j + 2;
+    aw[t] = *dxinv * *dxinv / r;
+    ae[t] = *dxinv * *dxinv / r;
+    as[t] = *dyinv * *dyinv / r;
+    an[t] = *dyinv * *dyinv / r;
+    ab[t] = *dzinv * *dzinv / r;
+    at[t] = *dzinv * *dzinv / r;
+    ap[t] = aw[t] + ae[t] + as[t] + an[t] + ab[t] + at[t];
+  }
+  ap[3] = ap[3] - as[3];
+  as[3] = 0.0;
+  ap[NJ + 2] = ap[NJ + 2] - an[NJ + 2];
+  an[NJ + 2] = 0.0;
+  for (double* a : {aw, ae, as, an, ab, at, ap})
+    if (mode() == FMF_RESIDENT) sync_to_device(a, 0);
+}
+void cal_coef_solp_fft_(int* nj, double* as_p, double* an_p, double* as_f, double* an_f, double* ap_f) {
+  const int NJ = *nj;
+  for (int j = 1; j <= NJ; ++j) {
+    const int t = j + 2;
+    as_f[t] = as_p[t];
+    an_f[t] = an_p[t];
+    ap_f[t] = as_f[t] + an_f[t];
+  }
+  ap_f[3] = ap_f[3] - as_f[3];
+  as_f[3] = 0.0;
+  ap_f[NJ + 2] = ap_f[NJ + 2] - an_f[NJ + 2];
+  an_f[NJ + 2] = 0.0;
+  for (double* a : {as_f, an_f, ap_f})
+    if (mode() == FMF_RESIDENT) sync_to_device(a, 0);
+}
+void solp_fft_tdma1_(int* ni, int* nj, int* nk, double* fftdata, double* div, double* pr, double* pi) {
+  (void)fftdata;
+  GRID3;
+  const long nm = g.cells();
+  op::fft_forward_planes(s, g, call.in(div, N3), call.out(pr, nm), call.out(pi, nm));
+  call.finish();
+}
+void trans_r2w_(int* ipara, int* ID, int* ndiv, int* svall, int* key, double* sendbuf, double* recvbuf, double* r,
+                double* w) {
+  (void)ID;
+  (void)key;
+  (void)sendbuf;
+  (void)recvbuf;
+  if (!one_rank(ipara) || *ndiv != 1) return;
+  const long nm = (long)svall[0] * svall[1] * svall[2];
+  Call call;
+  op::copy(stream(), nm, call.in(r, nm), call.out(w, nm));
+  call.finish();
+}
+void trans_w2r_(int* ipara, int* ID, int* ndiv, int* svall, int* key, double* sendbuf, double* recvbuf, double* w,
+                double* r) {
+  (void)ID;
+  (void)key;
+  (void)sendbuf;
+  (void)recvbuf;
+  if (!one_rank(ipara) || *ndiv != 1) return;
+  const long nm = (long)svall[0] * svall[1] * svall[2];
+  Call call;
+  op::copy(stream(), nm, call.in(w, nm), call.out(r, nm));
+  call.finish();
+}
+void solp_fft_tdma2_(int* ID, int* ndiv, int* svall, double* rho, double* dxinv, double* dzinv, double* as_f,
+                     double* an_f, double* ap_f, double* atdma, double* btdma_r, double* btdma_i, double* pr,
+                     double* pi) {
+  (void)atdma;
+  (void)btdma_r;
+  (void)btdma_i;
+  if (*ndiv != 1 || *ID != 0) {
+    set_status(FMF_ERR_UNSUPPORTED);
+    return;
+  }
+  int ni = svall[0], nj = svall[1], nk = svall[2];
+  if (!check_grid(ni, nj, nk)) return;
+  const Grid g(ni, nj, nk);
+  const long nm = g.cells();
+  Call call;
+  op::tdma_modes(stream(), g, *rho, *dxinv, *dzinv, call.in(as_f, nj + 6), call.in(an_f, nj + 6),
+                 call.in(ap_f, nj + 6), call.out(pr, nm), call.out(pi, nm));
+  call.finish();
+}
+void solp_fft_tdma3_(int* ni, int* nj, int* nk, double* fftdata, double* pr, double* pi, double* dp) {
+  (void)fftdata;
+  GRID3;
+  const long nm = g.cells();
+  op::fft_inverse_planes(s, g, call.in(pr, nm), call.in(pi, nm), call.out(dp, N3));
+  call.finish();
+}
+void solp_fft_tdma4_(int* ipara, int* ID, int* ndiv, int* ni, int* nj, int* nk, int* nstep, int* imon_t,
+                     double* rho, double* dxinv, double* dyinv, double* dzinv, double* div, double* dp) {
+  if (!one_rank(ipara)) return;
+  (void)ndiv;
+  if (*imon_t <= 0 || (*nstep % *imon_t) != 0) return;
+  GRID3;
+  double* d = (double*)scratch(sizeof(double) * 2, 3);
+  op::poisson_residual(s, g, *rho, *dxinv, *dyinv, *dzinv, call.in(div, N3), call.in(dp, N3), d);
+  double h[2];
+  FMF_CUDA(cudaMemcpyAsync(h, d, sizeof(h), cudaMemcpyDeviceToHost, s));
+  FMF_CUDA(cudaStreamSynchronize(s));
+  const double N = (double)g.cells();
+  const double err = std::sqrt(h[0] / N) + 1.0e-99, err0 = std::sqrt(h[1] / N) + 1.0e-99;
+  if (*ID == 0) std::printf("Err_solp %10d%20.10E%20.10E%20.10E\n", *nstep, err / err0, err, err0);
+  call.finish();
+}
+void bnd_avzero_(int* ipara, int* ndiv, int* ni, int* nj, int* nk, double* q) {
+  if (!one_rank(ipara)) return;
+  (void)ndiv;
+  GRID3;
+  op::bnd_avzero(s, g, call.out(q, N3));
+  call.finish();
+}
+void corunp_explicit_(int* nID, int* ni, int* nj, int* nk, double* rho, double* dxinv, double* dyinv,
+                      double* dzinv, double* dt, double* dp, double* phat, double* un, double* vn, double* wn,
+                      double* pn) {
+  if (!walls_only(nID)) return;
+  GRID3;
+  op::corunp_explicit(s, g, *rho, *dxinv, *dyinv, *dzinv, *dt, call.in(dp, N3), call.in(phat, N3),
+                      call.out(un, N3), call.out(vn, N3), call.out(wn, N3), call.out(pn, N3));
+  call.finish();
+}
+
+double fmf_interface_lower(int ni, int nj, int nk, const double* phi, double dx, double xl) {
+  const Grid g(ni, nj, nk);
+  double sum_x = 0.0;
+  for (int k = 1; k <= nk; ++k) {
+    double xk = 0.0;
+    for (int i = 1; i <= ni; ++i) {
+      const double p1 = phi[g.at(i, 1, k)], p2 = phi[g.at(i + 1, 1, k)];
+      if (p1 > 0.5 && p2 < 0.5) {
+        xk = ((double)i - 0.5) * dx + (0.5 - p1) * dx / (p2 - p1) - xl * 0.75;
+        break;
+      }
+    }
+    sum_x = sum_x + xk;
+  }
+  return -(sum_x / (double)nk);
+}
+void find_interface_positions_lower_(int* ni, int* nj, int* nk, double* phi, double* dx, double* dy, double* dz,
+                                     double* xl) {
+  (void)dy;
+  (void)dz;
+  if (mode() == FMF_RESIDENT) sync_to_host(phi, 0);
+  const double v = fmf_interface_lower(*ni, *nj, *nk, phi, *dx, *xl);
+  std::printf(" Lower Interface Position (Average over k):\n %.15E\n", v);
+}
+
+// ---------------------------------------------------------------- part 2
+void fmf_dev_cal_advu_weno5(int ni, int nj, int nk, double dxinv, double dyinv, double dzinv, const double* u,
+                            const double* v, const double* w, double* au, double* av, double* aw) {
+  if (!check_grid(ni, nj, nk)) return;
+  op::cal_advu_weno5(stream(), Grid(ni, nj, nk), dxinv, dyinv, dzinv, u, v, w, au, av, aw);
+  FMF_CUDA(cudaGetLastError());
+}
+void fmf_dev_bnd_periodic(int ni, int nj, int nk, double* qk) {
+  if (!check_grid(ni, nj, nk)) return;
+  op::bnd_periodic(stream(), Grid(ni, nj, nk), qk);
+  FMF_CUDA(cudaGetLastError());
+}
+
+}  // extern "C"

@@ -1,0 +1,214 @@
+// runtime.cu -- library runtime: status, stream, scratch, and the host-array
+// registry that mirrors the caller's arrays in HBM.
+#include <map>
+#include <mutex>
+#include <vector>
+
+#include "runtime.cuh"
+
+namespace fmf {
+
+static int g_status = 0;
+static long long g_launches = 0;
+static cudaStream_t g_stream = nullptr;
+static bool g_own_stream = false;
+static int g_mode = 0;  // FMF_RESIDENT
+
+void set_status(int code) {
+  if (code != 0) g_status = code;
+}
+int get_status() { return g_status; }
+int take_status() {
+  const int s = g_status;
+  g_status = 0;
+  return s;
+}
+bool cuda_ok(cudaError_t e, const char* where) {
+  if (e == cudaSuccess) return true;
+  std::fprintf(stderr, "fmf: CUDA error %s (%s) at %s\n", cudaGetErrorName(e), cudaGetErrorString(e), where);
+  set_status(1);
+  return false;
+}
+void count_launch(int n) { g_launches += n; }
+long long launches() { return g_launches; }
+
+cudaStream_t stream() {
+  if (!g_stream) {
+    if (FMF_CUDA(cudaStreamCreateWithFlags(&g_stream, cudaStreamNonBlocking))) g_own_stream = true;
+  }
+  return g_stream;
+}
+void set_stream(cudaStream_t s) {
+  if (s) {
+    g_stream = s;
+    g_own_stream = false;
+  } else {
+    g_stream = nullptr;
+    stream();
+  }
+}
+int mode() { return g_mode; }
+void set_mode(int m) { g_mode = m; }
+
+// ---- scratch ----------------------------------------------------------------
+struct Slot {
+  void* p = nullptr;
+  size_t bytes = 0;
+};
+static Slot g_slots[16];
+void* scratch(size_t bytes, int slot) {
+  Slot& s = g_slots[slot];
+  if (s.bytes >= bytes) return s.p;
+  if (s.p) {
+    FMF_CUDA(cudaStreamSynchronize(stream()));
+    FMF_CUDA(cudaFree(s.p));
+  }
+  s.p = nullptr;
+  s.bytes = 0;
+  if (!FMF_CUDA(cudaMalloc(&s.p, bytes))) {
+    set_status(5);
+    return nullptr;
+  }
+  s.bytes = bytes;
+  return s.p;
+}
+
+// ---- host-array registry -------------------------------------------------
+// Entries are keyed by host start address and never overlap: a request that
+// overlaps existing mirrors without being contained in one of them merges them
+// into one mirror covering the union (device contents of the old mirrors win
+// over host contents; the rest of the union is uploaded from the host).
+struct Entry {
+  uintptr_t end;
+  char* dev;
+};
+static std::map<uintptr_t, Entry> g_reg;
+static std::mutex g_mu;
+
+static char* lookup_locked(uintptr_t a, uintptr_t b, bool* fresh) {
+  *fresh = false;
+  auto it = g_reg.upper_bound(a);
+  if (it != g_reg.begin()) {
+    auto pv = std::prev(it);
+    if (pv->first <= a && pv->second.end >= b) return pv->second.dev + (a - pv->first);
+  }
+  // collect overlapping entries
+  uintptr_t lo = a, hi = b;
+  std::vector<std::map<uintptr_t, Entry>::iterator> ov;
+  it = g_reg.upper_bound(a);
+  if (it != g_reg.begin()) {
+    auto pv = std::prev(it);
+    if (pv->second.end > a) ov.push_back(pv);
+  }
+  for (; it != g_reg.end() && it->first < b; ++it) ov.push_back(it);
+  for (auto& e : ov) {
+    lo = std::min(lo, e->first);
+    hi = std::max(hi, e->second.end);
+  }
+  char* dev = nullptr;
+  if (!FMF_CUDA(cudaMalloc(&dev, hi - lo))) {
+    set_status(5);
+    return nullptr;
+  }
+  cudaStream_t s = stream();
+  FMF_CUDA(cudaMemcpyAsync(dev, (const void*)lo, hi - lo, cudaMemcpyHostToDevice, s));
+  for (auto& e : ov) {
+    FMF_CUDA(cudaMemcpyAsync(dev + (e->first - lo), e->second.dev, e->second.end - e->first,
+                             cudaMemcpyDeviceToDevice, s));
+  }
+  FMF_CUDA(cudaStreamSynchronize(s));
+  for (auto& e : ov) {
+    FMF_CUDA(cudaFree(e->second.dev));
+    g_reg.erase(e);
+  }
+  g_reg[lo] = Entry{hi, dev};
+  *fresh = true;
+  return dev + (a - lo);
+}
+
+void* mirror(const void* host, size_t bytes, bool* fresh) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  const uintptr_t a = (uintptr_t)host;
+  return lookup_locked(a, a + bytes, fresh);
+}
+
+int sync_to_host(const void* host, size_t bytes_or_0) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  const uintptr_t a = (uintptr_t)host;
+  auto it = g_reg.upper_bound(a);
+  if (it == g_reg.begin()) return 2;
+  --it;
+  if (a >= it->second.end) return 2;
+  const size_t n = bytes_or_0 ? bytes_or_0 : (size_t)(it->second.end - a);
+  FMF_CUDA(cudaMemcpyAsync((void*)a, it->second.dev + (a - it->first), n, cudaMemcpyDeviceToHost, stream()));
+  FMF_CUDA(cudaStreamSynchronize(stream()));
+  return get_status();
+}
+int sync_to_device(const void* host, size_t bytes_or_0) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  const uintptr_t a = (uintptr_t)host;
+  auto it = g_reg.upper_bound(a);
+  if (it == g_reg.begin()) return 2;
+  --it;
+  if (a >= it->second.end) return 2;
+  const size_t n = bytes_or_0 ? bytes_or_0 : (size_t)(it->second.end - a);
+  FMF_CUDA(cudaMemcpyAsync(it->second.dev + (a - it->first), (const void*)a, n, cudaMemcpyHostToDevice, stream()));
+  FMF_CUDA(cudaStreamSynchronize(stream()));
+  return get_status();
+}
+int sync_all_to_host() {
+  std::lock_guard<std::mutex> lk(g_mu);
+  for (auto& e : g_reg)
+    FMF_CUDA(cudaMemcpyAsync((void*)e.first, e.second.dev, e.second.end - e.first, cudaMemcpyDeviceToHost, stream()));
+  FMF_CUDA(cudaStreamSynchronize(stream()));
+  return get_status();
+}
+int forget(const void* host) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  const uintptr_t a = (uintptr_t)host;
+  auto it = g_reg.upper_bound(a);
+  if (it == g_reg.begin()) return 0;
+  --it;
+  if (a >= it->second.end) return 0;
+  FMF_CUDA(cudaStreamSynchronize(stream()));
+  FMF_CUDA(cudaFree(it->second.dev));
+  g_reg.erase(it);
+  return 0;
+}
+int reset_registry() {
+  std::lock_guard<std::mutex> lk(g_mu);
+  FMF_CUDA(cudaStreamSynchronize(stream()));
+  for (auto& e : g_reg) FMF_CUDA(cudaFree(e.second.dev));
+  g_reg.clear();
+  return 0;
+}
+
+// ---- one call's argument set -----------------------------------------------
+double* Call::arr(void* host, size_t ndouble, bool written) {
+  if (!host) {
+    ok = false;
+    set_status(2);
+    return nullptr;
+  }
+  bool fresh = false;
+  double* d = (double*)mirror(host, ndouble * sizeof(double), &fresh);
+  if (!d) {
+    ok = false;
+    return nullptr;
+  }
+  if (mode() == 1 && !fresh) {
+    FMF_CUDA(cudaMemcpyAsync(d, host, ndouble * sizeof(double), cudaMemcpyHostToDevice, stream()));
+  }
+  if (written) outs.push_back(Out{host, d, ndouble * sizeof(double)});
+  return d;
+}
+void Call::finish() {
+  cudaStream_t s = stream();
+  FMF_CUDA(cudaGetLastError());
+  if (mode() == 1) {
+    for (auto& o : outs) FMF_CUDA(cudaMemcpyAsync(o.host, o.dev, o.bytes, cudaMemcpyDeviceToHost, s));
+    FMF_CUDA(cudaStreamSynchronize(s));
+  }
+}
+
+}  // namespace fmf

@@ -1,0 +1,38 @@
+// runtime.cuh -- library runtime shared by the C-ABI translation units.
+#pragma once
+#include <vector>
+
+#include "fmf_common.cuh"
+
+namespace fmf {
+
+int take_status();
+long long launches();
+void set_stream(cudaStream_t s);
+int mode();
+void set_mode(int m);
+void* mirror(const void* host, size_t bytes, bool* fresh);
+int sync_to_host(const void* host, size_t bytes_or_0);
+int sync_to_device(const void* host, size_t bytes_or_0);
+int sync_all_to_host();
+int forget(const void* host);
+int reset_registry();
+
+// The array arguments of one drop-in call: arr() returns the device mirror of a
+// host array (uploading it when first seen, or on every call in coherent mode);
+// finish() downloads the written arrays in coherent mode.
+struct Call {
+  struct Out {
+    void* host;
+    void* dev;
+    size_t bytes;
+  };
+  std::vector<Out> outs;
+  bool ok = true;
+  double* arr(void* host, size_t ndouble, bool written);
+  double* in(void* host, size_t ndouble) { return arr(host, ndouble, false); }
+  double* out(void* host, size_t ndouble) { return arr(host, ndouble, true); }
+  void finish();
+};
+
+}  // namespace fmf

@@ -1,0 +1,431 @@
+// step.cu -- the device-resident time step (include/fmf_capi.h part 3).
+//
+// fmf_ctx_step runs main.f90:473-697 on the GPU with every field resident in HBM:
+// the state rotation of :686-697 is a pointer rotation, the MPI calls of the
+// reference are absent (one rank), and the only host<->device traffic per step is
+// the 8-byte SOR residual read once per outer iteration (the stop test of
+// solu_sor4.f:291-293).
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "../../include/fmf_capi.h"
+#include "ops.cuh"
+#include "runtime.cuh"
+
+using namespace fmf;
+
+struct fmf_ctx {
+  fmf_params prm;
+  Grid g;
+  cudaStream_t s = nullptr;
+  bool own_stream = false;
+  std::vector<void*> allocs;
+  long long bytes = 0;
+  // state
+  double *u, *v, *w, *uo, *vo, *wo, *p, *po;
+  double *phi, *phin;  // two slices each: [0] = slice 0, [n] = slice 1
+  double *un, *vn, *wn, *pn;
+  // walls
+  double *theta0, *zeta, *l1, *l2, *theta;
+  // work
+  double *phix, *phiy, *phiz, *flx, *fly, *flz, *rho, *rhon, *rmu, *rmun;
+  double *adv[3], *advo[3], *phat, *prs[3], *sk, *tau, *vis[3];
+  double *rn[4], *rnn[4], *rkap, *rkapn, *fst[3], *fstn[3], *sfst[3], *sfstn[3], *src[3];
+  double* coef[45];
+  double *dp, *div, *pr, *pi;
+  double *as_f, *an_f, *ap_f;
+  double* red;  // small reduction outputs
+  double* host_err = nullptr;  // pinned
+  std::vector<int> sor_iters;
+};
+
+namespace {
+double* alloc(fmf_ctx* c, long n) {
+  void* p = nullptr;
+  if (!FMF_CUDA(cudaMalloc(&p, sizeof(double) * n))) {
+    set_status(FMF_ERR_NOMEM);
+    return nullptr;
+  }
+  FMF_CUDA(cudaMemsetAsync(p, 0, sizeof(double) * n, c->s));
+  c->allocs.push_back(p);
+  c->bytes += (long long)sizeof(double) * n;
+  return (double*)p;
+}
+const int kNID_free = -1;
+}  // namespace
+
+extern "C" {
+
+int fmf_ctx_create(const fmf_params* prm, fmf_ctx** out) {
+  if (!prm || !out) return FMF_ERR_ARG;
+  auto p2 = [](int n) { return n >= 4 && (n & (n - 1)) == 0; };
+  if (!p2(prm->ni) || !p2(prm->nj) || !p2(prm->nk) || prm->ni < 16) return FMF_ERR_ARG;
+  fmf_ctx* c = new fmf_ctx();
+  c->prm = *prm;
+  c->g = Grid(prm->ni, prm->nj, prm->nk);
+  if (!FMF_CUDA(cudaStreamCreateWithFlags(&c->s, cudaStreamNonBlocking))) {
+    delete c;
+    return FMF_ERR_CUDA;
+  }
+  c->own_stream = true;
+  const long n = c->g.n, nm = c->g.cells();
+  double** f3[] = {&c->u, &c->v, &c->w, &c->uo, &c->vo, &c->wo, &c->p, &c->po, &c->un, &c->vn, &c->wn, &c->pn,
+                   &c->theta0, &c->zeta, &c->l1, &c->l2, &c->theta, &c->phix, &c->phiy, &c->phiz, &c->flx,
+                   &c->fly, &c->flz, &c->rho, &c->rhon, &c->rmu, &c->rmun, &c->phat, &c->dp, &c->div};
+  for (auto f : f3) *f = alloc(c, n);
+  c->phi = alloc(c, 2 * n);
+  c->phin = alloc(c, 2 * n);
+  for (int q = 0; q < 3; ++q) {
+    c->adv[q] = alloc(c, n);
+    c->advo[q] = alloc(c, n);
+    c->prs[q] = alloc(c, n);
+    c->vis[q] = alloc(c, n);
+    c->fst[q] = alloc(c, n);
+    c->fstn[q] = alloc(c, n);
+    c->sfst[q] = alloc(c, n);
+    c->sfstn[q] = alloc(c, n);
+    c->src[q] = alloc(c, n);
+  }
+  c->sk = alloc(c, 6 * n);
+  c->tau = alloc(c, 6 * n);
+  for (int q = 0; q < 4; ++q) {
+    c->rn[q] = alloc(c, 3 * n);
+    c->rnn[q] = alloc(c, 3 * n);
+  }
+  c->rkap = alloc(c, 3 * n);
+  c->rkapn = alloc(c, 3 * n);
+  for (int q = 0; q < 45; ++q) c->coef[q] = alloc(c, n);
+  c->pr = alloc(c, nm);
+  c->pi = alloc(c, nm);
+  c->as_f = alloc(c, prm->nj + 6);
+  c->an_f = alloc(c, prm->nj + 6);
+  c->ap_f = alloc(c, prm->nj + 6);
+  c->red = alloc(c, 64);
+  FMF_CUDA(cudaMallocHost(&c->host_err, sizeof(double) * 8));
+  if (get_status()) {
+    fmf_ctx_destroy(c);
+    return take_status();
+  }
+  // cal_coef_prs.f:28-54 + cal_coef_solp_fft.f:25-39 (main.f90:467-468), on the host
+  const int NJ = prm->nj;
+  std::vector<double> as(NJ + 6, 0.0), an(NJ + 6, 0.0), ap(NJ + 6, 0.0);
+  const double dyinv = 1.0 / prm->dy;
+  for (int j = 1; j <= NJ; ++j) {
+    as[j + 2] = dyinv * dyinv / prm->rhog;
+    an[j + 2] = dyinv * dyinv / prm->rhog;
+    ap[j + 2] = as[j + 2] + an[j + 2];
+  }
+  ap[3] = ap[3] - as[3];
+  as[3] = 0.0;
+  ap[NJ + 2] = ap[NJ + 2] - an[NJ + 2];
+  an[NJ + 2] = 0.0;
+  FMF_CUDA(cudaMemcpyAsync(c->as_f, as.data(), sizeof(double) * (NJ + 6), cudaMemcpyHostToDevice, c->s));
+  FMF_CUDA(cudaMemcpyAsync(c->an_f, an.data(), sizeof(double) * (NJ + 6), cudaMemcpyHostToDevice, c->s));
+  FMF_CUDA(cudaMemcpyAsync(c->ap_f, ap.data(), sizeof(double) * (NJ + 6), cudaMemcpyHostToDevice, c->s));
+  FMF_CUDA(cudaStreamSynchronize(c->s));
+  *out = c;
+  return take_status();
+}
+
+int fmf_ctx_destroy(fmf_ctx* c) {
+  if (!c) return 0;
+  if (c->s) cudaStreamSynchronize(c->s);
+  for (void* p : c->allocs) cudaFree(p);
+  if (c->host_err) cudaFreeHost(c->host_err);
+  if (c->own_stream && c->s) cudaStreamDestroy(c->s);
+  delete c;
+  return take_status();
+}
+
+int fmf_ctx_set_stream(fmf_ctx* c, void* st) {
+  if (!c) return FMF_ERR_ARG;
+  cudaStreamSynchronize(c->s);
+  if (c->own_stream) cudaStreamDestroy(c->s);
+  if (st) {
+    c->s = (cudaStream_t)st;
+    c->own_stream = false;
+  } else {
+    FMF_CUDA(cudaStreamCreateWithFlags(&c->s, cudaStreamNonBlocking));
+    c->own_stream = true;
+  }
+  return take_status();
+}
+
+int fmf_ctx_set_walls(fmf_ctx* c, const double* th, const double* ze, const double* l1, const double* l2) {
+  if (!c || !th || !ze || !l1 || !l2) return FMF_ERR_ARG;
+  const size_t b = sizeof(double) * c->g.n;
+  FMF_CUDA(cudaMemcpyAsync(c->theta0, th, b, cudaMemcpyHostToDevice, c->s));
+  FMF_CUDA(cudaMemcpyAsync(c->zeta, ze, b, cudaMemcpyHostToDevice, c->s));
+  FMF_CUDA(cudaMemcpyAsync(c->l1, l1, b, cudaMemcpyHostToDevice, c->s));
+  FMF_CUDA(cudaMemcpyAsync(c->l2, l2, b, cudaMemcpyHostToDevice, c->s));
+  return take_status();
+}
+
+static double* field_ptr(fmf_ctx* c, int f) {
+  const long n = c->g.n;
+  switch (f) {
+    case 0: return c->u;
+    case 1: return c->v;
+    case 2: return c->w;
+    case 3: return c->uo;
+    case 4: return c->vo;
+    case 5: return c->wo;
+    case 6: return c->p;
+    case 7: return c->po;
+    case 8: return c->phi;
+    case 9: return c->phi + n;
+    case 10: return c->phin;
+    case 11: return c->phin + n;
+    default: return nullptr;
+  }
+}
+
+int fmf_ctx_upload(fmf_ctx* c, const double* const* st) {
+  if (!c || !st) return FMF_ERR_ARG;
+  const size_t b = sizeof(double) * c->g.n;
+  for (int f = 0; f < 12; ++f) FMF_CUDA(cudaMemcpyAsync(field_ptr(c, f), st[f], b, cudaMemcpyHostToDevice, c->s));
+  return take_status();
+}
+int fmf_ctx_download(fmf_ctx* c, double* const* st) {
+  if (!c || !st) return FMF_ERR_ARG;
+  const size_t b = sizeof(double) * c->g.n;
+  for (int f = 0; f < 12; ++f) FMF_CUDA(cudaMemcpyAsync(st[f], field_ptr(c, f), b, cudaMemcpyDeviceToHost, c->s));
+  return take_status();
+}
+int fmf_ctx_state_device_ptr(fmf_ctx* c, int f, void** out) {
+  if (!c || !out || f < 0 || f > 11) return FMF_ERR_ARG;
+  *out = field_ptr(c, f);
+  return 0;
+}
+long long fmf_ctx_device_bytes(fmf_ctx* c) { return c ? c->bytes : 0; }
+int fmf_ctx_synchronize(fmf_ctx* c) {
+  if (!c) return FMF_ERR_ARG;
+  FMF_CUDA(cudaStreamSynchronize(c->s));
+  return take_status();
+}
+int fmf_ctx_sor_iterations(fmf_ctx* c, int* out, int cap) {
+  if (!c) return 0;
+  const int n = (int)c->sor_iters.size();
+  for (int t = 0; t < n && t < cap; ++t) out[t] = c->sor_iters[t];
+  return n;
+}
+
+// main.f90:322-366 (start-up boundary pass) on the uploaded state
+int fmf_ctx_init_bc(fmf_ctx* c) {
+  if (!c) return FMF_ERR_ARG;
+  const fmf_params& P = c->prm;
+  const Grid& g = c->g;
+  cudaStream_t s = c->s;
+  const long n = g.n;
+  double* phi0 = c->phi;
+  double* phi1 = c->phi + n;
+  op::gnbc(s, g, c->u, c->w, P.uwall, c->theta0, P.sigma, c->zeta, c->theta);
+  op::bnd_contact_angle(s, g, phi1, c->theta, P.dx, P.dy, P.dz);
+  op::bnd_periodic(s, g, phi1);
+  op::summation(s, g, phi0, phi1);
+  op::copy(s, n, c->u, c->un);
+  op::copy(s, n, c->v, c->vn);
+  op::copy(s, n, c->w, c->wn);
+  op::bndu(s, g, c->u, c->v, c->w, P.uwall, P.dy, c->l1, c->l2, phi1);
+  op::bndu(s, g, c->uo, c->vo, c->wo, P.uwall, P.dy, c->l1, c->l2, phi1);
+  op::bndu(s, g, c->un, c->vn, c->wn, P.uwall, P.dy, c->l1, c->l2, phi1);
+  for (double* q : {c->u, c->v, c->w, c->uo, c->vo, c->wo, c->un, c->vn, c->wn}) op::bnd_periodic(s, g, q);
+  op::gnbc(s, g, c->u, c->w, P.uwall, c->theta0, P.sigma, c->zeta, c->theta);
+  op::bnd_contact_angle(s, g, phi0, c->theta, P.dx, P.dy, P.dz);
+  op::bnd_periodic(s, g, phi0);
+  FMF_CUDA(cudaGetLastError());
+  return take_status();
+}
+
+static int step_once(fmf_ctx* c) {
+  const fmf_params& P = c->prm;
+  const Grid& g = c->g;
+  cudaStream_t s = c->s;
+  const long n = g.n;
+  const double dxinv = 1.0 / P.dx, dyinv = 1.0 / P.dy, dzinv = 1.0 / P.dz, dt = P.dt;
+  double* phi0 = c->phi;
+  double* phi1 = c->phi + n;
+  double* phin0 = c->phin;
+  double* phin1 = c->phin + n;
+  // :491-503 transport
+  op::cal_grad_p2a(s, g, dxinv, dyinv, dzinv, phi1, c->phix, c->phiy, c->phiz);
+  op::solphi_mthinc1(s, g, dxinv, dyinv, dzinv, dt, P.bet_mthinc, phi1, c->phix, c->phiy, c->phiz, c->u, c->v,
+                     c->w, c->flx, c->fly, c->flz);
+  op::solphi_mthinc2(s, g, dxinv, dyinv, dzinv, dt, c->u, c->v, c->w, c->flx, c->fly, c->flz, phi1, phin1);
+  op::cal_grad_p2a(s, g, dxinv, dyinv, dzinv, phin1, c->phix, c->phiy, c->phiz);
+  op::solphi_mthinc3(s, g, dxinv, dyinv, dzinv, P.bet_mthinc, c->phix, c->phiy, c->phiz, phi1, phin1, c->red);
+  op::gnbc(s, g, c->u, c->w, P.uwall, c->theta0, P.sigma, c->zeta, c->theta);
+  op::bnd_contact_angle(s, g, phin1, c->theta, P.dx, P.dy, P.dz);
+  op::bnd_periodic(s, g, phin1);
+  // :509-517
+  op::summation(s, g, phin0, phin1);
+  op::bnd_neumann(s, g, phin0);
+  op::bnd_contact_angle(s, g, phi0, c->theta, P.dx, P.dy, P.dz);  // gnbc result unchanged since :498
+  op::bnd_periodic(s, g, phin0);
+  // :526-529
+  op::cal_arith_mean(s, g, phi0, P.rhol, P.rhog, c->rho);
+  op::cal_arith_mean(s, g, phin0, P.rhol, P.rhog, c->rhon);
+  op::cal_arith_mean(s, g, phi0, P.rmul, P.rmug, c->rmu);
+  op::cal_arith_mean(s, g, phin0, P.rmul, P.rmug, c->rmun);
+  // :532-541
+  op::cal_advu_weno5(s, g, dxinv, dyinv, dzinv, c->u, c->v, c->w, c->adv[0], c->adv[1], c->adv[2]);
+  op::cal_advu_weno5(s, g, dxinv, dyinv, dzinv, c->uo, c->vo, c->wo, c->advo[0], c->advo[1], c->advo[2]);
+  op::calphat(s, g, c->p, c->po, c->phat);
+  op::cal_grad_prs(s, g, dxinv, dyinv, dzinv, c->phat, c->prs[0], c->prs[1], c->prs[2]);
+  op::calsij(s, g, dxinv, dyinv, dzinv, c->u, c->v, c->w, c->sk);
+  op::cal_tau(s, g, c->sk, c->rmu, c->tau, false);
+  op::cal_div_tensor(s, g, dxinv, dyinv, dzinv, c->tau, c->vis[0], c->vis[1], c->vis[2]);
+  // :545-570 surface tension
+  for (int q = 0; q < 3; ++q) {
+    op::fill(s, n, c->sfst[q], 0.0);
+    op::fill(s, n, c->sfstn[q], 0.0);
+  }
+  static const int offs[4][3] = {{1, 1, 1}, {0, 0, 1}, {0, 1, 0}, {1, 0, 0}};
+  op::cal_grad_p2a(s, g, dxinv, dyinv, dzinv, phi1, c->phix, c->phiy, c->phiz);
+  for (int q = 0; q < 4; ++q)
+    op::calrn(s, g, dxinv, dyinv, dzinv, offs[q][0], offs[q][1], offs[q][2], c->phix, c->phiy, c->phiz, c->rn[q]);
+  op::cal_grad_p2a(s, g, dxinv, dyinv, dzinv, phin1, c->phix, c->phiy, c->phiz);
+  for (int q = 0; q < 4; ++q)
+    op::calrn(s, g, dxinv, dyinv, dzinv, offs[q][0], offs[q][1], offs[q][2], c->phix, c->phiy, c->phiz, c->rnn[q]);
+  op::calrkap(s, g, dxinv, dyinv, dzinv, c->rn[0], c->rn[1], c->rn[2], c->rn[3], c->rkap);
+  op::calrkap(s, g, dxinv, dyinv, dzinv, c->rnn[0], c->rnn[1], c->rnn[2], c->rnn[3], c->rkapn);
+  op::cal_grad_prs(s, g, dxinv, dyinv, dzinv, phi1, c->phix, c->phiy, c->phiz);
+  op::calfst(s, g, P.rhol, P.rhog, P.sigma, c->phix, c->phiy, c->phiz, c->rkap, c->fst[0], c->fst[1], c->fst[2]);
+  op::cal_grad_prs(s, g, dxinv, dyinv, dzinv, phin1, c->phix, c->phiy, c->phiz);
+  op::calfst(s, g, P.rhol, P.rhog, P.sigma, c->phix, c->phiy, c->phiz, c->rkapn, c->fstn[0], c->fstn[1],
+             c->fstn[2]);
+  op::sum_fst(s, g, c->fst[0], c->fst[1], c->fst[2], c->sfst[0], c->sfst[1], c->sfst[2]);
+  op::sum_fst(s, g, c->fstn[0], c->fstn[1], c->fstn[2], c->sfstn[0], c->sfstn[1], c->sfstn[2]);
+  // :579-603 (cal_av of rho/rhon at :571-573 feeds nothing downstream)
+  const double* advp[3] = {c->adv[0], c->adv[1], c->adv[2]};
+  const double* advop[3] = {c->advo[0], c->advo[1], c->advo[2]};
+  const double* prsp[3] = {c->prs[0], c->prs[1], c->prs[2]};
+  const double* visp[3] = {c->vis[0], c->vis[1], c->vis[2]};
+  const double* fstp[3] = {c->sfst[0], c->sfst[1], c->sfst[2]};
+  const double* fstnp[3] = {c->sfstn[0], c->sfstn[1], c->sfstn[2]};
+  op::cal_srcu(s, g, dt, P.grvb, P.grvp, c->u, c->v, c->w, c->rho, c->rhon, advp, advop, prsp, visp, fstp, fstnp,
+               c->src);
+  op::cal_coef_vis(s, g, dxinv, dyinv, dzinv, c->rmun, c->coef, P.harmonic != 0);
+  // :605-623
+  op::copy(s, n, c->u, c->un);
+  op::copy(s, n, c->v, c->vn);
+  op::copy(s, n, c->w, c->wn);
+  const double* cf[45];
+  for (int q = 0; q < 45; ++q) cf[q] = c->coef[q];
+  const double* srcp[3] = {c->src[0], c->src[1], c->src[2]};
+  double err = 0.0, err0 = 0.0;
+  int lp;
+  for (lp = 0; lp <= 20; ++lp) {
+    op::sor_iteration(s, g, dt, c->rho, c->rhon, cf, srcp, c->un, c->vn, c->wn, P.uwall, P.dy, c->l1, c->l2, phi1,
+                      c->red + 8);
+    FMF_CUDA(cudaMemcpyAsync(c->host_err, c->red + 8, sizeof(double), cudaMemcpyDeviceToHost, s));
+    FMF_CUDA(cudaStreamSynchronize(s));
+    const double e = c->host_err[0];
+    if (!std::isfinite(e)) {
+      set_status(FMF_ERR_NONFINITE);
+      break;
+    }
+    err = std::sqrt(e / (double)g.cells()) + 1.0e-99;
+    if (lp == 0) err0 = err;
+    if (err / err0 <= 1.0e-3) break;
+  }
+  c->sor_iters.push_back((lp <= 20 ? lp : 20) + 1);
+  // :625-646
+  op::bndu(s, g, c->un, c->vn, c->wn, P.uwall, P.dy, c->l1, c->l2, phi1);
+  op::bnd_periodic(s, g, c->un);
+  op::bnd_periodic(s, g, c->vn);
+  op::bnd_periodic(s, g, c->wn);
+  op::caldiv(s, g, dxinv, dyinv, dzinv, dt, c->un, c->vn, c->wn, c->div, nullptr);
+  op::fft_forward_planes(s, g, c->div, c->pr, c->pi);
+  op::tdma_modes(s, g, P.rhog, dxinv, dzinv, c->as_f, c->an_f, c->ap_f, c->pr, c->pi);
+  op::fft_inverse_planes(s, g, c->pr, c->pi, c->dp);
+  op::bnd_avzero(s, g, c->dp);
+  op::bnd_neumann(s, g, c->dp);
+  op::bnd_periodic(s, g, c->dp);
+  // :648-661
+  op::corunp_explicit(s, g, P.rhog, dxinv, dyinv, dzinv, dt, c->dp, c->phat, c->un, c->vn, c->wn, c->pn);
+  op::bndu(s, g, c->un, c->vn, c->wn, P.uwall, P.dy, c->l1, c->l2, phi1);
+  op::bnd_periodic(s, g, c->un);
+  op::bnd_periodic(s, g, c->vn);
+  op::bnd_periodic(s, g, c->wn);
+  op::bnd_avzero(s, g, c->pn);
+  op::bnd_neumann(s, g, c->pn);
+  op::bnd_periodic(s, g, c->pn);
+  // :686-697 rotation by pointer; phin keeps phi's values (cpy leaves its source intact)
+  double* t;
+  t = c->uo; c->uo = c->u; c->u = c->un; c->un = t;
+  t = c->vo; c->vo = c->v; c->v = c->vn; c->vn = t;
+  t = c->wo; c->wo = c->w; c->w = c->wn; c->wn = t;
+  t = c->po; c->po = c->p; c->p = c->pn; c->pn = t;
+  t = c->phi; c->phi = c->phin; c->phin = t;
+  op::copy(s, 2 * n, c->phi, c->phin);
+  FMF_CUDA(cudaGetLastError());
+  return get_status();
+}
+
+// Times one stage of the step on the context's stream with CUDA events, reps
+// launches after one warm-up launch, on the current state (the state is not
+// advanced: stages write only work arrays).  Stage 0: WENO5 advection of (u,v,w);
+// 1: one outer SOR iteration on copies of the velocity; 2: pressure FFT+TDMA+inverse;
+// 3: MTHINC fluxes.  *ms = mean milliseconds per launch of the stage.
+int fmf_ctx_time_stage(fmf_ctx* c, int stage, int reps, float* ms) {
+  if (!c || !ms || reps <= 0 || stage < 0 || stage > 3) return FMF_ERR_ARG;
+  const fmf_params& P = c->prm;
+  const Grid& g = c->g;
+  cudaStream_t s = c->s;
+  const double dxinv = 1.0 / P.dx, dyinv = 1.0 / P.dy, dzinv = 1.0 / P.dz;
+  const long n = g.n;
+  const double* cf[45];
+  for (int q = 0; q < 45; ++q) cf[q] = c->coef[q];
+  const double* srcp[3] = {c->src[0], c->src[1], c->src[2]};
+  auto run = [&]() {
+    switch (stage) {
+      case 0:
+        op::cal_advu_weno5(s, g, dxinv, dyinv, dzinv, c->u, c->v, c->w, c->adv[0], c->adv[1], c->adv[2]);
+        break;
+      case 1:
+        op::sor_iteration(s, g, P.dt, c->rho, c->rhon, cf, srcp, c->un, c->vn, c->wn, P.uwall, P.dy, c->l1, c->l2,
+                          c->phi + n, c->red + 8);
+        break;
+      case 2:
+        op::fft_forward_planes(s, g, c->div, c->pr, c->pi);
+        op::tdma_modes(s, g, P.rhog, dxinv, dzinv, c->as_f, c->an_f, c->ap_f, c->pr, c->pi);
+        op::fft_inverse_planes(s, g, c->pr, c->pi, c->dp);
+        break;
+      case 3:
+        op::solphi_mthinc1(s, g, dxinv, dyinv, dzinv, P.dt, P.bet_mthinc, c->phi + n, c->phix, c->phiy, c->phiz,
+                           c->u, c->v, c->w, c->flx, c->fly, c->flz);
+        break;
+    }
+  };
+  if (stage == 1) {
+    op::copy(s, n, c->u, c->un);
+    op::copy(s, n, c->v, c->vn);
+    op::copy(s, n, c->w, c->wn);
+  }
+  run();
+  cudaEvent_t e0, e1;
+  FMF_CUDA(cudaEventCreate(&e0));
+  FMF_CUDA(cudaEventCreate(&e1));
+  FMF_CUDA(cudaEventRecord(e0, s));
+  for (int r = 0; r < reps; ++r) run();
+  FMF_CUDA(cudaEventRecord(e1, s));
+  FMF_CUDA(cudaEventSynchronize(e1));
+  float t = 0.f;
+  FMF_CUDA(cudaEventElapsedTime(&t, e0, e1));
+  *ms = t / (float)reps;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  return take_status();
+}
+
+int fmf_ctx_step(fmf_ctx* c, int nsteps) {
+  if (!c || nsteps < 0) return FMF_ERR_ARG;
+  c->sor_iters.clear();
+  for (int t = 0; t < nsteps; ++t)
+    if (step_once(c)) break;
+  return take_status();
+}
+
+}  // extern "C"

@@ -1,0 +1,175 @@
+"""ctypes binding of libfmf.so (the CUDA product).
+
+``load()`` raises when the library is missing: there is no CPU fallback.
+``Stepper`` drives the fused device-resident time step (``fmf_ctx_*``); the
+drop-in subroutines (``<name>_``) are reached through ``lib()`` with the same
+arguments the Fortran caller passes (every argument by reference).
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+from . import config as fcfg
+from .build import LIB
+
+_lib = None
+
+FMF_FP64, FMF_MIXED = 0, 1
+FMF_RESIDENT, FMF_COHERENT = 0, 1
+
+
+class FmfError(RuntimeError):
+    pass
+
+
+class Params(ctypes.Structure):
+    _fields_ = [("ni", ctypes.c_int), ("nj", ctypes.c_int), ("nk", ctypes.c_int),
+                ("dx", ctypes.c_double), ("dy", ctypes.c_double), ("dz", ctypes.c_double),
+                ("dt", ctypes.c_double), ("rhol", ctypes.c_double), ("rhog", ctypes.c_double),
+                ("rmul", ctypes.c_double), ("rmug", ctypes.c_double), ("sigma", ctypes.c_double),
+                ("uwall", ctypes.c_double), ("grvb", ctypes.c_double), ("grvp", ctypes.c_double),
+                ("bet_mthinc", ctypes.c_double), ("harmonic", ctypes.c_int), ("precision", ctypes.c_int)]
+
+
+def params(cfg: fcfg.Config, precision: int = FMF_FP64) -> Params:
+    return Params(cfg.ni, cfg.nj, cfg.nk, cfg.dx, cfg.dy, cfg.dz, cfg.dt, cfg.rhol, cfg.rhog,
+                  cfg.rmul, cfg.rmug, cfg.sigma, cfg.uwall, cfg.grvb, cfg.grvp, cfg.bet_mthinc,
+                  cfg.harmonic, precision)
+
+
+def load(path: str | None = None):
+    """Load libfmf.so; raise FmfError if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = path or LIB
+    if not os.path.exists(path):
+        raise FmfError(f"{path} is missing: build it with fmf.build.build() (nvcc, sm_103a)")
+    L = ctypes.CDLL(path)
+    vp, ip, dp = ctypes.c_void_p, ctypes.c_int, ctypes.c_double
+    L.fmf_ctx_create.argtypes = [ctypes.POINTER(Params), ctypes.POINTER(vp)]
+    L.fmf_ctx_create.restype = ip
+    for name in ("fmf_ctx_destroy", "fmf_ctx_init_bc", "fmf_ctx_synchronize"):
+        getattr(L, name).argtypes = [vp]
+        getattr(L, name).restype = ip
+    L.fmf_ctx_step.argtypes = [vp, ip]
+    L.fmf_ctx_step.restype = ip
+    L.fmf_ctx_set_stream.argtypes = [vp, vp]
+    L.fmf_ctx_set_walls.argtypes = [vp, vp, vp, vp, vp]
+    L.fmf_ctx_upload.argtypes = [vp, ctypes.POINTER(vp)]
+    L.fmf_ctx_download.argtypes = [vp, ctypes.POINTER(vp)]
+    L.fmf_ctx_sor_iterations.argtypes = [vp, ctypes.POINTER(ctypes.c_int), ip]
+    L.fmf_ctx_sor_iterations.restype = ip
+    L.fmf_ctx_state_device_ptr.argtypes = [vp, ip, ctypes.POINTER(vp)]
+    L.fmf_ctx_device_bytes.argtypes = [vp]
+    L.fmf_ctx_device_bytes.restype = ctypes.c_longlong
+    L.fmf_kernel_launches.restype = ctypes.c_longlong
+    L.fmf_error_string.restype = ctypes.c_char_p
+    L.fmf_last_sor_ratio.restype = dp
+    L.fmf_interface_lower.restype = dp
+    L.fmf_interface_lower.argtypes = [ip, ip, ip, vp, dp, dp]
+    L.fmf_set_stream.argtypes = [vp]
+    for name in ("fmf_sync_to_host", "fmf_sync_to_device", "fmf_forget"):
+        getattr(L, name).argtypes = [vp]
+    _lib = L
+    return L
+
+
+def lib():
+    return load()
+
+
+def check(code: int, what: str = "") -> None:
+    if code:
+        msg = lib().fmf_error_string(code).decode()
+        raise FmfError(f"{what}: {msg} ({code})")
+
+
+# ---- Fortran-style argument helpers -----------------------------------------
+def I(x: int):
+    return ctypes.byref(ctypes.c_int(int(x)))
+
+
+def D(x: float):
+    return ctypes.byref(ctypes.c_double(float(x)))
+
+
+def P(a: np.ndarray):
+    assert a.dtype == np.float64 and a.flags.c_contiguous
+    return ctypes.c_void_p(a.ctypes.data)
+
+
+def IA(vals):
+    return (ctypes.c_int * len(vals))(*vals)
+
+
+def _ptr_array(arrs):
+    return (ctypes.c_void_p * len(arrs))(*[a.ctypes.data for a in arrs])
+
+
+class Stepper:
+    """The fused device-resident time step on one GPU."""
+
+    def __init__(self, cfg: fcfg.Config, precision: int = FMF_FP64, stream=None):
+        self.cfg = cfg
+        self._prm = params(cfg, precision)
+        h = ctypes.c_void_p()
+        check(lib().fmf_ctx_create(ctypes.byref(self._prm), ctypes.byref(h)), "fmf_ctx_create")
+        self.h = h
+        if stream is not None:
+            check(lib().fmf_ctx_set_stream(self.h, ctypes.c_void_p(stream)), "set_stream")
+        self.walls = fcfg.wall_arrays(cfg)
+        th, ze, l1, l2 = self.walls
+        check(lib().fmf_ctx_set_walls(self.h, P(th), P(ze), P(l1), P(l2)), "set_walls")
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().fmf_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def upload(self, st: np.ndarray):
+        self._up = st  # keep the host buffer alive while the copy is in flight
+        check(lib().fmf_ctx_upload(self.h, _ptr_array(list(st))), "upload")
+
+    def download(self, st: np.ndarray):
+        check(lib().fmf_ctx_download(self.h, _ptr_array(list(st))), "download")
+
+    def init_bc(self):
+        check(lib().fmf_ctx_init_bc(self.h), "init_bc")
+
+    def step(self, n: int = 1):
+        check(lib().fmf_ctx_step(self.h, int(n)), "step")
+
+    def sync(self):
+        check(lib().fmf_ctx_synchronize(self.h), "synchronize")
+
+    def sor_iterations(self):
+        buf = (ctypes.c_int * 100000)()
+        n = lib().fmf_ctx_sor_iterations(self.h, buf, 100000)
+        return list(buf[:n])
+
+    def device_bytes(self) -> int:
+        return int(lib().fmf_ctx_device_bytes(self.h))
+
+    def initial_state(self) -> np.ndarray:
+        st = fcfg.raw_state(self.cfg)
+        self.upload(st)
+        self.init_bc()
+        self.download(st)
+        self.sync()
+        return st
+
+    def get_state(self) -> np.ndarray:
+        st = np.zeros((12,) + self.cfg.shape)
+        self.download(st)
+        self.sync()
+        return st

@@ -1,0 +1,308 @@
+/*
+ * fmf_capi.h -- C-ABI of the GB300 (sm_103a) implementation of the per-time-step
+ * two-phase update of toruneko1129/fel-multi-phase-flow.
+ *
+ * Part 1: drop-in replacements.  Each `<name>_` keeps the reference Fortran
+ * subroutine's name (gfortran/ifx external-name mangling: lower case plus one
+ * trailing underscore) and its argument list and order.  Every argument is passed
+ * by reference, exactly as Fortran 77 passes it: integers are int32, reals are
+ * double, arrays are the caller's host arrays, column-major with origin -2, i.e.
+ * a pointer to element (-2,-2,-2) of a (-2:ni+3,-2:nj+3,-2:nk+3) array.
+ * The routines return nothing, like the originals; a failure is recorded and
+ * read with fmf_last_error().  The comment above each declaration cites the
+ * reference file:line whose subroutine it replaces.
+ *
+ * Residency.  Host arrays are mirrored in HBM by a registry keyed by host
+ * address.  In FMF_RESIDENT mode (default) the first call that sees an array
+ * uploads it; afterwards the device copy is authoritative and consecutive calls
+ * move no data between host and device.  Host code that reads an array (I/O,
+ * diagnostics) calls fmf_sync_to_host(ptr) first; host code that writes one
+ * calls fmf_sync_to_device(ptr) afterwards.  In FMF_COHERENT mode every call
+ * uploads all of its array arguments and downloads every array it writes before
+ * returning, so the routines behave exactly like the host originals.
+ *
+ * Scratch arguments of the reference (fftdata, atdma, btdma_*, key, sendjb,
+ * recvjb, sendbuf, recvbuf) are accepted and not touched: the device code keeps
+ * its own scratch.  With one rank (ipara=0) the reference's MPI routines are
+ * in-device copies or no-ops (bnd_comm.f:18, trans_r2w.f:23-38).
+ *
+ * Part 2: device-pointer variants fmf_dev_<name>: the same arguments, but every
+ * array is a device pointer (scalars stay host pointers), enqueued on the
+ * library stream (fmf_set_stream).
+ *
+ * Part 3: the fused, device-resident time step (fmf_ctx_*), which runs the
+ * whole of main.f90:473-697 on the GPU.
+ *
+ * Threading: one host thread drives the library at a time (the reference's
+ * single-threaded caller contract).  All work goes to one CUDA stream.
+ */
+#ifndef FMF_CAPI_H
+#define FMF_CAPI_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------------ */
+/* status, residency                                                         */
+/* ------------------------------------------------------------------------ */
+enum {
+  FMF_OK = 0,
+  FMF_ERR_CUDA = 1,        /* a CUDA runtime call failed */
+  FMF_ERR_ARG = 2,         /* invalid argument (size, null pointer, grid not a power of two) */
+  FMF_ERR_NONFINITE = 3,   /* NaN/Inf met in a reduction (volume sum, SOR residual, mean) */
+  FMF_ERR_ITER_CAP = 4,    /* the SOR hit its 21-iteration cap (reported, not fatal) */
+  FMF_ERR_NOMEM = 5,       /* device allocation failed */
+  FMF_ERR_UNSUPPORTED = 6  /* a multi-rank (ipara=1) argument on the one-GPU build */
+};
+enum { FMF_RESIDENT = 0, FMF_COHERENT = 1 };
+
+int fmf_last_error(void);                 /* last status, then cleared */
+const char* fmf_error_string(int code);
+int fmf_set_mode(int mode);               /* FMF_RESIDENT or FMF_COHERENT */
+int fmf_set_stream(void* cuda_stream);    /* NULL: the library's own stream */
+int fmf_sync_to_host(void* host_ptr);     /* copy one mirrored array back */
+int fmf_sync_to_device(void* host_ptr);   /* re-upload one mirrored array */
+int fmf_sync_all_to_host(void);
+int fmf_forget(void* host_ptr);           /* drop one mirror (host array about to be freed) */
+int fmf_reset(void);                      /* drop every mirror */
+int fmf_device_synchronize(void);
+/* kernels this library launched since load (a counter kept by its launch helpers) */
+long long fmf_kernel_launches(void);
+
+/* ------------------------------------------------------------------------ */
+/* Part 1: drop-in replacements of the reference subroutines                 */
+/* ------------------------------------------------------------------------ */
+
+/* srcs/cal_grad_p2a.f:1-76 (svall is svall(2), the global nj) */
+void cal_grad_p2a_(int* ID, int* svall, int* ni, int* nj, int* nk, double* dxinv,
+                   double* dyinv_array, double* dzinv, double* q, double* qx, double* qy,
+                   double* qz);
+/* srcs/solphi_mthinc1.f:1-292 */
+void solphi_mthinc1_(int* ni, int* nj, int* nk, double* dxinv, double* dyinv, double* dzinv,
+                     double* dt, double* bet_mthinc, double* phi, double* phix, double* phiy,
+                     double* phiz, double* u, double* v, double* w, double* flphix,
+                     double* flphiy, double* flphiz);
+/* srcs/solphi_mthinc2.f:1-48 */
+void solphi_mthinc2_(int* ni, int* nj, int* nk, double* dxinv, double* dyinv, double* dzinv,
+                     double* dt, double* u, double* v, double* w, double* flphix, double* flphiy,
+                     double* flphiz, double* phi, double* phin);
+/* srcs/solphi_mthinc3.f:1-163 */
+void solphi_mthinc3_(int* ipara, int* ni, int* nj, int* nk, double* dxinv, double* dyinv,
+                     double* dzinv, double* bet_mthinc, double* phix, double* phiy, double* phiz,
+                     double* phi, double* phin);
+/* srcs/summation.f:1-54 (qk is the 4-D array qk(...,0:nbub)) */
+void summation_(int* ni, int* nj, int* nk, double* qk, int* nbub);
+/* srcs/gnbc.f90:1-100 */
+void gnbc_(int* nID, int* ni, int* nj, int* nk, double* uk, double* wk, double* uwall,
+           double* theta_0_array, double* surface_tension, double* zeta_array,
+           double* theta_array);
+/* srcs/bnd_contact_angle.f90:1-88 */
+void bnd_contact_angle_(int* nID, int* ni, int* nj, int* nk, double* qk, double* theta_array,
+                        double* dx, double* dy, double* dz);
+/* srcs/bndu.f:1-161 */
+void bndu_(int* nID, int* ni, int* nj, int* nk, double* uk, double* vk, double* wk,
+           double* uwall, double* dy, double* l1, double* l2, double* phi);
+/* srcs/bnd_periodic.f:1-44 */
+void bnd_periodic_(int* ni, int* nj, int* nk, double* qk);
+/* srcs/bnd_neumann.f:1-46 */
+void bnd_neumann_(int* nID, int* ni, int* nj, int* nk, double* qk);
+/* srcs/bnd_comm.f:1-121 (ipara=0: nothing to exchange on one GPU) */
+void bnd_comm_(int* ipara, int* nID, int* ni, int* nj, int* nk, int* key, double* sendjb,
+               double* recvjb, double* qk);
+/* srcs/cal_advu_weno5.f:1-258 with srcs/weno5.h:1-71 */
+void cal_advu_weno5_(int* ni, int* nj, int* nk, double* dxinv, double* dyinv, double* dzinv,
+                     double* u, double* v, double* w, double* adv_u, double* adv_v,
+                     double* adv_w);
+/* srcs/cal_arith_mean.f:1-29 */
+void cal_arith_mean_(int* ni, int* nj, int* nk, double* phik, double* ql, double* qg, double* qk);
+/* srcs/cal_harm_mean.f:30-58 */
+void cal_harm_mean_(int* ni, int* nj, int* nk, double* phik, double* ql, double* qg, double* qk);
+/* srcs/calphat.f:1-26 */
+void calphat_(int* ni, int* nj, int* nk, double* p, double* po, double* phat);
+/* srcs/cal_grad_prs.f:1-41 */
+void cal_grad_prs_(int* ni, int* nj, int* nk, double* dxinv, double* dyinv, double* dzinv,
+                   double* q, double* qx_u, double* qy_v, double* qz_w);
+/* srcs/calsij.f:1-143 (sk is sk(...,6)) */
+void calsij_(int* ni, int* nj, int* nk, double* dxinv, double* dyinv, double* dzinv, double* uk,
+             double* vk, double* wk, double* sk);
+/* srcs/cal_arith_tau.f:1-121 */
+void cal_arith_tau_(int* ni, int* nj, int* nk, double* s, double* rmu, double* tau);
+/* srcs/cal_harm_tau.f:1-121 */
+void cal_harm_tau_(int* ni, int* nj, int* nk, double* s, double* rmu, double* tau);
+/* srcs/cal_div_tensor.f:1-89 */
+void cal_div_tensor_(int* ni, int* nj, int* nk, double* dxinv, double* dyinv, double* dzinv,
+                     double* tauk, double* uk, double* vk, double* wk);
+/* srcs/calrn.f:1-91 (rn is rn(...,3)) */
+void calrn_(int* ni, int* nj, int* nk, double* dxinv, double* dyinv, double* dzinv, int* ip,
+            int* jp, int* kp, double* phix, double* phiy, double* phiz, double* rn);
+/* srcs/calrkap.f:1-101 */
+void calrkap_(int* ni, int* nj, int* nk, double* dxinv, double* dyinv, double* dzinv,
+              double* rn_pp, double* rn_12, double* rn_13, double* rn_23, double* rkap);
+/* srcs/cal_grad_p2uvw.f:1-47 */
+void cal_grad_p2uvw_(int* ID, int* svall, int* ni, int* nj, int* nk, double* dxinv,
+                     double* dyinv_array, double* dzinv, double* q, double* qx_u, double* qy_v,
+                     double* qz_w);
+/* srcs/calfst.f:1-49 */
+void calfst_(int* ni, int* nj, int* nk, double* rhol, double* rhog, double* surface_tension,
+             double* phix_u, double* phiy_v, double* phiz_w, double* rkap, double* fst_u,
+             double* fst_v, double* fst_w);
+/* srcs/sum_fst.f:1-37 */
+void sum_fst_(int* ni, int* nj, int* nk, double* fst_u, double* fst_v, double* fst_w,
+              double* sum_fst_u, double* sum_fst_v, double* sum_fst_w);
+/* srcs/init_q.f:1-29 */
+void init_q_(int* ni, int* nj, int* nk, double* q1, double* q2, double* q3);
+/* srcs/cal_av.f:1-40 */
+void cal_av_(int* ipara, int* ndiv, int* ni, int* nj, int* nk, double* q, double* av);
+/* srcs/cal_srcu.f:1-141 */
+void cal_srcu_(int* nID, int* ni, int* nj, int* nk, double* rho_av, double* dt, double* grvb,
+               double* grvp, double* u, double* v, double* w, double* rho, double* rhon,
+               double* adv_u, double* adv_v, double* adv_w, double* adv_uo, double* adv_vo,
+               double* adv_wo, double* prs_u, double* prs_v, double* prs_w, double* vis_u,
+               double* vis_v, double* vis_w, double* fst_u, double* fst_v, double* fst_w,
+               double* fst_un, double* fst_vn, double* fst_wn, double* src_u, double* src_v,
+               double* src_w);
+/* srcs/cpy.f:1-24 */
+void cpy_(int* ni, int* nj, int* nk, double* q1, double* q2);
+/* srcs/cal_arith_coef_vis.f:1-411 */
+void cal_arith_coef_vis_(int* ni, int* nj, int* nk, double* dxinv, double* dyinv, double* dzinv,
+                         double* rmuk, double* au_w_uk, double* au_e_uk, double* au_s_uk,
+                         double* au_n_uk, double* au_b_uk, double* au_t_uk, double* au_p_uk,
+                         double* av_ws_uk, double* av_es_uk, double* av_wn_uk, double* av_en_uk,
+                         double* aw_wb_uk, double* aw_eb_uk, double* aw_wt_uk, double* aw_et_uk,
+                         double* av_w_vk, double* av_e_vk, double* av_s_vk, double* av_n_vk,
+                         double* av_b_vk, double* av_t_vk, double* av_p_vk, double* au_sw_vk,
+                         double* au_nw_vk, double* au_se_vk, double* au_ne_vk, double* aw_sb_vk,
+                         double* aw_nb_vk, double* aw_st_vk, double* aw_nt_vk, double* aw_w_wk,
+                         double* aw_e_wk, double* aw_s_wk, double* aw_n_wk, double* aw_b_wk,
+                         double* aw_t_wk, double* aw_p_wk, double* au_bw_wk, double* au_tw_wk,
+                         double* au_be_wk, double* au_te_wk, double* av_bs_wk, double* av_ts_wk,
+                         double* av_bn_wk, double* av_tn_wk);
+/* srcs/cal_harm_coef_vis.f:1-411 (same arguments) */
+void cal_harm_coef_vis_(int* ni, int* nj, int* nk, double* dxinv, double* dyinv, double* dzinv,
+                        double* rmuk, double* au_w_uk, double* au_e_uk, double* au_s_uk,
+                        double* au_n_uk, double* au_b_uk, double* au_t_uk, double* au_p_uk,
+                        double* av_ws_uk, double* av_es_uk, double* av_wn_uk, double* av_en_uk,
+                        double* aw_wb_uk, double* aw_eb_uk, double* aw_wt_uk, double* aw_et_uk,
+                        double* av_w_vk, double* av_e_vk, double* av_s_vk, double* av_n_vk,
+                        double* av_b_vk, double* av_t_vk, double* av_p_vk, double* au_sw_vk,
+                        double* au_nw_vk, double* au_se_vk, double* au_ne_vk, double* aw_sb_vk,
+                        double* aw_nb_vk, double* aw_st_vk, double* aw_nt_vk, double* aw_w_wk,
+                        double* aw_e_wk, double* aw_s_wk, double* aw_n_wk, double* aw_b_wk,
+                        double* aw_t_wk, double* aw_p_wk, double* au_bw_wk, double* au_tw_wk,
+                        double* au_be_wk, double* au_te_wk, double* av_bs_wk, double* av_ts_wk,
+                        double* av_bn_wk, double* av_tn_wk);
+/* srcs/solu_sor4.f:1-308 */
+void solu_sor4_(int* ipara, int* ID, int* nID, int* ndiv, int* ni, int* nj, int* nk, int* key,
+                double* sendjb, double* recvjb, int* nstep, int* imon_t, double* dt, double* rho,
+                double* rhon, double* au_w_u, double* au_e_u, double* au_s_u, double* au_n_u,
+                double* au_b_u, double* au_t_u, double* au_p_u, double* av_ws_u,
+                double* av_es_u, double* av_wn_u, double* av_en_u, double* aw_wb_u,
+                double* aw_eb_u, double* aw_wt_u, double* aw_et_u, double* av_w_v,
+                double* av_e_v, double* av_s_v, double* av_n_v, double* av_b_v, double* av_t_v,
+                double* av_p_v, double* au_sw_v, double* au_nw_v, double* au_se_v,
+                double* au_ne_v, double* aw_sb_v, double* aw_nb_v, double* aw_st_v,
+                double* aw_nt_v, double* aw_w_w, double* aw_e_w, double* aw_s_w, double* aw_n_w,
+                double* aw_b_w, double* aw_t_w, double* aw_p_w, double* au_bw_w, double* au_tw_w,
+                double* au_be_w, double* au_te_w, double* av_bs_w, double* av_ts_w,
+                double* av_bn_w, double* av_tn_w, double* src_u, double* src_v, double* src_w,
+                double* un, double* vn, double* wn, double* uwall, double* dy, double* l1,
+                double* l2, double* phi);
+/* srcs/caldiv.f:1-70 */
+void caldiv_(int* ipara, int* ndiv, int* ni, int* nj, int* nk, double* dxinv, double* dyinv,
+             double* dzinv, double* dt, double* uk, double* vk, double* wk, double* div,
+             double* err_div);
+/* srcs/cal_coef_prs.f:1-57 (1-D arrays (-2:nj+3)) */
+void cal_coef_prs_(int* nj, double* rho, double* dxinv, double* dyinv, double* dzinv,
+                   double* aw_pk, double* ae_pk, double* as_pk, double* an_pk, double* ab_pk,
+                   double* at_pk, double* ap_pk);
+/* srcs/cal_coef_solp_fft.f:1-42 */
+void cal_coef_solp_fft_(int* nj, double* as_p, double* an_p, double* as_p_fft, double* an_p_fft,
+                        double* ap_p_fft);
+/* srcs/solp_fft_tdma1.f:1-50 (fftdata: scratch, not used) */
+void solp_fft_tdma1_(int* ni, int* nj, int* nk, double* fftdata, double* div, double* phir_r,
+                     double* phir_i);
+/* srcs/trans_r2w.f:1-111 (serial branch :23-38) */
+void trans_r2w_(int* ipara, int* ID, int* ndiv, int* svall, int* key, double* sendbuf,
+                double* recvbuf, double* r, double* w);
+/* srcs/trans_w2r.f:1-111 (serial branch :23-38) */
+void trans_w2r_(int* ipara, int* ID, int* ndiv, int* svall, int* key, double* sendbuf,
+                double* recvbuf, double* w, double* r);
+/* srcs/solp_fft_tdma2.f:1-91 (atdma, btdma_r, btdma_i: scratch, not used) */
+void solp_fft_tdma2_(int* ID, int* ndiv, int* svall, double* rho, double* dxinv, double* dzinv,
+                     double* as_p_fft, double* an_p_fft, double* ap_p_fft, double* atdma,
+                     double* btdma_r, double* btdma_i, double* phiw_r, double* phiw_i);
+/* srcs/solp_fft_tdma3.f:1-48 */
+void solp_fft_tdma3_(int* ni, int* nj, int* nk, double* fftdata, double* phir_r, double* phir_i,
+                     double* dp);
+/* srcs/solp_fft_tdma4.f:1-98 (prints the Err_solp monitor line every imon_t steps) */
+void solp_fft_tdma4_(int* ipara, int* ID, int* ndiv, int* ni, int* nj, int* nk, int* nstep,
+                     int* imon_t, double* rho, double* dxinv, double* dyinv, double* dzinv,
+                     double* div, double* dp);
+/* srcs/bnd_avzero.f:1-27 */
+void bnd_avzero_(int* ipara, int* ndiv, int* ni, int* nj, int* nk, double* q);
+/* srcs/corunp_explicit.f:1-78 */
+void corunp_explicit_(int* nID, int* ni, int* nj, int* nk, double* rho, double* dxinv,
+                      double* dyinv, double* dzinv, double* dt, double* dp, double* phat,
+                      double* un, double* vn, double* wn, double* pn);
+/* srcs/find_interface_positions_lower.f90:1-35 (prints -x_avg like the reference) */
+void find_interface_positions_lower_(int* ni, int* nj, int* nk, double* phi, double* dx,
+                                     double* dy, double* dz, double* xl);
+
+/* Monitors the reference prints, returned instead of printed (no counterpart
+ * with this signature in the reference; the values are those of
+ * srcs/solu_sor4.f:298-305 and srcs/solp_fft_tdma4.f:84-93). */
+int fmf_last_sor_iterations(void);      /* lp+1 of the last solu_sor4_ call */
+double fmf_last_sor_ratio(void);        /* err/err0 of the last solu_sor4_ call */
+double fmf_interface_lower(int ni, int nj, int nk, const double* phi_host, double dx,
+                           double xl);
+
+/* ------------------------------------------------------------------------ */
+/* Part 2: device-pointer variants (arrays are device pointers)             */
+/* ------------------------------------------------------------------------ */
+void fmf_dev_cal_advu_weno5(int ni, int nj, int nk, double dxinv, double dyinv, double dzinv,
+                            const double* u, const double* v, const double* w, double* adv_u,
+                            double* adv_v, double* adv_w);
+void fmf_dev_bnd_periodic(int ni, int nj, int nk, double* qk);
+
+/* ------------------------------------------------------------------------ */
+/* Part 3: the fused device-resident step (main.f90:473-697)                */
+/* ------------------------------------------------------------------------ */
+typedef struct {
+  int ni, nj, nk;                 /* nj: the wall-normal count; all powers of two */
+  double dx, dy, dz, dt;
+  double rhol, rhog, rmul, rmug;  /* phi=0 fluid (l) and phi=1 fluid (g) */
+  double sigma, uwall, grvb, grvp, bet_mthinc;
+  int harmonic;                   /* 0: cal_arith_coef_vis (as main.f90 calls it), 1: harmonic */
+  int precision;                  /* FMF_FP64 or FMF_MIXED */
+} fmf_params;
+enum { FMF_FP64 = 0, FMF_MIXED = 1 };
+
+typedef struct fmf_ctx fmf_ctx;
+/* state order: u v w uo vo wo p po phi0 phi1 phin0 phin1, each (ni+6)(nj+6)(nk+6) doubles */
+int fmf_ctx_create(const fmf_params* prm, fmf_ctx** out);
+int fmf_ctx_destroy(fmf_ctx* ctx);
+/* walls: theta0, zeta, l1, l2 as full 3-D host arrays (only the j=1 and j=nj planes are read) */
+int fmf_ctx_set_walls(fmf_ctx* ctx, const double* theta0, const double* zeta, const double* l1,
+                      const double* l2);
+int fmf_ctx_upload(fmf_ctx* ctx, const double* const* state);   /* host -> device, async */
+int fmf_ctx_download(fmf_ctx* ctx, double* const* state);       /* device -> host, async */
+int fmf_ctx_init_bc(fmf_ctx* ctx);                  /* start-up boundary pass, main.f90:322-366 */
+int fmf_ctx_step(fmf_ctx* ctx, int nsteps);         /* enqueue nsteps full time steps */
+int fmf_ctx_synchronize(fmf_ctx* ctx);
+int fmf_ctx_set_stream(fmf_ctx* ctx, void* cuda_stream);
+/* per-step SOR iteration counts of the last fmf_ctx_step call (up to cap entries) */
+int fmf_ctx_sor_iterations(fmf_ctx* ctx, int* out, int cap);
+/* device pointers of the state fields (for zero-copy consumers) */
+int fmf_ctx_state_device_ptr(fmf_ctx* ctx, int field, void** out);
+/* bytes of device memory held by the context */
+long long fmf_ctx_device_bytes(fmf_ctx* ctx);
+/* CUDA-event time of one stage of the step on the context stream (mean ms per
+ * launch over reps): 0 WENO5 advection, 1 one outer SOR iteration, 2 pressure
+ * FFT+TDMA, 3 MTHINC fluxes.  Measurement support; no counterpart in the reference. */
+int fmf_ctx_time_stage(fmf_ctx* ctx, int stage, int reps, float* ms);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
