@@ -196,7 +196,9 @@ double* Call::arr(void* host, size_t ndouble, bool written) {
     ok = false;
     return nullptr;
   }
-  if (mode() == 1 && !fresh) {
+  // coherent mode: the host copy is authoritative on entry (a merge may have
+  // placed older device contents over part of this range)
+  if (mode() == 1) {
     FMF_CUDA(cudaMemcpyAsync(d, host, ndouble * sizeof(double), cudaMemcpyHostToDevice, stream()));
   }
   if (written) outs.push_back(Out{host, d, ndouble * sizeof(double)});

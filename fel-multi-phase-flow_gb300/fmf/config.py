@@ -45,6 +45,7 @@ class Config:
     sigma: float = 1.0
     uwall: float = -1.0     # lower wall moves at -uwall, upper at +uwall (bndu.f:47,81)
     slip: float = 0.1       # slip length l1 = l2
+    zeta_coef: float | None = 0.1  # GNBC friction coefficient zeta (None: main.f90:172 formula)
     theta_lo: float = 90.0  # static angle, lower wall (deg)
     theta_hi: float = 90.0  # static angle, upper wall (deg)
     init: str = "stripe"    # stripe | stripe_perturbed | droplet
@@ -78,7 +79,12 @@ class Config:
 
     @property
     def zeta(self) -> float:
-        # main.f90:172: zeta = 0.21 * 6 * (mu_l / l1 + mu_g / l2)
+        """Contact-line friction coefficient of the GNBC law cos(theta_d) = cos(theta_0) -
+        zeta*u_cl/sigma (gnbc.f90:47).  The workloads state one "GNBC slip coefficient" of
+        0.1; it is used both as this zeta and as the Navier slip length (bndu.f:39-45).
+        zeta_coef=None falls back to the reference's own formula (main.f90:172)."""
+        if self.zeta_coef is not None:
+            return self.zeta_coef
         return 0.21 * 6.0 * (self.rmul / self.slip + self.rmug / self.slip)
 
     def scaled(self, ni: int, nj: int, nk: int, **kw) -> "Config":
