@@ -50,6 +50,14 @@ int g_last_sor_iters = 0;
 double g_last_sor_ratio = 0.0;
 }  // namespace
 
+// Every array argument is resolved (evaluated as a macro argument) before the
+// launch; nothing is launched if any of them failed.
+template <class F, class... A>
+inline void launch_if(Call& call, F f, A... a) {
+  if (call.ok) f(a...);
+}
+#define FMF_LAUNCH(fn, ...) launch_if(call, [&](auto... a_) { fn(a_...); }, __VA_ARGS__)
+
 #define GRID3 \
   if (!check_grid(*ni, *nj, *nk)) return; \
   const Grid g(*ni, *nj, *nk);            \
@@ -101,14 +109,14 @@ void cal_grad_p2a_(int* ID, int* svall, int* ni, int* nj, int* nk, double* dxinv
   GRID3;
   double dy;
   if (!uniform_dy(dyinv_array, *ID, *nj, &dy)) return;
-  op::cal_grad_p2a(s, g, *dxinv, dy, *dzinv, call.in(q, N3), call.out(qx, N3), call.out(qy, N3), call.out(qz, N3));
+  FMF_LAUNCH(op::cal_grad_p2a, s, g, *dxinv, dy, *dzinv, call.in(q, N3), call.out(qx, N3), call.out(qy, N3), call.out(qz, N3));
   call.finish();
 }
 void solphi_mthinc1_(int* ni, int* nj, int* nk, double* dxinv, double* dyinv, double* dzinv, double* dt,
                      double* bet, double* phi, double* phix, double* phiy, double* phiz, double* u, double* v,
                      double* w, double* flx, double* fly, double* flz) {
   GRID3;
-  op::solphi_mthinc1(s, g, *dxinv, *dyinv, *dzinv, *dt, *bet, call.in(phi, N3), call.in(phix, N3),
+  FMF_LAUNCH(op::solphi_mthinc1, s, g, *dxinv, *dyinv, *dzinv, *dt, *bet, call.in(phi, N3), call.in(phix, N3),
                      call.in(phiy, N3), call.in(phiz, N3), call.in(u, N3), call.in(v, N3), call.in(w, N3),
                      call.out(flx, N3), call.out(fly, N3), call.out(flz, N3));
   call.finish();
@@ -117,7 +125,7 @@ void solphi_mthinc2_(int* ni, int* nj, int* nk, double* dxinv, double* dyinv, do
                      double* u, double* v, double* w, double* flx, double* fly, double* flz, double* phi,
                      double* phin) {
   GRID3;
-  op::solphi_mthinc2(s, g, *dxinv, *dyinv, *dzinv, *dt, call.in(u, N3), call.in(v, N3), call.in(w, N3),
+  FMF_LAUNCH(op::solphi_mthinc2, s, g, *dxinv, *dyinv, *dzinv, *dt, call.in(u, N3), call.in(v, N3), call.in(w, N3),
                      call.in(flx, N3), call.in(fly, N3), call.in(flz, N3), call.in(phi, N3), call.out(phin, N3));
   call.finish();
 }
@@ -126,7 +134,7 @@ void solphi_mthinc3_(int* ipara, int* ni, int* nj, int* nk, double* dxinv, doubl
   if (!one_rank(ipara)) return;
   GRID3;
   double* sums = (double*)scratch(sizeof(double) * 4, 2);
-  op::solphi_mthinc3(s, g, *dxinv, *dyinv, *dzinv, *bet, call.in(phix, N3), call.in(phiy, N3),
+  FMF_LAUNCH(op::solphi_mthinc3, s, g, *dxinv, *dyinv, *dzinv, *bet, call.in(phix, N3), call.in(phiy, N3),
                      call.in(phiz, N3), call.in(phi, N3), call.out(phin, N3), sums);
   call.finish();
 }
@@ -137,7 +145,7 @@ void summation_(int* ni, int* nj, int* nk, double* qk, int* nbub) {
     return;
   }
   double* d = call.out(qk, 2 * N3);
-  op::summation(s, g, d, d + N3);
+  FMF_LAUNCH(op::summation, s, g, d, d + N3);
   call.finish();
 }
 
@@ -146,7 +154,7 @@ void gnbc_(int* nID, int* ni, int* nj, int* nk, double* uk, double* wk, double* 
            double* sigma, double* zeta, double* theta) {
   if (!walls_only(nID)) return;
   GRID3;
-  op::gnbc(s, g, call.in(uk, N3), call.in(wk, N3), *uwall, call.in(theta0, N3), *sigma, call.in(zeta, N3),
+  FMF_LAUNCH(op::gnbc, s, g, call.in(uk, N3), call.in(wk, N3), *uwall, call.in(theta0, N3), *sigma, call.in(zeta, N3),
            call.out(theta, N3));
   call.finish();
 }
@@ -154,26 +162,26 @@ void bnd_contact_angle_(int* nID, int* ni, int* nj, int* nk, double* qk, double*
                         double* dz) {
   if (!walls_only(nID)) return;
   GRID3;
-  op::bnd_contact_angle(s, g, call.out(qk, N3), call.in(theta, N3), *dx, *dy, *dz);
+  FMF_LAUNCH(op::bnd_contact_angle, s, g, call.out(qk, N3), call.in(theta, N3), *dx, *dy, *dz);
   call.finish();
 }
 void bndu_(int* nID, int* ni, int* nj, int* nk, double* uk, double* vk, double* wk, double* uwall, double* dy,
            double* l1, double* l2, double* phi) {
   if (!walls_only(nID)) return;
   GRID3;
-  op::bndu(s, g, call.out(uk, N3), call.out(vk, N3), call.out(wk, N3), *uwall, *dy, call.in(l1, N3),
+  FMF_LAUNCH(op::bndu, s, g, call.out(uk, N3), call.out(vk, N3), call.out(wk, N3), *uwall, *dy, call.in(l1, N3),
            call.in(l2, N3), call.in(phi, N3));
   call.finish();
 }
 void bnd_periodic_(int* ni, int* nj, int* nk, double* qk) {
   GRID3;
-  op::bnd_periodic(s, g, call.out(qk, N3));
+  FMF_LAUNCH(op::bnd_periodic, s, g, call.out(qk, N3));
   call.finish();
 }
 void bnd_neumann_(int* nID, int* ni, int* nj, int* nk, double* qk) {
   if (!walls_only(nID)) return;
   GRID3;
-  op::bnd_neumann(s, g, call.out(qk, N3));
+  FMF_LAUNCH(op::bnd_neumann, s, g, call.out(qk, N3));
   call.finish();
 }
 void bnd_comm_(int* ipara, int*, int*, int*, int*, int*, double*, double*, double*) { one_rank(ipara); }
@@ -182,7 +190,7 @@ void bnd_comm_(int* ipara, int*, int*, int*, int*, int*, double*, double*, doubl
 void cal_advu_weno5_(int* ni, int* nj, int* nk, double* dxinv, double* dyinv, double* dzinv, double* u,
                      double* v, double* w, double* au, double* av, double* aw) {
   GRID3;
-  op::cal_advu_weno5(s, g, *dxinv, *dyinv, *dzinv, call.in(u, N3), call.in(v, N3), call.in(w, N3),
+  FMF_LAUNCH(op::cal_advu_weno5, s, g, *dxinv, *dyinv, *dzinv, call.in(u, N3), call.in(v, N3), call.in(w, N3),
                      call.out(au, N3), call.out(av, N3), call.out(aw, N3));
   call.finish();
 }
@@ -190,47 +198,47 @@ void cal_advu_weno5_(int* ni, int* nj, int* nk, double* dxinv, double* dyinv, do
 // ---------------------------------------------------------------- C6
 void cal_arith_mean_(int* ni, int* nj, int* nk, double* phik, double* ql, double* qg, double* qk) {
   GRID3;
-  op::cal_arith_mean(s, g, call.in(phik, N3), *ql, *qg, call.out(qk, N3));
+  FMF_LAUNCH(op::cal_arith_mean, s, g, call.in(phik, N3), *ql, *qg, call.out(qk, N3));
   call.finish();
 }
 void cal_harm_mean_(int* ni, int* nj, int* nk, double* phik, double* ql, double* qg, double* qk) {
   GRID3;
-  op::cal_harm_mean(s, g, call.in(phik, N3), *ql, *qg, call.out(qk, N3));
+  FMF_LAUNCH(op::cal_harm_mean, s, g, call.in(phik, N3), *ql, *qg, call.out(qk, N3));
   call.finish();
 }
 void calphat_(int* ni, int* nj, int* nk, double* p, double* po, double* phat) {
   GRID3;
-  op::calphat(s, g, call.in(p, N3), call.in(po, N3), call.out(phat, N3));
+  FMF_LAUNCH(op::calphat, s, g, call.in(p, N3), call.in(po, N3), call.out(phat, N3));
   call.finish();
 }
 void cal_grad_prs_(int* ni, int* nj, int* nk, double* dxinv, double* dyinv, double* dzinv, double* q,
                    double* qx, double* qy, double* qz) {
   GRID3;
-  op::cal_grad_prs(s, g, *dxinv, *dyinv, *dzinv, call.in(q, N3), call.out(qx, N3), call.out(qy, N3),
+  FMF_LAUNCH(op::cal_grad_prs, s, g, *dxinv, *dyinv, *dzinv, call.in(q, N3), call.out(qx, N3), call.out(qy, N3),
                    call.out(qz, N3));
   call.finish();
 }
 void calsij_(int* ni, int* nj, int* nk, double* dxinv, double* dyinv, double* dzinv, double* uk, double* vk,
              double* wk, double* sk) {
   GRID3;
-  op::calsij(s, g, *dxinv, *dyinv, *dzinv, call.in(uk, N3), call.in(vk, N3), call.in(wk, N3),
+  FMF_LAUNCH(op::calsij, s, g, *dxinv, *dyinv, *dzinv, call.in(uk, N3), call.in(vk, N3), call.in(wk, N3),
              call.out(sk, 6 * N3));
   call.finish();
 }
 void cal_arith_tau_(int* ni, int* nj, int* nk, double* sk, double* rmu, double* tau) {
   GRID3;
-  op::cal_tau(s, g, call.in(sk, 6 * N3), call.in(rmu, N3), call.out(tau, 6 * N3), false);
+  FMF_LAUNCH(op::cal_tau, s, g, call.in(sk, 6 * N3), call.in(rmu, N3), call.out(tau, 6 * N3), false);
   call.finish();
 }
 void cal_harm_tau_(int* ni, int* nj, int* nk, double* sk, double* rmu, double* tau) {
   GRID3;
-  op::cal_tau(s, g, call.in(sk, 6 * N3), call.in(rmu, N3), call.out(tau, 6 * N3), true);
+  FMF_LAUNCH(op::cal_tau, s, g, call.in(sk, 6 * N3), call.in(rmu, N3), call.out(tau, 6 * N3), true);
   call.finish();
 }
 void cal_div_tensor_(int* ni, int* nj, int* nk, double* dxinv, double* dyinv, double* dzinv, double* tau,
                      double* uk, double* vk, double* wk) {
   GRID3;
-  op::cal_div_tensor(s, g, *dxinv, *dyinv, *dzinv, call.in(tau, 6 * N3), call.out(uk, N3), call.out(vk, N3),
+  FMF_LAUNCH(op::cal_div_tensor, s, g, *dxinv, *dyinv, *dzinv, call.in(tau, 6 * N3), call.out(uk, N3), call.out(vk, N3),
                      call.out(wk, N3));
   call.finish();
 }
@@ -241,14 +249,14 @@ void calrn_(int* ni, int* nj, int* nk, double* dxinv, double* dyinv, double* dzi
     set_status(FMF_ERR_ARG);
     return;
   }
-  op::calrn(s, g, *dxinv, *dyinv, *dzinv, *ip, *jp, *kp, call.in(phix, N3), call.in(phiy, N3),
+  FMF_LAUNCH(op::calrn, s, g, *dxinv, *dyinv, *dzinv, *ip, *jp, *kp, call.in(phix, N3), call.in(phiy, N3),
             call.in(phiz, N3), call.out(rn, 3 * N3));
   call.finish();
 }
 void calrkap_(int* ni, int* nj, int* nk, double* dxinv, double* dyinv, double* dzinv, double* rpp,
               double* r12, double* r13, double* r23, double* rkap) {
   GRID3;
-  op::calrkap(s, g, *dxinv, *dyinv, *dzinv, call.in(rpp, 3 * N3), call.in(r12, 3 * N3), call.in(r13, 3 * N3),
+  FMF_LAUNCH(op::calrkap, s, g, *dxinv, *dyinv, *dzinv, call.in(rpp, 3 * N3), call.in(r12, 3 * N3), call.in(r13, 3 * N3),
               call.in(r23, 3 * N3), call.out(rkap, 3 * N3));
   call.finish();
 }
@@ -258,29 +266,29 @@ void cal_grad_p2uvw_(int* ID, int* svall, int* ni, int* nj, int* nk, double* dxi
   GRID3;
   double dy;
   if (!uniform_dy(dyinv_array, *ID, *nj, &dy)) return;
-  op::cal_grad_prs(s, g, *dxinv, dy, *dzinv, call.in(q, N3), call.out(qx, N3), call.out(qy, N3),
+  FMF_LAUNCH(op::cal_grad_prs, s, g, *dxinv, dy, *dzinv, call.in(q, N3), call.out(qx, N3), call.out(qy, N3),
                    call.out(qz, N3));
   call.finish();
 }
 void calfst_(int* ni, int* nj, int* nk, double* rhol, double* rhog, double* sigma, double* gx, double* gy,
              double* gz, double* rkap, double* fu, double* fv, double* fw) {
   GRID3;
-  op::calfst(s, g, *rhol, *rhog, *sigma, call.in(gx, N3), call.in(gy, N3), call.in(gz, N3),
+  FMF_LAUNCH(op::calfst, s, g, *rhol, *rhog, *sigma, call.in(gx, N3), call.in(gy, N3), call.in(gz, N3),
              call.in(rkap, 3 * N3), call.out(fu, N3), call.out(fv, N3), call.out(fw, N3));
   call.finish();
 }
 void sum_fst_(int* ni, int* nj, int* nk, double* fu, double* fv, double* fw, double* su, double* sv,
               double* sw) {
   GRID3;
-  op::sum_fst(s, g, call.in(fu, N3), call.in(fv, N3), call.in(fw, N3), call.out(su, N3), call.out(sv, N3),
+  FMF_LAUNCH(op::sum_fst, s, g, call.in(fu, N3), call.in(fv, N3), call.in(fw, N3), call.out(su, N3), call.out(sv, N3),
               call.out(sw, N3));
   call.finish();
 }
 void init_q_(int* ni, int* nj, int* nk, double* q1, double* q2, double* q3) {
   GRID3;
-  op::fill(s, N3, call.out(q1, N3), 0.0);
-  op::fill(s, N3, call.out(q2, N3), 0.0);
-  op::fill(s, N3, call.out(q3, N3), 0.0);
+  FMF_LAUNCH(op::fill, s, N3, call.out(q1, N3), 0.0);
+  FMF_LAUNCH(op::fill, s, N3, call.out(q2, N3), 0.0);
+  FMF_LAUNCH(op::fill, s, N3, call.out(q3, N3), 0.0);
   call.finish();
 }
 void cal_av_(int* ipara, int* ndiv, int* ni, int* nj, int* nk, double* q, double* av) {
@@ -288,7 +296,7 @@ void cal_av_(int* ipara, int* ndiv, int* ni, int* nj, int* nk, double* q, double
   (void)ndiv;
   GRID3;
   double* d = (double*)scratch(sizeof(double) * 2, 3);
-  op::cal_av(s, g, call.in(q, N3), d);
+  FMF_LAUNCH(op::cal_av, s, g, call.in(q, N3), d);
   FMF_CUDA(cudaMemcpyAsync(av, d, sizeof(double), cudaMemcpyDeviceToHost, s));
   FMF_CUDA(cudaStreamSynchronize(s));
   if (!std::isfinite(*av)) set_status(FMF_ERR_NONFINITE);
@@ -310,13 +318,13 @@ void cal_srcu_(int* nID, int* ni, int* nj, int* nk, double* rho_av, double* dt, 
   const double* fst[3] = {call.in(fst_u, N3), call.in(fst_v, N3), call.in(fst_w, N3)};
   const double* fstn[3] = {call.in(fst_un, N3), call.in(fst_vn, N3), call.in(fst_wn, N3)};
   double* src[3] = {call.out(src_u, N3), call.out(src_v, N3), call.out(src_w, N3)};
-  op::cal_srcu(s, g, *dt, *grvb, *grvp, call.in(u, N3), call.in(v, N3), call.in(w, N3), call.in(rho, N3),
+  FMF_LAUNCH(op::cal_srcu, s, g, *dt, *grvb, *grvp, call.in(u, N3), call.in(v, N3), call.in(w, N3), call.in(rho, N3),
                call.in(rhon, N3), adv, advo, prs, vis, fst, fstn, src);
   call.finish();
 }
 void cpy_(int* ni, int* nj, int* nk, double* q1, double* q2) {
   GRID3;
-  op::copy(s, N3, call.in(q1, N3), call.out(q2, N3));
+  FMF_LAUNCH(op::copy, s, N3, call.in(q1, N3), call.out(q2, N3));
   call.finish();
 }
 
@@ -326,7 +334,7 @@ static void coef_vis_impl(int* ni, int* nj, int* nk, double* dxinv, double* dyin
   GRID3;
   double* d[45];
   for (int q = 0; q < 45; ++q) d[q] = call.out(c45[q], N3);
-  op::cal_coef_vis(s, g, *dxinv, *dyinv, *dzinv, call.in(rmu, N3), d, harmonic);
+  FMF_LAUNCH(op::cal_coef_vis, s, g, *dxinv, *dyinv, *dzinv, call.in(rmu, N3), d, harmonic);
   call.finish();
 }
 #define C45_PARAMS                                                                                        \
@@ -372,6 +380,7 @@ void solu_sor4_(int* ipara, int* ID, int* nID, int* ndiv, int* ni, int* nj, int*
   const double* dl2 = call.in(l2, N3);
   const double* dphi = call.in(phi, N3);
   double* es = (double*)scratch(sizeof(double) * 2, 1);
+  if (!call.ok || !es) return;
   double err = 0.0, err0 = 0.0;
   int lp;
   for (lp = 0; lp <= 20; ++lp) {
@@ -401,7 +410,7 @@ void caldiv_(int* ipara, int* ndiv, int* ni, int* nj, int* nk, double* dxinv, do
   (void)ndiv;
   GRID3;
   double* e = (double*)scratch(sizeof(double) * 2, 3);
-  op::caldiv(s, g, *dxinv, *dyinv, *dzinv, *dt, call.in(uk, N3), call.in(vk, N3), call.in(wk, N3),
+  FMF_LAUNCH(op::caldiv, s, g, *dxinv, *dyinv, *dzinv, *dt, call.in(uk, N3), call.in(vk, N3), call.in(wk, N3),
              call.out(div, N3), e);
   FMF_CUDA(cudaMemcpyAsync(err_div, e, sizeof(double), cudaMemcpyDeviceToHost, s));
   FMF_CUDA(cudaStreamSynchronize(s));
@@ -448,7 +457,7 @@ void solp_fft_tdma1_(int* ni, int* nj, int* nk, double* fftdata, double* div, do
   (void)fftdata;
   GRID3;
   const long nm = g.cells();
-  op::fft_forward_planes(s, g, call.in(div, N3), call.out(pr, nm), call.out(pi, nm));
+  FMF_LAUNCH(op::fft_forward_planes, s, g, call.in(div, N3), call.out(pr, nm), call.out(pi, nm));
   call.finish();
 }
 void trans_r2w_(int* ipara, int* ID, int* ndiv, int* svall, int* key, double* sendbuf, double* recvbuf, double* r,
@@ -460,7 +469,7 @@ void trans_r2w_(int* ipara, int* ID, int* ndiv, int* svall, int* key, double* se
   if (!one_rank(ipara) || *ndiv != 1) return;
   const long nm = (long)svall[0] * svall[1] * svall[2];
   Call call;
-  op::copy(stream(), nm, call.in(r, nm), call.out(w, nm));
+  FMF_LAUNCH(op::copy, stream(), nm, call.in(r, nm), call.out(w, nm));
   call.finish();
 }
 void trans_w2r_(int* ipara, int* ID, int* ndiv, int* svall, int* key, double* sendbuf, double* recvbuf, double* w,
@@ -472,7 +481,7 @@ void trans_w2r_(int* ipara, int* ID, int* ndiv, int* svall, int* key, double* se
   if (!one_rank(ipara) || *ndiv != 1) return;
   const long nm = (long)svall[0] * svall[1] * svall[2];
   Call call;
-  op::copy(stream(), nm, call.in(w, nm), call.out(r, nm));
+  FMF_LAUNCH(op::copy, stream(), nm, call.in(w, nm), call.out(r, nm));
   call.finish();
 }
 void solp_fft_tdma2_(int* ID, int* ndiv, int* svall, double* rho, double* dxinv, double* dzinv, double* as_f,
@@ -490,7 +499,7 @@ void solp_fft_tdma2_(int* ID, int* ndiv, int* svall, double* rho, double* dxinv,
   const Grid g(ni, nj, nk);
   const long nm = g.cells();
   Call call;
-  op::tdma_modes(stream(), g, *rho, *dxinv, *dzinv, call.in(as_f, nj + 6), call.in(an_f, nj + 6),
+  FMF_LAUNCH(op::tdma_modes, stream(), g, *rho, *dxinv, *dzinv, call.in(as_f, nj + 6), call.in(an_f, nj + 6),
                  call.in(ap_f, nj + 6), call.out(pr, nm), call.out(pi, nm));
   call.finish();
 }
@@ -498,7 +507,7 @@ void solp_fft_tdma3_(int* ni, int* nj, int* nk, double* fftdata, double* pr, dou
   (void)fftdata;
   GRID3;
   const long nm = g.cells();
-  op::fft_inverse_planes(s, g, call.in(pr, nm), call.in(pi, nm), call.out(dp, N3));
+  FMF_LAUNCH(op::fft_inverse_planes, s, g, call.in(pr, nm), call.in(pi, nm), call.out(dp, N3));
   call.finish();
 }
 void solp_fft_tdma4_(int* ipara, int* ID, int* ndiv, int* ni, int* nj, int* nk, int* nstep, int* imon_t,
@@ -508,7 +517,7 @@ void solp_fft_tdma4_(int* ipara, int* ID, int* ndiv, int* ni, int* nj, int* nk, 
   if (*imon_t <= 0 || (*nstep % *imon_t) != 0) return;
   GRID3;
   double* d = (double*)scratch(sizeof(double) * 2, 3);
-  op::poisson_residual(s, g, *rho, *dxinv, *dyinv, *dzinv, call.in(div, N3), call.in(dp, N3), d);
+  FMF_LAUNCH(op::poisson_residual, s, g, *rho, *dxinv, *dyinv, *dzinv, call.in(div, N3), call.in(dp, N3), d);
   double h[2];
   FMF_CUDA(cudaMemcpyAsync(h, d, sizeof(h), cudaMemcpyDeviceToHost, s));
   FMF_CUDA(cudaStreamSynchronize(s));
@@ -521,7 +530,7 @@ void bnd_avzero_(int* ipara, int* ndiv, int* ni, int* nj, int* nk, double* q) {
   if (!one_rank(ipara)) return;
   (void)ndiv;
   GRID3;
-  op::bnd_avzero(s, g, call.out(q, N3));
+  FMF_LAUNCH(op::bnd_avzero, s, g, call.out(q, N3));
   call.finish();
 }
 void corunp_explicit_(int* nID, int* ni, int* nj, int* nk, double* rho, double* dxinv, double* dyinv,
@@ -529,7 +538,7 @@ void corunp_explicit_(int* nID, int* ni, int* nj, int* nk, double* rho, double* 
                       double* pn) {
   if (!walls_only(nID)) return;
   GRID3;
-  op::corunp_explicit(s, g, *rho, *dxinv, *dyinv, *dzinv, *dt, call.in(dp, N3), call.in(phat, N3),
+  FMF_LAUNCH(op::corunp_explicit, s, g, *rho, *dxinv, *dyinv, *dzinv, *dt, call.in(dp, N3), call.in(phat, N3),
                       call.out(un, N3), call.out(vn, N3), call.out(wn, N3), call.out(pn, N3));
   call.finish();
 }
@@ -563,11 +572,19 @@ void find_interface_positions_lower_(int* ni, int* nj, int* nk, double* phi, dou
 void fmf_dev_cal_advu_weno5(int ni, int nj, int nk, double dxinv, double dyinv, double dzinv, const double* u,
                             const double* v, const double* w, double* au, double* av, double* aw) {
   if (!check_grid(ni, nj, nk)) return;
+  if (!u || !v || !w || !au || !av || !aw) {
+    set_status(FMF_ERR_ARG);
+    return;
+  }
   op::cal_advu_weno5(stream(), Grid(ni, nj, nk), dxinv, dyinv, dzinv, u, v, w, au, av, aw);
   FMF_CUDA(cudaGetLastError());
 }
 void fmf_dev_bnd_periodic(int ni, int nj, int nk, double* qk) {
   if (!check_grid(ni, nj, nk)) return;
+  if (!qk) {
+    set_status(FMF_ERR_ARG);
+    return;
+  }
   op::bnd_periodic(stream(), Grid(ni, nj, nk), qk);
   FMF_CUDA(cudaGetLastError());
 }

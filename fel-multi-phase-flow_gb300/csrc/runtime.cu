@@ -85,7 +85,7 @@ struct Entry {
 static std::map<uintptr_t, Entry> g_reg;
 static std::mutex g_mu;
 
-static char* lookup_locked(uintptr_t a, uintptr_t b, bool* fresh) {
+static char* lookup_locked(uintptr_t a, uintptr_t b, bool* fresh, const std::vector<uintptr_t>* protect) {
   *fresh = false;
   auto it = g_reg.upper_bound(a);
   if (it != g_reg.begin()) {
@@ -104,6 +104,15 @@ static char* lookup_locked(uintptr_t a, uintptr_t b, bool* fresh) {
   for (auto& e : ov) {
     lo = std::min(lo, e->first);
     hi = std::max(hi, e->second.end);
+    // a mirror already handed to this call must stay where it is
+    if (protect)
+      for (uintptr_t key : *protect)
+        if (key == e->first) {
+          std::fprintf(stderr, "fmf: arguments of one call overlap partially in host memory; register the "
+                               "enclosing array first (fmf_sync_to_device)\n");
+          set_status(2);
+          return nullptr;
+        }
   }
   char* dev = nullptr;
   if (!FMF_CUDA(cudaMalloc(&dev, hi - lo))) {
@@ -126,10 +135,15 @@ static char* lookup_locked(uintptr_t a, uintptr_t b, bool* fresh) {
   return dev + (a - lo);
 }
 
-void* mirror(const void* host, size_t bytes, bool* fresh) {
+void* mirror(const void* host, size_t bytes, bool* fresh, std::vector<uintptr_t>* protect) {
   std::lock_guard<std::mutex> lk(g_mu);
   const uintptr_t a = (uintptr_t)host;
-  return lookup_locked(a, a + bytes, fresh);
+  char* d = lookup_locked(a, a + bytes, fresh, protect);
+  if (d && protect) {
+    auto it = std::prev(g_reg.upper_bound(a));
+    protect->push_back(it->first);
+  }
+  return d;
 }
 
 int sync_to_host(const void* host, size_t bytes_or_0) {
@@ -184,33 +198,51 @@ int reset_registry() {
 }
 
 // ---- one call's argument set -----------------------------------------------
+// Resident mode: registry mirrors; a mirror handed out earlier in this call is
+// protected from merges.  Coherent mode: a temporary device buffer per argument,
+// uploaded now and (if written) downloaded and freed in finish(); nothing persists.
 double* Call::arr(void* host, size_t ndouble, bool written) {
-  if (!host) {
-    ok = false;
-    set_status(2);
-    return nullptr;
-  }
-  bool fresh = false;
-  double* d = (double*)mirror(host, ndouble * sizeof(double), &fresh);
-  if (!d) {
+  if (!host || !ok) {
+    if (!host) set_status(2);
     ok = false;
     return nullptr;
   }
-  // coherent mode: the host copy is authoritative on entry (a merge may have
-  // placed older device contents over part of this range)
+  const size_t bytes = ndouble * sizeof(double);
+  double* d = nullptr;
   if (mode() == 1) {
-    FMF_CUDA(cudaMemcpyAsync(d, host, ndouble * sizeof(double), cudaMemcpyHostToDevice, stream()));
+    if (!FMF_CUDA(cudaMalloc((void**)&d, bytes))) {
+      set_status(5);
+      ok = false;
+      return nullptr;
+    }
+    temps.push_back(d);
+    FMF_CUDA(cudaMemcpyAsync(d, host, bytes, cudaMemcpyHostToDevice, stream()));
+  } else {
+    bool fresh = false;
+    d = (double*)mirror(host, bytes, &fresh, &protect);
+    if (!d) {
+      ok = false;
+      return nullptr;
+    }
   }
-  if (written) outs.push_back(Out{host, d, ndouble * sizeof(double)});
+  if (written) outs.push_back(Out{host, d, bytes});
   return d;
 }
 void Call::finish() {
   cudaStream_t s = stream();
   FMF_CUDA(cudaGetLastError());
   if (mode() == 1) {
-    for (auto& o : outs) FMF_CUDA(cudaMemcpyAsync(o.host, o.dev, o.bytes, cudaMemcpyDeviceToHost, s));
+    if (ok)
+      for (auto& o : outs) FMF_CUDA(cudaMemcpyAsync(o.host, o.dev, o.bytes, cudaMemcpyDeviceToHost, s));
     FMF_CUDA(cudaStreamSynchronize(s));
   }
+  release();
+}
+void Call::release() {
+  if (temps.empty()) return;
+  FMF_CUDA(cudaStreamSynchronize(stream()));
+  for (double* t : temps) FMF_CUDA(cudaFree(t));
+  temps.clear();
 }
 
 }  // namespace fmf

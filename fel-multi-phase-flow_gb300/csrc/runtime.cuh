@@ -1,5 +1,6 @@
 // runtime.cuh -- library runtime shared by the C-ABI translation units.
 #pragma once
+#include <cstdint>
 #include <vector>
 
 #include "fmf_common.cuh"
@@ -11,16 +12,18 @@ long long launches();
 void set_stream(cudaStream_t s);
 int mode();
 void set_mode(int m);
-void* mirror(const void* host, size_t bytes, bool* fresh);
+void* mirror(const void* host, size_t bytes, bool* fresh, std::vector<uintptr_t>* protect);
 int sync_to_host(const void* host, size_t bytes_or_0);
 int sync_to_device(const void* host, size_t bytes_or_0);
 int sync_all_to_host();
 int forget(const void* host);
 int reset_registry();
 
-// The array arguments of one drop-in call: arr() returns the device mirror of a
-// host array (uploading it when first seen, or on every call in coherent mode);
-// finish() downloads the written arrays in coherent mode.
+// The array arguments of one drop-in call.  arr() returns the device copy of a
+// host array: in resident mode the registry mirror (uploaded when first seen),
+// in coherent mode a temporary buffer uploaded now.  An entry point resolves all
+// of its arrays first and launches only if ok is still true; finish() downloads
+// the written arrays in coherent mode and frees the temporaries.
 struct Call {
   struct Out {
     void* host;
@@ -28,11 +31,15 @@ struct Call {
     size_t bytes;
   };
   std::vector<Out> outs;
+  std::vector<uintptr_t> protect;
+  std::vector<double*> temps;
   bool ok = true;
   double* arr(void* host, size_t ndouble, bool written);
   double* in(void* host, size_t ndouble) { return arr(host, ndouble, false); }
   double* out(void* host, size_t ndouble) { return arr(host, ndouble, true); }
   void finish();
+  void release();
+  ~Call() { release(); }
 };
 
 }  // namespace fmf

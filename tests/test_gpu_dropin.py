@@ -149,7 +149,7 @@ def test_gnbc_contact_angle_bndu(orc, L):
     theta = np.zeros(SH)
     args = [("ia", NID)] + dims() + [("a", u), ("a", w), ("d", -1.0), ("a", th0), ("d", 1.0), ("a", ze),
                                      ("a", theta)]
-    o, g = both(orc, L, "gnbc", args, [6])
+    o, g = both(orc, L, "gnbc", args, [4])
     check(o, g, TRANSC)
     args = [("ia", NID)] + dims() + [("a", phi_field()), ("a", o[0]), ("d", CFG.dx), ("d", CFG.dy), ("d", CFG.dz)]
     o2, g2 = both(orc, L, "bnd_contact_angle", args, [0])
@@ -287,7 +287,7 @@ def test_pressure(orc, L):
     args = [("i", 0), ("i", 1), ("ia", [NI, NJ, NK]), ("d", 1.0), ("d", 1 / CFG.dx), ("d", 1 / CFG.dz),
             ("a", as_f), ("a", an_f), ("a", ap_f), ("none", None), ("none", None), ("none", None),
             ("a", o[0]), ("a", o[1])]
-    o2, g2 = both(orc, L, "solp_fft_tdma2", args, [6, 7])
+    o2, g2 = both(orc, L, "solp_fft_tdma2", args, [3, 4])
     check(o2, g2, 1e-12)
     args = dims() + [("a", np.zeros(2 * n)), ("a", o2[0]), ("a", o2[1]), ("a", np.zeros(SH))]
     o3, g3 = both(orc, L, "solp_fft_tdma3", args, [3])
