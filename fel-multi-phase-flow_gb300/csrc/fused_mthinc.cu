@@ -1,0 +1,183 @@
+// fused_mthinc.cu -- MTHINC fluxes (solphi_mthinc1.f) for the fused step.
+//
+// Two kernels instead of one thread per cell on the full 0..n+1 range:
+//   k_classify: every cell forms its normal from the 8 vertex gradients; cells
+//     outside the interface band write their truncated upwind fluxes at once,
+//     band cells are appended to a compact list;
+//   k_band: one thread per band cell (list entry) runs the 10 Newton steps and
+//     writes the swept-volume fluxes.
+// A warp then carries band cells only, instead of idling on the bulk cells that
+// share its x-run.  The sigmoid derivative uses 1/cosh^2(a) = 4 s (1 - s) with
+// s = 1/(1 + exp(-2a)) (same function, one exp per Gauss point).
+//
+// Face ownership: a face is written by its donor cell (u>0: the west cell, u<0:
+// the east cell) or left zero; cells write their east/north/top face when u>=0
+// and their west/south/bottom face when u<0, so every face in 0..n of every
+// interior row gets exactly one writer (solphi_mthinc1.f:121-130 zeroes first;
+// faces nobody donates through hold the zero written by k_classify's owner).
+#include "fused.cuh"
+
+namespace fmf {
+namespace fused {
+
+namespace {
+struct MC {
+  double gp1, gp2, lim, eps_trunc, bet, dt, dxi, dyi, dzi;
+};
+
+__device__ __forceinline__ double avg8(const double* __restrict__ p, long c, long X, long Y, long Z) {
+  return (__ldg(p + c - X - Y - Z) + __ldg(p + c - Y - Z) + __ldg(p + c - X - Z) + __ldg(p + c - Z) +
+          __ldg(p + c - X - Y) + __ldg(p + c - Y) + __ldg(p + c - X) + __ldg(p + c)) *
+         0.125;
+}
+
+// sum over the 8 Gauss points of w/(1+exp(-2 bet (x_t + d))); optionally the sum of s(1-s)
+__device__ __forceinline__ double sig8(const double* a, double w, double m2b, double d, double* sd) {
+  double s = 0.0, q = 0.0;
+#pragma unroll
+  for (int t = 0; t < 8; ++t) {
+    const double e = exp(m2b * (a[t] + d));
+    const double r = 1.0 / (1.0 + e);
+    s += r;
+    if (sd) q += e * r * r;  // s(1-s) with 1-s = e/(1+e), exact in relative terms for any a
+  }
+  if (sd) *sd = q;
+  return w * s;
+}
+__device__ __forceinline__ void gauss8(double* a, double rnx, double rny, double rnz, double x1g, double x2g,
+                                       double y1g, double y2g, double z1g, double z2g) {
+  const double x1 = rnx * x1g, x2 = rnx * x2g, y1 = rny * y1g, y2 = rny * y2g, z1 = rnz * z1g, z2 = rnz * z2g;
+  a[0] = x1 + y1 + z1;
+  a[1] = x2 + y1 + z1;
+  a[2] = x1 + y2 + z1;
+  a[3] = x2 + y2 + z1;
+  a[4] = x1 + y1 + z2;
+  a[5] = x2 + y1 + z2;
+  a[6] = x1 + y2 + z2;
+  a[7] = x2 + y2 + z2;
+}
+
+__global__ void __launch_bounds__(256) k_classify(Grid g, MC m, const double* __restrict__ phi,
+                                                  const double* __restrict__ gx, const double* __restrict__ gy,
+                                                  const double* __restrict__ gz, const double* __restrict__ u,
+                                                  const double* __restrict__ v, const double* __restrict__ w,
+                                                  double* __restrict__ fx, double* __restrict__ fy,
+                                                  double* __restrict__ fz, int* __restrict__ list,
+                                                  int* __restrict__ count) {
+  const int i = (int)(blockIdx.x * blockDim.x + threadIdx.x);
+  const int j = (int)(blockIdx.y * blockDim.y + threadIdx.y);
+  const int k = (int)blockIdx.z;
+  if (i > g.ni + 1 || j > g.nj + 1) return;
+  const long X = 1, Y = g.sy, Z = g.sz;
+  const long c = g.at(i, j, k);
+  const double rnx = avg8(gx, c, X, Y, Z), rny = avg8(gy, c, X, Y, Z), rnz = avg8(gz, c, X, Y, Z);
+  const double q00 = sqrt(rnx * rnx + rny * rny + rnz * rnz);
+  const double uw = __ldg(u + c - X), ue = __ldg(u + c), vs = __ldg(v + c - Y), vn = __ldg(v + c),
+               wb = __ldg(w + c - Z), wt = __ldg(w + c);
+  const bool band = !(q00 <= m.lim);
+  if (band) {
+    const int slot = atomicAdd(count, 1);
+    list[slot] = (int)c;
+  }
+  double phi00 = 0.0;
+  if (!band) {
+    phi00 = __ldg(phi + c);
+    if (phi00 <= m.eps_trunc) phi00 = 0.0;
+    if (1.0 - phi00 <= m.eps_trunc) phi00 = 1.0;
+  }
+  // owned faces: east/north/top when the velocity there is >= 0 (this cell donates or
+  // the flux is zero), west/south/bottom when < 0; band cells leave the donated
+  // faces to k_band but still zero the owned faces they do not donate through.
+  if (ue >= 0.0) fx[c] = band ? 0.0 : ue * phi00 * m.dt * m.dxi;
+  if (uw < 0.0) fx[c - X] = band ? 0.0 : uw * phi00 * m.dt * m.dxi;
+  if (vn >= 0.0) fy[c] = band ? 0.0 : vn * phi00 * m.dt * m.dyi;
+  if (vs < 0.0) fy[c - Y] = band ? 0.0 : vs * phi00 * m.dt * m.dyi;
+  if (wt >= 0.0) fz[c] = band ? 0.0 : wt * phi00 * m.dt * m.dzi;
+  if (wb < 0.0) fz[c - Z] = band ? 0.0 : wb * phi00 * m.dt * m.dzi;
+  // west/south/bottom faces of the first cells with no in-range donor stay zero
+  if (i == 0 && uw >= 0.0) fx[c - X] = 0.0;
+  if (j == 0 && vs >= 0.0) fy[c - Y] = 0.0;
+  if (k == 0 && wb >= 0.0) fz[c - Z] = 0.0;
+  if (i == g.ni + 1 && ue < 0.0) fx[c] = 0.0;
+  if (j == g.nj + 1 && vn < 0.0) fy[c] = 0.0;
+  if (k == g.nk + 1 && wt < 0.0) fz[c] = 0.0;
+}
+
+__global__ void __launch_bounds__(128) k_band(Grid g, MC m, const double* __restrict__ phi,
+                                              const double* __restrict__ gx, const double* __restrict__ gy,
+                                              const double* __restrict__ gz, const double* __restrict__ u,
+                                              const double* __restrict__ v, const double* __restrict__ w,
+                                              double* __restrict__ fx, double* __restrict__ fy,
+                                              double* __restrict__ fz, const int* __restrict__ list,
+                                              const int* __restrict__ count) {
+  const int n = *count;
+  const long X = 1, Y = g.sy, Z = g.sz;
+  const double m2b = -2.0 * m.bet, gp1 = m.gp1, gp2 = m.gp2;
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
+    const long c = list[e];
+    double rnx = avg8(gx, c, X, Y, Z), rny = avg8(gy, c, X, Y, Z), rnz = avg8(gz, c, X, Y, Z);
+    const double q00 = sqrt(rnx * rnx + rny * rny + rnz * rnz);
+    const double coef = 1.0 / q00;
+    rnx *= coef;
+    rny *= coef;
+    rnz *= coef;
+    double a[8];
+    gauss8(a, rnx, rny, rnz, gp1, gp2, gp1, gp2, gp1, gp2);
+    const double ph = __ldg(phi + c);
+    double ddd = 0.0;
+#pragma unroll 1
+    for (int it = 0; it < 10; ++it) {
+      double sd;
+      const double f = sig8(a, 0.125, m2b, ddd, &sd) - ph;
+      // df = 0.5 bet sum 0.125/cosh^2 = 0.5 bet * 0.125 * 4 * sum s(1-s)
+      const double df = 0.25 * m.bet * sd;
+      ddd = ddd - f * df / (df * df + 1.0e-99);
+    }
+    const double uw = __ldg(u + c - X), ue = __ldg(u + c), vs = __ldg(v + c - Y), vn = __ldg(v + c),
+                 wb = __ldg(w + c - Z), wt = __ldg(w + c);
+    auto side = [&](double vel, double dinv, int axis, bool minus, double* out) {
+      const double vd = vel * m.dt * dinv;
+      const double st = minus ? -0.5 : 0.5 - vd, en = minus ? -0.5 - vd : 0.5;
+      const double g1 = (st + en) * 0.5 + (-st + en) * gp1, g2 = (st + en) * 0.5 + (-st + en) * gp2;
+      double b[8];
+      if (axis == 0) gauss8(b, rnx, rny, rnz, g1, g2, gp1, gp2, gp1, gp2);
+      else if (axis == 1) gauss8(b, rnx, rny, rnz, gp1, gp2, g1, g2, gp1, gp2);
+      else gauss8(b, rnx, rny, rnz, gp1, gp2, gp1, gp2, g1, g2);
+      *out = sig8(b, 0.125 * vd, m2b, ddd, nullptr);
+    };
+    if (uw < 0.0) side(uw, m.dxi, 0, true, fx + c - X);
+    if (ue > 0.0) side(ue, m.dxi, 0, false, fx + c);
+    if (vs < 0.0) side(vs, m.dyi, 1, true, fy + c - Y);
+    if (vn > 0.0) side(vn, m.dyi, 1, false, fy + c);
+    if (wb < 0.0) side(wb, m.dzi, 2, true, fz + c - Z);
+    if (wt > 0.0) side(wt, m.dzi, 2, false, fz + c);
+  }
+}
+}  // namespace
+
+void mthinc_fluxes(cudaStream_t s, const Grid& g, double dxinv, double dyinv, double dzinv, double dt, double bet,
+                   const double* phi, const double* gx, const double* gy, const double* gz, const double* u,
+                   const double* v, const double* w, double* fx, double* fy, double* fz, int* list, int* count) {
+  MC m;
+  const double dx = 1.0 / dxinv, dy = 1.0 / dyinv, dz = 1.0 / dzinv;
+  m.gp1 = -0.5 / std::sqrt(3.0);
+  m.gp2 = 0.5 / std::sqrt(3.0);
+  const double dcellinv = 1.0 / std::sqrt((dx * dx + dy * dy + dz * dz) / 3.0);
+  const double ch = std::cosh(-bet * 1.5);
+  m.lim = bet / (2.0 * (ch * ch)) * dcellinv;
+  m.eps_trunc = 0.5 * (std::tanh(-bet * 2.5) + 1.0);
+  m.bet = bet;
+  m.dt = dt;
+  m.dxi = dxinv;
+  m.dyi = dyinv;
+  m.dzi = dzinv;
+  FMF_CUDA(cudaMemsetAsync(count, 0, sizeof(int), s));
+  dim3 b(32, 8, 1);
+  dim3 gr((unsigned)((g.ni + 2 + 31) / 32), (unsigned)((g.nj + 2 + 7) / 8), (unsigned)(g.nk + 2));
+  k_classify<<<gr, b, 0, s>>>(g, m, phi, gx, gy, gz, u, v, w, fx, fy, fz, list, count);
+  k_band<<<152 * 8, 128, 0, s>>>(g, m, phi, gx, gy, gz, u, v, w, fx, fy, fz, list, count);
+  count_launch(2);
+}
+
+}  // namespace fused
+}  // namespace fmf

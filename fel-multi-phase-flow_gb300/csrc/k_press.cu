@@ -5,6 +5,9 @@
 // forward, /(ni*nk); sign +1 inverse, unnormalised) is computed by radix-2
 // decimation-in-time FFTs in shared memory: one block per x-line, then one block
 // per tile of 16 x-wavenumbers for the z-lines.
+#include <map>
+#include <vector>
+
 #include "ops.cuh"
 
 namespace fmf {
@@ -30,44 +33,45 @@ void caldiv(cudaStream_t s, const Grid& g, double dxinv, double dyinv, double dz
 }
 
 namespace {
-// In-place radix-2 DIT FFT of L complex values in shared memory (re, im), executed
-// cooperatively by nthr threads starting at thread index t0 of the group.
-__device__ void smem_fft(double* re, double* im, int L, int sign, int t, int nthr) {
-  // bit reversal
+// In-place radix-2 decimation-in-time FFT of L complex values in shared memory
+// (re, im), run by the nthr threads t = 0..nthr-1 of a group; every thread of the
+// block reaches the same __syncthreads.  tw[m] = (cos, sin)(2 pi m / L), m < L/2,
+// computed on the host; stage len uses tw[m * L/len] (the same angle as
+// 2 pi m / len), sign -1 forward, +1 inverse.
+__device__ void group_fft(double* re, double* im, int L, double sgn, int t, int nthr, const double2* __restrict__ tw) {
   int lg = 0;
   while ((1 << lg) < L) ++lg;
   for (int a = t; a < L; a += nthr) {
     const int b = (int)(__brev((unsigned)a) >> (32 - lg));
     if (a < b) {
-      const double tr = re[a], ti = im[a];
+      const double t0 = re[a], t1 = im[a];
       re[a] = re[b];
       im[a] = im[b];
-      re[b] = tr;
-      im[b] = ti;
+      re[b] = t0;
+      im[b] = t1;
     }
   }
   __syncthreads();
-  for (int len = 2; len <= L; len <<= 1) {
+  for (int len = 2, step = L / 2; len <= L; len <<= 1, step >>= 1) {
     const int h = len >> 1;
     for (int q = t; q < L / 2; q += nthr) {
-      const int m = q % h, sblk = (q / h) * len;
-      const int a = sblk + m, b = a + h;
-      double sn, cs;
-      sincospi((double)(2 * m) / (double)len, &sn, &cs);
-      const double wr = cs, wi = sign * sn;
-      const double tr = wr * re[b] - wi * im[b];
-      const double ti = wr * im[b] + wi * re[b];
-      re[b] = re[a] - tr;
-      im[b] = im[a] - ti;
-      re[a] = re[a] + tr;
-      im[a] = im[a] + ti;
+      const int m = q & (h - 1), a = (q - m) * 2 + m, b = a + h;
+      const double2 w = __ldg(tw + m * step);
+      const double wr = w.x, wi = sgn * w.y;
+      const double xr = wr * re[b] - wi * im[b];
+      const double xi = wr * im[b] + wi * re[b];
+      re[b] = re[a] - xr;
+      im[b] = im[a] - xi;
+      re[a] = re[a] + xr;
+      im[a] = im[a] + xi;
     }
     __syncthreads();
   }
 }
 
 // x-lines: one block per (j,k) row.  Forward: real div -> complex T(kx, j, k).
-__global__ void __launch_bounds__(256) k_fft_x_fwd(Grid g, const double* div, double* tr, double* ti) {
+__global__ void __launch_bounds__(256) k_fft_x_fwd(Grid g, const double* div, double* tr, double* ti,
+                                                   const double2* tw) {
   extern __shared__ double sm[];
   const int L = g.ni;
   double* re = sm;
@@ -79,7 +83,7 @@ __global__ void __launch_bounds__(256) k_fft_x_fwd(Grid g, const double* div, do
     im[a] = 0.0;
   }
   __syncthreads();
-  smem_fft(re, im, L, -1, threadIdx.x, blockDim.x);
+  group_fft(re, im, L, -1.0, threadIdx.x, blockDim.x, tw);
   const long o = ((long)(k - 1) * g.nj + (j - 1)) * L;
   for (int a = threadIdx.x; a < L; a += blockDim.x) {
     tr[o + a] = re[a];
@@ -87,7 +91,8 @@ __global__ void __launch_bounds__(256) k_fft_x_fwd(Grid g, const double* div, do
   }
 }
 // Inverse x: complex T(kx, j, k) -> real part into dp(1..ni, j, k).
-__global__ void __launch_bounds__(256) k_fft_x_inv(Grid g, const double* tr, const double* ti, double* dp) {
+__global__ void __launch_bounds__(256) k_fft_x_inv(Grid g, const double* tr, const double* ti, double* dp,
+                                                   const double2* tw) {
   extern __shared__ double sm[];
   const int L = g.ni;
   double* re = sm;
@@ -99,16 +104,16 @@ __global__ void __launch_bounds__(256) k_fft_x_inv(Grid g, const double* tr, con
     im[a] = ti[o + a];
   }
   __syncthreads();
-  smem_fft(re, im, L, +1, threadIdx.x, blockDim.x);
+  group_fft(re, im, L, +1.0, threadIdx.x, blockDim.x, tw);
   const long c0 = g.at(1, j, k);
   for (int a = threadIdx.x; a < L; a += blockDim.x) dp[c0 + a] = re[a];
 }
 
-constexpr int kTile = 16;  // x-wavenumbers per z-line block
+constexpr int kTile = 16;  // x-wavenumbers per z-line block (16 threads per column)
 
 // z-lines forward: T(kx, j, k) for kx in a tile -> phir(ix, j, iz) / (ni*nk), centred.
 __global__ void __launch_bounds__(256) k_fft_z_fwd(Grid g, const double* tr, const double* ti, double* pr,
-                                                   double* pi) {
+                                                   double* pi, const double2* tw) {
   extern __shared__ double sm[];
   const int L = g.nk, NI = g.ni, NJ = g.nj;
   const int j = 1 + blockIdx.y;
@@ -120,43 +125,8 @@ __global__ void __launch_bounds__(256) k_fft_z_fwd(Grid g, const double* tr, con
     sm[col * 2 * L + L + kz] = ti[o];
   }
   __syncthreads();
-  // 16 columns, 16 threads each (blockDim 256)
-  const int col = threadIdx.x / 16, tcol = threadIdx.x % 16;
-  {
-    double* re = sm + col * 2 * L;
-    double* im = re + L;
-    // bit reversal + butterflies, group-local synchronisation through __syncthreads
-    int lg = 0;
-    while ((1 << lg) < L) ++lg;
-    for (int a = tcol; a < L; a += 16) {
-      const int b = (int)(__brev((unsigned)a) >> (32 - lg));
-      if (a < b) {
-        const double t0 = re[a], t1 = im[a];
-        re[a] = re[b];
-        im[a] = im[b];
-        re[b] = t0;
-        im[b] = t1;
-      }
-    }
-    __syncthreads();
-    for (int len = 2; len <= L; len <<= 1) {
-      const int h = len >> 1;
-      for (int q = tcol; q < L / 2; q += 16) {
-        const int m = q % h, sblk = (q / h) * len;
-        const int a = sblk + m, b = a + h;
-        double sn, cs;
-        sincospi((double)(2 * m) / (double)len, &sn, &cs);
-        const double wr = cs, wi = -sn;
-        const double xr = wr * re[b] - wi * im[b];
-        const double xi = wr * im[b] + wi * re[b];
-        re[b] = re[a] - xr;
-        im[b] = im[a] - xi;
-        re[a] = re[a] + xr;
-        im[a] = im[a] + xi;
-      }
-      __syncthreads();
-    }
-  }
+  const int col = threadIdx.x / 16;
+  group_fft(sm + col * 2 * L, sm + col * 2 * L + L, L, -1.0, threadIdx.x % 16, 16, tw);
   const double scale = (double)((long)NI * g.nk);
   for (int e = threadIdx.x; e < L * kTile; e += blockDim.x) {
     const int cl = e % kTile, kz = e / kTile;
@@ -169,7 +139,7 @@ __global__ void __launch_bounds__(256) k_fft_z_fwd(Grid g, const double* tr, con
 }
 // z-lines inverse: phir(ix, j, iz) -> T(kx, j, k)
 __global__ void __launch_bounds__(256) k_fft_z_inv(Grid g, const double* pr, const double* pi, double* tr,
-                                                   double* ti) {
+                                                   double* ti, const double2* tw) {
   extern __shared__ double sm[];
   const int L = g.nk, NI = g.ni, NJ = g.nj;
   const int j = 1 + blockIdx.y;
@@ -183,41 +153,8 @@ __global__ void __launch_bounds__(256) k_fft_z_inv(Grid g, const double* pr, con
     sm[cl * 2 * L + L + kz] = pi[o];
   }
   __syncthreads();
-  const int col = threadIdx.x / 16, tcol = threadIdx.x % 16;
-  {
-    double* re = sm + col * 2 * L;
-    double* im = re + L;
-    int lg = 0;
-    while ((1 << lg) < L) ++lg;
-    for (int a = tcol; a < L; a += 16) {
-      const int b = (int)(__brev((unsigned)a) >> (32 - lg));
-      if (a < b) {
-        const double t0 = re[a], t1 = im[a];
-        re[a] = re[b];
-        im[a] = im[b];
-        re[b] = t0;
-        im[b] = t1;
-      }
-    }
-    __syncthreads();
-    for (int len = 2; len <= L; len <<= 1) {
-      const int h = len >> 1;
-      for (int q = tcol; q < L / 2; q += 16) {
-        const int m = q % h, sblk = (q / h) * len;
-        const int a = sblk + m, b = a + h;
-        double sn, cs;
-        sincospi((double)(2 * m) / (double)len, &sn, &cs);
-        const double wr = cs, wi = sn;
-        const double xr = wr * re[b] - wi * im[b];
-        const double xi = wr * im[b] + wi * re[b];
-        re[b] = re[a] - xr;
-        im[b] = im[a] - xi;
-        re[a] = re[a] + xr;
-        im[a] = im[a] + xi;
-      }
-      __syncthreads();
-    }
-  }
+  const int col = threadIdx.x / 16;
+  group_fft(sm + col * 2 * L, sm + col * 2 * L + L, L, +1.0, threadIdx.x % 16, 16, tw);
   for (int e = threadIdx.x; e < L * kTile; e += blockDim.x) {
     const int cl = e % kTile, kz = e / kTile;
     const long o = ((long)kz * NJ + (j - 1)) * NI + kx0 + cl;
@@ -227,24 +164,45 @@ __global__ void __launch_bounds__(256) k_fft_z_inv(Grid g, const double* pr, con
 }
 }  // namespace
 
+// (cos, sin)(2 pi m / L) for m < L/2 in device memory, one table per length,
+// kept for the life of the library.
+const double2* fft_twiddles(int L) {
+  static std::map<int, double2*> cache;
+  auto it = cache.find(L);
+  if (it != cache.end()) return it->second;
+  std::vector<double2> h(L / 2 > 0 ? L / 2 : 1);
+  const double two_pi = 6.283185307179586476925286766559;
+  for (int m = 0; m < L / 2; ++m) {
+    const double ang = two_pi * (double)m / (double)L;
+    h[m] = make_double2(std::cos(ang), std::sin(ang));
+  }
+  double2* d = nullptr;
+  if (!FMF_CUDA(cudaMalloc(&d, sizeof(double2) * h.size()))) return nullptr;
+  FMF_CUDA(cudaMemcpy(d, h.data(), sizeof(double2) * h.size(), cudaMemcpyHostToDevice));
+  cache[L] = d;
+  return d;
+}
+
 // solp_fft_tdma1.f:20-48 (with trans_r2w's serial relabelling folded into the layout)
 void fft_forward_planes(cudaStream_t s, const Grid& g, const double* div, double* pr, double* pi) {
   const long nm = g.cells();
   double* t = (double*)scratch(sizeof(double) * 2 * nm, 5);
-  k_fft_x_fwd<<<dim3(g.nj, g.nk), 256, sizeof(double) * 2 * g.ni, s>>>(g, div, t, t + nm);
+  const double2 *twx = fft_twiddles(g.ni), *twz = fft_twiddles(g.nk);
+  k_fft_x_fwd<<<dim3(g.nj, g.nk), 256, sizeof(double) * 2 * g.ni, s>>>(g, div, t, t + nm, twx);
   const size_t smz = sizeof(double) * 2 * g.nk * kTile;
   cudaFuncSetAttribute(k_fft_z_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smz);
-  k_fft_z_fwd<<<dim3(g.ni / kTile, g.nj), 256, smz, s>>>(g, t, t + nm, pr, pi);
+  k_fft_z_fwd<<<dim3(g.ni / kTile, g.nj), 256, smz, s>>>(g, t, t + nm, pr, pi, twz);
   count_launch(2);
 }
 // solp_fft_tdma3.f:20-45
 void fft_inverse_planes(cudaStream_t s, const Grid& g, const double* pr, const double* pi, double* dp) {
   const long nm = g.cells();
   double* t = (double*)scratch(sizeof(double) * 2 * nm, 5);
+  const double2 *twx = fft_twiddles(g.ni), *twz = fft_twiddles(g.nk);
   const size_t smz = sizeof(double) * 2 * g.nk * kTile;
   cudaFuncSetAttribute(k_fft_z_inv, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smz);
-  k_fft_z_inv<<<dim3(g.ni / kTile, g.nj), 256, smz, s>>>(g, pr, pi, t, t + nm);
-  k_fft_x_inv<<<dim3(g.nj, g.nk), 256, sizeof(double) * 2 * g.ni, s>>>(g, t, t + nm, dp);
+  k_fft_z_inv<<<dim3(g.ni / kTile, g.nj), 256, smz, s>>>(g, pr, pi, t, t + nm, twz);
+  k_fft_x_inv<<<dim3(g.nj, g.nk), 256, sizeof(double) * 2 * g.ni, s>>>(g, t, t + nm, dp, twx);
   count_launch(2);
 }
 

@@ -10,6 +10,7 @@
 #include <vector>
 
 #include "../../include/fmf_capi.h"
+#include "fused.cuh"
 #include "ops.cuh"
 #include "runtime.cuh"
 
@@ -36,6 +37,7 @@ struct fmf_ctx {
   double *dp, *div, *pr, *pi;
   double *as_f, *an_f, *ap_f;
   double* red;  // small reduction outputs
+  int* band;    // MTHINC band-cell list, then its length
   double* host_err = nullptr;  // pinned
   std::vector<int> sor_iters;
 };
@@ -102,6 +104,10 @@ int fmf_ctx_create(const fmf_params* prm, fmf_ctx** out) {
   c->an_f = alloc(c, prm->nj + 6);
   c->ap_f = alloc(c, prm->nj + 6);
   c->red = alloc(c, 64);
+  {
+    const long nb = (long)(prm->ni + 2) * (prm->nj + 2) * (prm->nk + 2) + 1;
+    c->band = (int*)alloc(c, (nb + 1) / 2);
+  }
   FMF_CUDA(cudaMallocHost(&c->host_err, sizeof(double) * 8));
   if (get_status()) {
     fmf_ctx_destroy(c);
@@ -250,8 +256,11 @@ static int step_once(fmf_ctx* c) {
   double* phin1 = c->phin + n;
   // :491-503 transport
   op::cal_grad_p2a(s, g, dxinv, dyinv, dzinv, phi1, c->phix, c->phiy, c->phiz);
-  op::solphi_mthinc1(s, g, dxinv, dyinv, dzinv, dt, P.bet_mthinc, phi1, c->phix, c->phiy, c->phiz, c->u, c->v,
-                     c->w, c->flx, c->fly, c->flz);
+  {
+    const long nb = (long)(g.ni + 2) * (g.nj + 2) * (g.nk + 2);
+    fused::mthinc_fluxes(s, g, dxinv, dyinv, dzinv, dt, P.bet_mthinc, phi1, c->phix, c->phiy, c->phiz, c->u, c->v,
+                         c->w, c->flx, c->fly, c->flz, c->band, c->band + nb);
+  }
   op::solphi_mthinc2(s, g, dxinv, dyinv, dzinv, dt, c->u, c->v, c->w, c->flx, c->fly, c->flz, phi1, phin1);
   op::cal_grad_p2a(s, g, dxinv, dyinv, dzinv, phin1, c->phix, c->phiy, c->phiz);
   op::solphi_mthinc3(s, g, dxinv, dyinv, dzinv, P.bet_mthinc, c->phix, c->phiy, c->phiz, phi1, phin1, c->red);
@@ -269,8 +278,7 @@ static int step_once(fmf_ctx* c) {
   op::cal_arith_mean(s, g, phi0, P.rmul, P.rmug, c->rmu);
   op::cal_arith_mean(s, g, phin0, P.rmul, P.rmug, c->rmun);
   // :532-541
-  op::cal_advu_weno5(s, g, dxinv, dyinv, dzinv, c->u, c->v, c->w, c->adv[0], c->adv[1], c->adv[2]);
-  op::cal_advu_weno5(s, g, dxinv, dyinv, dzinv, c->uo, c->vo, c->wo, c->advo[0], c->advo[1], c->advo[2]);
+  fused::weno5_both(s, g, dxinv, dyinv, dzinv, c->u, c->v, c->w, c->uo, c->vo, c->wo, c->adv, c->advo);
   op::calphat(s, g, c->p, c->po, c->phat);
   op::cal_grad_prs(s, g, dxinv, dyinv, dzinv, c->phat, c->prs[0], c->prs[1], c->prs[2]);
   op::calsij(s, g, dxinv, dyinv, dzinv, c->u, c->v, c->w, c->sk);
@@ -368,7 +376,8 @@ static int step_once(fmf_ctx* c) {
 // launches after one warm-up launch, on the current state (the state is not
 // advanced: stages write only work arrays).  Stage 0: WENO5 advection of (u,v,w);
 // 1: one outer SOR iteration on copies of the velocity; 2: pressure FFT+TDMA+inverse;
-// 3: MTHINC fluxes.  *ms = mean milliseconds per launch of the stage.
+// 3: MTHINC fluxes.  *ms = mean milliseconds per launch of the stage (stage 0 covers
+// both advection levels, u and uo).
 int fmf_ctx_time_stage(fmf_ctx* c, int stage, int reps, float* ms) {
   if (!c || !ms || reps <= 0 || stage < 0 || stage > 3) return FMF_ERR_ARG;
   const fmf_params& P = c->prm;
@@ -382,7 +391,7 @@ int fmf_ctx_time_stage(fmf_ctx* c, int stage, int reps, float* ms) {
   auto run = [&]() {
     switch (stage) {
       case 0:
-        op::cal_advu_weno5(s, g, dxinv, dyinv, dzinv, c->u, c->v, c->w, c->adv[0], c->adv[1], c->adv[2]);
+        fused::weno5_both(s, g, dxinv, dyinv, dzinv, c->u, c->v, c->w, c->uo, c->vo, c->wo, c->adv, c->advo);
         break;
       case 1:
         op::sor_iteration(s, g, P.dt, c->rho, c->rhon, cf, srcp, c->un, c->vn, c->wn, P.uwall, P.dy, c->l1, c->l2,
@@ -394,8 +403,9 @@ int fmf_ctx_time_stage(fmf_ctx* c, int stage, int reps, float* ms) {
         op::fft_inverse_planes(s, g, c->pr, c->pi, c->dp);
         break;
       case 3:
-        op::solphi_mthinc1(s, g, dxinv, dyinv, dzinv, P.dt, P.bet_mthinc, c->phi + n, c->phix, c->phiy, c->phiz,
-                           c->u, c->v, c->w, c->flx, c->fly, c->flz);
+        fused::mthinc_fluxes(s, g, dxinv, dyinv, dzinv, P.dt, P.bet_mthinc, c->phi + n, c->phix, c->phiy,
+                             c->phiz, c->u, c->v, c->w, c->flx, c->fly, c->flz, c->band,
+                             c->band + (long)(g.ni + 2) * (g.nj + 2) * (g.nk + 2));
         break;
     }
   };
