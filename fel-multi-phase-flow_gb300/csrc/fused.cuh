@@ -19,5 +19,21 @@ void mthinc_fluxes(cudaStream_t s, const Grid& g, double dxinv, double dyinv, do
                    const double* phi, const double* gx, const double* gy, const double* gz, const double* u,
                    const double* v, const double* w, double* fx, double* fy, double* fz, int* list, int* count);
 
+// Viscous solve.  visc_prep: edge viscosities E[0..2] (xy, xz, yz edges, i,j,k in 0..n),
+// per-component A/B (AB[0..5] = Au Bu Av Bv Aw Bw) from mu, rho, rhon, src, and the
+// Navier-slip wall coefficients wallc (2*(nk+6)*(ni+6)*2 doubles) from phi, l1, l2.
+void visc_prep(cudaStream_t s, const Grid& g, double dxinv, double dyinv, double dzinv, double dt, int harmonic,
+               const double* mu, const double* rho, const double* rhon, const double* const* src, double* const* E,
+               double* const* AB, const double* l1, const double* l2, const double* phi, double dy, double* wallc);
+// bndu followed by bnd_periodic of the components whose bit is set in `normal`.
+void wall_halo(cudaStream_t s, const Grid& g, int normal, double uwall, const double* wallc, double* un, double* vn,
+               double* wn);
+// one outer iteration (u, v, w sweeps of 4 colour pairs each); errsum[0] = sum du^2;
+// part: sor_parts(g) doubles of scratch
+void sor_iteration(cudaStream_t s, const Grid& g, double dxinv, double dyinv, double dzinv, int harmonic,
+                   const double* mu, double* const* E, double* const* AB, double uwall, const double* wallc,
+                   double* un, double* vn, double* wn, double* part, double* errsum);
+long sor_parts(const Grid& g);
+
 }  // namespace fused
 }  // namespace fmf

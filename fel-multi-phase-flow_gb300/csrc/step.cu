@@ -33,7 +33,7 @@ struct fmf_ctx {
   double *phix, *phiy, *phiz, *flx, *fly, *flz, *rho, *rhon, *rmu, *rmun;
   double *adv[3], *advo[3], *phat, *prs[3], *sk, *tau, *vis[3];
   double *rn[4], *rnn[4], *rkap, *rkapn, *fst[3], *fstn[3], *sfst[3], *sfstn[3], *src[3];
-  double* coef[45];
+  double *edge[3], *ab[6], *wallc, *sorpart;  // fused viscous solve (fused_visc.cu)
   double *dp, *div, *pr, *pi;
   double *as_f, *an_f, *ap_f;
   double* red;  // small reduction outputs
@@ -97,7 +97,10 @@ int fmf_ctx_create(const fmf_params* prm, fmf_ctx** out) {
   }
   c->rkap = alloc(c, 3 * n);
   c->rkapn = alloc(c, 3 * n);
-  for (int q = 0; q < 45; ++q) c->coef[q] = alloc(c, n);
+  for (int q = 0; q < 3; ++q) c->edge[q] = alloc(c, n);
+  for (int q = 0; q < 6; ++q) c->ab[q] = alloc(c, n);
+  c->wallc = alloc(c, 4L * (prm->nk + 6) * (prm->ni + 6));
+  c->sorpart = alloc(c, fused::sor_parts(c->g));
   c->pr = alloc(c, nm);
   c->pi = alloc(c, nm);
   c->as_f = alloc(c, prm->nj + 6);
@@ -314,19 +317,19 @@ static int step_once(fmf_ctx* c) {
   const double* fstnp[3] = {c->sfstn[0], c->sfstn[1], c->sfstn[2]};
   op::cal_srcu(s, g, dt, P.grvb, P.grvp, c->u, c->v, c->w, c->rho, c->rhon, advp, advop, prsp, visp, fstp, fstnp,
                c->src);
-  op::cal_coef_vis(s, g, dxinv, dyinv, dzinv, c->rmun, c->coef, P.harmonic != 0);
+  // :590-603 coefficients (as edge viscosities) and the per-point update factors
+  const double* srcp[3] = {c->src[0], c->src[1], c->src[2]};
+  fused::visc_prep(s, g, dxinv, dyinv, dzinv, dt, P.harmonic, c->rmun, c->rho, c->rhon, srcp, c->edge, c->ab, c->l1,
+                   c->l2, phi1, P.dy, c->wallc);
   // :605-623
   op::copy(s, n, c->u, c->un);
   op::copy(s, n, c->v, c->vn);
   op::copy(s, n, c->w, c->wn);
-  const double* cf[45];
-  for (int q = 0; q < 45; ++q) cf[q] = c->coef[q];
-  const double* srcp[3] = {c->src[0], c->src[1], c->src[2]};
   double err = 0.0, err0 = 0.0;
   int lp;
   for (lp = 0; lp <= 20; ++lp) {
-    op::sor_iteration(s, g, dt, c->rho, c->rhon, cf, srcp, c->un, c->vn, c->wn, P.uwall, P.dy, c->l1, c->l2, phi1,
-                      c->red + 8);
+    fused::sor_iteration(s, g, dxinv, dyinv, dzinv, P.harmonic, c->rmun, c->edge, c->ab, P.uwall, c->wallc, c->un,
+                         c->vn, c->wn, c->sorpart, c->red + 8);
     FMF_CUDA(cudaMemcpyAsync(c->host_err, c->red + 8, sizeof(double), cudaMemcpyDeviceToHost, s));
     FMF_CUDA(cudaStreamSynchronize(s));
     const double e = c->host_err[0];
@@ -340,10 +343,7 @@ static int step_once(fmf_ctx* c) {
   }
   c->sor_iters.push_back((lp <= 20 ? lp : 20) + 1);
   // :625-646
-  op::bndu(s, g, c->un, c->vn, c->wn, P.uwall, P.dy, c->l1, c->l2, phi1);
-  op::bnd_periodic(s, g, c->un);
-  op::bnd_periodic(s, g, c->vn);
-  op::bnd_periodic(s, g, c->wn);
+  fused::wall_halo(s, g, 7, P.uwall, c->wallc, c->un, c->vn, c->wn);
   op::caldiv(s, g, dxinv, dyinv, dzinv, dt, c->un, c->vn, c->wn, c->div, nullptr);
   op::fft_forward_planes(s, g, c->div, c->pr, c->pi);
   op::tdma_modes(s, g, P.rhog, dxinv, dzinv, c->as_f, c->an_f, c->ap_f, c->pr, c->pi);
@@ -353,10 +353,7 @@ static int step_once(fmf_ctx* c) {
   op::bnd_periodic(s, g, c->dp);
   // :648-661
   op::corunp_explicit(s, g, P.rhog, dxinv, dyinv, dzinv, dt, c->dp, c->phat, c->un, c->vn, c->wn, c->pn);
-  op::bndu(s, g, c->un, c->vn, c->wn, P.uwall, P.dy, c->l1, c->l2, phi1);
-  op::bnd_periodic(s, g, c->un);
-  op::bnd_periodic(s, g, c->vn);
-  op::bnd_periodic(s, g, c->wn);
+  fused::wall_halo(s, g, 7, P.uwall, c->wallc, c->un, c->vn, c->wn);
   op::bnd_avzero(s, g, c->pn);
   op::bnd_neumann(s, g, c->pn);
   op::bnd_periodic(s, g, c->pn);
@@ -385,17 +382,14 @@ int fmf_ctx_time_stage(fmf_ctx* c, int stage, int reps, float* ms) {
   cudaStream_t s = c->s;
   const double dxinv = 1.0 / P.dx, dyinv = 1.0 / P.dy, dzinv = 1.0 / P.dz;
   const long n = g.n;
-  const double* cf[45];
-  for (int q = 0; q < 45; ++q) cf[q] = c->coef[q];
-  const double* srcp[3] = {c->src[0], c->src[1], c->src[2]};
   auto run = [&]() {
     switch (stage) {
       case 0:
         fused::weno5_both(s, g, dxinv, dyinv, dzinv, c->u, c->v, c->w, c->uo, c->vo, c->wo, c->adv, c->advo);
         break;
       case 1:
-        op::sor_iteration(s, g, P.dt, c->rho, c->rhon, cf, srcp, c->un, c->vn, c->wn, P.uwall, P.dy, c->l1, c->l2,
-                          c->phi + n, c->red + 8);
+        fused::sor_iteration(s, g, dxinv, dyinv, dzinv, P.harmonic, c->rmun, c->edge, c->ab, P.uwall, c->wallc,
+                             c->un, c->vn, c->wn, c->sorpart, c->red + 8);
         break;
       case 2:
         op::fft_forward_planes(s, g, c->div, c->pr, c->pi);
