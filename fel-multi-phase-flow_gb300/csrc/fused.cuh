@@ -25,6 +25,13 @@ void mthinc_fluxes(cudaStream_t s, const Grid& g, double dxinv, double dyinv, do
 void visc_prep(cudaStream_t s, const Grid& g, double dxinv, double dyinv, double dzinv, double dt, int harmonic,
                const double* mu, const double* rho, const double* rhon, const double* const* src, double* const* E,
                double* const* AB, const double* l1, const double* l2, const double* phi, double dy, double* wallc);
+// visc_prep with the momentum right-hand side of cal_srcu formed in registers
+void src_visc_prep(cudaStream_t s, const Grid& g, double dxinv, double dyinv, double dzinv, double dt, int harmonic,
+                   double grvb, double grvp, const double* u, const double* v, const double* w,
+                   const double* const* adv, const double* const* advo, const double* const* prs,
+                   const double* const* vis, const double* const* fst, const double* const* fstn, const double* mu,
+                   const double* rho, const double* rhon, double* const* E, double* const* AB, const double* l1,
+                   const double* l2, const double* phi, double dy, double* wallc);
 // bndu followed by bnd_periodic of the components whose bit is set in `normal`.
 void wall_halo(cudaStream_t s, const Grid& g, int normal, double uwall, const double* wallc, double* un, double* vn,
                double* wn);

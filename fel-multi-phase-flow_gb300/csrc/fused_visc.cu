@@ -84,6 +84,55 @@ __global__ void __launch_bounds__(256) k_ab(Grid g, VP p, const double* __restri
   }
 }
 
+// cal_srcu.f:53-137 fused with the update factors: src is formed in registers
+// (1/rho00 taken once per face) and only A = 0.5/(rho00*D), B = src/D are stored.
+struct SrcIn {
+  const double *u, *v, *w, *rho, *rhon, *adv[3], *advo[3], *prs[3], *vis[3], *fst[3], *fstn[3];
+  double grvb, grvp;
+};
+__global__ void __launch_bounds__(256) k_src_ab(Grid g, VP p, SrcIn in, const double* __restrict__ mu,
+                                                const double* __restrict__ exy, const double* __restrict__ exz,
+                                                const double* __restrict__ eyz, double* __restrict__ au,
+                                                double* __restrict__ bu, double* __restrict__ av, double* __restrict__ bv,
+                                                double* __restrict__ aw, double* __restrict__ bw) {
+  const int i = 1 + (int)(blockIdx.x * blockDim.x + threadIdx.x);
+  const int j = 1 + (int)(blockIdx.y * blockDim.y + threadIdx.y);
+  const int k = 1 + (int)blockIdx.z;
+  if (i > g.ni || j > g.nj) return;
+  const long X = 1, Y = g.sy, Z = g.sz;
+  const long c = g.at(i, j, k);
+  const double r0 = __ldg(in.rho + c), n0 = __ldg(in.rhon + c);
+  auto src = [&](int q, const double* vel, double rinv, double grav) {
+    return __ldg(vel + c) * p.dtinv - __ldg(in.adv[q] + c) * 1.5 + __ldg(in.advo[q] + c) * 0.5 -
+           __ldg(in.prs[q] + c) * rinv + __ldg(in.vis[q] + c) * rinv * 0.5 + __ldg(in.fst[q] + c) * 0.5 +
+           __ldg(in.fstn[q] + c) * 0.5 + grav;
+  };
+  {
+    const double r = (r0 + __ldg(in.rho + c + X) + n0 + __ldg(in.rhon + c + X)) * 0.25, ri = 1.0 / r;
+    const double ap = p.dz2 * __ldg(exz + c - Z) + p.dy2 * __ldg(exy + c - Y) + p.dx2 * __ldg(mu + c) * 2.0 +
+                      p.dx2 * __ldg(mu + c + X) * 2.0 + p.dy2 * __ldg(exy + c) + p.dz2 * __ldg(exz + c);
+    const double Di = 1.0 / (p.dtinv + ap * ri * 0.5);
+    au[c] = 0.5 * ri * Di;
+    bu[c] = src(0, in.u, ri, in.grvb) * Di;
+  }
+  if (j <= g.nj - 1) {
+    const double r = (r0 + __ldg(in.rho + c + Y) + n0 + __ldg(in.rhon + c + Y)) * 0.25, ri = 1.0 / r;
+    const double ap = p.dz2 * __ldg(eyz + c - Z) + p.dy2 * __ldg(mu + c) * 2.0 + p.dx2 * __ldg(exy + c - X) +
+                      p.dx2 * __ldg(exy + c) + p.dy2 * __ldg(mu + c + Y) * 2.0 + p.dz2 * __ldg(eyz + c);
+    const double Di = 1.0 / (p.dtinv + ap * ri * 0.5);
+    av[c] = 0.5 * ri * Di;
+    bv[c] = src(1, in.v, ri, in.grvp) * Di;
+  }
+  {
+    const double r = (r0 + __ldg(in.rho + c + Z) + n0 + __ldg(in.rhon + c + Z)) * 0.25, ri = 1.0 / r;
+    const double ap = p.dz2 * __ldg(mu + c) * 2.0 + p.dy2 * __ldg(eyz + c - Y) + p.dx2 * __ldg(exz + c - X) +
+                      p.dx2 * __ldg(exz + c) + p.dy2 * __ldg(eyz + c) + p.dz2 * __ldg(mu + c + Z) * 2.0;
+    const double Di = 1.0 / (p.dtinv + ap * ri * 0.5);
+    aw[c] = 0.5 * ri * Di;
+    bw[c] = src(2, in.w, ri, 0.0) * Di;
+  }
+}
+
 // One colour pair of one component.  Thread (a, b, kk) covers, for the pair whose
 // first colour has parities (pi,pj,pk), the point (pi+2a, pj+2b, pk+2kk) and the
 // point of the second colour (all parities flipped) at (pi'+2a, pj'+2b, pk'+2kk).
@@ -299,6 +348,45 @@ void visc_prep(cudaStream_t s, const Grid& g, double dxinv, double dyinv, double
   k_edges<<<dim3((g.ni + 1 + 31) / 32, (g.nj + 1 + 7) / 8, g.nk + 1), b, 0, s>>>(g, p, mu, E[0], E[1], E[2]);
   k_ab<<<dim3((g.ni + 31) / 32, (g.nj + 7) / 8, g.nk), b, 0, s>>>(g, p, mu, E[0], E[1], E[2], rho, rhon, src[0], src[1],
                                                                  src[2], AB[0], AB[1], AB[2], AB[3], AB[4], AB[5]);
+  k_wall_coef<<<dim3((g.ni + 6 + 31) / 32, (2 * (g.nk + 6) + 7) / 8), b, 0, s>>>(g, dy, l1, l2, phi, wallc);
+  count_launch(3);
+}
+
+void src_visc_prep(cudaStream_t s, const Grid& g, double dxinv, double dyinv, double dzinv, double dt, int harmonic,
+                   double grvb, double grvp, const double* u, const double* v, const double* w,
+                   const double* const* adv, const double* const* advo, const double* const* prs,
+                   const double* const* vis, const double* const* fst, const double* const* fstn, const double* mu,
+                   const double* rho, const double* rhon, double* const* E, double* const* AB, const double* l1,
+                   const double* l2, const double* phi, double dy, double* wallc) {
+  VP p;
+  p.dtinv = 1.0 / dt;
+  p.dx2 = dxinv * dxinv;
+  p.dy2 = dyinv * dyinv;
+  p.dz2 = dzinv * dzinv;
+  p.dxy = dxinv * dyinv;
+  p.dxz = dxinv * dzinv;
+  p.dyz = dyinv * dzinv;
+  p.harmonic = harmonic;
+  SrcIn in;
+  in.u = u;
+  in.v = v;
+  in.w = w;
+  in.rho = rho;
+  in.rhon = rhon;
+  for (int q = 0; q < 3; ++q) {
+    in.adv[q] = adv[q];
+    in.advo[q] = advo[q];
+    in.prs[q] = prs[q];
+    in.vis[q] = vis[q];
+    in.fst[q] = fst[q];
+    in.fstn[q] = fstn[q];
+  }
+  in.grvb = grvb;
+  in.grvp = grvp;
+  dim3 b(32, 8, 1);
+  k_edges<<<dim3((g.ni + 1 + 31) / 32, (g.nj + 1 + 7) / 8, g.nk + 1), b, 0, s>>>(g, p, mu, E[0], E[1], E[2]);
+  k_src_ab<<<dim3((g.ni + 31) / 32, (g.nj + 7) / 8, g.nk), b, 0, s>>>(g, p, in, mu, E[0], E[1], E[2], AB[0], AB[1],
+                                                                     AB[2], AB[3], AB[4], AB[5]);
   k_wall_coef<<<dim3((g.ni + 6 + 31) / 32, (2 * (g.nk + 6) + 7) / 8), b, 0, s>>>(g, dy, l1, l2, phi, wallc);
   count_launch(3);
 }

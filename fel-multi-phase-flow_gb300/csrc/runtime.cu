@@ -55,9 +55,24 @@ struct Slot {
   void* p = nullptr;
   size_t bytes = 0;
 };
-static Slot g_slots[16];
+struct ScratchSet {
+  Slot slots[16];
+};
+static ScratchSet g_global_set;
+// A time-step context owns its scratch: graphs captured from it keep pointing at
+// buffers that no other caller can grow or free.
+static thread_local ScratchSet* g_set = nullptr;
+void* scratch_set_create() { return new ScratchSet(); }
+void scratch_set_destroy(void* p) {
+  ScratchSet* s = (ScratchSet*)p;
+  if (!s) return;
+  for (Slot& sl : s->slots)
+    if (sl.p) cudaFree(sl.p);
+  delete s;
+}
+void scratch_set_use(void* p) { g_set = (ScratchSet*)p; }
 void* scratch(size_t bytes, int slot) {
-  Slot& s = g_slots[slot];
+  Slot& s = (g_set ? g_set : &g_global_set)->slots[slot];
   if (s.bytes >= bytes) return s.p;
   if (s.p) {
     FMF_CUDA(cudaStreamSynchronize(stream()));

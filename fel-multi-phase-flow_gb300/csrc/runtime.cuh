@@ -18,6 +18,9 @@ int sync_to_device(const void* host, size_t bytes_or_0);
 int sync_all_to_host();
 int forget(const void* host);
 int reset_registry();
+void* scratch_set_create();
+void scratch_set_destroy(void* set);
+void scratch_set_use(void* set);  // nullptr: the library-wide set
 
 // The array arguments of one drop-in call.  arr() returns the device copy of a
 // host array: in resident mode the registry mirror (uploaded when first seen),

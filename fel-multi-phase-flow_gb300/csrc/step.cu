@@ -6,7 +6,9 @@
 // the 8-byte SOR residual read once per outer iteration (the stop test of
 // solu_sor4.f:291-293).
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
+#include <map>
 #include <vector>
 
 #include "../../include/fmf_capi.h"
@@ -16,7 +18,26 @@
 
 using namespace fmf;
 
+struct GraphKey {
+  int seg;
+  const double* p[14];
+  bool operator<(const GraphKey& o) const {
+    if (seg != o.seg) return seg < o.seg;
+    for (int t = 0; t < 14; ++t)
+      if (p[t] != o.p[t]) return p[t] < o.p[t];
+    return false;
+  }
+};
+struct GraphEntry {
+  cudaGraphExec_t exec;
+  long long launches;
+};
+
 struct fmf_ctx {
+  bool graphs = true;  // replay captured CUDA graphs (FMF_GRAPHS=0 disables)
+  bool warm = false;   // the first step runs eagerly (allocates scratch, twiddle tables)
+  void* scr = nullptr; // this context's scratch set
+  std::map<GraphKey, GraphEntry> cache;
   fmf_params prm;
   Grid g;
   cudaStream_t s = nullptr;
@@ -65,6 +86,8 @@ int fmf_ctx_create(const fmf_params* prm, fmf_ctx** out) {
   if (!p2(prm->ni) || !p2(prm->nj) || !p2(prm->nk) || prm->ni < 16) return FMF_ERR_ARG;
   fmf_ctx* c = new fmf_ctx();
   c->prm = *prm;
+  if (const char* e = std::getenv("FMF_GRAPHS")) c->graphs = std::atoi(e) != 0;
+  c->scr = scratch_set_create();
   c->g = Grid(prm->ni, prm->nj, prm->nk);
   if (!FMF_CUDA(cudaStreamCreateWithFlags(&c->s, cudaStreamNonBlocking))) {
     delete c;
@@ -140,6 +163,8 @@ int fmf_ctx_create(const fmf_params* prm, fmf_ctx** out) {
 int fmf_ctx_destroy(fmf_ctx* c) {
   if (!c) return 0;
   if (c->s) cudaStreamSynchronize(c->s);
+  for (auto& e : c->cache) cudaGraphExecDestroy(e.second.exec);
+  scratch_set_destroy(c->scr);
   for (void* p : c->allocs) cudaFree(p);
   if (c->host_err) cudaFreeHost(c->host_err);
   if (c->own_stream && c->s) cudaStreamDestroy(c->s);
@@ -170,6 +195,12 @@ int fmf_ctx_set_walls(fmf_ctx* c, const double* th, const double* ze, const doub
   FMF_CUDA(cudaMemcpyAsync(c->l2, l2, b, cudaMemcpyHostToDevice, c->s));
   return take_status();
 }
+
+// Routes fmf::scratch to the context's own scratch set while the context works.
+struct ScratchScope {
+  explicit ScratchScope(void* set) { scratch_set_use(set); }
+  ~ScratchScope() { scratch_set_use(nullptr); }
+};
 
 static double* field_ptr(fmf_ctx* c, int f) {
   const long n = c->g.n;
@@ -223,6 +254,7 @@ int fmf_ctx_sor_iterations(fmf_ctx* c, int* out, int cap) {
 // main.f90:322-366 (start-up boundary pass) on the uploaded state
 int fmf_ctx_init_bc(fmf_ctx* c) {
   if (!c) return FMF_ERR_ARG;
+  ScratchScope scope(c->scr);
   const fmf_params& P = c->prm;
   const Grid& g = c->g;
   cudaStream_t s = c->s;
@@ -247,7 +279,13 @@ int fmf_ctx_init_bc(fmf_ctx* c) {
   return take_status();
 }
 
-static int step_once(fmf_ctx* c) {
+// ---- the step in three segments ---------------------------------------------
+// seg_pre: main.f90:489-607 (transport, properties, right-hand side, solver set-up)
+// seg_iter: one outer iteration of solu_sor4 (its residual lands in red[8])
+// seg_post: main.f90:625-697 (pressure solve, projection, boundary conditions, rotation
+// of phin into phi).  The pointer rotation of u/uo/un, p/po/pn and phi/phin is done
+// on the host between steps.
+static void seg_pre(fmf_ctx* c) {
   const fmf_params& P = c->prm;
   const Grid& g = c->g;
   cudaStream_t s = c->s;
@@ -315,33 +353,31 @@ static int step_once(fmf_ctx* c) {
   const double* visp[3] = {c->vis[0], c->vis[1], c->vis[2]};
   const double* fstp[3] = {c->sfst[0], c->sfst[1], c->sfst[2]};
   const double* fstnp[3] = {c->sfstn[0], c->sfstn[1], c->sfstn[2]};
-  op::cal_srcu(s, g, dt, P.grvb, P.grvp, c->u, c->v, c->w, c->rho, c->rhon, advp, advop, prsp, visp, fstp, fstnp,
-               c->src);
-  // :590-603 coefficients (as edge viscosities) and the per-point update factors
-  const double* srcp[3] = {c->src[0], c->src[1], c->src[2]};
-  fused::visc_prep(s, g, dxinv, dyinv, dzinv, dt, P.harmonic, c->rmun, c->rho, c->rhon, srcp, c->edge, c->ab, c->l1,
-                   c->l2, phi1, P.dy, c->wallc);
-  // :605-623
+  // :579-603: cal_srcu and the coefficients (as edge viscosities) folded into the
+  // per-point update factors of the viscous solve
+  fused::src_visc_prep(s, g, dxinv, dyinv, dzinv, dt, P.harmonic, P.grvb, P.grvp, c->u, c->v, c->w, advp, advop,
+                       prsp, visp, fstp, fstnp, c->rmun, c->rho, c->rhon, c->edge, c->ab, c->l1, c->l2, phi1, P.dy,
+                       c->wallc);
+  // :605-607
   op::copy(s, n, c->u, c->un);
   op::copy(s, n, c->v, c->vn);
   op::copy(s, n, c->w, c->wn);
-  double err = 0.0, err0 = 0.0;
-  int lp;
-  for (lp = 0; lp <= 20; ++lp) {
-    fused::sor_iteration(s, g, dxinv, dyinv, dzinv, P.harmonic, c->rmun, c->edge, c->ab, P.uwall, c->wallc, c->un,
-                         c->vn, c->wn, c->sorpart, c->red + 8);
-    FMF_CUDA(cudaMemcpyAsync(c->host_err, c->red + 8, sizeof(double), cudaMemcpyDeviceToHost, s));
-    FMF_CUDA(cudaStreamSynchronize(s));
-    const double e = c->host_err[0];
-    if (!std::isfinite(e)) {
-      set_status(FMF_ERR_NONFINITE);
-      break;
-    }
-    err = std::sqrt(e / (double)g.cells()) + 1.0e-99;
-    if (lp == 0) err0 = err;
-    if (err / err0 <= 1.0e-3) break;
-  }
-  c->sor_iters.push_back((lp <= 20 ? lp : 20) + 1);
+}
+
+static void seg_iter(fmf_ctx* c) {
+  const fmf_params& P = c->prm;
+  const double dxinv = 1.0 / P.dx, dyinv = 1.0 / P.dy, dzinv = 1.0 / P.dz;
+  fused::sor_iteration(c->s, c->g, dxinv, dyinv, dzinv, P.harmonic, c->rmun, c->edge, c->ab, P.uwall, c->wallc, c->un,
+                       c->vn, c->wn, c->sorpart, c->red + 8);
+  FMF_CUDA(cudaMemcpyAsync(c->host_err, c->red + 8, sizeof(double), cudaMemcpyDeviceToHost, c->s));
+}
+
+static void seg_post(fmf_ctx* c) {
+  const fmf_params& P = c->prm;
+  const Grid& g = c->g;
+  cudaStream_t s = c->s;
+  const long n = g.n;
+  const double dxinv = 1.0 / P.dx, dyinv = 1.0 / P.dy, dzinv = 1.0 / P.dz, dt = P.dt;
   // :625-646
   fused::wall_halo(s, g, 7, P.uwall, c->wallc, c->un, c->vn, c->wn);
   op::caldiv(s, g, dxinv, dyinv, dzinv, dt, c->un, c->vn, c->wn, c->div, nullptr);
@@ -357,14 +393,67 @@ static int step_once(fmf_ctx* c) {
   op::bnd_avzero(s, g, c->pn);
   op::bnd_neumann(s, g, c->pn);
   op::bnd_periodic(s, g, c->pn);
-  // :686-697 rotation by pointer; phin keeps phi's values (cpy leaves its source intact)
+  // :695-697 phi(l) = phin(l); phin keeps its values (cpy leaves the source intact),
+  // so after the pointer swap below the new phin must equal the new phi
+  op::copy(s, 2 * n, c->phin, c->phi);
+}
+
+// Runs one segment: eagerly, or as a CUDA graph captured the first time this
+// segment is met with the current set of rotating buffer pointers and replayed
+// afterwards (the rotation cycles through six pointer sets).
+static void run_segment(fmf_ctx* c, int id, void (*fn)(fmf_ctx*)) {
+  if (!c->graphs) {
+    fn(c);
+    return;
+  }
+  GraphKey key{id, {c->u, c->v, c->w, c->uo, c->vo, c->wo, c->un, c->vn, c->wn, c->p, c->po, c->pn, c->phi, c->phin}};
+  auto it = c->cache.find(key);
+  if (it == c->cache.end()) {
+    const long long l0 = launches();
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    if (!FMF_CUDA(cudaStreamBeginCapture(c->s, cudaStreamCaptureModeRelaxed))) return;
+    fn(c);
+    if (!FMF_CUDA(cudaStreamEndCapture(c->s, &graph))) return;
+    if (!FMF_CUDA(cudaGraphInstantiate(&exec, graph, 0))) {
+      cudaGraphDestroy(graph);
+      return;
+    }
+    cudaGraphDestroy(graph);
+    const long long nl = launches() - l0;
+    count_launch((int)-nl);  // counted again at every replay below
+    it = c->cache.emplace(key, GraphEntry{exec, nl}).first;
+  }
+  FMF_CUDA(cudaGraphLaunch(it->second.exec, c->s));
+  count_launch((int)it->second.launches);
+}
+
+static int step_once(fmf_ctx* c) {
+  const Grid& g = c->g;
+  run_segment(c, 0, seg_pre);
+  double err = 0.0, err0 = 0.0;
+  int lp;
+  for (lp = 0; lp <= 20; ++lp) {
+    run_segment(c, 1, seg_iter);
+    FMF_CUDA(cudaStreamSynchronize(c->s));
+    const double e = c->host_err[0];
+    if (!std::isfinite(e)) {
+      set_status(FMF_ERR_NONFINITE);
+      break;
+    }
+    err = std::sqrt(e / (double)g.cells()) + 1.0e-99;
+    if (lp == 0) err0 = err;
+    if (err / err0 <= 1.0e-3) break;
+  }
+  c->sor_iters.push_back((lp <= 20 ? lp : 20) + 1);
+  run_segment(c, 2, seg_post);
+  // :686-697 rotation by pointer
   double* t;
   t = c->uo; c->uo = c->u; c->u = c->un; c->un = t;
   t = c->vo; c->vo = c->v; c->v = c->vn; c->vn = t;
   t = c->wo; c->wo = c->w; c->w = c->wn; c->wn = t;
   t = c->po; c->po = c->p; c->p = c->pn; c->pn = t;
   t = c->phi; c->phi = c->phin; c->phin = t;
-  op::copy(s, 2 * n, c->phi, c->phin);
   FMF_CUDA(cudaGetLastError());
   return get_status();
 }
@@ -377,6 +466,7 @@ static int step_once(fmf_ctx* c) {
 // both advection levels, u and uo).
 int fmf_ctx_time_stage(fmf_ctx* c, int stage, int reps, float* ms) {
   if (!c || !ms || reps <= 0 || stage < 0 || stage > 3) return FMF_ERR_ARG;
+  ScratchScope scope(c->scr);
   const fmf_params& P = c->prm;
   const Grid& g = c->g;
   cudaStream_t s = c->s;
@@ -426,9 +516,16 @@ int fmf_ctx_time_stage(fmf_ctx* c, int stage, int reps, float* ms) {
 
 int fmf_ctx_step(fmf_ctx* c, int nsteps) {
   if (!c || nsteps < 0) return FMF_ERR_ARG;
+  ScratchScope scope(c->scr);
   c->sor_iters.clear();
-  for (int t = 0; t < nsteps; ++t)
-    if (step_once(c)) break;
+  for (int t = 0; t < nsteps; ++t) {
+    const bool g = c->graphs;
+    if (!c->warm) c->graphs = false;  // first step eager: scratch and tables get allocated here
+    const int st = step_once(c);
+    c->graphs = g;
+    c->warm = true;
+    if (st) break;
+  }
   return take_status();
 }
 
