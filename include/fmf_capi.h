@@ -257,6 +257,20 @@ double fmf_last_sor_ratio(void);        /* err/err0 of the last solu_sor4_ call 
 double fmf_interface_lower(int ni, int nj, int nk, const double* phi_host, double dx,
                            double xl);
 
+/* Interior mean of q (the value cal_av_ returns in av) for callers that must not
+ * allocate device memory while they run: code working inside another
+ * framework's memory pool or a fixed memory budget, or in the middle of its own
+ * stream-ordered work.  No counterpart in the reference.  q (the
+ * (-2:ni+3,-2:nj+3,-2:nk+3) field) and av (one double) are device pointers;
+ * the work is enqueued on `stream` (NULL: the legacy default stream) and no
+ * cudaMalloc/cudaFree or allocating library routine is called.  Its scratch is a
+ * 512 KiB array compiled into the library, so ceil(nj/8)*nk must not exceed
+ * 65536 (FMF_ERR_ARG otherwise, nothing launched).  All calls on a GPU share
+ * that array: calls that overlap in time on one GPU race.  The first call on
+ * each device looks up the array's address; make it before any stream capture.
+ * Returns FMF_OK or an FMF_ERR_* code. */
+int fmf_cal_av_noalloc(int ni, int nj, int nk, const double* q, double* av, void* stream);
+
 /* ------------------------------------------------------------------------ */
 /* Part 2: device-pointer variants (arrays are device pointers)             */
 /* ------------------------------------------------------------------------ */
