@@ -29,6 +29,9 @@ sys.path.insert(0, os.path.join(REPO, "fel-multi-phase-flow_gb300"))
 sys.path.insert(0, os.path.join(REPO, "oracle"))
 
 WORKLOAD = "couette256"
+# DRAM bytes (read + write) per interior cell of one k_weno2 launch, from the ncu
+# capture summarised in profiles/k_weno2_couette256.md (None until captured)
+WENO_TRAFFIC_PER_CELL = None
 METRIC = "cell-updates/s/step plain FP64 vs mixed at stated error; adjoint/forward cost"
 UNIT = "cell-updates/s"
 
@@ -135,9 +138,25 @@ def main():
     ap.add_argument("--impl", default="fmf", choices=["fmf", "reference"])
     ap.add_argument("--workload", default=WORKLOAD)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile", action="store_true",
+                    help="no timing: start-up pass, --warmup steps, then --steps steps (for ncu launch lists)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
+        return
+    if args.profile:
+        from fmf import build as fbuild
+        from fmf import capi
+        from fmf import config as C
+        fbuild.build()
+        g = capi.Stepper(C.get(args.workload))
+        g.initial_state()
+        g.step(args.warmup)
+        g.sync()
+        g.step(args.steps)
+        g.sync()
+        print(json.dumps({"profile": args.workload, "sor_iterations": g.sor_iterations()}))
+        g.close()
         return
 
     import numpy as np
@@ -205,16 +224,28 @@ def main():
     e2e_dt = time.perf_counter() - t0
     e2e_value = world * cfg.cells * e2e_steps / e2e_dt
 
-    # dominant-stage roofline: WENO5 advection (stage 0), algorithmic bytes 6 words per cell
+    # Dominant kernel: WENO5 advection of both velocity levels (k_weno2, stage 0),
+    # FP64-ALU bound.  Algorithmic work per cell = the reference formula of weno5.h
+    # (140 flops per directional derivative, plus 6 differences and 6 for the
+    # advecting velocity, 9 directions and 3 accumulations per component) for the
+    # two cal_advu_weno5 calls: 2766 flops; algorithmic bytes 12 words (6 fields in,
+    # 6 out).  FP64 peak measured live by fmf_measure_fma_rate; HBM peak from
+    # MEASURED_PEAKS.json.
     ms_stage = ctypes.c_float()
     capi.check(L.fmf_ctx_time_stage(g.h, 0, 5, ctypes.byref(ms_stage)), "time_stage")
     peaks, peak_kind = _peaks()
-    weno_bytes = 6 * 8 * cfg.cells
-    achieved = weno_bytes / (ms_stage.value * 1e-3) / 1e9
-    roofline = {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
-                "frac": achieved / peaks["hbm_gbs"], "traffic": None,
-                "kernel": "cal_advu_weno5 (one call: u,v,w -> adv_u,adv_v,adv_w)",
-                "kernel_ms": ms_stage.value, "peak_source": peak_kind}
+    fp64 = ctypes.c_double()
+    L.fmf_measure_fma_rate.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_double)]
+    capi.check(L.fmf_measure_fma_rate(1, ctypes.byref(fp64)), "fma rate")
+    t_weno = ms_stage.value * 1e-3
+    flops = 2766.0 * cfg.cells
+    gbs = 12 * 8 * cfg.cells / t_weno / 1e9
+    roofline = {"bound": "fp64", "achieved": flops / t_weno / 1e12, "peak": fp64.value, "unit": "TFLOP/s",
+                "frac": flops / t_weno / 1e12 / fp64.value,
+                "traffic": WENO_TRAFFIC_PER_CELL * cfg.cells if WENO_TRAFFIC_PER_CELL else None,
+                "kernel": "k_weno2 (both cal_advu_weno5 calls of the step)", "kernel_ms": ms_stage.value,
+                "peak_source": "measured live (FP64 FMA chains, fmf_measure_fma_rate); HBM peak " + peak_kind,
+                "hbm": {"achieved": gbs, "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": gbs / peaks["hbm_gbs"]}}
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         v, dt = cpu_baseline_sample(cfg, 1)

@@ -315,6 +315,10 @@ long long fmf_ctx_device_bytes(fmf_ctx* ctx);
  * launch over reps): 0 WENO5 advection, 1 one outer SOR iteration, 2 pressure
  * FFT+TDMA, 3 MTHINC fluxes.  Measurement support; no counterpart in the reference. */
 int fmf_ctx_time_stage(fmf_ctx* ctx, int stage, int reps, float* ms);
+/* FMA throughput of this GPU in TFLOP/s (fp64=1: double, 0: float), from a
+ * register-only kernel timed with CUDA events; the FP64 roofline denominator.
+ * Measurement support; no counterpart in the reference. */
+int fmf_measure_fma_rate(int fp64, double* tflops);
 
 #ifdef __cplusplus
 }
