@@ -30,8 +30,9 @@ sys.path.insert(0, os.path.join(REPO, "oracle"))
 
 WORKLOAD = "couette256"
 # DRAM bytes (read + write) per interior cell of one k_weno2 launch, from the ncu
-# capture summarised in profiles/k_weno2_couette256.md (None until captured)
-WENO_TRAFFIC_PER_CELL = None
+# capture summarised in profiles/k_weno2_couette256.md (230.8 MB + 174.2 MB over
+# 4,194,304 cells); scaled to the workload by its cell count
+WENO_TRAFFIC_PER_CELL = (230.801920e6 + 174.222848e6) / 4194304
 METRIC = "cell-updates/s/step plain FP64 vs mixed at stated error; adjoint/forward cost"
 UNIT = "cell-updates/s"
 
@@ -246,6 +247,41 @@ def main():
                 "kernel": "k_weno2 (both cal_advu_weno5 calls of the step)", "kernel_ms": ms_stage.value,
                 "peak_source": "measured live (FP64 FMA chains, fmf_measure_fma_rate); HBM peak " + peak_kind,
                 "hbm": {"achieved": gbs, "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": gbs / peaks["hbm_gbs"]}}
+    # Mixed precision (FP32 WENO5 / MTHINC Newton+fluxes / SOR sweeps, FP64 pressure,
+    # projection, divergence, volume sums and state): throughput on the same workload,
+    # and the error of phi, u, v, w, p against the FP64 step after the same steps
+    # from the same initial state.
+    gm = capi.Stepper(cfg, precision=capi.FMF_MIXED, stream=stream.cuda_stream)
+    gm.upload(st)
+    gm.step(args.warmup)
+    gm.sync()
+    barrier()
+    e0.record(stream)
+    gm.step(args.steps)
+    e1.record(stream)
+    e1.synchronize()
+    ms_mixed = e0.elapsed_time(e1)
+    n_err = args.warmup + args.steps
+    g.upload(st)
+    g.step(n_err)
+    ref = g.get_state()
+    gm.upload(st)
+    gm.step(n_err)
+    mix = gm.get_state()
+    ms_stage_m = ctypes.c_float()
+    capi.check(L.fmf_ctx_time_stage(gm.h, 0, 5, ctypes.byref(ms_stage_m)), "time_stage mixed")
+    gm.close()
+
+    def rel(f):
+        a, b = C.interior(mix[f]), C.interior(ref[f])
+        return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))
+
+    mixed = {"value": world * cfg.cells * args.steps / (ms_mixed * 1e-3), "unit": UNIT,
+             "ms_per_step": ms_mixed / args.steps, "speedup_vs_fp64": ms / ms_mixed,
+             "steps_compared": n_err,
+             "max_rel_err_vs_fp64": {"phi": rel(9), "u": rel(0), "v": rel(1), "w": rel(2), "p": rel(6)},
+             "weno5_ms": ms_stage_m.value,
+             "precision": "fp32: WENO5, MTHINC Newton + Gauss-point fluxes, SOR sweeps; fp64: everything else"}
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         v, dt = cpu_baseline_sample(cfg, 1)
@@ -262,7 +298,8 @@ def main():
                            "parallelism": "replicas" if world > 1 else "single"},
                 "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 12 * bytes_field,
                         "d2h_bytes_per_step": 12 * bytes_field},
-                "gpu_launches": int(launches), "clocks": clk, "roofline": roofline, "cpu_baseline": cpu}
+                "gpu_launches": int(launches), "clocks": clk, "roofline": roofline, "cpu_baseline": cpu,
+                "mixed": mixed}
         print(json.dumps(line), flush=True)
     g.close()
 

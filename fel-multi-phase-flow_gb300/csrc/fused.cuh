@@ -10,14 +10,15 @@ namespace fused {
 
 void weno5_both(cudaStream_t s, const Grid& g, double dxi, double dyi, double dzi, const double* u,
                 const double* v, const double* w, const double* uo, const double* vo, const double* wo,
-                double* const* adv, double* const* advo);
+                double* const* adv, double* const* advo, bool fp32 = false);
 
 // solphi_mthinc1 for the faces solphi_mthinc2 reads (every face of rows 1..n in
 // the two directions normal to it, faces 0..n along it); list/count: device scratch
 // of >= (ni+2)(nj+2)(nk+2) ints and one int.
 void mthinc_fluxes(cudaStream_t s, const Grid& g, double dxinv, double dyinv, double dzinv, double dt, double bet,
                    const double* phi, const double* gx, const double* gy, const double* gz, const double* u,
-                   const double* v, const double* w, double* fx, double* fy, double* fz, int* list, int* count);
+                   const double* v, const double* w, double* fx, double* fy, double* fz, int* list, int* count,
+                   bool fp32 = false);
 
 // Viscous solve.  visc_prep: edge viscosities E[0..2] (xy, xz, yz edges, i,j,k in 0..n),
 // per-component A/B (AB[0..5] = Au Bu Av Bv Aw Bw) from mu, rho, rhon, src, and the
@@ -39,7 +40,7 @@ void wall_halo(cudaStream_t s, const Grid& g, int normal, double uwall, const do
 // part: sor_parts(g) doubles of scratch
 void sor_iteration(cudaStream_t s, const Grid& g, double dxinv, double dyinv, double dzinv, int harmonic,
                    const double* mu, double* const* E, double* const* AB, double uwall, const double* wallc,
-                   double* un, double* vn, double* wn, double* part, double* errsum);
+                   double* un, double* vn, double* wn, double* part, double* errsum, bool fp32 = false);
 long sor_parts(const Grid& g);
 
 }  // namespace fused

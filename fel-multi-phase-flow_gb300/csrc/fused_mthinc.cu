@@ -31,22 +31,26 @@ __device__ __forceinline__ double avg8(const double* __restrict__ p, long c, lon
          0.125;
 }
 
+__device__ __forceinline__ double ex(double x) { return exp(x); }
+__device__ __forceinline__ float ex(float x) { return expf(fminf(x, 80.0f)); }
+
 // sum over the 8 Gauss points of w/(1+exp(-2 bet (x_t + d))); optionally the sum of s(1-s)
-__device__ __forceinline__ double sig8(const double* a, double w, double m2b, double d, double* sd) {
-  double s = 0.0, q = 0.0;
+template <class R>
+__device__ __forceinline__ R sig8(const R* a, R w, R m2b, R d, R* sd) {
+  R s = 0, q = 0;
 #pragma unroll
   for (int t = 0; t < 8; ++t) {
-    const double e = exp(m2b * (a[t] + d));
-    const double r = 1.0 / (1.0 + e);
+    const R e = ex(m2b * (a[t] + d));
+    const R r = (R)1 / ((R)1 + e);
     s += r;
     if (sd) q += e * r * r;  // s(1-s) with 1-s = e/(1+e), exact in relative terms for any a
   }
   if (sd) *sd = q;
   return w * s;
 }
-__device__ __forceinline__ void gauss8(double* a, double rnx, double rny, double rnz, double x1g, double x2g,
-                                       double y1g, double y2g, double z1g, double z2g) {
-  const double x1 = rnx * x1g, x2 = rnx * x2g, y1 = rny * y1g, y2 = rny * y2g, z1 = rnz * z1g, z2 = rnz * z2g;
+template <class R>
+__device__ __forceinline__ void gauss8(R* a, R rnx, R rny, R rnz, R x1g, R x2g, R y1g, R y2g, R z1g, R z2g) {
+  const R x1 = rnx * x1g, x2 = rnx * x2g, y1 = rny * y1g, y2 = rny * y2g, z1 = rnz * z1g, z2 = rnz * z2g;
   a[0] = x1 + y1 + z1;
   a[1] = x2 + y1 + z1;
   a[2] = x1 + y2 + z1;
@@ -103,6 +107,11 @@ __global__ void __launch_bounds__(256) k_classify(Grid g, MC m, const double* __
   if (k == g.nk + 1 && wt < 0.0) fz[c] = 0.0;
 }
 
+// R = double: the FP64 step.  R = float: the mixed-precision step (normal, band
+// test and the fluxes' storage stay double; the Newton solve and the Gauss-point
+// integrals run in float with the exponent argument clamped to the float range
+// and the Newton regularisation 1e-99 raised to 1e-30).
+template <class R>
 __global__ void __launch_bounds__(128) k_band(Grid g, MC m, const double* __restrict__ phi,
                                               const double* __restrict__ gx, const double* __restrict__ gy,
                                               const double* __restrict__ gz, const double* __restrict__ u,
@@ -112,38 +121,37 @@ __global__ void __launch_bounds__(128) k_band(Grid g, MC m, const double* __rest
                                               const int* __restrict__ count) {
   const int n = *count;
   const long X = 1, Y = g.sy, Z = g.sz;
-  const double m2b = -2.0 * m.bet, gp1 = m.gp1, gp2 = m.gp2;
+  const R m2b = (R)(-2.0 * m.bet), gp1 = (R)m.gp1, gp2 = (R)m.gp2, bet = (R)m.bet, dtt = (R)m.dt;
+  const R reg = sizeof(R) == 8 ? (R)1.0e-99 : (R)1.0e-30;
   for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
     const long c = list[e];
-    double rnx = avg8(gx, c, X, Y, Z), rny = avg8(gy, c, X, Y, Z), rnz = avg8(gz, c, X, Y, Z);
-    const double q00 = sqrt(rnx * rnx + rny * rny + rnz * rnz);
+    double nx = avg8(gx, c, X, Y, Z), ny = avg8(gy, c, X, Y, Z), nz = avg8(gz, c, X, Y, Z);
+    const double q00 = sqrt(nx * nx + ny * ny + nz * nz);
     const double coef = 1.0 / q00;
-    rnx *= coef;
-    rny *= coef;
-    rnz *= coef;
-    double a[8];
-    gauss8(a, rnx, rny, rnz, gp1, gp2, gp1, gp2, gp1, gp2);
-    const double ph = __ldg(phi + c);
-    double ddd = 0.0;
+    const R rnx = (R)(nx * coef), rny = (R)(ny * coef), rnz = (R)(nz * coef);
+    R a[8];
+    gauss8<R>(a, rnx, rny, rnz, gp1, gp2, gp1, gp2, gp1, gp2);
+    const R ph = (R)__ldg(phi + c);
+    R ddd = 0;
 #pragma unroll 1
     for (int it = 0; it < 10; ++it) {
-      double sd;
-      const double f = sig8(a, 0.125, m2b, ddd, &sd) - ph;
+      R sd;
+      const R f = sig8<R>(a, (R)0.125, m2b, ddd, &sd) - ph;
       // df = 0.5 bet sum 0.125/cosh^2 = 0.5 bet * 0.125 * 4 * sum s(1-s)
-      const double df = 0.25 * m.bet * sd;
-      ddd = ddd - f * df / (df * df + 1.0e-99);
+      const R df = (R)0.25 * bet * sd;
+      ddd = ddd - f * df / (df * df + reg);
     }
     const double uw = __ldg(u + c - X), ue = __ldg(u + c), vs = __ldg(v + c - Y), vn = __ldg(v + c),
                  wb = __ldg(w + c - Z), wt = __ldg(w + c);
     auto side = [&](double vel, double dinv, int axis, bool minus, double* out) {
-      const double vd = vel * m.dt * dinv;
-      const double st = minus ? -0.5 : 0.5 - vd, en = minus ? -0.5 - vd : 0.5;
-      const double g1 = (st + en) * 0.5 + (-st + en) * gp1, g2 = (st + en) * 0.5 + (-st + en) * gp2;
-      double b[8];
-      if (axis == 0) gauss8(b, rnx, rny, rnz, g1, g2, gp1, gp2, gp1, gp2);
-      else if (axis == 1) gauss8(b, rnx, rny, rnz, gp1, gp2, g1, g2, gp1, gp2);
-      else gauss8(b, rnx, rny, rnz, gp1, gp2, gp1, gp2, g1, g2);
-      *out = sig8(b, 0.125 * vd, m2b, ddd, nullptr);
+      const R vd = (R)vel * dtt * (R)dinv;
+      const R st = minus ? (R)-0.5 : (R)0.5 - vd, en = minus ? (R)-0.5 - vd : (R)0.5;
+      const R g1 = (st + en) * (R)0.5 + (-st + en) * gp1, g2 = (st + en) * (R)0.5 + (-st + en) * gp2;
+      R b[8];
+      if (axis == 0) gauss8<R>(b, rnx, rny, rnz, g1, g2, gp1, gp2, gp1, gp2);
+      else if (axis == 1) gauss8<R>(b, rnx, rny, rnz, gp1, gp2, g1, g2, gp1, gp2);
+      else gauss8<R>(b, rnx, rny, rnz, gp1, gp2, gp1, gp2, g1, g2);
+      *out = (double)sig8<R>(b, (R)0.125 * vd, m2b, ddd, nullptr);
     };
     if (uw < 0.0) side(uw, m.dxi, 0, true, fx + c - X);
     if (ue > 0.0) side(ue, m.dxi, 0, false, fx + c);
@@ -157,7 +165,8 @@ __global__ void __launch_bounds__(128) k_band(Grid g, MC m, const double* __rest
 
 void mthinc_fluxes(cudaStream_t s, const Grid& g, double dxinv, double dyinv, double dzinv, double dt, double bet,
                    const double* phi, const double* gx, const double* gy, const double* gz, const double* u,
-                   const double* v, const double* w, double* fx, double* fy, double* fz, int* list, int* count) {
+                   const double* v, const double* w, double* fx, double* fy, double* fz, int* list, int* count,
+                   bool fp32) {
   MC m;
   const double dx = 1.0 / dxinv, dy = 1.0 / dyinv, dz = 1.0 / dzinv;
   m.gp1 = -0.5 / std::sqrt(3.0);
@@ -175,7 +184,10 @@ void mthinc_fluxes(cudaStream_t s, const Grid& g, double dxinv, double dyinv, do
   dim3 b(32, 8, 1);
   dim3 gr((unsigned)((g.ni + 2 + 31) / 32), (unsigned)((g.nj + 2 + 7) / 8), (unsigned)(g.nk + 2));
   k_classify<<<gr, b, 0, s>>>(g, m, phi, gx, gy, gz, u, v, w, fx, fy, fz, list, count);
-  k_band<<<152 * 8, 128, 0, s>>>(g, m, phi, gx, gy, gz, u, v, w, fx, fy, fz, list, count);
+  if (fp32)
+    k_band<float><<<152 * 8, 128, 0, s>>>(g, m, phi, gx, gy, gz, u, v, w, fx, fy, fz, list, count);
+  else
+    k_band<double><<<152 * 8, 128, 0, s>>>(g, m, phi, gx, gy, gz, u, v, w, fx, fy, fz, list, count);
   count_launch(2);
 }
 

@@ -136,7 +136,10 @@ __global__ void __launch_bounds__(256) k_src_ab(Grid g, VP p, SrcIn in, const do
 // One colour pair of one component.  Thread (a, b, kk) covers, for the pair whose
 // first colour has parities (pi,pj,pk), the point (pi+2a, pj+2b, pk+2kk) and the
 // point of the second colour (all parities flipped) at (pi'+2a, pj'+2b, pk'+2kk).
-template <int COMP>
+// R = double: the FP64 step.  R = float: the mixed-precision step -- the iterates
+// stay in double storage, the 14-neighbour sum and the update are formed in float,
+// and the increment d = q_new - q and the residual sum are taken in double.
+template <int COMP, class R>
 __global__ void __launch_bounds__(256) k_pair(Grid g, VP p, int pi, int pj, int pk, const double* __restrict__ mu,
                                               const double* __restrict__ exy, const double* __restrict__ exz,
                                               const double* __restrict__ eyz, const double* __restrict__ A,
@@ -146,6 +149,7 @@ __global__ void __launch_bounds__(256) k_pair(Grid g, VP p, int pi, int pj, int 
   const int tid = threadIdx.y * 32 + threadIdx.x;
   const int jmax = COMP == 1 ? g.nj - 1 : g.nj;
   const long X = 1, Y = g.sy, Z = g.sz;
+  const R dx2 = (R)p.dx2, dy2 = (R)p.dy2, dz2 = (R)p.dz2, dxy = (R)p.dxy, dxz = (R)p.dxz, dyz = (R)p.dyz;
   double e = 0.0;
 #pragma unroll
   for (int h = 0; h < 2; ++h) {
@@ -154,30 +158,32 @@ __global__ void __launch_bounds__(256) k_pair(Grid g, VP p, int pi, int pj, int 
     const int k = (h ? 3 - pk : pk) + 2 * (int)blockIdx.z;
     if (i > g.ni || j > jmax || k > g.nk) continue;
     const long c = g.at(i, j, k);
-    double visn, q;
+    auto U = [&](long o) { return (R)un[c + o]; };
+    auto V = [&](long o) { return (R)vn[c + o]; };
+    auto W = [&](long o) { return (R)wn[c + o]; };
+    auto M = [&](const double* a, long o) { return (R)__ldg(a + c + o); };
+    R visn;
+    double q;
     if (COMP == 0) {
-      const double ym = __ldg(exy + c - Y), yp = __ldg(exy + c), zm = __ldg(exz + c - Z), zp = __ldg(exz + c);
-      visn = p.dz2 * (zm * un[c - Z] + zp * un[c + Z]) + p.dy2 * (ym * un[c - Y] + yp * un[c + Y]) +
-             2.0 * p.dx2 * (__ldg(mu + c) * un[c - X] + __ldg(mu + c + X) * un[c + X]) +
-             p.dxy * (ym * (vn[c - Y] - vn[c + X - Y]) + yp * (vn[c + X] - vn[c])) +
-             p.dxz * (zm * (wn[c - Z] - wn[c + X - Z]) + zp * (wn[c + X] - wn[c]));
+      const R ym = M(exy, -Y), yp = M(exy, 0), zm = M(exz, -Z), zp = M(exz, 0);
+      visn = dz2 * (zm * U(-Z) + zp * U(Z)) + dy2 * (ym * U(-Y) + yp * U(Y)) +
+             (R)2 * dx2 * (M(mu, 0) * U(-X) + M(mu, X) * U(X)) + dxy * (ym * (V(-Y) - V(X - Y)) + yp * (V(X) - V(0))) +
+             dxz * (zm * (W(-Z) - W(X - Z)) + zp * (W(X) - W(0)));
       q = un[c];
     } else if (COMP == 1) {
-      const double xm = __ldg(exy + c - X), xp = __ldg(exy + c), zm = __ldg(eyz + c - Z), zp = __ldg(eyz + c);
-      visn = p.dz2 * (zm * vn[c - Z] + zp * vn[c + Z]) +
-             2.0 * p.dy2 * (__ldg(mu + c) * vn[c - Y] + __ldg(mu + c + Y) * vn[c + Y]) +
-             p.dx2 * (xm * vn[c - X] + xp * vn[c + X]) + p.dxy * (xm * (un[c - X] - un[c - X + Y]) + xp * (un[c + Y] - un[c])) +
-             p.dyz * (zm * (wn[c - Z] - wn[c + Y - Z]) + zp * (wn[c + Y] - wn[c]));
+      const R xm = M(exy, -X), xp = M(exy, 0), zm = M(eyz, -Z), zp = M(eyz, 0);
+      visn = dz2 * (zm * V(-Z) + zp * V(Z)) + (R)2 * dy2 * (M(mu, 0) * V(-Y) + M(mu, Y) * V(Y)) +
+             dx2 * (xm * V(-X) + xp * V(X)) + dxy * (xm * (U(-X) - U(-X + Y)) + xp * (U(Y) - U(0))) +
+             dyz * (zm * (W(-Z) - W(Y - Z)) + zp * (W(Y) - W(0)));
       q = vn[c];
     } else {
-      const double xm = __ldg(exz + c - X), xp = __ldg(exz + c), ym = __ldg(eyz + c - Y), yp = __ldg(eyz + c);
-      visn = 2.0 * p.dz2 * (__ldg(mu + c) * wn[c - Z] + __ldg(mu + c + Z) * wn[c + Z]) +
-             p.dy2 * (ym * wn[c - Y] + yp * wn[c + Y]) + p.dx2 * (xm * wn[c - X] + xp * wn[c + X]) +
-             p.dxz * (xm * (un[c - X] - un[c - X + Z]) + xp * (un[c + Z] - un[c])) +
-             p.dyz * (ym * (vn[c - Y] - vn[c - Y + Z]) + yp * (vn[c + Z] - vn[c]));
+      const R xm = M(exz, -X), xp = M(exz, 0), ym = M(eyz, -Y), yp = M(eyz, 0);
+      visn = (R)2 * dz2 * (M(mu, 0) * W(-Z) + M(mu, Z) * W(Z)) + dy2 * (ym * W(-Y) + yp * W(Y)) +
+             dx2 * (xm * W(-X) + xp * W(X)) + dxz * (xm * (U(-X) - U(-X + Z)) + xp * (U(Z) - U(0))) +
+             dyz * (ym * (V(-Y) - V(-Y + Z)) + yp * (V(Z) - V(0)));
       q = wn[c];
     }
-    const double qn = __ldg(A + c) * visn + __ldg(B + c);
+    const double qn = (double)(M(A, 0) * visn + M(B, 0));
     const double d = qn - q;
     if (COMP == 0) un[c] = qn;
     else if (COMP == 1) vn[c] = qn;
@@ -402,7 +408,7 @@ void wall_halo(cudaStream_t s, const Grid& g, int normal, double uwall, const do
 
 void sor_iteration(cudaStream_t s, const Grid& g, double dxinv, double dyinv, double dzinv, int harmonic,
                    const double* mu, double* const* E, double* const* AB, double uwall, const double* wallc,
-                   double* un, double* vn, double* wn, double* part, double* errsum) {
+                   double* un, double* vn, double* wn, double* part, double* errsum, bool fp32) {
   VP p;
   p.dtinv = 0.0;
   p.dx2 = dxinv * dxinv;
@@ -420,12 +426,19 @@ void sor_iteration(cudaStream_t s, const Grid& g, double dxinv, double dyinv, do
   for (int comp = 0; comp < 3; ++comp) {
     for (int pr = 0; pr < 4; ++pr) {
       double* pp = part + (long)(comp * 4 + pr) * nb;
-      if (comp == 0)
-        k_pair<0><<<grd, blk, 0, s>>>(g, p, pi_[pr], pj_[pr], pk_[pr], mu, E[0], E[1], E[2], AB[0], AB[1], un, vn, wn, pp);
-      else if (comp == 1)
-        k_pair<1><<<grd, blk, 0, s>>>(g, p, pi_[pr], pj_[pr], pk_[pr], mu, E[0], E[1], E[2], AB[2], AB[3], un, vn, wn, pp);
-      else
-        k_pair<2><<<grd, blk, 0, s>>>(g, p, pi_[pr], pj_[pr], pk_[pr], mu, E[0], E[1], E[2], AB[4], AB[5], un, vn, wn, pp);
+#define FMF_PAIR(C, R)                                                                                      \
+  k_pair<C, R><<<grd, blk, 0, s>>>(g, p, pi_[pr], pj_[pr], pk_[pr], mu, E[0], E[1], E[2], AB[2 * C], AB[2 * C + 1], \
+                                   un, vn, wn, pp)
+      if (fp32) {
+        if (comp == 0) FMF_PAIR(0, float);
+        else if (comp == 1) FMF_PAIR(1, float);
+        else FMF_PAIR(2, float);
+      } else {
+        if (comp == 0) FMF_PAIR(0, double);
+        else if (comp == 1) FMF_PAIR(1, double);
+        else FMF_PAIR(2, double);
+      }
+#undef FMF_PAIR
       count_launch();
       wall_halo(s, g, 1 << comp, uwall, wallc, un, vn, wn);
     }

@@ -84,6 +84,7 @@ int fmf_ctx_create(const fmf_params* prm, fmf_ctx** out) {
   if (!prm || !out) return FMF_ERR_ARG;
   auto p2 = [](int n) { return n >= 4 && (n & (n - 1)) == 0; };
   if (!p2(prm->ni) || !p2(prm->nj) || !p2(prm->nk) || prm->ni < 16) return FMF_ERR_ARG;
+  if (prm->precision != FMF_FP64 && prm->precision != FMF_MIXED) return FMF_ERR_ARG;
   fmf_ctx* c = new fmf_ctx();
   c->prm = *prm;
   if (const char* e = std::getenv("FMF_GRAPHS")) c->graphs = std::atoi(e) != 0;
@@ -300,7 +301,7 @@ static void seg_pre(fmf_ctx* c) {
   {
     const long nb = (long)(g.ni + 2) * (g.nj + 2) * (g.nk + 2);
     fused::mthinc_fluxes(s, g, dxinv, dyinv, dzinv, dt, P.bet_mthinc, phi1, c->phix, c->phiy, c->phiz, c->u, c->v,
-                         c->w, c->flx, c->fly, c->flz, c->band, c->band + nb);
+                         c->w, c->flx, c->fly, c->flz, c->band, c->band + nb, P.precision == FMF_MIXED);
   }
   op::solphi_mthinc2(s, g, dxinv, dyinv, dzinv, dt, c->u, c->v, c->w, c->flx, c->fly, c->flz, phi1, phin1);
   op::cal_grad_p2a(s, g, dxinv, dyinv, dzinv, phin1, c->phix, c->phiy, c->phiz);
@@ -319,7 +320,8 @@ static void seg_pre(fmf_ctx* c) {
   op::cal_arith_mean(s, g, phi0, P.rmul, P.rmug, c->rmu);
   op::cal_arith_mean(s, g, phin0, P.rmul, P.rmug, c->rmun);
   // :532-541
-  fused::weno5_both(s, g, dxinv, dyinv, dzinv, c->u, c->v, c->w, c->uo, c->vo, c->wo, c->adv, c->advo);
+  fused::weno5_both(s, g, dxinv, dyinv, dzinv, c->u, c->v, c->w, c->uo, c->vo, c->wo, c->adv, c->advo,
+                    P.precision == FMF_MIXED);
   op::calphat(s, g, c->p, c->po, c->phat);
   op::cal_grad_prs(s, g, dxinv, dyinv, dzinv, c->phat, c->prs[0], c->prs[1], c->prs[2]);
   op::calsij(s, g, dxinv, dyinv, dzinv, c->u, c->v, c->w, c->sk);
@@ -368,7 +370,7 @@ static void seg_iter(fmf_ctx* c) {
   const fmf_params& P = c->prm;
   const double dxinv = 1.0 / P.dx, dyinv = 1.0 / P.dy, dzinv = 1.0 / P.dz;
   fused::sor_iteration(c->s, c->g, dxinv, dyinv, dzinv, P.harmonic, c->rmun, c->edge, c->ab, P.uwall, c->wallc, c->un,
-                       c->vn, c->wn, c->sorpart, c->red + 8);
+                       c->vn, c->wn, c->sorpart, c->red + 8, P.precision == FMF_MIXED);
   FMF_CUDA(cudaMemcpyAsync(c->host_err, c->red + 8, sizeof(double), cudaMemcpyDeviceToHost, c->s));
 }
 
@@ -472,14 +474,15 @@ int fmf_ctx_time_stage(fmf_ctx* c, int stage, int reps, float* ms) {
   cudaStream_t s = c->s;
   const double dxinv = 1.0 / P.dx, dyinv = 1.0 / P.dy, dzinv = 1.0 / P.dz;
   const long n = g.n;
+  const bool mixed = P.precision == FMF_MIXED;
   auto run = [&]() {
     switch (stage) {
       case 0:
-        fused::weno5_both(s, g, dxinv, dyinv, dzinv, c->u, c->v, c->w, c->uo, c->vo, c->wo, c->adv, c->advo);
+        fused::weno5_both(s, g, dxinv, dyinv, dzinv, c->u, c->v, c->w, c->uo, c->vo, c->wo, c->adv, c->advo, mixed);
         break;
       case 1:
         fused::sor_iteration(s, g, dxinv, dyinv, dzinv, P.harmonic, c->rmun, c->edge, c->ab, P.uwall, c->wallc,
-                             c->un, c->vn, c->wn, c->sorpart, c->red + 8);
+                             c->un, c->vn, c->wn, c->sorpart, c->red + 8, mixed);
         break;
       case 2:
         op::fft_forward_planes(s, g, c->div, c->pr, c->pi);
@@ -489,7 +492,7 @@ int fmf_ctx_time_stage(fmf_ctx* c, int stage, int reps, float* ms) {
       case 3:
         fused::mthinc_fluxes(s, g, dxinv, dyinv, dzinv, P.dt, P.bet_mthinc, c->phi + n, c->phix, c->phiy,
                              c->phiz, c->u, c->v, c->w, c->flx, c->fly, c->flz, c->band,
-                             c->band + (long)(g.ni + 2) * (g.nj + 2) * (g.nk + 2));
+                             c->band + (long)(g.ni + 2) * (g.nj + 2) * (g.nk + 2), mixed);
         break;
     }
   };
