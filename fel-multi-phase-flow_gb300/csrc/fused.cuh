@@ -20,6 +20,13 @@ void mthinc_fluxes(cudaStream_t s, const Grid& g, double dxinv, double dyinv, do
                    const double* v, const double* w, double* fx, double* fy, double* fz, int* list, int* count,
                    bool fp32 = false);
 
+// CSF force of one field on the interior u, v, w points (fu/fv/fw), replacing
+// cal_grad_p2a + calrn x4 + calrkap + cal_grad_p2uvw + calfst; needs ni % 32 == 0
+// and nj % 8 == 0 (csf_supported).
+bool csf_supported(const Grid& g);
+void csf_force(cudaStream_t s, const Grid& g, double dxinv, double dyinv, double dzinv, double rhol, double rhog,
+               double sigma, const double* phi, double* fu, double* fv, double* fw);
+
 // Viscous solve.  visc_prep: edge viscosities E[0..2] (xy, xz, yz edges, i,j,k in 0..n),
 // per-component A/B (AB[0..5] = Au Bu Av Bv Aw Bw) from mu, rho, rhon, src, and the
 // Navier-slip wall coefficients wallc (2*(nk+6)*(ni+6)*2 doubles) from phi, l1, l2.

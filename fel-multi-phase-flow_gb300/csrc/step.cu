@@ -286,6 +286,8 @@ int fmf_ctx_init_bc(fmf_ctx* c) {
 // seg_post: main.f90:625-697 (pressure solve, projection, boundary conditions, rotation
 // of phin into phi).  The pointer rotation of u/uo/un, p/po/pn and phi/phin is done
 // on the host between steps.
+static void csf_dropin(fmf_ctx* c, const double* phi1, const double* phin1);
+
 static void seg_pre(fmf_ctx* c) {
   const fmf_params& P = c->prm;
   const Grid& g = c->g;
@@ -328,6 +330,39 @@ static void seg_pre(fmf_ctx* c) {
   op::cal_tau(s, g, c->sk, c->rmu, c->tau, false);
   op::cal_div_tensor(s, g, dxinv, dyinv, dzinv, c->tau, c->vis[0], c->vis[1], c->vis[2]);
   // :545-570 surface tension
+  if (fused::csf_supported(g)) {
+    fused::csf_force(s, g, dxinv, dyinv, dzinv, P.rhol, P.rhog, P.sigma, phi1, c->sfst[0], c->sfst[1], c->sfst[2]);
+    fused::csf_force(s, g, dxinv, dyinv, dzinv, P.rhol, P.rhog, P.sigma, phin1, c->sfstn[0], c->sfstn[1],
+                     c->sfstn[2]);
+  } else {
+    csf_dropin(c, phi1, phin1);
+  }
+  // :579-603 (cal_av of rho/rhon at :571-573 feeds nothing downstream)
+  const double* advp[3] = {c->adv[0], c->adv[1], c->adv[2]};
+  const double* advop[3] = {c->advo[0], c->advo[1], c->advo[2]};
+  const double* prsp[3] = {c->prs[0], c->prs[1], c->prs[2]};
+  const double* visp[3] = {c->vis[0], c->vis[1], c->vis[2]};
+  const double* fstp[3] = {c->sfst[0], c->sfst[1], c->sfst[2]};
+  const double* fstnp[3] = {c->sfstn[0], c->sfstn[1], c->sfstn[2]};
+  // :579-603: cal_srcu and the coefficients (as edge viscosities) folded into the
+  // per-point update factors of the viscous solve
+  fused::src_visc_prep(s, g, dxinv, dyinv, dzinv, dt, P.harmonic, P.grvb, P.grvp, c->u, c->v, c->w, advp, advop,
+                       prsp, visp, fstp, fstnp, c->rmun, c->rho, c->rhon, c->edge, c->ab, c->l1, c->l2, phi1, P.dy,
+                       c->wallc);
+  // :605-607
+  op::copy(s, n, c->u, c->un);
+  op::copy(s, n, c->v, c->vn);
+  op::copy(s, n, c->w, c->wn);
+}
+
+// The surface-tension block as the reference's sequence of subroutines (grids the
+// fused kernel does not tile: ni not a multiple of 32 or nj not a multiple of 8).
+static void csf_dropin(fmf_ctx* c, const double* phi1, const double* phin1) {
+  const fmf_params& P = c->prm;
+  const Grid& g = c->g;
+  cudaStream_t s = c->s;
+  const long n = g.n;
+  const double dxinv = 1.0 / P.dx, dyinv = 1.0 / P.dy, dzinv = 1.0 / P.dz;
   for (int q = 0; q < 3; ++q) {
     op::fill(s, n, c->sfst[q], 0.0);
     op::fill(s, n, c->sfstn[q], 0.0);
@@ -348,22 +383,6 @@ static void seg_pre(fmf_ctx* c) {
              c->fstn[2]);
   op::sum_fst(s, g, c->fst[0], c->fst[1], c->fst[2], c->sfst[0], c->sfst[1], c->sfst[2]);
   op::sum_fst(s, g, c->fstn[0], c->fstn[1], c->fstn[2], c->sfstn[0], c->sfstn[1], c->sfstn[2]);
-  // :579-603 (cal_av of rho/rhon at :571-573 feeds nothing downstream)
-  const double* advp[3] = {c->adv[0], c->adv[1], c->adv[2]};
-  const double* advop[3] = {c->advo[0], c->advo[1], c->advo[2]};
-  const double* prsp[3] = {c->prs[0], c->prs[1], c->prs[2]};
-  const double* visp[3] = {c->vis[0], c->vis[1], c->vis[2]};
-  const double* fstp[3] = {c->sfst[0], c->sfst[1], c->sfst[2]};
-  const double* fstnp[3] = {c->sfstn[0], c->sfstn[1], c->sfstn[2]};
-  // :579-603: cal_srcu and the coefficients (as edge viscosities) folded into the
-  // per-point update factors of the viscous solve
-  fused::src_visc_prep(s, g, dxinv, dyinv, dzinv, dt, P.harmonic, P.grvb, P.grvp, c->u, c->v, c->w, advp, advop,
-                       prsp, visp, fstp, fstnp, c->rmun, c->rho, c->rhon, c->edge, c->ab, c->l1, c->l2, phi1, P.dy,
-                       c->wallc);
-  // :605-607
-  op::copy(s, n, c->u, c->un);
-  op::copy(s, n, c->v, c->vn);
-  op::copy(s, n, c->w, c->wn);
 }
 
 static void seg_iter(fmf_ctx* c) {
