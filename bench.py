@@ -139,6 +139,7 @@ def main():
     ap.add_argument("--impl", default="fmf", choices=["fmf", "reference"])
     ap.add_argument("--workload", default=WORKLOAD)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"], help="--profile only")
     ap.add_argument("--profile", action="store_true",
                     help="no timing: start-up pass, --warmup steps, then --steps steps (for ncu launch lists)")
     args = ap.parse_args()
@@ -150,7 +151,8 @@ def main():
         from fmf import capi
         from fmf import config as C
         fbuild.build()
-        g = capi.Stepper(C.get(args.workload))
+        prec = capi.FMF_MIXED if args.precision == "mixed" else capi.FMF_FP64
+        g = capi.Stepper(C.get(args.workload), precision=prec)
         g.initial_state()
         g.step(args.warmup)
         g.sync()
