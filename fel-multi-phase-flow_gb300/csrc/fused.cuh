@@ -22,18 +22,15 @@ void mthinc_fluxes(cudaStream_t s, const Grid& g, double dxinv, double dyinv, do
 
 // CSF force of one field on the interior u, v, w points (fu/fv/fw), replacing
 // cal_grad_p2a + calrn x4 + calrkap + cal_grad_p2uvw + calfst; needs ni % 32 == 0
-// and nj % 8 == 0 (csf_supported).
+// and nj % 8 == 0 (csf_supported).  fp32: normals and curvature in FP32.
 bool csf_supported(const Grid& g);
 void csf_force(cudaStream_t s, const Grid& g, double dxinv, double dyinv, double dzinv, double rhol, double rhog,
-               double sigma, const double* phi, double* fu, double* fv, double* fw);
+               double sigma, const double* phi, double* fu, double* fv, double* fw, bool fp32 = false);
 
-// Viscous solve.  visc_prep: edge viscosities E[0..2] (xy, xz, yz edges, i,j,k in 0..n),
-// per-component A/B (AB[0..5] = Au Bu Av Bv Aw Bw) from mu, rho, rhon, src, and the
-// Navier-slip wall coefficients wallc (2*(nk+6)*(ni+6)*2 doubles) from phi, l1, l2.
-void visc_prep(cudaStream_t s, const Grid& g, double dxinv, double dyinv, double dzinv, double dt, int harmonic,
-               const double* mu, const double* rho, const double* rhon, const double* const* src, double* const* E,
-               double* const* AB, const double* l1, const double* l2, const double* phi, double dy, double* wallc);
-// visc_prep with the momentum right-hand side of cal_srcu formed in registers
+// Viscous solve.  src_visc_prep: edge viscosities E[0..2] (xy, xz, yz edges, i,j,k in
+// 0..n), per-component A/B (AB[0..5] = Au Bu Av Bv Aw Bw) with the momentum
+// right-hand side of cal_srcu formed in registers, and the Navier-slip wall
+// coefficients wallc (2*(nk+6)*(ni+6)*2 doubles) from phi, l1, l2.
 void src_visc_prep(cudaStream_t s, const Grid& g, double dxinv, double dyinv, double dzinv, double dt, int harmonic,
                    double grvb, double grvp, const double* u, const double* v, const double* w,
                    const double* const* adv, const double* const* advo, const double* const* prs,
@@ -47,8 +44,35 @@ void wall_halo(cudaStream_t s, const Grid& g, int normal, double uwall, const do
 // part: sor_parts(g) doubles of scratch
 void sor_iteration(cudaStream_t s, const Grid& g, double dxinv, double dyinv, double dzinv, int harmonic,
                    const double* mu, double* const* E, double* const* AB, double uwall, const double* wallc,
-                   double* un, double* vn, double* wn, double* part, double* errsum, bool fp32 = false);
+                   double* un, double* vn, double* wn, double* part, double* errsum);
 long sor_parts(const Grid& g);
+
+// Mixed-precision viscous solve (one step of iterative refinement).  Buffers:
+struct RefineBufs {
+  float* d[3];  // corrections d = un - u, v, w (n floats each)
+  float* a[3];  // A per component (n)
+  float* r[3];  // R = A*visn(u) + B - u, formed in FP64 (n)
+  float* mu;    // mu (n)
+  float* e[3];  // edge viscosities (n)
+  float* gw;    // wall constants, refine_floats(g, 0)
+  float* gx;    // x-halo constants, refine_floats(g, 1)
+  float* gz;    // z-halo constants, refine_floats(g, 2)
+};
+long refine_floats(const Grid& g, int part);
+// src_visc_prep's E and wallc, then rb.a, rb.r, rb.mu, rb.e, the wall/halo constants
+// from u, v, w, and zero corrections
+void refine_prep(cudaStream_t s, const Grid& g, double dxinv, double dyinv, double dzinv, double dt, int harmonic,
+                 double grvb, double grvp, const double* u, const double* v, const double* w,
+                 const double* const* adv, const double* const* advo, const double* const* prs,
+                 const double* const* vis, const double* const* fst, const double* const* fstn, const double* mu,
+                 const double* rho, const double* rhon, double* const* E, const double* l1, const double* l2,
+                 const double* phi, double dy, double uwall, double* wallc, const RefineBufs& rb);
+// one outer iteration on the corrections; errsum[0] = sum of squared increments
+void sor_iteration_refine(cudaStream_t s, const Grid& g, double dxinv, double dyinv, double dzinv,
+                          const RefineBufs& rb, double* part, double* errsum);
+// un = u + d, vn = v + d_v, wn = w + d_w at every point
+void refine_finish(cudaStream_t s, const Grid& g, const double* u, const double* v, const double* w,
+                   const RefineBufs& rb, double* un, double* vn, double* wn);
 
 }  // namespace fused
 }  // namespace fmf

@@ -15,6 +15,13 @@
 // Vertex gradients G of planes k, k+1 and the normals of planes k-1..k+1 live in
 // shared memory; H(k+1) = G(k)+G(k+1) gives both n12(k+1) and, summed over the
 // four surrounding (i,j), npp(k+1).  Each normal is formed once per block.
+//
+// Two instantiations: R = double (the FP64 step; phi read straight from global
+// memory) and R = float (the mixed-precision step; each phi plane is converted once
+// into a shared-memory ring of three planes, everything after that is FP32 and the
+// three forces are widened to double on the store).
+#include <type_traits>
+
 #include "fused.cuh"
 
 namespace fmf {
@@ -25,31 +32,71 @@ constexpr int TX = 32, TY = 8;
 constexpr int GX = TX + 2, GY = TY + 2;  // G and H region: i in [I0-1, I0+TX], j in [J0-1, J0+TY]
 constexpr int NX = TX + 1, NY = TY + 1;  // normal regions
 constexpr int GP = GX * GY, NP = NX * NY;
+constexpr int QX = GX + 1, QY = GY + 1;  // staged phi plane: i in [I0-1, I0+TX+1], j in [J0-1, J0+TY+1]
+constexpr int QP = QX * QY;
 
+template <class R>
+constexpr bool kStaged = std::is_same<R, float>::value;
+
+template <class R>
 struct CsfP {
-  double dxi, dyi, dzi, gx, gy, gz, vs, st;
+  R dxi, dyi, dzi, gx, gy, gz, vs, st;
 };
 
+template <class R>
 struct Smem {
-  double G[2][3][GP];       // vertex gradients, two planes (ring)
-  double H[3][GP];          // G(k) + G(k+1)
-  double pp[2][3][NP];      // npp, planes k and k+1 (ring); region i in [I0, I0+TX], j in [J0, J0+TY]
-  double a12[2][2][NP];     // n12 (x, y), planes k and k+1; region i in [I0-1, I0+TX-1], j in [J0-1, J0+TY-1]
-  double a13[2][2][NP];     // n13 (x, z), planes k-1 and k; same region
-  double a23[2][2][NP];     // n23 (y, z), planes k-1 and k; same region
+  R G[2][3][GP];    // vertex gradients, two planes (ring)
+  R H[3][GP];       // G(k) + G(k+1)
+  R pp[2][3][NP];   // npp, planes k and k+1 (ring); region i in [I0, I0+TX], j in [J0, J0+TY]
+  R a12[2][2][NP];  // n12 (x, y), planes k and k+1; region i in [I0-1, I0+TX-1], j in [J0-1, J0+TY-1]
+  R a13[2][2][NP];  // n13 (x, z), planes k-1 and k; same region
+  R a23[2][2][NP];  // n23 (y, z), planes k-1 and k; same region
+  R Q[kStaged<R> ? 3 : 1][kStaged<R> ? QP : 1];  // staged phi planes, slot = plane % 3
 };
 
+// 1/sqrt(s) for s in the FP32 normal range: Newton-Raphson on f(y) = y^-2 - s,
+// y <- y (3 - s y^2)/2, seeded with the FP32 reciprocal square root (relative error
+// ~3e-7 after the rounding of s); the error squares per step, so two steps reach
+// FP64 rounding.  Eight FP64 operations instead of a square root and a division.
+__device__ __forceinline__ double rsqrt_newton(double s) {
+  double y = (double)rsqrtf((float)s);
+#pragma unroll
+  for (int it = 0; it < 2; ++it) y = y * fma(-0.5 * s * y, y, 1.5);
+  return y;
+}
+// N(v) = v/(|v| + vs).  Where |v| exceeds vs by more than 1e12 the relative
+// correction vs/|v| is below 1e-12 and 1/|v| is used; smaller |v| (including zero
+// gradients) takes the exact expression.  |v|^2 is below 1e6 dxinv^2 for phi in
+// [0, 1], inside the FP32 range.
 __device__ __forceinline__ void unit(double x, double y, double z, double vs, double* o) {
   const double s = x * x + y * y + z * z;
-  const double inv = 1.0 / (sqrt(s) + vs);
+  const double big = vs * 1.0e12;
+  const double inv = (s > big * big && s < 1.0e30) ? rsqrt_newton(s) : 1.0 / (sqrt(s) + vs);
+  o[0] = x * inv;
+  o[1] = y * inv;
+  o[2] = z * inv;
+}
+// FP32: where |v| < 1e-15 the squares would leave the normal range, so numerator
+// and denominator are both scaled by 2^64 first (an exact power-of-two scaling).
+__device__ __forceinline__ void unit(float x, float y, float z, float vs, float* o) {
+  float s = x * x + y * y + z * z;
+  if (s < 1.0e-30f) {
+    const float c = 18446744073709551616.0f;  // 2^64
+    x *= c;
+    y *= c;
+    z *= c;
+    vs *= c;
+    s = x * x + y * y + z * z;
+  }
+  const float inv = 1.0f / (sqrtf(s) + vs);
   o[0] = x * inv;
   o[1] = y * inv;
   o[2] = z * inv;
 }
 
-// vertex gradient at (i+1/2, j+1/2, k+1/2) into slot
-__device__ void grad_plane(const Grid& g, const CsfP& p, const double* __restrict__ phi, int I0, int J0, int k,
-                           double (*G)[GP]) {
+// vertex gradient at (i+1/2, j+1/2, k+1/2), straight from phi in global memory
+__device__ void grad_plane(const Grid& g, const CsfP<double>& p, const double* __restrict__ phi, int I0, int J0,
+                           int k, double (*G)[GP]) {
   const long X = 1, Y = g.sy, Z = g.sz;
   for (int e = threadIdx.x; e < GP; e += blockDim.x) {
     const int a = e % GX, b = e / GX;
@@ -63,106 +110,144 @@ __device__ void grad_plane(const Grid& g, const CsfP& p, const double* __restric
     G[2][e] = (-q000 - qp00 - q0p0 - qpp0 + q00p + qp0p + q0pp + qppp) * p.gz;
   }
 }
+// the same from two staged planes (Qa = plane k, Qb = plane k+1)
+template <class R>
+__device__ void grad_staged(const CsfP<R>& p, const R* Qa, const R* Qb, R (*G)[GP]) {
+  for (int e = threadIdx.x; e < GP; e += blockDim.x) {
+    const int a = e % GX, b = e / GX;
+    const int c = b * QX + a;
+    const R q000 = Qa[c], qp00 = Qa[c + 1], q0p0 = Qa[c + QX], qpp0 = Qa[c + QX + 1];
+    const R q00p = Qb[c], qp0p = Qb[c + 1], q0pp = Qb[c + QX], qppp = Qb[c + QX + 1];
+    G[0][e] = (-q000 + qp00 - q0p0 + qpp0 - q00p + qp0p - q0pp + qppp) * p.gx;
+    G[1][e] = (-q000 - qp00 + q0p0 + qpp0 - q00p - qp0p + q0pp + qppp) * p.gy;
+    G[2][e] = (-q000 - qp00 - q0p0 - qpp0 + q00p + qp0p + q0pp + qppp) * p.gz;
+  }
+}
+// phi plane k (i in [I0-1, I0+TX+1], j in [J0-1, J0+TY+1]) into Q, converted to R
+template <class R>
+__device__ void stage_plane(const Grid& g, const double* __restrict__ phi, int I0, int J0, int k, R* Q) {
+  for (int e = threadIdx.x; e < QP; e += blockDim.x) {
+    const int a = e % QX, b = e / QX;
+    Q[e] = (R)__ldg(phi + g.at(I0 - 1 + a, J0 - 1 + b, k));
+  }
+}
 // n13 and n23 of plane k from G(k) (slot gk) into ring slot s
-__device__ void side_normals(const CsfP& p, Smem& S, int gk, int s) {
+template <class R>
+__device__ void side_normals(const CsfP<R>& p, Smem<R>& S, int gk, int s) {
   for (int e = threadIdx.x; e < NP; e += blockDim.x) {
-    const int a = e % NX, b = e / NX;           // normal point (I0-1+a, J0-1+b)
-    const int ga = a, gb = b;                    // same point in the G region (offset -1,-1)
+    const int a = e % NX, b = e / NX;  // normal point (I0-1+a, J0-1+b)
+    const int ga = a, gb = b;          // same point in the G region (offset -1,-1)
     const int c0 = gb * GX + ga;
-    double o[3];
+    R o[3];
     // n13(i,j): mean of G(i, j-1) and G(i, j)
     const int cm = (gb - 1) * GX + ga;
     if (gb >= 1) {
-      unit((S.G[gk][0][cm] + S.G[gk][0][c0]) * 0.5, (S.G[gk][1][cm] + S.G[gk][1][c0]) * 0.5,
-           (S.G[gk][2][cm] + S.G[gk][2][c0]) * 0.5, p.vs, o);
+      unit((S.G[gk][0][cm] + S.G[gk][0][c0]) * R(0.5), (S.G[gk][1][cm] + S.G[gk][1][c0]) * R(0.5),
+           (S.G[gk][2][cm] + S.G[gk][2][c0]) * R(0.5), p.vs, o);
       S.a13[s][0][e] = o[0];
       S.a13[s][1][e] = o[2];
     }
     // n23(i,j): mean of G(i-1, j) and G(i, j)
     if (ga >= 1) {
       const int cw = gb * GX + ga - 1;
-      unit((S.G[gk][0][cw] + S.G[gk][0][c0]) * 0.5, (S.G[gk][1][cw] + S.G[gk][1][c0]) * 0.5,
-           (S.G[gk][2][cw] + S.G[gk][2][c0]) * 0.5, p.vs, o);
+      unit((S.G[gk][0][cw] + S.G[gk][0][c0]) * R(0.5), (S.G[gk][1][cw] + S.G[gk][1][c0]) * R(0.5),
+           (S.G[gk][2][cw] + S.G[gk][2][c0]) * R(0.5), p.vs, o);
       S.a23[s][0][e] = o[1];
       S.a23[s][1][e] = o[2];
     }
   }
 }
 // H = G(gk) + G(gk1); then npp (slot s) and n12 (slot s) of the plane of G(gk1)
-__device__ void centre_normals(const CsfP& p, Smem& S, int gk, int gk1, int s) {
+template <class R>
+__device__ void centre_normals(const CsfP<R>& p, Smem<R>& S, int gk, int gk1, int s) {
   for (int e = threadIdx.x; e < GP; e += blockDim.x)
     for (int q = 0; q < 3; ++q) S.H[q][e] = S.G[gk][q][e] + S.G[gk1][q][e];
   __syncthreads();
   for (int e = threadIdx.x; e < NP; e += blockDim.x) {
     const int a = e % NX, b = e / NX;
-    double o[3];
+    R o[3];
     // npp at (I0+a, J0+b): H over (i-1..i, j-1..j) = G region (a..a+1, b..b+1)
     const int h00 = b * GX + a, h10 = h00 + 1, h01 = h00 + GX, h11 = h01 + 1;
-    unit((S.H[0][h00] + S.H[0][h10] + S.H[0][h01] + S.H[0][h11]) * 0.125,
-         (S.H[1][h00] + S.H[1][h10] + S.H[1][h01] + S.H[1][h11]) * 0.125,
-         (S.H[2][h00] + S.H[2][h10] + S.H[2][h01] + S.H[2][h11]) * 0.125, p.vs, o);
+    unit((S.H[0][h00] + S.H[0][h10] + S.H[0][h01] + S.H[0][h11]) * R(0.125),
+         (S.H[1][h00] + S.H[1][h10] + S.H[1][h01] + S.H[1][h11]) * R(0.125),
+         (S.H[2][h00] + S.H[2][h10] + S.H[2][h01] + S.H[2][h11]) * R(0.125), p.vs, o);
     S.pp[s][0][e] = o[0];
     S.pp[s][1][e] = o[1];
     S.pp[s][2][e] = o[2];
     // n12 at (I0-1+a, J0-1+b): H at the same point
-    unit(S.H[0][h00] * 0.5, S.H[1][h00] * 0.5, S.H[2][h00] * 0.5, p.vs, o);
+    unit(S.H[0][h00] * R(0.5), S.H[1][h00] * R(0.5), S.H[2][h00] * R(0.5), p.vs, o);
     S.a12[s][0][e] = o[0];
     S.a12[s][1][e] = o[1];
   }
 }
 
-template <bool ACC>
-__global__ void __launch_bounds__(256) k_csf(Grid g, CsfP p, int kchunk, const double* __restrict__ phi,
+template <class R>
+__global__ void __launch_bounds__(256) k_csf(Grid g, CsfP<R> p, int kchunk, const double* __restrict__ phi,
                                              double* __restrict__ fu, double* __restrict__ fv,
                                              double* __restrict__ fw) {
   extern __shared__ double smraw[];
-  Smem& S = *reinterpret_cast<Smem*>(smraw);
+  Smem<R>& S = *reinterpret_cast<Smem<R>*>(smraw);
   const int I0 = 1 + blockIdx.x * TX, J0 = 1 + blockIdx.y * TY;
   const int kb = 1 + blockIdx.z * kchunk, ke = min(g.nk, kb + kchunk - 1);
   int gA = 0, gB = 1;  // G slots: gA holds plane k, gB the next
   int sp = 0;          // pp/n12 slot of plane k
   int sm = 0;          // n13/n23 slot of plane k-1
   // warm-up: G(kb-1) -> gB, G(kb) -> gA; n13/n23(kb-1) from gB; npp/n12(kb) from both
-  grad_plane(g, p, phi, I0, J0, kb - 1, S.G[gB]);
-  grad_plane(g, p, phi, I0, J0, kb, S.G[gA]);
+  if constexpr (kStaged<R>) {
+    for (int q = kb - 1; q <= kb + 1; ++q) stage_plane(g, phi, I0, J0, q, S.Q[q % 3]);
+    __syncthreads();
+    grad_staged(p, S.Q[(kb - 1) % 3], S.Q[kb % 3], S.G[gB]);
+    grad_staged(p, S.Q[kb % 3], S.Q[(kb + 1) % 3], S.G[gA]);
+  } else {
+    grad_plane(g, p, phi, I0, J0, kb - 1, S.G[gB]);
+    grad_plane(g, p, phi, I0, J0, kb, S.G[gA]);
+  }
   __syncthreads();
   side_normals(p, S, gB, sm);
   centre_normals(p, S, gB, gA, sp);
   __syncthreads();
   const int tx = threadIdx.x % TX, ty = threadIdx.x / TX;
   const int i = I0 + tx, j = J0 + ty;
-  const long X = 1, Y = g.sy, Z = g.sz;
   for (int k = kb; k <= ke; ++k) {
     // G(k+1) -> gB; n13/n23(k) from gA; npp/n12(k+1)
-    grad_plane(g, p, phi, I0, J0, k + 1, S.G[gB]);
+    if constexpr (kStaged<R>) {
+      stage_plane(g, phi, I0, J0, k + 2, S.Q[(k + 2) % 3]);  // the slot of plane k-1, unused from here on
+      __syncthreads();
+      grad_staged(p, S.Q[(k + 1) % 3], S.Q[(k + 2) % 3], S.G[gB]);
+    } else {
+      grad_plane(g, p, phi, I0, J0, k + 1, S.G[gB]);
+    }
     __syncthreads();
     side_normals(p, S, gA, sm ^ 1);
     centre_normals(p, S, gA, gB, sp ^ 1);
     __syncthreads();
     if (i <= g.ni && j <= g.nj) {
       const long c = g.at(i, j, k);
-      const int e = ty * NX + tx;          // npp point (i, j)
+      const int e = ty * NX + tx;            // npp point (i, j)
       const int f = (ty + 1) * NX + tx + 1;  // n12/n13/n23 point (i, j)
-      const double ku = (S.pp[sp][0][e + 1] - S.pp[sp][0][e]) * p.dxi + (S.a12[sp][1][f] - S.a12[sp][1][f - NX]) * p.dyi +
-                        (S.a13[sm ^ 1][1][f] - S.a13[sm][1][f]) * p.dzi;
-      const double kv = (S.a12[sp][0][f] - S.a12[sp][0][f - 1]) * p.dxi + (S.pp[sp][1][e + NX] - S.pp[sp][1][e]) * p.dyi +
-                        (S.a23[sm ^ 1][1][f] - S.a23[sm][1][f]) * p.dzi;
-      const double kw = (S.a13[sm ^ 1][0][f] - S.a13[sm ^ 1][0][f - 1]) * p.dxi +
-                        (S.a23[sm ^ 1][0][f] - S.a23[sm ^ 1][0][f - NX]) * p.dyi +
-                        (S.pp[sp ^ 1][2][e] - S.pp[sp][2][e]) * p.dzi;
-      const double ph = __ldg(phi + c);
-      const double a = -p.st * ku * ((__ldg(phi + c + X) - ph) * p.dxi);
-      const double b = -p.st * kv * ((__ldg(phi + c + Y) - ph) * p.dyi);
-      const double d = -p.st * kw * ((__ldg(phi + c + Z) - ph) * p.dzi);
-      if (ACC) {
-        fu[c] += a;
-        fv[c] += b;
-        fw[c] += d;
+      const R ku = (S.pp[sp][0][e + 1] - S.pp[sp][0][e]) * p.dxi + (S.a12[sp][1][f] - S.a12[sp][1][f - NX]) * p.dyi +
+                   (S.a13[sm ^ 1][1][f] - S.a13[sm][1][f]) * p.dzi;
+      const R kv = (S.a12[sp][0][f] - S.a12[sp][0][f - 1]) * p.dxi + (S.pp[sp][1][e + NX] - S.pp[sp][1][e]) * p.dyi +
+                   (S.a23[sm ^ 1][1][f] - S.a23[sm][1][f]) * p.dzi;
+      const R kw = (S.a13[sm ^ 1][0][f] - S.a13[sm ^ 1][0][f - 1]) * p.dxi +
+                   (S.a23[sm ^ 1][0][f] - S.a23[sm ^ 1][0][f - NX]) * p.dyi + (S.pp[sp ^ 1][2][e] - S.pp[sp][2][e]) * p.dzi;
+      R ph, px, py, pz;
+      if constexpr (kStaged<R>) {
+        const int cq = (ty + 1) * QX + tx + 1;
+        const R* Qk = S.Q[k % 3];
+        ph = Qk[cq];
+        px = Qk[cq + 1];
+        py = Qk[cq + QX];
+        pz = S.Q[(k + 1) % 3][cq];
       } else {
-        fu[c] = a;
-        fv[c] = b;
-        fw[c] = d;
+        ph = __ldg(phi + c);
+        px = __ldg(phi + c + 1);
+        py = __ldg(phi + c + g.sy);
+        pz = __ldg(phi + c + g.sz);
       }
+      fu[c] = (double)(-p.st * ku * ((px - ph) * p.dxi));
+      fv[c] = (double)(-p.st * kv * ((py - ph) * p.dyi));
+      fw[c] = (double)(-p.st * kw * ((pz - ph) * p.dzi));
     }
     __syncthreads();
     gA ^= 1;
@@ -171,27 +256,36 @@ __global__ void __launch_bounds__(256) k_csf(Grid g, CsfP p, int kchunk, const d
     sm ^= 1;
   }
 }
+
+template <class R>
+void launch_csf(cudaStream_t s, const Grid& g, double dxinv, double dyinv, double dzinv, double rhol, double rhog,
+                double sigma, const double* phi, double* fu, double* fv, double* fw) {
+  CsfP<R> p;
+  p.dxi = (R)dxinv;
+  p.dyi = (R)dyinv;
+  p.dzi = (R)dzinv;
+  p.gx = (R)(0.25 * dxinv);
+  p.gy = (R)(0.25 * dyinv);
+  p.gz = (R)(0.25 * dzinv);
+  p.vs = (R)(std::sqrt(dxinv * dxinv + dyinv * dyinv + dzinv * dzinv) * 1.0e-30);
+  p.st = (R)(2.0 * sigma / (rhol + rhog));
+  const int kchunk = g.nk >= 64 ? 16 : (g.nk >= 16 ? 8 : g.nk);
+  const size_t smem = sizeof(Smem<R>);
+  cudaFuncSetAttribute(k_csf<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  dim3 gr((unsigned)(g.ni / TX), (unsigned)(g.nj / TY), (unsigned)((g.nk + kchunk - 1) / kchunk));
+  k_csf<R><<<gr, 256, smem, s>>>(g, p, kchunk, phi, fu, fv, fw);
+  count_launch();
+}
 }  // namespace
 
 bool csf_supported(const Grid& g) { return g.ni % TX == 0 && g.nj % TY == 0; }
 
 void csf_force(cudaStream_t s, const Grid& g, double dxinv, double dyinv, double dzinv, double rhol, double rhog,
-               double sigma, const double* phi, double* fu, double* fv, double* fw) {
-  CsfP p;
-  p.dxi = dxinv;
-  p.dyi = dyinv;
-  p.dzi = dzinv;
-  p.gx = 0.25 * dxinv;
-  p.gy = 0.25 * dyinv;
-  p.gz = 0.25 * dzinv;
-  p.vs = std::sqrt(dxinv * dxinv + dyinv * dyinv + dzinv * dzinv) * 1.0e-30;
-  p.st = 2.0 * sigma / (rhol + rhog);
-  const int kchunk = g.nk >= 64 ? 16 : (g.nk >= 16 ? 8 : g.nk);
-  const size_t smem = sizeof(Smem);
-  cudaFuncSetAttribute(k_csf<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  dim3 gr((unsigned)(g.ni / TX), (unsigned)(g.nj / TY), (unsigned)((g.nk + kchunk - 1) / kchunk));
-  k_csf<false><<<gr, 256, smem, s>>>(g, p, kchunk, phi, fu, fv, fw);
-  count_launch();
+               double sigma, const double* phi, double* fu, double* fv, double* fw, bool fp32) {
+  if (fp32)
+    launch_csf<float>(s, g, dxinv, dyinv, dzinv, rhol, rhog, sigma, phi, fu, fv, fw);
+  else
+    launch_csf<double>(s, g, dxinv, dyinv, dzinv, rhol, rhog, sigma, phi, fu, fv, fw);
 }
 
 }  // namespace fused

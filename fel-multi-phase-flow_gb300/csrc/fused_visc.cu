@@ -4,8 +4,8 @@
 // The 45 coefficient arrays are products of six viscosities and constant grid
 // factors (cal_arith_coef_vis.f:211-231): for u at (i+1/2,j,k) the x-viscosities
 // are the cell values mu(i), mu(i+1) and the y/z ones are edge means shared with
-// the neighbours.  k_prep stores the three edge means once per step (the same
-// 4-cell sums, in the same order, as the reference) together with, per component,
+// the neighbours.  k_edges stores the three edge means once per step (the same
+// 4-cell sums, in the same order, as the reference) and k_src_ab, per component,
 // A = 0.5/(rho00*D) and B = src/D with D = 1/dt + 0.5*a_p/rho00, so a point update
 // of solu_sor4.f:150-170 becomes q_new = A*visn + B with visn the 14-neighbour sum.
 // Colours are processed in their independent pairs (1,2) (3,4) (5,6) (7,8): two
@@ -13,6 +13,11 @@
 // per pair gives the sequential result.  The wall/halo refresh after every second
 // colour (bndu + bnd_periodic of the swept component, solu_sor4.f:176-180) is three
 // ordered plane kernels.
+//
+// The mixed-precision step solves the same system by one step of iterative
+// refinement: the residual of the first sweep is formed in FP64 at u, then the
+// sweeps run in FP32 on the correction d = un - u (FP32 storage and arithmetic),
+// and un = u + d is formed in FP64 at the end.
 #include "fused.cuh"
 
 namespace fmf {
@@ -30,8 +35,12 @@ __device__ __forceinline__ double mean4(double a, double b, double c, double d, 
 }
 
 // Edge viscosities over i,j,k in 0..n, then A/B per component over the interior.
+// f[0..2] non-null: FP32 copies of the three edge arrays as well.
+struct F3 {
+  float* f[3];
+};
 __global__ void __launch_bounds__(256) k_edges(Grid g, VP p, const double* __restrict__ mu, double* __restrict__ exy,
-                                               double* __restrict__ exz, double* __restrict__ eyz) {
+                                               double* __restrict__ exz, double* __restrict__ eyz, F3 f) {
   const int i = (int)(blockIdx.x * blockDim.x + threadIdx.x);
   const int j = (int)(blockIdx.y * blockDim.y + threadIdx.y);
   const int k = (int)blockIdx.z;
@@ -39,62 +48,42 @@ __global__ void __launch_bounds__(256) k_edges(Grid g, VP p, const double* __res
   const long X = 1, Y = g.sy, Z = g.sz;
   const long c = g.at(i, j, k);
   const double m0 = __ldg(mu + c), mx = __ldg(mu + c + X), my = __ldg(mu + c + Y), mz = __ldg(mu + c + Z);
-  exy[c] = mean4(m0, mx, my, __ldg(mu + c + X + Y), p.harmonic);
-  exz[c] = mean4(m0, mx, mz, __ldg(mu + c + X + Z), p.harmonic);
-  eyz[c] = mean4(m0, my, mz, __ldg(mu + c + Y + Z), p.harmonic);
-}
-
-__global__ void __launch_bounds__(256) k_ab(Grid g, VP p, const double* __restrict__ mu,
-                                            const double* __restrict__ exy, const double* __restrict__ exz,
-                                            const double* __restrict__ eyz, const double* __restrict__ rho,
-                                            const double* __restrict__ rhon, const double* __restrict__ su,
-                                            const double* __restrict__ sv, const double* __restrict__ sw,
-                                            double* __restrict__ au, double* __restrict__ bu, double* __restrict__ av,
-                                            double* __restrict__ bv, double* __restrict__ aw, double* __restrict__ bw) {
-  const int i = 1 + (int)(blockIdx.x * blockDim.x + threadIdx.x);
-  const int j = 1 + (int)(blockIdx.y * blockDim.y + threadIdx.y);
-  const int k = 1 + (int)blockIdx.z;
-  if (i > g.ni || j > g.nj) return;
-  const long X = 1, Y = g.sy, Z = g.sz;
-  const long c = g.at(i, j, k);
-  const double r0 = __ldg(rho + c), n0 = __ldg(rhon + c);
-  {  // u: a_p = 2dx2(mu_i + mu_i+1) + dy2(exy_j-1 + exy_j) + dz2(exz_k-1 + exz_k)
-    const double r = (r0 + __ldg(rho + c + X) + n0 + __ldg(rhon + c + X)) * 0.25;
-    const double ap = p.dz2 * __ldg(exz + c - Z) + p.dy2 * __ldg(exy + c - Y) + p.dx2 * __ldg(mu + c) * 2.0 +
-                      p.dx2 * __ldg(mu + c + X) * 2.0 + p.dy2 * __ldg(exy + c) + p.dz2 * __ldg(exz + c);
-    const double D = p.dtinv + ap / r * 0.5;
-    au[c] = 0.5 / (r * D);
-    bu[c] = __ldg(su + c) / D;
-  }
-  if (j <= g.nj - 1) {  // v
-    const double r = (r0 + __ldg(rho + c + Y) + n0 + __ldg(rhon + c + Y)) * 0.25;
-    const double ap = p.dz2 * __ldg(eyz + c - Z) + p.dy2 * __ldg(mu + c) * 2.0 + p.dx2 * __ldg(exy + c - X) +
-                      p.dx2 * __ldg(exy + c) + p.dy2 * __ldg(mu + c + Y) * 2.0 + p.dz2 * __ldg(eyz + c);
-    const double D = p.dtinv + ap / r * 0.5;
-    av[c] = 0.5 / (r * D);
-    bv[c] = __ldg(sv + c) / D;
-  }
-  {  // w
-    const double r = (r0 + __ldg(rho + c + Z) + n0 + __ldg(rhon + c + Z)) * 0.25;
-    const double ap = p.dz2 * __ldg(mu + c) * 2.0 + p.dy2 * __ldg(eyz + c - Y) + p.dx2 * __ldg(exz + c - X) +
-                      p.dx2 * __ldg(exz + c) + p.dy2 * __ldg(eyz + c) + p.dz2 * __ldg(mu + c + Z) * 2.0;
-    const double D = p.dtinv + ap / r * 0.5;
-    aw[c] = 0.5 / (r * D);
-    bw[c] = __ldg(sw + c) / D;
+  const double a = mean4(m0, mx, my, __ldg(mu + c + X + Y), p.harmonic);
+  const double b = mean4(m0, mx, mz, __ldg(mu + c + X + Z), p.harmonic);
+  const double d = mean4(m0, my, mz, __ldg(mu + c + Y + Z), p.harmonic);
+  exy[c] = a;
+  exz[c] = b;
+  eyz[c] = d;
+  if (f.f[0]) {
+    f.f[0][c] = (float)a;
+    f.f[1][c] = (float)b;
+    f.f[2][c] = (float)d;
   }
 }
 
-// cal_srcu.f:53-137 fused with the update factors: src is formed in registers
-// (1/rho00 taken once per face) and only A = 0.5/(rho00*D), B = src/D are stored.
+// cal_srcu.f:53-137 fused with the update factors: src is formed in registers and
+// only A = 0.5/(rho00*D), B = src/D are stored.  With T = 1/(rho00/dt + a_p/2)
+// these are A = T/2 and B = (rho00*(explicit terms) - prs + vis/2)*T: one division
+// per component.
 struct SrcIn {
   const double *u, *v, *w, *rho, *rhon, *adv[3], *advo[3], *prs[3], *vis[3], *fst[3], *fstn[3];
   double grvb, grvp;
 };
+// Outputs: FP64 A and B per component, or (REFINE) FP32 A and the FP64 first-sweep
+// residual R = A*visn(u) + B - u rounded to FP32 (the right-hand side of the
+// correction sweeps of the mixed-precision solve).
+struct ABOut {
+  double *a[3], *b[3];
+  float *af[3], *rf[3];
+};
+template <int COMP, class T>
+__device__ __forceinline__ T visn_at(const Grid& g, const VP& p, long c, const T* __restrict__ mu,
+                                     const T* __restrict__ exy, const T* __restrict__ exz,
+                                     const T* __restrict__ eyz, const T* un, const T* vn, const T* wn);
+template <bool REFINE>
 __global__ void __launch_bounds__(256) k_src_ab(Grid g, VP p, SrcIn in, const double* __restrict__ mu,
                                                 const double* __restrict__ exy, const double* __restrict__ exz,
-                                                const double* __restrict__ eyz, double* __restrict__ au,
-                                                double* __restrict__ bu, double* __restrict__ av, double* __restrict__ bv,
-                                                double* __restrict__ aw, double* __restrict__ bw) {
+                                                const double* __restrict__ eyz, ABOut out) {
   const int i = 1 + (int)(blockIdx.x * blockDim.x + threadIdx.x);
   const int j = 1 + (int)(blockIdx.y * blockDim.y + threadIdx.y);
   const int k = 1 + (int)blockIdx.z;
@@ -102,55 +91,95 @@ __global__ void __launch_bounds__(256) k_src_ab(Grid g, VP p, SrcIn in, const do
   const long X = 1, Y = g.sy, Z = g.sz;
   const long c = g.at(i, j, k);
   const double r0 = __ldg(in.rho + c), n0 = __ldg(in.rhon + c);
-  auto src = [&](int q, const double* vel, double rinv, double grav) {
-    return __ldg(vel + c) * p.dtinv - __ldg(in.adv[q] + c) * 1.5 + __ldg(in.advo[q] + c) * 0.5 -
-           __ldg(in.prs[q] + c) * rinv + __ldg(in.vis[q] + c) * rinv * 0.5 + __ldg(in.fst[q] + c) * 0.5 +
-           __ldg(in.fstn[q] + c) * 0.5 + grav;
+  // rho00 * src
+  auto rsrc = [&](int q, const double* vel, double r, double grav) {
+    return r * (__ldg(vel + c) * p.dtinv - __ldg(in.adv[q] + c) * 1.5 + __ldg(in.advo[q] + c) * 0.5 +
+                __ldg(in.fst[q] + c) * 0.5 + __ldg(in.fstn[q] + c) * 0.5 + grav) -
+           __ldg(in.prs[q] + c) + __ldg(in.vis[q] + c) * 0.5;
+  };
+  auto store = [&](int q, double A, double B, double visn, const double* vel) {
+    if (REFINE) {
+      out.af[q][c] = (float)A;
+      out.rf[q][c] = (float)(A * visn + B - __ldg(vel + c));
+    } else {
+      out.a[q][c] = A;
+      out.b[q][c] = B;
+    }
   };
   {
-    const double r = (r0 + __ldg(in.rho + c + X) + n0 + __ldg(in.rhon + c + X)) * 0.25, ri = 1.0 / r;
+    const double r = (r0 + __ldg(in.rho + c + X) + n0 + __ldg(in.rhon + c + X)) * 0.25;
     const double ap = p.dz2 * __ldg(exz + c - Z) + p.dy2 * __ldg(exy + c - Y) + p.dx2 * __ldg(mu + c) * 2.0 +
                       p.dx2 * __ldg(mu + c + X) * 2.0 + p.dy2 * __ldg(exy + c) + p.dz2 * __ldg(exz + c);
-    const double Di = 1.0 / (p.dtinv + ap * ri * 0.5);
-    au[c] = 0.5 * ri * Di;
-    bu[c] = src(0, in.u, ri, in.grvb) * Di;
+    const double T = 1.0 / (r * p.dtinv + ap * 0.5);
+    const double vn = REFINE ? visn_at<0, double>(g, p, c, mu, exy, exz, eyz, in.u, in.v, in.w) : 0.0;
+    store(0, 0.5 * T, rsrc(0, in.u, r, in.grvb) * T, vn, in.u);
   }
   if (j <= g.nj - 1) {
-    const double r = (r0 + __ldg(in.rho + c + Y) + n0 + __ldg(in.rhon + c + Y)) * 0.25, ri = 1.0 / r;
+    const double r = (r0 + __ldg(in.rho + c + Y) + n0 + __ldg(in.rhon + c + Y)) * 0.25;
     const double ap = p.dz2 * __ldg(eyz + c - Z) + p.dy2 * __ldg(mu + c) * 2.0 + p.dx2 * __ldg(exy + c - X) +
                       p.dx2 * __ldg(exy + c) + p.dy2 * __ldg(mu + c + Y) * 2.0 + p.dz2 * __ldg(eyz + c);
-    const double Di = 1.0 / (p.dtinv + ap * ri * 0.5);
-    av[c] = 0.5 * ri * Di;
-    bv[c] = src(1, in.v, ri, in.grvp) * Di;
+    const double T = 1.0 / (r * p.dtinv + ap * 0.5);
+    const double vn = REFINE ? visn_at<1, double>(g, p, c, mu, exy, exz, eyz, in.u, in.v, in.w) : 0.0;
+    store(1, 0.5 * T, rsrc(1, in.v, r, in.grvp) * T, vn, in.v);
   }
   {
-    const double r = (r0 + __ldg(in.rho + c + Z) + n0 + __ldg(in.rhon + c + Z)) * 0.25, ri = 1.0 / r;
+    const double r = (r0 + __ldg(in.rho + c + Z) + n0 + __ldg(in.rhon + c + Z)) * 0.25;
     const double ap = p.dz2 * __ldg(mu + c) * 2.0 + p.dy2 * __ldg(eyz + c - Y) + p.dx2 * __ldg(exz + c - X) +
                       p.dx2 * __ldg(exz + c) + p.dy2 * __ldg(eyz + c) + p.dz2 * __ldg(mu + c + Z) * 2.0;
-    const double Di = 1.0 / (p.dtinv + ap * ri * 0.5);
-    aw[c] = 0.5 * ri * Di;
-    bw[c] = src(2, in.w, ri, 0.0) * Di;
+    const double T = 1.0 / (r * p.dtinv + ap * 0.5);
+    const double vn = REFINE ? visn_at<2, double>(g, p, c, mu, exy, exz, eyz, in.u, in.v, in.w) : 0.0;
+    store(2, 0.5 * T, rsrc(2, in.w, r, 0.0) * T, vn, in.w);
   }
 }
 
 // One colour pair of one component.  Thread (a, b, kk) covers, for the pair whose
 // first colour has parities (pi,pj,pk), the point (pi+2a, pj+2b, pk+2kk) and the
 // point of the second colour (all parities flipped) at (pi'+2a, pj'+2b, pk'+2kk).
-// R = double: the FP64 step.  R = float: the mixed-precision step -- the iterates
-// stay in double storage, the 14-neighbour sum and the update are formed in float,
-// and the increment d = q_new - q and the residual sum are taken in double.
-template <int COMP, class R>
-__global__ void __launch_bounds__(256) k_pair(Grid g, VP p, int pi, int pj, int pk, const double* __restrict__ mu,
-                                              const double* __restrict__ exy, const double* __restrict__ exz,
-                                              const double* __restrict__ eyz, const double* __restrict__ A,
-                                              const double* __restrict__ B, double* un, double* vn, double* wn,
-                                              double* __restrict__ part) {
-  __shared__ double sh[256];
-  const int tid = threadIdx.y * 32 + threadIdx.x;
-  const int jmax = COMP == 1 ? g.nj - 1 : g.nj;
+// T is the storage type of the iterates and coefficients and the arithmetic type.
+//
+// visn of component COMP at point c (solu_sor4.f:150-170 without the A/B factors)
+template <int COMP, class T>
+__device__ __forceinline__ T visn_at(const Grid& g, const VP& p, long c, const T* __restrict__ mu,
+                                     const T* __restrict__ exy, const T* __restrict__ exz,
+                                     const T* __restrict__ eyz, const T* un, const T* vn, const T* wn) {
   const long X = 1, Y = g.sy, Z = g.sz;
-  const R dx2 = (R)p.dx2, dy2 = (R)p.dy2, dz2 = (R)p.dz2, dxy = (R)p.dxy, dxz = (R)p.dxz, dyz = (R)p.dyz;
-  double e = 0.0;
+  const T dx2 = (T)p.dx2, dy2 = (T)p.dy2, dz2 = (T)p.dz2, dxy = (T)p.dxy, dxz = (T)p.dxz, dyz = (T)p.dyz;
+  auto U = [&](long o) { return un[c + o]; };
+  auto V = [&](long o) { return vn[c + o]; };
+  auto W = [&](long o) { return wn[c + o]; };
+  auto M = [&](const T* a, long o) { return __ldg(a + c + o); };
+  if (COMP == 0) {
+    const T ym = M(exy, -Y), yp = M(exy, 0), zm = M(exz, -Z), zp = M(exz, 0);
+    return dz2 * (zm * U(-Z) + zp * U(Z)) + dy2 * (ym * U(-Y) + yp * U(Y)) +
+           (T)2 * dx2 * (M(mu, 0) * U(-X) + M(mu, X) * U(X)) + dxy * (ym * (V(-Y) - V(X - Y)) + yp * (V(X) - V(0))) +
+           dxz * (zm * (W(-Z) - W(X - Z)) + zp * (W(X) - W(0)));
+  } else if (COMP == 1) {
+    const T xm = M(exy, -X), xp = M(exy, 0), zm = M(eyz, -Z), zp = M(eyz, 0);
+    return dz2 * (zm * V(-Z) + zp * V(Z)) + (T)2 * dy2 * (M(mu, 0) * V(-Y) + M(mu, Y) * V(Y)) +
+           dx2 * (xm * V(-X) + xp * V(X)) + dxy * (xm * (U(-X) - U(-X + Y)) + xp * (U(Y) - U(0))) +
+           dyz * (zm * (W(-Z) - W(Y - Z)) + zp * (W(Y) - W(0)));
+  } else {
+    const T xm = M(exz, -X), xp = M(exz, 0), ym = M(eyz, -Y), yp = M(eyz, 0);
+    return (T)2 * dz2 * (M(mu, 0) * W(-Z) + M(mu, Z) * W(Z)) + dy2 * (ym * W(-Y) + yp * W(Y)) +
+           dx2 * (xm * W(-X) + xp * W(X)) + dxz * (xm * (U(-X) - U(-X + Z)) + xp * (U(Z) - U(0))) +
+           dyz * (ym * (V(-Y) - V(-Y + Z)) + yp * (V(Z) - V(0)));
+  }
+}
+
+// T = double: the FP64 step, q_new = A*visn(q) + B on the velocity itself.
+// T = float: the mixed-precision step, d_new = A*visn(d) + R on the correction
+// d = un - u (R is the FP64 first-sweep residual; see refine_prep).
+// part[block] = the block's sum of (q_new - q)^2.
+template <int COMP, class T>
+__global__ void __launch_bounds__(256) k_pair(Grid g, VP p, int pi, int pj, int pk, const T* __restrict__ mu,
+                                              const T* __restrict__ exy, const T* __restrict__ exz,
+                                              const T* __restrict__ eyz, const T* __restrict__ A,
+                                              const T* __restrict__ B, T* un, T* vn, T* wn,
+                                              double* __restrict__ part) {
+  __shared__ T sh[8];
+  const int jmax = COMP == 1 ? g.nj - 1 : g.nj;
+  T* q = COMP == 0 ? un : (COMP == 1 ? vn : wn);
+  T e = 0;
 #pragma unroll
   for (int h = 0; h < 2; ++h) {
     const int i = (h ? 3 - pi : pi) + 2 * (int)(blockIdx.x * 32 + threadIdx.x);
@@ -158,45 +187,20 @@ __global__ void __launch_bounds__(256) k_pair(Grid g, VP p, int pi, int pj, int 
     const int k = (h ? 3 - pk : pk) + 2 * (int)blockIdx.z;
     if (i > g.ni || j > jmax || k > g.nk) continue;
     const long c = g.at(i, j, k);
-    auto U = [&](long o) { return (R)un[c + o]; };
-    auto V = [&](long o) { return (R)vn[c + o]; };
-    auto W = [&](long o) { return (R)wn[c + o]; };
-    auto M = [&](const double* a, long o) { return (R)__ldg(a + c + o); };
-    R visn;
-    double q;
-    if (COMP == 0) {
-      const R ym = M(exy, -Y), yp = M(exy, 0), zm = M(exz, -Z), zp = M(exz, 0);
-      visn = dz2 * (zm * U(-Z) + zp * U(Z)) + dy2 * (ym * U(-Y) + yp * U(Y)) +
-             (R)2 * dx2 * (M(mu, 0) * U(-X) + M(mu, X) * U(X)) + dxy * (ym * (V(-Y) - V(X - Y)) + yp * (V(X) - V(0))) +
-             dxz * (zm * (W(-Z) - W(X - Z)) + zp * (W(X) - W(0)));
-      q = un[c];
-    } else if (COMP == 1) {
-      const R xm = M(exy, -X), xp = M(exy, 0), zm = M(eyz, -Z), zp = M(eyz, 0);
-      visn = dz2 * (zm * V(-Z) + zp * V(Z)) + (R)2 * dy2 * (M(mu, 0) * V(-Y) + M(mu, Y) * V(Y)) +
-             dx2 * (xm * V(-X) + xp * V(X)) + dxy * (xm * (U(-X) - U(-X + Y)) + xp * (U(Y) - U(0))) +
-             dyz * (zm * (W(-Z) - W(Y - Z)) + zp * (W(Y) - W(0)));
-      q = vn[c];
-    } else {
-      const R xm = M(exz, -X), xp = M(exz, 0), ym = M(eyz, -Y), yp = M(eyz, 0);
-      visn = (R)2 * dz2 * (M(mu, 0) * W(-Z) + M(mu, Z) * W(Z)) + dy2 * (ym * W(-Y) + yp * W(Y)) +
-             dx2 * (xm * W(-X) + xp * W(X)) + dxz * (xm * (U(-X) - U(-X + Z)) + xp * (U(Z) - U(0))) +
-             dyz * (ym * (V(-Y) - V(-Y + Z)) + yp * (V(Z) - V(0)));
-      q = wn[c];
-    }
-    const double qn = (double)(M(A, 0) * visn + M(B, 0));
-    const double d = qn - q;
-    if (COMP == 0) un[c] = qn;
-    else if (COMP == 1) vn[c] = qn;
-    else wn[c] = qn;
+    const T visn = visn_at<COMP, T>(g, p, c, mu, exy, exz, eyz, un, vn, wn);
+    const T qn = __ldg(A + c) * visn + __ldg(B + c);
+    const T d = qn - q[c];
+    q[c] = qn;
     e += d * d;
   }
-  sh[tid] = e;
+  for (int o = 16; o > 0; o >>= 1) e += __shfl_down_sync(0xffffffffu, e, o);
+  if (threadIdx.x == 0) sh[threadIdx.y] = e;
   __syncthreads();
-  for (int st = 128; st > 0; st >>= 1) {
-    if (tid < st) sh[tid] += sh[tid + st];
-    __syncthreads();
+  if (threadIdx.y == 0 && threadIdx.x == 0) {
+    T t = 0;
+    for (int w = 0; w < 8; ++w) t += sh[w];
+    part[((long)blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x] = (double)t;
   }
-  if (tid == 0) part[((long)blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x] = sh[0];
 }
 
 // --- wall/halo refresh: bndu(un,vn,wn) then bnd_periodic(swept component) ----------
@@ -218,8 +222,13 @@ __global__ void __launch_bounds__(256) k_wall_coef(Grid g, double dy, const doub
   wc[o] = (2.0 * dy) / (2.0 * ls + dy);
   wc[o + 1] = (2.0 * ls - dy) / (2.0 * ls + dy);
 }
-__global__ void __launch_bounds__(256) k_wall(Grid g, double uwall, const double* __restrict__ wc, double* uk,
-                                              double* vk, double* wk) {
+// The three refresh kernels issue every load of a thread before its first store: in
+// each of them the points written and the points read are disjoint (ghost rows are
+// written from interior rows; halo copies read rows the same kernel never writes),
+// so this is the sequential result with one memory round trip per thread.
+__global__ void __launch_bounds__(256) k_wall(Grid g, double uwall, const double* __restrict__ wc,
+                                              double* __restrict__ uk, double* __restrict__ vk,
+                                              double* __restrict__ wk) {
   const int i = -2 + (int)(blockIdx.x * blockDim.x + threadIdx.x);
   const int kk = -2 + (int)(blockIdx.y * blockDim.y + threadIdx.y);
   if (i > g.ni + 3 || kk > 2 * (g.nk + 6) - 3) return;
@@ -231,16 +240,15 @@ __global__ void __launch_bounds__(256) k_wall(Grid g, double uwall, const double
   const long Y = g.sy;
   if (!side) {
     const long c = g.at(i, 1, k);
-    const double u1 = uk[c];
+    const double u1 = uk[c], v1 = vk[c], v2 = vk[c + Y], w1 = wk[c];
     const double u0 = c1 * (-uwall) + c2 * u1;
     const double um1 = 2.0 * u0 - u1;
     uk[c - Y] = u0;
     uk[c - 2 * Y] = um1;
     uk[c - 3 * Y] = 2.0 * um1 - u0;
-    vk[c - 3 * Y] = -vk[c + Y];
-    vk[c - 2 * Y] = -vk[c];
+    vk[c - 3 * Y] = -v2;
+    vk[c - 2 * Y] = -v1;
     vk[c - Y] = 0.0;
-    const double w1 = wk[c];
     const double w0 = c2 * w1;
     const double wm1 = 2.0 * w0 - w1;
     wk[c - Y] = w0;
@@ -248,18 +256,17 @@ __global__ void __launch_bounds__(256) k_wall(Grid g, double uwall, const double
     wk[c - 3 * Y] = 2.0 * wm1 - w0;
   } else {
     const long c = g.at(i, NJ, k);
-    const double u1 = uk[c];
+    const double u1 = uk[c], w1 = wk[c];
+    const double vm1 = vk[c - Y], vm2 = vk[c - 2 * Y], vm3 = vk[c - 3 * Y];
     const double u0 = c1 * uwall + c2 * u1;
     const double up2 = 2.0 * u0 - u1;
     uk[c + Y] = u0;
     uk[c + 2 * Y] = up2;
     uk[c + 3 * Y] = 2.0 * up2 - u0;
-    const double vm1 = vk[c - Y], vm2 = vk[c - 2 * Y], vm3 = vk[c - 3 * Y];
     vk[c] = 0.0;
     vk[c + Y] = -vm1;
     vk[c + 2 * Y] = -vm2;
     vk[c + 3 * Y] = -vm3;
-    const double w1 = wk[c];
     const double w0 = c2 * w1;
     const double wp2 = 2.0 * w0 - w1;
     wk[c + Y] = w0;
@@ -270,34 +277,43 @@ __global__ void __launch_bounds__(256) k_wall(Grid g, double uwall, const double
 // x halos of all three components.  Bit c of `normal` set: component c gets the
 // plain periodic copy (bnd_periodic applied after bndu overwrites bndu's halos);
 // clear: bndu's copy, which for u is shifted by one (bndu.f:107-109).
-__global__ void __launch_bounds__(256) k_halo_x(Grid g, int normal, double* uk, double* vk, double* wk) {
+__global__ void __launch_bounds__(256) k_halo_x(Grid g, int normal, double* __restrict__ uk,
+                                                double* __restrict__ vk, double* __restrict__ wk) {
   const int j = -2 + (int)(blockIdx.x * blockDim.x + threadIdx.x);
   const int k = -2 + (int)(blockIdx.y * blockDim.y + threadIdx.y);
   if (j > g.nj + 3 || k > g.nk + 3) return;
   const int NI = g.ni;
   const long r = g.at(0, j, k);
   double* q[3] = {uk, vk, wk};
+  const bool shifted = !(normal & 1);
+  // sources of the destinations -2, -1, 0, ni+1, ni+2, ni+3 (offsets from r);
+  // bndu's u: u(0)=u(ni+1), u(-1)=u(ni), u(-2)=u(ni-1), u(ni+1) untouched
+  double t[3][6];
+#pragma unroll
+  for (int cmp = 0; cmp < 3; ++cmp) {
+    const double* a = q[cmp];
+    const int sh = (cmp == 0 && shifted) ? 1 : 0;
+    t[cmp][0] = a[r + NI - 2 + sh];
+    t[cmp][1] = a[r + NI - 1 + sh];
+    t[cmp][2] = a[r + NI + sh];
+    t[cmp][3] = sh ? 0.0 : a[r + 1];
+    t[cmp][4] = a[r + 2];
+    t[cmp][5] = a[r + 3];
+  }
 #pragma unroll
   for (int cmp = 0; cmp < 3; ++cmp) {
     double* a = q[cmp];
-    if (cmp == 0 && !(normal & 1)) {  // bndu's u: u(0)=u(ni+1), u(-1)=u(ni), u(-2)=u(ni-1), u(ni+1) untouched
-      a[r] = a[r + NI + 1];
-      a[r - 1] = a[r + NI];
-      a[r - 2] = a[r + NI - 1];
-      a[r + NI + 2] = a[r + 2];
-      a[r + NI + 3] = a[r + 3];
-    } else {
-      a[r - 2] = a[r + NI - 2];
-      a[r - 1] = a[r + NI - 1];
-      a[r] = a[r + NI];
-      a[r + NI + 1] = a[r + 1];
-      a[r + NI + 2] = a[r + 2];
-      a[r + NI + 3] = a[r + 3];
-    }
+    a[r - 2] = t[cmp][0];
+    a[r - 1] = t[cmp][1];
+    a[r] = t[cmp][2];
+    if (!(cmp == 0 && shifted)) a[r + NI + 1] = t[cmp][3];
+    a[r + NI + 2] = t[cmp][4];
+    a[r + NI + 3] = t[cmp][5];
   }
 }
 // z halos; for w bndu's copy is shifted by one (bndu.f:144-146).
-__global__ void __launch_bounds__(256) k_halo_z(Grid g, int normal, double* uk, double* vk, double* wk) {
+__global__ void __launch_bounds__(256) k_halo_z(Grid g, int normal, double* __restrict__ uk,
+                                                double* __restrict__ vk, double* __restrict__ wk) {
   const int i = -2 + (int)(blockIdx.x * blockDim.x + threadIdx.x);
   const int j = -2 + (int)(blockIdx.y * blockDim.y + threadIdx.y);
   if (i > g.ni + 3 || j > g.nj + 3) return;
@@ -305,25 +321,278 @@ __global__ void __launch_bounds__(256) k_halo_z(Grid g, int normal, double* uk, 
   const long Z = g.sz;
   const long r = g.at(i, j, 0);
   double* q[3] = {uk, vk, wk};
+  const bool shifted = !(normal & 4);
+  // bndu's w: w(0)=w(nk+1), w(-1)=w(nk), w(-2)=w(nk-1), w(nk+1) untouched
+  double t[3][6];
+#pragma unroll
+  for (int cmp = 0; cmp < 3; ++cmp) {
+    const double* a = q[cmp];
+    const int sh = (cmp == 2 && shifted) ? 1 : 0;
+    t[cmp][0] = a[r + (NK - 2 + sh) * Z];
+    t[cmp][1] = a[r + (NK - 1 + sh) * Z];
+    t[cmp][2] = a[r + (NK + sh) * Z];
+    t[cmp][3] = sh ? 0.0 : a[r + Z];
+    t[cmp][4] = a[r + 2 * Z];
+    t[cmp][5] = a[r + 3 * Z];
+  }
 #pragma unroll
   for (int cmp = 0; cmp < 3; ++cmp) {
     double* a = q[cmp];
-    if (cmp == 2 && !(normal & 4)) {  // bndu's w: w(0)=w(nk+1), ..., w(nk+1) untouched
-      a[r] = a[r + (NK + 1) * Z];
-      a[r - Z] = a[r + NK * Z];
-      a[r - 2 * Z] = a[r + (NK - 1) * Z];
-      a[r + (NK + 2) * Z] = a[r + 2 * Z];
-      a[r + (NK + 3) * Z] = a[r + 3 * Z];
+    a[r - 2 * Z] = t[cmp][0];
+    a[r - Z] = t[cmp][1];
+    a[r] = t[cmp][2];
+    if (!(cmp == 2 && shifted)) a[r + (NK + 1) * Z] = t[cmp][3];
+    a[r + (NK + 2) * Z] = t[cmp][4];
+    a[r + (NK + 3) * Z] = t[cmp][5];
+  }
+}
+// --- mixed precision: FP32 sweeps on the correction d = un - u ---------------------
+// During the solve un = u + d holds at every point, halos and wall ghosts included:
+// d starts at zero (un = u, main.f90:605-607) and every operation on un has an
+// exact counterpart on d.  A sweep q_new = A*visn(q) + B becomes d_new = A*visn(d) + R
+// with R = A*visn(u) + B - u; each wall/halo operation dst = f(src) is affine with
+// fixed coefficients, so it becomes d_dst = f_lin(d_src) + gamma_dst with
+// gamma_dst = f(u_src) - u_dst, formed once per step in FP64 from u.
+//
+// Wall constants per (side, k, i), 12 floats: c2, gamma_u[3], gamma_v[4], gamma_w[3], pad.
+constexpr int kGW = 12;
+// x-halo constants per (j, k) and z-halo constants per (i, j), 24 floats: the six
+// destinations of the plain copy of u, v, w and the five of bndu's shifted copy
+// (u in x: slots 6..10, v 12..17, w 18..23; z: u 0..5, v 6..11, w 12..17, shifted w 18..22).
+constexpr int kGH = 24;
+
+__device__ __forceinline__ long wall_slot(const Grid& g, int side, int k, int i) {
+  return (((long)side * (g.nk + 6) + (k + 2)) * (g.ni + 6) + (i + 2));
+}
+
+__global__ void __launch_bounds__(256) k_gamma_wall(Grid g, double uwall, const double* __restrict__ wc,
+                                                    const double* __restrict__ u, const double* __restrict__ v,
+                                                    const double* __restrict__ w, float* __restrict__ gw) {
+  const int i = -2 + (int)(blockIdx.x * blockDim.x + threadIdx.x);
+  const int kk = -2 + (int)(blockIdx.y * blockDim.y + threadIdx.y);
+  if (i > g.ni + 3 || kk > 2 * (g.nk + 6) - 3) return;
+  const int side = kk >= g.nk + 4 ? 1 : 0;
+  const int k = side ? kk - (g.nk + 6) : kk;
+  const long o = wall_slot(g, side, k, i);
+  const double c1 = wc[2 * o], c2 = wc[2 * o + 1];
+  const long Y = g.sy;
+  const long c = g.at(i, side ? g.nj : 1, k);
+  const long t = side ? Y : -Y;  // towards the ghost rows
+  float* G = gw + o * kGW;
+  // u, w: q(g1) = K + c2 q(c), q(g2) = 2 q(g1) - q(c), q(g3) = 2 q(g2) - q(g1)
+  auto lin = [&](const double* q, double K, float* out) {
+    const double q1 = q[c], g1 = q[c + t], g2 = q[c + 2 * t], g3 = q[c + 3 * t];
+    out[0] = (float)(K + c2 * q1 - g1);
+    out[1] = (float)(2.0 * g1 - q1 - g2);
+    out[2] = (float)(2.0 * g2 - g1 - g3);
+  };
+  G[0] = (float)c2;
+  lin(u, side ? c1 * uwall : c1 * (-uwall), G + 1);
+  lin(w, 0.0, G + 8);
+  if (!side) {  // v(0) = 0, v(-1) = -v(1), v(-2) = -v(2)
+    G[4] = (float)(-v[c - Y]);
+    G[5] = (float)(-v[c] - v[c - 2 * Y]);
+    G[6] = (float)(-v[c + Y] - v[c - 3 * Y]);
+    G[7] = 0.f;
+  } else {  // v(nj) = 0, v(nj+m) = -v(nj-m), m = 1..3
+    G[4] = (float)(-v[c]);
+    G[5] = (float)(-v[c - Y] - v[c + Y]);
+    G[6] = (float)(-v[c - 2 * Y] - v[c + 2 * Y]);
+    G[7] = (float)(-v[c - 3 * Y] - v[c + 3 * Y]);
+  }
+  G[11] = 0.f;
+}
+__global__ void __launch_bounds__(256) k_gamma_x(Grid g, const double* __restrict__ u, const double* __restrict__ v,
+                                                 const double* __restrict__ w, float* __restrict__ gx) {
+  const int j = -2 + (int)(blockIdx.x * blockDim.x + threadIdx.x);
+  const int k = -2 + (int)(blockIdx.y * blockDim.y + threadIdx.y);
+  if (j > g.nj + 3 || k > g.nk + 3) return;
+  const int NI = g.ni;
+  const long r = g.at(0, j, k);
+  float* G = gx + ((long)(k + 2) * (g.nj + 6) + (j + 2)) * kGH;
+  const int dst[6] = {-2, -1, 0, NI + 1, NI + 2, NI + 3};
+  const int src[6] = {NI - 2, NI - 1, NI, 1, 2, 3};
+  const double* q[3] = {u, v, w};
+  const int base[3] = {0, 12, 18};
+  for (int cmp = 0; cmp < 3; ++cmp)
+    for (int t = 0; t < 6; ++t) G[base[cmp] + t] = (float)(q[cmp][r + src[t]] - q[cmp][r + dst[t]]);
+  // bndu's u: destinations -2, -1, 0, ni+2, ni+3 from ni-1, ni, ni+1, 2, 3
+  const int sd[5] = {-2, -1, 0, NI + 2, NI + 3};
+  const int ss[5] = {NI - 1, NI, NI + 1, 2, 3};
+  for (int t = 0; t < 5; ++t) G[6 + t] = (float)(u[r + ss[t]] - u[r + sd[t]]);
+  G[11] = 0.f;
+}
+__global__ void __launch_bounds__(256) k_gamma_z(Grid g, const double* __restrict__ u, const double* __restrict__ v,
+                                                 const double* __restrict__ w, float* __restrict__ gz) {
+  const int i = -2 + (int)(blockIdx.x * blockDim.x + threadIdx.x);
+  const int j = -2 + (int)(blockIdx.y * blockDim.y + threadIdx.y);
+  if (i > g.ni + 3 || j > g.nj + 3) return;
+  const int NK = g.nk;
+  const long Z = g.sz;
+  const long r = g.at(i, j, 0);
+  float* G = gz + ((long)(j + 2) * (g.ni + 6) + (i + 2)) * kGH;
+  const int dst[6] = {-2, -1, 0, NK + 1, NK + 2, NK + 3};
+  const int src[6] = {NK - 2, NK - 1, NK, 1, 2, 3};
+  const double* q[3] = {u, v, w};
+  for (int cmp = 0; cmp < 3; ++cmp)
+    for (int t = 0; t < 6; ++t) G[6 * cmp + t] = (float)(q[cmp][r + src[t] * Z] - q[cmp][r + dst[t] * Z]);
+  const int sd[5] = {-2, -1, 0, NK + 2, NK + 3};
+  const int ss[5] = {NK - 1, NK, NK + 1, 2, 3};
+  for (int t = 0; t < 5; ++t) G[18 + t] = (float)(w[r + ss[t] * Z] - w[r + sd[t] * Z]);
+  G[23] = 0.f;
+}
+
+// k_wall on the corrections
+__global__ void __launch_bounds__(256) k_wall_d(Grid g, const float* __restrict__ gw, float* __restrict__ du,
+                                                float* __restrict__ dv, float* __restrict__ dw) {
+  const int i = -2 + (int)(blockIdx.x * blockDim.x + threadIdx.x);
+  const int kk = -2 + (int)(blockIdx.y * blockDim.y + threadIdx.y);
+  if (i > g.ni + 3 || kk > 2 * (g.nk + 6) - 3) return;
+  const int side = kk >= g.nk + 4 ? 1 : 0;
+  const int k = side ? kk - (g.nk + 6) : kk;
+  const float4* G4 = reinterpret_cast<const float4*>(gw + wall_slot(g, side, k, i) * kGW);
+  const float4 a = __ldg(G4), b = __ldg(G4 + 1), e = __ldg(G4 + 2);
+  const float c2 = a.x;
+  const long Y = g.sy;
+  const long c = g.at(i, side ? g.nj : 1, k);
+  const long t = side ? Y : -Y;
+  const float u1 = du[c], w1 = dw[c];
+  float v1, v2, v3;
+  if (!side) {
+    v1 = dv[c];
+    v2 = dv[c + Y];
+    v3 = 0.f;
+  } else {
+    v1 = dv[c - Y];
+    v2 = dv[c - 2 * Y];
+    v3 = dv[c - 3 * Y];
+  }
+  const float ug1 = c2 * u1 + a.y, ug2 = 2.f * ug1 - u1 + a.z, ug3 = 2.f * ug2 - ug1 + a.w;
+  du[c + t] = ug1;
+  du[c + 2 * t] = ug2;
+  du[c + 3 * t] = ug3;
+  const float wg1 = c2 * w1 + e.x, wg2 = 2.f * wg1 - w1 + e.y, wg3 = 2.f * wg2 - wg1 + e.z;
+  dw[c + t] = wg1;
+  dw[c + 2 * t] = wg2;
+  dw[c + 3 * t] = wg3;
+  if (!side) {
+    dv[c - Y] = b.x;
+    dv[c - 2 * Y] = -v1 + b.y;
+    dv[c - 3 * Y] = -v2 + b.z;
+  } else {
+    dv[c] = b.x;
+    dv[c + Y] = -v1 + b.y;
+    dv[c + 2 * Y] = -v2 + b.z;
+    dv[c + 3 * Y] = -v3 + b.w;
+  }
+}
+// k_halo_x on the corrections
+__global__ void __launch_bounds__(256) k_halo_x_d(Grid g, int normal, const float* __restrict__ gx,
+                                                  float* __restrict__ du, float* __restrict__ dv,
+                                                  float* __restrict__ dw) {
+  const int j = -2 + (int)(blockIdx.x * blockDim.x + threadIdx.x);
+  const int k = -2 + (int)(blockIdx.y * blockDim.y + threadIdx.y);
+  if (j > g.nj + 3 || k > g.nk + 3) return;
+  const int NI = g.ni;
+  const long r = g.at(0, j, k);
+  const float* G = gx + ((long)(k + 2) * (g.nj + 6) + (j + 2)) * kGH;
+  float* q[3] = {du, dv, dw};
+  const bool shifted = !(normal & 1);
+  float t[3][6];
+#pragma unroll
+  for (int cmp = 0; cmp < 3; ++cmp) {
+    const float* a = q[cmp];
+    const int sh = (cmp == 0 && shifted) ? 1 : 0;
+    t[cmp][0] = a[r + NI - 2 + sh];
+    t[cmp][1] = a[r + NI - 1 + sh];
+    t[cmp][2] = a[r + NI + sh];
+    t[cmp][3] = sh ? 0.f : a[r + 1];
+    t[cmp][4] = a[r + 2];
+    t[cmp][5] = a[r + 3];
+  }
+#pragma unroll
+  for (int cmp = 0; cmp < 3; ++cmp) {
+    float* a = q[cmp];
+    if (cmp == 0 && shifted) {
+      const float* s = G + 6;
+      a[r - 2] = t[0][0] + __ldg(s);
+      a[r - 1] = t[0][1] + __ldg(s + 1);
+      a[r] = t[0][2] + __ldg(s + 2);
+      a[r + NI + 2] = t[0][4] + __ldg(s + 3);
+      a[r + NI + 3] = t[0][5] + __ldg(s + 4);
     } else {
-      a[r - 2 * Z] = a[r + (NK - 2) * Z];
-      a[r - Z] = a[r + (NK - 1) * Z];
-      a[r] = a[r + NK * Z];
-      a[r + (NK + 1) * Z] = a[r + Z];
-      a[r + (NK + 2) * Z] = a[r + 2 * Z];
-      a[r + (NK + 3) * Z] = a[r + 3 * Z];
+      const float* s = G + (cmp == 0 ? 0 : (cmp == 1 ? 12 : 18));
+      a[r - 2] = t[cmp][0] + __ldg(s);
+      a[r - 1] = t[cmp][1] + __ldg(s + 1);
+      a[r] = t[cmp][2] + __ldg(s + 2);
+      a[r + NI + 1] = t[cmp][3] + __ldg(s + 3);
+      a[r + NI + 2] = t[cmp][4] + __ldg(s + 4);
+      a[r + NI + 3] = t[cmp][5] + __ldg(s + 5);
     }
   }
 }
+// k_halo_z on the corrections
+__global__ void __launch_bounds__(256) k_halo_z_d(Grid g, int normal, const float* __restrict__ gz,
+                                                  float* __restrict__ du, float* __restrict__ dv,
+                                                  float* __restrict__ dw) {
+  const int i = -2 + (int)(blockIdx.x * blockDim.x + threadIdx.x);
+  const int j = -2 + (int)(blockIdx.y * blockDim.y + threadIdx.y);
+  if (i > g.ni + 3 || j > g.nj + 3) return;
+  const int NK = g.nk;
+  const long Z = g.sz;
+  const long r = g.at(i, j, 0);
+  const float* G = gz + ((long)(j + 2) * (g.ni + 6) + (i + 2)) * kGH;
+  float* q[3] = {du, dv, dw};
+  const bool shifted = !(normal & 4);
+  float t[3][6];
+#pragma unroll
+  for (int cmp = 0; cmp < 3; ++cmp) {
+    const float* a = q[cmp];
+    const int sh = (cmp == 2 && shifted) ? 1 : 0;
+    t[cmp][0] = a[r + (NK - 2 + sh) * Z];
+    t[cmp][1] = a[r + (NK - 1 + sh) * Z];
+    t[cmp][2] = a[r + (NK + sh) * Z];
+    t[cmp][3] = sh ? 0.f : a[r + Z];
+    t[cmp][4] = a[r + 2 * Z];
+    t[cmp][5] = a[r + 3 * Z];
+  }
+#pragma unroll
+  for (int cmp = 0; cmp < 3; ++cmp) {
+    float* a = q[cmp];
+    if (cmp == 2 && shifted) {
+      const float* s = G + 18;
+      a[r - 2 * Z] = t[2][0] + __ldg(s);
+      a[r - Z] = t[2][1] + __ldg(s + 1);
+      a[r] = t[2][2] + __ldg(s + 2);
+      a[r + (NK + 2) * Z] = t[2][4] + __ldg(s + 3);
+      a[r + (NK + 3) * Z] = t[2][5] + __ldg(s + 4);
+    } else {
+      const float* s = G + 6 * cmp;
+      a[r - 2 * Z] = t[cmp][0] + __ldg(s);
+      a[r - Z] = t[cmp][1] + __ldg(s + 1);
+      a[r] = t[cmp][2] + __ldg(s + 2);
+      a[r + (NK + 1) * Z] = t[cmp][3] + __ldg(s + 3);
+      a[r + (NK + 2) * Z] = t[cmp][4] + __ldg(s + 4);
+      a[r + (NK + 3) * Z] = t[cmp][5] + __ldg(s + 5);
+    }
+  }
+}
+__global__ void k_to_float(long n, const double* __restrict__ a, float* __restrict__ b) {
+  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x)
+    b[t] = (float)a[t];
+}
+// un = u + du, vn = v + dv, wn = w + dw at every point
+__global__ void k_refine_finish(long n, const double* __restrict__ u, const double* __restrict__ v,
+                                const double* __restrict__ w, const float* __restrict__ du,
+                                const float* __restrict__ dv, const float* __restrict__ dw, double* __restrict__ un,
+                                double* __restrict__ vn, double* __restrict__ wn) {
+  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) {
+    un[t] = u[t] + (double)du[t];
+    vn[t] = v[t] + (double)dv[t];
+    wn[t] = w[t] + (double)dw[t];
+  }
+}
+
 __global__ void k_sum_parts2(const double* part, long n, double* out) {
   __shared__ double sh[256];
   double a = 0.0;
@@ -336,13 +605,10 @@ __global__ void k_sum_parts2(const double* part, long n, double* out) {
   }
   if (threadIdx.x == 0) out[0] = sh[0];
 }
-}  // namespace
 
-void visc_prep(cudaStream_t s, const Grid& g, double dxinv, double dyinv, double dzinv, double dt, int harmonic,
-               const double* mu, const double* rho, const double* rhon, const double* const* src, double* const* E,
-               double* const* AB, const double* l1, const double* l2, const double* phi, double dy, double* wallc) {
+VP make_vp(double dxinv, double dyinv, double dzinv, double dt, int harmonic) {
   VP p;
-  p.dtinv = 1.0 / dt;
+  p.dtinv = dt > 0.0 ? 1.0 / dt : 0.0;
   p.dx2 = dxinv * dxinv;
   p.dy2 = dyinv * dyinv;
   p.dz2 = dzinv * dzinv;
@@ -350,29 +616,25 @@ void visc_prep(cudaStream_t s, const Grid& g, double dxinv, double dyinv, double
   p.dxz = dxinv * dzinv;
   p.dyz = dyinv * dzinv;
   p.harmonic = harmonic;
-  dim3 b(32, 8, 1);
-  k_edges<<<dim3((g.ni + 1 + 31) / 32, (g.nj + 1 + 7) / 8, g.nk + 1), b, 0, s>>>(g, p, mu, E[0], E[1], E[2]);
-  k_ab<<<dim3((g.ni + 31) / 32, (g.nj + 7) / 8, g.nk), b, 0, s>>>(g, p, mu, E[0], E[1], E[2], rho, rhon, src[0], src[1],
-                                                                 src[2], AB[0], AB[1], AB[2], AB[3], AB[4], AB[5]);
-  k_wall_coef<<<dim3((g.ni + 6 + 31) / 32, (2 * (g.nk + 6) + 7) / 8), b, 0, s>>>(g, dy, l1, l2, phi, wallc);
-  count_launch(3);
+  return p;
 }
+const dim3 kB(32, 8, 1);
+dim3 wall_grid(const Grid& g) { return dim3((g.ni + 6 + 31) / 32, (2 * (g.nk + 6) + 7) / 8); }
+dim3 xh_grid(const Grid& g) { return dim3((g.nj + 6 + 31) / 32, (g.nk + 6 + 7) / 8); }
+dim3 zh_grid(const Grid& g) { return dim3((g.ni + 6 + 31) / 32, (g.nj + 6 + 7) / 8); }
+dim3 pair_grid(const Grid& g) {
+  return dim3((unsigned)((g.ni / 2 + 31) / 32), (unsigned)((g.nj / 2 + 7) / 8), (unsigned)(g.nk / 2));
+}
+// first colour of each pair (solu_sor4.f:94-120): (1,1,1) (1,1,2) (1,2,1) (2,1,1)
+const int kPi[4] = {1, 1, 1, 2}, kPj[4] = {1, 1, 2, 1}, kPk[4] = {1, 2, 1, 1};
 
-void src_visc_prep(cudaStream_t s, const Grid& g, double dxinv, double dyinv, double dzinv, double dt, int harmonic,
-                   double grvb, double grvp, const double* u, const double* v, const double* w,
-                   const double* const* adv, const double* const* advo, const double* const* prs,
-                   const double* const* vis, const double* const* fst, const double* const* fstn, const double* mu,
-                   const double* rho, const double* rhon, double* const* E, double* const* AB, const double* l1,
-                   const double* l2, const double* phi, double dy, double* wallc) {
-  VP p;
-  p.dtinv = 1.0 / dt;
-  p.dx2 = dxinv * dxinv;
-  p.dy2 = dyinv * dyinv;
-  p.dz2 = dzinv * dzinv;
-  p.dxy = dxinv * dyinv;
-  p.dxz = dxinv * dzinv;
-  p.dyz = dyinv * dzinv;
-  p.harmonic = harmonic;
+// k_edges + k_src_ab<REFINE> + k_wall_coef
+template <bool REFINE>
+void src_prep(cudaStream_t s, const Grid& g, const VP& p, const double* u, const double* v, const double* w,
+              const double* const* adv, const double* const* advo, const double* const* prs,
+              const double* const* vis, const double* const* fst, const double* const* fstn, double grvb,
+              double grvp, const double* mu, const double* rho, const double* rhon, double* const* E, F3 ef,
+              ABOut out, const double* l1, const double* l2, const double* phi, double dy, double* wallc) {
   SrcIn in;
   in.u = u;
   in.v = v;
@@ -389,61 +651,125 @@ void src_visc_prep(cudaStream_t s, const Grid& g, double dxinv, double dyinv, do
   }
   in.grvb = grvb;
   in.grvp = grvp;
-  dim3 b(32, 8, 1);
-  k_edges<<<dim3((g.ni + 1 + 31) / 32, (g.nj + 1 + 7) / 8, g.nk + 1), b, 0, s>>>(g, p, mu, E[0], E[1], E[2]);
-  k_src_ab<<<dim3((g.ni + 31) / 32, (g.nj + 7) / 8, g.nk), b, 0, s>>>(g, p, in, mu, E[0], E[1], E[2], AB[0], AB[1],
-                                                                     AB[2], AB[3], AB[4], AB[5]);
-  k_wall_coef<<<dim3((g.ni + 6 + 31) / 32, (2 * (g.nk + 6) + 7) / 8), b, 0, s>>>(g, dy, l1, l2, phi, wallc);
+  k_edges<<<dim3((g.ni + 1 + 31) / 32, (g.nj + 1 + 7) / 8, g.nk + 1), kB, 0, s>>>(g, p, mu, E[0], E[1], E[2], ef);
+  k_src_ab<REFINE><<<dim3((g.ni + 31) / 32, (g.nj + 7) / 8, g.nk), kB, 0, s>>>(g, p, in, mu, E[0], E[1], E[2], out);
+  k_wall_coef<<<wall_grid(g), kB, 0, s>>>(g, dy, l1, l2, phi, wallc);
   count_launch(3);
+}
+
+// The colour-pair sweeps of one outer iteration: per component 4 pairs, each
+// followed by the wall/halo refresh; then the residual sum into errsum[0].
+template <class T, class PairFn, class HaloFn>
+void sweep_all(cudaStream_t s, const Grid& g, double* part, double* errsum, PairFn pair, HaloFn halo) {
+  const long nb = (long)pair_grid(g).x * pair_grid(g).y * pair_grid(g).z;
+  for (int comp = 0; comp < 3; ++comp) {
+    for (int pr = 0; pr < 4; ++pr) {
+      pair(comp, pr, part + (long)(comp * 4 + pr) * nb);
+      count_launch();
+      halo(1 << comp);
+    }
+  }
+  k_sum_parts2<<<1, 256, 0, s>>>(part, nb * 12, errsum);
+  count_launch();
+}
+}  // namespace
+
+void src_visc_prep(cudaStream_t s, const Grid& g, double dxinv, double dyinv, double dzinv, double dt, int harmonic,
+                   double grvb, double grvp, const double* u, const double* v, const double* w,
+                   const double* const* adv, const double* const* advo, const double* const* prs,
+                   const double* const* vis, const double* const* fst, const double* const* fstn, const double* mu,
+                   const double* rho, const double* rhon, double* const* E, double* const* AB, const double* l1,
+                   const double* l2, const double* phi, double dy, double* wallc) {
+  ABOut out{};
+  for (int q = 0; q < 3; ++q) {
+    out.a[q] = AB[2 * q];
+    out.b[q] = AB[2 * q + 1];
+  }
+  src_prep<false>(s, g, make_vp(dxinv, dyinv, dzinv, dt, harmonic), u, v, w, adv, advo, prs, vis, fst, fstn, grvb,
+                  grvp, mu, rho, rhon, E, F3{{nullptr, nullptr, nullptr}}, out, l1, l2, phi, dy, wallc);
 }
 
 void wall_halo(cudaStream_t s, const Grid& g, int normal, double uwall, const double* wallc, double* un, double* vn,
                double* wn) {
-  dim3 b(32, 8, 1);
-  k_wall<<<dim3((g.ni + 6 + 31) / 32, (2 * (g.nk + 6) + 7) / 8), b, 0, s>>>(g, uwall, wallc, un, vn, wn);
-  k_halo_x<<<dim3((g.nj + 6 + 31) / 32, (g.nk + 6 + 7) / 8), b, 0, s>>>(g, normal, un, vn, wn);
-  k_halo_z<<<dim3((g.ni + 6 + 31) / 32, (g.nj + 6 + 7) / 8), b, 0, s>>>(g, normal, un, vn, wn);
+  k_wall<<<wall_grid(g), kB, 0, s>>>(g, uwall, wallc, un, vn, wn);
+  k_halo_x<<<xh_grid(g), kB, 0, s>>>(g, normal, un, vn, wn);
+  k_halo_z<<<zh_grid(g), kB, 0, s>>>(g, normal, un, vn, wn);
   count_launch(3);
 }
 
 void sor_iteration(cudaStream_t s, const Grid& g, double dxinv, double dyinv, double dzinv, int harmonic,
                    const double* mu, double* const* E, double* const* AB, double uwall, const double* wallc,
-                   double* un, double* vn, double* wn, double* part, double* errsum, bool fp32) {
-  VP p;
-  p.dtinv = 0.0;
-  p.dx2 = dxinv * dxinv;
-  p.dy2 = dyinv * dyinv;
-  p.dz2 = dzinv * dzinv;
-  p.dxy = dxinv * dyinv;
-  p.dxz = dxinv * dzinv;
-  p.dyz = dyinv * dzinv;
-  p.harmonic = harmonic;
-  // first colour of each pair (solu_sor4.f:94-120): (1,1,1) (1,1,2) (1,2,1) (2,1,1)
-  static const int pi_[4] = {1, 1, 1, 2}, pj_[4] = {1, 1, 2, 1}, pk_[4] = {1, 2, 1, 1};
-  const dim3 blk(32, 8, 1);
-  const dim3 grd((unsigned)((g.ni / 2 + 31) / 32), (unsigned)((g.nj / 2 + 7) / 8), (unsigned)(g.nk / 2));
-  const long nb = (long)grd.x * grd.y * grd.z;
-  for (int comp = 0; comp < 3; ++comp) {
-    for (int pr = 0; pr < 4; ++pr) {
-      double* pp = part + (long)(comp * 4 + pr) * nb;
-#define FMF_PAIR(C, R)                                                                                      \
-  k_pair<C, R><<<grd, blk, 0, s>>>(g, p, pi_[pr], pj_[pr], pk_[pr], mu, E[0], E[1], E[2], AB[2 * C], AB[2 * C + 1], \
-                                   un, vn, wn, pp)
-      if (fp32) {
-        if (comp == 0) FMF_PAIR(0, float);
-        else if (comp == 1) FMF_PAIR(1, float);
-        else FMF_PAIR(2, float);
-      } else {
-        if (comp == 0) FMF_PAIR(0, double);
-        else if (comp == 1) FMF_PAIR(1, double);
-        else FMF_PAIR(2, double);
-      }
+                   double* un, double* vn, double* wn, double* part, double* errsum) {
+  const VP p = make_vp(dxinv, dyinv, dzinv, 0.0, harmonic);
+  const dim3 grd = pair_grid(g);
+  sweep_all<double>(
+      s, g, part, errsum,
+      [&](int comp, int pr, double* pp) {
+#define FMF_PAIR(C) \
+  k_pair<C, double><<<grd, kB, 0, s>>>(g, p, kPi[pr], kPj[pr], kPk[pr], mu, E[0], E[1], E[2], AB[2 * C], AB[2 * C + 1], un, vn, wn, pp)
+        if (comp == 0) FMF_PAIR(0);
+        else if (comp == 1) FMF_PAIR(1);
+        else FMF_PAIR(2);
 #undef FMF_PAIR
-      count_launch();
-      wall_halo(s, g, 1 << comp, uwall, wallc, un, vn, wn);
-    }
+      },
+      [&](int normal) { wall_halo(s, g, normal, uwall, wallc, un, vn, wn); });
+}
+
+long refine_floats(const Grid& g, int part) {
+  switch (part) {
+    case 0: return 2L * (g.nk + 6) * (g.ni + 6) * kGW;
+    case 1: return (long)(g.nj + 6) * (g.nk + 6) * kGH;
+    default: return (long)(g.ni + 6) * (g.nj + 6) * kGH;
   }
-  k_sum_parts2<<<1, 256, 0, s>>>(part, nb * 12, errsum);
+}
+
+void refine_prep(cudaStream_t s, const Grid& g, double dxinv, double dyinv, double dzinv, double dt, int harmonic,
+                 double grvb, double grvp, const double* u, const double* v, const double* w,
+                 const double* const* adv, const double* const* advo, const double* const* prs,
+                 const double* const* vis, const double* const* fst, const double* const* fstn, const double* mu,
+                 const double* rho, const double* rhon, double* const* E, const double* l1, const double* l2,
+                 const double* phi, double dy, double uwall, double* wallc, const RefineBufs& rb) {
+  ABOut out{};
+  for (int q = 0; q < 3; ++q) {
+    out.af[q] = rb.a[q];
+    out.rf[q] = rb.r[q];
+  }
+  src_prep<true>(s, g, make_vp(dxinv, dyinv, dzinv, dt, harmonic), u, v, w, adv, advo, prs, vis, fst, fstn, grvb,
+                 grvp, mu, rho, rhon, E, F3{{rb.e[0], rb.e[1], rb.e[2]}}, out, l1, l2, phi, dy, wallc);
+  k_to_float<<<4 * 152, 256, 0, s>>>(g.n, mu, rb.mu);
+  k_gamma_wall<<<wall_grid(g), kB, 0, s>>>(g, uwall, wallc, u, v, w, rb.gw);
+  k_gamma_x<<<xh_grid(g), kB, 0, s>>>(g, u, v, w, rb.gx);
+  k_gamma_z<<<zh_grid(g), kB, 0, s>>>(g, u, v, w, rb.gz);
+  count_launch(4);
+  for (int q = 0; q < 3; ++q) FMF_CUDA(cudaMemsetAsync(rb.d[q], 0, sizeof(float) * g.n, s));
+}
+
+void sor_iteration_refine(cudaStream_t s, const Grid& g, double dxinv, double dyinv, double dzinv,
+                          const RefineBufs& rb, double* part, double* errsum) {
+  const VP p = make_vp(dxinv, dyinv, dzinv, 0.0, 0);
+  const dim3 grd = pair_grid(g);
+  float *du = rb.d[0], *dv = rb.d[1], *dw = rb.d[2];
+  sweep_all<float>(
+      s, g, part, errsum,
+      [&](int comp, int pr, double* pp) {
+#define FMF_PAIR(C) \
+  k_pair<C, float><<<grd, kB, 0, s>>>(g, p, kPi[pr], kPj[pr], kPk[pr], rb.mu, rb.e[0], rb.e[1], rb.e[2], rb.a[C], rb.r[C], du, dv, dw, pp)
+        if (comp == 0) FMF_PAIR(0);
+        else if (comp == 1) FMF_PAIR(1);
+        else FMF_PAIR(2);
+#undef FMF_PAIR
+      },
+      [&](int normal) {
+        k_wall_d<<<wall_grid(g), kB, 0, s>>>(g, rb.gw, du, dv, dw);
+        k_halo_x_d<<<xh_grid(g), kB, 0, s>>>(g, normal, rb.gx, du, dv, dw);
+        k_halo_z_d<<<zh_grid(g), kB, 0, s>>>(g, normal, rb.gz, du, dv, dw);
+        count_launch(3);
+      });
+}
+
+void refine_finish(cudaStream_t s, const Grid& g, const double* u, const double* v, const double* w,
+                   const RefineBufs& rb, double* un, double* vn, double* wn) {
+  k_refine_finish<<<4 * 152, 256, 0, s>>>(g.n, u, v, w, rb.d[0], rb.d[1], rb.d[2], un, vn, wn);
   count_launch();
 }
 

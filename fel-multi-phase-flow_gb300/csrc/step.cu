@@ -59,6 +59,8 @@ struct fmf_ctx {
   double *as_f, *an_f, *ap_f;
   double* red;  // small reduction outputs
   int* band;    // MTHINC band-cell list, then its length
+  bool mixed = false;        // precision == FMF_MIXED
+  fused::RefineBufs rb{};    // FP32 buffers of the mixed-precision viscous solve
   double* host_err = nullptr;  // pinned
   std::vector<int> sor_iters;
 };
@@ -75,7 +77,7 @@ double* alloc(fmf_ctx* c, long n) {
   c->bytes += (long long)sizeof(double) * n;
   return (double*)p;
 }
-const int kNID_free = -1;
+float* allocf(fmf_ctx* c, long n) { return (float*)alloc(c, (n + 1) / 2); }
 }  // namespace
 
 extern "C" {
@@ -131,6 +133,20 @@ int fmf_ctx_create(const fmf_params* prm, fmf_ctx** out) {
   c->an_f = alloc(c, prm->nj + 6);
   c->ap_f = alloc(c, prm->nj + 6);
   c->red = alloc(c, 64);
+  c->mixed = prm->precision == FMF_MIXED;
+  if (c->mixed) {
+    fused::RefineBufs& rb = c->rb;
+    for (int q = 0; q < 3; ++q) {
+      rb.d[q] = allocf(c, n);
+      rb.a[q] = allocf(c, n);
+      rb.r[q] = allocf(c, n);
+      rb.e[q] = allocf(c, n);
+    }
+    rb.mu = allocf(c, n);
+    rb.gw = allocf(c, fused::refine_floats(c->g, 0));
+    rb.gx = allocf(c, fused::refine_floats(c->g, 1));
+    rb.gz = allocf(c, fused::refine_floats(c->g, 2));
+  }
   {
     const long nb = (long)(prm->ni + 2) * (prm->nj + 2) * (prm->nk + 2) + 1;
     c->band = (int*)alloc(c, (nb + 1) / 2);
@@ -331,9 +347,11 @@ static void seg_pre(fmf_ctx* c) {
   op::cal_div_tensor(s, g, dxinv, dyinv, dzinv, c->tau, c->vis[0], c->vis[1], c->vis[2]);
   // :545-570 surface tension
   if (fused::csf_supported(g)) {
-    fused::csf_force(s, g, dxinv, dyinv, dzinv, P.rhol, P.rhog, P.sigma, phi1, c->sfst[0], c->sfst[1], c->sfst[2]);
+    const bool f32 = P.precision == FMF_MIXED;
+    fused::csf_force(s, g, dxinv, dyinv, dzinv, P.rhol, P.rhog, P.sigma, phi1, c->sfst[0], c->sfst[1], c->sfst[2],
+                     f32);
     fused::csf_force(s, g, dxinv, dyinv, dzinv, P.rhol, P.rhog, P.sigma, phin1, c->sfstn[0], c->sfstn[1],
-                     c->sfstn[2]);
+                     c->sfstn[2], f32);
   } else {
     csf_dropin(c, phi1, phin1);
   }
@@ -346,6 +364,14 @@ static void seg_pre(fmf_ctx* c) {
   const double* fstnp[3] = {c->sfstn[0], c->sfstn[1], c->sfstn[2]};
   // :579-603: cal_srcu and the coefficients (as edge viscosities) folded into the
   // per-point update factors of the viscous solve
+  if (c->mixed) {
+    // the FP64 residual at u and the wall/halo constants of the correction solve;
+    // un = u (:605-607) holds implicitly through zero corrections
+    fused::refine_prep(s, g, dxinv, dyinv, dzinv, dt, P.harmonic, P.grvb, P.grvp, c->u, c->v, c->w, advp, advop,
+                       prsp, visp, fstp, fstnp, c->rmun, c->rho, c->rhon, c->edge, c->l1, c->l2, phi1, P.dy, P.uwall,
+                       c->wallc, c->rb);
+    return;
+  }
   fused::src_visc_prep(s, g, dxinv, dyinv, dzinv, dt, P.harmonic, P.grvb, P.grvp, c->u, c->v, c->w, advp, advop,
                        prsp, visp, fstp, fstnp, c->rmun, c->rho, c->rhon, c->edge, c->ab, c->l1, c->l2, phi1, P.dy,
                        c->wallc);
@@ -388,8 +414,11 @@ static void csf_dropin(fmf_ctx* c, const double* phi1, const double* phin1) {
 static void seg_iter(fmf_ctx* c) {
   const fmf_params& P = c->prm;
   const double dxinv = 1.0 / P.dx, dyinv = 1.0 / P.dy, dzinv = 1.0 / P.dz;
-  fused::sor_iteration(c->s, c->g, dxinv, dyinv, dzinv, P.harmonic, c->rmun, c->edge, c->ab, P.uwall, c->wallc, c->un,
-                       c->vn, c->wn, c->sorpart, c->red + 8, P.precision == FMF_MIXED);
+  if (c->mixed)
+    fused::sor_iteration_refine(c->s, c->g, dxinv, dyinv, dzinv, c->rb, c->sorpart, c->red + 8);
+  else
+    fused::sor_iteration(c->s, c->g, dxinv, dyinv, dzinv, P.harmonic, c->rmun, c->edge, c->ab, P.uwall, c->wallc,
+                         c->un, c->vn, c->wn, c->sorpart, c->red + 8);
   FMF_CUDA(cudaMemcpyAsync(c->host_err, c->red + 8, sizeof(double), cudaMemcpyDeviceToHost, c->s));
 }
 
@@ -399,6 +428,7 @@ static void seg_post(fmf_ctx* c) {
   cudaStream_t s = c->s;
   const long n = g.n;
   const double dxinv = 1.0 / P.dx, dyinv = 1.0 / P.dy, dzinv = 1.0 / P.dz, dt = P.dt;
+  if (c->mixed) fused::refine_finish(s, g, c->u, c->v, c->w, c->rb, c->un, c->vn, c->wn);
   // :625-646
   fused::wall_halo(s, g, 7, P.uwall, c->wallc, c->un, c->vn, c->wn);
   op::caldiv(s, g, dxinv, dyinv, dzinv, dt, c->un, c->vn, c->wn, c->div, nullptr);
@@ -500,8 +530,11 @@ int fmf_ctx_time_stage(fmf_ctx* c, int stage, int reps, float* ms) {
         fused::weno5_both(s, g, dxinv, dyinv, dzinv, c->u, c->v, c->w, c->uo, c->vo, c->wo, c->adv, c->advo, mixed);
         break;
       case 1:
-        fused::sor_iteration(s, g, dxinv, dyinv, dzinv, P.harmonic, c->rmun, c->edge, c->ab, P.uwall, c->wallc,
-                             c->un, c->vn, c->wn, c->sorpart, c->red + 8, mixed);
+        if (mixed)
+          fused::sor_iteration_refine(s, g, dxinv, dyinv, dzinv, c->rb, c->sorpart, c->red + 8);
+        else
+          fused::sor_iteration(s, g, dxinv, dyinv, dzinv, P.harmonic, c->rmun, c->edge, c->ab, P.uwall, c->wallc,
+                               c->un, c->vn, c->wn, c->sorpart, c->red + 8);
         break;
       case 2:
         op::fft_forward_planes(s, g, c->div, c->pr, c->pi);
