@@ -1,0 +1,494 @@
+// adj_bc.cu -- adjoints of the boundary conditions, copies and linear stencils of
+// the step (k_bc.cu, k_glue.cu, k_press.cu, fused_visc.cu wall/halo kernels).
+#include "adj.cuh"
+
+namespace fmf {
+namespace adj {
+
+namespace {
+// out[0] = sum of a[0..n-1] (two-stage tree; partials in scratch slot 11)
+__global__ void k_sum_stage(const double* a, long n, double* part) {
+  __shared__ double sh[256];
+  double acc = 0.0;
+  for (long t = blockIdx.x * 256L + threadIdx.x; t < n; t += (long)gridDim.x * 256) acc += a[t];
+  sh[threadIdx.x] = acc;
+  __syncthreads();
+  for (int st = 128; st > 0; st >>= 1) {
+    if ((int)threadIdx.x < st) sh[threadIdx.x] += sh[threadIdx.x + st];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[blockIdx.x] = sh[0];
+}
+void sum_all(cudaStream_t s, long n, const double* a, double* out) {
+  const int nb = 152 * 4;
+  double* part = (double*)scratch(sizeof(double) * nb, 11);
+  k_sum_stage<<<nb, 256, 0, s>>>(a, n, part);
+  k_sum_stage<<<1, 256, 0, s>>>(part, nb, out);
+  count_launch(2);
+}
+}  // namespace
+
+// bnd_periodic: x copies over every (j,k) then z copies over every (i,j); the adjoint
+// runs z first.  Sources and destinations of one row are disjoint.
+void periodic_T(cudaStream_t s, const Grid& g, double* lq) {
+  const Grid G = g;
+  range2(s, -2, g.ni + 3, -2, g.nj + 3, [=] __device__(int i, int j) {
+    const int NK = G.nk;
+    const long Z = G.sz, r = G.at(i, j, 0);
+    const int dst[6] = {-2, -1, 0, NK + 1, NK + 2, NK + 3}, src[6] = {NK - 2, NK - 1, NK, 1, 2, 3};
+    double L[6];
+    for (int t = 0; t < 6; ++t) {
+      L[t] = lq[r + dst[t] * Z];
+      lq[r + dst[t] * Z] = 0.0;
+    }
+    for (int t = 0; t < 6; ++t) lq[r + src[t] * Z] += L[t];
+  });
+  range2(s, -2, g.nj + 3, -2, g.nk + 3, [=] __device__(int j, int k) {
+    const int NI = G.ni;
+    const long r = G.at(0, j, k);
+    const int dst[6] = {-2, -1, 0, NI + 1, NI + 2, NI + 3}, src[6] = {NI - 2, NI - 1, NI, 1, 2, 3};
+    double L[6];
+    for (int t = 0; t < 6; ++t) {
+      L[t] = lq[r + dst[t]];
+      lq[r + dst[t]] = 0.0;
+    }
+    for (int t = 0; t < 6; ++t) lq[r + src[t]] += L[t];
+  });
+}
+
+void neumann_T(cudaStream_t s, const Grid& g, double* lq) {
+  const Grid G = g;
+  range2(s, -2, g.ni + 3, -2, g.nk + 3, [=] __device__(int i, int k) {
+    const int NJ = G.nj;
+    const int dst[6] = {-2, -1, 0, NJ + 1, NJ + 2, NJ + 3}, src[6] = {3, 2, 1, NJ, NJ - 1, NJ - 2};
+    double L[6];
+    for (int t = 0; t < 6; ++t) {
+      L[t] = lq[G.at(i, dst[t], k)];
+      lq[G.at(i, dst[t], k)] = 0.0;
+    }
+    for (int t = 0; t < 6; ++t) lq[G.at(i, src[t], k)] += L[t];
+  });
+}
+
+// q -= mean(interior q) at every point: lq[interior] -= sum(lq)/cells
+void avzero_T(cudaStream_t s, const Grid& g, double* lq) {
+  const Grid G = g;
+  double* S = (double*)scratch(sizeof(double) * 2, 12);
+  sum_all(s, g.n, lq, S);
+  const double inv = 1.0 / (double)g.cells();
+  range3(s, 1, g.ni, 1, g.nj, 1, g.nk, [=] __device__(int i, int j, int k) { lq[G.at(i, j, k)] -= S[0] * inv; });
+}
+
+void summation_T(cudaStream_t s, const Grid& g, const double* q1, double* lq0, double* lq1) {
+  const Grid G = g;
+  range3(s, -2, g.ni + 3, -2, g.nj + 3, -2, g.nk + 3, [=] __device__(int i, int j, int k) {
+    const long c = G.at(i, j, k);
+    const bool in = i >= 1 && i <= G.ni && j >= 1 && j <= G.nj && k >= 1 && k <= G.nk;
+    const double x = q1[c];
+    const double m = (!in || (x >= 0.0 && x <= 1.0)) ? 1.0 : 0.0;
+    lq1[c] += m * lq0[c];
+    lq0[c] = 0.0;
+  });
+}
+
+void gnbc_T(cudaStream_t s, const Grid& g, const double* uk, const double* wk, double uwall, const double* theta0,
+            double sigma, const double* zeta, const double* ltheta, double* lu, double* lw, double* ltheta0,
+            double* lzeta) {
+  const Grid G = g;
+  const double pi = std::acos(-1.0);
+  range2(s, -2, g.ni + 3, -2, 2 * (g.nk + 6) - 3, [=] __device__(int i, int kk) {
+    const int side = kk >= G.nk + 4 ? 1 : 0;
+    const int k = side ? kk - (G.nk + 6) : kk;
+    const int ja = side ? G.nj : 0, jb = ja + 1, jw = side ? G.nj : 1;
+    const long c = G.at(i, jw, k);
+    const double lt = ltheta[c];
+    if (lt == 0.0) return;
+    const double us = side ? -uwall : uwall;
+    const int mi = (i + G.ni + 2) % (G.ni + 3);
+    const long p0 = G.at(mi, ja, k), p1 = G.at(mi, jb, k), p2 = G.at(i, ja, k), p3 = G.at(i, jb, k);
+    const double ucx = (uk[p0] + uk[p1] + uk[p2] + uk[p3]) / 4.0 + us;
+    const double ucz = (wk[p0] + wk[p1] + wk[p2] + wk[p3]) / 4.0;
+    const double r = sqrt(ucx * ucx + ucz * ucz + 1.0e-12);
+    const double sg = signbit(ucx) ? -1.0 : 1.0;
+    double ucl = sg * r;
+    const double flip = (i <= G.ni / 2) ? -1.0 : 1.0;
+    ucl *= flip;
+    const double th0 = theta0[c] * (pi / 180.0);
+    const double ct = cos(th0) - zeta[c] * ucl / sigma;
+    if (!(ct > -1.0 && ct < 1.0)) return;  // clamped: no dependence
+    const double L = lt * (-(180.0 / pi) / sqrt(1.0 - ct * ct));
+    ltheta0[c] += L * (-sin(th0)) * (pi / 180.0);
+    lzeta[c] += L * (-ucl / sigma);
+    const double lucl = L * (-zeta[c] / sigma) * flip;
+    const double lr = sg * lucl;
+    const double lx = lr * ucx / r * 0.25, lz = lr * ucz / r * 0.25;
+    const long ps[4] = {p0, p1, p2, p3};
+    for (int t = 0; t < 4; ++t) {
+      aadd(lu + ps[t], lx);
+      aadd(lw + ps[t], lz);
+    }
+  });
+}
+
+void contact_angle_T(cudaStream_t s, const Grid& g, const double* qk, const double* theta, double dx, double dy,
+                     double dz, double* lq, double* ltheta) {
+  const Grid G = g;
+  const double pi = std::acos(-1.0), ax = dy / dx, az = dy / dz;
+  range2(s, -1, g.ni + 2, -1, 2 * (g.nk + 4) - 2, [=] __device__(int i, int kk) {
+    const int side = kk >= G.nk + 3 ? 1 : 0;
+    const int k = side ? kk - (G.nk + 4) : kk;
+    const int jw = side ? G.nj : 1;
+    const long g0 = side ? G.at(i, G.nj + 1, k) : G.at(i, 0, k);
+    const long g1 = side ? G.at(i, G.nj + 2, k) : G.at(i, -1, k);
+    const long g2 = side ? G.at(i, G.nj + 3, k) : G.at(i, -2, k);
+    const double L0 = lq[g0], L1 = lq[g1], L2 = lq[g2];
+    lq[g0] = 0.0;
+    lq[g1] = 0.0;
+    lq[g2] = 0.0;
+    if (L0 == 0.0 && L1 == 0.0 && L2 == 0.0) return;
+    const double eps = 1.0e-20;
+    using D1 = Dual<1>;
+    const long cw = G.at(i, jw, k);
+    const D1 th = D1::var(theta[cw], 0) * (pi / 180.0);
+    const D1 ct = dcos(th), sn = dsin(th);
+    const double sg = (i - G.ni / 2) >= 0 ? 1.0 : -1.0;
+    D1 nx = sn * (sg * ax), nz = sn * (sg * az), ny = ct;
+    const D1 nrm = dsqrt(nx * nx + ny * ny + nz * nz + eps);
+    nx = nx / nrm;
+    ny = ny / nrm;
+    nz = nz / nrm;
+    const D1 A = ny / (nx + eps) * (0.5 * ax), B = ny / (nz + eps) * (0.5 * az);
+    const double Dx = qk[G.at(i + 1, jw, k)] - qk[G.at(i - 1, jw, k)];
+    const double Dz = qk[G.at(i, jw, k + 1)] - qk[G.at(i, jw, k - 1)];
+    // gh = q1 - A Dx - B Dz; ghosts gh, 2gh - q1, 3gh - 2q1
+    const double lgh = L0 + 2.0 * L1 + 3.0 * L2;
+    aadd(lq + cw, L0 + L1 + L2);  // q1: through gh (lgh) and directly (-L1 - 2 L2)
+    aadd(lq + G.at(i + 1, jw, k), -A.v * lgh);
+    aadd(lq + G.at(i - 1, jw, k), A.v * lgh);
+    aadd(lq + G.at(i, jw, k + 1), -B.v * lgh);
+    aadd(lq + G.at(i, jw, k - 1), B.v * lgh);
+    ltheta[cw] += (-Dx * lgh) * A.d[0] + (-Dz * lgh) * B.d[0];
+  });
+}
+
+void wall_T(cudaStream_t s, const Grid& g, double uwall, const double* wc, const double* uk, const double* wk,
+            double* lu, double* lv, double* lw, double* lwc) {
+  const Grid G = g;
+  range2(s, -2, g.ni + 3, -2, 2 * (g.nk + 6) - 3, [=] __device__(int i, int kk) {
+    const int side = kk >= G.nk + 4 ? 1 : 0;
+    const int k = side ? kk - (G.nk + 6) : kk;
+    const long o = (((long)side * (G.nk + 6) + (k + 2)) * (G.ni + 6) + (i + 2)) * 2;
+    const double c2 = wc[o + 1];
+    const long Y = G.sy;
+    const long c = G.at(i, side ? G.nj : 1, k);
+    const long t = side ? Y : -Y;
+    const double L1 = lu[c + t], L2 = lu[c + 2 * t], L3 = lu[c + 3 * t];
+    const double M1 = lw[c + t], M2 = lw[c + 2 * t], M3 = lw[c + 3 * t];
+    lu[c + t] = lu[c + 2 * t] = lu[c + 3 * t] = 0.0;
+    lw[c + t] = lw[c + 2 * t] = lw[c + 3 * t] = 0.0;
+    lu[c] += c2 * L1 + (2.0 * c2 - 1.0) * L2 + (3.0 * c2 - 2.0) * L3;
+    lw[c] += c2 * M1 + (2.0 * c2 - 1.0) * M2 + (3.0 * c2 - 2.0) * M3;
+    const double SL = L1 + 2.0 * L2 + 3.0 * L3, SM = M1 + 2.0 * M2 + 3.0 * M3;
+    if (lwc) {
+      lwc[o] += (side ? uwall : -uwall) * SL;
+      lwc[o + 1] += uk[c] * SL + wk[c] * SM;
+    }
+    if (!side) {  // v(0) = 0, v(-1) = -v(1), v(-2) = -v(2)
+      const double a = lv[c - 2 * Y], b = lv[c - 3 * Y];
+      lv[c - Y] = lv[c - 2 * Y] = lv[c - 3 * Y] = 0.0;
+      lv[c] -= a;
+      lv[c + Y] -= b;
+    } else {  // v(nj) = 0, v(nj+m) = -v(nj-m)
+      const double a = lv[c + Y], b = lv[c + 2 * Y], d = lv[c + 3 * Y];
+      lv[c] = lv[c + Y] = lv[c + 2 * Y] = lv[c + 3 * Y] = 0.0;
+      lv[c - Y] -= a;
+      lv[c - 2 * Y] -= b;
+      lv[c - 3 * Y] -= d;
+    }
+  });
+}
+
+void halo_x_T(cudaStream_t s, const Grid& g, int normal, double* lu, double* lv, double* lw) {
+  const Grid G = g;
+  range2(s, -2, g.nj + 3, -2, g.nk + 3, [=] __device__(int j, int k) {
+    const int NI = G.ni;
+    const long r = G.at(0, j, k);
+    double* q[3] = {lu, lv, lw};
+    for (int cmp = 0; cmp < 3; ++cmp) {
+      double* a = q[cmp];
+      if (cmp == 0 && !(normal & 1)) {
+        const int dst[5] = {-2, -1, 0, NI + 2, NI + 3}, src[5] = {NI - 1, NI, NI + 1, 2, 3};
+        double L[5];
+        for (int t = 0; t < 5; ++t) {
+          L[t] = a[r + dst[t]];
+          a[r + dst[t]] = 0.0;
+        }
+        for (int t = 0; t < 5; ++t) a[r + src[t]] += L[t];
+      } else {
+        const int dst[6] = {-2, -1, 0, NI + 1, NI + 2, NI + 3}, src[6] = {NI - 2, NI - 1, NI, 1, 2, 3};
+        double L[6];
+        for (int t = 0; t < 6; ++t) {
+          L[t] = a[r + dst[t]];
+          a[r + dst[t]] = 0.0;
+        }
+        for (int t = 0; t < 6; ++t) a[r + src[t]] += L[t];
+      }
+    }
+  });
+}
+
+void halo_z_T(cudaStream_t s, const Grid& g, int normal, double* lu, double* lv, double* lw) {
+  const Grid G = g;
+  range2(s, -2, g.ni + 3, -2, g.nj + 3, [=] __device__(int i, int j) {
+    const int NK = G.nk;
+    const long Z = G.sz, r = G.at(i, j, 0);
+    double* q[3] = {lu, lv, lw};
+    for (int cmp = 0; cmp < 3; ++cmp) {
+      double* a = q[cmp];
+      if (cmp == 2 && !(normal & 4)) {
+        const int dst[5] = {-2, -1, 0, NK + 2, NK + 3}, src[5] = {NK - 1, NK, NK + 1, 2, 3};
+        double L[5];
+        for (int t = 0; t < 5; ++t) {
+          L[t] = a[r + dst[t] * Z];
+          a[r + dst[t] * Z] = 0.0;
+        }
+        for (int t = 0; t < 5; ++t) a[r + src[t] * Z] += L[t];
+      } else {
+        const int dst[6] = {-2, -1, 0, NK + 1, NK + 2, NK + 3}, src[6] = {NK - 2, NK - 1, NK, 1, 2, 3};
+        double L[6];
+        for (int t = 0; t < 6; ++t) {
+          L[t] = a[r + dst[t] * Z];
+          a[r + dst[t] * Z] = 0.0;
+        }
+        for (int t = 0; t < 6; ++t) a[r + src[t] * Z] += L[t];
+      }
+    }
+  });
+}
+
+void wall_halo_T(cudaStream_t s, const Grid& g, int normal, double uwall, const double* wc, const double* u,
+                 const double* w, double* lu, double* lv, double* lw, double* lwc) {
+  halo_z_T(s, g, normal, lu, lv, lw);
+  halo_x_T(s, g, normal, lu, lv, lw);
+  wall_T(s, g, uwall, wc, u, w, lu, lv, lw, lwc);
+}
+
+void wall_coef_T(cudaStream_t s, const Grid& g, double dy, const double* l1, const double* l2, const double* phi,
+                 const double* lwc, double* lphi, double* ll1, double* ll2) {
+  const Grid G = g;
+  range2(s, -2, g.ni + 3, -2, 2 * (g.nk + 6) - 3, [=] __device__(int i, int kk) {
+    const int side = kk >= G.nk + 4 ? 1 : 0;
+    const int k = side ? kk - (G.nk + 6) : kk;
+    const int jw = side ? G.nj : 1;
+    const long o = (((long)side * (G.nk + 6) + (k + 2)) * (G.ni + 6) + (i + 2)) * 2;
+    const double lc1 = lwc[o], lc2 = lwc[o + 1];
+    if (lc1 == 0.0 && lc2 == 0.0) return;
+    using D3 = Dual<3>;
+    const long ca = G.at(i, jw, k), cb = G.at((i + 1) % (G.ni + 3), jw, k);
+    const D3 pa = D3::var((phi[ca] + phi[cb]) / 2.0, 0);
+    const D3 L1 = D3::var(l1[ca], 1), L2 = D3::var(l2[ca], 2);
+    const D3 i1 = pa / L1, i2 = (1.0 - pa) / L2;
+    const D3 ls = 1.0 / (i1 + i2);
+    const D3 c1 = (2.0 * dy) / (2.0 * ls + dy), c2 = (2.0 * ls - dy) / (2.0 * ls + dy);
+    const double lpa = lc1 * c1.d[0] + lc2 * c2.d[0];
+    aadd(lphi + ca, 0.5 * lpa);
+    aadd(lphi + cb, 0.5 * lpa);
+    ll1[ca] += lc1 * c1.d[1] + lc2 * c2.d[1];
+    ll2[ca] += lc1 * c1.d[2] + lc2 * c2.d[2];
+  });
+}
+
+// ---- linear stencils ----------------------------------------------------------
+void grad_p2a_T(cudaStream_t s, const Grid& g, double dxi, double dyi, double dzi, const double* lqx,
+                const double* lqy, const double* lqz, double* lq) {
+  const Grid G = g;
+  range3(s, -2, g.ni + 3, -2, g.nj + 3, -2, g.nk + 3, [=] __device__(int x, int y, int z) {
+    double acc = 0.0;
+    for (int c = 0; c < 2; ++c)
+      for (int b = 0; b < 2; ++b)
+        for (int a = 0; a < 2; ++a) {
+          const int i = x - a, j = y - b, k = z - c;
+          if (i < -2 || i > G.ni + 2 || j < -2 || j > G.nj + 2 || k < -2 || k > G.nk + 2) continue;
+          const long v = G.at(i, j, k);
+          acc += 0.25 * ((a ? dxi : -dxi) * lqx[v] + (b ? dyi : -dyi) * lqy[v] + (c ? dzi : -dzi) * lqz[v]);
+        }
+    lq[G.at(x, y, z)] += acc;
+  });
+}
+
+void grad_prs_T(cudaStream_t s, const Grid& g, double dxi, double dyi, double dzi, const double* lqx,
+                const double* lqy, const double* lqz, double* lq) {
+  const Grid G = g;
+  range3(s, -2, g.ni + 3, -2, g.nj + 3, -2, g.nk + 3, [=] __device__(int i, int j, int k) {
+    auto in = [&](int a, int b, int c) {
+      return a >= -2 && a <= G.ni + 2 && b >= -2 && b <= G.nj + 2 && c >= -2 && c <= G.nk + 2;
+    };
+    double acc = 0.0;
+    if (in(i, j, k)) {
+      const long c = G.at(i, j, k);
+      acc -= dxi * lqx[c] + dyi * lqy[c] + dzi * lqz[c];
+    }
+    if (in(i - 1, j, k)) acc += dxi * lqx[G.at(i - 1, j, k)];
+    if (in(i, j - 1, k)) acc += dyi * lqy[G.at(i, j - 1, k)];
+    if (in(i, j, k - 1)) acc += dzi * lqz[G.at(i, j, k - 1)];
+    lq[G.at(i, j, k)] += acc;
+  });
+}
+
+void mean_T(cudaStream_t s, const Grid& g, double ql, double qg, const double* lq, double* lphi) {
+  const double f = qg - ql;
+  flat(s, g.n, [=] __device__(long t) { lphi[t] += f * lq[t]; });
+}
+
+void caldiv_T(cudaStream_t s, const Grid& g, double dxi, double dyi, double dzi, double dt, const double* ldiv,
+              double* lu, double* lv, double* lw) {
+  const Grid G = g;
+  const double f = 1.0 / dt;
+  range3(s, -2, g.ni + 3, -2, g.nj + 3, -2, g.nk + 3, [=] __device__(int i, int j, int k) {
+    auto D = [&](int a, int b, int c) {
+      return (a >= -1 && b >= -1 && c >= -1 && a <= G.ni + 3 && b <= G.nj + 3 && c <= G.nk + 3)
+                 ? ldiv[G.at(a, b, c)] * f
+                 : 0.0;
+    };
+    const long c = G.at(i, j, k);
+    const double d0 = D(i, j, k);
+    lu[c] += dxi * (d0 - D(i + 1, j, k));
+    lv[c] += dyi * (d0 - D(i, j + 1, k));
+    lw[c] += dzi * (d0 - D(i, j, k + 1));
+  });
+}
+
+void corunp_T(cudaStream_t s, const Grid& g, double rho, double dxi, double dyi, double dzi, double dt,
+              const double* lun, const double* lvn, const double* lwn, const double* lpn, double* ldp,
+              double* lphat) {
+  const Grid G = g;
+  const double f = dt / rho;
+  range3(s, -2, g.ni + 3, -2, g.nj + 3, -2, g.nk + 3, [=] __device__(int i, int j, int k) {
+    auto in = [&](int a, int b, int c) { return a >= 1 && a <= G.ni && b >= 1 && b <= G.nj && c >= 1 && c <= G.nk; };
+    auto inv_ = [&](int a, int b, int c) { return in(a, b, c) && b <= G.nj - 1; };
+    const long c = G.at(i, j, k);
+    double acc = 0.0;  // velocity corrections that read dp(c)
+    if (in(i, j, k)) acc += dxi * lun[c] + dzi * lwn[c];
+    if (inv_(i, j, k)) acc += dyi * lvn[c];
+    if (in(i - 1, j, k)) acc -= dxi * lun[c - 1];
+    if (inv_(i, j - 1, k)) acc -= dyi * lvn[c - G.sy];
+    if (in(i, j, k - 1)) acc -= dzi * lwn[c - G.sz];
+    const double lp = in(i, j, k) ? lpn[c] : 0.0;  // pn = phat + dp
+    ldp[c] += f * acc + lp;
+    lphat[c] += lp;
+  });
+}
+
+void calsij_T(cudaStream_t s, const Grid& g, double dxi, double dyi, double dzi, const double* lsk, double* lu,
+              double* lv, double* lw) {
+  const Grid G = g;
+  range3(s, -2, g.ni + 3, -2, g.nj + 3, -2, g.nk + 3, [=] __device__(int i, int j, int k) {
+    const long X = 1, Y = G.sy, Z = G.sz, n = G.n;
+    const long c = G.at(i, j, k);
+    double L;
+    if (i >= -1 && (L = lsk[c]) != 0.0) {
+      aadd(lu + c, dxi * L);
+      aadd(lu + c - X, -dxi * L);
+    }
+    if (j >= -1 && (L = lsk[c + n]) != 0.0) {
+      aadd(lv + c, dyi * L);
+      aadd(lv + c - Y, -dyi * L);
+    }
+    if (i >= -1 && j >= -1 && k >= -1 && (L = lsk[c + 2 * n]) != 0.0) {
+      aadd(lw + c, dzi * L);
+      aadd(lw + c - Z, -dzi * L);
+    }
+    if (j <= G.nj + 2 && i <= G.ni + 2 && (L = 0.5 * lsk[c + 3 * n]) != 0.0) {
+      aadd(lu + c + Y, dyi * L);
+      aadd(lu + c, -dyi * L);
+      aadd(lv + c + X, dxi * L);
+      aadd(lv + c, -dxi * L);
+    }
+    if (k <= G.nk + 2 && i <= G.ni + 2 && (L = 0.5 * lsk[c + 4 * n]) != 0.0) {
+      aadd(lu + c + Z, dzi * L);
+      aadd(lu + c, -dzi * L);
+      aadd(lw + c + X, dxi * L);
+      aadd(lw + c, -dxi * L);
+    }
+    if (k <= G.nk + 2 && j <= G.nj + 2 && (L = 0.5 * lsk[c + 5 * n]) != 0.0) {
+      aadd(lv + c + Z, dzi * L);
+      aadd(lv + c, -dzi * L);
+      aadd(lw + c + Y, dyi * L);
+      aadd(lw + c, -dyi * L);
+    }
+  });
+}
+
+// arithmetic edge means only (the step's cal_arith_tau)
+void tau_T(cudaStream_t s, const Grid& g, const double* sk, const double* mu, const double* ltau, double* lsk,
+           double* lmu) {
+  const Grid G = g;
+  range3(s, -2, g.ni + 3, -2, g.nj + 3, -2, g.nk + 3, [=] __device__(int i, int j, int k) {
+    const long X = 1, Y = G.sy, Z = G.sz, n = G.n;
+    const long c = G.at(i, j, k);
+    double lm = 0.0;
+    for (int l = 0; l < 3; ++l) {
+      const double L = ltau[c + l * n];
+      lsk[c + l * n] += L * mu[c] * 2.0;
+      lm += L * sk[c + l * n] * 2.0;
+    }
+    aadd(lmu + c, lm);
+    auto edge = [&](int l, long a, long b, long d, long e) {
+      const double L = ltau[c + l * n];
+      if (L == 0.0) return;
+      const double m4 = 0.25 * mu[a] + 0.25 * mu[b] + 0.25 * mu[d] + 0.25 * mu[e];
+      lsk[c + l * n] += L * m4 * 2.0;
+      const double lm4 = L * sk[c + l * n] * 2.0 * 0.25;
+      aadd(lmu + a, lm4);
+      aadd(lmu + b, lm4);
+      aadd(lmu + d, lm4);
+      aadd(lmu + e, lm4);
+    };
+    if (j <= G.nj + 2 && i <= G.ni + 2) edge(3, c, c + X, c + Y, c + X + Y);
+    if (k <= G.nk + 2 && i <= G.ni + 2) edge(4, c, c + X, c + Z, c + X + Z);
+    if (k <= G.nk + 2 && j <= G.nj + 2) edge(5, c, c + Y, c + Z, c + Y + Z);
+  });
+}
+
+void div_tensor_T(cudaStream_t s, const Grid& g, double dxi, double dyi, double dzi, const double* lvu,
+                  const double* lvv, const double* lvw, double* lt) {
+  const Grid G = g;
+  range3(s, -2, g.ni + 3, -2, g.nj + 3, -2, g.nk + 3, [=] __device__(int i, int j, int k) {
+    const long X = 1, Y = G.sy, Z = G.sz, n = G.n;
+    const long c = G.at(i, j, k);
+    double* t1 = lt;
+    double* t2 = lt + n;
+    double* t3 = lt + 2 * n;
+    double* t4 = lt + 3 * n;
+    double* t5 = lt + 4 * n;
+    double* t6 = lt + 5 * n;
+    double L;
+    if (k >= -1 && j >= -1 && i <= G.ni + 2 && (L = lvu[c]) != 0.0) {
+      aadd(t1 + c + X, dxi * L);
+      aadd(t1 + c, -dxi * L);
+      aadd(t4 + c, dyi * L);
+      aadd(t4 + c - Y, -dyi * L);
+      aadd(t5 + c, dzi * L);
+      aadd(t5 + c - Z, -dzi * L);
+    }
+    if (k >= -1 && j <= G.nj + 2 && i >= -1 && (L = lvv[c]) != 0.0) {
+      aadd(t4 + c, dxi * L);
+      aadd(t4 + c - X, -dxi * L);
+      aadd(t2 + c + Y, dyi * L);
+      aadd(t2 + c, -dyi * L);
+      aadd(t6 + c, dzi * L);
+      aadd(t6 + c - Z, -dzi * L);
+    }
+    if (k <= G.nk + 2 && j >= -1 && i >= -1 && (L = lvw[c]) != 0.0) {
+      aadd(t5 + c, dxi * L);
+      aadd(t5 + c - X, -dxi * L);
+      aadd(t6 + c, dyi * L);
+      aadd(t6 + c - Y, -dyi * L);
+      aadd(t3 + c + Z, dzi * L);
+      aadd(t3 + c, -dzi * L);
+    }
+  });
+}
+
+}  // namespace adj
+}  // namespace fmf

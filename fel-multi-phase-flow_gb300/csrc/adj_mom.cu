@@ -1,0 +1,248 @@
+// adj_mom.cu -- adjoints of the WENO5 advection (cal_advu_weno5 + weno5.h) and of
+// the CSF surface-tension force (cal_grad_p2a, calrn x4, calrkap, cal_grad_p2uvw,
+// calfst).
+#include "adj.cuh"
+#include "ops.cuh"
+
+namespace fmf {
+namespace adj {
+
+namespace {
+// One side of weno5.h: r = w1 d1 + w2 d2 + w3 d3 with the product-form weights, and
+// its reverse sweep (la[0..4] += dr/d(a5, a3, a1, b1, b3) * lr).
+struct Side {
+  double d1, d2, d3, t[6], s1, s2, s3, P1, P2, P3, m1, m2, m3, D, w1, w3, r;
+};
+__device__ __forceinline__ void side_fwd(double a5, double a3, double a1, double b1, double b3, Side& S) {
+  S.d1 = a5 * 2.0 - a3 * 7.0 + a1 * 11.0;
+  S.d2 = -a3 + a1 * 5.0 + b1 * 2.0;
+  S.d3 = a1 * 2.0 + b1 * 5.0 - b3;
+  S.t[0] = a5 - a3 * 2.0 + a1;
+  S.t[1] = a5 - a3 * 4.0 + a1 * 3.0;
+  S.t[2] = a3 - a1 * 2.0 + b1;
+  S.t[3] = a3 - b1;
+  S.t[4] = a1 - b1 * 2.0 + b3;
+  S.t[5] = a1 * 3.0 - b1 * 4.0 + b3;
+  S.s1 = S.t[0] * S.t[0] * 13.0 + S.t[1] * S.t[1] * 3.0;
+  S.s2 = S.t[2] * S.t[2] * 13.0 + S.t[3] * S.t[3] * 3.0;
+  S.s3 = S.t[4] * S.t[4] * 13.0 + S.t[5] * S.t[5] * 3.0;
+  S.P1 = S.s2 * S.s3;
+  S.P2 = S.s1 * S.s3;
+  S.P3 = S.s1 * S.s2;
+  S.m1 = S.P1 * S.P1;
+  S.m2 = S.P2 * S.P2 * 6.0;
+  S.m3 = S.P3 * S.P3 * 3.0;
+  S.D = S.m1 + S.m2 + S.m3 + 1.0e-80;
+  S.w1 = S.m1 / S.D;
+  S.w3 = S.m3 / S.D;
+  S.r = S.w1 * S.d1 + (1.0 - S.w1 - S.w3) * S.d2 + S.w3 * S.d3;
+}
+__device__ __forceinline__ void side_rev(const Side& S, double lr, double* la) {
+  const double w2 = 1.0 - S.w1 - S.w3;
+  const double ld1 = lr * S.w1, ld2 = lr * w2, ld3 = lr * S.w3;
+  const double lw1 = lr * (S.d1 - S.d2), lw3 = lr * (S.d3 - S.d2);
+  const double G = lw1 * S.w1 + lw3 * S.w3;
+  const double lm1 = (lw1 - G) / S.D, lm2 = -G / S.D, lm3 = (lw3 - G) / S.D;
+  const double lP1 = 2.0 * S.P1 * lm1, lP2 = 12.0 * S.P2 * lm2, lP3 = 6.0 * S.P3 * lm3;
+  const double ls1 = lP2 * S.s3 + lP3 * S.s2, ls2 = lP1 * S.s3 + lP3 * S.s1, ls3 = lP1 * S.s2 + lP2 * S.s1;
+  const double lt0 = 26.0 * S.t[0] * ls1, lt1 = 6.0 * S.t[1] * ls1;
+  const double lt2 = 26.0 * S.t[2] * ls2, lt3 = 6.0 * S.t[3] * ls2;
+  const double lt4 = 26.0 * S.t[4] * ls3, lt5 = 6.0 * S.t[5] * ls3;
+  la[0] += 2.0 * ld1 + lt0 + lt1;
+  la[1] += -7.0 * ld1 - ld2 - 2.0 * lt0 - 4.0 * lt1 + lt2 + lt3;
+  la[2] += 11.0 * ld1 + 5.0 * ld2 + 2.0 * ld3 + lt0 + 3.0 * lt1 - 2.0 * lt2 + lt4 + 3.0 * lt5;
+  la[3] += 2.0 * ld2 + 5.0 * ld3 + lt2 - lt3 - 2.0 * lt4 - 4.0 * lt5;
+  la[4] += -ld3 + lt4 + lt5;
+}
+// adjoint of  out += weno5_line(q, c, S, vel) * di  given lout; returns lvel
+__device__ double wline_T(const double* q, double* lq, long c, long S, double vel, double lout, double di) {
+  const double lr = lout * di;
+  if (lr == 0.0) return 0.0;
+  const double m3 = q[c - 3 * S], m2 = q[c - 2 * S], m1 = q[c - S], z0 = q[c], p1 = q[c + S], p2 = q[c + 2 * S],
+               p3 = q[c + 3 * S];
+  const double dm5 = -m3 + m2, dm3 = -m2 + m1, dm1 = -m1 + z0, dp1 = -z0 + p1, dp3 = -p1 + p2, dp5 = -p2 + p3;
+  // lD[0..5] = adjoints of (dm5, dm3, dm1, dp1, dp3, dp5)
+  double lD[6] = {0, 0, 0, 0, 0, 0};
+  double lvel = 0.0;
+  Side A, B;
+  const bool needA = vel >= 0.0, needB = vel <= 0.0;
+  if (needA) side_fwd(dm5, dm3, dm1, dp1, dp3, A);
+  if (needB) side_fwd(dp5, dp3, dp1, dm1, dm3, B);
+  if (vel > 0.0) {
+    double la[5] = {0, 0, 0, 0, 0};
+    side_rev(A, lr * 2.0 * vel / 12.0, la);
+    lD[0] += la[0]; lD[1] += la[1]; lD[2] += la[2]; lD[3] += la[3]; lD[4] += la[4];
+    lvel = lr * 2.0 * A.r / 12.0;
+  } else if (vel < 0.0) {
+    double la[5] = {0, 0, 0, 0, 0};
+    side_rev(B, lr * 2.0 * vel / 12.0, la);
+    lD[5] += la[0]; lD[4] += la[1]; lD[3] += la[2]; lD[2] += la[3]; lD[1] += la[4];
+    lvel = lr * 2.0 * B.r / 12.0;
+  } else {
+    lvel = lr * (A.r + B.r) / 12.0;
+  }
+  // differences -> points m3 m2 m1 z0 p1 p2 p3
+  aadd(lq + c - 3 * S, -lD[0]);
+  aadd(lq + c - 2 * S, lD[0] - lD[1]);
+  aadd(lq + c - S, lD[1] - lD[2]);
+  aadd(lq + c, lD[2] - lD[3]);
+  aadd(lq + c + S, lD[3] - lD[4]);
+  aadd(lq + c + 2 * S, lD[4] - lD[5]);
+  aadd(lq + c + 3 * S, lD[5]);
+  return lvel;
+}
+}  // namespace
+
+void weno_T(cudaStream_t s, const Grid& g, double dxi, double dyi, double dzi, const double* u, const double* v,
+            const double* w, const double* const* ladv, double* lu, double* lv, double* lw) {
+  const Grid G = g;
+  const double *la0 = ladv[0], *la1 = ladv[1], *la2 = ladv[2];
+  range3(s, 1, g.ni, 1, g.nj, 1, g.nk, [=] __device__(int i, int j, int k) {
+    const long X = 1, Y = G.sy, Z = G.sz;
+    const long c = G.at(i, j, k);
+    double L, vel, lvel;
+    // velocity means: ((a + b) 0.5 + (d + e) 0.5) 0.5 -> 0.25 to each point
+    auto spread = [&](double* lq, long a, long b, long d, long e, double lv_) {
+      const double q = 0.25 * lv_;
+      aadd(lq + a, q);
+      aadd(lq + b, q);
+      aadd(lq + d, q);
+      aadd(lq + e, q);
+    };
+    if ((L = la0[c]) != 0.0) {
+      vel = ((u[c - X] + u[c]) * 0.5 + (u[c] + u[c + X]) * 0.5) * 0.5;
+      lvel = wline_T(u, lu, c, X, vel, L, dxi);
+      spread(lu, c - X, c, c, c + X, lvel);
+      vel = ((v[c - Y] + v[c + X - Y]) * 0.5 + (v[c] + v[c + X]) * 0.5) * 0.5;
+      lvel = wline_T(u, lu, c, Y, vel, L, dyi);
+      spread(lv, c - Y, c + X - Y, c, c + X, lvel);
+      vel = ((w[c - Z] + w[c + X - Z]) * 0.5 + (w[c] + w[c + X]) * 0.5) * 0.5;
+      lvel = wline_T(u, lu, c, Z, vel, L, dzi);
+      spread(lw, c - Z, c + X - Z, c, c + X, lvel);
+    }
+    if ((L = la1[c]) != 0.0) {
+      vel = ((u[c - X] + u[c - X + Y]) * 0.5 + (u[c] + u[c + Y]) * 0.5) * 0.5;
+      lvel = wline_T(v, lv, c, X, vel, L, dxi);
+      spread(lu, c - X, c - X + Y, c, c + Y, lvel);
+      vel = ((v[c - Y] + v[c]) * 0.5 + (v[c] + v[c + Y]) * 0.5) * 0.5;
+      lvel = wline_T(v, lv, c, Y, vel, L, dyi);
+      spread(lv, c - Y, c, c, c + Y, lvel);
+      vel = ((w[c - Z] + w[c + Y - Z]) * 0.5 + (w[c] + w[c + Y]) * 0.5) * 0.5;
+      lvel = wline_T(v, lv, c, Z, vel, L, dzi);
+      spread(lw, c - Z, c + Y - Z, c, c + Y, lvel);
+    }
+    if ((L = la2[c]) != 0.0) {
+      vel = ((u[c - X] + u[c - X + Z]) * 0.5 + (u[c] + u[c + Z]) * 0.5) * 0.5;
+      lvel = wline_T(w, lw, c, X, vel, L, dxi);
+      spread(lu, c - X, c - X + Z, c, c + Z, lvel);
+      vel = ((v[c - Y] + v[c - Y + Z]) * 0.5 + (v[c] + v[c + Z]) * 0.5) * 0.5;
+      lvel = wline_T(w, lw, c, Y, vel, L, dyi);
+      spread(lv, c - Y, c - Y + Z, c, c + Z, lvel);
+      vel = ((w[c - Z] + w[c]) * 0.5 + (w[c] + w[c + Z]) * 0.5) * 0.5;
+      lvel = wline_T(w, lw, c, Z, vel, L, dzi);
+      spread(lw, c - Z, c, c, c + Z, lvel);
+    }
+  });
+}
+
+// ---- CSF --------------------------------------------------------------------------
+void csf_T(cudaStream_t s, const Grid& g, double dxi, double dyi, double dzi, double rhol, double rhog,
+           double sigma, const double* phi, const double* const* lf, double* lphi, double* work) {
+  const Grid G = g;
+  const long n = g.n;
+  double* Gv = work;             // vertex gradient (3n)
+  double* rn = work + 3 * n;     // the four normal families (12n)
+  double* kap = work + 15 * n;   // curvature at u, v, w points (3n)
+  double* gq = work + 18 * n;    // face gradient of phi (3n)
+  double* lG = work + 21 * n;    // adjoint of the vertex gradient (3n)
+  double* lrn = work + 24 * n;   // adjoint of the normals (12n)
+  double* lkap = work + 36 * n;  // adjoint of the curvature (3n)
+  double* lgq = work + 39 * n;   // adjoint of the face gradient (3n)
+  static const int offs[4][3] = {{1, 1, 1}, {0, 0, 1}, {0, 1, 0}, {1, 0, 0}};
+  // forward recompute
+  op::cal_grad_p2a(s, g, dxi, dyi, dzi, phi, Gv, Gv + n, Gv + 2 * n);
+  for (int q = 0; q < 4; ++q)
+    op::calrn(s, g, dxi, dyi, dzi, offs[q][0], offs[q][1], offs[q][2], Gv, Gv + n, Gv + 2 * n, rn + 3 * n * q);
+  op::calrkap(s, g, dxi, dyi, dzi, rn, rn + 3 * n, rn + 6 * n, rn + 9 * n, kap);
+  op::cal_grad_prs(s, g, dxi, dyi, dzi, phi, gq, gq + n, gq + 2 * n);
+  FMF_CUDA(cudaMemsetAsync(lG, 0, sizeof(double) * 21 * n, s));
+  // calfst: f_c = -st kap_c g_c
+  const double st = 2.0 * sigma / (rhol + rhog);
+  const double *lf0 = lf[0], *lf1 = lf[1], *lf2 = lf[2];
+  flat(s, n, [=] __device__(long t) {
+    const double L[3] = {lf0[t], lf1[t], lf2[t]};
+    for (int q = 0; q < 3; ++q) {
+      lkap[t + q * n] = -st * gq[t + q * n] * L[q];
+      lgq[t + q * n] = -st * kap[t + q * n] * L[q];
+    }
+  });
+  grad_prs_T(s, g, dxi, dyi, dzi, lgq, lgq + n, lgq + 2 * n, lphi);
+  // calrkap (pp = family 0, r12 = 1, r13 = 2, r23 = 3)
+  double* lpp = lrn;
+  double* l12 = lrn + 3 * n;
+  double* l13 = lrn + 6 * n;
+  double* l23 = lrn + 9 * n;
+  range3(s, -2, g.ni + 3, -2, g.nj + 3, -2, g.nk + 3, [=] __device__(int i, int j, int k) {
+    const long X = 1, Y = G.sy, Z = G.sz;
+    const long c = G.at(i, j, k);
+    double L;
+    if (k >= -1 && j >= -1 && i <= G.ni + 2 && (L = lkap[c]) != 0.0) {
+      aadd(lpp + c + X, dxi * L);
+      aadd(lpp + c, -dxi * L);
+      aadd(l12 + c + n, dyi * L);
+      aadd(l12 + c - Y + n, -dyi * L);
+      aadd(l13 + c + 2 * n, dzi * L);
+      aadd(l13 + c - Z + 2 * n, -dzi * L);
+    }
+    if (k >= -1 && j <= G.nj + 2 && i >= -1 && (L = lkap[c + n]) != 0.0) {
+      aadd(l12 + c, dxi * L);
+      aadd(l12 + c - X, -dxi * L);
+      aadd(lpp + c + Y + n, dyi * L);
+      aadd(lpp + c + n, -dyi * L);
+      aadd(l23 + c + 2 * n, dzi * L);
+      aadd(l23 + c - Z + 2 * n, -dzi * L);
+    }
+    if (k <= G.nk + 2 && j >= -1 && i >= -1 && (L = lkap[c + 2 * n]) != 0.0) {
+      aadd(l13 + c, dxi * L);
+      aadd(l13 + c - X, -dxi * L);
+      aadd(l23 + c + n, dyi * L);
+      aadd(l23 + c - Y + n, -dyi * L);
+      aadd(lpp + c + Z + 2 * n, dzi * L);
+      aadd(lpp + c + 2 * n, -dzi * L);
+    }
+  });
+  // calrn: N(v) = v/(|v| + vs) of the 8-point mean v
+  const double vs = std::sqrt(dxi * dxi + dyi * dyi + dzi * dzi) * 1.0e-30;
+  for (int q = 0; q < 4; ++q) {
+    const int ip = offs[q][0], jp = offs[q][1], kp = offs[q][2];
+    const double* L3 = lrn + 3 * n * q;
+    range3(s, -2, g.ni + 3 - ip, -2, g.nj + 3 - jp, -2, g.nk + 3 - kp, [=] __device__(int i, int j, int k) {
+      const long c = G.at(i, j, k);
+      const long X = ip, Y = jp ? G.sy : 0, Z = kp ? G.sz : 0;
+      const long o = c + X + Y + Z;
+      const double lx = L3[o], ly = L3[o + n], lz = L3[o + 2 * n];
+      if (lx == 0.0 && ly == 0.0 && lz == 0.0) return;
+      const long pts[8] = {c, c + X, c + Y, c + X + Y, c + Z, c + X + Z, c + Y + Z, c + X + Y + Z};
+      double r[3] = {0.0, 0.0, 0.0};
+      for (int q3 = 0; q3 < 3; ++q3) {
+        const double* p = Gv + q3 * n;
+        r[q3] = (p[pts[0]] + p[pts[1]] + p[pts[2]] + p[pts[3]] + p[pts[4]] + p[pts[5]] + p[pts[6]] + p[pts[7]]) * 0.125;
+      }
+      const double m = sqrt(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]);
+      const double a = m + vs;
+      // dN/dv = I/a - v v^T/(a^2 m), formed with the unit vector e = v/m
+      double e[3] = {0.0, 0.0, 0.0}, corr = 0.0;
+      if (m > 0.0) {
+        for (int q3 = 0; q3 < 3; ++q3) e[q3] = r[q3] / m;
+        corr = (e[0] * lx + e[1] * ly + e[2] * lz) * (m / (a * a));
+      }
+      const double lv[3] = {lx / a - e[0] * corr, ly / a - e[1] * corr, lz / a - e[2] * corr};
+      for (int q3 = 0; q3 < 3; ++q3)
+        for (int t = 0; t < 8; ++t) aadd(lG + q3 * n + pts[t], 0.125 * lv[q3]);
+    });
+  }
+  grad_p2a_T(s, g, dxi, dyi, dzi, lG, lG + n, lG + 2 * n, lphi);
+}
+
+}  // namespace adj
+}  // namespace fmf

@@ -1,0 +1,716 @@
+// adj_step.cu -- the adjoint of the K-step rollout (include/fmf_capi.h part 4).
+//
+// Objective: J = find_interface_positions_lower (find_interface_positions_lower.f90:
+// 15-32) of phi slice 0 after K steps, started from a state to which the start-up
+// boundary pass (main.f90:322-366) is applied first.  Parameters: the per-wall-cell
+// static angle theta0, the GNBC coefficient zeta, the slip lengths l1, l2 (all four as
+// full arrays, read on the wall planes) and the initial phi (slice 1).
+//
+// Forward: the FP64 step of step.cu written out with its intermediates kept
+// (record_step), with the viscous solve run to a configurable tolerance.  Reverse:
+// for each step, newest first, the step is recomputed from its start state and the
+// adjoint kernels of adj_*.cu run in the opposite order.  Start states are
+// checkpointed every C steps and recomputed between checkpoints (C ~ sqrt(K)).
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <vector>
+
+#include "../../include/fmf_capi.h"
+#include "adj.cuh"
+#include "fused.cuh"
+#include "ops.cuh"
+#include "runtime.cuh"
+
+using namespace fmf;
+
+namespace {
+enum { SU, SV, SW, SUO, SVO, SWO, SP, SPO, SPHI0, SPHI1, SPHIN0, SPHIN1, NSTATE };
+}
+
+struct fmf_adj {
+  fmf_params prm;
+  Grid g;
+  cudaStream_t s = nullptr;
+  void* scr = nullptr;
+  std::vector<void*> allocs;
+  double sor_tol = 1.0e-3;
+  int sor_max = 21;
+  double adj_tol = 1.0e-12;
+  int adj_max = 200;
+  // walls
+  double *theta0, *zeta, *l1, *l2;
+  // working state (the step runs in place on it)
+  double* S[NSTATE];
+  // record of one step
+  double *gx1[3], *fl[3], *pa, *gxn[3], *pb, *pass, *sums, *pc, *theta, *phn1f;
+  double *rho, *rhon, *rmu, *rmun, *adv[3], *advo[3], *phat, *prs[3], *sk, *tau, *vis[3];
+  double *sfst[3], *sfstn[3], *E[3], *AB[6], *wallc, *ustar[3], *un2[3], *snaps, *sorpart;
+  double *un[3], *pn, *dp, *div, *pr, *pi, *as_f, *an_f, *ap_f, *red;
+  double* csfwork;  // forward CSF chain (drop-in): G(3n) rn(12n) kap(3n) g(3n) f(3n)
+  // adjoints
+  double* lS[NSTATE];  // adjoint of the step-start state (in/out of reverse_step)
+  double *lgx[3], *lfl[3], *lrn, *ltheta, *lphn0, *lphn1, *lrho, *lrhon, *lrmu, *lrmun;
+  double *ladv[3], *ladvo[3], *lphat, *lprs[3], *lsk, *ltau, *lvis[3], *lsfst[3], *lsfstn[3];
+  double *lE[3], *lAB[6], *lwc, *lun[3], *lam[3], *lpn, *ldp, *ldiv, *lpre, *work;
+  double *gtheta0, *gzeta, *gl1, *gl2;  // parameter gradients
+  // init_bc record
+  double *ib_theta1, *ib_theta2, *ib_phi1, *ib_phi0, *ib_u, *ib_w, *ib_wallc;
+  // checkpoints
+  std::vector<double*> ckpt;
+  std::vector<double*> seg;
+  int sor_total = 0, adj_total = 0;
+};
+
+namespace {
+double* dalloc(fmf_adj* a, long n) {
+  void* p = nullptr;
+  if (!FMF_CUDA(cudaMalloc(&p, sizeof(double) * n))) {
+    set_status(FMF_ERR_NOMEM);
+    return nullptr;
+  }
+  FMF_CUDA(cudaMemsetAsync(p, 0, sizeof(double) * n, a->s));
+  a->allocs.push_back(p);
+  return (double*)p;
+}
+struct Scope {
+  explicit Scope(void* set) { scratch_set_use(set); }
+  ~Scope() { scratch_set_use(nullptr); }
+};
+void zero(fmf_adj* a, double* p, long n) { FMF_CUDA(cudaMemsetAsync(p, 0, sizeof(double) * n, a->s)); }
+void dcopy(fmf_adj* a, const double* src, double* dst, long n) {
+  FMF_CUDA(cudaMemcpyAsync(dst, src, sizeof(double) * n, cudaMemcpyDeviceToDevice, a->s));
+}
+
+// objective and its gradient on phi (slice 0): one thread per k finds the first
+// crossing phi(i,1,k) > 0.5 > phi(i+1,1,k); out[0] = J; lphi (zeroed by the caller)
+// receives dJ/dphi at the two crossing points
+__global__ void k_interface(Grid g, const double* phi, double dx, double xl, double* xk, double* lphi) {
+  const int k = 1 + (int)(blockIdx.x * blockDim.x + threadIdx.x);
+  if (k > g.nk) return;
+  double x = 0.0;
+  const double w = -1.0 / (double)g.nk;
+  for (int i = 1; i <= g.ni; ++i) {
+    const double p1 = phi[g.at(i, 1, k)], p2 = phi[g.at(i + 1, 1, k)];
+    if (p1 > 0.5 && p2 < 0.5) {
+      const double d = p2 - p1;
+      x = ((double)i - 0.5) * dx + (0.5 - p1) * dx / d - xl * 0.75;
+      if (lphi) {
+        lphi[g.at(i, 1, k)] = w * dx * (0.5 - p2) / (d * d);
+        lphi[g.at(i + 1, 1, k)] = -w * dx * (0.5 - p1) / (d * d);
+      }
+      break;
+    }
+  }
+  xk[k - 1] = x;
+}
+__global__ void k_mean_neg(const double* xk, int nk, double* out) {
+  if (threadIdx.x != 0) return;
+  double s = 0.0;
+  for (int k = 0; k < nk; ++k) s = s + xk[k];
+  out[0] = -(s / (double)nk);
+}
+
+__global__ void k_nonfinite(const double* p, long n, int* flag) {
+  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x)
+    if (!isfinite(p[t])) {
+      *flag = 1;
+      return;
+    }
+}
+// With FMF_ADJ_CHECK set in the environment: after each stage of the reverse step,
+// report on stderr the first stage that left a non-finite adjoint value.
+void check_stage(fmf_adj* a, const char* stage) {
+  static const bool on = std::getenv("FMF_ADJ_CHECK") != nullptr;
+  static bool reported = false;
+  if (!on || reported) return;
+  const long n = a->g.n;
+  int* flag = (int*)(a->sums + 6);
+  FMF_CUDA(cudaMemsetAsync(flag, 0, sizeof(int), a->s));
+  std::vector<std::pair<const char*, double*>> arrs = {
+      {"lS.u", a->lS[SU]},     {"lS.v", a->lS[SV]},   {"lS.w", a->lS[SW]},     {"lS.uo", a->lS[SUO]},
+      {"lS.p", a->lS[SP]},     {"lS.phi0", a->lS[SPHI0]}, {"lS.phi1", a->lS[SPHI1]}, {"lun0", a->lun[0]},
+      {"lun1", a->lun[1]},     {"lun2", a->lun[2]},   {"ldp", a->ldp},         {"ldiv", a->ldiv},
+      {"lphat", a->lphat},     {"lAB0", a->lAB[0]},   {"lAB1", a->lAB[1]},     {"lrmun", a->lrmun},
+      {"lrho", a->lrho},       {"lsfst0", a->lsfst[0]}, {"lphn0", a->lphn0},   {"lphn1", a->lphn1},
+      {"ltheta", a->ltheta},   {"lfl0", a->lfl[0]},   {"gtheta0", a->gtheta0}, {"gzeta", a->gzeta},
+      {"gl1", a->gl1}};
+  for (auto& e : arrs) {
+    k_nonfinite<<<256, 256, 0, a->s>>>(e.second, n, flag);
+    int h = 0;
+    FMF_CUDA(cudaMemcpyAsync(&h, flag, sizeof(int), cudaMemcpyDeviceToHost, a->s));
+    FMF_CUDA(cudaStreamSynchronize(a->s));
+    if (h) {
+      std::fprintf(stderr, "adjoint: non-finite value in %s after stage %s\n", e.first, stage);
+      reported = true;
+      return;
+    }
+  }
+}
+
+double objective(fmf_adj* a, const double* phi0, double* lphi) {
+  const Grid& g = a->g;
+  const double xl = a->prm.dx * a->prm.ni;
+  if (lphi) zero(a, lphi, g.n);
+  k_interface<<<(g.nk + 127) / 128, 128, 0, a->s>>>(g, phi0, a->prm.dx, xl, a->red + 16, lphi);
+  k_mean_neg<<<1, 32, 0, a->s>>>(a->red + 16, g.nk, a->red + 8);
+  count_launch(2);
+  double J = 0.0;
+  FMF_CUDA(cudaMemcpyAsync(&J, a->red + 8, sizeof(double), cudaMemcpyDeviceToHost, a->s));
+  FMF_CUDA(cudaStreamSynchronize(a->s));
+  return J;
+}
+}  // namespace
+
+namespace {
+// main.f90:322-366 on the working state, keeping what its adjoint reads
+void init_bc_fwd(fmf_adj* a) {
+  const fmf_params& P = a->prm;
+  const Grid& g = a->g;
+  cudaStream_t s = a->s;
+  const long n = g.n;
+  double** S = a->S;
+  op::gnbc(s, g, S[SU], S[SW], P.uwall, a->theta0, P.sigma, a->zeta, a->ib_theta1);
+  op::bnd_contact_angle(s, g, S[SPHI1], a->ib_theta1, P.dx, P.dy, P.dz);
+  op::bnd_periodic(s, g, S[SPHI1]);
+  dcopy(a, S[SPHI1], a->ib_phi1, n);
+  op::summation(s, g, S[SPHI0], S[SPHI1]);
+  fused::wall_coef(s, g, P.dy, a->l1, a->l2, S[SPHI1], a->ib_wallc);
+  op::bndu(s, g, S[SU], S[SV], S[SW], P.uwall, P.dy, a->l1, a->l2, S[SPHI1]);
+  op::bndu(s, g, S[SUO], S[SVO], S[SWO], P.uwall, P.dy, a->l1, a->l2, S[SPHI1]);
+  for (int f : {SU, SV, SW, SUO, SVO, SWO}) op::bnd_periodic(s, g, S[f]);
+  dcopy(a, S[SU], a->ib_u, n);
+  dcopy(a, S[SW], a->ib_w, n);
+  op::gnbc(s, g, S[SU], S[SW], P.uwall, a->theta0, P.sigma, a->zeta, a->ib_theta2);
+  op::bnd_contact_angle(s, g, S[SPHI0], a->ib_theta2, P.dx, P.dy, P.dz);
+  dcopy(a, S[SPHI0], a->ib_phi0, n);
+  op::bnd_periodic(s, g, S[SPHI0]);
+}
+
+// the CSF force of one field through the drop-in chain (main.f90:548-567)
+void csf_fwd(fmf_adj* a, const double* phi, double* const* f) {
+  const fmf_params& P = a->prm;
+  const Grid& g = a->g;
+  cudaStream_t s = a->s;
+  const long n = g.n;
+  const double dxi = 1.0 / P.dx, dyi = 1.0 / P.dy, dzi = 1.0 / P.dz;
+  double* G = a->csfwork;
+  double* rn = G + 3 * n;
+  double* kap = G + 15 * n;
+  double* gq = G + 18 * n;
+  static const int offs[4][3] = {{1, 1, 1}, {0, 0, 1}, {0, 1, 0}, {1, 0, 0}};
+  op::cal_grad_p2a(s, g, dxi, dyi, dzi, phi, G, G + n, G + 2 * n);
+  for (int q = 0; q < 4; ++q)
+    op::calrn(s, g, dxi, dyi, dzi, offs[q][0], offs[q][1], offs[q][2], G, G + n, G + 2 * n, rn + 3 * n * q);
+  op::calrkap(s, g, dxi, dyi, dzi, rn, rn + 3 * n, rn + 6 * n, rn + 9 * n, kap);
+  op::cal_grad_prs(s, g, dxi, dyi, dzi, phi, gq, gq + n, gq + 2 * n);
+  for (int q = 0; q < 3; ++q) op::fill(s, n, f[q], 0.0);
+  op::calfst(s, g, P.rhol, P.rhog, P.sigma, gq, gq + n, gq + 2 * n, kap, G, G + n, G + 2 * n);
+  op::sum_fst(s, g, G, G + n, G + 2 * n, f[0], f[1], f[2]);
+}
+
+// one FP64 step on a->S (main.f90:473-697), recording the intermediates
+int record_step(fmf_adj* a) {
+  const fmf_params& P = a->prm;
+  const Grid& g = a->g;
+  cudaStream_t s = a->s;
+  const long n = g.n;
+  const double dxi = 1.0 / P.dx, dyi = 1.0 / P.dy, dzi = 1.0 / P.dz, dt = P.dt;
+  double** S = a->S;
+  double *phi0 = S[SPHI0], *phi1 = S[SPHI1], *phn0 = S[SPHIN0], *phn1 = S[SPHIN1];
+  // :491-503
+  op::cal_grad_p2a(s, g, dxi, dyi, dzi, phi1, a->gx1[0], a->gx1[1], a->gx1[2]);
+  op::solphi_mthinc1(s, g, dxi, dyi, dzi, dt, P.bet_mthinc, phi1, a->gx1[0], a->gx1[1], a->gx1[2], S[SU], S[SV],
+                     S[SW], a->fl[0], a->fl[1], a->fl[2]);
+  op::solphi_mthinc2(s, g, dxi, dyi, dzi, dt, S[SU], S[SV], S[SW], a->fl[0], a->fl[1], a->fl[2], phi1, phn1);
+  dcopy(a, phn1, a->pa, n);
+  op::cal_grad_p2a(s, g, dxi, dyi, dzi, phn1, a->gxn[0], a->gxn[1], a->gxn[2]);
+  adj::mthinc3_record(s, g, dxi, dyi, dzi, P.bet_mthinc, a->gxn[0], a->gxn[1], a->gxn[2], a->pa, a->pb, a->pass);
+  op::solphi_mthinc3(s, g, dxi, dyi, dzi, P.bet_mthinc, a->gxn[0], a->gxn[1], a->gxn[2], phi1, phn1, a->sums);
+  dcopy(a, phn1, a->pc, n);
+  op::gnbc(s, g, S[SU], S[SW], P.uwall, a->theta0, P.sigma, a->zeta, a->theta);
+  op::bnd_contact_angle(s, g, phn1, a->theta, P.dx, P.dy, P.dz);
+  op::bnd_periodic(s, g, phn1);
+  dcopy(a, phn1, a->phn1f, n);
+  // :509-517
+  op::summation(s, g, phn0, phn1);
+  op::bnd_neumann(s, g, phn0);
+  op::bnd_contact_angle(s, g, phi0, a->theta, P.dx, P.dy, P.dz);
+  op::bnd_periodic(s, g, phn0);
+  // :526-541
+  op::cal_arith_mean(s, g, phi0, P.rhol, P.rhog, a->rho);
+  op::cal_arith_mean(s, g, phn0, P.rhol, P.rhog, a->rhon);
+  op::cal_arith_mean(s, g, phi0, P.rmul, P.rmug, a->rmu);
+  op::cal_arith_mean(s, g, phn0, P.rmul, P.rmug, a->rmun);
+  fused::weno5_both(s, g, dxi, dyi, dzi, S[SU], S[SV], S[SW], S[SUO], S[SVO], S[SWO], a->adv, a->advo, false);
+  op::calphat(s, g, S[SP], S[SPO], a->phat);
+  op::cal_grad_prs(s, g, dxi, dyi, dzi, a->phat, a->prs[0], a->prs[1], a->prs[2]);
+  op::calsij(s, g, dxi, dyi, dzi, S[SU], S[SV], S[SW], a->sk);
+  op::cal_tau(s, g, a->sk, a->rmu, a->tau, false);
+  op::cal_div_tensor(s, g, dxi, dyi, dzi, a->tau, a->vis[0], a->vis[1], a->vis[2]);
+  // :545-573
+  csf_fwd(a, phi1, a->sfst);
+  csf_fwd(a, phn1, a->sfstn);
+  // :579-623
+  const double* advp[3] = {a->adv[0], a->adv[1], a->adv[2]};
+  const double* advop[3] = {a->advo[0], a->advo[1], a->advo[2]};
+  const double* prsp[3] = {a->prs[0], a->prs[1], a->prs[2]};
+  const double* visp[3] = {a->vis[0], a->vis[1], a->vis[2]};
+  const double* fstp[3] = {a->sfst[0], a->sfst[1], a->sfst[2]};
+  const double* fstnp[3] = {a->sfstn[0], a->sfstn[1], a->sfstn[2]};
+  fused::src_visc_prep(s, g, dxi, dyi, dzi, dt, P.harmonic, P.grvb, P.grvp, S[SU], S[SV], S[SW], advp, advop, prsp,
+                       visp, fstp, fstnp, a->rmun, a->rho, a->rhon, a->E, a->AB, a->l1, a->l2, phi1, P.dy, a->wallc);
+  for (int q = 0; q < 3; ++q) dcopy(a, S[SU + q], a->un[q], n);
+  double err0 = 0.0;
+  int lp;
+  for (lp = 0; lp < a->sor_max; ++lp) {
+    fused::sor_iteration(s, g, dxi, dyi, dzi, P.harmonic, a->rmun, a->E, a->AB, P.uwall, a->wallc, a->un[0],
+                         a->un[1], a->un[2], a->sorpart, a->red + 4);
+    double e = 0.0;
+    FMF_CUDA(cudaMemcpyAsync(&e, a->red + 4, sizeof(double), cudaMemcpyDeviceToHost, s));
+    FMF_CUDA(cudaStreamSynchronize(s));
+    if (!std::isfinite(e)) {
+      set_status(FMF_ERR_NONFINITE);
+      break;
+    }
+    const double err = std::sqrt(e / (double)g.cells()) + 1.0e-99;
+    if (lp == 0) err0 = err;
+    if (err / err0 <= a->sor_tol) break;
+  }
+  a->sor_total += lp + 1;
+  for (int q = 0; q < 3; ++q) dcopy(a, a->un[q], a->ustar[q], n);
+  // :625-661
+  fused::wall_halo(s, g, 7, P.uwall, a->wallc, a->un[0], a->un[1], a->un[2]);
+  op::caldiv(s, g, dxi, dyi, dzi, dt, a->un[0], a->un[1], a->un[2], a->div, nullptr);
+  op::fft_forward_planes(s, g, a->div, a->pr, a->pi);
+  op::tdma_modes(s, g, P.rhog, dxi, dzi, a->as_f, a->an_f, a->ap_f, a->pr, a->pi);
+  op::fft_inverse_planes(s, g, a->pr, a->pi, a->dp);
+  op::bnd_avzero(s, g, a->dp);
+  op::bnd_neumann(s, g, a->dp);
+  op::bnd_periodic(s, g, a->dp);
+  op::corunp_explicit(s, g, P.rhog, dxi, dyi, dzi, dt, a->dp, a->phat, a->un[0], a->un[1], a->un[2], a->pn);
+  for (int q = 0; q < 3; ++q) dcopy(a, a->un[q], a->un2[q], n);
+  fused::wall_halo(s, g, 7, P.uwall, a->wallc, a->un[0], a->un[1], a->un[2]);
+  op::bnd_avzero(s, g, a->pn);
+  op::bnd_neumann(s, g, a->pn);
+  op::bnd_periodic(s, g, a->pn);
+  // :686-697 rotation (copies: the record keeps the step's inputs in the arrays above)
+  for (int q = 0; q < 3; ++q) {
+    dcopy(a, S[SU + q], S[SUO + q], n);
+    dcopy(a, a->un[q], S[SU + q], n);
+  }
+  dcopy(a, S[SP], S[SPO], n);
+  dcopy(a, a->pn, S[SP], n);
+  dcopy(a, phn0, phi0, n);
+  dcopy(a, phn1, phi1, n);
+  FMF_CUDA(cudaGetLastError());
+  return get_status();
+}
+
+void save_state(fmf_adj* a, double* dst) {
+  for (int f = 0; f < NSTATE; ++f) dcopy(a, a->S[f], dst + (long)f * a->g.n, a->g.n);
+}
+void load_state(fmf_adj* a, const double* src) {
+  for (int f = 0; f < NSTATE; ++f) dcopy(a, src + (long)f * a->g.n, a->S[f], a->g.n);
+}
+
+// Reverse of one step.  On entry lS holds the adjoint of the state after the step;
+// on exit the adjoint of the state before it.  The record of the step (record_step
+// run from that start state) must be current; the step-start state itself is passed
+// in st (NSTATE fields).
+void reverse_step(fmf_adj* a, const double* st) {
+  const fmf_params& P = a->prm;
+  const Grid& g = a->g;
+  cudaStream_t s = a->s;
+  const long n = g.n;
+  const double dxi = 1.0 / P.dx, dyi = 1.0 / P.dy, dzi = 1.0 / P.dz, dt = P.dt;
+  auto ST = [&](int f) { return st + (long)f * n; };
+  double** lS = a->lS;
+  // :686-697 rotation: u' = un, uo' = u, p' = pn, po' = p, phi' = phin' = phin
+  for (int q = 0; q < 3; ++q) {
+    dcopy(a, lS[SU + q], a->lun[q], n);
+    dcopy(a, lS[SUO + q], lS[SU + q], n);
+    zero(a, lS[SUO + q], n);
+  }
+  dcopy(a, lS[SP], a->lpn, n);
+  dcopy(a, lS[SPO], lS[SP], n);
+  zero(a, lS[SPO], n);
+  dcopy(a, lS[SPHI0], a->lphn0, n);
+  dcopy(a, lS[SPHI1], a->lphn1, n);
+  // the next step's phin adds to the same phin (it only feeds branches there: zero)
+  zero(a, lS[SPHI0], n);
+  zero(a, lS[SPHI1], n);
+  zero(a, lS[SPHIN0], n);
+  zero(a, lS[SPHIN1], n);
+  // clear the intermediate adjoints
+  for (int q = 0; q < 3; ++q) {
+    for (double* p : {a->lgx[q], a->lfl[q], a->ladv[q], a->ladvo[q], a->lprs[q], a->lvis[q], a->lsfst[q],
+                      a->lsfstn[q], a->lE[q]})
+      zero(a, p, n);
+  }
+  for (int q = 0; q < 6; ++q) zero(a, a->lAB[q], n);
+  for (double* p : {a->ltheta, a->lrho, a->lrhon, a->lrmu, a->lrmun, a->lphat, a->ldp, a->ldiv})
+    zero(a, p, n);
+  zero(a, a->lsk, 6 * n);
+  zero(a, a->ltau, 6 * n);
+  zero(a, a->lwc, 4L * (g.nk + 6) * (g.ni + 6));
+  // :655-661 pn boundary conditions, wall/halo of un
+  adj::periodic_T(s, g, a->lpn);
+  adj::neumann_T(s, g, a->lpn);
+  adj::avzero_T(s, g, a->lpn);
+  adj::wall_halo_T(s, g, 7, P.uwall, a->wallc, a->un2[0], a->un2[2], a->lun[0], a->lun[1], a->lun[2], a->lwc);
+  check_stage(a, "post-bc");
+  // :648-653 projection and pn = phat + dp
+  adj::corunp_T(s, g, P.rhog, dxi, dyi, dzi, dt, a->lun[0], a->lun[1], a->lun[2], a->lpn, a->ldp, a->lphat);
+  // :642-646 dp boundary conditions, then the Poisson solve (symmetric: the same solve)
+  adj::periodic_T(s, g, a->ldp);
+  adj::neumann_T(s, g, a->ldp);
+  adj::avzero_T(s, g, a->ldp);
+  op::fft_forward_planes(s, g, a->ldp, a->pr, a->pi);
+  op::tdma_modes(s, g, P.rhog, dxi, dzi, a->as_f, a->an_f, a->ap_f, a->pr, a->pi);
+  op::fft_inverse_planes(s, g, a->pr, a->pi, a->ldiv);
+  adj::caldiv_T(s, g, dxi, dyi, dzi, dt, a->ldiv, a->lun[0], a->lun[1], a->lun[2]);
+  check_stage(a, "poisson");
+  adj::wall_halo_T(s, g, 7, P.uwall, a->wallc, a->ustar[0], a->ustar[2], a->lun[0], a->lun[1], a->lun[2], a->lwc);
+  // :605-623 the viscous solve
+  adj::sor_replay(s, g, dxi, dyi, dzi, a->rmun, a->E, a->AB, P.uwall, a->wallc, a->ustar, a->snaps);
+  const double* lout[3] = {a->lun[0], a->lun[1], a->lun[2]};
+  a->adj_total += adj::sor_T(s, g, dxi, dyi, dzi, a->rmun, a->E, a->AB, P.uwall, a->wallc, a->ustar, a->snaps,
+                             lout, a->lam, a->lAB, a->lrmun, a->lE, a->lwc, a->adj_tol, a->adj_max, a->work);
+  check_stage(a, "sor");
+  // :579-603 momentum factors, edge viscosities, slip coefficients
+  {
+    adj::SrcArgs A;
+    A.u = ST(SU);
+    A.v = ST(SV);
+    A.w = ST(SW);
+    A.rho = a->rho;
+    A.rhon = a->rhon;
+    A.mu = a->rmun;
+    for (int q = 0; q < 3; ++q) {
+      A.E[q] = a->E[q];
+      A.adv[q] = a->adv[q];
+      A.advo[q] = a->advo[q];
+      A.prs[q] = a->prs[q];
+      A.vis[q] = a->vis[q];
+      A.fst[q] = a->sfst[q];
+      A.fstn[q] = a->sfstn[q];
+    }
+    adj::SrcAdj L;
+    for (int q = 0; q < 3; ++q) {
+      L.u[q] = lS[SU + q];
+      L.adv[q] = a->ladv[q];
+      L.advo[q] = a->ladvo[q];
+      L.prs[q] = a->lprs[q];
+      L.vis[q] = a->lvis[q];
+      L.fst[q] = a->lsfst[q];
+      L.fstn[q] = a->lsfstn[q];
+    }
+    L.rho = a->lrho;
+    L.rhon = a->lrhon;
+    L.mu = a->lrmun;
+    // diagonal edge pairs: u (exz, exy), v (eyz, exy), w (eyz, exz)
+    L.ea[0] = a->lE[1];
+    L.eb[0] = a->lE[0];
+    L.ea[1] = a->lE[2];
+    L.eb[1] = a->lE[0];
+    L.ea[2] = a->lE[2];
+    L.eb[2] = a->lE[1];
+    const double* lab[6] = {a->lAB[0], a->lAB[1], a->lAB[2], a->lAB[3], a->lAB[4], a->lAB[5]};
+    adj::src_ab_T(s, g, dxi, dyi, dzi, dt, P.grvb, P.grvp, A, lab, L);
+    const double* le[3] = {a->lE[0], a->lE[1], a->lE[2]};
+    adj::edges_T(s, g, P.harmonic, a->rmun, le, a->lrmun);
+    adj::wall_coef_T(s, g, P.dy, a->l1, a->l2, ST(SPHI1), a->lwc, lS[SPHI1], a->gl1, a->gl2);
+  check_stage(a, "src");
+  }
+  // :545-573 surface tension of phi(1) and phin(1)
+  {
+    const double* lf[3] = {a->lsfst[0], a->lsfst[1], a->lsfst[2]};
+    adj::csf_T(s, g, dxi, dyi, dzi, P.rhol, P.rhog, P.sigma, ST(SPHI1), lf, lS[SPHI1], a->work + 3 * n + 1024);
+    const double* lfn[3] = {a->lsfstn[0], a->lsfstn[1], a->lsfstn[2]};
+    adj::csf_T(s, g, dxi, dyi, dzi, P.rhol, P.rhog, P.sigma, a->phn1f, lfn, a->lphn1, a->work + 3 * n + 1024);
+  }
+  // :536-541 explicit viscous term, pressure gradient, advection
+  adj::div_tensor_T(s, g, dxi, dyi, dzi, a->lvis[0], a->lvis[1], a->lvis[2], a->ltau);
+  adj::tau_T(s, g, a->sk, a->rmu, a->ltau, a->lsk, a->lrmu);
+  adj::calsij_T(s, g, dxi, dyi, dzi, a->lsk, lS[SU], lS[SV], lS[SW]);
+  check_stage(a, "visc");
+  adj::grad_prs_T(s, g, dxi, dyi, dzi, a->lprs[0], a->lprs[1], a->lprs[2], a->lphat);
+  {
+    const Grid G = g;
+    double *lp = lS[SP], *lpo = lS[SPO];
+    const double* lph = a->lphat;
+    range3(s, -1, g.ni + 3, -2, g.nj + 3, -2, g.nk + 3, [=] __device__(int i, int j, int k) {
+      const long c = G.at(i, j, k);
+      lp[c] += 2.0 * lph[c];
+      lpo[c] -= lph[c];
+    });
+  }
+  {
+    const double* la[3] = {a->ladv[0], a->ladv[1], a->ladv[2]};
+    adj::weno_T(s, g, dxi, dyi, dzi, ST(SU), ST(SV), ST(SW), la, lS[SU], lS[SV], lS[SW]);
+    const double* lao[3] = {a->ladvo[0], a->ladvo[1], a->ladvo[2]};
+    adj::weno_T(s, g, dxi, dyi, dzi, ST(SUO), ST(SVO), ST(SWO), lao, lS[SUO], lS[SVO], lS[SWO]);
+  }
+  // :526-529 mixture properties (phi0 after its contact-angle ghosts, phin0)
+  adj::mean_T(s, g, P.rhol, P.rhog, a->lrho, lS[SPHI0]);
+  adj::mean_T(s, g, P.rmul, P.rmug, a->lrmu, lS[SPHI0]);
+  adj::mean_T(s, g, P.rhol, P.rhog, a->lrhon, a->lphn0);
+  adj::mean_T(s, g, P.rmul, P.rmug, a->lrmun, a->lphn0);
+  // :509-517
+  adj::periodic_T(s, g, a->lphn0);
+  adj::contact_angle_T(s, g, ST(SPHI0), a->theta, P.dx, P.dy, P.dz, lS[SPHI0], a->ltheta);
+  adj::neumann_T(s, g, a->lphn0);
+  adj::summation_T(s, g, a->phn1f, a->lphn0, a->lphn1);
+  check_stage(a, "means");
+  // :496-503
+  adj::periodic_T(s, g, a->lphn1);
+  adj::contact_angle_T(s, g, a->pc, a->theta, P.dx, P.dy, P.dz, a->lphn1, a->ltheta);
+  adj::gnbc_T(s, g, ST(SU), ST(SW), P.uwall, a->theta0, P.sigma, a->zeta, a->ltheta, lS[SU], lS[SW], a->gtheta0,
+              a->gzeta);
+  check_stage(a, "gnbc");
+  adj::mthinc3_T(s, g, a->pb, a->pass, a->sums, a->lphn1, lS[SPHI1], a->sums + 4);
+  adj::mthinc2_T(s, g, dxi, dyi, dzi, dt, ST(SU), ST(SV), ST(SW), a->fl[0], a->fl[1], a->fl[2], ST(SPHI1), a->pa,
+                 a->lphn1, lS[SPHI1], lS[SU], lS[SV], lS[SW], a->lfl[0], a->lfl[1], a->lfl[2], a->lpre);
+  adj::mthinc1_T(s, g, dxi, dyi, dzi, dt, P.bet_mthinc, ST(SPHI1), a->gx1[0], a->gx1[1], a->gx1[2], ST(SU), ST(SV),
+                 ST(SW), a->lfl[0], a->lfl[1], a->lfl[2], lS[SPHI1], a->lrn, lS[SU], lS[SV], lS[SW]);
+  adj::rn_avg_T(s, g, a->lrn, a->lgx[0], a->lgx[1], a->lgx[2]);
+  check_stage(a, "mthinc");
+  adj::grad_p2a_T(s, g, dxi, dyi, dzi, a->lgx[0], a->lgx[1], a->lgx[2], lS[SPHI1]);
+  FMF_CUDA(cudaGetLastError());
+}
+
+// reverse of init_bc_fwd; on entry lS = adjoint of the state it produced
+void reverse_init_bc(fmf_adj* a) {
+  const fmf_params& P = a->prm;
+  const Grid& g = a->g;
+  cudaStream_t s = a->s;
+  const long n = g.n;
+  double** lS = a->lS;
+  zero(a, a->ltheta, n);
+  zero(a, a->lwc, 4L * (g.nk + 6) * (g.ni + 6));
+  adj::periodic_T(s, g, lS[SPHI0]);
+  adj::contact_angle_T(s, g, a->ib_phi0, a->ib_theta2, P.dx, P.dy, P.dz, lS[SPHI0], a->ltheta);
+  adj::gnbc_T(s, g, a->ib_u, a->ib_w, P.uwall, a->theta0, P.sigma, a->zeta, a->ltheta, lS[SU], lS[SW], a->gtheta0,
+              a->gzeta);
+  zero(a, a->ltheta, n);
+  for (int f : {SU, SV, SW, SUO, SVO, SWO}) adj::periodic_T(s, g, lS[f]);
+  // bndu = wall ghosts, x halos (u shifted), z halos (w shifted); the velocity
+  // ghosts read the initial (zero) wall rows
+  for (int base : {SUO, SU}) {
+    adj::halo_z_T(s, g, 3, lS[base], lS[base + 1], lS[base + 2]);
+    adj::halo_x_T(s, g, 6, lS[base], lS[base + 1], lS[base + 2]);
+    adj::wall_T(s, g, P.uwall, a->ib_wallc, a->S[base], a->S[base + 2], lS[base], lS[base + 1], lS[base + 2],
+                a->lwc);
+  }
+  adj::wall_coef_T(s, g, P.dy, a->l1, a->l2, a->ib_phi1, a->lwc, lS[SPHI1], a->gl1, a->gl2);
+  adj::summation_T(s, g, a->ib_phi1, lS[SPHI0], lS[SPHI1]);
+  adj::periodic_T(s, g, lS[SPHI1]);
+  adj::contact_angle_T(s, g, a->ib_phi1, a->ib_theta1, P.dx, P.dy, P.dz, lS[SPHI1], a->ltheta);
+  adj::gnbc_T(s, g, a->S[SU], a->S[SW], P.uwall, a->theta0, P.sigma, a->zeta, a->ltheta, lS[SU], lS[SW],
+              a->gtheta0, a->gzeta);
+  FMF_CUDA(cudaGetLastError());
+}
+
+void upload_inputs(fmf_adj* a, const double* const* st, const double* th, const double* ze, const double* l1,
+                   const double* l2) {
+  const size_t b = sizeof(double) * a->g.n;
+  for (int f = 0; f < NSTATE; ++f) FMF_CUDA(cudaMemcpyAsync(a->S[f], st[f], b, cudaMemcpyHostToDevice, a->s));
+  FMF_CUDA(cudaMemcpyAsync(a->theta0, th, b, cudaMemcpyHostToDevice, a->s));
+  FMF_CUDA(cudaMemcpyAsync(a->zeta, ze, b, cudaMemcpyHostToDevice, a->s));
+  FMF_CUDA(cudaMemcpyAsync(a->l1, l1, b, cudaMemcpyHostToDevice, a->s));
+  FMF_CUDA(cudaMemcpyAsync(a->l2, l2, b, cudaMemcpyHostToDevice, a->s));
+}
+}  // namespace
+
+extern "C" {
+
+int fmf_adj_create(const fmf_params* prm, fmf_adj** out) {
+  if (!prm || !out) return FMF_ERR_ARG;
+  auto p2 = [](int v) { return v >= 4 && (v & (v - 1)) == 0; };
+  if (!p2(prm->ni) || !p2(prm->nj) || !p2(prm->nk) || prm->ni < 16) return FMF_ERR_ARG;
+  fmf_adj* a = new fmf_adj();
+  a->prm = *prm;
+  a->g = Grid(prm->ni, prm->nj, prm->nk);
+  a->scr = scratch_set_create();
+  if (!FMF_CUDA(cudaStreamCreateWithFlags(&a->s, cudaStreamNonBlocking))) {
+    delete a;
+    return FMF_ERR_CUDA;
+  }
+  const long n = a->g.n;
+  for (double** p : {&a->theta0, &a->zeta, &a->l1, &a->l2}) *p = dalloc(a, n);
+  for (int f = 0; f < NSTATE; ++f) a->S[f] = dalloc(a, n);
+  for (int q = 0; q < 3; ++q) {
+    for (double** p : {&a->gx1[q], &a->fl[q], &a->gxn[q], &a->adv[q], &a->advo[q], &a->prs[q], &a->vis[q],
+                       &a->sfst[q], &a->sfstn[q], &a->E[q], &a->ustar[q], &a->un2[q], &a->un[q], &a->lgx[q],
+                       &a->lfl[q], &a->ladv[q], &a->ladvo[q], &a->lprs[q], &a->lvis[q], &a->lsfst[q],
+                       &a->lsfstn[q], &a->lE[q], &a->lun[q], &a->lam[q]})
+      *p = dalloc(a, n);
+  }
+  for (int q = 0; q < 6; ++q) {
+    a->AB[q] = dalloc(a, n);
+    a->lAB[q] = dalloc(a, n);
+  }
+  for (double** p : {&a->pa, &a->pb, &a->pass, &a->pc, &a->theta, &a->phn1f, &a->rho, &a->rhon, &a->rmu, &a->rmun,
+                     &a->phat, &a->pn, &a->dp, &a->div, &a->ltheta, &a->lphn0, &a->lphn1, &a->lrho, &a->lrhon,
+                     &a->lrmu, &a->lrmun, &a->lphat, &a->lpn, &a->ldp, &a->ldiv, &a->lpre, &a->gtheta0, &a->gzeta,
+                     &a->gl1, &a->gl2, &a->ib_theta1, &a->ib_theta2, &a->ib_phi1, &a->ib_phi0, &a->ib_u, &a->ib_w})
+    *p = dalloc(a, n);
+  a->sums = dalloc(a, 8);
+  a->red = dalloc(a, 64 + prm->nk);
+  a->sk = dalloc(a, 6 * n);
+  a->tau = dalloc(a, 6 * n);
+  a->lsk = dalloc(a, 6 * n);
+  a->ltau = dalloc(a, 6 * n);
+  a->lrn = dalloc(a, 3 * n);
+  const long nwc = 4L * (prm->nk + 6) * (prm->ni + 6);
+  a->wallc = dalloc(a, nwc);
+  a->lwc = dalloc(a, nwc);
+  a->ib_wallc = dalloc(a, nwc);
+  a->snaps = dalloc(a, 39 * n);
+  a->sorpart = dalloc(a, fused::sor_parts(a->g));
+  a->csfwork = dalloc(a, 21 * n);
+  a->work = dalloc(a, 3 * n + 1024 + 42 * n);
+  for (int f = 0; f < NSTATE; ++f) a->lS[f] = dalloc(a, n);
+  const long nm = a->g.cells();
+  a->pr = dalloc(a, nm);
+  a->pi = dalloc(a, nm);
+  const int NJ = prm->nj;
+  a->as_f = dalloc(a, NJ + 6);
+  a->an_f = dalloc(a, NJ + 6);
+  a->ap_f = dalloc(a, NJ + 6);
+  if (get_status()) {
+    fmf_adj_destroy(a);
+    return take_status();
+  }
+  // cal_coef_prs.f:28-54 + cal_coef_solp_fft.f:25-39, as fmf_ctx_create
+  std::vector<double> as(NJ + 6, 0.0), an(NJ + 6, 0.0), ap(NJ + 6, 0.0);
+  const double dyinv = 1.0 / prm->dy;
+  for (int j = 1; j <= NJ; ++j) {
+    as[j + 2] = dyinv * dyinv / prm->rhog;
+    an[j + 2] = dyinv * dyinv / prm->rhog;
+    ap[j + 2] = as[j + 2] + an[j + 2];
+  }
+  ap[3] = ap[3] - as[3];
+  as[3] = 0.0;
+  ap[NJ + 2] = ap[NJ + 2] - an[NJ + 2];
+  an[NJ + 2] = 0.0;
+  FMF_CUDA(cudaMemcpyAsync(a->as_f, as.data(), sizeof(double) * (NJ + 6), cudaMemcpyHostToDevice, a->s));
+  FMF_CUDA(cudaMemcpyAsync(a->an_f, an.data(), sizeof(double) * (NJ + 6), cudaMemcpyHostToDevice, a->s));
+  FMF_CUDA(cudaMemcpyAsync(a->ap_f, ap.data(), sizeof(double) * (NJ + 6), cudaMemcpyHostToDevice, a->s));
+  FMF_CUDA(cudaStreamSynchronize(a->s));
+  *out = a;
+  return take_status();
+}
+
+int fmf_adj_destroy(fmf_adj* a) {
+  if (!a) return 0;
+  if (a->s) cudaStreamSynchronize(a->s);
+  for (double* p : a->ckpt) cudaFree(p);
+  for (double* p : a->seg) cudaFree(p);
+  for (void* p : a->allocs) cudaFree(p);
+  scratch_set_destroy(a->scr);
+  if (a->s) cudaStreamDestroy(a->s);
+  delete a;
+  return take_status();
+}
+
+int fmf_adj_set_solver(fmf_adj* a, double sor_tol, int sor_max, double adj_tol, int adj_max) {
+  if (!a || !(sor_tol > 0.0) || sor_max < 1 || !(adj_tol > 0.0) || adj_max < 1) return FMF_ERR_ARG;
+  a->sor_tol = sor_tol;
+  a->sor_max = sor_max;
+  a->adj_tol = adj_tol;
+  a->adj_max = adj_max;
+  return 0;
+}
+
+int fmf_adj_forward(fmf_adj* a, int K, const double* const* state0, const double* theta0, const double* zeta,
+                    const double* l1, const double* l2, double* J, double* const* state_out) {
+  if (!a || K < 0 || !state0 || !theta0 || !zeta || !l1 || !l2 || !J) return FMF_ERR_ARG;
+  Scope scope(a->scr);
+  upload_inputs(a, state0, theta0, zeta, l1, l2);
+  init_bc_fwd(a);
+  a->sor_total = 0;
+  for (int t = 0; t < K && !get_status(); ++t) record_step(a);
+  *J = objective(a, a->S[SPHI0], nullptr);
+  if (state_out)
+    for (int f = 0; f < NSTATE; ++f)
+      FMF_CUDA(cudaMemcpyAsync(state_out[f], a->S[f], sizeof(double) * a->g.n, cudaMemcpyDeviceToHost, a->s));
+  FMF_CUDA(cudaStreamSynchronize(a->s));
+  return take_status();
+}
+
+int fmf_adj_rollout(fmf_adj* a, int K, int every, const double* const* state0, const double* theta0,
+                    const double* zeta, const double* l1, const double* l2, double* J, double* g_theta0,
+                    double* g_zeta, double* g_l1, double* g_l2, double* g_phi) {
+  if (!a || K < 1 || !state0 || !theta0 || !zeta || !l1 || !l2 || !J) return FMF_ERR_ARG;
+  Scope scope(a->scr);
+  const long n = a->g.n;
+  if (every <= 0) every = (int)std::ceil(std::sqrt((double)K));
+  const int nck = (K + every - 1) / every;
+  // checkpoint and segment buffers (grown on demand)
+  while ((int)a->ckpt.size() < nck) {
+    void* p = nullptr;
+    if (!FMF_CUDA(cudaMalloc(&p, sizeof(double) * NSTATE * n))) return take_status();
+    a->ckpt.push_back((double*)p);
+  }
+  while ((int)a->seg.size() < every) {
+    void* p = nullptr;
+    if (!FMF_CUDA(cudaMalloc(&p, sizeof(double) * NSTATE * n))) return take_status();
+    a->seg.push_back((double*)p);
+  }
+  upload_inputs(a, state0, theta0, zeta, l1, l2);
+  for (double* p : {a->gtheta0, a->gzeta, a->gl1, a->gl2}) zero(a, p, n);
+  // forward with checkpoints
+  init_bc_fwd(a);
+  // keep the init_bc inputs' velocity wall rows (zero initial state) for its reverse
+  a->sor_total = 0;
+  a->adj_total = 0;
+  for (int t = 0; t < K && !get_status(); ++t) {
+    if (t % every == 0) save_state(a, a->ckpt[t / every]);
+    record_step(a);
+  }
+  if (get_status()) return take_status();
+  *J = objective(a, a->S[SPHI0], a->lS[SPHI0]);
+  for (int f = 0; f < NSTATE; ++f)
+    if (f != SPHI0) zero(a, a->lS[f], n);
+  // reverse, segment by segment
+  for (int c = nck - 1; c >= 0 && !get_status(); --c) {
+    const int t0 = c * every, t1 = std::min(K, t0 + every);
+    load_state(a, a->ckpt[c]);
+    for (int t = t0; t < t1; ++t) {
+      save_state(a, a->seg[t - t0]);
+      if (t + 1 < t1) record_step(a);
+    }
+    for (int t = t1 - 1; t >= t0 && !get_status(); --t) {
+      load_state(a, a->seg[t - t0]);
+      record_step(a);
+      reverse_step(a, a->seg[t - t0]);
+    }
+  }
+  // the start-up pass: recompute its record from the uploaded state
+  for (int f = 0; f < NSTATE; ++f)
+    FMF_CUDA(cudaMemcpyAsync(a->S[f], state0[f], sizeof(double) * n, cudaMemcpyHostToDevice, a->s));
+  init_bc_fwd(a);
+  for (int f = 0; f < NSTATE; ++f)
+    FMF_CUDA(cudaMemcpyAsync(a->S[f], state0[f], sizeof(double) * n, cudaMemcpyHostToDevice, a->s));
+  reverse_init_bc(a);
+  const size_t b = sizeof(double) * n;
+  if (g_theta0) FMF_CUDA(cudaMemcpyAsync(g_theta0, a->gtheta0, b, cudaMemcpyDeviceToHost, a->s));
+  if (g_zeta) FMF_CUDA(cudaMemcpyAsync(g_zeta, a->gzeta, b, cudaMemcpyDeviceToHost, a->s));
+  if (g_l1) FMF_CUDA(cudaMemcpyAsync(g_l1, a->gl1, b, cudaMemcpyDeviceToHost, a->s));
+  if (g_l2) FMF_CUDA(cudaMemcpyAsync(g_l2, a->gl2, b, cudaMemcpyDeviceToHost, a->s));
+  if (g_phi) FMF_CUDA(cudaMemcpyAsync(g_phi, a->lS[SPHI1], b, cudaMemcpyDeviceToHost, a->s));
+  FMF_CUDA(cudaStreamSynchronize(a->s));
+  return take_status();
+}
+
+int fmf_adj_iterations(fmf_adj* a, int* sor_total, int* adjoint_total) {
+  if (!a) return FMF_ERR_ARG;
+  if (sor_total) *sor_total = a->sor_total;
+  if (adjoint_total) *adjoint_total = a->adj_total;
+  return 0;
+}
+
+}  // extern "C"

@@ -1,0 +1,311 @@
+// adj_transport.cu -- adjoints of the MTHINC transport (solphi_mthinc1/2/3).
+//
+// solphi_mthinc1: a band cell's Newton offset d(n, phi) is differentiated through
+// the ten iterations the forward pass runs (forward-mode numbers seeded with the
+// unit normal and phi), and each outflow-face flux through its 8-point Gauss sum
+// (seeded with n, d and the swept fraction vd).  Bulk cells: flux = u phi00 dt/dx
+// with phi00 snapped (zero derivative) inside eps_trunc of 0 or 1.
+#include "adj.cuh"
+#include "ops.cuh"
+
+namespace fmf {
+namespace adj {
+
+namespace {
+struct MC {
+  double gp1, gp2, dcellinv, eps_mthinc, eps_trunc;
+};
+MC mconst(double dxi, double dyi, double dzi, double bet) {
+  MC m;
+  const double dx = 1.0 / dxi, dy = 1.0 / dyi, dz = 1.0 / dzi;
+  m.gp1 = -0.5 / std::sqrt(3.0);
+  m.gp2 = 0.5 / std::sqrt(3.0);
+  m.dcellinv = 1.0 / std::sqrt((dx * dx + dy * dy + dz * dz) / 3.0);
+  const double ch = std::cosh(-bet * 1.5);
+  m.eps_mthinc = bet / (2.0 * (ch * ch));
+  m.eps_trunc = 0.5 * (std::tanh(-bet * 2.5) + 1.0);
+  return m;
+}
+__device__ __forceinline__ double avg8(const double* p, long c, long X, long Y, long Z) {
+  return (p[c - X - Y - Z] + p[c - Y - Z] + p[c - X - Z] + p[c - Z] + p[c - X - Y] + p[c - Y] + p[c - X] + p[c]) *
+         0.125;
+}
+// w / (1 + exp(x)) with the derivative taken as 0 where exp(x) overflows (the
+// forward value is 0 there too)
+template <int N>
+__device__ __forceinline__ Dual<N> sigw(const Dual<N>& w, const Dual<N>& x) {
+  if (x.v > 700.0) return Dual<N>(0.0);
+  const double e = exp(x.v), s = 1.0 / (1.0 + e), ds = -e * s * s;
+  Dual<N> r(w.v * s);
+  for (int t = 0; t < N; ++t) r.d[t] = w.d[t] * s + w.v * ds * x.d[t];
+  return r;
+}
+// 1 / cosh(x)^2, 0 (with zero derivative) where cosh(x)^2 overflows
+template <int N>
+__device__ __forceinline__ Dual<N> sech2(const Dual<N>& x) {
+  if (fabs(x.v) > 350.0) return Dual<N>(0.0);
+  const double c = cosh(x.v), v = 1.0 / (c * c), dv = -2.0 * tanh(x.v) * v;
+  Dual<N> r(v);
+  for (int t = 0; t < N; ++t) r.d[t] = dv * x.d[t];
+  return r;
+}
+// the 8 Gauss-point offsets of mthinc_x.h for positions (x1,x2) (y1,y2) (z1,z2)
+template <class T>
+__device__ void gauss8(const T& nx, const T& ny, const T& nz, const T& xa, const T& xb, const T& ya, const T& yb,
+                       const T& za, const T& zb, T* a) {
+  const T x1 = nx * xa, x2 = nx * xb, y1 = ny * ya, y2 = ny * yb, z1 = nz * za, z2 = nz * zb;
+  a[0] = x1 + y1 + z1;
+  a[1] = x2 + y1 + z1;
+  a[2] = x1 + y2 + z1;
+  a[3] = x2 + y2 + z1;
+  a[4] = x1 + y1 + z2;
+  a[5] = x2 + y1 + z2;
+  a[6] = x1 + y2 + z2;
+  a[7] = x2 + y2 + z2;
+}
+template <class T>
+__device__ T sig8(const T* a, const T& wght, double bet, const T& d) {
+  const double m = -2.0 * bet;
+  T s = sigw(wght, (a[0] + d) * m);
+  for (int t = 1; t < 8; ++t) s = s + sigw(wght, (a[t] + d) * m);
+  return s;
+}
+// Newton offset of solphi_mthinc1.f:161-176 (10 iterations from d = 0)
+template <class T>
+__device__ T newton_d(const T& nx, const T& ny, const T& nz, const T& ph, const MC& M, double bet) {
+  T a[8];
+  const T g1(M.gp1), g2(M.gp2);
+  gauss8(nx, ny, nz, g1, g2, g1, g2, g1, g2, a);
+  T d(0.0);
+  for (int it = 0; it < 10; ++it) {
+    const T f = sig8(a, T(0.125), bet, d) - ph;
+    T acc(0.0);
+    for (int t = 0; t < 8; ++t) acc = acc + sech2((a[t] + d) * bet) * 0.125;
+    const T df = acc * (0.5 * bet);
+    d = d - f * df / (df * df + 1.0e-99);
+  }
+  return d;
+}
+// flux through one outflow face: dir 0/1/2, side 0 = the lower face (velocity < 0),
+// side 1 = the upper face (velocity > 0)
+template <class T>
+__device__ T face_flux(int dir, int side, const T& nx, const T& ny, const T& nz, const T& d, const T& vd,
+                       const MC& M, double bet) {
+  T st, en;
+  if (side == 0) {
+    st = T(-0.5);
+    en = -0.5 - vd;
+  } else {
+    st = 0.5 - vd;
+    en = T(0.5);
+  }
+  const T a1 = (st + en) * 0.5 + (-st + en) * M.gp1, a2 = (st + en) * 0.5 + (-st + en) * M.gp2;
+  const T g1(M.gp1), g2(M.gp2);
+  T a[8];
+  if (dir == 0) gauss8(nx, ny, nz, a1, a2, g1, g2, g1, g2, a);
+  else if (dir == 1) gauss8(nx, ny, nz, g1, g2, a1, a2, g1, g2, a);
+  else gauss8(nx, ny, nz, g1, g2, g1, g2, a1, a2, a);
+  return sig8(a, vd * 0.125, bet, d);
+}
+}  // namespace
+
+void mthinc1_T(cudaStream_t s, const Grid& g, double dxi, double dyi, double dzi, double dt, double bet,
+               const double* phi, const double* gx, const double* gy, const double* gz, const double* u,
+               const double* v, const double* w, const double* lfx, const double* lfy, const double* lfz,
+               double* lphi, double* lrn, double* lu, double* lv, double* lw) {
+  const Grid G = g;
+  const MC M = mconst(dxi, dyi, dzi, bet);
+  const long n = g.n;
+  range3(s, 0, g.ni + 1, 0, g.nj + 1, 0, g.nk + 1, [=] __device__(int i, int j, int k) {
+    const long X = 1, Y = G.sy, Z = G.sz;
+    const long c = G.at(i, j, k);
+    // faces in the order x-, x+, y-, y+, z-, z+: flux adjoints, velocities, scales
+    const long fo[6] = {c - X, c, c - Y, c, c - Z, c};
+    const double* lf[3] = {lfx, lfy, lfz};
+    const double* vel[3] = {u, v, w};
+    double* lvel[3] = {lu, lv, lw};
+    const double sc[3] = {dt * dxi, dt * dyi, dt * dzi};
+    double L[6], U[6];
+    bool any = false;
+    for (int f = 0; f < 6; ++f) {
+      L[f] = lf[f / 2][fo[f]];
+      U[f] = vel[f / 2][fo[f]];
+      any = any || L[f] != 0.0;
+    }
+    lrn[c] = 0.0;
+    lrn[c + n] = 0.0;
+    lrn[c + 2 * n] = 0.0;
+    if (!any) return;
+    double rnx = avg8(gx, c, X, Y, Z), rny = avg8(gy, c, X, Y, Z), rnz = avg8(gz, c, X, Y, Z);
+    const double q00 = sqrt(rnx * rnx + rny * rny + rnz * rnz);
+    if (q00 <= M.eps_mthinc * M.dcellinv) {
+      double phi00 = phi[c];
+      double dsnap = 1.0;
+      if (phi00 <= M.eps_trunc) {
+        phi00 = 0.0;
+        dsnap = 0.0;
+      }
+      if (1.0 - phi00 <= M.eps_trunc) {
+        phi00 = 1.0;
+        dsnap = 0.0;
+      }
+      double lp = 0.0;
+      for (int f = 0; f < 6; ++f) {
+        // owner of the face: the lower face if its velocity <= 0, the upper one if > 0
+        const bool own = (f & 1) ? (U[f] > 0.0) : (U[f] <= 0.0);
+        if (!own || L[f] == 0.0) continue;
+        aadd(lvel[f / 2] + fo[f], L[f] * phi00 * sc[f / 2]);
+        lp += L[f] * U[f] * sc[f / 2];
+      }
+      aadd(lphi + c, lp * dsnap);
+      return;
+    }
+    const double coef = 1.0 / q00;
+    const double nx = rnx * coef, ny = rny * coef, nz = rnz * coef;
+    using D4 = Dual<4>;
+    const D4 dd = newton_d(D4::var(nx, 0), D4::var(ny, 1), D4::var(nz, 2), D4::var(phi[c], 3), M, bet);
+    double ln[3] = {0.0, 0.0, 0.0}, ld = 0.0;
+    using D5 = Dual<5>;
+    for (int f = 0; f < 6; ++f) {
+      const bool own = (f & 1) ? (U[f] > 0.0) : (U[f] < 0.0);
+      if (!own || L[f] == 0.0) continue;
+      const double vd = U[f] * sc[f / 2];
+      const D5 fl = face_flux(f / 2, f & 1, D5::var(nx, 0), D5::var(ny, 1), D5::var(nz, 2), D5::var(dd.v, 3),
+                              D5::var(vd, 4), M, bet);
+      for (int q = 0; q < 3; ++q) ln[q] += L[f] * fl.d[q];
+      ld += L[f] * fl.d[3];
+      aadd(lvel[f / 2] + fo[f], L[f] * fl.d[4] * sc[f / 2]);
+    }
+    for (int q = 0; q < 3; ++q) ln[q] += ld * dd.d[q];
+    aadd(lphi + c, ld * dd.d[3]);
+    // n = r/|r|: lr = (ln - n (n.ln)) / |r|
+    const double dot = ln[0] * nx + ln[1] * ny + ln[2] * nz;
+    lrn[c] = (ln[0] - nx * dot) * coef;
+    lrn[c + n] = (ln[1] - ny * dot) * coef;
+    lrn[c + 2 * n] = (ln[2] - nz * dot) * coef;
+  });
+}
+
+// cell (i,j,k) averages the vertex gradients (i-1..i, j-1..j, k-1..k); gather over
+// the cells 0..n+1 that use vertex v
+void rn_avg_T(cudaStream_t s, const Grid& g, const double* lrn, double* lgx, double* lgy, double* lgz) {
+  const Grid G = g;
+  const long n = g.n;
+  range3(s, -2, g.ni + 2, -2, g.nj + 2, -2, g.nk + 2, [=] __device__(int a, int b, int e) {
+    double sx = 0.0, sy = 0.0, sz = 0.0;
+    for (int dc = 0; dc < 2; ++dc)
+      for (int db = 0; db < 2; ++db)
+        for (int da = 0; da < 2; ++da) {
+          const int i = a + da, j = b + db, k = e + dc;
+          if (i < 0 || i > G.ni + 1 || j < 0 || j > G.nj + 1 || k < 0 || k > G.nk + 1) continue;
+          const long c = G.at(i, j, k);
+          sx += lrn[c];
+          sy += lrn[c + n];
+          sz += lrn[c + 2 * n];
+        }
+    const long v = G.at(a, b, e);
+    lgx[v] += 0.125 * sx;
+    lgy[v] += 0.125 * sy;
+    lgz[v] += 0.125 * sz;
+  });
+}
+
+void mthinc2_T(cudaStream_t s, const Grid& g, double dxi, double dyi, double dzi, double dt, const double* u,
+               const double* v, const double* w, const double* fx, const double* fy, const double* fz,
+               const double* phi, const double* phin, double* lphin, double* lphi, double* lu, double* lv,
+               double* lw, double* lfx, double* lfy, double* lfz, double* lpre) {
+  const Grid G = g;
+  (void)phin;
+  // lpre = adjoint of the unclipped value (zero outside the interior)
+  range3(s, -2, g.ni + 3, -2, g.nj + 3, -2, g.nk + 3, [=] __device__(int i, int j, int k) {
+    const long X = 1, Y = G.sy, Z = G.sz;
+    const long c = G.at(i, j, k);
+    if (i < 1 || i > G.ni || j < 1 || j > G.nj || k < 1 || k > G.nk) {
+      lpre[c] = 0.0;
+      return;
+    }
+    const double div00 = (-u[c - X] + u[c]) * dxi + (-v[c - Y] + v[c]) * dyi + (-w[c - Z] + w[c]) * dzi;
+    const double p = phi[c] * (1.0 + dt * div00) + fx[c - X] - fx[c] + fy[c - Y] - fy[c] + fz[c - Z] - fz[c];
+    const double L = (p >= 0.0 && p <= 1.0) ? lphin[c] : 0.0;
+    lphin[c] = 0.0;
+    lpre[c] = L;
+    lphi[c] += L * (1.0 + dt * div00);
+  });
+  range3(s, -2, g.ni + 2, -2, g.nj + 2, -2, g.nk + 2, [=] __device__(int i, int j, int k) {
+    const long X = 1, Y = G.sy, Z = G.sz;
+    const long c = G.at(i, j, k);
+    const double p0 = lpre[c], px = lpre[c + X], py = lpre[c + Y], pz = lpre[c + Z];
+    lu[c] += dt * dxi * (phi[c] * p0 - phi[c + X] * px);
+    lv[c] += dt * dyi * (phi[c] * p0 - phi[c + Y] * py);
+    lw[c] += dt * dzi * (phi[c] * p0 - phi[c + Z] * pz);
+    lfx[c] += px - p0;
+    lfy[c] += py - p0;
+    lfz[c] += pz - p0;
+  });
+}
+
+// ---- solphi_mthinc3 -----------------------------------------------------------
+// Record: pb = pa after the band-test snap and the clip, pass = 1 where pb moved
+// with pa (not snapped, not clipped).
+void mthinc3_record(cudaStream_t s, const Grid& g, double dxi, double dyi, double dzi, double bet, const double* gx,
+                    const double* gy, const double* gz, const double* pa, double* pb, double* pass) {
+  const Grid G = g;
+  const MC M = mconst(dxi, dyi, dzi, bet);
+  range3(s, 1, g.ni, 1, g.nj, 1, g.nk, [=] __device__(int i, int j, int k) {
+    const long X = 1, Y = G.sy, Z = G.sz;
+    const long c = G.at(i, j, k);
+    const double rnx = avg8(gx, c, X, Y, Z), rny = avg8(gy, c, X, Y, Z), rnz = avg8(gz, c, X, Y, Z);
+    const double q00 = sqrt(rnx * rnx + rny * rny + rnz * rnz);
+    double p = pa[c];
+    double m = 1.0;
+    if (q00 <= M.eps_mthinc * M.dcellinv) {
+      if (p <= M.eps_trunc) {
+        p = 0.0;
+        m = 0.0;
+      }
+      if (1.0 - p <= M.eps_trunc) {
+        p = 1.0;
+        m = 0.0;
+      }
+    }
+    if (p > 1.0 || p < 0.0) m = 0.0;
+    pb[c] = fmax(fmin(p, 1.0), 0.0);
+    pass[c] = m;
+  });
+}
+
+// sums[0..2] = (sum phi, sum pb, sum pb^2 (1-pb)) as left by op::solphi_mthinc3;
+// scal: device scratch of >= 4 doubles
+void mthinc3_T(cudaStream_t s, const Grid& g, const double* pb, const double* pass, const double* sums,
+               double* lphin, double* lphi, double* scal) {
+  const Grid G = g;
+  // lambda_off = sum lc * pass_c * pb^2 (1-pb), pass_c: the final clip did not bind
+  reduce_interior<1>(
+      s, g,
+      [=] __device__(int i, int j, int k, double* r) {
+        const long c = G.at(i, j, k);
+        const double off = (sums[0] - sums[1]) / (sums[2] + 1.0e-99);
+        const double p = pb[c];
+        const double gp = p * p * (1.0 - p);
+        const double q = p + off * gp;
+        r[0] = (q >= 0.0 && q <= 1.0) ? lphin[c] * gp : 0.0;
+      },
+      scal, 10);
+  range3(s, 1, g.ni, 1, g.nj, 1, g.nk, [=] __device__(int i, int j, int k) {
+    const long c = G.at(i, j, k);
+    const double den = sums[2] + 1.0e-99;
+    const double off = (sums[0] - sums[1]) / den;
+    const double loff = scal[0];
+    const double lS1 = loff / den, lS2 = -loff / den, lDn = -loff * off / den;
+    const double p = pb[c];
+    const double gp = p * p * (1.0 - p), dg = 2.0 * p - 3.0 * p * p;
+    const double q = p + off * gp;
+    const double lc = (q >= 0.0 && q <= 1.0) ? lphin[c] : 0.0;
+    const double lb = lc * (1.0 + off * dg) + lS2 + lDn * dg;
+    lphin[c] = lb * pass[c];
+    lphi[c] += lS1;
+  });
+}
+
+}  // namespace adj
+}  // namespace fmf

@@ -37,6 +37,9 @@ void src_visc_prep(cudaStream_t s, const Grid& g, double dxinv, double dyinv, do
                    const double* const* vis, const double* const* fst, const double* const* fstn, const double* mu,
                    const double* rho, const double* rhon, double* const* E, double* const* AB, const double* l1,
                    const double* l2, const double* phi, double dy, double* wallc);
+// the Navier-slip coefficients wallc alone (as src_visc_prep computes them)
+void wall_coef(cudaStream_t s, const Grid& g, double dy, const double* l1, const double* l2, const double* phi,
+               double* wallc);
 // bndu followed by bnd_periodic of the components whose bit is set in `normal`.
 void wall_halo(cudaStream_t s, const Grid& g, int normal, double uwall, const double* wallc, double* un, double* vn,
                double* wn);

@@ -689,6 +689,12 @@ void src_visc_prep(cudaStream_t s, const Grid& g, double dxinv, double dyinv, do
                   grvp, mu, rho, rhon, E, F3{{nullptr, nullptr, nullptr}}, out, l1, l2, phi, dy, wallc);
 }
 
+void wall_coef(cudaStream_t s, const Grid& g, double dy, const double* l1, const double* l2, const double* phi,
+               double* wallc) {
+  k_wall_coef<<<wall_grid(g), kB, 0, s>>>(g, dy, l1, l2, phi, wallc);
+  count_launch();
+}
+
 void wall_halo(cudaStream_t s, const Grid& g, int normal, double uwall, const double* wallc, double* un, double* vn,
                double* wn) {
   k_wall<<<wall_grid(g), kB, 0, s>>>(g, uwall, wallc, un, vn, wn);

@@ -320,6 +320,33 @@ int fmf_ctx_time_stage(fmf_ctx* ctx, int stage, int reps, float* ms);
  * Measurement support; no counterpart in the reference. */
 int fmf_measure_fma_rate(int fp64, double* tflops);
 
+/* ===================================================================== part 4
+ * Adjoint of the K-step rollout.  No counterpart in the reference (it has no
+ * derivatives); the objective is its find_interface_positions_lower
+ * (find_interface_positions_lower.f90:15-32): J = -mean over k of the first
+ * phi(i,1,k) > 0.5 > phi(i+1,1,k) crossing of phi slice 0 after K steps, taken from
+ * a state to which the start-up boundary pass (main.f90:322-366) is applied first.
+ * The forward pass is the FP64 step (as fmf_ctx_step with precision FMF_FP64) with
+ * the viscous solve run to sor_tol; the reverse pass recomputes each step from
+ * checkpoints taken every `every` steps (0: ceil(sqrt(K))). */
+typedef struct fmf_adj fmf_adj;
+int fmf_adj_create(const fmf_params* prm, fmf_adj** out);
+int fmf_adj_destroy(fmf_adj* adj);
+/* viscous-solve stop rule err/err0 <= sor_tol within sor_max iterations (the
+ * reference: 1e-3, 21) and the transposed solve's relative tolerance / cap */
+int fmf_adj_set_solver(fmf_adj* adj, double sor_tol, int sor_max, double adj_tol, int adj_max);
+/* forward only: J after K steps; state_out (12 host fields) may be NULL */
+int fmf_adj_forward(fmf_adj* adj, int K, const double* const* state0, const double* theta0,
+                    const double* zeta, const double* l1, const double* l2, double* J,
+                    double* const* state_out);
+/* J and dJ/d(theta0, zeta, l1, l2, initial phi slice 1), each a host array of
+ * (ni+6)(nj+6)(nk+6) doubles (NULL: not returned) */
+int fmf_adj_rollout(fmf_adj* adj, int K, int every, const double* const* state0, const double* theta0,
+                    const double* zeta, const double* l1, const double* l2, double* J, double* g_theta0,
+                    double* g_zeta, double* g_l1, double* g_l2, double* g_phi);
+/* viscous-solve iterations of the last call: forward (all recomputations) and transposed */
+int fmf_adj_iterations(fmf_adj* adj, int* sor_total, int* adjoint_total);
+
 #ifdef __cplusplus
 }
 #endif

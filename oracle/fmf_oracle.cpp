@@ -30,6 +30,9 @@ struct Dim {
 
 inline double sq(double x) { return x * x; }
 
+double g_sor_tol = 1.0e-3;  // solu_sor4.f:291-293
+int g_sor_max = 21;
+
 // Fixed-order reduction: one partial per k plane (computed in i-fastest order),
 // summed in increasing k.  Deterministic for any thread count.
 template <class Fn>
@@ -1017,8 +1020,9 @@ int orc_solu_sor4_v(const int* nID, const int* ni, const int* nj, const int* nk,
   const long sx = 1, sy = D.nx, sz = D.nx * D.ny;
   double err0 = 0.0, err = 0.0;
   int lp;
+  const int lmax = g_sor_max - 1;
   std::vector<double> part(D.nk + 1);
-  for (lp = 0; lp <= 20; ++lp) {
+  for (lp = 0; lp <= lmax; ++lp) {
     double esum = 0.0;
     for (int comp = 0; comp < 3; ++comp) {
       double* q = comp == 0 ? un : (comp == 1 ? vn : wn);
@@ -1068,10 +1072,17 @@ int orc_solu_sor4_v(const int* nID, const int* ni, const int* nj, const int* nk,
     }
     err = std::sqrt(esum / (double)((long)D.ni * D.nj * D.nk)) + 1.0e-99;
     if (lp == 0) err0 = err;
-    if (err / err0 <= 1.0e-3) break;
+    if (err / err0 <= g_sor_tol) break;
   }
   if (err_out) *err_out = err / err0;
-  return (lp <= 20 ? lp : 20) + 1;
+  return (lp <= lmax ? lp : lmax) + 1;
+}
+
+// The stop rule of solu_sor4.f:291-293 is err/err0 <= 1e-3 within 21 iterations;
+// the adjoint's finite-difference checks need the solve converged much further.
+void orc_set_sor(double tol, int max_iter) {
+  g_sor_tol = tol;
+  g_sor_max = max_iter;
 }
 
 // ---------------------------------------------------------------------------

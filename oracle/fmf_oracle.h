@@ -127,6 +127,9 @@ int orc_solu_sor4_v(const int* nID, const int* ni, const int* nj, const int* nk,
                     const double* src_u, const double* src_v, const double* src_w, double* un,
                     double* vn, double* wn, const double* uwall, const double* dy,
                     const double* l1, const double* l2, const double* phi, double* err_out);
+/* stop rule of the outer iteration: err/err0 <= tol within max_iter iterations
+ * (the reference's 1e-3 and 21 unless changed) */
+void orc_set_sor(double tol, int max_iter);
 
 /* ---- C4 pressure ------------------------------------------------------- */
 void orc_caldiv(const int* ipara, const int* ndiv, const int* ni, const int* nj, const int* nk,
