@@ -185,6 +185,8 @@ void mthinc2_T(cudaStream_t s, const Grid& g, double dxi, double dyi, double dzi
 // where pb follows pa (gx..gz: vertex gradient of pa, as the forward pass used)
 void mthinc3_record(cudaStream_t s, const Grid& g, double dxi, double dyi, double dzi, double bet, const double* gx,
                     const double* gy, const double* gz, const double* pa, double* pb, double* pass);
+// adjoints of phin outside the interior (stale step-start values) -> lphin_start
+void phin_stale_T(cudaStream_t s, const Grid& g, const double* pass, double* lphin, double* lphin_start);
 // sums: (sum phi, sum pb, sum pb^2(1-pb)) of the forward pass; lphin in/out
 // (interior), lphi += the volume-sum term; scal: >= 4 doubles of device scratch
 void mthinc3_T(cudaStream_t s, const Grid& g, const double* pb, const double* pass, const double* sums,

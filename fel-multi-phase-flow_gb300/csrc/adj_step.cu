@@ -338,7 +338,14 @@ void reverse_step(fmf_adj* a, const double* st) {
   zero(a, lS[SPO], n);
   dcopy(a, lS[SPHI0], a->lphn0, n);
   dcopy(a, lS[SPHI1], a->lphn1, n);
-  // the next step's phin adds to the same phin (it only feeds branches there: zero)
+  {  // phin' is the same phin: its adjoint adds
+    double *p0 = a->lphn0, *p1 = a->lphn1;
+    const double *q0 = lS[SPHIN0], *q1 = lS[SPHIN1];
+    flat(s, n, [=] __device__(long t) {
+      p0[t] += q0[t];
+      p1[t] += q1[t];
+    });
+  }
   zero(a, lS[SPHI0], n);
   zero(a, lS[SPHI1], n);
   zero(a, lS[SPHIN0], n);
@@ -471,6 +478,7 @@ void reverse_step(fmf_adj* a, const double* st) {
               a->gzeta);
   check_stage(a, "gnbc");
   adj::mthinc3_T(s, g, a->pb, a->pass, a->sums, a->lphn1, lS[SPHI1], a->sums + 4);
+  adj::phin_stale_T(s, g, a->pass, a->lphn1, lS[SPHIN1]);
   adj::mthinc2_T(s, g, dxi, dyi, dzi, dt, ST(SU), ST(SV), ST(SW), a->fl[0], a->fl[1], a->fl[2], ST(SPHI1), a->pa,
                  a->lphn1, lS[SPHI1], lS[SU], lS[SV], lS[SW], a->lfl[0], a->lfl[1], a->lfl[2], a->lpre);
   adj::mthinc1_T(s, g, dxi, dyi, dzi, dt, P.bet_mthinc, ST(SPHI1), a->gx1[0], a->gx1[1], a->gx1[2], ST(SU), ST(SV),

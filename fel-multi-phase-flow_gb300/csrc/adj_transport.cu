@@ -251,9 +251,12 @@ void mthinc3_record(cudaStream_t s, const Grid& g, double dxi, double dyi, doubl
                     const double* gy, const double* gz, const double* pa, double* pb, double* pass) {
   const Grid G = g;
   const MC M = mconst(dxi, dyi, dzi, bet);
-  range3(s, 1, g.ni, 1, g.nj, 1, g.nk, [=] __device__(int i, int j, int k) {
+  // the snap covers cells 0..n+1 (the ring outside the interior holds the stale
+  // values of phin that bnd_contact_angle later reads); the clip the interior only
+  range3(s, 0, g.ni + 1, 0, g.nj + 1, 0, g.nk + 1, [=] __device__(int i, int j, int k) {
     const long X = 1, Y = G.sy, Z = G.sz;
     const long c = G.at(i, j, k);
+    const bool in = i >= 1 && i <= G.ni && j >= 1 && j <= G.nj && k >= 1 && k <= G.nk;
     const double rnx = avg8(gx, c, X, Y, Z), rny = avg8(gy, c, X, Y, Z), rnz = avg8(gz, c, X, Y, Z);
     const double q00 = sqrt(rnx * rnx + rny * rny + rnz * rnz);
     double p = pa[c];
@@ -268,9 +271,26 @@ void mthinc3_record(cudaStream_t s, const Grid& g, double dxi, double dyi, doubl
         m = 0.0;
       }
     }
-    if (p > 1.0 || p < 0.0) m = 0.0;
-    pb[c] = fmax(fmin(p, 1.0), 0.0);
+    if (in) {
+      if (p > 1.0 || p < 0.0) m = 0.0;
+      p = fmax(fmin(p, 1.0), 0.0);
+    }
+    pb[c] = p;
     pass[c] = m;
+  });
+}
+
+// phin outside the interior is not written by solphi_mthinc2: there it holds the
+// values phin had at the start of the step (after the band-test snap of
+// solphi_mthinc3 on cells 0..n+1).  Their adjoints go to the step-start phin.
+void phin_stale_T(cudaStream_t s, const Grid& g, const double* pass, double* lphin, double* lphin_start) {
+  const Grid G = g;
+  range3(s, -2, g.ni + 3, -2, g.nj + 3, -2, g.nk + 3, [=] __device__(int i, int j, int k) {
+    const long c = G.at(i, j, k);
+    if (i >= 1 && i <= G.ni && j >= 1 && j <= G.nj && k >= 1 && k <= G.nk) return;
+    const bool ring = i >= 0 && i <= G.ni + 1 && j >= 0 && j <= G.nj + 1 && k >= 0 && k <= G.nk + 1;
+    lphin_start[c] += lphin[c] * (ring ? pass[c] : 1.0);
+    lphin[c] = 0.0;
   });
 }
 
