@@ -10,6 +10,9 @@
 // and differentiated on the branch that was executed.
 #pragma once
 #include <cmath>
+#include <map>
+#include <utility>
+#include <vector>
 
 #include "fmf_common.cuh"
 
@@ -174,7 +177,7 @@ void div_tensor_T(cudaStream_t s, const Grid& g, double dxi, double dyi, double 
 void mthinc1_T(cudaStream_t s, const Grid& g, double dxi, double dyi, double dzi, double dt, double bet,
                const double* phi, const double* gx, const double* gy, const double* gz, const double* u,
                const double* v, const double* w, const double* lfx, const double* lfy, const double* lfz,
-               double* lphi, double* lrn, double* lu, double* lv, double* lw);
+               double* lphi, double* lrn, double* lu, double* lv, double* lw, const int* list, const int* count);
 // lrn (3 arrays of n: per cell the adjoint of the averaged vertex gradient) -> lgx..lgz
 void rn_avg_T(cudaStream_t s, const Grid& g, const double* lrn, double* lgx, double* lgy, double* lgz);
 void mthinc2_T(cudaStream_t s, const Grid& g, double dxi, double dyi, double dzi, double dt, const double* u,
@@ -193,8 +196,9 @@ void mthinc3_T(cudaStream_t s, const Grid& g, const double* pb, const double* pa
                double* lphin, double* lphi, double* scal);
 
 // ---- momentum ------------------------------------------------------------------
+// work: >= 63n doubles (per-line adjoints of the differences and velocities)
 void weno_T(cudaStream_t s, const Grid& g, double dxi, double dyi, double dzi, const double* u, const double* v,
-            const double* w, const double* const* ladv, double* lu, double* lv, double* lw);
+            const double* w, const double* const* ladv, double* lu, double* lv, double* lw, double* work);
 // CSF force of one field: lf (3 arrays) -> lphi; work: >= 42n doubles
 void csf_T(cudaStream_t s, const Grid& g, double dxi, double dyi, double dzi, double rhol, double rhog,
            double sigma, const double* phi, const double* const* lf, double* lphi, double* work);
@@ -220,13 +224,16 @@ void edges_T(cudaStream_t s, const Grid& g, int harmonic, const double* mu, cons
 void sor_replay(cudaStream_t s, const Grid& g, double dxi, double dyi, double dzi, const double* mu,
                 double* const* E, double* const* AB, double uwall, const double* wallc, const double* const* ustar,
                 double* snaps);
+// CUDA graphs of one transposed iteration, keyed by the buffers they read and write
+using GraphCache = std::map<std::vector<const void*>, std::pair<cudaGraphExec_t, long long>>;
 // transposed fixed-point solve and gradient collection; lam: 3 output arrays (the
 // converged adjoint of un*, consumed by the gradient pass); lAB, lmu, lE, lwc
-// accumulate; work: >= 3n + 520 doubles.  Returns the iterations used.
+// accumulate; work: >= 3n + 520 doubles; host_norm: 1 pinned double; cache may be
+// null (no graphs).  Returns the iterations used.
 int sor_T(cudaStream_t s, const Grid& g, double dxi, double dyi, double dzi, const double* mu, double* const* E,
           double* const* AB, double uwall, const double* wallc, const double* const* ustar, const double* snaps,
           const double* const* lout, double* const* lam, double* const* lAB, double* lmu, double* const* lE,
-          double* lwc, double tol, int maxit, double* work);
+          double* lwc, double tol, int maxit, double* work, double* host_norm, GraphCache* cache);
 
 }  // namespace adj
 }  // namespace fmf

@@ -28,45 +28,103 @@ void sum_all(cudaStream_t s, long n, const double* a, double* out) {
 }
 }  // namespace
 
+// Transposed copy along one line (stride S, N interior points): the adjoints of the
+// destinations -2, -1, 0, N+1, N+2, N+3 are added to their sources and cleared.
+// SHIFT: bndu's copy of the normal component (-2, -1, 0 from N-1, N, N+1; N+1 not
+// written).  The destination loads are issued together; the source updates run
+// one after another (sources can coincide when N = 4).
+template <bool SHIFT>
+__device__ __forceinline__ void line_T(double* __restrict__ a, long r, long S, int N) {
+  const long sh = SHIFT ? S : 0;
+  const double L0 = a[r - 2 * S], L1 = a[r - S], L2 = a[r], L4 = a[r + (N + 2) * S], L5 = a[r + (N + 3) * S];
+  const double L3 = SHIFT ? 0.0 : a[r + (N + 1) * S];
+  if (N >= 8) {  // six distinct sources: every load first, then every store
+    const double s0 = a[r + (N - 2) * S + sh], s1 = a[r + (N - 1) * S + sh], s2 = a[r + N * S + sh];
+    const double s3 = SHIFT ? 0.0 : a[r + S], s4 = a[r + 2 * S], s5 = a[r + 3 * S];
+    a[r - 2 * S] = 0.0;
+    a[r - S] = 0.0;
+    a[r] = 0.0;
+    if (!SHIFT) a[r + (N + 1) * S] = 0.0;
+    a[r + (N + 2) * S] = 0.0;
+    a[r + (N + 3) * S] = 0.0;
+    a[r + (N - 2) * S + sh] = s0 + L0;
+    a[r + (N - 1) * S + sh] = s1 + L1;
+    a[r + N * S + sh] = s2 + L2;
+    if (!SHIFT) a[r + S] = s3 + L3;
+    a[r + 2 * S] = s4 + L4;
+    a[r + 3 * S] = s5 + L5;
+    return;
+  }
+  a[r - 2 * S] = 0.0;
+  a[r - S] = 0.0;
+  a[r] = 0.0;
+  if (!SHIFT) a[r + (N + 1) * S] = 0.0;
+  a[r + (N + 2) * S] = 0.0;
+  a[r + (N + 3) * S] = 0.0;
+  a[r + (N - 2) * S + sh] += L0;
+  a[r + (N - 1) * S + sh] += L1;
+  a[r + N * S + sh] += L2;
+  if (!SHIFT) a[r + S] += L3;
+  a[r + 2 * S] += L4;
+  a[r + 3 * S] += L5;
+}
+// x lines (one thread per (j,k)), normal: bit c set = plain copy of component c
+__global__ void __launch_bounds__(256) k_halo_x_T(Grid g, int normal, double* __restrict__ lu,
+                                                  double* __restrict__ lv, double* __restrict__ lw) {
+  const int j = -2 + (int)(blockIdx.x * blockDim.x + threadIdx.x);
+  const int k = -2 + (int)(blockIdx.y * blockDim.y + threadIdx.y);
+  if (j > g.nj + 3 || k > g.nk + 3) return;
+  const long r = g.at(0, j, k);
+  if (normal & 1) line_T<false>(lu, r, 1, g.ni);
+  else line_T<true>(lu, r, 1, g.ni);
+  if (lv) line_T<false>(lv, r, 1, g.ni);
+  if (lw) line_T<false>(lw, r, 1, g.ni);
+}
+// z lines (one thread per (i,j)); w is the shifted component
+__global__ void __launch_bounds__(256) k_halo_z_T(Grid g, int normal, double* __restrict__ lu,
+                                                  double* __restrict__ lv, double* __restrict__ lw) {
+  const int i = -2 + (int)(blockIdx.x * blockDim.x + threadIdx.x);
+  const int j = -2 + (int)(blockIdx.y * blockDim.y + threadIdx.y);
+  if (i > g.ni + 3 || j > g.nj + 3) return;
+  const long r = g.at(i, j, 0);
+  if (lu) line_T<false>(lu, r, g.sz, g.nk);
+  if (lv) line_T<false>(lv, r, g.sz, g.nk);
+  if (lw) {
+    if (normal & 4) line_T<false>(lw, r, g.sz, g.nk);
+    else line_T<true>(lw, r, g.sz, g.nk);
+  }
+}
+dim3 xh_grid(const Grid& g) { return dim3((g.nj + 6 + 31) / 32, (g.nk + 6 + 7) / 8); }
+dim3 zh_grid(const Grid& g) { return dim3((g.ni + 6 + 31) / 32, (g.nj + 6 + 7) / 8); }
+
 // bnd_periodic: x copies over every (j,k) then z copies over every (i,j); the adjoint
-// runs z first.  Sources and destinations of one row are disjoint.
+// runs z first.
 void periodic_T(cudaStream_t s, const Grid& g, double* lq) {
-  const Grid G = g;
-  range2(s, -2, g.ni + 3, -2, g.nj + 3, [=] __device__(int i, int j) {
-    const int NK = G.nk;
-    const long Z = G.sz, r = G.at(i, j, 0);
-    const int dst[6] = {-2, -1, 0, NK + 1, NK + 2, NK + 3}, src[6] = {NK - 2, NK - 1, NK, 1, 2, 3};
-    double L[6];
-    for (int t = 0; t < 6; ++t) {
-      L[t] = lq[r + dst[t] * Z];
-      lq[r + dst[t] * Z] = 0.0;
-    }
-    for (int t = 0; t < 6; ++t) lq[r + src[t] * Z] += L[t];
-  });
-  range2(s, -2, g.nj + 3, -2, g.nk + 3, [=] __device__(int j, int k) {
-    const int NI = G.ni;
-    const long r = G.at(0, j, k);
-    const int dst[6] = {-2, -1, 0, NI + 1, NI + 2, NI + 3}, src[6] = {NI - 2, NI - 1, NI, 1, 2, 3};
-    double L[6];
-    for (int t = 0; t < 6; ++t) {
-      L[t] = lq[r + dst[t]];
-      lq[r + dst[t]] = 0.0;
-    }
-    for (int t = 0; t < 6; ++t) lq[r + src[t]] += L[t];
-  });
+  k_halo_z_T<<<zh_grid(g), dim3(32, 8), 0, s>>>(g, 4, nullptr, nullptr, lq);
+  k_halo_x_T<<<xh_grid(g), dim3(32, 8), 0, s>>>(g, 1, lq, nullptr, nullptr);
+  count_launch(2);
 }
 
 void neumann_T(cudaStream_t s, const Grid& g, double* lq) {
   const Grid G = g;
   range2(s, -2, g.ni + 3, -2, g.nk + 3, [=] __device__(int i, int k) {
     const int NJ = G.nj;
-    const int dst[6] = {-2, -1, 0, NJ + 1, NJ + 2, NJ + 3}, src[6] = {3, 2, 1, NJ, NJ - 1, NJ - 2};
-    double L[6];
-    for (int t = 0; t < 6; ++t) {
-      L[t] = lq[G.at(i, dst[t], k)];
-      lq[G.at(i, dst[t], k)] = 0.0;
-    }
-    for (int t = 0; t < 6; ++t) lq[G.at(i, src[t], k)] += L[t];
+    const long Y = G.sy, r = G.at(i, 0, k);
+    // destinations j = -2, -1, 0, NJ+1, NJ+2, NJ+3 from 3, 2, 1, NJ, NJ-1, NJ-2
+    const double L0 = lq[r - 2 * Y], L1 = lq[r - Y], L2 = lq[r], L3 = lq[r + (NJ + 1) * Y], L4 = lq[r + (NJ + 2) * Y],
+                 L5 = lq[r + (NJ + 3) * Y];
+    lq[r - 2 * Y] = 0.0;
+    lq[r - Y] = 0.0;
+    lq[r] = 0.0;
+    lq[r + (NJ + 1) * Y] = 0.0;
+    lq[r + (NJ + 2) * Y] = 0.0;
+    lq[r + (NJ + 3) * Y] = 0.0;
+    lq[r + 3 * Y] += L0;
+    lq[r + 2 * Y] += L1;
+    lq[r + Y] += L2;
+    lq[r + NJ * Y] += L3;
+    lq[r + (NJ - 1) * Y] += L4;
+    lq[r + (NJ - 2) * Y] += L5;
   });
 }
 
@@ -171,10 +229,14 @@ void contact_angle_T(cudaStream_t s, const Grid& g, const double* qk, const doub
   });
 }
 
-void wall_T(cudaStream_t s, const Grid& g, double uwall, const double* wc, const double* uk, const double* wk,
-            double* lu, double* lv, double* lw, double* lwc) {
-  const Grid G = g;
-  range2(s, -2, g.ni + 3, -2, 2 * (g.nk + 6) - 3, [=] __device__(int i, int kk) {
+__global__ void __launch_bounds__(256) k_wall_T(Grid G, double uwall, const double* __restrict__ wc,
+                                                const double* __restrict__ uk, const double* __restrict__ wk,
+                                                double* __restrict__ lu, double* __restrict__ lv,
+                                                double* __restrict__ lw, double* __restrict__ lwc) {
+  const int i = -2 + (int)(blockIdx.x * blockDim.x + threadIdx.x);
+  const int kk = -2 + (int)(blockIdx.y * blockDim.y + threadIdx.y);
+  if (i > G.ni + 3 || kk > 2 * (G.nk + 6) - 3) return;
+  {
     const int side = kk >= G.nk + 4 ? 1 : 0;
     const int k = side ? kk - (G.nk + 6) : kk;
     const long o = (((long)side * (G.nk + 6) + (k + 2)) * (G.ni + 6) + (i + 2)) * 2;
@@ -182,88 +244,50 @@ void wall_T(cudaStream_t s, const Grid& g, double uwall, const double* wc, const
     const long Y = G.sy;
     const long c = G.at(i, side ? G.nj : 1, k);
     const long t = side ? Y : -Y;
-    const double L1 = lu[c + t], L2 = lu[c + 2 * t], L3 = lu[c + 3 * t];
-    const double M1 = lw[c + t], M2 = lw[c + 2 * t], M3 = lw[c + 3 * t];
+    // every load first (ghost rows and the wall rows they came from are disjoint)
+    const double L1 = lu[c + t], L2 = lu[c + 2 * t], L3 = lu[c + 3 * t], U0 = lu[c];
+    const double M1 = lw[c + t], M2 = lw[c + 2 * t], M3 = lw[c + 3 * t], W0 = lw[c];
+    // v: side 0 ghosts 0, -1, -2 from -, 1, 2; side 1 ghosts nj, nj+1..3 from -, nj-1..3
+    const double va = lv[c + (side ? Y : -2 * Y)], vb = lv[c + (side ? 2 * Y : -3 * Y)];
+    const double vd = side ? lv[c + 3 * Y] : 0.0;
+    const double V0 = lv[c + (side ? -Y : 0)], V1 = lv[c + (side ? -2 * Y : Y)];
+    const double V2 = side ? lv[c - 3 * Y] : 0.0;
     lu[c + t] = lu[c + 2 * t] = lu[c + 3 * t] = 0.0;
     lw[c + t] = lw[c + 2 * t] = lw[c + 3 * t] = 0.0;
-    lu[c] += c2 * L1 + (2.0 * c2 - 1.0) * L2 + (3.0 * c2 - 2.0) * L3;
-    lw[c] += c2 * M1 + (2.0 * c2 - 1.0) * M2 + (3.0 * c2 - 2.0) * M3;
+    lu[c] = U0 + c2 * L1 + (2.0 * c2 - 1.0) * L2 + (3.0 * c2 - 2.0) * L3;
+    lw[c] = W0 + c2 * M1 + (2.0 * c2 - 1.0) * M2 + (3.0 * c2 - 2.0) * M3;
     const double SL = L1 + 2.0 * L2 + 3.0 * L3, SM = M1 + 2.0 * M2 + 3.0 * M3;
     if (lwc) {
       lwc[o] += (side ? uwall : -uwall) * SL;
       lwc[o + 1] += uk[c] * SL + wk[c] * SM;
     }
     if (!side) {  // v(0) = 0, v(-1) = -v(1), v(-2) = -v(2)
-      const double a = lv[c - 2 * Y], b = lv[c - 3 * Y];
       lv[c - Y] = lv[c - 2 * Y] = lv[c - 3 * Y] = 0.0;
-      lv[c] -= a;
-      lv[c + Y] -= b;
+      lv[c] = V0 - va;
+      lv[c + Y] = V1 - vb;
     } else {  // v(nj) = 0, v(nj+m) = -v(nj-m)
-      const double a = lv[c + Y], b = lv[c + 2 * Y], d = lv[c + 3 * Y];
       lv[c] = lv[c + Y] = lv[c + 2 * Y] = lv[c + 3 * Y] = 0.0;
-      lv[c - Y] -= a;
-      lv[c - 2 * Y] -= b;
-      lv[c - 3 * Y] -= d;
+      lv[c - Y] = V0 - va;
+      lv[c - 2 * Y] = V1 - vb;
+      lv[c - 3 * Y] = V2 - vd;
     }
-  });
+  }
+}
+void wall_T(cudaStream_t s, const Grid& g, double uwall, const double* wc, const double* uk, const double* wk,
+            double* lu, double* lv, double* lw, double* lwc) {
+  k_wall_T<<<dim3((g.ni + 6 + 31) / 32, (2 * (g.nk + 6) + 7) / 8), dim3(32, 8), 0, s>>>(g, uwall, wc, uk, wk, lu, lv,
+                                                                                       lw, lwc);
+  count_launch();
 }
 
 void halo_x_T(cudaStream_t s, const Grid& g, int normal, double* lu, double* lv, double* lw) {
-  const Grid G = g;
-  range2(s, -2, g.nj + 3, -2, g.nk + 3, [=] __device__(int j, int k) {
-    const int NI = G.ni;
-    const long r = G.at(0, j, k);
-    double* q[3] = {lu, lv, lw};
-    for (int cmp = 0; cmp < 3; ++cmp) {
-      double* a = q[cmp];
-      if (cmp == 0 && !(normal & 1)) {
-        const int dst[5] = {-2, -1, 0, NI + 2, NI + 3}, src[5] = {NI - 1, NI, NI + 1, 2, 3};
-        double L[5];
-        for (int t = 0; t < 5; ++t) {
-          L[t] = a[r + dst[t]];
-          a[r + dst[t]] = 0.0;
-        }
-        for (int t = 0; t < 5; ++t) a[r + src[t]] += L[t];
-      } else {
-        const int dst[6] = {-2, -1, 0, NI + 1, NI + 2, NI + 3}, src[6] = {NI - 2, NI - 1, NI, 1, 2, 3};
-        double L[6];
-        for (int t = 0; t < 6; ++t) {
-          L[t] = a[r + dst[t]];
-          a[r + dst[t]] = 0.0;
-        }
-        for (int t = 0; t < 6; ++t) a[r + src[t]] += L[t];
-      }
-    }
-  });
+  k_halo_x_T<<<xh_grid(g), dim3(32, 8), 0, s>>>(g, normal, lu, lv, lw);
+  count_launch();
 }
 
 void halo_z_T(cudaStream_t s, const Grid& g, int normal, double* lu, double* lv, double* lw) {
-  const Grid G = g;
-  range2(s, -2, g.ni + 3, -2, g.nj + 3, [=] __device__(int i, int j) {
-    const int NK = G.nk;
-    const long Z = G.sz, r = G.at(i, j, 0);
-    double* q[3] = {lu, lv, lw};
-    for (int cmp = 0; cmp < 3; ++cmp) {
-      double* a = q[cmp];
-      if (cmp == 2 && !(normal & 4)) {
-        const int dst[5] = {-2, -1, 0, NK + 2, NK + 3}, src[5] = {NK - 1, NK, NK + 1, 2, 3};
-        double L[5];
-        for (int t = 0; t < 5; ++t) {
-          L[t] = a[r + dst[t] * Z];
-          a[r + dst[t] * Z] = 0.0;
-        }
-        for (int t = 0; t < 5; ++t) a[r + src[t] * Z] += L[t];
-      } else {
-        const int dst[6] = {-2, -1, 0, NK + 1, NK + 2, NK + 3}, src[6] = {NK - 2, NK - 1, NK, 1, 2, 3};
-        double L[6];
-        for (int t = 0; t < 6; ++t) {
-          L[t] = a[r + dst[t] * Z];
-          a[r + dst[t] * Z] = 0.0;
-        }
-        for (int t = 0; t < 6; ++t) a[r + src[t] * Z] += L[t];
-      }
-    }
-  });
+  k_halo_z_T<<<zh_grid(g), dim3(32, 8), 0, s>>>(g, normal, lu, lv, lw);
+  count_launch();
 }
 
 void wall_halo_T(cudaStream_t s, const Grid& g, int normal, double uwall, const double* wc, const double* u,

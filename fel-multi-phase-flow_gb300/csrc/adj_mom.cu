@@ -54,15 +54,16 @@ __device__ __forceinline__ void side_rev(const Side& S, double lr, double* la) {
   la[3] += 2.0 * ld2 + 5.0 * ld3 + lt2 - lt3 - 2.0 * lt4 - 4.0 * lt5;
   la[4] += -ld3 + lt4 + lt5;
 }
-// adjoint of  out += weno5_line(q, c, S, vel) * di  given lout; returns lvel
-__device__ double wline_T(const double* q, double* lq, long c, long S, double vel, double lout, double di) {
+// adjoint of  out += weno5_line(q, c, S, vel) * di  given lout: lD[0..5] = the
+// adjoints of the six differences (dm5, dm3, dm1, dp1, dp3, dp5); returns lvel
+__device__ double wline_T(const double* __restrict__ q, long c, long S, double vel, double lout, double di,
+                          double* lD) {
+  for (int m = 0; m < 6; ++m) lD[m] = 0.0;
   const double lr = lout * di;
   if (lr == 0.0) return 0.0;
   const double m3 = q[c - 3 * S], m2 = q[c - 2 * S], m1 = q[c - S], z0 = q[c], p1 = q[c + S], p2 = q[c + 2 * S],
                p3 = q[c + 3 * S];
   const double dm5 = -m3 + m2, dm3 = -m2 + m1, dm1 = -m1 + z0, dp1 = -z0 + p1, dp3 = -p1 + p2, dp5 = -p2 + p3;
-  // lD[0..5] = adjoints of (dm5, dm3, dm1, dp1, dp3, dp5)
-  double lD[6] = {0, 0, 0, 0, 0, 0};
   double lvel = 0.0;
   Side A, B;
   const bool needA = vel >= 0.0, needB = vel <= 0.0;
@@ -81,68 +82,100 @@ __device__ double wline_T(const double* q, double* lq, long c, long S, double ve
   } else {
     lvel = lr * (A.r + B.r) / 12.0;
   }
-  // differences -> points m3 m2 m1 z0 p1 p2 p3
-  aadd(lq + c - 3 * S, -lD[0]);
-  aadd(lq + c - 2 * S, lD[0] - lD[1]);
-  aadd(lq + c - S, lD[1] - lD[2]);
-  aadd(lq + c, lD[2] - lD[3]);
-  aadd(lq + c + S, lD[3] - lD[4]);
-  aadd(lq + c + 2 * S, lD[4] - lD[5]);
-  aadd(lq + c + 3 * S, lD[5]);
   return lvel;
+}
+
+// Offsets (relative to the cell) of the four velocity points that form the
+// advecting velocity of line (component q, direction d); the line reads component d.
+__constant__ signed char kVelOff[9][4][3] = {
+    {{-1, 0, 0}, {0, 0, 0}, {0, 0, 0}, {1, 0, 0}},   {{0, -1, 0}, {1, -1, 0}, {0, 0, 0}, {1, 0, 0}},
+    {{0, 0, -1}, {1, 0, -1}, {0, 0, 0}, {1, 0, 0}},  {{-1, 0, 0}, {-1, 1, 0}, {0, 0, 0}, {0, 1, 0}},
+    {{0, -1, 0}, {0, 0, 0}, {0, 0, 0}, {0, 1, 0}},   {{0, 0, -1}, {0, 1, -1}, {0, 0, 0}, {0, 1, 0}},
+    {{-1, 0, 0}, {-1, 0, 1}, {0, 0, 0}, {0, 0, 1}},  {{0, -1, 0}, {0, -1, 1}, {0, 0, 0}, {0, 0, 1}},
+    {{0, 0, -1}, {0, 0, 0}, {0, 0, 0}, {0, 0, 1}}};
+
+// Pass 1: per interior cell and each of the 9 lines (one thread per cell and
+// line: grid z = 9 nk), the adjoints of the six differences (D, 54 arrays) and of
+// the advecting velocity (V, 9 arrays).
+__global__ void __launch_bounds__(256) k_weno_T1(Grid g, double dxi, double dyi, double dzi,
+                                                 const double* __restrict__ u, const double* __restrict__ v,
+                                                 const double* __restrict__ w, const double* __restrict__ la0,
+                                                 const double* __restrict__ la1, const double* __restrict__ la2,
+                                                 double* __restrict__ D, double* __restrict__ V) {
+  const int i = 1 + (int)(blockIdx.x * blockDim.x + threadIdx.x);
+  const int j = 1 + (int)(blockIdx.y * blockDim.y + threadIdx.y);
+  const int line = (int)blockIdx.z % 9, k = 1 + (int)blockIdx.z / 9;
+  if (i > g.ni || j > g.nj) return;
+  const int q = line / 3, d = line % 3;
+  const long X = 1, Y = g.sy, Z = g.sz, n = g.n;
+  const long c = g.at(i, j, k);
+  const double* vq = d == 0 ? u : (d == 1 ? v : w);
+  const signed char(*o)[3] = kVelOff[line];
+  const double a = vq[c + o[0][0] * X + o[0][1] * Y + o[0][2] * Z];
+  const double b = vq[c + o[1][0] * X + o[1][1] * Y + o[1][2] * Z];
+  const double e = vq[c + o[2][0] * X + o[2][1] * Y + o[2][2] * Z];
+  const double f = vq[c + o[3][0] * X + o[3][1] * Y + o[3][2] * Z];
+  const double vel = ((a + b) * 0.5 + (e + f) * 0.5) * 0.5;
+  const double L = (q == 0 ? la0 : (q == 1 ? la1 : la2))[c];
+  double lD[6];
+  const double lvel = wline_T(q == 0 ? u : (q == 1 ? v : w), c, d == 0 ? X : (d == 1 ? Y : Z), vel, L,
+                              d == 0 ? dxi : (d == 1 ? dyi : dzi), lD);
+#pragma unroll
+  for (int m = 0; m < 6; ++m) D[(long)(line * 6 + m) * n + c] = lD[m];
+  V[(long)line * n + c] = lvel;
+}
+// Pass 2: every point gathers what the lines of the cells around it owe it.
+__global__ void __launch_bounds__(256) k_weno_T2(Grid g, const double* __restrict__ D,
+                                                 const double* __restrict__ V, double* __restrict__ lu,
+                                                 double* __restrict__ lv, double* __restrict__ lw) {
+  const int x = -2 + (int)(blockIdx.x * blockDim.x + threadIdx.x);
+  const int y = -2 + (int)(blockIdx.y * blockDim.y + threadIdx.y);
+  const int z = -2 + (int)blockIdx.z;
+  if (x > g.ni + 3 || y > g.nj + 3) return;
+  const long n = g.n;
+  auto in = [&](int a, int b, int e) { return a >= 1 && a <= g.ni && b >= 1 && b <= g.nj && e >= 1 && e <= g.nk; };
+  // point x sits at stencil position o (-3..3) of the cell x - o*S; its coefficient
+  // there: o=-3: -D0, -2: D0-D1, -1: D1-D2, 0: D2-D3, 1: D3-D4, 2: D4-D5, 3: D5
+  double acc[3] = {0.0, 0.0, 0.0};
+  for (int p = 0; p < 3; ++p) {
+    for (int d = 0; d < 3; ++d) {
+      const int line = p * 3 + d;
+      const double* Dl = D + (long)line * 6 * n;
+      for (int o = -3; o <= 3; ++o) {
+        const int ci = x - (d == 0 ? o : 0), cj = y - (d == 1 ? o : 0), ck = z - (d == 2 ? o : 0);
+        if (!in(ci, cj, ck)) continue;
+        const long c = g.at(ci, cj, ck);
+        const int m = o + 3;  // 0..6
+        const double hi = m < 6 ? Dl[(long)m * n + c] : 0.0;     // + D_m
+        const double lo = m > 0 ? Dl[(long)(m - 1) * n + c] : 0.0;  // - D_{m-1}
+        acc[p] += lo - hi;
+      }
+    }
+    // velocity points: lines (q, p) read component p at 4 offsets
+    for (int q = 0; q < 3; ++q) {
+      const int line = q * 3 + p;
+      for (int t = 0; t < 4; ++t) {
+        const int ci = x - kVelOff[line][t][0], cj = y - kVelOff[line][t][1], ck = z - kVelOff[line][t][2];
+        if (!in(ci, cj, ck)) continue;
+        acc[p] += 0.25 * V[(long)line * n + g.at(ci, cj, ck)];
+      }
+    }
+  }
+  const long c = g.at(x, y, z);
+  lu[c] += acc[0];
+  lv[c] += acc[1];
+  lw[c] += acc[2];
 }
 }  // namespace
 
 void weno_T(cudaStream_t s, const Grid& g, double dxi, double dyi, double dzi, const double* u, const double* v,
-            const double* w, const double* const* ladv, double* lu, double* lv, double* lw) {
-  const Grid G = g;
-  const double *la0 = ladv[0], *la1 = ladv[1], *la2 = ladv[2];
-  range3(s, 1, g.ni, 1, g.nj, 1, g.nk, [=] __device__(int i, int j, int k) {
-    const long X = 1, Y = G.sy, Z = G.sz;
-    const long c = G.at(i, j, k);
-    double L, vel, lvel;
-    // velocity means: ((a + b) 0.5 + (d + e) 0.5) 0.5 -> 0.25 to each point
-    auto spread = [&](double* lq, long a, long b, long d, long e, double lv_) {
-      const double q = 0.25 * lv_;
-      aadd(lq + a, q);
-      aadd(lq + b, q);
-      aadd(lq + d, q);
-      aadd(lq + e, q);
-    };
-    if ((L = la0[c]) != 0.0) {
-      vel = ((u[c - X] + u[c]) * 0.5 + (u[c] + u[c + X]) * 0.5) * 0.5;
-      lvel = wline_T(u, lu, c, X, vel, L, dxi);
-      spread(lu, c - X, c, c, c + X, lvel);
-      vel = ((v[c - Y] + v[c + X - Y]) * 0.5 + (v[c] + v[c + X]) * 0.5) * 0.5;
-      lvel = wline_T(u, lu, c, Y, vel, L, dyi);
-      spread(lv, c - Y, c + X - Y, c, c + X, lvel);
-      vel = ((w[c - Z] + w[c + X - Z]) * 0.5 + (w[c] + w[c + X]) * 0.5) * 0.5;
-      lvel = wline_T(u, lu, c, Z, vel, L, dzi);
-      spread(lw, c - Z, c + X - Z, c, c + X, lvel);
-    }
-    if ((L = la1[c]) != 0.0) {
-      vel = ((u[c - X] + u[c - X + Y]) * 0.5 + (u[c] + u[c + Y]) * 0.5) * 0.5;
-      lvel = wline_T(v, lv, c, X, vel, L, dxi);
-      spread(lu, c - X, c - X + Y, c, c + Y, lvel);
-      vel = ((v[c - Y] + v[c]) * 0.5 + (v[c] + v[c + Y]) * 0.5) * 0.5;
-      lvel = wline_T(v, lv, c, Y, vel, L, dyi);
-      spread(lv, c - Y, c, c, c + Y, lvel);
-      vel = ((w[c - Z] + w[c + Y - Z]) * 0.5 + (w[c] + w[c + Y]) * 0.5) * 0.5;
-      lvel = wline_T(v, lv, c, Z, vel, L, dzi);
-      spread(lw, c - Z, c + Y - Z, c, c + Y, lvel);
-    }
-    if ((L = la2[c]) != 0.0) {
-      vel = ((u[c - X] + u[c - X + Z]) * 0.5 + (u[c] + u[c + Z]) * 0.5) * 0.5;
-      lvel = wline_T(w, lw, c, X, vel, L, dxi);
-      spread(lu, c - X, c - X + Z, c, c + Z, lvel);
-      vel = ((v[c - Y] + v[c - Y + Z]) * 0.5 + (v[c] + v[c + Z]) * 0.5) * 0.5;
-      lvel = wline_T(w, lw, c, Y, vel, L, dyi);
-      spread(lv, c - Y, c - Y + Z, c, c + Z, lvel);
-      vel = ((w[c - Z] + w[c]) * 0.5 + (w[c] + w[c + Z]) * 0.5) * 0.5;
-      lvel = wline_T(w, lw, c, Z, vel, L, dzi);
-      spread(lw, c - Z, c, c, c + Z, lvel);
-    }
-  });
+            const double* w, const double* const* ladv, double* lu, double* lv, double* lw, double* work) {
+  double* D = work;
+  double* V = work + 54 * g.n;
+  k_weno_T1<<<dim3((g.ni + 31) / 32, (g.nj + 7) / 8, 9 * g.nk), dim3(32, 8), 0, s>>>(g, dxi, dyi, dzi, u, v, w, ladv[0],
+                                                                               ladv[1], ladv[2], D, V);
+  k_weno_T2<<<dim3((g.ni + 6 + 31) / 32, (g.nj + 6 + 7) / 8, g.nk + 6), dim3(32, 8), 0, s>>>(g, D, V, lu, lv, lw);
+  count_launch(2);
 }
 
 // ---- CSF --------------------------------------------------------------------------

@@ -11,6 +11,7 @@
 // for each step, newest first, the step is recomputed from its start state and the
 // adjoint kernels of adj_*.cu run in the opposite order.  Start states are
 // checkpointed every C steps and recomputed between checkpoints (C ~ sqrt(K)).
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -49,6 +50,7 @@ struct fmf_adj {
   double *sfst[3], *sfstn[3], *E[3], *AB[6], *wallc, *ustar[3], *un2[3], *snaps, *sorpart;
   double *un[3], *pn, *dp, *div, *pr, *pi, *as_f, *an_f, *ap_f, *red;
   double* csfwork;  // forward CSF chain (drop-in): G(3n) rn(12n) kap(3n) g(3n) f(3n)
+  int* band;        // MTHINC band-cell list and its length
   // adjoints
   double* lS[NSTATE];  // adjoint of the step-start state (in/out of reverse_step)
   double *lgx[3], *lfl[3], *lrn, *ltheta, *lphn0, *lphn1, *lrho, *lrhon, *lrmu, *lrmun;
@@ -61,6 +63,21 @@ struct fmf_adj {
   std::vector<double*> ckpt;
   std::vector<double*> seg;
   int sor_total = 0, adj_total = 0;
+  double t_phase[3] = {0.0, 0.0, 0.0};  // seconds: forward, segment recomputation, reverse
+  // record slots: what reverse_step reads of one step (its intermediates and its
+  // start state), one slot per step of a checkpoint segment when memory allows
+  struct Rec {
+    double *gx1[3], *fl[3], *pb, *pass, *pc, *theta, *phn1f, *rho, *rhon, *rmu, *rmun;
+    double *adv[3], *advo[3], *prs[3], *vis[3], *sfst[3], *sfstn[3], *sk, *E[3], *AB[6], *ustar[3], *un2[3];
+    double *wallc, *sums, *state;
+    int* band;
+  };
+  std::vector<Rec> recs;
+  std::vector<void*> rec_blocks;
+  double* lblock = nullptr;  // the intermediate adjoints (one memset per reverse step)
+  long lblock_n = 0;
+  adj::GraphCache graphs;      // transposed viscous iterations, one per record slot
+  double* host_norm = nullptr;  // pinned
 };
 
 namespace {
@@ -79,6 +96,93 @@ struct Scope {
   ~Scope() { scratch_set_use(nullptr); }
 };
 void zero(fmf_adj* a, double* p, long n) { FMF_CUDA(cudaMemsetAsync(p, 0, sizeof(double) * n, a->s)); }
+
+// the record fields of a point at slot r
+void set_rec(fmf_adj* a, const fmf_adj::Rec& r) {
+  for (int q = 0; q < 3; ++q) {
+    a->gx1[q] = r.gx1[q];
+    a->fl[q] = r.fl[q];
+    a->adv[q] = r.adv[q];
+    a->advo[q] = r.advo[q];
+    a->prs[q] = r.prs[q];
+    a->vis[q] = r.vis[q];
+    a->sfst[q] = r.sfst[q];
+    a->sfstn[q] = r.sfstn[q];
+    a->E[q] = r.E[q];
+    a->ustar[q] = r.ustar[q];
+    a->un2[q] = r.un2[q];
+  }
+  for (int q = 0; q < 6; ++q) a->AB[q] = r.AB[q];
+  a->pb = r.pb;
+  a->pass = r.pass;
+  a->pc = r.pc;
+  a->theta = r.theta;
+  a->phn1f = r.phn1f;
+  a->rho = r.rho;
+  a->rhon = r.rhon;
+  a->rmu = r.rmu;
+  a->rmun = r.rmun;
+  a->sk = r.sk;
+  a->wallc = r.wallc;
+  a->sums = r.sums;
+  a->band = r.band;
+}
+long nwall(const Grid& g) { return 4L * (g.nk + 6) * (g.ni + 6); }
+long nband_d(const Grid& g) { return ((long)(g.ni + 2) * (g.nj + 2) * (g.nk + 2) + 2) / 2 + 1; }
+long slot_doubles(const Grid& g) { return 66 * g.n + nwall(g) + 8 + nband_d(g) + 16; }
+// carve one slot out of a block of slot_doubles(g) doubles
+fmf_adj::Rec carve(const Grid& g, double* p) {
+  const long n = g.n;
+  fmf_adj::Rec r;
+  auto take = [&](long k) {
+    double* q = p;
+    p += k;
+    return q;
+  };
+  for (int q = 0; q < 3; ++q) {
+    r.gx1[q] = take(n);
+    r.fl[q] = take(n);
+    r.adv[q] = take(n);
+    r.advo[q] = take(n);
+    r.prs[q] = take(n);
+    r.vis[q] = take(n);
+    r.sfst[q] = take(n);
+    r.sfstn[q] = take(n);
+    r.E[q] = take(n);
+    r.ustar[q] = take(n);
+    r.un2[q] = take(n);
+  }
+  for (int q = 0; q < 6; ++q) r.AB[q] = take(n);
+  r.pb = take(n);
+  r.pass = take(n);
+  r.pc = take(n);
+  r.theta = take(n);
+  r.phn1f = take(n);
+  r.rho = take(n);
+  r.rhon = take(n);
+  r.rmu = take(n);
+  r.rmun = take(n);
+  r.sk = take(6 * n);
+  r.state = take(12 * n);
+  r.wallc = take(nwall(g));
+  r.sums = take(8);
+  r.band = (int*)take(nband_d(g));
+  return r;
+}
+// grow the record slots to `want` (at least one), keeping 2 GiB of the device free
+void grow_recs(fmf_adj* a, int want) {
+  const size_t bytes = sizeof(double) * (size_t)slot_doubles(a->g);
+  while ((int)a->recs.size() < want) {
+    size_t fr = 0, tot = 0;
+    FMF_CUDA(cudaMemGetInfo(&fr, &tot));
+    if (!a->recs.empty() && fr < bytes + (2ull << 30)) break;
+    void* p = nullptr;
+    if (!FMF_CUDA(cudaMalloc(&p, bytes))) break;
+    FMF_CUDA(cudaMemsetAsync(p, 0, bytes, a->s));
+    a->rec_blocks.push_back(p);
+    a->recs.push_back(carve(a->g, (double*)p));
+  }
+}
 void dcopy(fmf_adj* a, const double* src, double* dst, long n) {
   FMF_CUDA(cudaMemcpyAsync(dst, src, sizeof(double) * n, cudaMemcpyDeviceToDevice, a->s));
 }
@@ -221,8 +325,11 @@ int record_step(fmf_adj* a) {
   double *phi0 = S[SPHI0], *phi1 = S[SPHI1], *phn0 = S[SPHIN0], *phn1 = S[SPHIN1];
   // :491-503
   op::cal_grad_p2a(s, g, dxi, dyi, dzi, phi1, a->gx1[0], a->gx1[1], a->gx1[2]);
-  op::solphi_mthinc1(s, g, dxi, dyi, dzi, dt, P.bet_mthinc, phi1, a->gx1[0], a->gx1[1], a->gx1[2], S[SU], S[SV],
-                     S[SW], a->fl[0], a->fl[1], a->fl[2]);
+  {
+    const long nb = (long)(g.ni + 2) * (g.nj + 2) * (g.nk + 2);
+    fused::mthinc_fluxes(s, g, dxi, dyi, dzi, dt, P.bet_mthinc, phi1, a->gx1[0], a->gx1[1], a->gx1[2], S[SU],
+                         S[SV], S[SW], a->fl[0], a->fl[1], a->fl[2], a->band, a->band + nb, false);
+  }
   op::solphi_mthinc2(s, g, dxi, dyi, dzi, dt, S[SU], S[SV], S[SW], a->fl[0], a->fl[1], a->fl[2], phi1, phn1);
   dcopy(a, phn1, a->pa, n);
   op::cal_grad_p2a(s, g, dxi, dyi, dzi, phn1, a->gxn[0], a->gxn[1], a->gxn[2]);
@@ -249,9 +356,15 @@ int record_step(fmf_adj* a) {
   op::calsij(s, g, dxi, dyi, dzi, S[SU], S[SV], S[SW], a->sk);
   op::cal_tau(s, g, a->sk, a->rmu, a->tau, false);
   op::cal_div_tensor(s, g, dxi, dyi, dzi, a->tau, a->vis[0], a->vis[1], a->vis[2]);
-  // :545-573
-  csf_fwd(a, phi1, a->sfst);
-  csf_fwd(a, phn1, a->sfstn);
+  // :545-573 (the fused kernel where the grid tiles; csf_T differentiates the same
+  // sequence of reference subroutines either way)
+  if (fused::csf_supported(g)) {
+    fused::csf_force(s, g, dxi, dyi, dzi, P.rhol, P.rhog, P.sigma, phi1, a->sfst[0], a->sfst[1], a->sfst[2]);
+    fused::csf_force(s, g, dxi, dyi, dzi, P.rhol, P.rhog, P.sigma, phn1, a->sfstn[0], a->sfstn[1], a->sfstn[2]);
+  } else {
+    csf_fwd(a, phi1, a->sfst);
+    csf_fwd(a, phn1, a->sfstn);
+  }
   // :579-623
   const double* advp[3] = {a->adv[0], a->adv[1], a->adv[2]};
   const double* advop[3] = {a->advo[0], a->advo[1], a->advo[2]};
@@ -351,17 +464,7 @@ void reverse_step(fmf_adj* a, const double* st) {
   zero(a, lS[SPHIN0], n);
   zero(a, lS[SPHIN1], n);
   // clear the intermediate adjoints
-  for (int q = 0; q < 3; ++q) {
-    for (double* p : {a->lgx[q], a->lfl[q], a->ladv[q], a->ladvo[q], a->lprs[q], a->lvis[q], a->lsfst[q],
-                      a->lsfstn[q], a->lE[q]})
-      zero(a, p, n);
-  }
-  for (int q = 0; q < 6; ++q) zero(a, a->lAB[q], n);
-  for (double* p : {a->ltheta, a->lrho, a->lrhon, a->lrmu, a->lrmun, a->lphat, a->ldp, a->ldiv})
-    zero(a, p, n);
-  zero(a, a->lsk, 6 * n);
-  zero(a, a->ltau, 6 * n);
-  zero(a, a->lwc, 4L * (g.nk + 6) * (g.ni + 6));
+  zero(a, a->lblock, a->lblock_n);
   // :655-661 pn boundary conditions, wall/halo of un
   adj::periodic_T(s, g, a->lpn);
   adj::neumann_T(s, g, a->lpn);
@@ -384,7 +487,8 @@ void reverse_step(fmf_adj* a, const double* st) {
   adj::sor_replay(s, g, dxi, dyi, dzi, a->rmun, a->E, a->AB, P.uwall, a->wallc, a->ustar, a->snaps);
   const double* lout[3] = {a->lun[0], a->lun[1], a->lun[2]};
   a->adj_total += adj::sor_T(s, g, dxi, dyi, dzi, a->rmun, a->E, a->AB, P.uwall, a->wallc, a->ustar, a->snaps,
-                             lout, a->lam, a->lAB, a->lrmun, a->lE, a->lwc, a->adj_tol, a->adj_max, a->work);
+                             lout, a->lam, a->lAB, a->lrmun, a->lE, a->lwc, a->adj_tol, a->adj_max, a->work,
+                             a->host_norm, &a->graphs);
   check_stage(a, "sor");
   // :579-603 momentum factors, edge viscosities, slip coefficients
   {
@@ -456,9 +560,10 @@ void reverse_step(fmf_adj* a, const double* st) {
   }
   {
     const double* la[3] = {a->ladv[0], a->ladv[1], a->ladv[2]};
-    adj::weno_T(s, g, dxi, dyi, dzi, ST(SU), ST(SV), ST(SW), la, lS[SU], lS[SV], lS[SW]);
+    adj::weno_T(s, g, dxi, dyi, dzi, ST(SU), ST(SV), ST(SW), la, lS[SU], lS[SV], lS[SW], a->work + 3 * n + 1024);
     const double* lao[3] = {a->ladvo[0], a->ladvo[1], a->ladvo[2]};
-    adj::weno_T(s, g, dxi, dyi, dzi, ST(SUO), ST(SVO), ST(SWO), lao, lS[SUO], lS[SVO], lS[SWO]);
+    adj::weno_T(s, g, dxi, dyi, dzi, ST(SUO), ST(SVO), ST(SWO), lao, lS[SUO], lS[SVO], lS[SWO],
+                a->work + 3 * n + 1024);
   }
   // :526-529 mixture properties (phi0 after its contact-angle ghosts, phin0)
   adj::mean_T(s, g, P.rhol, P.rhog, a->lrho, lS[SPHI0]);
@@ -482,7 +587,8 @@ void reverse_step(fmf_adj* a, const double* st) {
   adj::mthinc2_T(s, g, dxi, dyi, dzi, dt, ST(SU), ST(SV), ST(SW), a->fl[0], a->fl[1], a->fl[2], ST(SPHI1), a->pa,
                  a->lphn1, lS[SPHI1], lS[SU], lS[SV], lS[SW], a->lfl[0], a->lfl[1], a->lfl[2], a->lpre);
   adj::mthinc1_T(s, g, dxi, dyi, dzi, dt, P.bet_mthinc, ST(SPHI1), a->gx1[0], a->gx1[1], a->gx1[2], ST(SU), ST(SV),
-                 ST(SW), a->lfl[0], a->lfl[1], a->lfl[2], lS[SPHI1], a->lrn, lS[SU], lS[SV], lS[SW]);
+                 ST(SW), a->lfl[0], a->lfl[1], a->lfl[2], lS[SPHI1], a->lrn, lS[SU], lS[SV], lS[SW], a->band,
+                 a->band + (long)(g.ni + 2) * (g.nj + 2) * (g.nk + 2));
   adj::rn_avg_T(s, g, a->lrn, a->lgx[0], a->lgx[1], a->lgx[2]);
   check_stage(a, "mthinc");
   adj::grad_p2a_T(s, g, dxi, dyi, dzi, a->lgx[0], a->lgx[1], a->lgx[2], lS[SPHI1]);
@@ -549,37 +655,49 @@ int fmf_adj_create(const fmf_params* prm, fmf_adj** out) {
   const long n = a->g.n;
   for (double** p : {&a->theta0, &a->zeta, &a->l1, &a->l2}) *p = dalloc(a, n);
   for (int f = 0; f < NSTATE; ++f) a->S[f] = dalloc(a, n);
-  for (int q = 0; q < 3; ++q) {
-    for (double** p : {&a->gx1[q], &a->fl[q], &a->gxn[q], &a->adv[q], &a->advo[q], &a->prs[q], &a->vis[q],
-                       &a->sfst[q], &a->sfstn[q], &a->E[q], &a->ustar[q], &a->un2[q], &a->un[q], &a->lgx[q],
-                       &a->lfl[q], &a->ladv[q], &a->ladvo[q], &a->lprs[q], &a->lvis[q], &a->lsfst[q],
-                       &a->lsfstn[q], &a->lE[q], &a->lun[q], &a->lam[q]})
-      *p = dalloc(a, n);
-  }
-  for (int q = 0; q < 6; ++q) {
-    a->AB[q] = dalloc(a, n);
-    a->lAB[q] = dalloc(a, n);
-  }
-  for (double** p : {&a->pa, &a->pb, &a->pass, &a->pc, &a->theta, &a->phn1f, &a->rho, &a->rhon, &a->rmu, &a->rmun,
-                     &a->phat, &a->pn, &a->dp, &a->div, &a->ltheta, &a->lphn0, &a->lphn1, &a->lrho, &a->lrhon,
-                     &a->lrmu, &a->lrmun, &a->lphat, &a->lpn, &a->ldp, &a->ldiv, &a->lpre, &a->gtheta0, &a->gzeta,
-                     &a->gl1, &a->gl2, &a->ib_theta1, &a->ib_theta2, &a->ib_phi1, &a->ib_phi0, &a->ib_u, &a->ib_w})
+  for (int q = 0; q < 3; ++q)
+    for (double** p : {&a->gxn[q], &a->un[q], &a->lun[q], &a->lam[q]}) *p = dalloc(a, n);
+  for (double** p : {&a->pa, &a->phat, &a->pn, &a->dp, &a->div, &a->lphn0, &a->lphn1, &a->lpn, &a->lpre,
+                     &a->gtheta0, &a->gzeta, &a->gl1, &a->gl2, &a->ib_theta1, &a->ib_theta2, &a->ib_phi1,
+                     &a->ib_phi0, &a->ib_u, &a->ib_w})
     *p = dalloc(a, n);
-  a->sums = dalloc(a, 8);
   a->red = dalloc(a, 64 + prm->nk);
-  a->sk = dalloc(a, 6 * n);
   a->tau = dalloc(a, 6 * n);
-  a->lsk = dalloc(a, 6 * n);
-  a->ltau = dalloc(a, 6 * n);
-  a->lrn = dalloc(a, 3 * n);
+  a->lrn = dalloc(a, 4 * n);  // 3 normal adjoints + the band-cell marks of mthinc1_T
   const long nwc = 4L * (prm->nk + 6) * (prm->ni + 6);
-  a->wallc = dalloc(a, nwc);
-  a->lwc = dalloc(a, nwc);
+  // the intermediate adjoints cleared at the start of every reverse step, in one block
+  a->lblock_n = 53 * n + nwc;
+  {
+    double* p = dalloc(a, a->lblock_n);
+    a->lblock = p;
+    auto take = [&](long k) {
+      double* q = p;
+      p += k;
+      return q;
+    };
+    for (int q = 0; q < 3; ++q)
+      for (double** f : {&a->lgx[q], &a->lfl[q], &a->ladv[q], &a->ladvo[q], &a->lprs[q], &a->lvis[q], &a->lsfst[q],
+                         &a->lsfstn[q], &a->lE[q]})
+        *f = take(n);
+    for (int q = 0; q < 6; ++q) a->lAB[q] = take(n);
+    for (double** f : {&a->ltheta, &a->lrho, &a->lrhon, &a->lrmu, &a->lrmun, &a->lphat, &a->ldp, &a->ldiv})
+      *f = take(n);
+    a->lsk = take(6 * n);
+    a->ltau = take(6 * n);
+    a->lwc = take(nwc);
+  }
   a->ib_wallc = dalloc(a, nwc);
   a->snaps = dalloc(a, 39 * n);
   a->sorpart = dalloc(a, fused::sor_parts(a->g));
   a->csfwork = dalloc(a, 21 * n);
-  a->work = dalloc(a, 3 * n + 1024 + 42 * n);
+  a->work = dalloc(a, 3 * n + 1024 + 63 * n);  // SOR adjoint, then CSF (42n) or WENO5 (63n) adjoints
+  FMF_CUDA(cudaMallocHost(&a->host_norm, sizeof(double) * 2));
+  grow_recs(a, 1);  // the record of the current step
+  if (a->recs.empty()) {
+    fmf_adj_destroy(a);
+    return FMF_ERR_NOMEM;
+  }
+  set_rec(a, a->recs[0]);
   for (int f = 0; f < NSTATE; ++f) a->lS[f] = dalloc(a, n);
   const long nm = a->g.cells();
   a->pr = dalloc(a, nm);
@@ -617,6 +735,9 @@ int fmf_adj_destroy(fmf_adj* a) {
   if (a->s) cudaStreamSynchronize(a->s);
   for (double* p : a->ckpt) cudaFree(p);
   for (double* p : a->seg) cudaFree(p);
+  for (void* p : a->rec_blocks) cudaFree(p);
+  for (auto& e : a->graphs) cudaGraphExecDestroy(e.second.first);
+  if (a->host_norm) cudaFreeHost(a->host_norm);
   for (void* p : a->allocs) cudaFree(p);
   scratch_set_destroy(a->scr);
   if (a->s) cudaStreamDestroy(a->s);
@@ -657,13 +778,16 @@ int fmf_adj_rollout(fmf_adj* a, int K, int every, const double* const* state0, c
   const long n = a->g.n;
   if (every <= 0) every = (int)std::ceil(std::sqrt((double)K));
   const int nck = (K + every - 1) / every;
-  // checkpoint and segment buffers (grown on demand)
+  // checkpoints, and one record slot per step of a segment where memory allows
+  // (else segment start states only, each step recorded again before its reverse)
   while ((int)a->ckpt.size() < nck) {
     void* p = nullptr;
     if (!FMF_CUDA(cudaMalloc(&p, sizeof(double) * NSTATE * n))) return take_status();
     a->ckpt.push_back((double*)p);
   }
-  while ((int)a->seg.size() < every) {
+  grow_recs(a, every);
+  const bool slots = (int)a->recs.size() >= every;
+  while (!slots && (int)a->seg.size() < every) {
     void* p = nullptr;
     if (!FMF_CUDA(cudaMalloc(&p, sizeof(double) * NSTATE * n))) return take_status();
     a->seg.push_back((double*)p);
@@ -672,9 +796,19 @@ int fmf_adj_rollout(fmf_adj* a, int K, int every, const double* const* state0, c
   for (double* p : {a->gtheta0, a->gzeta, a->gl1, a->gl2}) zero(a, p, n);
   // forward with checkpoints
   init_bc_fwd(a);
-  // keep the init_bc inputs' velocity wall rows (zero initial state) for its reverse
   a->sor_total = 0;
   a->adj_total = 0;
+  set_rec(a, a->recs[0]);
+  using clk = std::chrono::steady_clock;
+  auto lap = [&](clk::time_point& t0) {
+    FMF_CUDA(cudaStreamSynchronize(a->s));
+    const clk::time_point t1 = clk::now();
+    const double dt = std::chrono::duration<double>(t1 - t0).count();
+    t0 = t1;
+    return dt;
+  };
+  for (double& t : a->t_phase) t = 0.0;
+  clk::time_point tp = clk::now();
   for (int t = 0; t < K && !get_status(); ++t) {
     if (t % every == 0) save_state(a, a->ckpt[t / every]);
     record_step(a);
@@ -683,20 +817,40 @@ int fmf_adj_rollout(fmf_adj* a, int K, int every, const double* const* state0, c
   *J = objective(a, a->S[SPHI0], a->lS[SPHI0]);
   for (int f = 0; f < NSTATE; ++f)
     if (f != SPHI0) zero(a, a->lS[f], n);
+  a->t_phase[0] += lap(tp);
   // reverse, segment by segment
   for (int c = nck - 1; c >= 0 && !get_status(); --c) {
     const int t0 = c * every, t1 = std::min(K, t0 + every);
     load_state(a, a->ckpt[c]);
-    for (int t = t0; t < t1; ++t) {
-      save_state(a, a->seg[t - t0]);
-      if (t + 1 < t1) record_step(a);
-    }
-    for (int t = t1 - 1; t >= t0 && !get_status(); --t) {
-      load_state(a, a->seg[t - t0]);
-      record_step(a);
-      reverse_step(a, a->seg[t - t0]);
+    if (slots) {
+      for (int t = t0; t < t1; ++t) {
+        set_rec(a, a->recs[t - t0]);
+        save_state(a, a->recs[t - t0].state);
+        record_step(a);
+      }
+      a->t_phase[1] += lap(tp);
+      for (int t = t1 - 1; t >= t0 && !get_status(); --t) {
+        set_rec(a, a->recs[t - t0]);
+        reverse_step(a, a->recs[t - t0].state);
+      }
+      a->t_phase[2] += lap(tp);
+    } else {
+      set_rec(a, a->recs[0]);
+      for (int t = t0; t < t1; ++t) {
+        save_state(a, a->seg[t - t0]);
+        if (t + 1 < t1) record_step(a);
+      }
+      a->t_phase[1] += lap(tp);
+      for (int t = t1 - 1; t >= t0 && !get_status(); --t) {
+        load_state(a, a->seg[t - t0]);
+        record_step(a);
+        a->t_phase[1] += lap(tp);
+        reverse_step(a, a->seg[t - t0]);
+        a->t_phase[2] += lap(tp);
+      }
     }
   }
+  set_rec(a, a->recs[0]);
   // the start-up pass: recompute its record from the uploaded state
   for (int f = 0; f < NSTATE; ++f)
     FMF_CUDA(cudaMemcpyAsync(a->S[f], state0[f], sizeof(double) * n, cudaMemcpyHostToDevice, a->s));
@@ -718,6 +872,12 @@ int fmf_adj_iterations(fmf_adj* a, int* sor_total, int* adjoint_total) {
   if (!a) return FMF_ERR_ARG;
   if (sor_total) *sor_total = a->sor_total;
   if (adjoint_total) *adjoint_total = a->adj_total;
+  return 0;
+}
+
+int fmf_adj_phase_seconds(fmf_adj* a, double* seconds3) {
+  if (!a || !seconds3) return FMF_ERR_ARG;
+  for (int t = 0; t < 3; ++t) seconds3[t] = a->t_phase[t];
   return 0;
 }
 

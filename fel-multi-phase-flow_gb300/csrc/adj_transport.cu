@@ -109,13 +109,83 @@ __device__ T face_flux(int dir, int side, const T& nx, const T& ny, const T& nz,
 }
 }  // namespace
 
+namespace {
+// band cells (the compact list of the forward pass's k_classify): the Newton offset
+// and the outflow-face fluxes, differentiated with forward-mode numbers
+__global__ void __launch_bounds__(128) k_band_T(Grid g, MC M, double sx, double sy, double sz, double bet,
+                                                const double* __restrict__ phi, const double* __restrict__ gx,
+                                                const double* __restrict__ gy, const double* __restrict__ gz,
+                                                const double* __restrict__ u, const double* __restrict__ v,
+                                                const double* __restrict__ w, const double* __restrict__ lfx,
+                                                const double* __restrict__ lfy, const double* __restrict__ lfz,
+                                                double* lphi, double* __restrict__ lrn, double* lu, double* lv,
+                                                double* lw, const int* __restrict__ list,
+                                                const int* __restrict__ count) {
+  const int nb = *count;
+  const long n = g.n;
+  const long X = 1, Y = g.sy, Z = g.sz;
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < nb; e += gridDim.x * blockDim.x) {
+    const long c = list[e];
+    double L[6], U[6];
+    bool any = false;
+#pragma unroll
+    for (int f = 0; f < 6; ++f) {
+      const long o = (f & 1) ? c : c - (f < 2 ? X : (f < 4 ? Y : Z));
+      const double* lf = f < 2 ? lfx : (f < 4 ? lfy : lfz);
+      const double* vl = f < 2 ? u : (f < 4 ? v : w);
+      L[f] = lf[o];
+      U[f] = vl[o];
+      any = any || ((f & 1) ? U[f] > 0.0 : U[f] < 0.0) && L[f] != 0.0;
+    }
+    if (!any) continue;
+    const double rnx = avg8(gx, c, X, Y, Z), rny = avg8(gy, c, X, Y, Z), rnz = avg8(gz, c, X, Y, Z);
+    const double q00 = sqrt(rnx * rnx + rny * rny + rnz * rnz);
+    const double coef = 1.0 / q00;
+    const double nx = rnx * coef, ny = rny * coef, nz = rnz * coef;
+    using D4 = Dual<4>;
+    const D4 dd = newton_d(D4::var(nx, 0), D4::var(ny, 1), D4::var(nz, 2), D4::var(phi[c], 3), M, bet);
+    double ln[3] = {0.0, 0.0, 0.0}, ld = 0.0;
+    using D5 = Dual<5>;
+    for (int f = 0; f < 6; ++f) {
+      const bool own = (f & 1) ? (U[f] > 0.0) : (U[f] < 0.0);
+      if (!own || L[f] == 0.0) continue;
+      const double sc = f < 2 ? sx : (f < 4 ? sy : sz);
+      const D5 fl = face_flux(f / 2, f & 1, D5::var(nx, 0), D5::var(ny, 1), D5::var(nz, 2), D5::var(dd.v, 3),
+                              D5::var(U[f] * sc, 4), M, bet);
+      ln[0] += L[f] * fl.d[0];
+      ln[1] += L[f] * fl.d[1];
+      ln[2] += L[f] * fl.d[2];
+      ld += L[f] * fl.d[3];
+      const long o = (f & 1) ? c : c - (f < 2 ? X : (f < 4 ? Y : Z));
+      aadd((f < 2 ? lu : (f < 4 ? lv : lw)) + o, L[f] * fl.d[4] * sc);
+    }
+    for (int q = 0; q < 3; ++q) ln[q] += ld * dd.d[q];
+    aadd(lphi + c, ld * dd.d[3]);
+    // n = r/|r|: lr = (ln - n (n.ln)) / |r|
+    const double dot = ln[0] * nx + ln[1] * ny + ln[2] * nz;
+    lrn[c] = (ln[0] - nx * dot) * coef;
+    lrn[c + n] = (ln[1] - ny * dot) * coef;
+    lrn[c + 2 * n] = (ln[2] - nz * dot) * coef;
+  }
+}
+__global__ void k_mark(const int* __restrict__ list, const int* __restrict__ count, double* __restrict__ flag) {
+  const int nb = *count;
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < nb; e += gridDim.x * blockDim.x) flag[list[e]] = 1.0;
+}
+}  // namespace
+
 void mthinc1_T(cudaStream_t s, const Grid& g, double dxi, double dyi, double dzi, double dt, double bet,
                const double* phi, const double* gx, const double* gy, const double* gz, const double* u,
                const double* v, const double* w, const double* lfx, const double* lfy, const double* lfz,
-               double* lphi, double* lrn, double* lu, double* lv, double* lw) {
+               double* lphi, double* lrn, double* lu, double* lv, double* lw, const int* list, const int* count) {
   const Grid G = g;
   const MC M = mconst(dxi, dyi, dzi, bet);
   const long n = g.n;
+  // lrn[3n + c] = 1 marks the band cells of the forward pass (its classification,
+  // not a recomputed one)
+  FMF_CUDA(cudaMemsetAsync(lrn, 0, sizeof(double) * 4 * n, s));
+  k_mark<<<152 * 4, 256, 0, s>>>(list, count, lrn + 3 * n);
+  count_launch();
   range3(s, 0, g.ni + 1, 0, g.nj + 1, 0, g.nk + 1, [=] __device__(int i, int j, int k) {
     const long X = 1, Y = G.sy, Z = G.sz;
     const long c = G.at(i, j, k);
@@ -132,13 +202,9 @@ void mthinc1_T(cudaStream_t s, const Grid& g, double dxi, double dyi, double dzi
       U[f] = vel[f / 2][fo[f]];
       any = any || L[f] != 0.0;
     }
-    lrn[c] = 0.0;
-    lrn[c + n] = 0.0;
-    lrn[c + 2 * n] = 0.0;
     if (!any) return;
-    double rnx = avg8(gx, c, X, Y, Z), rny = avg8(gy, c, X, Y, Z), rnz = avg8(gz, c, X, Y, Z);
-    const double q00 = sqrt(rnx * rnx + rny * rny + rnz * rnz);
-    if (q00 <= M.eps_mthinc * M.dcellinv) {
+    // bulk cells: those the forward pass did not put on its band list
+    if (lrn[c + 3 * n] == 0.0) {
       double phi00 = phi[c];
       double dsnap = 1.0;
       if (phi00 <= M.eps_trunc) {
@@ -158,32 +224,12 @@ void mthinc1_T(cudaStream_t s, const Grid& g, double dxi, double dyi, double dzi
         lp += L[f] * U[f] * sc[f / 2];
       }
       aadd(lphi + c, lp * dsnap);
-      return;
     }
-    const double coef = 1.0 / q00;
-    const double nx = rnx * coef, ny = rny * coef, nz = rnz * coef;
-    using D4 = Dual<4>;
-    const D4 dd = newton_d(D4::var(nx, 0), D4::var(ny, 1), D4::var(nz, 2), D4::var(phi[c], 3), M, bet);
-    double ln[3] = {0.0, 0.0, 0.0}, ld = 0.0;
-    using D5 = Dual<5>;
-    for (int f = 0; f < 6; ++f) {
-      const bool own = (f & 1) ? (U[f] > 0.0) : (U[f] < 0.0);
-      if (!own || L[f] == 0.0) continue;
-      const double vd = U[f] * sc[f / 2];
-      const D5 fl = face_flux(f / 2, f & 1, D5::var(nx, 0), D5::var(ny, 1), D5::var(nz, 2), D5::var(dd.v, 3),
-                              D5::var(vd, 4), M, bet);
-      for (int q = 0; q < 3; ++q) ln[q] += L[f] * fl.d[q];
-      ld += L[f] * fl.d[3];
-      aadd(lvel[f / 2] + fo[f], L[f] * fl.d[4] * sc[f / 2]);
-    }
-    for (int q = 0; q < 3; ++q) ln[q] += ld * dd.d[q];
-    aadd(lphi + c, ld * dd.d[3]);
-    // n = r/|r|: lr = (ln - n (n.ln)) / |r|
-    const double dot = ln[0] * nx + ln[1] * ny + ln[2] * nz;
-    lrn[c] = (ln[0] - nx * dot) * coef;
-    lrn[c + n] = (ln[1] - ny * dot) * coef;
-    lrn[c + 2 * n] = (ln[2] - nz * dot) * coef;
+    // band cells: k_band_T over the forward pass's band list
   });
+  k_band_T<<<152 * 8, 128, 0, s>>>(g, M, dt * dxi, dt * dyi, dt * dzi, bet, phi, gx, gy, gz, u, v, w, lfx, lfy, lfz,
+                                   lphi, lrn, lu, lv, lw, list, count);
+  count_launch();
 }
 
 // cell (i,j,k) averages the vertex gradients (i-1..i, j-1..j, k-1..k); gather over
@@ -224,8 +270,12 @@ void mthinc2_T(cudaStream_t s, const Grid& g, double dxi, double dyi, double dzi
       lpre[c] = 0.0;
       return;
     }
-    const double div00 = (-u[c - X] + u[c]) * dxi + (-v[c - Y] + v[c]) * dyi + (-w[c - Z] + w[c]) * dzi;
-    const double p = phi[c] * (1.0 + dt * div00) + fx[c - X] - fx[c] + fy[c - Y] - fy[c] + fz[c - Z] - fz[c];
+    // the forward value before its clip, rounded operation by operation as
+    // solphi_mthinc2 computes it (this file contracts multiply-adds elsewhere)
+    const double div00 = __dadd_rn(__dadd_rn(__dmul_rn(-u[c - X] + u[c], dxi), __dmul_rn(-v[c - Y] + v[c], dyi)),
+                                   __dmul_rn(-w[c - Z] + w[c], dzi));
+    const double p = __dmul_rn(phi[c], __dadd_rn(1.0, __dmul_rn(dt, div00))) + fx[c - X] - fx[c] + fy[c - Y] -
+                     fy[c] + fz[c - Z] - fz[c];
     const double L = (p >= 0.0 && p <= 1.0) ? lphin[c] : 0.0;
     lphin[c] = 0.0;
     lpre[c] = L;
@@ -258,7 +308,8 @@ void mthinc3_record(cudaStream_t s, const Grid& g, double dxi, double dyi, doubl
     const long c = G.at(i, j, k);
     const bool in = i >= 1 && i <= G.ni && j >= 1 && j <= G.nj && k >= 1 && k <= G.nk;
     const double rnx = avg8(gx, c, X, Y, Z), rny = avg8(gy, c, X, Y, Z), rnz = avg8(gz, c, X, Y, Z);
-    const double q00 = sqrt(rnx * rnx + rny * rny + rnz * rnz);
+    // the band test of solphi_mthinc3 rounded operation by operation as it computes it
+    const double q00 = sqrt(__dadd_rn(__dadd_rn(__dmul_rn(rnx, rnx), __dmul_rn(rny, rny)), __dmul_rn(rnz, rnz)));
     double p = pa[c];
     double m = 1.0;
     if (q00 <= M.eps_mthinc * M.dcellinv) {

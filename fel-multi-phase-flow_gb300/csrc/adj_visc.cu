@@ -10,8 +10,10 @@
 // more backward sweep that collects the gradients with respect to A, B, the edge
 // viscosities, mu and the slip coefficients.  The forward states before each sweep
 // of one cycle at the fixed point are replayed from un* (12 snapshots).
+#include "../../include/fmf_capi.h"
 #include "adj.cuh"
 #include "fused.cuh"
+#include "runtime.cuh"
 
 namespace fmf {
 namespace adj {
@@ -185,12 +187,24 @@ const int kPi[4] = {1, 1, 1, 2}, kPj[4] = {1, 1, 2, 1}, kPk[4] = {1, 2, 1, 1};
 dim3 pgrid(const Grid& g) {
   return dim3((unsigned)((g.ni / 2 + 31) / 32), (unsigned)((g.nj / 2 + 7) / 8), (unsigned)(g.nk / 2));
 }
-__global__ void k_diff_norm(const double* a, const double* b, long n, double* part) {
+__global__ void k_copy3(long n, Arr3 a, double* __restrict__ b) {
+  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) {
+    b[t] = a.a[0][t];
+    b[t + n] = a.a[1][t];
+    b[t + 2 * n] = a.a[2][t];
+  }
+}
+// l += lout; part[block] = sum of (l - prev)^2
+__global__ void k_add_diff3(long n, Arr3 l, CArr3 o, const double* __restrict__ prev, double* part) {
   __shared__ double sh[256];
   double acc = 0.0;
   for (long t = blockIdx.x * 256L + threadIdx.x; t < n; t += (long)gridDim.x * 256) {
-    const double d = a[t] - b[t];
-    acc += d * d;
+    for (int c = 0; c < 3; ++c) {
+      const double v = l.a[c][t] + o.a[c][t];
+      l.a[c][t] = v;
+      const double d = v - prev[t + c * n];
+      acc += d * d;
+    }
   }
   sh[threadIdx.x] = acc;
   __syncthreads();
@@ -210,7 +224,7 @@ __global__ void k_sum_small(const double* part, int n, double* out) {
     if ((int)threadIdx.x < st) sh[threadIdx.x] += sh[threadIdx.x + st];
     __syncthreads();
   }
-  if (threadIdx.x == 0) out[0] += sh[0];
+  if (threadIdx.x == 0) out[0] = sh[0];
 }
 }  // namespace
 
@@ -326,19 +340,16 @@ void sor_replay(cudaStream_t s, const Grid& g, double dxi, double dyi, double dz
 int sor_T(cudaStream_t s, const Grid& g, double dxi, double dyi, double dzi, const double* mu, double* const* E,
           double* const* AB, double uwall, const double* wallc, const double* const* ustar, const double* snaps,
           const double* const* lout, double* const* lam, double* const* lAB, double* lmu, double* const* lE,
-          double* lwc, double tol, int maxit, double* work) {
+          double* lwc, double tol, int maxit, double* work, double* host_norm, GraphCache* cache) {
   const VPa p = make_vpa(dxi, dyi, dzi);
   const long n = g.n;
   const CArr4 cf{{mu, E[0], E[1], E[2]}};
   const dim3 grd = pgrid(g), blk(32, 8);
-  double* prev = work;            // 3n
-  double* part = work + 3 * n;        // 512
-  double* nrm = work + 3 * n + 512;   // 2 doubles (read on the host)
-  double hn[2];
+  double* prev = work;              // 3n
+  double* part = work + 3 * n;      // 512
+  double* nrm = work + 3 * n + 512; // 1 double
   // l = lout
   for (int c = 0; c < 3; ++c) FMF_CUDA(cudaMemcpyAsync(lam[c], lout[c], sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
-  double n0 = -1.0;
-  int it = 0;
   auto backward_cycle = [&](bool grad) {
     const Arr3 L{{lam[0], lam[1], lam[2]}};
     for (int comp = 2; comp >= 0; --comp)
@@ -362,31 +373,61 @@ int sor_T(cudaStream_t s, const Grid& g, double dxi, double dyi, double dzi, con
         count_launch();
       }
   };
-  for (it = 0; it < maxit; ++it) {
-    for (int c = 0; c < 3; ++c)
-      FMF_CUDA(cudaMemcpyAsync(prev + c * n, lam[c], sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+  // one iteration l <- lout + G^T l and |l_new - l_old|^2 into nrm: 51 kernels,
+  // replayed as a CUDA graph (one per set of buffers)
+  const Arr3 L3{{lam[0], lam[1], lam[2]}};
+  const CArr3 O3{{lout[0], lout[1], lout[2]}};
+  auto iteration = [&]() {
+    k_copy3<<<608, 256, 0, s>>>(n, L3, prev);
     backward_cycle(false);
-    // l = lout + G^T l
-    for (int c = 0; c < 3; ++c) {
-      double* a = lam[c];
-      const double* b = lout[c];
-      flat(s, n, [=] __device__(long t) { a[t] += b[t]; });
+    k_add_diff3<<<512, 256, 0, s>>>(n, L3, O3, prev, part);
+    k_sum_small<<<1, 256, 0, s>>>(part, 512, nrm);
+    count_launch(3);
+  };
+  cudaGraphExec_t exec = nullptr;
+  long long per_launch = 0;
+  if (cache) {
+    const std::vector<const void*> key = {lam[0], lam[1], lam[2], lout[0], lout[1], lout[2], mu, E[0], E[1], E[2],
+                                          AB[0], AB[2], AB[4], wallc, ustar[0], ustar[2], work};
+    auto itc = cache->find(key);
+    if (itc == cache->end()) {
+      const long long l0 = launches();
+      cudaGraph_t graph = nullptr;
+      if (FMF_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeRelaxed))) {
+        iteration();
+        if (FMF_CUDA(cudaStreamEndCapture(s, &graph)) && FMF_CUDA(cudaGraphInstantiate(&exec, graph, 0))) {
+          per_launch = launches() - l0;
+          count_launch((int)-per_launch);
+          (*cache)[key] = {exec, per_launch};
+        }
+        if (graph) cudaGraphDestroy(graph);
+      }
+    } else {
+      exec = itc->second.first;
+      per_launch = itc->second.second;
     }
-    FMF_CUDA(cudaMemsetAsync(nrm, 0, sizeof(double) * 2, s));
-    for (int c = 0; c < 3; ++c) {
-      k_diff_norm<<<512, 256, 0, s>>>(lam[c], prev + c * n, n, part);
-      k_sum_small<<<1, 256, 0, s>>>(part, 512, nrm);
+  }
+  double n0 = -1.0;
+  int it = 0;
+  for (it = 0; it < maxit; ++it) {
+    if (exec) {
+      FMF_CUDA(cudaGraphLaunch(exec, s));
+      count_launch((int)per_launch);
+    } else {
+      iteration();
     }
-    count_launch(6);
-    FMF_CUDA(cudaMemcpyAsync(hn, nrm, sizeof(double), cudaMemcpyDeviceToHost, s));
+    FMF_CUDA(cudaMemcpyAsync(host_norm, nrm, sizeof(double), cudaMemcpyDeviceToHost, s));
     FMF_CUDA(cudaStreamSynchronize(s));
-    const double d = std::sqrt(hn[0]);
+    const double d = std::sqrt(host_norm[0]);
+    if (!std::isfinite(d)) {
+      set_status(FMF_ERR_NONFINITE);
+      break;
+    }
     if (n0 < 0.0) n0 = d;
     if (!(d > tol * (n0 + 1e-300))) break;
   }
   // gradient pass at the converged adjoint
   backward_cycle(true);
-  (void)prev;
   return it + 1;
 }
 

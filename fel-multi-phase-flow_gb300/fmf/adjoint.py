@@ -31,6 +31,7 @@ def _bind():
     L.fmf_adj_forward.argtypes = [vp, ip, vp, vp, vp, vp, vp, ctypes.POINTER(dp), vp]
     L.fmf_adj_rollout.argtypes = [vp, ip, ip, vp, vp, vp, vp, vp, ctypes.POINTER(dp), vp, vp, vp, vp, vp]
     L.fmf_adj_iterations.argtypes = [vp, ctypes.POINTER(ip), ctypes.POINTER(ip)]
+    L.fmf_adj_phase_seconds.argtypes = [vp, ctypes.POINTER(dp)]
     _bound = True
 
 
@@ -82,6 +83,12 @@ class Adjoint:
         a, b = ctypes.c_int(), ctypes.c_int()
         check(lib().fmf_adj_iterations(self.h, ctypes.byref(a), ctypes.byref(b)), "iterations")
         return a.value, b.value
+
+    def phase_seconds(self):
+        """(forward, segment recomputation, reverse) seconds of the last rollout."""
+        out = (ctypes.c_double * 3)()
+        check(lib().fmf_adj_phase_seconds(self.h, out), "phase_seconds")
+        return tuple(out)
 
 
 def rollout_function(adj: Adjoint, K: int, state0: np.ndarray, every: int = 0):

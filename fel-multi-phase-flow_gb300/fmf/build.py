@@ -3,8 +3,10 @@
 Each translation unit under csrc/ is compiled separately and in parallel, then
 linked into ``fmf/_lib/libfmf.so``.  The drop-in kernels are compiled with
 ``-fmad=false`` so that every multiply and add is rounded separately, in the
-reference's order; the fused step kernels (files named ``fused_*.cu``) let nvcc
-contract multiply-adds.
+reference's order; the fused step kernels (files named ``fused_*.cu``) and the
+arithmetic-heavy adjoint kernels (``adj_mom.cu``, ``adj_visc.cu``,
+``adj_transport.cu``, whose recomputed branch tests round operation by operation
+through explicit intrinsics) let nvcc contract multiply-adds.
 """
 from __future__ import annotations
 
@@ -36,7 +38,8 @@ def sources():
 def _flags(name: str):
     base = ["-O3", "-lineinfo", "-std=c++17", "--extended-lambda", "-Xcompiler", "-fPIC",
             "-Xcompiler", "-O2"] + ARCH
-    base += ["-fmad=true"] if name.startswith("fused_") else ["-fmad=false"]
+    contract = name.startswith("fused_") or name in ("adj_mom.cu", "adj_visc.cu", "adj_transport.cu")
+    base += ["-fmad=true"] if contract else ["-fmad=false"]
     return base
 
 

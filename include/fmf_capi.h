@@ -346,6 +346,9 @@ int fmf_adj_rollout(fmf_adj* adj, int K, int every, const double* const* state0,
                     double* g_zeta, double* g_l1, double* g_l2, double* g_phi);
 /* viscous-solve iterations of the last call: forward (all recomputations) and transposed */
 int fmf_adj_iterations(fmf_adj* adj, int* sor_total, int* adjoint_total);
+/* wall-clock seconds of the last fmf_adj_rollout: forward pass, segment
+ * recomputation, reverse steps */
+int fmf_adj_phase_seconds(fmf_adj* adj, double* seconds3);
 
 #ifdef __cplusplus
 }
