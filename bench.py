@@ -131,6 +131,57 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def adjoint_cost(K, stream):
+    """Adjoint/forward wall-clock ratio of the K-step rollout on the 128x64x64 Couette
+    workload (per-wall-cell angle 75 +- 5 deg), checkpoints every ceil(sqrt(K)):
+    fmf_adj_rollout (J and all gradients) against fmf_adj_forward (J) with the same
+    solver settings (viscous solve to the reference's 1e-3, transposed solve to
+    1e-6), and against the graph-replayed production step (fmf_ctx_step)."""
+    import math
+
+    from fmf import capi
+    from fmf import config as C
+    from fmf.adjoint import Adjoint
+
+    cfg = C.get("couette128")
+    st0 = C.raw_state(cfg)
+    walls = [w.copy() for w in C.wall_arrays(cfg)]
+    every = int(math.ceil(math.sqrt(K)))
+    A = Adjoint(cfg, sor_tol=1e-3, sor_max=21, adj_tol=1e-6, adj_max=200)
+    A.forward(2, st0, walls)
+    A.rollout(2, st0, walls, every=1)
+    t0 = time.perf_counter()
+    J = A.forward(K, st0, walls)
+    t_fwd = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    Ja, _ = A.rollout(K, st0, walls, every=every)
+    t_adj = time.perf_counter() - t0
+    phases = A.phase_seconds()
+    its = A.iterations()
+    A.close()
+    S = capi.Stepper(cfg, stream=stream.cuda_stream)
+    S.upload(st0)
+    S.init_bc()
+    S.step(2)
+    S.sync()
+    S.upload(st0)
+    S.init_bc()
+    S.sync()
+    t0 = time.perf_counter()
+    S.step(K)
+    S.sync()
+    t_ctx = time.perf_counter() - t0
+    S.close()
+    return {"workload": f"couette128 {cfg.ni}x{cfg.nj}x{cfg.nk}", "K": K, "checkpoint_every": every,
+            "objective": "find_interface_positions_lower after K steps", "J": J,
+            "parameters": "theta0, zeta, l1, l2 (wall planes), initial phi",
+            "forward_s": t_fwd, "rollout_s": t_adj, "adjoint_over_forward": t_adj / t_fwd,
+            "adjoint_over_graph_forward": t_adj / t_ctx, "graph_forward_s": t_ctx,
+            "phases_s": {"forward": phases[0], "recompute": phases[1], "reverse": phases[2]},
+            "viscous_iterations": {"forward_all": its[0], "transposed": its[1]},
+            "tolerances": {"sor": 1e-3, "adjoint": 1e-6}}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -139,6 +190,8 @@ def main():
     ap.add_argument("--impl", default="fmf", choices=["fmf", "reference"])
     ap.add_argument("--workload", default=WORKLOAD)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--adjoint-steps", type=int, default=200,
+                    help="K of the adjoint-cost measurement on 128x64x64 (0: skip)")
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"], help="--profile only")
     ap.add_argument("--profile", action="store_true",
                     help="no timing: start-up pass, --warmup steps, then --steps steps (for ncu launch lists)")
@@ -283,7 +336,12 @@ def main():
              "steps_compared": n_err,
              "max_rel_err_vs_fp64": {"phi": rel(9), "u": rel(0), "v": rel(1), "w": rel(2), "p": rel(6)},
              "weno5_ms": ms_stage_m.value,
-             "precision": "fp32: WENO5, MTHINC Newton + Gauss-point fluxes, SOR sweeps; fp64: everything else"}
+             "precision": "fp32: WENO5, MTHINC Newton + Gauss-point fluxes, CSF normals and curvature, viscous "
+                          "sweeps on FP32 corrections (FP64 residual, one refinement step); fp64: state, "
+                          "pressure FFT+TDMA, projection, divergence, volume sums"}
+    adjoint = None
+    if rank == 0 and args.adjoint_steps > 0:
+        adjoint = adjoint_cost(args.adjoint_steps, stream)
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         v, dt = cpu_baseline_sample(cfg, 1)
@@ -301,7 +359,7 @@ def main():
                 "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 12 * bytes_field,
                         "d2h_bytes_per_step": 12 * bytes_field},
                 "gpu_launches": int(launches), "clocks": clk, "roofline": roofline, "cpu_baseline": cpu,
-                "mixed": mixed}
+                "mixed": mixed, "adjoint": adjoint}
         print(json.dumps(line), flush=True)
     g.close()
 

@@ -809,8 +809,14 @@ int fmf_adj_rollout(fmf_adj* a, int K, int every, const double* const* state0, c
   };
   for (double& t : a->t_phase) t = 0.0;
   clk::time_point tp = clk::now();
+  // the last segment is recorded into its slots on the way (it is reversed first)
+  const int tlast = (nck - 1) * every;
   for (int t = 0; t < K && !get_status(); ++t) {
     if (t % every == 0) save_state(a, a->ckpt[t / every]);
+    if (slots && t >= tlast) {
+      set_rec(a, a->recs[t - tlast]);
+      save_state(a, a->recs[t - tlast].state);
+    }
     record_step(a);
   }
   if (get_status()) return take_status();
@@ -821,12 +827,14 @@ int fmf_adj_rollout(fmf_adj* a, int K, int every, const double* const* state0, c
   // reverse, segment by segment
   for (int c = nck - 1; c >= 0 && !get_status(); --c) {
     const int t0 = c * every, t1 = std::min(K, t0 + every);
-    load_state(a, a->ckpt[c]);
     if (slots) {
-      for (int t = t0; t < t1; ++t) {
-        set_rec(a, a->recs[t - t0]);
-        save_state(a, a->recs[t - t0].state);
-        record_step(a);
+      if (c != nck - 1) {
+        load_state(a, a->ckpt[c]);
+        for (int t = t0; t < t1; ++t) {
+          set_rec(a, a->recs[t - t0]);
+          save_state(a, a->recs[t - t0].state);
+          record_step(a);
+        }
       }
       a->t_phase[1] += lap(tp);
       for (int t = t1 - 1; t >= t0 && !get_status(); --t) {
@@ -835,6 +843,7 @@ int fmf_adj_rollout(fmf_adj* a, int K, int every, const double* const* state0, c
       }
       a->t_phase[2] += lap(tp);
     } else {
+      load_state(a, a->ckpt[c]);
       set_rec(a, a->recs[0]);
       for (int t = t0; t < t1; ++t) {
         save_state(a, a->seg[t - t0]);

@@ -86,6 +86,27 @@ __device__ T newton_d(const T& nx, const T& ny, const T& nz, const T& ph, const 
   }
   return d;
 }
+// the same ten steps in plain FP64; *last = the final step
+__device__ double newton_plain(double nx, double ny, double nz, double ph, const MC& M, double bet, double* last) {
+  double a[8];
+  gauss8(nx, ny, nz, M.gp1, M.gp2, M.gp1, M.gp2, M.gp1, M.gp2, a);
+  double d = 0.0, step = 0.0;
+  for (int it = 0; it < 10; ++it) {
+    double f = 0.0, acc = 0.0;
+    for (int t = 0; t < 8; ++t) {
+      const double x = a[t] + d;
+      f = f + 0.125 / (1.0 + exp(-2.0 * bet * x));
+      const double ch = cosh(bet * x);
+      acc = acc + 0.125 / (ch * ch);
+    }
+    f = f - ph;
+    const double df = 0.5 * bet * acc;
+    step = f * df / (df * df + 1.0e-99);
+    d = d - step;
+  }
+  *last = step;
+  return d;
+}
 // flux through one outflow face: dir 0/1/2, side 0 = the lower face (velocity < 0),
 // side 1 = the upper face (velocity > 0)
 template <class T>
@@ -143,7 +164,26 @@ __global__ void __launch_bounds__(128) k_band_T(Grid g, MC M, double sx, double 
     const double coef = 1.0 / q00;
     const double nx = rnx * coef, ny = rny * coef, nz = rnz * coef;
     using D4 = Dual<4>;
-    const D4 dd = newton_d(D4::var(nx, 0), D4::var(ny, 1), D4::var(nz, 2), D4::var(phi[c], 3), M, bet);
+    D4 dd;
+    {
+      // d by the ten Newton steps; where the last step moved d by less than
+      // 1e-13 (1 + |d|) the iteration has converged and dd/dv = -F_v/F_d at d
+      // (F = the 8-point mean - phi), else the derivatives are carried through
+      // the ten steps
+      double last = 0.0;
+      const double dv = newton_plain(nx, ny, nz, phi[c], M, bet, &last);
+      if (fabs(last) <= 1.0e-13 * (1.0 + fabs(dv))) {
+        using D5 = Dual<5>;
+        D5 a[8];
+        const D5 g1(M.gp1), g2(M.gp2);
+        gauss8(D5::var(nx, 0), D5::var(ny, 1), D5::var(nz, 2), g1, g2, g1, g2, g1, g2, a);
+        const D5 F = sig8(a, D5(0.125), bet, D5::var(dv, 4)) - D5::var(phi[c], 3);
+        dd.v = dv;
+        for (int q = 0; q < 4; ++q) dd.d[q] = -F.d[q] / F.d[4];
+      } else {
+        dd = newton_d(D4::var(nx, 0), D4::var(ny, 1), D4::var(nz, 2), D4::var(phi[c], 3), M, bet);
+      }
+    }
     double ln[3] = {0.0, 0.0, 0.0}, ld = 0.0;
     using D5 = Dual<5>;
     for (int f = 0; f < 6; ++f) {
