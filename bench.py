@@ -149,7 +149,7 @@ def adjoint_cost(K, stream):
     every = int(math.ceil(math.sqrt(K)))
     A = Adjoint(cfg, sor_tol=1e-3, sor_max=21, adj_tol=1e-6, adj_max=200)
     A.forward(2, st0, walls)
-    A.rollout(2, st0, walls, every=1)
+    A.rollout(min(K, every), st0, walls, every=every)  # allocates the checkpoint and record slots
     t0 = time.perf_counter()
     J = A.forward(K, st0, walls)
     t_fwd = time.perf_counter() - t0
@@ -192,7 +192,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--adjoint-steps", type=int, default=200,
                     help="K of the adjoint-cost measurement on 128x64x64 (0: skip)")
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"], help="--profile only")
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed", "adjoint"], help="--profile only")
     ap.add_argument("--profile", action="store_true",
                     help="no timing: start-up pass, --warmup steps, then --steps steps (for ncu launch lists)")
     args = ap.parse_args()
@@ -204,6 +204,19 @@ def main():
         from fmf import capi
         from fmf import config as C
         fbuild.build()
+        if args.precision == "adjoint":
+            # --steps K of the adjoint rollout on the workload (for ncu launch lists)
+            from fmf.adjoint import Adjoint
+            cfg = C.get(args.workload)
+            A = Adjoint(cfg, sor_tol=1e-3, sor_max=21, adj_tol=1e-6, adj_max=200)
+            st0 = C.raw_state(cfg)
+            walls = C.wall_arrays(cfg)
+            A.rollout(max(1, args.warmup), st0, walls)
+            J, _ = A.rollout(args.steps, st0, walls)
+            print(json.dumps({"profile": args.workload, "adjoint_steps": args.steps, "J": J,
+                              "iterations": A.iterations()}))
+            A.close()
+            return
         prec = capi.FMF_MIXED if args.precision == "mixed" else capi.FMF_FP64
         g = capi.Stepper(C.get(args.workload), precision=prec)
         g.initial_state()

@@ -320,6 +320,24 @@ int fmf_ctx_time_stage(fmf_ctx* ctx, int stage, int reps, float* ms);
  * Measurement support; no counterpart in the reference. */
 int fmf_measure_fma_rate(int fp64, double* tflops);
 
+/* ---- restart files (host code; no GPU needed) ---------------------------
+ * One Fortran unformatted sequential record, as the reference writes it: u v w p
+ * uo vo wo po (each (ni+6)(nj+6)(nk+6) doubles), phi(0:nbub), time (real*8),
+ * nstep (integer*4), framed with gfortran's 4-byte record markers (subrecords of
+ * at most 2^31-9 bytes).  fields: the 8 arrays in that order. */
+int fmf_write_checkpoint(const char* path, int ni, int nj, int nk, int nbub, int nstep, double time,
+                         const double* const* fields, const double* phi);
+int fmf_read_checkpoint(const char* path, int ni, int nj, int nk, int nbub, int* nstep, double* time,
+                        double* const* fields, double* phi);
+/* dataou.f:1-46: writes x<nstep> (x<nstep>_<ID> if ipara = 1); mirrored arrays are
+ * copied back from the device first */
+void dataou_(int* ipara, int* ID, int* ni, int* nj, int* nk, int* nbub, int* nstep, double* time, double* u,
+             double* v, double* w, double* p, double* uo, double* vo, double* wo, double* po, double* phi);
+/* datain.f:1-46: reads x.inp (x.inp_<ID> if ipara = 1); mirrored arrays are
+ * re-uploaded */
+void datain_(int* ipara, int* ID, int* ni, int* nj, int* nk, int* nbub, int* nstep, double* time, double* u,
+             double* v, double* w, double* p, double* uo, double* vo, double* wo, double* po, double* phi);
+
 /* ===================================================================== part 4
  * Adjoint of the K-step rollout.  No counterpart in the reference (it has no
  * derivatives); the objective is its find_interface_positions_lower

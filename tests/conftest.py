@@ -22,6 +22,13 @@ def orc():
 
 
 @pytest.fixture(scope="session")
+def fmf_built():
+    """Path of the built library (no GPU needed to load it or to call its host code)."""
+    from fmf import build
+    return build.build()
+
+
+@pytest.fixture(scope="session")
 def fmf_lib():
     """The CUDA library, built in-tree; a GPU test fails (not skips) when it is missing."""
     from fmf import build, capi
