@@ -177,7 +177,8 @@ void div_tensor_T(cudaStream_t s, const Grid& g, double dxi, double dyi, double 
 void mthinc1_T(cudaStream_t s, const Grid& g, double dxi, double dyi, double dzi, double dt, double bet,
                const double* phi, const double* gx, const double* gy, const double* gz, const double* u,
                const double* v, const double* w, const double* lfx, const double* lfy, const double* lfz,
-               double* lphi, double* lrn, double* lu, double* lv, double* lw, const int* list, const int* count);
+               double* lphi, double* lrn, double* lu, double* lv, double* lw, const int* list, const int* count,
+               const double* newton);
 // lrn (3 arrays of n: per cell the adjoint of the averaged vertex gradient) -> lgx..lgz
 void rn_avg_T(cudaStream_t s, const Grid& g, const double* lrn, double* lgx, double* lgy, double* lgz);
 void mthinc2_T(cudaStream_t s, const Grid& g, double dxi, double dyi, double dzi, double dt, const double* u,

@@ -9,9 +9,11 @@ namespace adj {
 
 namespace {
 // One side of weno5.h: r = w1 d1 + w2 d2 + w3 d3 with the product-form weights, and
-// its reverse sweep (la[0..4] += dr/d(a5, a3, a1, b1, b3) * lr).
+// its reverse sweep (la[0..4] += dr/d(a5, a3, a1, b1, b3) * lr).  The weights are
+// formed with one reciprocal of the denominator (iD), which the reverse sweep reuses:
+// an adjoint needs the derivative, not the forward's last bit.
 struct Side {
-  double d1, d2, d3, t[6], s1, s2, s3, P1, P2, P3, m1, m2, m3, D, w1, w3, r;
+  double d1, d2, d3, t[6], s1, s2, s3, P1, P2, P3, iD, w1, w3, r;
 };
 __device__ __forceinline__ void side_fwd(double a5, double a3, double a1, double b1, double b3, Side& S) {
   S.d1 = a5 * 2.0 - a3 * 7.0 + a1 * 11.0;
@@ -29,12 +31,10 @@ __device__ __forceinline__ void side_fwd(double a5, double a3, double a1, double
   S.P1 = S.s2 * S.s3;
   S.P2 = S.s1 * S.s3;
   S.P3 = S.s1 * S.s2;
-  S.m1 = S.P1 * S.P1;
-  S.m2 = S.P2 * S.P2 * 6.0;
-  S.m3 = S.P3 * S.P3 * 3.0;
-  S.D = S.m1 + S.m2 + S.m3 + 1.0e-80;
-  S.w1 = S.m1 / S.D;
-  S.w3 = S.m3 / S.D;
+  const double m1 = S.P1 * S.P1, m2 = S.P2 * S.P2 * 6.0, m3 = S.P3 * S.P3 * 3.0;
+  S.iD = 1.0 / (m1 + m2 + m3 + 1.0e-80);
+  S.w1 = m1 * S.iD;
+  S.w3 = m3 * S.iD;
   S.r = S.w1 * S.d1 + (1.0 - S.w1 - S.w3) * S.d2 + S.w3 * S.d3;
 }
 __device__ __forceinline__ void side_rev(const Side& S, double lr, double* la) {
@@ -42,7 +42,7 @@ __device__ __forceinline__ void side_rev(const Side& S, double lr, double* la) {
   const double ld1 = lr * S.w1, ld2 = lr * w2, ld3 = lr * S.w3;
   const double lw1 = lr * (S.d1 - S.d2), lw3 = lr * (S.d3 - S.d2);
   const double G = lw1 * S.w1 + lw3 * S.w3;
-  const double lm1 = (lw1 - G) / S.D, lm2 = -G / S.D, lm3 = (lw3 - G) / S.D;
+  const double lm1 = (lw1 - G) * S.iD, lm2 = -G * S.iD, lm3 = (lw3 - G) * S.iD;
   const double lP1 = 2.0 * S.P1 * lm1, lP2 = 12.0 * S.P2 * lm2, lP3 = 6.0 * S.P3 * lm3;
   const double ls1 = lP2 * S.s3 + lP3 * S.s2, ls2 = lP1 * S.s3 + lP3 * S.s1, ls3 = lP1 * S.s2 + lP2 * S.s1;
   const double lt0 = 26.0 * S.t[0] * ls1, lt1 = 6.0 * S.t[1] * ls1;
@@ -64,25 +64,25 @@ __device__ double wline_T(const double* __restrict__ q, long c, long S, double v
   const double m3 = q[c - 3 * S], m2 = q[c - 2 * S], m1 = q[c - S], z0 = q[c], p1 = q[c + S], p2 = q[c + 2 * S],
                p3 = q[c + 3 * S];
   const double dm5 = -m3 + m2, dm3 = -m2 + m1, dm1 = -m1 + z0, dp1 = -z0 + p1, dp3 = -p1 + p2, dp5 = -p2 + p3;
-  double lvel = 0.0;
-  Side A, B;
-  const bool needA = vel >= 0.0, needB = vel <= 0.0;
-  if (needA) side_fwd(dm5, dm3, dm1, dp1, dp3, A);
-  if (needB) side_fwd(dp5, dp3, dp1, dm1, dm3, B);
-  if (vel > 0.0) {
-    double la[5] = {0, 0, 0, 0, 0};
-    side_rev(A, lr * 2.0 * vel / 12.0, la);
-    lD[0] += la[0]; lD[1] += la[1]; lD[2] += la[2]; lD[3] += la[3]; lD[4] += la[4];
-    lvel = lr * 2.0 * A.r / 12.0;
-  } else if (vel < 0.0) {
-    double la[5] = {0, 0, 0, 0, 0};
-    side_rev(B, lr * 2.0 * vel / 12.0, la);
-    lD[5] += la[0]; lD[4] += la[1]; lD[3] += la[2]; lD[2] += la[3]; lD[1] += la[4];
-    lvel = lr * 2.0 * B.r / 12.0;
-  } else {
-    lvel = lr * (A.r + B.r) / 12.0;
+  // the upwind side (the other one carries the weight 0 in weno5.h), its inputs
+  // mirrored by selects so that one inlined copy serves both signs of vel
+  const bool neg = vel < 0.0;
+  Side A;
+  side_fwd(neg ? dp5 : dm5, neg ? dp3 : dm3, neg ? dp1 : dm1, neg ? dm1 : dp1, neg ? dm3 : dp3, A);
+  if (vel == 0.0) {  // both sides enter d(out)/d(vel); neither enters d(out)/d(q)
+    Side B;
+    side_fwd(dp5, dp3, dp1, dm1, dm3, B);
+    return lr * (A.r + B.r) / 12.0;
   }
-  return lvel;
+  double la[5] = {0, 0, 0, 0, 0};
+  side_rev(A, lr * 2.0 * vel / 12.0, la);
+  lD[0] = neg ? 0.0 : la[0];
+  lD[1] = neg ? la[4] : la[1];
+  lD[2] = neg ? la[3] : la[2];
+  lD[3] = neg ? la[2] : la[3];
+  lD[4] = neg ? la[1] : la[4];
+  lD[5] = neg ? la[0] : 0.0;
+  return lr * 2.0 * A.r / 12.0;
 }
 
 // Offsets (relative to the cell) of the four velocity points that form the
@@ -137,7 +137,9 @@ __global__ void __launch_bounds__(256) k_weno_T2(Grid g, const double* __restric
   // point x sits at stencil position o (-3..3) of the cell x - o*S; its coefficient
   // there: o=-3: -D0, -2: D0-D1, -1: D1-D2, 0: D2-D3, 1: D3-D4, 2: D4-D5, 3: D5
   double acc[3] = {0.0, 0.0, 0.0};
+#pragma unroll
   for (int p = 0; p < 3; ++p) {
+#pragma unroll
     for (int d = 0; d < 3; ++d) {
       const int line = p * 3 + d;
       const double* Dl = D + (long)line * 6 * n;
@@ -188,7 +190,7 @@ void csf_T(cudaStream_t s, const Grid& g, double dxi, double dyi, double dzi, do
   double* kap = work + 15 * n;   // curvature at u, v, w points (3n)
   double* gq = work + 18 * n;    // face gradient of phi (3n)
   double* lG = work + 21 * n;    // adjoint of the vertex gradient (3n)
-  double* lrn = work + 24 * n;   // adjoint of the normals (12n)
+  double* lv = work + 24 * n;    // per normal family: adjoint of its 8-point mean (12n)
   double* lkap = work + 36 * n;  // adjoint of the curvature (3n)
   double* lgq = work + 39 * n;   // adjoint of the face gradient (3n)
   static const int offs[4][3] = {{1, 1, 1}, {0, 0, 1}, {0, 1, 0}, {1, 0, 0}};
@@ -198,7 +200,6 @@ void csf_T(cudaStream_t s, const Grid& g, double dxi, double dyi, double dzi, do
     op::calrn(s, g, dxi, dyi, dzi, offs[q][0], offs[q][1], offs[q][2], Gv, Gv + n, Gv + 2 * n, rn + 3 * n * q);
   op::calrkap(s, g, dxi, dyi, dzi, rn, rn + 3 * n, rn + 6 * n, rn + 9 * n, kap);
   op::cal_grad_prs(s, g, dxi, dyi, dzi, phi, gq, gq + n, gq + 2 * n);
-  FMF_CUDA(cudaMemsetAsync(lG, 0, sizeof(double) * 21 * n, s));
   // calfst: f_c = -st kap_c g_c
   const double st = 2.0 * sigma / (rhol + rhog);
   const double *lf0 = lf[0], *lf1 = lf[1], *lf2 = lf[2];
@@ -210,56 +211,64 @@ void csf_T(cudaStream_t s, const Grid& g, double dxi, double dyi, double dzi, do
     }
   });
   grad_prs_T(s, g, dxi, dyi, dzi, lgq, lgq + n, lgq + 2 * n, lphi);
-  // calrkap (pp = family 0, r12 = 1, r13 = 2, r23 = 3)
-  double* lpp = lrn;
-  double* l12 = lrn + 3 * n;
-  double* l13 = lrn + 6 * n;
-  double* l23 = lrn + 9 * n;
+  // calrkap and calrn reversed as two gathers (no atomics).
+  // Families (calrkap's rn arguments): 0 = pp (offset 1,1,1), 1 = r12 (0,0,1),
+  // 2 = r13 (0,1,0), 3 = r23 (1,0,0).  Family f's normal at o is N(v) = v/(|v| + vs)
+  // of the mean v of Gv over o - {0,X_f} - {0,Y_f} - {0,Z_f} (X_f = 0 where the
+  // offset is 0), written by calrn for o_i in [-2 + ip, ni+3] (same in j, k).
+  // calrkap writes the u curvature where k >= -1, j >= -1, i <= ni+2, the v one where
+  // k >= -1, j <= nj+2, i >= -1, the w one where k <= nk+2, j >= -1, i >= -1.
+  const double vs = std::sqrt(dxi * dxi + dyi * dyi + dzi * dzi) * 1.0e-30;
+  // pass 1, per normal point o and family: the normal's adjoint gathered from the
+  // curvatures that read it, then lv = (dN/dv)^T lrn
   range3(s, -2, g.ni + 3, -2, g.nj + 3, -2, g.nk + 3, [=] __device__(int i, int j, int k) {
     const long X = 1, Y = G.sy, Z = G.sz;
     const long c = G.at(i, j, k);
-    double L;
-    if (k >= -1 && j >= -1 && i <= G.ni + 2 && (L = lkap[c]) != 0.0) {
-      aadd(lpp + c + X, dxi * L);
-      aadd(lpp + c, -dxi * L);
-      aadd(l12 + c + n, dyi * L);
-      aadd(l12 + c - Y + n, -dyi * L);
-      aadd(l13 + c + 2 * n, dzi * L);
-      aadd(l13 + c - Z + 2 * n, -dzi * L);
-    }
-    if (k >= -1 && j <= G.nj + 2 && i >= -1 && (L = lkap[c + n]) != 0.0) {
-      aadd(l12 + c, dxi * L);
-      aadd(l12 + c - X, -dxi * L);
-      aadd(lpp + c + Y + n, dyi * L);
-      aadd(lpp + c + n, -dyi * L);
-      aadd(l23 + c + 2 * n, dzi * L);
-      aadd(l23 + c - Z + 2 * n, -dzi * L);
-    }
-    if (k <= G.nk + 2 && j >= -1 && i >= -1 && (L = lkap[c + 2 * n]) != 0.0) {
-      aadd(l13 + c, dxi * L);
-      aadd(l13 + c - X, -dxi * L);
-      aadd(l23 + c + n, dyi * L);
-      aadd(l23 + c - Y + n, -dyi * L);
-      aadd(lpp + c + Z + 2 * n, dzi * L);
-      aadd(lpp + c + 2 * n, -dzi * L);
-    }
-  });
-  // calrn: N(v) = v/(|v| + vs) of the 8-point mean v
-  const double vs = std::sqrt(dxi * dxi + dyi * dyi + dzi * dzi) * 1.0e-30;
-  for (int q = 0; q < 4; ++q) {
-    const int ip = offs[q][0], jp = offs[q][1], kp = offs[q][2];
-    const double* L3 = lrn + 3 * n * q;
-    range3(s, -2, g.ni + 3 - ip, -2, g.nj + 3 - jp, -2, g.nk + 3 - kp, [=] __device__(int i, int j, int k) {
-      const long c = G.at(i, j, k);
-      const long X = ip, Y = jp ? G.sy : 0, Z = kp ? G.sz : 0;
-      const long o = c + X + Y + Z;
-      const double lx = L3[o], ly = L3[o + n], lz = L3[o + 2 * n];
-      if (lx == 0.0 && ly == 0.0 && lz == 0.0) return;
-      const long pts[8] = {c, c + X, c + Y, c + X + Y, c + Z, c + X + Z, c + Y + Z, c + X + Y + Z};
-      double r[3] = {0.0, 0.0, 0.0};
+    auto in = [&](int a, int b, int e) {
+      return a >= -2 && a <= G.ni + 3 && b >= -2 && b <= G.nj + 3 && e >= -2 && e <= G.nk + 3;
+    };
+    auto ku = [&](int a, int b, int e, long o) {
+      return in(a, b, e) && e >= -1 && b >= -1 && a <= G.ni + 2 ? lkap[o] : 0.0;
+    };
+    auto kv = [&](int a, int b, int e, long o) {
+      return in(a, b, e) && e >= -1 && b <= G.nj + 2 && a >= -1 ? lkap[o + n] : 0.0;
+    };
+    auto kw = [&](int a, int b, int e, long o) {
+      return in(a, b, e) && e <= G.nk + 2 && b >= -1 && a >= -1 ? lkap[o + 2 * n] : 0.0;
+    };
+    // kap_u = dxi (pp_x[+X] - pp_x) + dyi (r12_y - r12_y[-Y]) + dzi (r13_z - r13_z[-Z]),
+    // kap_v = dxi (r12_x - r12_x[-X]) + dyi (pp_y[+Y] - pp_y) + dzi (r23_z - r23_z[-Z]),
+    // kap_w = dxi (r13_x - r13_x[-X]) + dyi (r23_y - r23_y[-Y]) + dzi (pp_z[+Z] - pp_z)
+    double L[4][3];
+    L[0][0] = dxi * (ku(i - 1, j, k, c - X) - ku(i, j, k, c));
+    L[0][1] = dyi * (kv(i, j - 1, k, c - Y) - kv(i, j, k, c));
+    L[0][2] = dzi * (kw(i, j, k - 1, c - Z) - kw(i, j, k, c));
+    L[1][0] = dxi * (kv(i, j, k, c) - kv(i + 1, j, k, c + X));
+    L[1][1] = dyi * (ku(i, j, k, c) - ku(i, j + 1, k, c + Y));
+    L[1][2] = 0.0;
+    L[2][0] = dxi * (kw(i, j, k, c) - kw(i + 1, j, k, c + X));
+    L[2][1] = 0.0;
+    L[2][2] = dzi * (ku(i, j, k, c) - ku(i, j, k + 1, c + Z));
+    L[3][0] = 0.0;
+    L[3][1] = dyi * (kw(i, j, k, c) - kw(i, j + 1, k, c + Y));
+    L[3][2] = dzi * (kv(i, j, k, c) - kv(i, j, k + 1, c + Z));
+#pragma unroll
+    for (int f = 0; f < 4; ++f) {
+      const int ip = f == 0 || f == 3, jp = f == 0 || f == 2, kp = f == 0 || f == 1;
+      if (i < -2 + ip || j < -2 + jp || k < -2 + kp) continue;  // calrn does not write o
+      double* out = lv + 3 * n * f + c;
+      const double lx = L[f][0], ly = L[f][1], lz = L[f][2];
+      if (lx == 0.0 && ly == 0.0 && lz == 0.0) {
+        out[0] = out[n] = out[2 * n] = 0.0;
+        continue;
+      }
+      const long Xf = ip ? X : 0, Yf = jp ? Y : 0, Zf = kp ? Z : 0;
+      const long b = c - Xf - Yf - Zf;
+      double r[3];
+#pragma unroll
       for (int q3 = 0; q3 < 3; ++q3) {
-        const double* p = Gv + q3 * n;
-        r[q3] = (p[pts[0]] + p[pts[1]] + p[pts[2]] + p[pts[3]] + p[pts[4]] + p[pts[5]] + p[pts[6]] + p[pts[7]]) * 0.125;
+        const double* p = Gv + q3 * n + b;
+        r[q3] = (p[0] + p[Xf] + p[Yf] + p[Xf + Yf] + p[Zf] + p[Xf + Zf] + p[Yf + Zf] + p[Xf + Yf + Zf]) * 0.125;
       }
       const double m = sqrt(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]);
       const double a = m + vs;
@@ -269,11 +278,45 @@ void csf_T(cudaStream_t s, const Grid& g, double dxi, double dyi, double dzi, do
         for (int q3 = 0; q3 < 3; ++q3) e[q3] = r[q3] / m;
         corr = (e[0] * lx + e[1] * ly + e[2] * lz) * (m / (a * a));
       }
-      const double lv[3] = {lx / a - e[0] * corr, ly / a - e[1] * corr, lz / a - e[2] * corr};
-      for (int q3 = 0; q3 < 3; ++q3)
-        for (int t = 0; t < 8; ++t) aadd(lG + q3 * n + pts[t], 0.125 * lv[q3]);
-    });
-  }
+      out[0] = lx / a - e[0] * corr;
+      out[n] = ly / a - e[1] * corr;
+      out[2 * n] = lz / a - e[2] * corr;
+    }
+  });
+  // pass 2, per vertex p: 0.125 lv over the (family, corner) pairs whose mean reads
+  // p, i.e. o = p + {0,X_f} + {0,Y_f} + {0,Z_f} (families 1-3 read two points, four
+  // times each)
+  range3(s, -2, g.ni + 3, -2, g.nj + 3, -2, g.nk + 3, [=] __device__(int i, int j, int k) {
+    const long X = 1, Y = G.sy, Z = G.sz;
+    const long c = G.at(i, j, k);
+    auto ok = [&](int f, int a, int b, int e) {
+      const int ip = f == 0 || f == 3, jp = f == 0 || f == 2, kp = f == 0 || f == 1;
+      return a >= -2 + ip && a <= G.ni + 3 && b >= -2 + jp && b <= G.nj + 3 && e >= -2 + kp && e <= G.nk + 3;
+    };
+    const bool a1 = ok(1, i, j, k), b1 = ok(1, i, j, k + 1), a2 = ok(2, i, j, k), b2 = ok(2, i, j + 1, k),
+               a3 = ok(3, i, j, k), b3 = ok(3, i + 1, j, k);
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+      const double* L0 = lv + q * n + c;
+      double acc = 0.0;
+#pragma unroll
+      for (int t = 0; t < 8; ++t) {
+        const int di = t & 1, dj = (t >> 1) & 1, dk = t >> 2;
+        if (ok(0, i + di, j + dj, k + dk)) acc += L0[di * X + dj * Y + dk * Z];
+      }
+      const double* L1 = L0 + 3 * n;
+      const double* L2 = L0 + 6 * n;
+      const double* L3 = L0 + 9 * n;
+      double acc4 = 0.0;
+      if (a1) acc4 += L1[0];
+      if (b1) acc4 += L1[Z];
+      if (a2) acc4 += L2[0];
+      if (b2) acc4 += L2[Y];
+      if (a3) acc4 += L3[0];
+      if (b3) acc4 += L3[X];
+      lG[q * n + c] = 0.125 * (acc + 4.0 * acc4);
+    }
+  });
   grad_p2a_T(s, g, dxi, dyi, dzi, lG, lG + n, lG + 2 * n, lphi);
 }
 

@@ -16,6 +16,8 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <map>
+#include <string>
 #include <vector>
 
 #include "../../include/fmf_capi.h"
@@ -30,12 +32,51 @@ namespace {
 enum { SU, SV, SW, SUO, SVO, SWO, SP, SPO, SPHI0, SPHI1, SPHIN0, SPHIN1, NSTATE };
 }
 
+// Per-stage device time of the reverse steps (FMF_ADJ_TIME set: CUDA events at the
+// stage boundaries, summed per stage and printed to stderr when the handle closes)
+struct StageTimer {
+  bool on = std::getenv("FMF_ADJ_TIME") != nullptr;
+  std::vector<cudaEvent_t> ev;
+  std::vector<const char*> name;
+  size_t used = 0;
+  std::map<std::string, double> ms;
+  void mark(cudaStream_t s, const char* stage) {
+    if (!on) return;
+    if (used == ev.size()) {
+      cudaEvent_t e = nullptr;
+      if (cudaEventCreate(&e) != cudaSuccess) return;
+      ev.push_back(e);
+      name.push_back(nullptr);
+    }
+    name[used] = stage;
+    cudaEventRecord(ev[used++], s);
+  }
+  void flush(cudaStream_t s) {
+    if (!on || used == 0) return;
+    cudaStreamSynchronize(s);
+    for (size_t t = 1; t < used; ++t) {
+      float v = 0.0f;
+      if (cudaEventElapsedTime(&v, ev[t - 1], ev[t]) == cudaSuccess) ms[name[t]] += v;
+    }
+    used = 0;
+  }
+  ~StageTimer() {
+    if (on && !ms.empty()) {
+      double tot = 0.0;
+      for (auto& e : ms) tot += e.second;
+      for (auto& e : ms) std::fprintf(stderr, "adjoint stage %-10s %10.3f ms  %5.1f %%\n", e.first.c_str(), e.second, 100.0 * e.second / tot);
+    }
+    for (cudaEvent_t e : ev) cudaEventDestroy(e);
+  }
+};
+
 struct fmf_adj {
   fmf_params prm;
   Grid g;
   cudaStream_t s = nullptr;
   void* scr = nullptr;
   std::vector<void*> allocs;
+  StageTimer stimer;
   double sor_tol = 1.0e-3;
   int sor_max = 21;
   double adj_tol = 1.0e-12;
@@ -51,6 +92,7 @@ struct fmf_adj {
   double *un[3], *pn, *dp, *div, *pr, *pi, *as_f, *an_f, *ap_f, *red;
   double* csfwork;  // forward CSF chain (drop-in): G(3n) rn(12n) kap(3n) g(3n) f(3n)
   int* band;        // MTHINC band-cell list and its length
+  double* newton;   // per band-list entry: Newton offset, last Newton step
   // adjoints
   double* lS[NSTATE];  // adjoint of the step-start state (in/out of reverse_step)
   double *lgx[3], *lfl[3], *lrn, *ltheta, *lphn0, *lphn1, *lrho, *lrhon, *lrmu, *lrmun;
@@ -69,7 +111,7 @@ struct fmf_adj {
   struct Rec {
     double *gx1[3], *fl[3], *pb, *pass, *pc, *theta, *phn1f, *rho, *rhon, *rmu, *rmun;
     double *adv[3], *advo[3], *prs[3], *vis[3], *sfst[3], *sfstn[3], *sk, *E[3], *AB[6], *ustar[3], *un2[3];
-    double *wallc, *sums, *state;
+    double *wallc, *sums, *state, *newton;
     int* band;
   };
   std::vector<Rec> recs;
@@ -126,10 +168,12 @@ void set_rec(fmf_adj* a, const fmf_adj::Rec& r) {
   a->wallc = r.wallc;
   a->sums = r.sums;
   a->band = r.band;
+  a->newton = r.newton;
 }
 long nwall(const Grid& g) { return 4L * (g.nk + 6) * (g.ni + 6); }
 long nband_d(const Grid& g) { return ((long)(g.ni + 2) * (g.nj + 2) * (g.nk + 2) + 2) / 2 + 1; }
-long slot_doubles(const Grid& g) { return 66 * g.n + nwall(g) + 8 + nband_d(g) + 16; }
+long nband(const Grid& g) { return (long)(g.ni + 2) * (g.nj + 2) * (g.nk + 2); }
+long slot_doubles(const Grid& g) { return 66 * g.n + nwall(g) + 8 + 2 * nband(g) + nband_d(g) + 16; }
 // carve one slot out of a block of slot_doubles(g) doubles
 fmf_adj::Rec carve(const Grid& g, double* p) {
   const long n = g.n;
@@ -166,6 +210,7 @@ fmf_adj::Rec carve(const Grid& g, double* p) {
   r.state = take(12 * n);
   r.wallc = take(nwall(g));
   r.sums = take(8);
+  r.newton = take(2 * nband(g));
   r.band = (int*)take(nband_d(g));
   return r;
 }
@@ -226,6 +271,7 @@ __global__ void k_nonfinite(const double* p, long n, int* flag) {
 // With FMF_ADJ_CHECK set in the environment: after each stage of the reverse step,
 // report on stderr the first stage that left a non-finite adjoint value.
 void check_stage(fmf_adj* a, const char* stage) {
+  a->stimer.mark(a->s, stage);
   static const bool on = std::getenv("FMF_ADJ_CHECK") != nullptr;
   static bool reported = false;
   if (!on || reported) return;
@@ -328,7 +374,7 @@ int record_step(fmf_adj* a) {
   {
     const long nb = (long)(g.ni + 2) * (g.nj + 2) * (g.nk + 2);
     fused::mthinc_fluxes(s, g, dxi, dyi, dzi, dt, P.bet_mthinc, phi1, a->gx1[0], a->gx1[1], a->gx1[2], S[SU],
-                         S[SV], S[SW], a->fl[0], a->fl[1], a->fl[2], a->band, a->band + nb, false);
+                         S[SV], S[SW], a->fl[0], a->fl[1], a->fl[2], a->band, a->band + nb, false, a->newton);
   }
   op::solphi_mthinc2(s, g, dxi, dyi, dzi, dt, S[SU], S[SV], S[SW], a->fl[0], a->fl[1], a->fl[2], phi1, phn1);
   dcopy(a, phn1, a->pa, n);
@@ -440,6 +486,7 @@ void reverse_step(fmf_adj* a, const double* st) {
   const double dxi = 1.0 / P.dx, dyi = 1.0 / P.dy, dzi = 1.0 / P.dz, dt = P.dt;
   auto ST = [&](int f) { return st + (long)f * n; };
   double** lS = a->lS;
+  a->stimer.mark(s, "begin");
   // :686-697 rotation: u' = un, uo' = u, p' = pn, po' = p, phi' = phin' = phin
   for (int q = 0; q < 3; ++q) {
     dcopy(a, lS[SU + q], a->lun[q], n);
@@ -485,6 +532,7 @@ void reverse_step(fmf_adj* a, const double* st) {
   adj::wall_halo_T(s, g, 7, P.uwall, a->wallc, a->ustar[0], a->ustar[2], a->lun[0], a->lun[1], a->lun[2], a->lwc);
   // :605-623 the viscous solve
   adj::sor_replay(s, g, dxi, dyi, dzi, a->rmun, a->E, a->AB, P.uwall, a->wallc, a->ustar, a->snaps);
+  check_stage(a, "replay");
   const double* lout[3] = {a->lun[0], a->lun[1], a->lun[2]};
   a->adj_total += adj::sor_T(s, g, dxi, dyi, dzi, a->rmun, a->E, a->AB, P.uwall, a->wallc, a->ustar, a->snaps,
                              lout, a->lam, a->lAB, a->lrmun, a->lE, a->lwc, a->adj_tol, a->adj_max, a->work,
@@ -542,6 +590,7 @@ void reverse_step(fmf_adj* a, const double* st) {
     const double* lfn[3] = {a->lsfstn[0], a->lsfstn[1], a->lsfstn[2]};
     adj::csf_T(s, g, dxi, dyi, dzi, P.rhol, P.rhog, P.sigma, a->phn1f, lfn, a->lphn1, a->work + 3 * n + 1024);
   }
+  check_stage(a, "csf");
   // :536-541 explicit viscous term, pressure gradient, advection
   adj::div_tensor_T(s, g, dxi, dyi, dzi, a->lvis[0], a->lvis[1], a->lvis[2], a->ltau);
   adj::tau_T(s, g, a->sk, a->rmu, a->ltau, a->lsk, a->lrmu);
@@ -565,6 +614,7 @@ void reverse_step(fmf_adj* a, const double* st) {
     adj::weno_T(s, g, dxi, dyi, dzi, ST(SUO), ST(SVO), ST(SWO), lao, lS[SUO], lS[SVO], lS[SWO],
                 a->work + 3 * n + 1024);
   }
+  check_stage(a, "weno");
   // :526-529 mixture properties (phi0 after its contact-angle ghosts, phin0)
   adj::mean_T(s, g, P.rhol, P.rhog, a->lrho, lS[SPHI0]);
   adj::mean_T(s, g, P.rmul, P.rmug, a->lrmu, lS[SPHI0]);
@@ -584,14 +634,18 @@ void reverse_step(fmf_adj* a, const double* st) {
   check_stage(a, "gnbc");
   adj::mthinc3_T(s, g, a->pb, a->pass, a->sums, a->lphn1, lS[SPHI1], a->sums + 4);
   adj::phin_stale_T(s, g, a->pass, a->lphn1, lS[SPHIN1]);
+  check_stage(a, "mthinc3");
   adj::mthinc2_T(s, g, dxi, dyi, dzi, dt, ST(SU), ST(SV), ST(SW), a->fl[0], a->fl[1], a->fl[2], ST(SPHI1), a->pa,
                  a->lphn1, lS[SPHI1], lS[SU], lS[SV], lS[SW], a->lfl[0], a->lfl[1], a->lfl[2], a->lpre);
+  check_stage(a, "mthinc2");
   adj::mthinc1_T(s, g, dxi, dyi, dzi, dt, P.bet_mthinc, ST(SPHI1), a->gx1[0], a->gx1[1], a->gx1[2], ST(SU), ST(SV),
                  ST(SW), a->lfl[0], a->lfl[1], a->lfl[2], lS[SPHI1], a->lrn, lS[SU], lS[SV], lS[SW], a->band,
-                 a->band + (long)(g.ni + 2) * (g.nj + 2) * (g.nk + 2));
+                 a->band + nband(g), a->newton);
   adj::rn_avg_T(s, g, a->lrn, a->lgx[0], a->lgx[1], a->lgx[2]);
   check_stage(a, "mthinc");
   adj::grad_p2a_T(s, g, dxi, dyi, dzi, a->lgx[0], a->lgx[1], a->lgx[2], lS[SPHI1]);
+  check_stage(a, "gradp2a");
+  a->stimer.flush(s);
   FMF_CUDA(cudaGetLastError());
 }
 

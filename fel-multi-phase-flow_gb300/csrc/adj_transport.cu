@@ -86,27 +86,6 @@ __device__ T newton_d(const T& nx, const T& ny, const T& nz, const T& ph, const 
   }
   return d;
 }
-// the same ten steps in plain FP64; *last = the final step
-__device__ double newton_plain(double nx, double ny, double nz, double ph, const MC& M, double bet, double* last) {
-  double a[8];
-  gauss8(nx, ny, nz, M.gp1, M.gp2, M.gp1, M.gp2, M.gp1, M.gp2, a);
-  double d = 0.0, step = 0.0;
-  for (int it = 0; it < 10; ++it) {
-    double f = 0.0, acc = 0.0;
-    for (int t = 0; t < 8; ++t) {
-      const double x = a[t] + d;
-      f = f + 0.125 / (1.0 + exp(-2.0 * bet * x));
-      const double ch = cosh(bet * x);
-      acc = acc + 0.125 / (ch * ch);
-    }
-    f = f - ph;
-    const double df = 0.5 * bet * acc;
-    step = f * df / (df * df + 1.0e-99);
-    d = d - step;
-  }
-  *last = step;
-  return d;
-}
 // flux through one outflow face: dir 0/1/2, side 0 = the lower face (velocity < 0),
 // side 1 = the upper face (velocity > 0)
 template <class T>
@@ -141,7 +120,8 @@ __global__ void __launch_bounds__(128) k_band_T(Grid g, MC M, double sx, double 
                                                 const double* __restrict__ lfy, const double* __restrict__ lfz,
                                                 double* lphi, double* __restrict__ lrn, double* lu, double* lv,
                                                 double* lw, const int* __restrict__ list,
-                                                const int* __restrict__ count) {
+                                                const int* __restrict__ count, const double* __restrict__ newton,
+                                                long cap) {
   const int nb = *count;
   const long n = g.n;
   const long X = 1, Y = g.sy, Z = g.sz;
@@ -166,12 +146,11 @@ __global__ void __launch_bounds__(128) k_band_T(Grid g, MC M, double sx, double 
     using D4 = Dual<4>;
     D4 dd;
     {
-      // d by the ten Newton steps; where the last step moved d by less than
-      // 1e-13 (1 + |d|) the iteration has converged and dd/dv = -F_v/F_d at d
-      // (F = the 8-point mean - phi), else the derivatives are carried through
-      // the ten steps
-      double last = 0.0;
-      const double dv = newton_plain(nx, ny, nz, phi[c], M, bet, &last);
+      // d and the last of the forward pass's ten Newton steps (recorded per list
+      // entry); where that step moved d by less than 1e-13 (1 + |d|) the iteration
+      // has converged and dd/dv = -F_v/F_d at d (F = the 8-point mean - phi), else
+      // the derivatives are carried through the ten steps
+      const double dv = newton[e], last = newton[cap + e];
       if (fabs(last) <= 1.0e-13 * (1.0 + fabs(dv))) {
         using D5 = Dual<5>;
         D5 a[8];
@@ -217,7 +196,8 @@ __global__ void k_mark(const int* __restrict__ list, const int* __restrict__ cou
 void mthinc1_T(cudaStream_t s, const Grid& g, double dxi, double dyi, double dzi, double dt, double bet,
                const double* phi, const double* gx, const double* gy, const double* gz, const double* u,
                const double* v, const double* w, const double* lfx, const double* lfy, const double* lfz,
-               double* lphi, double* lrn, double* lu, double* lv, double* lw, const int* list, const int* count) {
+               double* lphi, double* lrn, double* lu, double* lv, double* lw, const int* list, const int* count,
+               const double* newton) {
   const Grid G = g;
   const MC M = mconst(dxi, dyi, dzi, bet);
   const long n = g.n;
@@ -268,7 +248,8 @@ void mthinc1_T(cudaStream_t s, const Grid& g, double dxi, double dyi, double dzi
     // band cells: k_band_T over the forward pass's band list
   });
   k_band_T<<<152 * 8, 128, 0, s>>>(g, M, dt * dxi, dt * dyi, dt * dzi, bet, phi, gx, gy, gz, u, v, w, lfx, lfy, lfz,
-                                   lphi, lrn, lu, lv, lw, list, count);
+                                   lphi, lrn, lu, lv, lw, list, count, newton,
+                                   (long)(g.ni + 2) * (g.nj + 2) * (g.nk + 2));
   count_launch();
 }
 

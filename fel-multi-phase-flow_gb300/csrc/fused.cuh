@@ -14,11 +14,13 @@ void weno5_both(cudaStream_t s, const Grid& g, double dxi, double dyi, double dz
 
 // solphi_mthinc1 for the faces solphi_mthinc2 reads (every face of rows 1..n in
 // the two directions normal to it, faces 0..n along it); list/count: device scratch
-// of >= (ni+2)(nj+2)(nk+2) ints and one int.
+// of >= (ni+2)(nj+2)(nk+2) ints and one int.  newton (optional, 2 (ni+2)(nj+2)(nk+2)
+// doubles): per list entry e the Newton offset at [e] and its last step at
+// [(ni+2)(nj+2)(nk+2) + e], for the adjoint.
 void mthinc_fluxes(cudaStream_t s, const Grid& g, double dxinv, double dyinv, double dzinv, double dt, double bet,
                    const double* phi, const double* gx, const double* gy, const double* gz, const double* u,
                    const double* v, const double* w, double* fx, double* fy, double* fz, int* list, int* count,
-                   bool fp32 = false);
+                   bool fp32 = false, double* newton = nullptr);
 
 // CSF force of one field on the interior u, v, w points (fu/fv/fw), replacing
 // cal_grad_p2a + calrn x4 + calrkap + cal_grad_p2uvw + calfst; needs ni % 32 == 0

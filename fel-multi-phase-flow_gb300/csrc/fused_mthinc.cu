@@ -118,7 +118,8 @@ __global__ void __launch_bounds__(128) k_band(Grid g, MC m, const double* __rest
                                               const double* __restrict__ v, const double* __restrict__ w,
                                               double* __restrict__ fx, double* __restrict__ fy,
                                               double* __restrict__ fz, const int* __restrict__ list,
-                                              const int* __restrict__ count) {
+                                              const int* __restrict__ count, double* __restrict__ newton,
+                                              long cap) {
   const int n = *count;
   const long X = 1, Y = g.sy, Z = g.sz;
   const R m2b = (R)(-2.0 * m.bet), gp1 = (R)m.gp1, gp2 = (R)m.gp2, bet = (R)m.bet, dtt = (R)m.dt;
@@ -132,14 +133,19 @@ __global__ void __launch_bounds__(128) k_band(Grid g, MC m, const double* __rest
     R a[8];
     gauss8<R>(a, rnx, rny, rnz, gp1, gp2, gp1, gp2, gp1, gp2);
     const R ph = (R)__ldg(phi + c);
-    R ddd = 0;
+    R ddd = 0, step = 0;
 #pragma unroll 1
     for (int it = 0; it < 10; ++it) {
       R sd;
       const R f = sig8<R>(a, (R)0.125, m2b, ddd, &sd) - ph;
       // df = 0.5 bet sum 0.125/cosh^2 = 0.5 bet * 0.125 * 4 * sum s(1-s)
       const R df = (R)0.25 * bet * sd;
-      ddd = ddd - f * df / (df * df + reg);
+      step = f * df / (df * df + reg);
+      ddd = ddd - step;
+    }
+    if (newton) {
+      newton[e] = (double)ddd;
+      newton[cap + e] = (double)step;
     }
     const double uw = __ldg(u + c - X), ue = __ldg(u + c), vs = __ldg(v + c - Y), vn = __ldg(v + c),
                  wb = __ldg(w + c - Z), wt = __ldg(w + c);
@@ -166,7 +172,7 @@ __global__ void __launch_bounds__(128) k_band(Grid g, MC m, const double* __rest
 void mthinc_fluxes(cudaStream_t s, const Grid& g, double dxinv, double dyinv, double dzinv, double dt, double bet,
                    const double* phi, const double* gx, const double* gy, const double* gz, const double* u,
                    const double* v, const double* w, double* fx, double* fy, double* fz, int* list, int* count,
-                   bool fp32) {
+                   bool fp32, double* newton) {
   MC m;
   const double dx = 1.0 / dxinv, dy = 1.0 / dyinv, dz = 1.0 / dzinv;
   m.gp1 = -0.5 / std::sqrt(3.0);
@@ -184,10 +190,11 @@ void mthinc_fluxes(cudaStream_t s, const Grid& g, double dxinv, double dyinv, do
   dim3 b(32, 8, 1);
   dim3 gr((unsigned)((g.ni + 2 + 31) / 32), (unsigned)((g.nj + 2 + 7) / 8), (unsigned)(g.nk + 2));
   k_classify<<<gr, b, 0, s>>>(g, m, phi, gx, gy, gz, u, v, w, fx, fy, fz, list, count);
+  const long cap = (long)(g.ni + 2) * (g.nj + 2) * (g.nk + 2);
   if (fp32)
-    k_band<float><<<152 * 8, 128, 0, s>>>(g, m, phi, gx, gy, gz, u, v, w, fx, fy, fz, list, count);
+    k_band<float><<<152 * 8, 128, 0, s>>>(g, m, phi, gx, gy, gz, u, v, w, fx, fy, fz, list, count, newton, cap);
   else
-    k_band<double><<<152 * 8, 128, 0, s>>>(g, m, phi, gx, gy, gz, u, v, w, fx, fy, fz, list, count);
+    k_band<double><<<152 * 8, 128, 0, s>>>(g, m, phi, gx, gy, gz, u, v, w, fx, fy, fz, list, count, newton, cap);
   count_launch(2);
 }
 
