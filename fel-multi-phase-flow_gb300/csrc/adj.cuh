@@ -10,6 +10,7 @@
 // and differentiated on the branch that was executed.
 #pragma once
 #include <cmath>
+#include <functional>
 #include <map>
 #include <utility>
 #include <vector>
@@ -227,6 +228,11 @@ void sor_replay(cudaStream_t s, const Grid& g, double dxi, double dyi, double dz
                 double* snaps);
 // CUDA graphs of one transposed iteration, keyed by the buffers they read and write
 using GraphCache = std::map<std::vector<const void*>, std::pair<cudaGraphExec_t, long long>>;
+// The executable graph of `body` for this set of buffers (key): captured on s the
+// first time, then taken from the cache; nullptr when capture fails (the caller
+// then runs body directly).  *per_launch = the kernels one replay launches.
+cudaGraphExec_t cached_graph(cudaStream_t s, GraphCache* cache, const std::vector<const void*>& key,
+                             const std::function<void()>& body, long long* per_launch);
 // transposed fixed-point solve and gradient collection; lam: 3 output arrays (the
 // converged adjoint of un*, consumed by the gradient pass); lAB, lmu, lE, lwc
 // accumulate; work: >= 3n + 520 doubles; host_norm: 1 pinned double; cache may be

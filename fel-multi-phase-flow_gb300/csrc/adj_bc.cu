@@ -94,14 +94,49 @@ __global__ void __launch_bounds__(256) k_halo_z_T(Grid g, int normal, double* __
     else line_T<true>(lw, r, g.sz, g.nk);
   }
 }
+// k_halo_x_T for ni >= 8 with 8 lanes per (j, k, component): lanes 0-2 move the
+// adjoints of the low ghosts -2..0 to their sources, lanes 3-5 those of ni+1..ni+3;
+// no lane's destination is another lane's source, so the lanes are independent.
+__global__ void __launch_bounds__(256) k_halo_x_T8(Grid g, int normal, double* __restrict__ lu,
+                                                   double* __restrict__ lv, double* __restrict__ lw) {
+  const long t = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  const int m = (int)(t & 7);
+  const long task = t >> 3;
+  const long JK = (long)(g.nj + 6) * (g.nk + 6);
+  if (m >= 6 || task >= 3 * JK) return;
+  const int cmp = (int)(task / JK);
+  const int rem = (int)(task % JK);
+  double* a = cmp == 0 ? lu : (cmp == 1 ? lv : lw);
+  if (!a) return;
+  const bool sh = cmp == 0 && !(normal & 1);
+  const long r = g.at(0, -2 + rem % (g.nj + 6), -2 + rem / (g.nj + 6));
+  long dst, src;
+  if (m < 3) {
+    dst = r + m - 2;
+    src = r + g.ni - 2 + m + (sh ? 1 : 0);
+  } else {
+    if (sh && m == 3) return;  // the shifted copy does not write ni+1
+    dst = r + g.ni + m - 2;
+    src = r + m - 2;
+  }
+  const double L = a[dst], v = a[src];
+  a[dst] = 0.0;
+  a[src] = v + L;
+}
 dim3 xh_grid(const Grid& g) { return dim3((g.nj + 6 + 31) / 32, (g.nk + 6 + 7) / 8); }
 dim3 zh_grid(const Grid& g) { return dim3((g.ni + 6 + 31) / 32, (g.nj + 6 + 7) / 8); }
+void launch_halo_x_T(cudaStream_t s, const Grid& g, int normal, double* lu, double* lv, double* lw) {
+  if (g.ni >= 8)
+    k_halo_x_T8<<<(unsigned)((24L * (g.nj + 6) * (g.nk + 6) + 255) / 256), 256, 0, s>>>(g, normal, lu, lv, lw);
+  else
+    k_halo_x_T<<<xh_grid(g), dim3(32, 8), 0, s>>>(g, normal, lu, lv, lw);
+}
 
 // bnd_periodic: x copies over every (j,k) then z copies over every (i,j); the adjoint
 // runs z first.
 void periodic_T(cudaStream_t s, const Grid& g, double* lq) {
   k_halo_z_T<<<zh_grid(g), dim3(32, 8), 0, s>>>(g, 4, nullptr, nullptr, lq);
-  k_halo_x_T<<<xh_grid(g), dim3(32, 8), 0, s>>>(g, 1, lq, nullptr, nullptr);
+  launch_halo_x_T(s, g, 1, lq, nullptr, nullptr);
   count_launch(2);
 }
 
@@ -281,7 +316,7 @@ void wall_T(cudaStream_t s, const Grid& g, double uwall, const double* wc, const
 }
 
 void halo_x_T(cudaStream_t s, const Grid& g, int normal, double* lu, double* lv, double* lw) {
-  k_halo_x_T<<<xh_grid(g), dim3(32, 8), 0, s>>>(g, normal, lu, lv, lw);
+  launch_halo_x_T(s, g, normal, lu, lv, lw);
   count_launch();
 }
 

@@ -270,17 +270,21 @@ void csf_T(cudaStream_t s, const Grid& g, double dxi, double dyi, double dzi, do
         const double* p = Gv + q3 * n + b;
         r[q3] = (p[0] + p[Xf] + p[Yf] + p[Xf + Yf] + p[Zf] + p[Xf + Zf] + p[Yf + Zf] + p[Xf + Yf + Zf]) * 0.125;
       }
-      const double m = sqrt(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]);
-      const double a = m + vs;
-      // dN/dv = I/a - v v^T/(a^2 m), formed with the unit vector e = v/m
-      double e[3] = {0.0, 0.0, 0.0}, corr = 0.0;
-      if (m > 0.0) {
-        for (int q3 = 0; q3 < 3; ++q3) e[q3] = r[q3] / m;
-        corr = (e[0] * lx + e[1] * ly + e[2] * lz) * (m / (a * a));
+      // dN/dv = I/a - v v^T/(a^2 m) with m = |v|, a = m + vs:
+      // lv = (l - v (v.l)/(m a)) / a, the factor formed as ((v.l)/m)/a, which stays
+      // finite for any m > 0
+      const double s2 = r[0] * r[0] + r[1] * r[1] + r[2] * r[2];
+      double ia, t = 0.0;
+      if (s2 > 0.0) {
+        const double im = rsqrt(s2);
+        ia = 1.0 / (s2 * im + vs);
+        t = ((r[0] * lx + r[1] * ly + r[2] * lz) * im) * ia;
+      } else {
+        ia = 1.0 / vs;
       }
-      out[0] = lx / a - e[0] * corr;
-      out[n] = ly / a - e[1] * corr;
-      out[2 * n] = lz / a - e[2] * corr;
+      out[0] = (lx - r[0] * t) * ia;
+      out[n] = (ly - r[1] * t) * ia;
+      out[2 * n] = (lz - r[2] * t) * ia;
     }
   });
   // pass 2, per vertex p: 0.125 lv over the (family, corner) pairs whose mean reads

@@ -119,6 +119,8 @@ struct fmf_adj {
   double* lblock = nullptr;  // the intermediate adjoints (one memset per reverse step)
   long lblock_n = 0;
   adj::GraphCache graphs;      // transposed viscous iterations, one per record slot
+  adj::GraphCache fgraphs;     // forward viscous iterations, one per record slot
+  adj::GraphCache rgraphs;     // replays of the last forward viscous cycle, one per record slot
   double* host_norm = nullptr;  // pinned
 };
 
@@ -421,11 +423,27 @@ int record_step(fmf_adj* a) {
   fused::src_visc_prep(s, g, dxi, dyi, dzi, dt, P.harmonic, P.grvb, P.grvp, S[SU], S[SV], S[SW], advp, advop, prsp,
                        visp, fstp, fstnp, a->rmun, a->rho, a->rhon, a->E, a->AB, a->l1, a->l2, phi1, P.dy, a->wallc);
   for (int q = 0; q < 3; ++q) dcopy(a, S[SU + q], a->un[q], n);
+  // one outer iteration (12 colour-pair sweeps and their refreshes), replayed as a
+  // CUDA graph per record slot
+  auto iteration = [&]() {
+    fused::sor_iteration(s, g, dxi, dyi, dzi, P.harmonic, a->rmun, a->E, a->AB, P.uwall, a->wallc, a->un[0],
+                         a->un[1], a->un[2], a->sorpart, a->red + 4);
+  };
+  long long per_launch = 0;
+  const cudaGraphExec_t exec =
+      adj::cached_graph(s, &a->fgraphs,
+                        {a->rmun, a->E[0], a->E[1], a->E[2], a->AB[0], a->AB[1], a->AB[2], a->AB[3], a->AB[4],
+                         a->AB[5], a->wallc, a->un[0], a->un[1], a->un[2], a->sorpart, a->red},
+                        iteration, &per_launch);
   double err0 = 0.0;
   int lp;
   for (lp = 0; lp < a->sor_max; ++lp) {
-    fused::sor_iteration(s, g, dxi, dyi, dzi, P.harmonic, a->rmun, a->E, a->AB, P.uwall, a->wallc, a->un[0],
-                         a->un[1], a->un[2], a->sorpart, a->red + 4);
+    if (exec) {
+      FMF_CUDA(cudaGraphLaunch(exec, s));
+      count_launch((int)per_launch);
+    } else {
+      iteration();
+    }
     double e = 0.0;
     FMF_CUDA(cudaMemcpyAsync(&e, a->red + 4, sizeof(double), cudaMemcpyDeviceToHost, s));
     FMF_CUDA(cudaStreamSynchronize(s));
@@ -531,7 +549,23 @@ void reverse_step(fmf_adj* a, const double* st) {
   check_stage(a, "poisson");
   adj::wall_halo_T(s, g, 7, P.uwall, a->wallc, a->ustar[0], a->ustar[2], a->lun[0], a->lun[1], a->lun[2], a->lwc);
   // :605-623 the viscous solve
-  adj::sor_replay(s, g, dxi, dyi, dzi, a->rmun, a->E, a->AB, P.uwall, a->wallc, a->ustar, a->snaps);
+  {  // the 12 sweep snapshots of the fixed point, replayed as a CUDA graph per record slot
+    auto replay = [&]() {
+      adj::sor_replay(s, g, dxi, dyi, dzi, a->rmun, a->E, a->AB, P.uwall, a->wallc, a->ustar, a->snaps);
+    };
+    long long per_launch = 0;
+    const cudaGraphExec_t exec =
+        adj::cached_graph(s, &a->rgraphs,
+                          {a->rmun, a->E[0], a->E[1], a->E[2], a->AB[0], a->AB[1], a->AB[2], a->AB[3], a->AB[4],
+                           a->AB[5], a->wallc, a->ustar[0], a->ustar[1], a->ustar[2], a->snaps},
+                          replay, &per_launch);
+    if (exec) {
+      FMF_CUDA(cudaGraphLaunch(exec, s));
+      count_launch((int)per_launch);
+    } else {
+      replay();
+    }
+  }
   check_stage(a, "replay");
   const double* lout[3] = {a->lun[0], a->lun[1], a->lun[2]};
   a->adj_total += adj::sor_T(s, g, dxi, dyi, dzi, a->rmun, a->E, a->AB, P.uwall, a->wallc, a->ustar, a->snaps,
@@ -791,6 +825,8 @@ int fmf_adj_destroy(fmf_adj* a) {
   for (double* p : a->seg) cudaFree(p);
   for (void* p : a->rec_blocks) cudaFree(p);
   for (auto& e : a->graphs) cudaGraphExecDestroy(e.second.first);
+  for (auto& e : a->fgraphs) cudaGraphExecDestroy(e.second.first);
+  for (auto& e : a->rgraphs) cudaGraphExecDestroy(e.second.first);
   if (a->host_norm) cudaFreeHost(a->host_norm);
   for (void* p : a->allocs) cudaFree(p);
   scratch_set_destroy(a->scr);

@@ -337,6 +337,32 @@ void sor_replay(cudaStream_t s, const Grid& g, double dxi, double dyi, double dz
     }
 }
 
+cudaGraphExec_t cached_graph(cudaStream_t s, GraphCache* cache, const std::vector<const void*>& key,
+                             const std::function<void()>& body, long long* per_launch) {
+  auto itc = cache->find(key);
+  if (itc != cache->end()) {
+    *per_launch = itc->second.second;
+    return itc->second.first;
+  }
+  *per_launch = 0;
+  cudaGraphExec_t exec = nullptr;
+  cudaGraph_t graph = nullptr;
+  const long long l0 = launches();
+  if (!FMF_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeRelaxed))) return nullptr;
+  body();
+  // the captured launches did not run: they are counted when the graph is replayed
+  const long long captured = launches() - l0;
+  count_launch((int)-captured);
+  if (FMF_CUDA(cudaStreamEndCapture(s, &graph)) && FMF_CUDA(cudaGraphInstantiate(&exec, graph, 0))) {
+    *per_launch = captured;
+    (*cache)[key] = {exec, captured};
+  } else {
+    exec = nullptr;
+  }
+  if (graph) cudaGraphDestroy(graph);
+  return exec;
+}
+
 int sor_T(cudaStream_t s, const Grid& g, double dxi, double dyi, double dzi, const double* mu, double* const* E,
           double* const* AB, double uwall, const double* wallc, const double* const* ustar, const double* snaps,
           const double* const* lout, double* const* lam, double* const* lAB, double* lmu, double* const* lE,
@@ -384,29 +410,13 @@ int sor_T(cudaStream_t s, const Grid& g, double dxi, double dyi, double dzi, con
     k_sum_small<<<1, 256, 0, s>>>(part, 512, nrm);
     count_launch(3);
   };
-  cudaGraphExec_t exec = nullptr;
   long long per_launch = 0;
-  if (cache) {
-    const std::vector<const void*> key = {lam[0], lam[1], lam[2], lout[0], lout[1], lout[2], mu, E[0], E[1], E[2],
-                                          AB[0], AB[2], AB[4], wallc, ustar[0], ustar[2], work};
-    auto itc = cache->find(key);
-    if (itc == cache->end()) {
-      const long long l0 = launches();
-      cudaGraph_t graph = nullptr;
-      if (FMF_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeRelaxed))) {
-        iteration();
-        if (FMF_CUDA(cudaStreamEndCapture(s, &graph)) && FMF_CUDA(cudaGraphInstantiate(&exec, graph, 0))) {
-          per_launch = launches() - l0;
-          count_launch((int)-per_launch);
-          (*cache)[key] = {exec, per_launch};
-        }
-        if (graph) cudaGraphDestroy(graph);
-      }
-    } else {
-      exec = itc->second.first;
-      per_launch = itc->second.second;
-    }
-  }
+  cudaGraphExec_t exec =
+      cache ? cached_graph(s, cache,
+                           {lam[0], lam[1], lam[2], lout[0], lout[1], lout[2], mu, E[0], E[1], E[2], AB[0], AB[2],
+                            AB[4], wallc, ustar[0], ustar[2], work},
+                           iteration, &per_launch)
+            : nullptr;
   double n0 = -1.0;
   int it = 0;
   for (it = 0; it < maxit; ++it) {

@@ -346,6 +346,28 @@ __global__ void __launch_bounds__(256) k_halo_z(Grid g, int normal, double* __re
     a[r + (NK + 3) * Z] = t[cmp][5];
   }
 }
+// k_halo_x for ni >= 8 with 8 lanes per (j, k, component): lanes 0-2 write the low
+// ghosts -2..0, lanes 3-5 the high ghosts ni+1..ni+3, each from its interior source
+// (none of which the kernel writes).  A warp then reads and writes a few contiguous
+// runs instead of 32 rows, and the work spreads over every SM.
+__global__ void __launch_bounds__(256) k_halo_x8(Grid g, int normal, double* __restrict__ uk,
+                                                 double* __restrict__ vk, double* __restrict__ wk) {
+  const long t = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  const int m = (int)(t & 7);
+  const long task = t >> 3;
+  const long JK = (long)(g.nj + 6) * (g.nk + 6);
+  if (m >= 6 || task >= 3 * JK) return;
+  const int cmp = (int)(task / JK);
+  const int rem = (int)(task % JK);
+  double* a = cmp == 0 ? uk : (cmp == 1 ? vk : wk);
+  const bool sh = cmp == 0 && !(normal & 1);  // bndu's u: u(-2..0) = u(ni-1..ni+1), u(ni+1) kept
+  const long r = g.at(0, -2 + rem % (g.nj + 6), -2 + rem / (g.nj + 6));
+  if (m < 3) {
+    a[r + m - 2] = a[r + g.ni - 2 + m + (sh ? 1 : 0)];
+  } else if (!(sh && m == 3)) {
+    a[r + g.ni + m - 2] = a[r + m - 2];
+  }
+}
 // --- mixed precision: FP32 sweeps on the correction d = un - u ---------------------
 // During the solve un = u + d holds at every point, halos and wall ghosts included:
 // d starts at zero (un = u, main.f90:605-607) and every operation on un has an
@@ -698,7 +720,10 @@ void wall_coef(cudaStream_t s, const Grid& g, double dy, const double* l1, const
 void wall_halo(cudaStream_t s, const Grid& g, int normal, double uwall, const double* wallc, double* un, double* vn,
                double* wn) {
   k_wall<<<wall_grid(g), kB, 0, s>>>(g, uwall, wallc, un, vn, wn);
-  k_halo_x<<<xh_grid(g), kB, 0, s>>>(g, normal, un, vn, wn);
+  if (g.ni >= 8)
+    k_halo_x8<<<(unsigned)((24L * (g.nj + 6) * (g.nk + 6) + 255) / 256), 256, 0, s>>>(g, normal, un, vn, wn);
+  else
+    k_halo_x<<<xh_grid(g), kB, 0, s>>>(g, normal, un, vn, wn);
   k_halo_z<<<zh_grid(g), kB, 0, s>>>(g, normal, un, vn, wn);
   count_launch(3);
 }
