@@ -1,6 +1,8 @@
 // capi.cu -- the drop-in C-ABI (include/fmf_capi.h, parts 1 and 2).
 #include <cmath>
+#include <cstdio>
 #include <cstring>
+#include <vector>
 
 #include "../../include/fmf_capi.h"
 #include "ops.cuh"
@@ -563,9 +565,111 @@ void find_interface_positions_lower_(int* ni, int* nj, int* nk, double* phi, dou
                                      double* xl) {
   (void)dy;
   (void)dz;
-  if (mode() == FMF_RESIDENT) sync_to_host(phi, 0);
-  const double v = fmf_interface_lower(*ni, *nj, *nk, phi, *dx, *xl);
-  std::printf(" Lower Interface Position (Average over k):\n %.15E\n", v);
+  GRID3;
+  double* d = (double*)scratch(sizeof(double) * 2, 3);
+  FMF_LAUNCH(op::diag_interface_lower, s, g, *dx, *xl, call.in(phi, N3), d);
+  double v = 0.0;
+  if (call.ok) {
+    FMF_CUDA(cudaMemcpyAsync(&v, d, sizeof(double), cudaMemcpyDeviceToHost, s));
+    FMF_CUDA(cudaStreamSynchronize(s));
+    std::printf(" Lower Interface Position (Average over k):\n %.15E\n", v);
+  }
+  call.finish();
+}
+
+// find_interface_positions_upper.f90:1-26: every crossing of the top wall row,
+// printed as "x z" lines in the reference's order
+void find_interface_positions_upper_(int* ni, int* nj, int* nk, double* phi, double* dx, double* dy, double* dz,
+                                     double* xl) {
+  (void)dy;
+  GRID3;
+  const int cap = *ni * *nk;
+  double* xz = (double*)scratch(sizeof(double) * (2L * cap + 1), 13);
+  int* cnt = (int*)(xz + 2L * cap);
+  FMF_LAUNCH(op::diag_interface_upper, s, g, *dx, *dz, *xl, call.in(phi, N3), xz, cnt, cap);
+  if (call.ok) {
+    int c = 0;
+    FMF_CUDA(cudaMemcpyAsync(&c, cnt, sizeof(int), cudaMemcpyDeviceToHost, s));
+    FMF_CUDA(cudaStreamSynchronize(s));
+    if (c > cap) c = cap;  // cannot happen: at most one crossing per (i, k)
+    std::vector<double> h(2L * (c > 0 ? c : 1));
+    if (c > 0) {
+      FMF_CUDA(cudaMemcpyAsync(h.data(), xz, sizeof(double) * 2 * c, cudaMemcpyDeviceToHost, s));
+      FMF_CUDA(cudaStreamSynchronize(s));
+    }
+    for (int t = 0; t < c; ++t) std::printf(" %23.15E %23.15E\n", h[2 * t], h[2 * t + 1]);
+  }
+  call.finish();
+}
+// find_interface_positions.f90:1-26 is the same routine as the upper one
+void find_interface_positions_(int* ni, int* nj, int* nk, double* phi, double* dx, double* dy, double* dz,
+                               double* xl) {
+  find_interface_positions_upper_(ni, nj, nk, phi, dx, dy, dz, xl);
+}
+
+// cal_vel.f:1-82: vel = sum(phi u)/sum(phi) (and v, w), re = rhol vel 2 radius / rmul
+void cal_vel_(int* ipara, int* ni, int* nj, int* nk, double* radius, double* rhol, double* rmul, double* u,
+              double* v, double* w, double* phi, double* vel, double* re) {
+  if (!one_rank(ipara)) return;
+  GRID3;
+  double* d = (double*)scratch(sizeof(double) * 6, 3);
+  FMF_LAUNCH(op::diag_vel, s, g, *radius, *rhol, *rmul, call.in(u, N3), call.in(v, N3), call.in(w, N3),
+             call.in(phi, N3), d);
+  if (call.ok) {
+    double h[6];
+    FMF_CUDA(cudaMemcpyAsync(h, d, sizeof(h), cudaMemcpyDeviceToHost, s));
+    FMF_CUDA(cudaStreamSynchronize(s));
+    for (int q = 0; q < 3; ++q) {
+      vel[q] = h[q];
+      re[q] = h[3 + q];
+    }
+    if (!std::isfinite(h[0]) || !std::isfinite(h[1]) || !std::isfinite(h[2])) set_status(FMF_ERR_NONFINITE);
+  }
+  call.finish();
+}
+
+// cal_center.f:1-121: centre of mass of phi with x unwrapped across the periodic
+// direction, its x velocity, and the (center_pre, area_pre, lap) state update;
+// the four sums run on the device, the scalar bookkeeping on the host
+void cal_center_(int* ipara, int* ID, int* svall, int* ni, int* nj, int* nk, double* xl, double* yl, double* zl,
+                 double* dt, double* rhog, double* phi, double* center, double* center_pre1, double* center_pre2,
+                 int* area_pre1, int* area_pre2, int* lap, double* velocity) {
+  (void)zl;
+  (void)rhog;
+  if (!one_rank(ipara)) return;
+  GRID3;
+  const double L = *xl;
+  if (*svall <= 0 || !(L > 0.0)) {
+    set_status(FMF_ERR_ARG);
+    return;
+  }
+  const double delta = *yl / (double)*svall;
+  const double sensor1 = L * 0.25, sensor2 = L * 0.75;
+  if (*area_pre1 == 1 && *area_pre2 == 3) *lap = *lap + 1;
+  double* d = (double*)scratch(sizeof(double) * 4, 3);
+  FMF_LAUNCH(op::diag_center_sums, s, g, *ID, delta, L, *area_pre1, *lap, call.in(phi, N3), d);
+  if (call.ok) {
+    double h[4];
+    FMF_CUDA(cudaMemcpyAsync(h, d, sizeof(h), cudaMemcpyDeviceToHost, s));
+    FMF_CUDA(cudaStreamSynchronize(s));
+    for (int q = 0; q < 3; ++q) center[q] = h[1 + q] / h[0];
+    *velocity = (center[0] - *center_pre1) / *dt;
+    *center_pre2 = *center_pre1;
+    *center_pre1 = center[0];
+    double cc = center[0];
+    *area_pre2 = *area_pre1;
+    if (cc > L && std::isfinite(cc)) {  // the reference's loop never ends on inf
+      for (;;) {
+        cc = cc - L;
+        if (cc < L) break;
+      }
+    }
+    if (cc < sensor1) *area_pre1 = 1;
+    if (cc > sensor2) *area_pre1 = 3;
+    if (sensor1 <= cc && cc <= sensor2) *area_pre1 = 2;
+    if (!std::isfinite(center[0])) set_status(FMF_ERR_NONFINITE);
+  }
+  call.finish();
 }
 
 // ---------------------------------------------------------------- part 2
@@ -586,6 +690,45 @@ void fmf_dev_bnd_periodic(int ni, int nj, int nk, double* qk) {
     return;
   }
   op::bnd_periodic(stream(), Grid(ni, nj, nk), qk);
+  FMF_CUDA(cudaGetLastError());
+}
+void fmf_dev_cal_vel(int ni, int nj, int nk, double radius, double rhol, double rmul, const double* u,
+                     const double* v, const double* w, const double* phi, double* out6) {
+  if (!check_grid(ni, nj, nk)) return;
+  if (!u || !v || !w || !phi || !out6) {
+    set_status(FMF_ERR_ARG);
+    return;
+  }
+  op::diag_vel(stream(), Grid(ni, nj, nk), radius, rhol, rmul, u, v, w, phi, out6);
+  FMF_CUDA(cudaGetLastError());
+}
+void fmf_dev_cal_center_sums(int ni, int nj, int nk, int ID, double delta, double xl, int area_pre1, int lap,
+                             const double* phi, double* out4) {
+  if (!check_grid(ni, nj, nk)) return;
+  if (!phi || !out4) {
+    set_status(FMF_ERR_ARG);
+    return;
+  }
+  op::diag_center_sums(stream(), Grid(ni, nj, nk), ID, delta, xl, area_pre1, lap, phi, out4);
+  FMF_CUDA(cudaGetLastError());
+}
+void fmf_dev_interface_upper(int ni, int nj, int nk, const double* phi, double dx, double dz, double xl,
+                             double* xz, int* count, int cap) {
+  if (!check_grid(ni, nj, nk)) return;
+  if (!phi || !count || cap < 0 || (cap > 0 && !xz)) {
+    set_status(FMF_ERR_ARG);
+    return;
+  }
+  op::diag_interface_upper(stream(), Grid(ni, nj, nk), dx, dz, xl, phi, xz, count, cap);
+  FMF_CUDA(cudaGetLastError());
+}
+void fmf_dev_interface_lower(int ni, int nj, int nk, const double* phi, double dx, double xl, double* out1) {
+  if (!check_grid(ni, nj, nk)) return;
+  if (!phi || !out1) {
+    set_status(FMF_ERR_ARG);
+    return;
+  }
+  op::diag_interface_lower(stream(), Grid(ni, nj, nk), dx, xl, phi, out1);
   FMF_CUDA(cudaGetLastError());
 }
 

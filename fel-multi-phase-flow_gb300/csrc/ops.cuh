@@ -64,6 +64,20 @@ void fill(cudaStream_t s, long n, double* q, double value);
 void copy(cudaStream_t s, long n, const double* a, double* b);
 // interior mean -> out[0] (device)
 void cal_av(cudaStream_t s, const Grid& g, const double* q, double* out);
+// Monitors (diag.cu), results in device memory, nothing read back:
+// cal_vel.f:36-80 -- out[0..2] = vel, out[3..5] = re
+void diag_vel(cudaStream_t s, const Grid& g, double radius, double rhol, double rmul, const double* u,
+              const double* v, const double* w, const double* phi, double* out);
+// cal_center.f:36-76 -- out[0] = sum phi, out[1..3] = sum phi * (x, y, z) with x
+// unwrapped for (area_pre1, lap); delta = yl / svall
+void diag_center_sums(cudaStream_t s, const Grid& g, int ID, double delta, double xl, int area_pre1, int lap,
+                      const double* phi, double* out);
+// find_interface_positions_upper.f90:13-24 -- the crossings of row nj in print order:
+// xz[2c], xz[2c+1] = (x, z) for c < min(count, cap), *count = number of crossings
+void diag_interface_upper(cudaStream_t s, const Grid& g, double dx, double dz, double xl, const double* phi,
+                          double* xz, int* count, int cap);
+// find_interface_positions_lower.f90:15-32 -- out[0] = -x_avg
+void diag_interface_lower(cudaStream_t s, const Grid& g, double dx, double xl, const double* phi, double* out);
 void cal_srcu(cudaStream_t s, const Grid& g, double dt, double grvb, double grvp, const double* u,
               const double* v, const double* w, const double* rho, const double* rhon,
               const double* const* adv, const double* const* advo, const double* const* prs,

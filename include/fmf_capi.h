@@ -245,9 +245,26 @@ void bnd_avzero_(int* ipara, int* ndiv, int* ni, int* nj, int* nk, double* q);
 void corunp_explicit_(int* nID, int* ni, int* nj, int* nk, double* rho, double* dxinv,
                       double* dyinv, double* dzinv, double* dt, double* dp, double* phat,
                       double* un, double* vn, double* wn, double* pn);
-/* srcs/find_interface_positions_lower.f90:1-35 (prints -x_avg like the reference) */
+/* srcs/find_interface_positions_lower.f90:1-35 (prints -x_avg like the reference;
+ * computed on the device, one double read back) */
 void find_interface_positions_lower_(int* ni, int* nj, int* nk, double* phi, double* dx,
                                      double* dy, double* dz, double* xl);
+/* srcs/find_interface_positions_upper.f90:1-26 (prints each crossing "x z" of the top
+ * wall row in the reference's k-outer, i-inner order) */
+void find_interface_positions_upper_(int* ni, int* nj, int* nk, double* phi, double* dx,
+                                     double* dy, double* dz, double* xl);
+/* srcs/find_interface_positions.f90:1-26 (the same routine as the upper one) */
+void find_interface_positions_(int* ni, int* nj, int* nk, double* phi, double* dx, double* dy,
+                               double* dz, double* xl);
+/* srcs/cal_vel.f:1-82 (vel(3), re(3) out; ipara must be 0: one GPU holds the domain) */
+void cal_vel_(int* ipara, int* ni, int* nj, int* nk, double* radius, double* rhol, double* rmul,
+              double* u, double* v, double* w, double* phi, double* vel, double* re);
+/* srcs/cal_center.f:1-121 (center(3), velocity out; center_pre1/2, area_pre1/2, lap
+ * updated as the reference updates them; zl and rhog unused as in the reference) */
+void cal_center_(int* ipara, int* ID, int* svall, int* ni, int* nj, int* nk, double* xl,
+                 double* yl, double* zl, double* dt, double* rhog, double* phi, double* center,
+                 double* center_pre1, double* center_pre2, int* area_pre1, int* area_pre2,
+                 int* lap, double* velocity);
 
 /* Monitors the reference prints, returned instead of printed (no counterpart
  * with this signature in the reference; the values are those of
@@ -278,6 +295,24 @@ void fmf_dev_cal_advu_weno5(int ni, int nj, int nk, double dxinv, double dyinv, 
                             const double* u, const double* v, const double* w, double* adv_u,
                             double* adv_v, double* adv_w);
 void fmf_dev_bnd_periodic(int ni, int nj, int nk, double* qk);
+/* Monitors on device arrays, results left in device memory (nothing is read back,
+ * no host synchronisation):
+ * srcs/cal_vel.f:36-80 -- out6[0..2] = vel, out6[3..5] = re */
+void fmf_dev_cal_vel(int ni, int nj, int nk, double radius, double rhol, double rmul,
+                     const double* u, const double* v, const double* w, const double* phi,
+                     double* out6);
+/* srcs/cal_center.f:36-76 -- out4 = sum phi, sum phi*x, sum phi*y, sum phi*z with x
+ * unwrapped for (area_pre1, lap) and delta = yl/svall; the caller keeps the
+ * lap/area state (center = out4[1..3] / out4[0]) */
+void fmf_dev_cal_center_sums(int ni, int nj, int nk, int ID, double delta, double xl,
+                             int area_pre1, int lap, const double* phi, double* out4);
+/* srcs/find_interface_positions_upper.f90:13-24 -- xz[2c], xz[2c+1] = (x, z) of the
+ * crossings in print order for c < min(*count, cap); *count (device int) = their number */
+void fmf_dev_interface_upper(int ni, int nj, int nk, const double* phi, double dx, double dz,
+                             double xl, double* xz, int* count, int cap);
+/* srcs/find_interface_positions_lower.f90:15-32 -- out1[0] = -x_avg */
+void fmf_dev_interface_lower(int ni, int nj, int nk, const double* phi, double dx, double xl,
+                             double* out1);
 
 /* ------------------------------------------------------------------------ */
 /* Part 3: the fused device-resident step (main.f90:473-697)                */

@@ -1387,6 +1387,104 @@ double orc_interface_lower(const int* ni, const int* nj, const int* nk, const do
   return -(sum_x / (double)D.nk);
 }
 
+// cal_vel.f:1-82 -- phi-weighted mean velocity of the dispersed phase and its
+// Reynolds numbers (the four sums are a 4-double allreduce in the MPI build).
+void orc_cal_vel(const int* ipara, const int* ni, const int* nj, const int* nk, const double* radius,
+                 const double* rhol, const double* rmul, const double* u, const double* v, const double* w,
+                 const double* phi, double* vel, double* re) {
+  (void)ipara;
+  Dim D(*ni, *nj, *nk);
+  double sp = 0.0, su = 0.0, sv = 0.0, sw = 0.0;
+  for (int k = 1; k <= D.nk; ++k)
+    for (int j = 1; j <= D.nj; ++j)
+      for (int i = 1; i <= D.ni; ++i) {
+        const double p = F(phi, i, j, k);
+        sp = sp + p;
+        su = su + p * F(u, i, j, k);
+        sv = sv + p * F(v, i, j, k);
+        sw = sw + p * F(w, i, j, k);
+      }
+  vel[0] = su / sp;
+  vel[1] = sv / sp;
+  vel[2] = sw / sp;
+  const double dia = (*radius) * 2.0;
+  for (int q = 0; q < 3; ++q) re[q] = (*rhol) * vel[q] * dia / (*rmul);
+}
+
+// cal_center.f:1-121 -- centre of mass of phi with the x position unwrapped across
+// the periodic direction (lap counts the passes; area 1/2/3 = x below xl/4, between,
+// above 3xl/4), the x velocity from the previous centre, and the state update.
+void orc_cal_center(const int* ipara, const int* ID, const int* svall, const int* ni, const int* nj,
+                    const int* nk, const double* xl, const double* yl, const double* zl, const double* dt,
+                    const double* rhog, const double* phi, double* center, double* center_pre1,
+                    double* center_pre2, int* area_pre1, int* area_pre2, int* lap, double* velocity) {
+  (void)ipara;
+  (void)zl;
+  (void)rhog;
+  Dim D(*ni, *nj, *nk);
+  const double L = *xl;
+  const double delta = (*yl) / (double)(*svall);
+  const double sensor1 = L * 0.25, sensor2 = L * 0.75;
+  if (*area_pre1 == 1 && *area_pre2 == 3) *lap = *lap + 1;
+  double wt = 0.0, wx = 0.0, wy = 0.0, wz = 0.0;
+  for (int k = 1; k <= D.nk; ++k)
+    for (int j = 1; j <= D.nj; ++j)
+      for (int i = 1; i <= D.ni; ++i) {
+        const double p = F(phi, i, j, k);
+        wt = wt + p;
+        double x = delta * ((double)i - 0.5);
+        const double y = delta * ((double)(j + (*ID) * D.nj) - 0.5);
+        const double z = delta * ((double)k - 0.5);
+        if (*area_pre1 == 3 && x < sensor1) x = x + L;
+        if (*area_pre1 == 1 && x > sensor2) x = x - L;
+        x = x + L * (double)(*lap);
+        wx = wx + p * x;
+        wy = wy + p * y;
+        wz = wz + p * z;
+      }
+  center[0] = wx / wt;
+  center[1] = wy / wt;
+  center[2] = wz / wt;
+  *velocity = (center[0] - *center_pre1) / (*dt);
+  *center_pre2 = *center_pre1;
+  *center_pre1 = center[0];
+  double cc = center[0];
+  *area_pre2 = *area_pre1;
+  if (cc > L && L > 0.0 && std::isfinite(cc)) {  // the reference's loop never ends on inf
+    for (;;) {
+      cc = cc - L;
+      if (cc < L) break;
+    }
+  }
+  if (cc < sensor1) *area_pre1 = 1;
+  if (cc > sensor2) *area_pre1 = 3;
+  if (sensor1 <= cc && cc <= sensor2) *area_pre1 = 2;
+}
+
+// find_interface_positions_upper.f90:1-26 (find_interface_positions.f90 is the same
+// routine): every crossing phi(i,nj,k) > 0.5 > phi(i+1,nj,k) of the top wall row, in
+// the reference's print order (k outer, i inner).  Writes up to cap (x, z) pairs and
+// returns the number of crossings.
+int orc_interface_upper(const int* ni, const int* nj, const int* nk, const double* phi, const double* dx,
+                        const double* dz, const double* xl, double* xz, int cap) {
+  Dim D(*ni, *nj, *nk);
+  int c = 0;
+  for (int k = 1; k <= D.nk; ++k) {
+    const double z = ((double)k - 0.5) * (*dz);
+    for (int i = 1; i <= D.ni; ++i) {
+      const double p1 = F(phi, i, D.nj, k), p2 = F(phi, i + 1, D.nj, k);
+      if (p1 > 0.5 && p2 < 0.5) {
+        if (c < cap) {
+          xz[2 * c] = ((double)i - 0.5) * (*dx) + (0.5 - p1) * (*dx) / (p2 - p1) - (*xl) * 0.75;
+          xz[2 * c + 1] = z;
+        }
+        ++c;
+      }
+    }
+  }
+  return c;
+}
+
 // ---------------------------------------------------------------------------
 // The step driver.
 struct orc_ws {

@@ -170,6 +170,17 @@ void orc_fft2d(double* data, int n1, int n2, int sign);
 double orc_interface_lower(const int* ni, const int* nj, const int* nk, const double* phi,
                            const double* dx, const double* xl);
 
+/* ---- monitors: cal_vel.f, cal_center.f, find_interface_positions_upper.f90 */
+void orc_cal_vel(const int* ipara, const int* ni, const int* nj, const int* nk, const double* radius,
+                 const double* rhol, const double* rmul, const double* u, const double* v, const double* w,
+                 const double* phi, double* vel, double* re);
+void orc_cal_center(const int* ipara, const int* ID, const int* svall, const int* ni, const int* nj,
+                    const int* nk, const double* xl, const double* yl, const double* zl, const double* dt,
+                    const double* rhog, const double* phi, double* center, double* center_pre1,
+                    double* center_pre2, int* area_pre1, int* area_pre2, int* lap, double* velocity);
+int orc_interface_upper(const int* ni, const int* nj, const int* nk, const double* phi, const double* dx,
+                        const double* dz, const double* xl, double* xz, int cap);
+
 /* ---- the step driver: main.f90:473-697 ---------------------------------- */
 typedef struct {
   int ni, nj, nk;
