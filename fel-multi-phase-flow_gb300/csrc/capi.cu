@@ -672,6 +672,206 @@ void cal_center_(int* ipara, int* ID, int* svall, int* ni, int* nj, int* nk, dou
   call.finish();
 }
 
+// ---------------------------------------------------------------- output (f3)
+// mk_all.f:1-56: qk_all = wrk_all = qk over rows jst..jen (the whole array on one GPU)
+void mk_all_(int* ipara, int* ID, int* nID, int* ndiv, int* ni, int* nj, int* nk, double* wrk_all, double* qk,
+             double* qk_all) {
+  (void)ID;
+  if (!one_rank(ipara) || !walls_only(nID)) return;
+  if (*ndiv != 1) {
+    set_status(FMF_ERR_UNSUPPORTED);
+    return;
+  }
+  GRID3;
+  const double* q = call.in(qk, N3);
+  double* a = call.out(qk_all, N3);
+  double* w = call.out(wrk_all, N3);
+  if (call.ok) {
+    FMF_CUDA(cudaMemcpyAsync(a, q, sizeof(double) * N3, cudaMemcpyDeviceToDevice, s));
+    FMF_CUDA(cudaMemcpyAsync(w, q, sizeof(double) * N3, cudaMemcpyDeviceToDevice, s));
+  }
+  call.finish();
+}
+}  // extern "C"
+namespace {
+void mk_slice(int axis, int* ipara, int* nID, int* ndiv, int* ni, int* nj, int* nk, int* fixed, int* ip, int* jp,
+              int* kp, double* wrk_slice, double* qk, double* qk_slice) {
+  if (!one_rank(ipara)) return;
+  if (*ndiv != 1) {
+    set_status(FMF_ERR_UNSUPPORTED);
+    return;
+  }
+  GRID3;
+  const int lim = axis == 1 ? *nj : *nk;
+  if (*fixed < -2 || *fixed > lim + 2 || *ip < 0 || *ip > 1 || *jp < 0 || *jp > 1 || *kp < 0 || *kp > 1) {
+    set_status(FMF_ERR_ARG);
+    return;
+  }
+  // rows from 0 where the domain ends below (nID(Z_MINUS) / nID(Y_MINUS) < 0), else 1
+  const int st = (nID ? nID[axis == 1 ? 2 : 1] : -1) < 0 ? 0 : 1;
+  const long ns = (long)(*ni + 1) * ((axis == 1 ? *nk : *nj) + 1);
+  const double* q = call.in(qk, N3);
+  double* o = call.out(qk_slice, ns);
+  double* w = call.out(wrk_slice, ns);
+  FMF_LAUNCH(op::slice, s, g, q, axis, *fixed, *ip, *jp, *kp, st, o);
+  if (call.ok) FMF_CUDA(cudaMemcpyAsync(w, o, sizeof(double) * ns, cudaMemcpyDeviceToDevice, s));
+  call.finish();
+}
+// mkvtk_phi.f / mkvtk_phil.f / mkvtk_p.f: ghosts in place, vertex means, one file
+void mkvtk(int kind, const char* fname, const char* scalar, int* svall, int* nstep, double* dx, double* dy,
+           double* dz, double* qk) {
+  int ni_ = svall[0], nj_ = svall[1], nk_ = svall[2];
+  int *ni = &ni_, *nj = &nj_, *nk = &nk_;
+  GRID3;
+  const long nv = (long)(ni_ + 1) * (nj_ + 1) * (nk_ + 1);
+  double* q = call.out(qk, N3);
+  double* v = (double*)scratch(sizeof(double) * nv, 14);
+  FMF_LAUNCH(op::vtk_ghosts, s, g, q, kind);
+  FMF_LAUNCH(op::vtk_vertex, s, g, q, v);
+  if (call.ok) {
+    std::vector<double> h((size_t)nv);
+    FMF_CUDA(cudaMemcpyAsync(h.data(), v, sizeof(double) * nv, cudaMemcpyDeviceToHost, s));
+    FMF_CUDA(cudaStreamSynchronize(s));
+    const double org[3] = {0.0, 0.0, 0.0}, sp[3] = {*dx, *dy, *dz};
+    if (!get_status()) {
+      const int st = op::write_vtk(fname, scalar, *nstep, ni_ + 1, nj_ + 1, nk_ + 1, org, sp, h.data());
+      if (st) set_status(st);
+    }
+  }
+  call.finish();
+}
+}  // namespace
+extern "C" {
+// mk_slice_j.f:1-60 (8-point means at row j over i 0..ni, k 0..nk)
+void mk_slice_j_(int* ipara, int* ID, int* nID, int* ndiv, int* ni, int* nj, int* nk, int* j, int* ip, int* jp,
+                 int* kp, double* wrk_slice, double* qk, double* qk_slice) {
+  (void)ID;
+  mk_slice(1, ipara, nID, ndiv, ni, nj, nk, j, ip, jp, kp, wrk_slice, qk, qk_slice);
+}
+// mk_slice_k.f:1-60 (8-point means at plane k over i 0..ni, j 0..nj)
+void mk_slice_k_(int* ipara, int* ID, int* nID, int* ndiv, int* ni, int* nj, int* nk, int* k, int* ip, int* jp,
+                 int* kp, double* wrk_slice, double* qk, double* qk_slice) {
+  (void)ID;
+  mk_slice(2, ipara, nID, ndiv, ni, nj, nk, k, ip, jp, kp, wrk_slice, qk, qk_slice);
+}
+// mkvtk_phi.f:1-87 -> phi_<nstep>.vtk
+void mkvtk_phi_(int* svall, int* nstep, double* dx, double* dy, double* dz, double* q) {
+  char f[48];
+  std::snprintf(f, sizeof(f), "phi_%07d.vtk", *nstep);
+  mkvtk(0, f, "phi", svall, nstep, dx, dy, dz, q);
+}
+// mkvtk_phil.f:1-88 -> phi<l>_<nstep>.vtk
+void mkvtk_phil_(int* svall, int* nstep, double* dx, double* dy, double* dz, double* q, int* l) {
+  char f[48];
+  std::snprintf(f, sizeof(f), "phi%02d_%07d.vtk", *l, *nstep);
+  mkvtk(1, f, "p", svall, nstep, dx, dy, dz, q);
+}
+// mkvtk_p.f:1-91 -> p_<nstep>.vtk
+void mkvtk_p_(int* svall, int* nstep, double* dx, double* dy, double* dz, double* q) {
+  char f[48];
+  std::snprintf(f, sizeof(f), "p_%07d.vtk", *nstep);
+  mkvtk(2, f, "p", svall, nstep, dx, dy, dz, q);
+}
+// mkvtk_q.f:1-79 -> q1_<nstep>.vtk (q where the x-vorticity is > 0), q2_ (< 0)
+void mkvtk_q_(int* svall, int* nstep, double* dx, double* dy, double* dz, double* vorx, double* q) {
+  int ni_ = svall[0], nj_ = svall[1], nk_ = svall[2];
+  int *ni = &ni_, *nj = &nj_, *nk = &nk_;
+  GRID3;
+  const long nc = (long)ni_ * nj_ * nk_;
+  const double* vx = call.in(vorx, N3);
+  const double* qq = call.in(q, N3);
+  double* o = (double*)scratch(sizeof(double) * 2 * nc, 14);
+  FMF_LAUNCH(op::vtk_q, s, g, vx, qq, o, o + nc);
+  if (call.ok) {
+    std::vector<double> h((size_t)(2 * nc));
+    FMF_CUDA(cudaMemcpyAsync(h.data(), o, sizeof(double) * 2 * nc, cudaMemcpyDeviceToHost, s));
+    FMF_CUDA(cudaStreamSynchronize(s));
+    const double org[3] = {*dx * 0.5, *dy * 0.5, *dz * 0.5}, sp[3] = {*dx, *dy, *dz};
+    for (int t = 0; t < 2 && !get_status(); ++t) {
+      char f[48];
+      std::snprintf(f, sizeof(f), "q%d_%07d.vtk", t + 1, *nstep);
+      const int st = op::write_vtk(f, "p", *nstep, ni_, nj_, nk_, org, sp, h.data() + t * nc);
+      if (st) set_status(st);
+    }
+  }
+  call.finish();
+}
+
+}  // extern "C"
+namespace {
+// the slice files of mkuwp.h / mkuvp.h: rows of (a, b, [0,] u, v, phi) with values
+// below 1e-40 in magnitude written as 0, a blank record after each row
+int write_slice(const char* fname, int n1, int n2, double d1, double d2, bool zero_col, const double* s1,
+                const double* s2, const double* s3) {
+  FILE* f = std::fopen(fname, "w");
+  if (!f) return FMF_ERR_ARG;
+  auto clip = [](double x) { return std::fabs(x) < 1.0e-40 ? 0.0 : x; };
+  for (int b = 0; b <= n2; ++b) {
+    for (int a = 0; a <= n1; ++a) {
+      const long o = (long)b * (n1 + 1) + a;
+      double v[6];
+      int m = 0;
+      v[m++] = (double)a * d1;
+      v[m++] = (double)b * d2;
+      if (zero_col) v[m++] = 0.0;
+      v[m++] = clip(s1[o]);
+      v[m++] = clip(s2[o]);
+      v[m++] = clip(s3[o]);
+      op::write_e20(f, v, m);
+    }
+    std::fputc('\n', f);
+  }
+  const bool ok = std::fclose(f) == 0;
+  if (ok) std::printf(" output %s\n", fname);
+  return ok ? 0 : FMF_ERR_ARG;
+}
+int append_log(const char* fname, const double* v, int n) {
+  FILE* f = std::fopen(fname, "a");
+  if (!f) return FMF_ERR_ARG;
+  op::write_e20(f, v, n);
+  return std::fclose(f) == 0 ? 0 : FMF_ERR_ARG;
+}
+}  // namespace
+extern "C" {
+int fmf_write_uwphi(int nstep, const int* svall, double dx, double dz, const double* u_slice, const double* w_slice,
+                    const double* phi_slice) {
+  if (!svall || !u_slice || !w_slice || !phi_slice) return FMF_ERR_ARG;
+  char f[48];
+  std::snprintf(f, sizeof(f), "uwphi%07d", nstep);
+  return write_slice(f, svall[0], svall[2], dx, dz, false, u_slice, w_slice, phi_slice);
+}
+int fmf_write_uvwp(int nstep, const int* svall, double dx, double dy, const double* u_slice, const double* v_slice,
+                   const double* phi_slice) {
+  if (!svall || !u_slice || !v_slice || !phi_slice) return FMF_ERR_ARG;
+  char f[48];
+  std::snprintf(f, sizeof(f), "uvwp%07d", nstep);
+  return write_slice(f, svall[0], svall[1], dx, dy, true, u_slice, v_slice, phi_slice);
+}
+// mk_center.f:1-23: appends time, center(3), velocity, |(cx, cz) - (0.5, 0.5)| to center_<l>.dat
+void mk_center_(int* nstep, double* time, double* center, double* velocity, int* l) {
+  (void)nstep;
+  char f[48];
+  std::snprintf(f, sizeof(f), "center_%02d.dat", *l);
+  const double a = center[0] - 0.5, b = center[2] - 0.5;
+  const double v[6] = {*time, center[0], center[1], center[2], *velocity, std::sqrt(a * a + b * b)};
+  const int st = append_log(f, v, 6);
+  if (st) set_status(st);
+}
+// mk_vel.f:1-20: appends time, vel(3), re(1), re(2), velocity to velocity_<l>.dat
+void mk_vel_(int* nstep, double* time, double* vel, double* re, double* velocity, int* l) {
+  (void)nstep;
+  char f[48];
+  std::snprintf(f, sizeof(f), "velocity_%02d.dat", *l);
+  const double v[7] = {*time, vel[0], vel[1], vel[2], re[0], re[1], *velocity};
+  const int st = append_log(f, v, 7);
+  if (st) set_status(st);
+}
+int fmf_format_fortran_e(char* buf, int bufsize, double x, int w, int d) {
+  if (!buf || w < 1 || d < 1 || d > 30 || bufsize < w + 1) return FMF_ERR_ARG;
+  op::fortran_e(buf, x, w, d);
+  return 0;
+}
+
 // ---------------------------------------------------------------- part 2
 void fmf_dev_cal_advu_weno5(int ni, int nj, int nk, double dxinv, double dyinv, double dzinv, const double* u,
                             const double* v, const double* w, double* au, double* av, double* aw) {

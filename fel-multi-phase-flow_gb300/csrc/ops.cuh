@@ -4,6 +4,7 @@
 // from fmf::scratch).  Each one reproduces exactly the write set of the
 // subroutine it replaces (cited in the .cu file that defines it).
 #pragma once
+#include <cstdio>
 #include "fmf_common.cuh"
 
 namespace fmf {
@@ -78,6 +79,21 @@ void diag_interface_upper(cudaStream_t s, const Grid& g, double dx, double dz, d
                           double* xz, int* count, int cap);
 // find_interface_positions_lower.f90:15-32 -- out[0] = -x_avg
 void diag_interface_lower(cudaStream_t s, const Grid& g, double dx, double xl, const double* phi, double* out);
+// Field output (vtk.cu).  vtk_ghosts: the ghost fill of mkvtk_*.f in place (kind 0
+// phi: copies in y and z; 1 phil: zeros in y, copies in z; 2 p: copies in y,
+// periodic in z; x periodic for all); vtk_vertex: the 8-point means at the
+// (mi+1)(mj+1)(mk+1) vertices 0..m; vtk_q: mkvtk_q.f's two masked copies of q;
+// slice: mk_slice_j.f (axis 1, fixed j) / mk_slice_k.f (axis 2, fixed k)
+void vtk_ghosts(cudaStream_t s, const Grid& g, double* q, int kind);
+void vtk_vertex(cudaStream_t s, const Grid& g, const double* q, double* out);
+void vtk_q(cudaStream_t s, const Grid& g, const double* vorx, const double* q, double* out1, double* out2);
+void slice(cudaStream_t s, const Grid& g, const double* q, int axis, int fixed, int ip, int jp, int kp, int st,
+           double* out);
+// host: Fortran Ew.d output (w characters + NUL), the VTK file, one '(20e20.10)' record
+void fortran_e(char* out, double x, int w, int d);
+int write_vtk(const char* fname, const char* scalar, int nstep, int nx, int ny, int nz, const double* origin,
+              const double* spacing, const double* vals);
+void write_e20(FILE* f, const double* v, int n);
 void cal_srcu(cudaStream_t s, const Grid& g, double dt, double grvb, double grvp, const double* u,
               const double* v, const double* w, const double* rho, const double* rhon,
               const double* const* adv, const double* const* advo, const double* const* prs,

@@ -266,6 +266,43 @@ void cal_center_(int* ipara, int* ID, int* svall, int* ni, int* nj, int* nk, dou
                  double* center_pre1, double* center_pre2, int* area_pre1, int* area_pre2,
                  int* lap, double* velocity);
 
+/* Field output.  The gathers and cell-to-vertex means run on the device; the files
+ * are written by the host in the reference's formats (Fortran Ew.d numbers), in the
+ * working directory, with the reference's names. */
+/* srcs/mk_all.f:1-56 (one rank: qk_all = wrk_all = qk; ndiv must be 1) */
+void mk_all_(int* ipara, int* ID, int* nID, int* ndiv, int* ni, int* nj, int* nk, double* wrk_all,
+             double* qk, double* qk_all);
+/* srcs/mk_slice_j.f:1-60 (qk_slice(0:ni,0:nk) = 8-point means at row j; ndiv must be 1) */
+void mk_slice_j_(int* ipara, int* ID, int* nID, int* ndiv, int* ni, int* nj, int* nk, int* j,
+                 int* ip, int* jp, int* kp, double* wrk_slice, double* qk, double* qk_slice);
+/* srcs/mk_slice_k.f:1-60 (qk_slice(0:ni,0:nj) = 8-point means at plane k) */
+void mk_slice_k_(int* ipara, int* ID, int* nID, int* ndiv, int* ni, int* nj, int* nk, int* k,
+                 int* ip, int* jp, int* kp, double* wrk_slice, double* qk, double* qk_slice);
+/* srcs/mkvtk_phi.f:1-87 (fills q's ghosts in place as the reference does; phi_<nstep>.vtk) */
+void mkvtk_phi_(int* svall, int* nstep, double* dx, double* dy, double* dz, double* q);
+/* srcs/mkvtk_phil.f:1-88 (phi<l>_<nstep>.vtk) */
+void mkvtk_phil_(int* svall, int* nstep, double* dx, double* dy, double* dz, double* q, int* l);
+/* srcs/mkvtk_p.f:1-91 (p_<nstep>.vtk) */
+void mkvtk_p_(int* svall, int* nstep, double* dx, double* dy, double* dz, double* q);
+/* srcs/mkvtk_q.f:1-79 (q1_<nstep>.vtk, q2_<nstep>.vtk) */
+void mkvtk_q_(int* svall, int* nstep, double* dx, double* dy, double* dz, double* vorx, double* q);
+/* srcs/mk_center.f:1-23 (appends one record to center_<l>.dat) */
+void mk_center_(int* nstep, double* time, double* center, double* velocity, int* l);
+/* srcs/mk_vel.f:1-20 (appends one record to velocity_<l>.dat) */
+void mk_vel_(int* nstep, double* time, double* vel, double* re, double* velocity, int* l);
+/* The slice files the reference writes inline from srcs/mkuwp.h:1-23 (uwphi<nstep>: x, z,
+ * u, w, phi over i 0..svall(1), k 0..svall(3)) and srcs/mkuvp.h:1-24 (uvwp<nstep>: x, y,
+ * 0, u, v, phi over i 0..svall(1), j 0..svall(2)); the slices are host arrays as
+ * mk_slice_j_/mk_slice_k_ return them.  Return FMF_OK or FMF_ERR_ARG. */
+int fmf_write_uwphi(int nstep, const int* svall, double dx, double dz, const double* u_slice,
+                    const double* w_slice, const double* phi_slice);
+int fmf_write_uvwp(int nstep, const int* svall, double dx, double dy, const double* u_slice,
+                   const double* v_slice, const double* phi_slice);
+/* x as Fortran's Ew.d edit descriptor writes it (w characters and a NUL into buf,
+ * bufsize >= w + 1); the formatter of the writers above.  Returns FMF_OK or
+ * FMF_ERR_ARG. */
+int fmf_format_fortran_e(char* buf, int bufsize, double x, int w, int d);
+
 /* Monitors the reference prints, returned instead of printed (no counterpart
  * with this signature in the reference; the values are those of
  * srcs/solu_sor4.f:298-305 and srcs/solp_fft_tdma4.f:84-93). */

@@ -9,8 +9,10 @@
 #include "fmf_oracle.h"
 
 #include <cmath>
+#include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <string>
 #include <vector>
 
 namespace {
@@ -1483,6 +1485,200 @@ int orc_interface_upper(const int* ni, const int* nj, const int* nk, const doubl
     }
   }
   return c;
+}
+
+// ---------------------------------------------------------------------------
+// Field output: mkvtk_phi.f / mkvtk_phil.f / mkvtk_p.f / mkvtk_q.f, mk_slice_j.f /
+// mk_slice_k.f, the slice files of mkuwp.h / mkuvp.h, mk_center.f, mk_vel.f.
+
+// Fortran Ew.d output (scale factor 0): optional sign, "0.", d digits of the value
+// rounded to nearest, exponent as E+dd (|e| <= 99) or +ddd (|e| <= 999); when the
+// field is one character too short the optional 0 goes; a field that still does
+// not fit prints w asterisks.
+static std::string orc_fe(double x, int w, int d) {
+  std::string r;
+  if (x != x) {
+    r = "NaN";
+  } else if (std::isinf(x)) {
+    r = x < 0 ? (w >= 9 ? "-Infinity" : "-Inf") : (w >= 8 ? "Infinity" : "Inf");
+  } else {
+    // d significant decimal digits of |x| and the decimal exponent of the first one
+    char t[80];
+    std::snprintf(t, sizeof(t), "%.*e", d - 1, std::fabs(x));
+    std::string mant;
+    const char* p = t;
+    for (; *p && *p != 'e'; ++p)
+      if (*p >= '0' && *p <= '9') mant += *p;
+    const int e10 = std::atoi(p + 1);
+    const bool allzero = mant.find_first_not_of('0') == std::string::npos;
+    const int ex = allzero ? 0 : e10 + 1;  // 0.d1d2.. x 10^ex
+    const bool neg = std::signbit(x);
+    std::string expo;
+    const int m = ex < 0 ? -ex : ex;
+    char b[16];
+    if (m < 100) {
+      std::snprintf(b, sizeof(b), "E%c%d%d", ex < 0 ? '-' : '+', m / 10, m % 10);
+      expo = b;
+    } else if (m < 1000) {
+      std::snprintf(b, sizeof(b), "%c%d", ex < 0 ? '-' : '+', m);
+      expo = b;
+    }
+    if (expo.empty()) return std::string((size_t)w, '*');
+    r = (neg ? "-0." : "0.") + mant + expo;
+    if ((int)r.size() == w + 1) r = (neg ? "-." : ".") + mant + expo;
+  }
+  if ((int)r.size() > w) return std::string((size_t)w, '*');
+  return std::string((size_t)(w - (int)r.size()), ' ') + r;
+}
+void orc_format_e(char* buf, double x, int w, int d) {
+  const std::string s = orc_fe(x, w, d);
+  std::memcpy(buf, s.c_str(), s.size() + 1);
+}
+
+static int orc_vtk_file(const char* fname, const char* scalar, int nstep, int nx, int ny, int nz, const double* o,
+                        const double* a, const std::vector<double>& v) {
+  FILE* f = std::fopen(fname, "w");
+  if (!f) return 1;
+  std::string s = "# vtk DataFile Version 2.0\nt=" + std::to_string(nstep) + "\nASCII\nDATASET STRUCTURED_POINTS\n";
+  s += "DIMENSIONS " + std::to_string(nx) + " " + std::to_string(ny) + " " + std::to_string(nz) + "\n";
+  s += "ORIGIN " + orc_fe(o[0], 11, 4) + " " + orc_fe(o[1], 11, 4) + " " + orc_fe(o[2], 11, 4) + "\n";
+  s += "ASPECT_RATIO " + orc_fe(a[0], 11, 4) + " " + orc_fe(a[1], 11, 4) + " " + orc_fe(a[2], 11, 4) + "\n\n";
+  s += "POINT_DATA " + std::to_string((long)nx * ny * nz) + "\nSCALARS " + scalar + " float\nLOOKUP_TABLE default\n";
+  std::fputs(s.c_str(), f);
+  for (double x : v) std::fprintf(f, "%s\n", orc_fe(x, 10, 3).c_str());
+  return std::fclose(f) == 0 ? 0 : 1;
+}
+
+// mkvtk_phi.f (kind 0), mkvtk_phil.f (kind 1, file phi<l>_), mkvtk_p.f (kind 2):
+// the ghost fill of q in place, then the 8-point vertex means
+int orc_mkvtk(int kind, const int* svall, const int* nstep, const double* dx, const double* dy, const double* dz,
+              double* q, const int* l) {
+  Dim D(svall[0], svall[1], svall[2]);
+  const int mi = D.ni, mj = D.nj, mk = D.nk;
+  for (int k = 0; k <= mk + 1; ++k)
+    for (int j = 0; j <= mj + 1; ++j) {
+      F(q, 0, j, k) = F(q, mi, j, k);
+      F(q, mi + 1, j, k) = F(q, 1, j, k);
+    }
+  for (int k = 0; k <= mk + 1; ++k)
+    for (int i = 0; i <= mi + 1; ++i) {
+      F(q, i, 0, k) = kind == 1 ? 0.0 : F(q, i, 1, k);
+      F(q, i, mj + 1, k) = kind == 1 ? 0.0 : F(q, i, mj, k);
+    }
+  for (int j = 0; j <= mj + 1; ++j)
+    for (int i = 0; i <= mi + 1; ++i) {
+      F(q, i, j, 0) = kind == 2 ? F(q, i, j, mk) : F(q, i, j, 1);
+      F(q, i, j, mk + 1) = kind == 2 ? F(q, i, j, 1) : F(q, i, j, mk);
+    }
+  std::vector<double> v;
+  v.reserve((size_t)(mi + 1) * (mj + 1) * (mk + 1));
+  for (int k = 0; k <= mk; ++k)
+    for (int j = 0; j <= mj; ++j)
+      for (int i = 0; i <= mi; ++i)
+        v.push_back((+F(q, i, j, k) + F(q, i + 1, j, k) + F(q, i, j + 1, k) + F(q, i + 1, j + 1, k) +
+                     F(q, i, j, k + 1) + F(q, i + 1, j, k + 1) + F(q, i, j + 1, k + 1) + F(q, i + 1, j + 1, k + 1)) *
+                    0.125);
+  char fname[48];
+  if (kind == 1) std::snprintf(fname, sizeof(fname), "phi%02d_%07d.vtk", *l, *nstep);
+  else std::snprintf(fname, sizeof(fname), kind == 0 ? "phi_%07d.vtk" : "p_%07d.vtk", *nstep);
+  const double o[3] = {0.0, 0.0, 0.0}, a[3] = {*dx, *dy, *dz};
+  return orc_vtk_file(fname, kind == 0 ? "phi" : "p", *nstep, mi + 1, mj + 1, mk + 1, o, a, v);
+}
+
+// mkvtk_q.f: q at the cells where the mean of the 4 surrounding x-vorticities is
+// > 0 (q1_ file) or < 0 (q2_ file), 0 elsewhere
+int orc_mkvtk_q(const int* svall, const int* nstep, const double* dx, const double* dy, const double* dz,
+                const double* vorx, const double* q) {
+  Dim D(svall[0], svall[1], svall[2]);
+  const double o[3] = {*dx * 0.5, *dy * 0.5, *dz * 0.5}, a[3] = {*dx, *dy, *dz};
+  for (int t = 1; t <= 2; ++t) {
+    std::vector<double> v;
+    for (int k = 1; k <= D.nk; ++k)
+      for (int j = 1; j <= D.nj; ++j)
+        for (int i = 1; i <= D.ni; ++i) {
+          const double vm =
+              (F(vorx, i, j - 1, k - 1) + F(vorx, i, j, k - 1) + F(vorx, i, j - 1, k) + F(vorx, i, j, k)) * 0.25;
+          double q00 = F(q, i, j, k);
+          if (t == 1 ? vm <= 0.0 : vm >= 0.0) q00 = 0.0;
+          v.push_back(q00);
+        }
+    char fname[48];
+    std::snprintf(fname, sizeof(fname), "q%d_%07d.vtk", t, *nstep);
+    if (orc_vtk_file(fname, "p", *nstep, D.ni, D.nj, D.nk, o, a, v)) return 1;
+  }
+  return 0;
+}
+
+// mk_slice_j.f (axis 1: fixed j, rows k) and mk_slice_k.f (axis 2: fixed k, rows j)
+// with one rank: out(0:ni, 0:n), rows below the start zero
+void orc_mk_slice(int axis, const int* nID, const int* ni, const int* nj, const int* nk, const int* fixed,
+                  const int* ip, const int* jp, const int* kp, const double* qk, double* out) {
+  Dim D(*ni, *nj, *nk);
+  const int n = axis == 1 ? D.nk : D.nj;
+  const int st = nID[axis == 1 ? 2 : 1] < 0 ? 0 : 1;
+  for (int r = 0; r <= n; ++r)
+    for (int i = 0; i <= D.ni; ++i) {
+      double v = 0.0;
+      if (r >= st) {
+        const int j = axis == 1 ? *fixed : r, k = axis == 1 ? r : *fixed;
+        const int a = *ip, b = *jp, c = *kp;
+        v = (F(qk, i, j, k) + F(qk, i + a, j, k) + F(qk, i, j + b, k) + F(qk, i + a, j + b, k) + F(qk, i, j, k + c) +
+             F(qk, i + a, j, k + c) + F(qk, i, j + b, k + c) + F(qk, i + a, j + b, k + c)) *
+            0.125;
+      }
+      out[(long)r * (D.ni + 1) + i] = v;
+    }
+}
+
+// mkuwp.h (kind 0: uwphi<nstep>, x z u w phi) and mkuvp.h (kind 1: uvwp<nstep>,
+// x y 0 u v phi): one '(20e20.10)' record per point, a blank record per row
+int orc_write_slices(int kind, int nstep, const int* svall, double d1, double d2, const double* s1, const double* s2,
+                     const double* s3) {
+  char fname[48];
+  std::snprintf(fname, sizeof(fname), kind == 0 ? "uwphi%07d" : "uvwp%07d", nstep);
+  FILE* f = std::fopen(fname, "w");
+  if (!f) return 1;
+  const int n1 = svall[0], n2 = kind == 0 ? svall[2] : svall[1];
+  for (int b = 0; b <= n2; ++b) {
+    for (int a = 0; a <= n1; ++a) {
+      const long o = (long)b * (n1 + 1) + a;
+      double u = s1[o], v = s2[o], q = s3[o];
+      if (std::fabs(u) < 1.0e-40) u = 0.0;
+      if (std::fabs(v) < 1.0e-40) v = 0.0;
+      if (std::fabs(q) < 1.0e-40) q = 0.0;
+      std::string line = orc_fe((double)a * d1, 20, 10) + orc_fe((double)b * d2, 20, 10);
+      if (kind == 1) line += orc_fe(0.0, 20, 10);
+      line += orc_fe(u, 20, 10) + orc_fe(v, 20, 10) + orc_fe(q, 20, 10);
+      std::fprintf(f, "%s\n", line.c_str());
+    }
+    std::fputc('\n', f);
+  }
+  return std::fclose(f) == 0 ? 0 : 1;
+}
+
+// mk_center.f / mk_vel.f: append one '(20e20.10)' record
+int orc_mk_center(const double* time, const double* center, const double* velocity, const int* l) {
+  char fname[48];
+  std::snprintf(fname, sizeof(fname), "center_%02d.dat", *l);
+  FILE* f = std::fopen(fname, "a");
+  if (!f) return 1;
+  const double v[6] = {*time, center[0], center[1], center[2], *velocity,
+                       std::sqrt((center[0] - 0.5) * (center[0] - 0.5) + (center[2] - 0.5) * (center[2] - 0.5))};
+  std::string line;
+  for (double x : v) line += orc_fe(x, 20, 10);
+  std::fprintf(f, "%s\n", line.c_str());
+  return std::fclose(f) == 0 ? 0 : 1;
+}
+int orc_mk_vel(const double* time, const double* vel, const double* re, const double* velocity, const int* l) {
+  char fname[48];
+  std::snprintf(fname, sizeof(fname), "velocity_%02d.dat", *l);
+  FILE* f = std::fopen(fname, "a");
+  if (!f) return 1;
+  const double v[7] = {*time, vel[0], vel[1], vel[2], re[0], re[1], *velocity};
+  std::string line;
+  for (double x : v) line += orc_fe(x, 20, 10);
+  std::fprintf(f, "%s\n", line.c_str());
+  return std::fclose(f) == 0 ? 0 : 1;
 }
 
 // ---------------------------------------------------------------------------

@@ -181,6 +181,22 @@ void orc_cal_center(const int* ipara, const int* ID, const int* svall, const int
 int orc_interface_upper(const int* ni, const int* nj, const int* nk, const double* phi, const double* dx,
                         const double* dz, const double* xl, double* xz, int cap);
 
+/* ---- field output: mkvtk_*.f, mk_slice_j/k.f, mkuwp.h/mkuvp.h, mk_center.f, mk_vel.f
+ * (files in the working directory; return 0 on success) */
+void orc_format_e(char* buf, double x, int w, int d);
+int orc_mkvtk(int kind, const int* svall, const int* nstep, const double* dx, const double* dy,
+              const double* dz, double* q, const int* l);
+int orc_mkvtk_q(const int* svall, const int* nstep, const double* dx, const double* dy,
+                const double* dz, const double* vorx, const double* q);
+void orc_mk_slice(int axis, const int* nID, const int* ni, const int* nj, const int* nk,
+                  const int* fixed, const int* ip, const int* jp, const int* kp, const double* qk,
+                  double* out);
+int orc_write_slices(int kind, int nstep, const int* svall, double d1, double d2, const double* s1,
+                     const double* s2, const double* s3);
+int orc_mk_center(const double* time, const double* center, const double* velocity, const int* l);
+int orc_mk_vel(const double* time, const double* vel, const double* re, const double* velocity,
+               const int* l);
+
 /* ---- the step driver: main.f90:473-697 ---------------------------------- */
 typedef struct {
   int ni, nj, nk;
