@@ -202,8 +202,11 @@ void mthinc3_T(cudaStream_t s, const Grid& g, const double* pb, const double* pa
 void weno_T(cudaStream_t s, const Grid& g, double dxi, double dyi, double dzi, const double* u, const double* v,
             const double* w, const double* const* ladv, double* lu, double* lv, double* lw, double* work);
 // CSF force of one field: lf (3 arrays) -> lphi; work: >= 42n doubles
+// kap: the curvatures the forward pass recorded at the interior u, v, w points
+// (fused csf_force), or nullptr to recompute them (calrn x4 + calrkap)
 void csf_T(cudaStream_t s, const Grid& g, double dxi, double dyi, double dzi, double rhol, double rhog,
-           double sigma, const double* phi, const double* const* lf, double* lphi, double* work);
+           double sigma, const double* phi, const double* const* lf, double* lphi, double* work,
+           const double* kap = nullptr);
 
 // ---- viscous solve -------------------------------------------------------------
 struct SrcArgs {

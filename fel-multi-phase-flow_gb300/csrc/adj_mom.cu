@@ -182,7 +182,8 @@ void weno_T(cudaStream_t s, const Grid& g, double dxi, double dyi, double dzi, c
 
 // ---- CSF --------------------------------------------------------------------------
 void csf_T(cudaStream_t s, const Grid& g, double dxi, double dyi, double dzi, double rhol, double rhog,
-           double sigma, const double* phi, const double* const* lf, double* lphi, double* work) {
+           double sigma, const double* phi, const double* const* lf, double* lphi, double* work,
+           const double* kap_rec) {
   const Grid G = g;
   const long n = g.n;
   double* Gv = work;             // vertex gradient (3n)
@@ -196,9 +197,13 @@ void csf_T(cudaStream_t s, const Grid& g, double dxi, double dyi, double dzi, do
   static const int offs[4][3] = {{1, 1, 1}, {0, 0, 1}, {0, 1, 0}, {1, 0, 0}};
   // forward recompute
   op::cal_grad_p2a(s, g, dxi, dyi, dzi, phi, Gv, Gv + n, Gv + 2 * n);
-  for (int q = 0; q < 4; ++q)
-    op::calrn(s, g, dxi, dyi, dzi, offs[q][0], offs[q][1], offs[q][2], Gv, Gv + n, Gv + 2 * n, rn + 3 * n * q);
-  op::calrkap(s, g, dxi, dyi, dzi, rn, rn + 3 * n, rn + 6 * n, rn + 9 * n, kap);
+  if (!kap_rec) {
+    for (int q = 0; q < 4; ++q)
+      op::calrn(s, g, dxi, dyi, dzi, offs[q][0], offs[q][1], offs[q][2], Gv, Gv + n, Gv + 2 * n, rn + 3 * n * q);
+    op::calrkap(s, g, dxi, dyi, dzi, rn, rn + 3 * n, rn + 6 * n, rn + 9 * n, kap);
+  } else {
+    kap = (double*)kap_rec;  // read only; valid where the force adjoints can be non-zero
+  }
   op::cal_grad_prs(s, g, dxi, dyi, dzi, phi, gq, gq + n, gq + 2 * n);
   // calfst: f_c = -st kap_c g_c
   const double st = 2.0 * sigma / (rhol + rhog);
@@ -207,7 +212,7 @@ void csf_T(cudaStream_t s, const Grid& g, double dxi, double dyi, double dzi, do
     const double L[3] = {lf0[t], lf1[t], lf2[t]};
     for (int q = 0; q < 3; ++q) {
       lkap[t + q * n] = -st * gq[t + q * n] * L[q];
-      lgq[t + q * n] = -st * kap[t + q * n] * L[q];
+      lgq[t + q * n] = L[q] != 0.0 ? -st * kap[t + q * n] * L[q] : 0.0;
     }
   });
   grad_prs_T(s, g, dxi, dyi, dzi, lgq, lgq + n, lgq + 2 * n, lphi);

@@ -93,6 +93,7 @@ struct fmf_adj {
   double* csfwork;  // forward CSF chain (drop-in): G(3n) rn(12n) kap(3n) g(3n) f(3n)
   int* band;        // MTHINC band-cell list and its length
   double* newton;   // per band-list entry: Newton offset, last Newton step
+  double *kap, *kapn;  // curvatures of phi and phin at the u, v, w points (fused CSF)
   // adjoints
   double* lS[NSTATE];  // adjoint of the step-start state (in/out of reverse_step)
   double *lgx[3], *lfl[3], *lrn, *ltheta, *lphn0, *lphn1, *lrho, *lrhon, *lrmu, *lrmun;
@@ -111,7 +112,7 @@ struct fmf_adj {
   struct Rec {
     double *gx1[3], *fl[3], *pb, *pass, *pc, *theta, *phn1f, *rho, *rhon, *rmu, *rmun;
     double *adv[3], *advo[3], *prs[3], *vis[3], *sfst[3], *sfstn[3], *sk, *E[3], *AB[6], *ustar[3], *un2[3];
-    double *wallc, *sums, *state, *newton;
+    double *wallc, *sums, *state, *newton, *kap, *kapn;
     int* band;
   };
   std::vector<Rec> recs;
@@ -171,11 +172,13 @@ void set_rec(fmf_adj* a, const fmf_adj::Rec& r) {
   a->sums = r.sums;
   a->band = r.band;
   a->newton = r.newton;
+  a->kap = r.kap;
+  a->kapn = r.kapn;
 }
 long nwall(const Grid& g) { return 4L * (g.nk + 6) * (g.ni + 6); }
 long nband_d(const Grid& g) { return ((long)(g.ni + 2) * (g.nj + 2) * (g.nk + 2) + 2) / 2 + 1; }
 long nband(const Grid& g) { return (long)(g.ni + 2) * (g.nj + 2) * (g.nk + 2); }
-long slot_doubles(const Grid& g) { return 66 * g.n + nwall(g) + 8 + 2 * nband(g) + nband_d(g) + 16; }
+long slot_doubles(const Grid& g) { return 72 * g.n + nwall(g) + 8 + 2 * nband(g) + nband_d(g) + 16; }
 // carve one slot out of a block of slot_doubles(g) doubles
 fmf_adj::Rec carve(const Grid& g, double* p) {
   const long n = g.n;
@@ -213,6 +216,8 @@ fmf_adj::Rec carve(const Grid& g, double* p) {
   r.wallc = take(nwall(g));
   r.sums = take(8);
   r.newton = take(2 * nband(g));
+  r.kap = take(3 * g.n);
+  r.kapn = take(3 * g.n);
   r.band = (int*)take(nband_d(g));
   return r;
 }
@@ -407,8 +412,10 @@ int record_step(fmf_adj* a) {
   // :545-573 (the fused kernel where the grid tiles; csf_T differentiates the same
   // sequence of reference subroutines either way)
   if (fused::csf_supported(g)) {
-    fused::csf_force(s, g, dxi, dyi, dzi, P.rhol, P.rhog, P.sigma, phi1, a->sfst[0], a->sfst[1], a->sfst[2]);
-    fused::csf_force(s, g, dxi, dyi, dzi, P.rhol, P.rhog, P.sigma, phn1, a->sfstn[0], a->sfstn[1], a->sfstn[2]);
+    fused::csf_force(s, g, dxi, dyi, dzi, P.rhol, P.rhog, P.sigma, phi1, a->sfst[0], a->sfst[1], a->sfst[2], false,
+                     a->kap);
+    fused::csf_force(s, g, dxi, dyi, dzi, P.rhol, P.rhog, P.sigma, phn1, a->sfstn[0], a->sfstn[1], a->sfstn[2],
+                     false, a->kapn);
   } else {
     csf_fwd(a, phi1, a->sfst);
     csf_fwd(a, phn1, a->sfstn);
@@ -620,9 +627,13 @@ void reverse_step(fmf_adj* a, const double* st) {
   // :545-573 surface tension of phi(1) and phin(1)
   {
     const double* lf[3] = {a->lsfst[0], a->lsfst[1], a->lsfst[2]};
-    adj::csf_T(s, g, dxi, dyi, dzi, P.rhol, P.rhog, P.sigma, ST(SPHI1), lf, lS[SPHI1], a->work + 3 * n + 1024);
+    // the curvatures recorded by the fused forward kernel where the grid tiles
+    const bool rec = fused::csf_supported(g);
+    adj::csf_T(s, g, dxi, dyi, dzi, P.rhol, P.rhog, P.sigma, ST(SPHI1), lf, lS[SPHI1], a->work + 3 * n + 1024,
+               rec ? a->kap : nullptr);
     const double* lfn[3] = {a->lsfstn[0], a->lsfstn[1], a->lsfstn[2]};
-    adj::csf_T(s, g, dxi, dyi, dzi, P.rhol, P.rhog, P.sigma, a->phn1f, lfn, a->lphn1, a->work + 3 * n + 1024);
+    adj::csf_T(s, g, dxi, dyi, dzi, P.rhol, P.rhog, P.sigma, a->phn1f, lfn, a->lphn1, a->work + 3 * n + 1024,
+               rec ? a->kapn : nullptr);
   }
   check_stage(a, "csf");
   // :536-541 explicit viscous term, pressure gradient, advection

@@ -24,10 +24,12 @@ void mthinc_fluxes(cudaStream_t s, const Grid& g, double dxinv, double dyinv, do
 
 // CSF force of one field on the interior u, v, w points (fu/fv/fw), replacing
 // cal_grad_p2a + calrn x4 + calrkap + cal_grad_p2uvw + calfst; needs ni % 32 == 0
-// and nj % 8 == 0 (csf_supported).  fp32: normals and curvature in FP32.
+// and nj % 8 == 0 (csf_supported).  fp32: normals and curvature in FP32.  kap
+// (optional, 3 arrays of n): the curvatures at the interior u, v, w points.
 bool csf_supported(const Grid& g);
 void csf_force(cudaStream_t s, const Grid& g, double dxinv, double dyinv, double dzinv, double rhol, double rhog,
-               double sigma, const double* phi, double* fu, double* fv, double* fw, bool fp32 = false);
+               double sigma, const double* phi, double* fu, double* fv, double* fw, bool fp32 = false,
+               double* kap = nullptr);
 
 // Viscous solve.  src_visc_prep: edge viscosities E[0..2] (xy, xz, yz edges, i,j,k in
 // 0..n), per-component A/B (AB[0..5] = Au Bu Av Bv Aw Bw) with the momentum

@@ -184,7 +184,7 @@ __device__ void centre_normals(const CsfP<R>& p, Smem<R>& S, int gk, int gk1, in
 template <class R>
 __global__ void __launch_bounds__(256) k_csf(Grid g, CsfP<R> p, int kchunk, const double* __restrict__ phi,
                                              double* __restrict__ fu, double* __restrict__ fv,
-                                             double* __restrict__ fw) {
+                                             double* __restrict__ fw, double* __restrict__ kap) {
   extern __shared__ double smraw[];
   Smem<R>& S = *reinterpret_cast<Smem<R>*>(smraw);
   const int I0 = 1 + blockIdx.x * TX, J0 = 1 + blockIdx.y * TY;
@@ -248,6 +248,11 @@ __global__ void __launch_bounds__(256) k_csf(Grid g, CsfP<R> p, int kchunk, cons
       fu[c] = (double)(-p.st * ku * ((px - ph) * p.dxi));
       fv[c] = (double)(-p.st * kv * ((py - ph) * p.dyi));
       fw[c] = (double)(-p.st * kw * ((pz - ph) * p.dzi));
+      if (kap) {  // the curvatures at the u, v, w points, kept for the adjoint
+        kap[c] = (double)ku;
+        kap[c + g.n] = (double)kv;
+        kap[c + 2 * g.n] = (double)kw;
+      }
     }
     __syncthreads();
     gA ^= 1;
@@ -259,7 +264,7 @@ __global__ void __launch_bounds__(256) k_csf(Grid g, CsfP<R> p, int kchunk, cons
 
 template <class R>
 void launch_csf(cudaStream_t s, const Grid& g, double dxinv, double dyinv, double dzinv, double rhol, double rhog,
-                double sigma, const double* phi, double* fu, double* fv, double* fw) {
+                double sigma, const double* phi, double* fu, double* fv, double* fw, double* kap) {
   CsfP<R> p;
   p.dxi = (R)dxinv;
   p.dyi = (R)dyinv;
@@ -273,7 +278,7 @@ void launch_csf(cudaStream_t s, const Grid& g, double dxinv, double dyinv, doubl
   const size_t smem = sizeof(Smem<R>);
   cudaFuncSetAttribute(k_csf<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   dim3 gr((unsigned)(g.ni / TX), (unsigned)(g.nj / TY), (unsigned)((g.nk + kchunk - 1) / kchunk));
-  k_csf<R><<<gr, 256, smem, s>>>(g, p, kchunk, phi, fu, fv, fw);
+  k_csf<R><<<gr, 256, smem, s>>>(g, p, kchunk, phi, fu, fv, fw, kap);
   count_launch();
 }
 }  // namespace
@@ -281,11 +286,11 @@ void launch_csf(cudaStream_t s, const Grid& g, double dxinv, double dyinv, doubl
 bool csf_supported(const Grid& g) { return g.ni % TX == 0 && g.nj % TY == 0; }
 
 void csf_force(cudaStream_t s, const Grid& g, double dxinv, double dyinv, double dzinv, double rhol, double rhog,
-               double sigma, const double* phi, double* fu, double* fv, double* fw, bool fp32) {
+               double sigma, const double* phi, double* fu, double* fv, double* fw, bool fp32, double* kap) {
   if (fp32)
-    launch_csf<float>(s, g, dxinv, dyinv, dzinv, rhol, rhog, sigma, phi, fu, fv, fw);
+    launch_csf<float>(s, g, dxinv, dyinv, dzinv, rhol, rhog, sigma, phi, fu, fv, fw, kap);
   else
-    launch_csf<double>(s, g, dxinv, dyinv, dzinv, rhol, rhog, sigma, phi, fu, fv, fw);
+    launch_csf<double>(s, g, dxinv, dyinv, dzinv, rhol, rhog, sigma, phi, fu, fv, fw, kap);
 }
 
 }  // namespace fused

@@ -141,7 +141,11 @@ __global__ void __launch_bounds__(128) k_band(Grid g, MC m, const double* __rest
       // df = 0.5 bet sum 0.125/cosh^2 = 0.5 bet * 0.125 * 4 * sum s(1-s)
       const R df = (R)0.25 * bet * sd;
       step = f * df / (df * df + reg);
-      ddd = ddd - step;
+      const R dn = ddd - step;
+      // once d no longer changes, every remaining iteration recomputes the same
+      // f, df and step: stopping here is the ten-step result bit for bit
+      if (dn == ddd) break;
+      ddd = dn;
     }
     if (newton) {
       newton[e] = (double)ddd;

@@ -43,7 +43,11 @@ __device__ __forceinline__ double wdir(const double* __restrict__ q, long c, lon
   const double m3 = __ldg(q + c - 3 * S), m2 = __ldg(q + c - 2 * S), m1 = __ldg(q + c - S), z0 = __ldg(q + c),
                p1 = __ldg(q + c + S), p2 = __ldg(q + c + 2 * S), p3 = __ldg(q + c + 3 * S);
   const double dm5 = m2 - m3, dm3 = m1 - m2, dm1 = z0 - m1, dp1 = p1 - z0, dp3 = p2 - p1, dp5 = p3 - p2;
-  const double r = vel > 0.0 ? weno_side<double>(dm5, dm3, dm1, dp1, dp3) : weno_side<double>(dp5, dp3, dp1, dm1, dm3);
+  // the upwind side's inputs chosen by selects: one inlined side, no divergence
+  // where the velocity changes sign inside a warp
+  const bool pos = vel > 0.0;
+  const double r = weno_side<double>(pos ? dm5 : dp5, pos ? dm3 : dp3, pos ? dm1 : dp1, pos ? dp1 : dm1,
+                                     pos ? dp3 : dm3);
   return (vel + vel) * r * (1.0 / 12.0);
 }
 
@@ -91,7 +95,8 @@ __device__ __forceinline__ float wdir_f32(const double* __restrict__ q, long c, 
   // differences formed in double (cancellation-free), arithmetic in float
   const float dm5 = (float)(m2 - m3), dm3 = (float)(m1 - m2), dm1 = (float)(z0 - m1), dp1 = (float)(p1 - z0),
               dp3 = (float)(p2 - p1), dp5 = (float)(p3 - p2);
-  const float r = vel > 0.0f ? weno_side_f32(dm5, dm3, dm1, dp1, dp3) : weno_side_f32(dp5, dp3, dp1, dm1, dm3);
+  const bool pos = vel > 0.0f;
+  const float r = weno_side_f32(pos ? dm5 : dp5, pos ? dm3 : dp3, pos ? dm1 : dp1, pos ? dp1 : dm1, pos ? dp3 : dm3);
   return (vel + vel) * r * (1.0f / 12.0f);
 }
 __global__ void __launch_bounds__(128) k_weno2_f32(Grid g, double dxi_, double dyi_, double dzi_,
