@@ -1,6 +1,7 @@
 // adj_bc.cu -- adjoints of the boundary conditions, copies and linear stencils of
 // the step (k_bc.cu, k_glue.cu, k_press.cu, fused_visc.cu wall/halo kernels).
 #include "adj.cuh"
+#include "refresh.cuh"
 
 namespace fmf {
 namespace adj {
@@ -308,6 +309,146 @@ __global__ void __launch_bounds__(256) k_wall_T(Grid G, double uwall, const doub
     }
   }
 }
+// The owned rows of one source column next to wall SIDE (side 0: rows -2..2, side 1:
+// rows nj-3..nj+3) with its x, z and corner images gathered in, the wall transpose
+// applied and the images cleared; returns L1 + 2 L2 + 3 L3 of u or w (the weight of
+// the slip coefficient), 0 for v.  Every load is issued before the first store.
+template <int SIDE>
+__device__ __forceinline__ double wall_col_T(const Grid& G, double* __restrict__ a, int cmp, int i, int k, int ix,
+                                             int kz, double c2) {
+  constexpr int NR = SIDE ? 7 : 5;
+  const int j0 = SIDE ? G.nj - 3 : -2;
+  const long Y = G.sy;
+  const bool hx = ix != kNoHalo, hz = kz != kNoHalo;
+  const long c0 = G.at(i, j0, k), cx = hx ? G.at(ix, j0, k) : c0, cz = hz ? G.at(i, j0, kz) : c0,
+             cxz = hx && hz ? G.at(ix, j0, kz) : c0;
+  double gv[NR], vx[NR], vz[NR], vxz[NR];
+#pragma unroll
+  for (int r = 0; r < NR; ++r) {
+    gv[r] = a[c0 + r * Y];
+    vx[r] = hx ? a[cx + r * Y] : 0.0;
+    vz[r] = hz ? a[cz + r * Y] : 0.0;
+    vxz[r] = hx && hz ? a[cxz + r * Y] : 0.0;
+  }
+#pragma unroll
+  for (int r = 0; r < NR; ++r) gv[r] += vx[r] + vz[r] + vxz[r];
+  double S = 0.0;
+  if (cmp != 1) {  // u, w: the wall row is r = 3 (j = 1 or nj), its ghosts on the far side
+    constexpr int t1 = SIDE ? 1 : -1;
+    const double L1 = gv[3 + t1], L2 = gv[3 + 2 * t1], L3 = gv[3 + 3 * t1];
+    gv[3] += c2 * L1 + (2.0 * c2 - 1.0) * L2 + (3.0 * c2 - 2.0) * L3;
+    gv[3 + t1] = gv[3 + 2 * t1] = gv[3 + 3 * t1] = 0.0;
+    S = L1 + 2.0 * L2 + 3.0 * L3;
+  } else {
+    if constexpr (SIDE == 0) {  // v(0) = 0, v(-1) = -v(1), v(-2) = -v(2); rows -2..2 are r = 0..4
+      gv[3] -= gv[1];
+      gv[4] -= gv[0];
+      gv[0] = gv[1] = gv[2] = 0.0;
+    } else {  // v(nj) = 0, v(nj+m) = -v(nj-m); rows nj-3..nj+3 are r = 0..6
+      gv[2] -= gv[4];
+      gv[1] -= gv[5];
+      gv[0] -= gv[6];
+      gv[3] = gv[4] = gv[5] = gv[6] = 0.0;
+    }
+  }
+#pragma unroll
+  for (int r = 0; r < NR; ++r) {
+    a[c0 + r * Y] = gv[r];
+    if (hx) a[cx + r * Y] = 0.0;
+    if (hz) a[cz + r * Y] = 0.0;
+    if (hx && hz) a[cxz + r * Y] = 0.0;
+  }
+  return S;
+}
+// Transpose of the one-pass refresh (ni, nj, nk >= 8): the same result as halo_z_T,
+// halo_x_T and k_wall_T in that order.  Every ghost column is a copy of its source
+// column, so the adjoint of a source column is its own plus that of its images (the
+// x, z and corner destinations that copy it); the wall transpose then runs on the
+// source column only (on the cleared ghost columns it moves zeros).  Blocks [0, nbW):
+// one thread per (column, wall, component) owning rows -2..2 (or nj-3..nj+3) of a
+// source column and its images: gathers them, applies the wall transpose, clears
+// the images;
+// [nbW, nbW + nb1): rows 3..nj-4 of the x-source columns (8 lanes per (j, k,
+// component), with the z and corner images where k has one); the rest: rows
+// 3..nj-4 of the columns with a z image only.  Each point has one owner.
+__global__ void __launch_bounds__(256) k_refresh_T(Grid G, int normal, double uwall, const double* __restrict__ wc,
+                                                   const double* __restrict__ uk, const double* __restrict__ wk,
+                                                   double* __restrict__ lu, double* __restrict__ lv,
+                                                   double* __restrict__ lw, double* __restrict__ lwc, int nbW,
+                                                   int nb1) {
+  const int shu = !(normal & 1), shw = !(normal & 4);
+  const int NI = G.ni, NJ = G.nj, NK = G.nk;
+  const int b = (int)blockIdx.x;
+  if (b < nbW) {
+    const long t = (long)b * 256 + threadIdx.x;
+    const int W = NI + 6;
+    if (t >= 6L * W * (NK + 6)) return;
+    const int i = (int)(t % W) - 2;
+    const long r = t / W;
+    const int kk = (int)(r % (2 * (NK + 6)));
+    const int cmp = (int)(r / (2 * (NK + 6)));
+    const int side = kk >= NK + 6 ? 1 : 0;
+    const int k = kk - side * (NK + 6) - 2;
+    const int sx = cmp == 0 ? shu : 0, sz = cmp == 2 ? shw : 0;
+    if (halo_src(i, NI, sx) != i || halo_src(k, NK, sz) != k) return;  // a ghost column of this component
+    const long o = (((long)side * (NK + 6) + (k + 2)) * W + (i + 2)) * 2;
+    const double c2 = wc[o + 1];
+    double* a = cmp == 0 ? lu : (cmp == 1 ? lv : lw);
+    const int ix = halo_image(i, NI, sx), kz = halo_image(k, NK, sz);
+    const double S = side ? wall_col_T<1>(G, a, cmp, i, k, ix, kz, c2) : wall_col_T<0>(G, a, cmp, i, k, ix, kz, c2);
+    if (lwc && cmp != 1 && S != 0.0) {
+      // u and w of a column both feed lwc[o + 1]: atomic there
+      const long c = G.at(i, side ? NJ : 1, k);
+      if (cmp == 0) lwc[o] += (side ? uwall : -uwall) * S;
+      atomicAdd(lwc + o + 1, (cmp == 0 ? uk[c] : wk[c]) * S);
+    }
+    return;
+  }
+  if (b < nbW + nb1) {
+    const long t = (long)(b - nbW) * 256 + threadIdx.x;
+    const int m = (int)(t & 7);
+    const long task = t >> 3;
+    const int nj2 = NJ - 6;  // rows 3..nj-4
+    if (m >= 6 || task >= 3L * nj2 * (NK + 6)) return;
+    const int cmp = (int)(task / ((long)nj2 * (NK + 6)));
+    const int rem = (int)(task % ((long)nj2 * (NK + 6)));
+    const int j = 3 + rem % nj2, k = -2 + rem / nj2;
+    const int sx = cmp == 0 ? shu : 0, sz = cmp == 2 ? shw : 0;
+    if (halo_src(k, NK, sz) != k) return;  // a z destination: gathered by its source
+    const int d = halo_dest(m, NI, sx);
+    if (d == kNoHalo) return;
+    const int is = halo_src(d, NI, sx), kz = halo_image(k, NK, sz);
+    double* a = cmp == 0 ? lu : (cmp == 1 ? lv : lw);
+    const long c = G.at(is, j, k), e = G.at(d, j, k);
+    double v = a[c] + a[e];
+    a[e] = 0.0;
+    if (kz != kNoHalo) {
+      const long f = G.at(is, j, kz), h = G.at(d, j, kz);
+      v += a[f] + a[h];
+      a[f] = 0.0;
+      a[h] = 0.0;
+    }
+    a[c] = v;
+    return;
+  }
+  const long t = (long)(b - nbW - nb1) * 256 + threadIdx.x;
+  const int nj2 = NJ - 6;
+  const int i = 1 + (int)(t % (NI + 1));
+  long r = t / (NI + 1);
+  const int m = (int)(r % 6);
+  r /= 6;
+  const int j = 3 + (int)(r % nj2);
+  const int cmp = (int)(r / nj2);
+  if (cmp >= 3) return;
+  const int sx = cmp == 0 ? shu : 0, sz = cmp == 2 ? shw : 0;
+  if (halo_src(i, NI, sx) != i || halo_image(i, NI, sx) != kNoHalo) return;  // x ghost, or done with its x image
+  const int d = halo_dest(m, NK, sz);
+  if (d == kNoHalo) return;
+  double* a = cmp == 0 ? lu : (cmp == 1 ? lv : lw);
+  const long c = G.at(i, j, halo_src(d, NK, sz)), e = G.at(i, j, d);
+  a[c] += a[e];
+  a[e] = 0.0;
+}
 void wall_T(cudaStream_t s, const Grid& g, double uwall, const double* wc, const double* uk, const double* wk,
             double* lu, double* lv, double* lw, double* lwc) {
   k_wall_T<<<dim3((g.ni + 6 + 31) / 32, (2 * (g.nk + 6) + 7) / 8), dim3(32, 8), 0, s>>>(g, uwall, wc, uk, wk, lu, lv,
@@ -327,6 +468,14 @@ void halo_z_T(cudaStream_t s, const Grid& g, int normal, double* lu, double* lv,
 
 void wall_halo_T(cudaStream_t s, const Grid& g, int normal, double uwall, const double* wc, const double* u,
                  const double* w, double* lu, double* lv, double* lw, double* lwc) {
+  if (refresh_one_pass(g.ni, g.nj, g.nk)) {
+    const long tw = 6L * (g.ni + 6) * (g.nk + 6), t1 = 24L * (g.nj - 6) * (g.nk + 6),
+               t2 = 18L * (g.ni + 1) * (g.nj - 6);
+    const int nbW = (int)((tw + 255) / 256), nb1 = (int)((t1 + 255) / 256), nb2 = (int)((t2 + 255) / 256);
+    k_refresh_T<<<nbW + nb1 + nb2, 256, 0, s>>>(g, normal, uwall, wc, u, w, lu, lv, lw, lwc, nbW, nb1);
+    count_launch();
+    return;
+  }
   halo_z_T(s, g, normal, lu, lv, lw);
   halo_x_T(s, g, normal, lu, lv, lw);
   wall_T(s, g, uwall, wc, u, w, lu, lv, lw, lwc);

@@ -382,9 +382,8 @@ int sor_T(cudaStream_t s, const Grid& g, double dxi, double dyi, double dzi, con
       for (int pr = 3; pr >= 0; --pr) {
         const int idx = comp * 4 + pr;
         // transposed refresh; the slip-coefficient adjoint only in the gradient pass
-        halo_z_T(s, g, 1 << comp, lam[0], lam[1], lam[2]);
-        halo_x_T(s, g, 1 << comp, lam[0], lam[1], lam[2]);
-        wall_T(s, g, uwall, wallc, ustar[0], ustar[2], lam[0], lam[1], lam[2], grad ? lwc : nullptr);
+        wall_halo_T(s, g, 1 << comp, uwall, wallc, ustar[0], ustar[2], lam[0], lam[1], lam[2],
+                    grad ? lwc : nullptr);
         if (grad) {
           const CArr3 dq{{snaps + (3 * idx) * n, snaps + (3 * idx + 1) * n, snaps + (3 * idx + 2) * n}};
           const Arr4 lcf{{lmu, lE[0], lE[1], lE[2]}};

@@ -11,14 +11,15 @@
 // Colours are processed in their independent pairs (1,2) (3,4) (5,6) (7,8): two
 // colours that differ in every index parity never read each other, so one launch
 // per pair gives the sequential result.  The wall/halo refresh after every second
-// colour (bndu + bnd_periodic of the swept component, solu_sor4.f:176-180) is three
-// ordered plane kernels.
+// colour (bndu + bnd_periodic of the swept component, solu_sor4.f:176-180) is one
+// kernel (k_refresh; three ordered plane kernels on grids under 8 cells a side).
 //
 // The mixed-precision step solves the same system by one step of iterative
 // refinement: the residual of the first sweep is formed in FP64 at u, then the
 // sweeps run in FP32 on the correction d = un - u (FP32 storage and arithmetic),
 // and un = u + d is formed in FP64 at the end.
 #include "fused.cuh"
+#include "refresh.cuh"
 
 namespace fmf {
 namespace fused {
@@ -367,6 +368,107 @@ __global__ void __launch_bounds__(256) k_halo_x8(Grid g, int normal, double* __r
   } else if (!(sh && m == 3)) {
     a[r + g.ni + m - 2] = a[r + m - 2];
   }
+}
+// k_wall, k_halo_x and k_halo_z in one pass (ni, nj, nk >= 8).  Composed, the three
+// give every refreshed point as a function of points none of them writes: a ghost
+// column (x or z destination) holds its source column's values, its wall rows
+// included, and the wall rows of a column are the extrapolation of its source
+// column's interior rows with that column's coefficients.  So the threads write
+// their points in any order.  Blocks [0, nbW): the wall rows of every column, one
+// thread per (column, wall); [nbW, nbW + nbX): the other rows of the x-ghost
+// columns, 8 lanes per (j, k, component); the rest: the other rows of the z-ghost
+// planes over the columns that are not x destinations.
+__global__ void __launch_bounds__(256) k_refresh(Grid g, int normal, double uwall, const double* __restrict__ wc,
+                                                 double* __restrict__ uk, double* __restrict__ vk,
+                                                 double* __restrict__ wk, int nbW, int nbX) {
+  const int shu = !(normal & 1), shw = !(normal & 4);  // bndu's shifted copies: u along x, w along z
+  const int NI = g.ni, NJ = g.nj, NK = g.nk;
+  const long Y = g.sy;
+  const int b = (int)blockIdx.x;
+  if (b < nbW) {
+    const long t = (long)b * 256 + threadIdx.x;
+    const int W = NI + 6;
+    if (t >= 2L * W * (NK + 6)) return;
+    const int i = (int)(t % W) - 2;
+    const int kk = (int)(t / W);
+    const int side = kk >= NK + 6 ? 1 : 0;
+    const int k = kk - side * (NK + 6) - 2;
+    const int jw = side ? NJ : 1;
+    auto wco = [&](int ci, int ck) { return (((long)side * (NK + 6) + (ck + 2)) * W + (ci + 2)) * 2; };
+    // u from its source column
+    const int iu = halo_src(i, NI, shu), ku = halo_src(k, NK, 0);
+    const long ou = wco(iu, ku);
+    const double u1 = uk[g.at(iu, jw, ku)];
+    // v, w
+    const int iv = halo_src(i, NI, 0), kv = halo_src(k, NK, 0);
+    const int iw = halo_src(i, NI, 0), kw = halo_src(k, NK, shw);
+    const double w1 = wk[g.at(iw, jw, kw)];
+    const double c2w = wc[wco(iw, kw) + 1];
+    const long cv = g.at(iv, jw, kv);
+    double va, vb, vc = 0.0;
+    if (!side) {
+      va = vk[cv];
+      vb = vk[cv + Y];
+    } else {
+      va = vk[cv - Y];
+      vb = vk[cv - 2 * Y];
+      vc = vk[cv - 3 * Y];
+    }
+    const double c1 = wc[ou], c2 = wc[ou + 1];
+    const long c = g.at(i, jw, k);
+    const long t1 = side ? Y : -Y;
+    const double u0 = c1 * (side ? uwall : -uwall) + c2 * u1;
+    const double um = 2.0 * u0 - u1;
+    uk[c + t1] = u0;
+    uk[c + 2 * t1] = um;
+    uk[c + 3 * t1] = 2.0 * um - u0;
+    const double w0 = c2w * w1;
+    const double wm = 2.0 * w0 - w1;
+    wk[c + t1] = w0;
+    wk[c + 2 * t1] = wm;
+    wk[c + 3 * t1] = 2.0 * wm - w0;
+    if (!side) {  // v(0) = 0, v(-1) = -v(1), v(-2) = -v(2)
+      vk[c - 3 * Y] = -vb;
+      vk[c - 2 * Y] = -va;
+      vk[c - Y] = 0.0;
+    } else {  // v(nj) = 0, v(nj+m) = -v(nj-m)
+      vk[c] = 0.0;
+      vk[c + Y] = -va;
+      vk[c + 2 * Y] = -vb;
+      vk[c + 3 * Y] = -vc;
+    }
+    return;
+  }
+  if (b < nbW + nbX) {
+    const long t = (long)(b - nbW) * 256 + threadIdx.x;
+    const int m = (int)(t & 7);
+    const long task = t >> 3;
+    if (m >= 6 || task >= 3L * NJ * (NK + 6)) return;
+    const int cmp = (int)(task / ((long)NJ * (NK + 6)));
+    const int rem = (int)(task % ((long)NJ * (NK + 6)));
+    const int j = 1 + rem % NJ, k = -2 + rem / NJ;
+    if (cmp == 1 && j == NJ) return;  // a wall row of v
+    const int sx = cmp == 0 ? shu : 0, sz = cmp == 2 ? shw : 0;
+    const int d = halo_dest(m, NI, sx);
+    if (d == kNoHalo) return;
+    double* a = cmp == 0 ? uk : (cmp == 1 ? vk : wk);
+    a[g.at(d, j, k)] = a[g.at(halo_src(d, NI, sx), j, halo_src(k, NK, sz))];
+    return;
+  }
+  const long t = (long)(b - nbW - nbX) * 256 + threadIdx.x;
+  const int i = 1 + (int)(t % (NI + 1));
+  long r = t / (NI + 1);
+  const int m = (int)(r % 6);
+  r /= 6;
+  const int j = 1 + (int)(r % NJ);
+  const int cmp = (int)(r / NJ);
+  if (cmp >= 3 || (cmp == 1 && j == NJ)) return;
+  const int sx = cmp == 0 ? shu : 0, sz = cmp == 2 ? shw : 0;
+  if (halo_src(i, NI, sx) != i) return;  // an x-ghost column: done above
+  const int d = halo_dest(m, NK, sz);
+  if (d == kNoHalo) return;
+  double* a = cmp == 0 ? uk : (cmp == 1 ? vk : wk);
+  a[g.at(i, j, d)] = a[g.at(i, j, halo_src(d, NK, sz))];
 }
 // --- mixed precision: FP32 sweeps on the correction d = un - u ---------------------
 // During the solve un = u + d holds at every point, halos and wall ghosts included:
@@ -719,6 +821,13 @@ void wall_coef(cudaStream_t s, const Grid& g, double dy, const double* l1, const
 
 void wall_halo(cudaStream_t s, const Grid& g, int normal, double uwall, const double* wallc, double* un, double* vn,
                double* wn) {
+  if (refresh_one_pass(g.ni, g.nj, g.nk)) {
+    const long tw = 2L * (g.ni + 6) * (g.nk + 6), tx = 24L * g.nj * (g.nk + 6), tz = 18L * (g.ni + 1) * g.nj;
+    const int nbW = (int)((tw + 255) / 256), nbX = (int)((tx + 255) / 256), nbZ = (int)((tz + 255) / 256);
+    k_refresh<<<nbW + nbX + nbZ, 256, 0, s>>>(g, normal, uwall, wallc, un, vn, wn, nbW, nbX);
+    count_launch();
+    return;
+  }
   k_wall<<<wall_grid(g), kB, 0, s>>>(g, uwall, wallc, un, vn, wn);
   if (g.ni >= 8)
     k_halo_x8<<<(unsigned)((24L * (g.nj + 6) * (g.nk + 6) + 255) / 256), 256, 0, s>>>(g, normal, un, vn, wn);
