@@ -131,9 +131,10 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
-def adjoint_cost(K, stream):
+def adjoint_cost(K, stream, every):
     """Adjoint/forward wall-clock ratio of the K-step rollout on the 128x64x64 Couette
-    workload (per-wall-cell angle 75 +- 5 deg), checkpoints every ceil(sqrt(K)):
+    workload (per-wall-cell angle 75 +- 5 deg), checkpoints every `every` steps (16 for
+    K = 200 as the workload states, about sqrt(K); 0: ceil(sqrt(K))):
     fmf_adj_rollout (J and all gradients) against fmf_adj_forward (J) with the same
     solver settings (viscous solve to the reference's 1e-3, transposed solve to
     1e-6), and against the graph-replayed production step (fmf_ctx_step)."""
@@ -146,10 +147,11 @@ def adjoint_cost(K, stream):
     cfg = C.get("couette128")
     st0 = C.raw_state(cfg)
     walls = [w.copy() for w in C.wall_arrays(cfg)]
-    every = int(math.ceil(math.sqrt(K)))
+    every = every if every > 0 else int(math.ceil(math.sqrt(K)))
     A = Adjoint(cfg, sor_tol=1e-3, sor_max=21, adj_tol=1e-6, adj_max=200)
     A.forward(2, st0, walls)
-    A.rollout(min(K, every), st0, walls, every=every)  # allocates the checkpoint and record slots
+    # allocates the checkpoint and record slots (two segments: the recomputing worker's too)
+    A.rollout(min(K, 2 * every), st0, walls, every=every)
     t0 = time.perf_counter()
     J = A.forward(K, st0, walls)
     t_fwd = time.perf_counter() - t0
@@ -192,6 +194,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--adjoint-steps", type=int, default=200,
                     help="K of the adjoint-cost measurement on 128x64x64 (0: skip)")
+    ap.add_argument("--adjoint-every", type=int, default=16,
+                    help="checkpoint interval of the adjoint rollout (0: ceil(sqrt(K)))")
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed", "adjoint"], help="--profile only")
     ap.add_argument("--profile", action="store_true",
                     help="no timing: start-up pass, --warmup steps, then --steps steps (for ncu launch lists)")
@@ -354,7 +358,7 @@ def main():
                           "pressure FFT+TDMA, projection, divergence, volume sums"}
     adjoint = None
     if rank == 0 and args.adjoint_steps > 0:
-        adjoint = adjoint_cost(args.adjoint_steps, stream)
+        adjoint = adjoint_cost(args.adjoint_steps, stream, args.adjoint_every)
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         v, dt = cpu_baseline_sample(cfg, 1)

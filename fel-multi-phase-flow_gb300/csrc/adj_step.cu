@@ -18,6 +18,7 @@
 #include <cstring>
 #include <map>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/fmf_capi.h"
@@ -123,6 +124,7 @@ struct fmf_adj {
   adj::GraphCache fgraphs;     // forward viscous iterations, one per record slot
   adj::GraphCache rgraphs;     // replays of the last forward viscous cycle, one per record slot
   double* host_norm = nullptr;  // pinned
+  fmf_adj* worker = nullptr;    // recomputes the next segment while this handle reverses one
 };
 
 namespace {
@@ -831,6 +833,7 @@ int fmf_adj_create(const fmf_params* prm, fmf_adj** out) {
 
 int fmf_adj_destroy(fmf_adj* a) {
   if (!a) return 0;
+  if (a->worker) fmf_adj_destroy(a->worker);
   if (a->s) cudaStreamSynchronize(a->s);
   for (double* p : a->ckpt) cudaFree(p);
   for (double* p : a->seg) cudaFree(p);
@@ -871,6 +874,33 @@ int fmf_adj_forward(fmf_adj* a, int K, const double* const* state0, const double
   return take_status();
 }
 
+// The handle that recomputes segment c-1 (on its own stream, scratch set and record
+// slots, from a host thread of its own) while `a` reverses segment c; nullptr where
+// its slots do not fit or FMF_ADJ_SERIAL is set.  The walls are copied from `a`.
+static fmf_adj* overlap_worker(fmf_adj* a, int every) {
+  if (std::getenv("FMF_ADJ_SERIAL")) return nullptr;
+  if (!a->worker && fmf_adj_create(&a->prm, &a->worker) != 0) {
+    a->worker = nullptr;
+    take_status();
+    return nullptr;
+  }
+  fmf_adj* w = a->worker;
+  w->sor_tol = a->sor_tol;
+  w->sor_max = a->sor_max;
+  {
+    Scope sc(w->scr);
+    grow_recs(w, every);
+  }
+  if ((int)w->recs.size() < every) return nullptr;
+  const size_t b = sizeof(double) * a->g.n;
+  const double* src[4] = {a->theta0, a->zeta, a->l1, a->l2};
+  double* dst[4] = {w->theta0, w->zeta, w->l1, w->l2};
+  for (int q = 0; q < 4; ++q) FMF_CUDA(cudaMemcpyAsync(dst[q], src[q], b, cudaMemcpyDeviceToDevice, a->s));
+  FMF_CUDA(cudaStreamSynchronize(a->s));
+  w->sor_total = 0;
+  return get_status() ? nullptr : w;
+}
+
 int fmf_adj_rollout(fmf_adj* a, int K, int every, const double* const* state0, const double* theta0,
                     const double* zeta, const double* l1, const double* l2, double* J, double* g_theta0,
                     double* g_zeta, double* g_l1, double* g_l2, double* g_phi) {
@@ -895,6 +925,7 @@ int fmf_adj_rollout(fmf_adj* a, int K, int every, const double* const* state0, c
   }
   upload_inputs(a, state0, theta0, zeta, l1, l2);
   for (double* p : {a->gtheta0, a->gzeta, a->gl1, a->gl2}) zero(a, p, n);
+  fmf_adj* w = slots && nck > 1 ? overlap_worker(a, every) : nullptr;
   // forward with checkpoints
   init_bc_fwd(a);
   a->sor_total = 0;
@@ -928,7 +959,38 @@ int fmf_adj_rollout(fmf_adj* a, int K, int every, const double* const* state0, c
   // reverse, segment by segment
   for (int c = nck - 1; c >= 0 && !get_status(); --c) {
     const int t0 = c * every, t1 = std::min(K, t0 + every);
-    if (slots) {
+    if (w) {
+      // a->recs holds segment c (recorded during the forward pass or by the worker
+      // in the previous round); the worker records segment c-1 into its own slots
+      double t_rec = 0.0;
+      std::thread th;
+      if (c >= 1) {
+        th = std::thread([a, w, c, every, &t_rec]() {
+          Scope sc(w->scr);
+          const clk::time_point ta = clk::now();
+          const int u0 = (c - 1) * every;
+          load_state(w, a->ckpt[c - 1]);
+          for (int t = u0; t < u0 + every && !get_status(); ++t) {
+            set_rec(w, w->recs[t - u0]);
+            save_state(w, w->recs[t - u0].state);
+            record_step(w);
+          }
+          FMF_CUDA(cudaStreamSynchronize(w->s));
+          t_rec = std::chrono::duration<double>(clk::now() - ta).count();
+        });
+      }
+      for (int t = t1 - 1; t >= t0 && !get_status(); --t) {
+        set_rec(a, a->recs[t - t0]);
+        reverse_step(a, a->recs[t - t0].state);
+      }
+      a->t_phase[2] += lap(tp);
+      if (th.joinable()) {
+        th.join();
+        a->t_phase[1] += t_rec;  // overlapped with the reverse steps above
+        a->t_phase[2] += lap(tp);  // the wait for the worker, if it finished last
+        std::swap(a->recs, w->recs);
+      }
+    } else if (slots) {
       if (c != nck - 1) {
         load_state(a, a->ckpt[c]);
         for (int t = t0; t < t1; ++t) {
@@ -960,6 +1022,7 @@ int fmf_adj_rollout(fmf_adj* a, int K, int every, const double* const* state0, c
       }
     }
   }
+  if (w) a->sor_total += w->sor_total;
   set_rec(a, a->recs[0]);
   // the start-up pass: recompute its record from the uploaded state
   for (int f = 0; f < NSTATE; ++f)

@@ -1,5 +1,6 @@
 // runtime.cu -- library runtime: status, stream, scratch, and the host-array
 // registry that mirrors the caller's arrays in HBM.
+#include <atomic>
 #include <map>
 #include <mutex>
 #include <vector>
@@ -8,8 +9,9 @@
 
 namespace fmf {
 
-static int g_status = 0;
-static long long g_launches = 0;
+// atomic: the adjoint rollout runs a second host thread
+static std::atomic<int> g_status{0};
+static std::atomic<long long> g_launches{0};
 static cudaStream_t g_stream = nullptr;
 static bool g_own_stream = false;
 static int g_mode = 0;  // FMF_RESIDENT
@@ -18,11 +20,7 @@ void set_status(int code) {
   if (code != 0) g_status = code;
 }
 int get_status() { return g_status; }
-int take_status() {
-  const int s = g_status;
-  g_status = 0;
-  return s;
-}
+int take_status() { return g_status.exchange(0); }
 bool cuda_ok(cudaError_t e, const char* where) {
   if (e == cudaSuccess) return true;
   std::fprintf(stderr, "fmf: CUDA error %s (%s) at %s\n", cudaGetErrorName(e), cudaGetErrorString(e), where);
