@@ -749,7 +749,11 @@ int fmf_adj_create(const fmf_params* prm, fmf_adj** out) {
   a->prm = *prm;
   a->g = Grid(prm->ni, prm->nj, prm->nk);
   a->scr = scratch_set_create();
-  if (!FMF_CUDA(cudaStreamCreateWithFlags(&a->s, cudaStreamNonBlocking))) {
+  // the highest stream priority: the reverse steps are the critical path when a
+  // worker recomputes the next segment beside them (the worker runs at the lowest)
+  int least = 0, greatest = 0;
+  FMF_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+  if (!FMF_CUDA(cudaStreamCreateWithPriority(&a->s, cudaStreamNonBlocking, greatest))) {
     delete a;
     return FMF_ERR_CUDA;
   }
@@ -879,10 +883,22 @@ int fmf_adj_forward(fmf_adj* a, int K, const double* const* state0, const double
 // its slots do not fit or FMF_ADJ_SERIAL is set.  The walls are copied from `a`.
 static fmf_adj* overlap_worker(fmf_adj* a, int every) {
   if (std::getenv("FMF_ADJ_SERIAL")) return nullptr;
-  if (!a->worker && fmf_adj_create(&a->prm, &a->worker) != 0) {
-    a->worker = nullptr;
-    take_status();
-    return nullptr;
+  if (!a->worker) {
+    if (fmf_adj_create(&a->prm, &a->worker) != 0) {
+      a->worker = nullptr;
+      take_status();
+      return nullptr;
+    }
+    // the worker's stream at the lowest priority: it fills what the reverse leaves idle
+    fmf_adj* w = a->worker;
+    int least = 0, greatest = 0;
+    cudaStream_t ls = nullptr;
+    if (FMF_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest)) &&
+        FMF_CUDA(cudaStreamCreateWithPriority(&ls, cudaStreamNonBlocking, least))) {
+      FMF_CUDA(cudaStreamSynchronize(w->s));
+      FMF_CUDA(cudaStreamDestroy(w->s));
+      w->s = ls;
+    }
   }
   fmf_adj* w = a->worker;
   w->sor_tol = a->sor_tol;
