@@ -131,6 +131,53 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def mixed_case(name, steps, warmup, stream):
+    """FP64 and mixed-precision steps on one workload: CUDA-event time per step of
+    each (inputs resident, steps after `warmup`), and the per-field error of the mixed
+    state against the FP64 state after the same warmup + steps from the same initial
+    state."""
+    import numpy as np
+    import torch
+
+    from fmf import capi
+    from fmf import config as C
+
+    cfg = C.get(name)
+    out = {"workload": f"{name} {cfg.ni}x{cfg.nj}x{cfg.nk}", "steps": steps, "warmup": warmup}
+    states = {}
+    st = None
+    for prec, key in ((capi.FMF_FP64, "fp64"), (capi.FMF_MIXED, "mixed")):
+        g = capi.Stepper(cfg, precision=prec, stream=stream.cuda_stream)
+        if st is None:
+            st = g.initial_state()  # after the start-up boundary pass; the mixed run starts from it too
+        else:
+            g.upload(st)
+        g.step(warmup)
+        g.sync()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        g.step(steps)
+        e1.record(stream)
+        e1.synchronize()
+        out[key + "_ms_per_step"] = e0.elapsed_time(e1) / steps
+        states[key] = g.get_state()
+        g.close()
+    ref, mix = states["fp64"], states["mixed"]
+
+    def rel(f):
+        a, b = C.interior(mix[f]), C.interior(ref[f])
+        return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))
+
+    out["value_fp64"] = cfg.cells / (out["fp64_ms_per_step"] * 1e-3)
+    out["value_mixed"] = cfg.cells / (out["mixed_ms_per_step"] * 1e-3)
+    out["unit"] = UNIT
+    out["speedup_vs_fp64"] = out["fp64_ms_per_step"] / out["mixed_ms_per_step"]
+    out["steps_compared"] = warmup + steps
+    out["max_rel_err_vs_fp64"] = {"phi": rel(9), "u": rel(0), "v": rel(1), "w": rel(2), "p": rel(6)}
+    return out
+
+
 def adjoint_cost(K, stream, every):
     """Adjoint/forward wall-clock ratio of the K-step rollout on the 128x64x64 Couette
     workload (per-wall-cell angle 75 +- 5 deg), checkpoints every `every` steps (16 for
@@ -194,6 +241,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--adjoint-steps", type=int, default=200,
                     help="K of the adjoint-cost measurement on 128x64x64 (0: skip)")
+    ap.add_argument("--mixed-workload", default="droplet512",
+                    help="second FP64-vs-mixed measurement (the sessile-drop workload; '' to skip)")
     ap.add_argument("--adjoint-every", type=int, default=16,
                     help="checkpoint interval of the adjoint rollout (0: ceil(sqrt(K)))")
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed", "adjoint"], help="--profile only")
@@ -356,6 +405,10 @@ def main():
              "precision": "fp32: WENO5, MTHINC Newton + Gauss-point fluxes, CSF normals and curvature, viscous "
                           "sweeps on FP32 corrections (FP64 residual, one refinement step); fp64: state, "
                           "pressure FFT+TDMA, projection, divergence, volume sums"}
+    mixed_droplet = None
+    if rank == 0 and args.mixed_workload:
+        g.close()
+        mixed_droplet = mixed_case(args.mixed_workload, 5, 3, stream)
     adjoint = None
     if rank == 0 and args.adjoint_steps > 0:
         adjoint = adjoint_cost(args.adjoint_steps, stream, args.adjoint_every)
@@ -376,7 +429,7 @@ def main():
                 "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 12 * bytes_field,
                         "d2h_bytes_per_step": 12 * bytes_field},
                 "gpu_launches": int(launches), "clocks": clk, "roofline": roofline, "cpu_baseline": cpu,
-                "mixed": mixed, "adjoint": adjoint}
+                "mixed": mixed, "mixed_droplet": mixed_droplet, "adjoint": adjoint}
         print(json.dumps(line), flush=True)
     g.close()
 

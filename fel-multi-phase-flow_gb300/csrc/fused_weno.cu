@@ -56,7 +56,11 @@ __device__ __forceinline__ double wdir(const double* __restrict__ q, long c, lon
 // the five differences are divided by their largest magnitude s first (the
 // weights are unchanged by a common scale; the sum is multiplied back by s), and
 // the reference's additive 1e-80 becomes 1e-80/s^8 in scaled units, evaluated as a
-// power of two and clamped to the float range.
+// power of two and clamped to [2^-126, 2^127].  The lower clamp is the smallest
+// normal float: where all three smoothness indicators are 0 (data exactly linear
+// in float) the denominator is that term alone and its reciprocal must stay finite
+// (2^-149 gave 1/e = inf and 0 * inf = NaN); the weights are then 0, 1, 0 as in
+// the reference's limit.
 __device__ __forceinline__ float weno_side_f32(float a5, float a3, float a1, float b1, float b3) {
   const float s = fmaxf(fmaxf(fmaxf(fabsf(a5), fabsf(a3)), fmaxf(fabsf(a1), fabsf(b1))), fabsf(b3));
   if (s == 0.0f) return 0.0f;
@@ -82,7 +86,7 @@ __device__ __forceinline__ float weno_side_f32(float a5, float a3, float a1, flo
   m2 = m2 * m2 * 6.0f;
   m3 = m3 * m3 * 3.0f;
   // 1e-80 / s^8 = 2^(log2(1e-80) - 8 log2 s)
-  const float e = exp2f(fminf(fmaxf(-265.754f - 8.0f * log2f(s), -149.0f), 127.0f));
+  const float e = exp2f(fminf(fmaxf(-265.754f - 8.0f * log2f(s), -126.0f), 127.0f));
   const float inv = 1.0f / (m1 + m2 + m3 + e);
   const float w1 = m1 * inv, w3 = m3 * inv;
   const float w2 = 1.0f - w1 - w3;
