@@ -28,7 +28,10 @@ def _relerr(a, b):
     return np.abs(C.interior(a) - C.interior(b)).max() / max(np.abs(C.interior(b)).max(), 1e-30)
 
 
-@pytest.mark.parametrize("name,shape,steps", [("couette256", (128, 64, 64), 20), ("droplet256", (64, 32, 32), 10)])
+# the full 256x128x128 Couette case for 30 steps: its linear velocity profile makes
+# all three FP32 smoothness indicators of some lines exactly 0 (first at step 15)
+@pytest.mark.parametrize("name,shape,steps", [("couette256", (128, 64, 64), 20), ("couette256", (256, 128, 128), 30),
+                                              ("droplet256", (64, 32, 32), 10)])
 def test_mixed_matches_fp64(fmf_lib, name, shape, steps):
     cfg = C.get(name, ni=shape[0], nj=shape[1], nk=shape[2])
     g = capi.Stepper(cfg)
