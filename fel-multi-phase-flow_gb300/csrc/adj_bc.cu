@@ -322,16 +322,22 @@ __device__ __forceinline__ double wall_col_T(const Grid& G, double* __restrict__
   const bool hx = ix != kNoHalo, hz = kz != kNoHalo;
   const long c0 = G.at(i, j0, k), cx = hx ? G.at(ix, j0, k) : c0, cz = hz ? G.at(i, j0, kz) : c0,
              cxz = hx && hz ? G.at(ix, j0, kz) : c0;
-  double gv[NR], vx[NR], vz[NR], vxz[NR];
+  double gv[NR];
 #pragma unroll
-  for (int r = 0; r < NR; ++r) {
-    gv[r] = a[c0 + r * Y];
-    vx[r] = hx ? a[cx + r * Y] : 0.0;
-    vz[r] = hz ? a[cz + r * Y] : 0.0;
-    vxz[r] = hx && hz ? a[cxz + r * Y] : 0.0;
+  for (int r = 0; r < NR; ++r) gv[r] = a[c0 + r * Y];
+  // the images one column at a time (most source columns have none): few registers
+  // live, which keeps the occupancy of the whole kernel up
+#pragma unroll 1
+  for (int q = 0; q < 3; ++q) {
+    const bool has = q == 0 ? hx : (q == 1 ? hz : hx && hz);
+    if (!has) continue;
+    const long ci = q == 0 ? cx : (q == 1 ? cz : cxz);
+    double v[NR];
+#pragma unroll
+    for (int r = 0; r < NR; ++r) v[r] = a[ci + r * Y];
+#pragma unroll
+    for (int r = 0; r < NR; ++r) gv[r] += v[r];
   }
-#pragma unroll
-  for (int r = 0; r < NR; ++r) gv[r] += vx[r] + vz[r] + vxz[r];
   double S = 0.0;
   if (cmp != 1) {  // u, w: the wall row is r = 3 (j = 1 or nj), its ghosts on the far side
     constexpr int t1 = SIDE ? 1 : -1;
