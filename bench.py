@@ -54,12 +54,13 @@ class Clocks:
 
     def __init__(self):
         self.p = None
-        self.path = os.path.join(REPO, "gpurun_out", "clocks_bench.csv")
+        self.path = None
 
     def start(self):
         try:
-            os.makedirs(os.path.dirname(self.path), exist_ok=True)
-            self.f = open(self.path, "w")
+            import tempfile
+            fd, self.path = tempfile.mkstemp(prefix="fmf_clocks_", suffix=".csv")
+            self.f = os.fdopen(fd, "w")
             self.p = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
                                        "-lms", "200", "-i", os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0]],
                                       stdout=self.f, stderr=subprocess.DEVNULL)
@@ -86,6 +87,10 @@ class Clocks:
             for nm, val in zip(names, parts[5:9]):
                 if val.lower() == "active":
                     reasons.add(nm)
+        try:
+            os.remove(self.path)
+        except OSError:
+            pass
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
                 "reasons": sorted(reasons), "samples": len(sm)}
 
