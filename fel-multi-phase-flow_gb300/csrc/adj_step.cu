@@ -977,7 +977,7 @@ int fmf_adj_rollout(fmf_adj* a, int K, int every, const double* const* state0, c
     const int t0 = c * every, t1 = std::min(K, t0 + every);
     if (w) {
       // a->recs holds segment c (recorded during the forward pass or by the worker
-      // in the previous round); the worker records segment c-1 into its own slots
+      // in the previous iteration); the worker records segment c-1 into its own slots
       double t_rec = 0.0;
       std::thread th;
       if (c >= 1) {
