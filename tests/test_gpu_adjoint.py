@@ -137,6 +137,21 @@ def test_checkpoint_interval_does_not_change_gradient(setup):
         assert np.abs(a - c).max() <= 1e-10 * scale
 
 
+def test_overlapped_recomputation_matches_serial(setup, monkeypatch):
+    """Segments recomputed by the second handle beside the reverse steps (the default)
+    and recomputed in line (FMF_ADJ_SERIAL) give the same J and gradients."""
+    cfg, adj, st0, walls, J, grads = setup
+    Jo, go = adj.rollout(K, st0, walls, every=2)
+    monkeypatch.setenv("FMF_ADJ_SERIAL", "1")
+    Js, gs = adj.rollout(K, st0, walls, every=2)
+    monkeypatch.delenv("FMF_ADJ_SERIAL")
+    assert Jo == J and Js == J
+    for a, b, c in zip(grads, go, gs):
+        scale = max(np.abs(a).max(), 1e-300)
+        assert np.abs(b - c).max() <= 1e-10 * scale
+        assert np.abs(a - b).max() <= 1e-10 * scale
+
+
 def test_torch_autograd_function(setup):
     torch = pytest.importorskip("torch")
     from fmf.adjoint import rollout_function
