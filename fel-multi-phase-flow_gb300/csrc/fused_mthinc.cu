@@ -48,6 +48,38 @@ __device__ __forceinline__ R sig8(const R* a, R w, R m2b, R d, R* sd) {
   if (sd) *sd = q;
   return w * s;
 }
+// The same sums with exp(m2b (a_t + d)) factorised: a_t = x + y + z over the Gauss
+// offsets of the three axes, so exp(m2b a_t) = X Y Z of per-axis factors (E_t,
+// gexp8) and only exp(m2b d) changes with d.  Every factor is bounded by the
+// normal's unit length times the Gauss offsets; where exp(m2b d) overflows or
+// underflows, so does the unfactorised exponential.  Six exponentials per cell
+// and one per Newton step instead of eight per step.
+template <class R>
+__device__ __forceinline__ R sig8f(const R* E, R w, R ed, R* sd) {
+  R s = 0, q = 0;
+#pragma unroll
+  for (int t = 0; t < 8; ++t) {
+    const R e = E[t] * ed;
+    const R r = (R)1 / ((R)1 + e);
+    s += r;
+    if (sd) q += e * r * r;
+  }
+  if (sd) *sd = q;
+  return w * s;
+}
+// E_t in gauss8's order (x fastest): factors X1 X2, Y1 Y2, Z1 Z2
+template <class R>
+__device__ __forceinline__ void gexp8(R* E, R X1, R X2, R Y1, R Y2, R Z1, R Z2) {
+  const R a = X1 * Y1, b = X2 * Y1, c = X1 * Y2, d = X2 * Y2;
+  E[0] = a * Z1;
+  E[1] = b * Z1;
+  E[2] = c * Z1;
+  E[3] = d * Z1;
+  E[4] = a * Z2;
+  E[5] = b * Z2;
+  E[6] = c * Z2;
+  E[7] = d * Z2;
+}
 template <class R>
 __device__ __forceinline__ void gauss8(R* a, R rnx, R rny, R rnz, R x1g, R x2g, R y1g, R y2g, R z1g, R z2g) {
   const R x1 = rnx * x1g, x2 = rnx * x2g, y1 = rny * y1g, y2 = rny * y2g, z1 = rnz * z1g, z2 = rnz * z2g;
@@ -130,22 +162,28 @@ __global__ void __launch_bounds__(128) k_band(Grid g, MC m, const double* __rest
     const double q00 = sqrt(nx * nx + ny * ny + nz * nz);
     const double coef = 1.0 / q00;
     const R rnx = (R)(nx * coef), rny = (R)(ny * coef), rnz = (R)(nz * coef);
-    R a[8];
-    gauss8<R>(a, rnx, rny, rnz, gp1, gp2, gp1, gp2, gp1, gp2);
+    // per-axis factors exp(m2b n gp) of the centred Gauss points
+    const R X1 = ex(m2b * rnx * gp1), X2 = ex(m2b * rnx * gp2), Y1 = ex(m2b * rny * gp1),
+            Y2 = ex(m2b * rny * gp2), Z1 = ex(m2b * rnz * gp1), Z2 = ex(m2b * rnz * gp2);
+    R E[8];
+    gexp8<R>(E, X1, X2, Y1, Y2, Z1, Z2);
     const R ph = (R)__ldg(phi + c);
     R ddd = 0, step = 0;
 #pragma unroll 1
     for (int it = 0; it < 10; ++it) {
       R sd;
-      const R f = sig8<R>(a, (R)0.125, m2b, ddd, &sd) - ph;
+      const R f = sig8f<R>(E, (R)0.125, ex(m2b * ddd), &sd) - ph;
       // df = 0.5 bet sum 0.125/cosh^2 = 0.5 bet * 0.125 * 4 * sum s(1-s)
       const R df = (R)0.25 * bet * sd;
       step = f * df / (df * df + reg);
       const R dn = ddd - step;
       // once d no longer changes, every remaining iteration recomputes the same
-      // f, df and step: stopping here is the ten-step result bit for bit
+      // f, df and step: stopping here is the ten-step result bit for bit.  In
+      // float the iterate can dither in its last bit instead; there a step below
+      // float precision ends the loop.
       if (dn == ddd) break;
       ddd = dn;
+      if (sizeof(R) == 4 && fabs((double)step) <= 1.0e-7 * (1.0 + fabs((double)ddd))) break;
     }
     if (newton) {
       newton[e] = (double)ddd;
@@ -153,15 +191,17 @@ __global__ void __launch_bounds__(128) k_band(Grid g, MC m, const double* __rest
     }
     const double uw = __ldg(u + c - X), ue = __ldg(u + c), vs = __ldg(v + c - Y), vn = __ldg(v + c),
                  wb = __ldg(w + c - Z), wt = __ldg(w + c);
+    const R edf = ex(m2b * ddd);  // exp(m2b d) at the offset found
     auto side = [&](double vel, double dinv, int axis, bool minus, double* out) {
       const R vd = (R)vel * dtt * (R)dinv;
       const R st = minus ? (R)-0.5 : (R)0.5 - vd, en = minus ? (R)-0.5 - vd : (R)0.5;
       const R g1 = (st + en) * (R)0.5 + (-st + en) * gp1, g2 = (st + en) * (R)0.5 + (-st + en) * gp2;
-      R b[8];
-      if (axis == 0) gauss8<R>(b, rnx, rny, rnz, g1, g2, gp1, gp2, gp1, gp2);
-      else if (axis == 1) gauss8<R>(b, rnx, rny, rnz, gp1, gp2, g1, g2, gp1, gp2);
-      else gauss8<R>(b, rnx, rny, rnz, gp1, gp2, gp1, gp2, g1, g2);
-      *out = (double)sig8<R>(b, (R)0.125 * vd, m2b, ddd, nullptr);
+      // the flux axis takes the swept interval's Gauss points, the others the centred ones
+      R Eb[8];
+      if (axis == 0) gexp8<R>(Eb, ex(m2b * rnx * g1), ex(m2b * rnx * g2), Y1, Y2, Z1, Z2);
+      else if (axis == 1) gexp8<R>(Eb, X1, X2, ex(m2b * rny * g1), ex(m2b * rny * g2), Z1, Z2);
+      else gexp8<R>(Eb, X1, X2, Y1, Y2, ex(m2b * rnz * g1), ex(m2b * rnz * g2));
+      *out = (double)sig8f<R>(Eb, (R)0.125 * vd, edf, nullptr);
     };
     if (uw < 0.0) side(uw, m.dxi, 0, true, fx + c - X);
     if (ue > 0.0) side(ue, m.dxi, 0, false, fx + c);
