@@ -1,10 +1,12 @@
 // adj_transport.cu -- adjoints of the MTHINC transport (solphi_mthinc1/2/3).
 //
-// solphi_mthinc1: a band cell's Newton offset d(n, phi) is differentiated through
-// the ten iterations the forward pass runs (forward-mode numbers seeded with the
-// unit normal and phi), and each outflow-face flux through its 8-point Gauss sum
-// (seeded with n, d and the swept fraction vd).  Bulk cells: flux = u phi00 dt/dx
-// with phi00 snapped (zero derivative) inside eps_trunc of 0 or 1.
+// solphi_mthinc1: a band cell's Newton offset d(n, phi) is differentiated at its
+// root where the forward pass's iteration converged (implicit function: the
+// derivatives of the 8-point Gauss sum by hand), else through the ten iterations
+// (forward-mode numbers seeded with the unit normal and phi); each outflow-face
+// flux through its 8-point Gauss sum by hand (with respect to n, d and the swept
+// fraction vd).  Bulk cells: flux = u phi00 dt/dx with phi00 snapped (zero
+// derivative) inside eps_trunc of 0 or 1.
 #include "adj.cuh"
 #include "ops.cuh"
 
@@ -86,32 +88,43 @@ __device__ T newton_d(const T& nx, const T& ny, const T& nz, const T& ph, const 
   }
   return d;
 }
-// flux through one outflow face: dir 0/1/2, side 0 = the lower face (velocity < 0),
-// side 1 = the upper face (velocity > 0)
-template <class T>
-__device__ T face_flux(int dir, int side, const T& nx, const T& ny, const T& nz, const T& d, const T& vd,
-                       const MC& M, double bet) {
-  T st, en;
-  if (side == 0) {
-    st = T(-0.5);
-    en = -0.5 - vd;
-  } else {
-    st = 0.5 - vd;
-    en = T(0.5);
-  }
-  const T a1 = (st + en) * 0.5 + (-st + en) * M.gp1, a2 = (st + en) * 0.5 + (-st + en) * M.gp2;
-  const T g1(M.gp1), g2(M.gp2);
-  T a[8];
-  if (dir == 0) gauss8(nx, ny, nz, a1, a2, g1, g2, g1, g2, a);
-  else if (dir == 1) gauss8(nx, ny, nz, g1, g2, a1, a2, g1, g2, a);
-  else gauss8(nx, ny, nz, g1, g2, g1, g2, a1, a2, a);
-  return sig8(a, vd * 0.125, bet, d);
-}
 }  // namespace
 
 namespace {
+// Logistic sums over the 8 Gauss points with the exponentials factorised: point t
+// (gauss8's order, x index fastest) has z_t = m (x_i + y_j + z_k + d), and with the
+// per-axis factors eX[i] = exp(m n_x p_x[i]) (likewise y, z) and ed = exp(m d),
+// e_t = exp(z_t) = eX[i] eY[j] eZ[k] ed.  s_t = 1/(1 + e_t) and ds_t = ds/dz =
+// -e_t s_t^2 (both 0 where e_t overflows, as sigw takes them).  Returns the sum of
+// s_t and, per axis and Gauss index, the sum of ds_t over the points with it.
+struct GSums {
+  double s, sx[2], sy[2], sz[2];
+};
+__device__ __forceinline__ GSums gsums(const double* eX, const double* eY, const double* eZ, double ed) {
+  GSums G = {0.0, {0.0, 0.0}, {0.0, 0.0}, {0.0, 0.0}};
+#pragma unroll
+  for (int k = 0; k < 2; ++k)
+#pragma unroll
+    for (int j = 0; j < 2; ++j)
+#pragma unroll
+      for (int i = 0; i < 2; ++i) {
+        const double e = eX[i] * eY[j] * eZ[k] * ed;
+        double r = 0.0, ds = 0.0;
+        if (e < INFINITY) {
+          r = 1.0 / (1.0 + e);
+          ds = -(e * r) * r;
+        }
+        G.s += r;
+        G.sx[i] += ds;
+        G.sy[j] += ds;
+        G.sz[k] += ds;
+      }
+  return G;
+}
+
 // band cells (the compact list of the forward pass's k_classify): the Newton offset
-// and the outflow-face fluxes, differentiated with forward-mode numbers
+// and the outflow-face fluxes, differentiated by hand (analytic derivatives of the
+// Gauss-point sums); the offsets that did not converge through forward-mode numbers
 __global__ void __launch_bounds__(128) k_band_T(Grid g, MC M, double sx, double sy, double sz, double bet,
                                                 const double* __restrict__ phi, const double* __restrict__ gx,
                                                 const double* __restrict__ gy, const double* __restrict__ gz,
@@ -145,6 +158,11 @@ __global__ void __launch_bounds__(128) k_band_T(Grid g, MC M, double sx, double 
     const double nx = rnx * coef, ny = rny * coef, nz = rnz * coef;
     using D4 = Dual<4>;
     D4 dd;
+    // per-axis factors of the centred Gauss points (m = -2 bet)
+    const double mb = -2.0 * bet;
+    const double eX[2] = {exp(mb * nx * M.gp1), exp(mb * nx * M.gp2)},
+                 eY[2] = {exp(mb * ny * M.gp1), exp(mb * ny * M.gp2)},
+                 eZ[2] = {exp(mb * nz * M.gp1), exp(mb * nz * M.gp2)};
     {
       // d and the last of the forward pass's ten Newton steps (recorded per list
       // entry); where that step moved d by less than 1e-13 (1 + |d|) the iteration
@@ -152,31 +170,47 @@ __global__ void __launch_bounds__(128) k_band_T(Grid g, MC M, double sx, double 
       // the derivatives are carried through the ten steps
       const double dv = newton[e], last = newton[cap + e];
       if (fabs(last) <= 1.0e-13 * (1.0 + fabs(dv))) {
-        using D5 = Dual<5>;
-        D5 a[8];
-        const D5 g1(M.gp1), g2(M.gp2);
-        gauss8(D5::var(nx, 0), D5::var(ny, 1), D5::var(nz, 2), g1, g2, g1, g2, g1, g2, a);
-        const D5 F = sig8(a, D5(0.125), bet, D5::var(dv, 4)) - D5::var(phi[c], 3);
+        // F = 0.125 sum s_t - phi: F_d = 0.125 m sum ds, F_n = 0.125 m sum ds p_n, F_phi = -1
+        const GSums S = gsums(eX, eY, eZ, exp(mb * dv));
+        const double Fd = 0.125 * mb * (S.sx[0] + S.sx[1]);
         dd.v = dv;
-        for (int q = 0; q < 4; ++q) dd.d[q] = -F.d[q] / F.d[4];
+        dd.d[0] = -0.125 * mb * (S.sx[0] * M.gp1 + S.sx[1] * M.gp2) / Fd;
+        dd.d[1] = -0.125 * mb * (S.sy[0] * M.gp1 + S.sy[1] * M.gp2) / Fd;
+        dd.d[2] = -0.125 * mb * (S.sz[0] * M.gp1 + S.sz[1] * M.gp2) / Fd;
+        dd.d[3] = 1.0 / Fd;
       } else {
         dd = newton_d(D4::var(nx, 0), D4::var(ny, 1), D4::var(nz, 2), D4::var(phi[c], 3), M, bet);
       }
     }
     double ln[3] = {0.0, 0.0, 0.0}, ld = 0.0;
-    using D5 = Dual<5>;
+    const double edf = exp(mb * dd.v);
     for (int f = 0; f < 6; ++f) {
       const bool own = (f & 1) ? (U[f] > 0.0) : (U[f] < 0.0);
       if (!own || L[f] == 0.0) continue;
+      const int dir = f / 2, side = f & 1;
       const double sc = f < 2 ? sx : (f < 4 ? sy : sz);
-      const D5 fl = face_flux(f / 2, f & 1, D5::var(nx, 0), D5::var(ny, 1), D5::var(nz, 2), D5::var(dd.v, 3),
-                              D5::var(U[f] * sc, 4), M, bet);
-      ln[0] += L[f] * fl.d[0];
-      ln[1] += L[f] * fl.d[1];
-      ln[2] += L[f] * fl.d[2];
-      ld += L[f] * fl.d[3];
-      const long o = (f & 1) ? c : c - (f < 2 ? X : (f < 4 ? Y : Z));
-      aadd((f < 2 ? lu : (f < 4 ? lv : lw)) + o, L[f] * fl.d[4] * sc);
+      const double vd = U[f] * sc;
+      // face_flux: the flux axis's Gauss points over the swept interval [st, en]
+      const double st = side ? 0.5 - vd : -0.5, en = side ? 0.5 : -0.5 - vd;
+      const double pf[2] = {(st + en) * 0.5 + (-st + en) * M.gp1, (st + en) * 0.5 + (-st + en) * M.gp2};
+      const double dpf[2] = {side ? -0.5 + M.gp1 : -0.5 - M.gp1, side ? -0.5 + M.gp2 : -0.5 - M.gp2};  // d pf / d vd
+      const double nd = dir == 0 ? nx : (dir == 1 ? ny : nz);
+      const double eF[2] = {exp(mb * nd * pf[0]), exp(mb * nd * pf[1])};
+      const GSums S = gsums(dir == 0 ? eF : eX, dir == 1 ? eF : eY, dir == 2 ? eF : eZ, edf);
+      // flux = w sum s_t (w = vd/8): d/dd = w m sum ds; d/dn_a = w m sum ds p_a;
+      // d/dvd = sum s / 8 + w m n_dir sum ds dp_dir/dvd
+      const double wm = 0.125 * vd * mb, Lf = L[f];
+      const double px0 = dir == 0 ? pf[0] : M.gp1, px1 = dir == 0 ? pf[1] : M.gp2;
+      const double py0 = dir == 1 ? pf[0] : M.gp1, py1 = dir == 1 ? pf[1] : M.gp2;
+      const double pz0 = dir == 2 ? pf[0] : M.gp1, pz1 = dir == 2 ? pf[1] : M.gp2;
+      ln[0] += Lf * wm * (S.sx[0] * px0 + S.sx[1] * px1);
+      ln[1] += Lf * wm * (S.sy[0] * py0 + S.sy[1] * py1);
+      ln[2] += Lf * wm * (S.sz[0] * pz0 + S.sz[1] * pz1);
+      ld += Lf * wm * (S.sx[0] + S.sx[1]);
+      const double* sF = dir == 0 ? S.sx : (dir == 1 ? S.sy : S.sz);
+      const double lvd = 0.125 * S.s + wm * nd * (sF[0] * dpf[0] + sF[1] * dpf[1]);
+      const long o = side ? c : c - (dir == 0 ? X : (dir == 1 ? Y : Z));
+      aadd((dir == 0 ? lu : (dir == 1 ? lv : lw)) + o, Lf * lvd * sc);
     }
     for (int q = 0; q < 3; ++q) ln[q] += ld * dd.d[q];
     aadd(lphi + c, ld * dd.d[3]);
