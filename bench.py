@@ -293,8 +293,9 @@ def main():
     from fmf import capi
     from fmf import config as C
 
-    rank = int(os.environ.get("RANK", "0"))
-    world = int(os.environ.get("WORLD_SIZE", "1"))
+    from fmf import replicas
+
+    rank, world = replicas.world()
     local = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(local)
     if world > 1:
@@ -311,8 +312,7 @@ def main():
 
     def barrier():
         torch.cuda.synchronize()
-        if world > 1:
-            torch.distributed.barrier()
+        replicas.barrier()
 
     clocks = Clocks()
     barrier()
@@ -329,11 +329,8 @@ def main():
     barrier()
     clk = clocks.stop()
     iters = g.sor_iterations()
-    if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
-    value = world * cfg.cells * args.steps / (ms * 1e-3)
+    ms = replicas.max_over_ranks(ms)
+    value = replicas.throughput(cfg.cells, args.steps, ms * 1e-3)
 
     # e2e: host buffers through the C-ABI, upload + step + download every step
     pinned = torch.empty((12,) + cfg.shape, dtype=torch.float64, pin_memory=True)
@@ -348,8 +345,8 @@ def main():
         g.step(1)
         g.download(host)
         g.sync()
-    e2e_dt = time.perf_counter() - t0
-    e2e_value = world * cfg.cells * e2e_steps / e2e_dt
+    e2e_dt = replicas.max_over_ranks(time.perf_counter() - t0)
+    e2e_value = replicas.throughput(cfg.cells, e2e_steps, e2e_dt)
 
     # Dominant kernel: WENO5 advection of both velocity levels (k_weno2, stage 0),
     # FP64-ALU bound.  Algorithmic work per cell = the reference formula of weno5.h
@@ -386,7 +383,7 @@ def main():
     gm.step(args.steps)
     e1.record(stream)
     e1.synchronize()
-    ms_mixed = e0.elapsed_time(e1)
+    ms_mixed = replicas.max_over_ranks(e0.elapsed_time(e1))
     n_err = args.warmup + args.steps
     g.upload(st)
     g.step(n_err)
@@ -402,7 +399,7 @@ def main():
         a, b = C.interior(mix[f]), C.interior(ref[f])
         return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))
 
-    mixed = {"value": world * cfg.cells * args.steps / (ms_mixed * 1e-3), "unit": UNIT,
+    mixed = {"value": replicas.throughput(cfg.cells, args.steps, ms_mixed * 1e-3), "unit": UNIT,
              "ms_per_step": ms_mixed / args.steps, "speedup_vs_fp64": ms / ms_mixed,
              "steps_compared": n_err,
              "max_rel_err_vs_fp64": {"phi": rel(9), "u": rel(0), "v": rel(1), "w": rel(2), "p": rel(6)},
