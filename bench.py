@@ -29,10 +29,14 @@ sys.path.insert(0, os.path.join(REPO, "fel-multi-phase-flow_gb300"))
 sys.path.insert(0, os.path.join(REPO, "oracle"))
 
 WORKLOAD = "couette256"
-# DRAM bytes (read + write) per interior cell of one k_weno2 launch, from the ncu
-# capture summarised in profiles/k_weno2_couette256.md (230.8 MB + 174.2 MB over
-# 4,194,304 cells); scaled to the workload by its cell count
-WENO_TRAFFIC_PER_CELL = (230.801920e6 + 174.222848e6) / 4194304
+# Per interior cell of one k_weno2 launch, from the ncu capture summarised in
+# profiles/k_weno2_couette256.md (4,194,304 cells): DRAM bytes read + written
+# (228.9 MB + 173.4 MB), and the executed FP64 instructions (DADD 955.7 M, DMUL
+# 1219.5 M, DFMA 1885.8 M thread instructions); scaled to the workload by its cell
+# count
+WENO_TRAFFIC_PER_CELL = (228.919040e6 + 173.449216e6) / 4194304
+WENO_FP64_INST_PER_CELL = (955711488 + 1219493888 + 1885798400) / 4194304
+WENO_FP64_FLOPS_PER_CELL = (955711488 + 1219493888 + 2 * 1885798400) / 4194304
 METRIC = "cell-updates/s/step plain FP64 vs mixed at stated error; adjoint/forward cost"
 UNIT = "cell-updates/s"
 
@@ -349,12 +353,15 @@ def main():
     e2e_value = replicas.throughput(cfg.cells, e2e_steps, e2e_dt)
 
     # Dominant kernel: WENO5 advection of both velocity levels (k_weno2, stage 0),
-    # FP64-ALU bound.  Algorithmic work per cell = the reference formula of weno5.h
-    # (140 flops per directional derivative, plus 6 differences and 6 for the
-    # advecting velocity, 9 directions and 3 accumulations per component) for the
-    # two cal_advu_weno5 calls: 2766 flops; algorithmic bytes 12 words (6 fields in,
-    # 6 out).  FP64 peak measured live by fmf_measure_fma_rate; HBM peak from
-    # MEASURED_PEAKS.json.
+    # FP64-pipe bound.  The FP64 roofline counts executed FP64 instructions (ncu
+    # DADD + DMUL + DFMA per cell, WENO_FP64_INST_PER_CELL) against the FP64 pipe's
+    # instruction rate, half the FMA-chain flop rate fmf_measure_fma_rate measures
+    # live (an FMA is one instruction and two flops).  Also reported: the executed
+    # flops (FMA = 2) and the rate of the reference formula's flops (weno5.h, both
+    # one-sided reconstructions: 2766 per cell for the two calls), which exceeds
+    # the peak because the kernel evaluates the upwind side only, in fewer
+    # operations.  Algorithmic bytes 12 words per cell (6 fields in, 6 out); HBM
+    # peak from MEASURED_PEAKS.json.
     ms_stage = ctypes.c_float()
     capi.check(L.fmf_ctx_time_stage(g.h, 0, 5, ctypes.byref(ms_stage)), "time_stage")
     peaks, peak_kind = _peaks()
@@ -362,13 +369,19 @@ def main():
     L.fmf_measure_fma_rate.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_double)]
     capi.check(L.fmf_measure_fma_rate(1, ctypes.byref(fp64)), "fma rate")
     t_weno = ms_stage.value * 1e-3
-    flops = 2766.0 * cfg.cells
+    inst_rate = WENO_FP64_INST_PER_CELL * cfg.cells / t_weno / 1e12
+    inst_peak = fp64.value / 2.0
     gbs = 12 * 8 * cfg.cells / t_weno / 1e9
-    roofline = {"bound": "fp64", "achieved": flops / t_weno / 1e12, "peak": fp64.value, "unit": "TFLOP/s",
-                "frac": flops / t_weno / 1e12 / fp64.value,
-                "traffic": WENO_TRAFFIC_PER_CELL * cfg.cells if WENO_TRAFFIC_PER_CELL else None,
+    roofline = {"bound": "fp64", "achieved": inst_rate, "peak": inst_peak, "unit": "T FP64 instructions/s",
+                "frac": inst_rate / inst_peak,
+                "traffic": WENO_TRAFFIC_PER_CELL * cfg.cells,
                 "kernel": "k_weno2 (both cal_advu_weno5 calls of the step)", "kernel_ms": ms_stage.value,
-                "peak_source": "measured live (FP64 FMA chains, fmf_measure_fma_rate); HBM peak " + peak_kind,
+                "fp64_inst_per_cell": WENO_FP64_INST_PER_CELL,
+                "executed_tflops": WENO_FP64_FLOPS_PER_CELL * cfg.cells / t_weno / 1e12,
+                "reference_formula_tflops": 2766.0 * cfg.cells / t_weno / 1e12,
+                "fma_peak_tflops": fp64.value,
+                "peak_source": "FP64 FMA chains measured live (fmf_measure_fma_rate), one instruction per FMA; "
+                               "HBM peak " + peak_kind,
                 "hbm": {"achieved": gbs, "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": gbs / peaks["hbm_gbs"]}}
     # Mixed precision (FP32 WENO5 / MTHINC Newton+fluxes / SOR sweeps, FP64 pressure,
     # projection, divergence, volume sums and state): throughput on the same workload,

@@ -3,52 +3,61 @@
 //
 // weno5.h forms both one-sided reconstructions and multiplies the unused one by
 // vel-|vel| = 0 (or vel+|vel| = 0); here only the upwind side is evaluated, which
-// gives the same value and halves the FP64 work.  The grid has one thread per
+// gives the same value and halves the FP64 work, in a rearranged form of the same
+// quotient (wdir) that needs about two thirds of the remaining FP64 operations.  The grid has one thread per
 // interior cell (x fastest, 32 x 4 block, one k plane per grid z).
 #include "fused.cuh"
+#include "recip.cuh"
 #include "weno5_core.cuh"
 
 namespace fmf {
 namespace fused {
 
 namespace {
-// One-sided derivative: (a5,a3,a1,b1,b3) = (dfm5,dfm3,dfm1,dfp1,dfp3) for vel>0 and
-// (dfp5,dfp3,dfp1,dfm1,dfm3) for vel<0 (weno5.h:2-70 with the sides exchanged).
-template <class R>
-__device__ __forceinline__ R weno_side(R a5, R a3, R a1, R b1, R b3) {
-  const R d1 = a5 * (R)2 - a3 * (R)7 + a1 * (R)11;
-  const R d2 = -a3 + a1 * (R)5 + b1 * (R)2;
-  const R d3 = a1 * (R)2 + b1 * (R)5 - b3;
-  R t1 = a5 - a3 * (R)2 + a1, t2 = a5 - a3 * (R)4 + a1 * (R)3;
-  const R s1 = t1 * t1 * (R)13 + t2 * t2 * (R)3;
-  t1 = a3 - a1 * (R)2 + b1;
+// One directional derivative of weno5.h:2-70 times dxi, from the upwind side
+// only (the reference multiplies the other side by vel -/+ |vel| = 0).
+//  * vsum = 4 vel exactly: the reference's ((a+b)*0.5 + (c+d)*0.5)*0.5 scales
+//    (a+b) + (c+d) by powers of two only, so vsum = (a+b) + (c+d) and the term
+//    (vel + |vel|)/12 * dxi (or vel - |vel|) is |vsum| * dxi/24 on the side used.
+//  * The five differences are taken walking from the upwind end, q[c-3S]..q[c+2S]
+//    for vel > 0 (dfm5, dfm3, dfm1, dfp1, dfp3) and q[c+3S]..q[c-2S] for vel < 0,
+//    where they are -(dfp5, dfp3, dfp1, dfm1, dfm3); the reconstruction is odd in
+//    its inputs, so the sign of vel cancels and one formula serves both sides.
+//  * Weights: with the reference's m1 = (s2 s3)^2, m2 = 6 (s1 s3)^2,
+//    m3 = 3 (s1 s2)^2, w1 = m1 / (m1 + m2 + m3 + 1e-80), w3 likewise and
+//    w2 = 1 - w1 - w3, its sum w1 d1 + w2 d2 + w3 d3 equals
+//    (m1 d1 + m2 d2 + m3 d3 + 1e-80 d2) / (m1 + m2 + m3 + 1e-80).  That quotient
+//    is formed here with every s divided by 3 and every m by 486 (the factors 6
+//    and 3 moved onto d1/6 and d3/2), the 1e-80 divided by 486 and added to m2:
+//    the same value with fewer FP64 operations.
+// kx = dxi / 24.
+__device__ __forceinline__ double wdir(const double* __restrict__ q, long c, long S, double vsum, double kx) {
+  if (vsum == 0.0) return 0.0;
+  const long st = vsum > 0.0 ? S : -S;
+  const double* p = q + c - 3 * st;
+  const double q0 = __ldg(p), q1 = __ldg(p + st), q2 = __ldg(p + 2 * st), q3 = __ldg(p + 3 * st),
+               q4 = __ldg(p + 4 * st), q5 = __ldg(p + 5 * st);
+  const double a5 = q1 - q0, a3 = q2 - q1, a1 = q3 - q2, b1 = q4 - q3, b3 = q5 - q4;
+  constexpr double c13 = 13.0 / 3.0;
+  // s/3 = (13/3) t1^2 + t2^2 (weno5.h's 13 t1^2 + 3 t2^2)
+  double t1 = fma(a3, -2.0, a5 + a1), t2 = fma(a3, -4.0, fma(a1, 3.0, a5));
+  const double s1 = fma(t1 * c13, t1, t2 * t2);
+  t1 = fma(a1, -2.0, a3 + b1);
   t2 = a3 - b1;
-  const R s2 = t1 * t1 * (R)13 + t2 * t2 * (R)3;
-  t1 = a1 - b1 * (R)2 + b3;
-  t2 = a1 * (R)3 - b1 * (R)4 + b3;
-  const R s3 = t1 * t1 * (R)13 + t2 * t2 * (R)3;
-  R m1 = s2 * s3, m2 = s1 * s3, m3 = s1 * s2;
-  m1 = m1 * m1;
-  m2 = m2 * m2 * (R)6;
-  m3 = m3 * m3 * (R)3;
-  const R inv = (R)1 / (m1 + m2 + m3 + (R)1.0e-80);
-  const R w1 = m1 * inv, w3 = m3 * inv;
-  const R w2 = (R)1 - w1 - w3;
-  return w1 * d1 + w2 * d2 + w3 * d3;
-}
-
-// derivative of q along stride S at c with advecting velocity vel
-__device__ __forceinline__ double wdir(const double* __restrict__ q, long c, long S, double vel) {
-  if (vel == 0.0) return 0.0;
-  const double m3 = __ldg(q + c - 3 * S), m2 = __ldg(q + c - 2 * S), m1 = __ldg(q + c - S), z0 = __ldg(q + c),
-               p1 = __ldg(q + c + S), p2 = __ldg(q + c + 2 * S), p3 = __ldg(q + c + 3 * S);
-  const double dm5 = m2 - m3, dm3 = m1 - m2, dm1 = z0 - m1, dp1 = p1 - z0, dp3 = p2 - p1, dp5 = p3 - p2;
-  // the upwind side's inputs chosen by selects: one inlined side, no divergence
-  // where the velocity changes sign inside a warp
-  const bool pos = vel > 0.0;
-  const double r = weno_side<double>(pos ? dm5 : dp5, pos ? dm3 : dp3, pos ? dm1 : dp1, pos ? dp1 : dm1,
-                                     pos ? dp3 : dm3);
-  return (vel + vel) * r * (1.0 / 12.0);
+  const double s2 = fma(t1 * c13, t1, t2 * t2);
+  t1 = fma(b1, -2.0, a1 + b3);
+  t2 = fma(b1, -4.0, fma(a1, 3.0, b3));
+  const double s3 = fma(t1 * c13, t1, t2 * t2);
+  const double x = s2 * s3, y = s1 * s3, z = s1 * s2;
+  const double X = x * x, Y = fma(y, y, 1.0e-80 / 486.0), Z = z * z;
+  // d1/6, d2, d3/2 of weno5.h (d1 = 2 a5 - 7 a3 + 11 a1, d2 = -a3 + 5 a1 + 2 b1,
+  // d3 = 2 a1 + 5 b1 - b3)
+  const double d1 = fma(a1, 11.0 / 6.0, fma(a3, -7.0 / 6.0, a5 * (1.0 / 3.0)));
+  const double d2 = fma(b1, 2.0, fma(a1, 5.0, -a3));
+  const double d3 = fma(b1, 2.5, fma(b3, -0.5, a1));
+  const double num = fma(Z, d3, fma(Y, d2, X * d1));
+  const double den = fma(X, 1.0 / 6.0, fma(Z, 0.5, Y));
+  return (fabs(vsum) * kx) * (num * recip_nr(den));
 }
 
 // FP32 variant for the mixed-precision step.  The product-form weights scale like
@@ -163,6 +172,7 @@ __global__ void __launch_bounds__(128) k_weno2(Grid g, double dxi, double dyi, d
   if (i > g.ni || j > g.nj) return;
   const long X = 1, Y = g.sy, Z = g.sz;
   const long c = g.at(i, j, k);
+  const double kx = dxi * (1.0 / 24.0), ky = dyi * (1.0 / 24.0), kz = dzi * (1.0 / 24.0);
 #pragma unroll 1
   for (int lev = 0; lev < 2; ++lev) {
     const double* U = lev ? uo : u;
@@ -171,30 +181,21 @@ __global__ void __launch_bounds__(128) k_weno2(Grid g, double dxi, double dyi, d
     const double u0 = __ldg(U + c), uxm = __ldg(U + c - X), uxp = __ldg(U + c + X);
     const double v0 = __ldg(V + c), vym = __ldg(V + c - Y), vyp = __ldg(V + c + Y);
     const double w0 = __ldg(W + c), wzm = __ldg(W + c - Z), wzp = __ldg(W + c + Z);
-    double vel, a;
-    // u (cal_advu_weno5.f:80-120)
-    vel = ((uxm + u0) * 0.5 + (u0 + uxp) * 0.5) * 0.5;
-    a = wdir(U, c, X, vel) * dxi;
-    vel = ((vym + __ldg(V + c + X - Y)) * 0.5 + (v0 + __ldg(V + c + X)) * 0.5) * 0.5;
-    a += wdir(U, c, Y, vel) * dyi;
-    vel = ((wzm + __ldg(W + c + X - Z)) * 0.5 + (w0 + __ldg(W + c + X)) * 0.5) * 0.5;
-    a += wdir(U, c, Z, vel) * dzi;
+    double a;
+    // u (cal_advu_weno5.f:80-120); each vsum is 4 times the reference's vel
+    a = wdir(U, c, X, (uxm + u0) + (u0 + uxp), kx);
+    a += wdir(U, c, Y, (vym + __ldg(V + c + X - Y)) + (v0 + __ldg(V + c + X)), ky);
+    a += wdir(U, c, Z, (wzm + __ldg(W + c + X - Z)) + (w0 + __ldg(W + c + X)), kz);
     (lev ? auo : au)[c] = a;
     // v (:147-187)
-    vel = ((uxm + __ldg(U + c - X + Y)) * 0.5 + (u0 + __ldg(U + c + Y)) * 0.5) * 0.5;
-    a = wdir(V, c, X, vel) * dxi;
-    vel = ((vym + v0) * 0.5 + (v0 + vyp) * 0.5) * 0.5;
-    a += wdir(V, c, Y, vel) * dyi;
-    vel = ((wzm + __ldg(W + c + Y - Z)) * 0.5 + (w0 + __ldg(W + c + Y)) * 0.5) * 0.5;
-    a += wdir(V, c, Z, vel) * dzi;
+    a = wdir(V, c, X, (uxm + __ldg(U + c - X + Y)) + (u0 + __ldg(U + c + Y)), kx);
+    a += wdir(V, c, Y, (vym + v0) + (v0 + vyp), ky);
+    a += wdir(V, c, Z, (wzm + __ldg(W + c + Y - Z)) + (w0 + __ldg(W + c + Y)), kz);
     (lev ? avo : av)[c] = a;
     // w (:214-254)
-    vel = ((uxm + __ldg(U + c - X + Z)) * 0.5 + (u0 + __ldg(U + c + Z)) * 0.5) * 0.5;
-    a = wdir(W, c, X, vel) * dxi;
-    vel = ((vym + __ldg(V + c - Y + Z)) * 0.5 + (v0 + __ldg(V + c + Z)) * 0.5) * 0.5;
-    a += wdir(W, c, Y, vel) * dyi;
-    vel = ((wzm + w0) * 0.5 + (w0 + wzp) * 0.5) * 0.5;
-    a += wdir(W, c, Z, vel) * dzi;
+    a = wdir(W, c, X, (uxm + __ldg(U + c - X + Z)) + (u0 + __ldg(U + c + Z)), kx);
+    a += wdir(W, c, Y, (vym + __ldg(V + c - Y + Z)) + (v0 + __ldg(V + c + Z)), ky);
+    a += wdir(W, c, Z, (wzm + w0) + (w0 + wzp), kz);
     (lev ? awo : aw)[c] = a;
   }
 }

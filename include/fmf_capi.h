@@ -391,6 +391,11 @@ int fmf_ctx_time_stage(fmf_ctx* ctx, int stage, int reps, float* ms);
  * register-only kernel timed with CUDA events; the FP64 roofline denominator.
  * Measurement support; no counterpart in the reference. */
 int fmf_measure_fma_rate(int fp64, double* tflops);
+/* Largest relative error, over n positive normal doubles spread over 2^-1000 ..
+ * 2^1000, of the division-free reciprocal the fused WENO5 kernel uses (Newton-
+ * Raphson from an approximate reciprocal) against the IEEE quotient 1.0 / x.
+ * Verification support; no counterpart in the reference. */
+int fmf_check_reciprocal(long long n, double* max_rel_err);
 
 /* ---- restart files (host code; no GPU needed) ---------------------------
  * One Fortran unformatted sequential record, as the reference writes it: u v w p

@@ -94,3 +94,15 @@ def test_invariants_full_size(fmf_lib):
     assert np.abs(d).max() <= 1e-8 * np.abs(C.interior(u)).max() / cfg.dx
     assert np.isfinite(out).all()
     g.close()
+
+
+def test_division_free_reciprocal(fmf_lib):
+    """The WENO5 kernel's Newton-Raphson reciprocal against the IEEE quotient over
+    2^-1000 .. 2^1000: within two units in the last place."""
+    import ctypes
+
+    L = fmf_lib
+    L.fmf_check_reciprocal.argtypes = [ctypes.c_longlong, ctypes.POINTER(ctypes.c_double)]
+    err = ctypes.c_double(-1.0)
+    assert L.fmf_check_reciprocal(1 << 22, ctypes.byref(err)) == 0
+    assert 0.0 <= err.value <= 2 * 2.0 ** -52, err.value
