@@ -8,9 +8,12 @@
 namespace fmf {
 namespace fused {
 
+// cal_advu_weno5 of (u, v, w) into adv and of (uo, vo, wo) into advo, interior
+// cells.  fp32: FP32 arithmetic on the split pairs (hi, lo) of the six fields,
+// written into `split` (6 n float2) first.
 void weno5_both(cudaStream_t s, const Grid& g, double dxi, double dyi, double dzi, const double* u,
                 const double* v, const double* w, const double* uo, const double* vo, const double* wo,
-                double* const* adv, double* const* advo, bool fp32 = false);
+                double* const* adv, double* const* advo, bool fp32 = false, float2* split = nullptr);
 
 // solphi_mthinc1 for the faces solphi_mthinc2 reads (every face of rows 1..n in
 // the two directions normal to it, faces 0..n along it); list/count: device scratch

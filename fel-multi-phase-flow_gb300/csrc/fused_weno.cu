@@ -6,6 +6,7 @@
 // gives the same value and halves the FP64 work, in a rearranged form of the same
 // quotient (wdir) that needs about two thirds of the remaining FP64 operations.  The grid has one thread per
 // interior cell (x fastest, 32 x 4 block, one k plane per grid z).
+#include "../../include/fmf_capi.h"
 #include "fused.cuh"
 #include "recip.cuh"
 #include "weno5_core.cuh"
@@ -60,101 +61,120 @@ __device__ __forceinline__ double wdir(const double* __restrict__ q, long c, lon
   return (fabs(vsum) * kx) * (num * recip_nr(den));
 }
 
-// FP32 variant for the mixed-precision step.  The product-form weights scale like
-// the 8th power of the differences, so float would underflow for smooth fields;
-// the five differences are divided by their largest magnitude s first (the
-// weights are unchanged by a common scale; the sum is multiplied back by s), and
-// the reference's additive 1e-80 becomes 1e-80/s^8 in scaled units, evaluated as a
-// power of two and clamped to [2^-126, 2^127].  The lower clamp is the smallest
-// normal float: where all three smoothness indicators are 0 (data exactly linear
-// in float) the denominator is that term alone and its reciprocal must stay finite
-// (2^-149 gave 1/e = inf and 0 * inf = NaN); the weights are then 0, 1, 0 as in
-// the reference's limit.
-__device__ __forceinline__ float weno_side_f32(float a5, float a3, float a1, float b1, float b3) {
+// FP32 variant for the mixed-precision step.
+//
+// Inputs: the six velocity fields as float pairs (hi, lo), hi = (float)q and
+// lo = (float)(q - hi), written once per step by k_split6 (q - hi is exact in
+// double, so hi + lo holds q to about 2^-48).  A difference is formed as
+// (hi1 - hi0) + (lo1 - lo0): accurate to float precision relative to the
+// difference itself, as a double difference rounded to float would be, but
+// on the FP32 pipe (converting each double where a stencil reads it put about
+// thirteen conversions per point on GB300's FP64 pipe).
+//
+// The derivative is wdir's rearranged quotient in float.  The product-form
+// weights scale like the 8th power of the differences, so float would underflow
+// for smooth fields: the five differences are divided by their largest magnitude
+// s first (the quotient is unchanged by a common scale; the result is multiplied
+// back by s), and wdir's additive 1e-80/486 becomes 1e-80/486/s^8 in scaled
+// units, evaluated as a power of two and clamped to [2^-126, 2^100].  The lower
+// clamp keeps the denominator a normal float where all three smoothness
+// indicators are 0 (data exactly linear in float: the quotient is then d2, the
+// reference's limit); the upper keeps eps * d2 finite.  Differences below 2^-100
+// (a flat stencil) give 0.
+__global__ void k_split6(long n, const double* __restrict__ u, const double* __restrict__ v,
+                         const double* __restrict__ w, const double* __restrict__ uo, const double* __restrict__ vo,
+                         const double* __restrict__ wo, float2* __restrict__ out) {
+  const double* src[6] = {u, v, w, uo, vo, wo};
+  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) {
+#pragma unroll
+    for (int f = 0; f < 6; ++f) {
+      const double q = __ldg(src[f] + t);
+      const float hi = (float)q;
+      out[f * n + t] = make_float2(hi, (float)(q - (double)hi));
+    }
+  }
+}
+
+__device__ __forceinline__ float lg2_approx(float x) {
+  float r;
+  asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+__device__ __forceinline__ float ex2_approx(float x) {
+  float r;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+
+__device__ __forceinline__ float wdir_f32(const float2* __restrict__ q, long c, long S, float vsum, float kx) {
+  if (vsum == 0.0f) return 0.0f;
+  const long st = vsum > 0.0f ? S : -S;
+  const float2* p = q + c - 3 * st;
+  const float2 q0 = __ldg(p), q1 = __ldg(p + st), q2 = __ldg(p + 2 * st), q3 = __ldg(p + 3 * st),
+               q4 = __ldg(p + 4 * st), q5 = __ldg(p + 5 * st);
+  float a5 = (q1.x - q0.x) + (q1.y - q0.y), a3 = (q2.x - q1.x) + (q2.y - q1.y), a1 = (q3.x - q2.x) + (q3.y - q2.y),
+        b1 = (q4.x - q3.x) + (q4.y - q3.y), b3 = (q5.x - q4.x) + (q5.y - q4.y);
   const float s = fmaxf(fmaxf(fmaxf(fabsf(a5), fabsf(a3)), fmaxf(fabsf(a1), fabsf(b1))), fabsf(b3));
-  if (s == 0.0f) return 0.0f;
-  const float is = 1.0f / s;
+  if (s < 0x1p-100f) return 0.0f;
+  const float is = __fdividef(1.0f, s);
   a5 *= is;
   a3 *= is;
   a1 *= is;
   b1 *= is;
   b3 *= is;
-  const float d1 = a5 * 2.0f - a3 * 7.0f + a1 * 11.0f;
-  const float d2 = -a3 + a1 * 5.0f + b1 * 2.0f;
-  const float d3 = a1 * 2.0f + b1 * 5.0f - b3;
-  float t1 = a5 - a3 * 2.0f + a1, t2 = a5 - a3 * 4.0f + a1 * 3.0f;
-  const float s1 = t1 * t1 * 13.0f + t2 * t2 * 3.0f;
-  t1 = a3 - a1 * 2.0f + b1;
+  constexpr float c13 = 13.0f / 3.0f;
+  float t1 = fmaf(a3, -2.0f, a5 + a1), t2 = fmaf(a3, -4.0f, fmaf(a1, 3.0f, a5));
+  const float s1 = fmaf(t1 * c13, t1, t2 * t2);
+  t1 = fmaf(a1, -2.0f, a3 + b1);
   t2 = a3 - b1;
-  const float s2 = t1 * t1 * 13.0f + t2 * t2 * 3.0f;
-  t1 = a1 - b1 * 2.0f + b3;
-  t2 = a1 * 3.0f - b1 * 4.0f + b3;
-  const float s3 = t1 * t1 * 13.0f + t2 * t2 * 3.0f;
-  float m1 = s2 * s3, m2 = s1 * s3, m3 = s1 * s2;
-  m1 = m1 * m1;
-  m2 = m2 * m2 * 6.0f;
-  m3 = m3 * m3 * 3.0f;
-  // 1e-80 / s^8 = 2^(log2(1e-80) - 8 log2 s)
-  const float e = exp2f(fminf(fmaxf(-265.754f - 8.0f * log2f(s), -126.0f), 127.0f));
-  const float inv = 1.0f / (m1 + m2 + m3 + e);
-  const float w1 = m1 * inv, w3 = m3 * inv;
-  const float w2 = 1.0f - w1 - w3;
-  return (w1 * d1 + w2 * d2 + w3 * d3) * s;
+  const float s2 = fmaf(t1 * c13, t1, t2 * t2);
+  t1 = fmaf(b1, -2.0f, a1 + b3);
+  t2 = fmaf(b1, -4.0f, fmaf(a1, 3.0f, b3));
+  const float s3 = fmaf(t1 * c13, t1, t2 * t2);
+  // log2(1e-80 / 486) = -274.679
+  const float eps = ex2_approx(fminf(fmaxf(-274.679f - 8.0f * lg2_approx(s), -126.0f), 100.0f));
+  const float x = s2 * s3, y = s1 * s3, z = s1 * s2;
+  const float X = x * x, Y = fmaf(y, y, eps), Z = z * z;
+  const float d1 = fmaf(a1, 11.0f / 6.0f, fmaf(a3, -7.0f / 6.0f, a5 * (1.0f / 3.0f)));
+  const float d2 = fmaf(b1, 2.0f, fmaf(a1, 5.0f, -a3));
+  const float d3 = fmaf(b1, 2.5f, fmaf(b3, -0.5f, a1));
+  const float num = fmaf(Z, d3, fmaf(Y, d2, X * d1));
+  const float den = fmaf(X, 1.0f / 6.0f, fmaf(Z, 0.5f, Y));
+  return (fabsf(vsum) * kx) * (__fdividef(num, den) * s);
 }
-__device__ __forceinline__ float wdir_f32(const double* __restrict__ q, long c, long S, float vel) {
-  if (vel == 0.0f) return 0.0f;
-  const double m3 = __ldg(q + c - 3 * S), m2 = __ldg(q + c - 2 * S), m1 = __ldg(q + c - S), z0 = __ldg(q + c),
-               p1 = __ldg(q + c + S), p2 = __ldg(q + c + 2 * S), p3 = __ldg(q + c + 3 * S);
-  // differences formed in double (cancellation-free), arithmetic in float
-  const float dm5 = (float)(m2 - m3), dm3 = (float)(m1 - m2), dm1 = (float)(z0 - m1), dp1 = (float)(p1 - z0),
-              dp3 = (float)(p2 - p1), dp5 = (float)(p3 - p2);
-  const bool pos = vel > 0.0f;
-  const float r = weno_side_f32(pos ? dm5 : dp5, pos ? dm3 : dp3, pos ? dm1 : dp1, pos ? dp1 : dm1, pos ? dp3 : dm3);
-  return (vel + vel) * r * (1.0f / 12.0f);
-}
-__global__ void __launch_bounds__(128) k_weno2_f32(Grid g, double dxi_, double dyi_, double dzi_,
-                                                   const double* __restrict__ u, const double* __restrict__ v,
-                                                   const double* __restrict__ w, const double* __restrict__ uo,
-                                                   const double* __restrict__ vo, const double* __restrict__ wo,
-                                                   double* __restrict__ au, double* __restrict__ av,
-                                                   double* __restrict__ aw, double* __restrict__ auo,
-                                                   double* __restrict__ avo, double* __restrict__ awo) {
+// V[f] = the split pair arrays of u, v, w (f = 0..2) and uo, vo, wo (3..5)
+__global__ void __launch_bounds__(128) k_weno2_f32(Grid g, float kx, float ky, float kz,
+                                                   const float2* __restrict__ sp, double* __restrict__ au,
+                                                   double* __restrict__ av, double* __restrict__ aw,
+                                                   double* __restrict__ auo, double* __restrict__ avo,
+                                                   double* __restrict__ awo) {
   const int i = 1 + (int)(blockIdx.x * blockDim.x + threadIdx.x);
   const int j = 1 + (int)(blockIdx.y * blockDim.y + threadIdx.y);
   const int k = 1 + (int)blockIdx.z;
   if (i > g.ni || j > g.nj) return;
-  const float dxi = (float)dxi_, dyi = (float)dyi_, dzi = (float)dzi_;
   const long X = 1, Y = g.sy, Z = g.sz;
   const long c = g.at(i, j, k);
 #pragma unroll 1
   for (int lev = 0; lev < 2; ++lev) {
-    const double* U = lev ? uo : u;
-    const double* V = lev ? vo : v;
-    const double* W = lev ? wo : w;
-    const float u0 = (float)__ldg(U + c), uxm = (float)__ldg(U + c - X), uxp = (float)__ldg(U + c + X);
-    const float v0 = (float)__ldg(V + c), vym = (float)__ldg(V + c - Y), vyp = (float)__ldg(V + c + Y);
-    const float w0 = (float)__ldg(W + c), wzm = (float)__ldg(W + c - Z), wzp = (float)__ldg(W + c + Z);
-    float vel, a;
-    vel = ((uxm + u0) * 0.5f + (u0 + uxp) * 0.5f) * 0.5f;
-    a = wdir_f32(U, c, X, vel) * dxi;
-    vel = ((vym + (float)__ldg(V + c + X - Y)) * 0.5f + (v0 + (float)__ldg(V + c + X)) * 0.5f) * 0.5f;
-    a += wdir_f32(U, c, Y, vel) * dyi;
-    vel = ((wzm + (float)__ldg(W + c + X - Z)) * 0.5f + (w0 + (float)__ldg(W + c + X)) * 0.5f) * 0.5f;
-    a += wdir_f32(U, c, Z, vel) * dzi;
+    const float2* U = sp + (long)(3 * lev) * g.n;
+    const float2* V = U + g.n;
+    const float2* W = V + g.n;
+    auto h = [](const float2* a, long o) { return __ldg(&a[o].x); };
+    const float u0 = h(U, c), uxm = h(U, c - X), uxp = h(U, c + X);
+    const float v0 = h(V, c), vym = h(V, c - Y), vyp = h(V, c + Y);
+    const float w0 = h(W, c), wzm = h(W, c - Z), wzp = h(W, c + Z);
+    float a;
+    a = wdir_f32(U, c, X, (uxm + u0) + (u0 + uxp), kx);
+    a += wdir_f32(U, c, Y, (vym + h(V, c + X - Y)) + (v0 + h(V, c + X)), ky);
+    a += wdir_f32(U, c, Z, (wzm + h(W, c + X - Z)) + (w0 + h(W, c + X)), kz);
     (lev ? auo : au)[c] = (double)a;
-    vel = ((uxm + (float)__ldg(U + c - X + Y)) * 0.5f + (u0 + (float)__ldg(U + c + Y)) * 0.5f) * 0.5f;
-    a = wdir_f32(V, c, X, vel) * dxi;
-    vel = ((vym + v0) * 0.5f + (v0 + vyp) * 0.5f) * 0.5f;
-    a += wdir_f32(V, c, Y, vel) * dyi;
-    vel = ((wzm + (float)__ldg(W + c + Y - Z)) * 0.5f + (w0 + (float)__ldg(W + c + Y)) * 0.5f) * 0.5f;
-    a += wdir_f32(V, c, Z, vel) * dzi;
+    a = wdir_f32(V, c, X, (uxm + h(U, c - X + Y)) + (u0 + h(U, c + Y)), kx);
+    a += wdir_f32(V, c, Y, (vym + v0) + (v0 + vyp), ky);
+    a += wdir_f32(V, c, Z, (wzm + h(W, c + Y - Z)) + (w0 + h(W, c + Y)), kz);
     (lev ? avo : av)[c] = (double)a;
-    vel = ((uxm + (float)__ldg(U + c - X + Z)) * 0.5f + (u0 + (float)__ldg(U + c + Z)) * 0.5f) * 0.5f;
-    a = wdir_f32(W, c, X, vel) * dxi;
-    vel = ((vym + (float)__ldg(V + c - Y + Z)) * 0.5f + (v0 + (float)__ldg(V + c + Z)) * 0.5f) * 0.5f;
-    a += wdir_f32(W, c, Y, vel) * dyi;
-    vel = ((wzm + w0) * 0.5f + (w0 + wzp) * 0.5f) * 0.5f;
-    a += wdir_f32(W, c, Z, vel) * dzi;
+    a = wdir_f32(W, c, X, (uxm + h(U, c - X + Z)) + (u0 + h(U, c + Z)), kx);
+    a += wdir_f32(W, c, Y, (vym + h(V, c - Y + Z)) + (v0 + h(V, c + Z)), ky);
+    a += wdir_f32(W, c, Z, (wzm + w0) + (w0 + wzp), kz);
     (lev ? awo : aw)[c] = (double)a;
   }
 }
@@ -202,17 +222,26 @@ __global__ void __launch_bounds__(128) k_weno2(Grid g, double dxi, double dyi, d
 }  // namespace
 
 // Both levels; only interior cells are written (the fused step never reads the
-// halo of the advection terms, which cal_advu_weno5.f:44-52 sets to zero).
+// halo of the advection terms, which cal_advu_weno5.f:44-52 sets to zero).  The
+// FP32 variant first writes the split pairs of the six fields into `split`
+// (6 n float2).
 void weno5_both(cudaStream_t s, const Grid& g, double dxi, double dyi, double dzi, const double* u,
                 const double* v, const double* w, const double* uo, const double* vo, const double* wo,
-                double* const* adv, double* const* advo, bool fp32) {
+                double* const* adv, double* const* advo, bool fp32, float2* split) {
   dim3 b(32, 4, 1);
   dim3 gr((unsigned)((g.ni + 31) / 32), (unsigned)((g.nj + 3) / 4), (unsigned)g.nk);
-  if (fp32)
-    k_weno2_f32<<<gr, b, 0, s>>>(g, dxi, dyi, dzi, u, v, w, uo, vo, wo, adv[0], adv[1], adv[2], advo[0], advo[1],
-                                 advo[2]);
-  else
-    k_weno2<<<gr, b, 0, s>>>(g, dxi, dyi, dzi, u, v, w, uo, vo, wo, adv[0], adv[1], adv[2], advo[0], advo[1], advo[2]);
+  if (fp32) {
+    if (!split) {
+      set_status(FMF_ERR_ARG);
+      return;
+    }
+    k_split6<<<152 * 8, 256, 0, s>>>(g.n, u, v, w, uo, vo, wo, split);
+    k_weno2_f32<<<gr, b, 0, s>>>(g, (float)(dxi / 24.0), (float)(dyi / 24.0), (float)(dzi / 24.0), split, adv[0],
+                                 adv[1], adv[2], advo[0], advo[1], advo[2]);
+    count_launch(2);
+    return;
+  }
+  k_weno2<<<gr, b, 0, s>>>(g, dxi, dyi, dzi, u, v, w, uo, vo, wo, adv[0], adv[1], adv[2], advo[0], advo[1], advo[2]);
   count_launch();
 }
 

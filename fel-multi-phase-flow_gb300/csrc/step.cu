@@ -61,6 +61,7 @@ struct fmf_ctx {
   int* band;    // MTHINC band-cell list, then its length
   bool mixed = false;        // precision == FMF_MIXED
   fused::RefineBufs rb{};    // FP32 buffers of the mixed-precision viscous solve
+  float2* wsplit = nullptr;  // mixed: split pairs of u, v, w, uo, vo, wo for the FP32 WENO5 (6 n)
   double* host_err = nullptr;  // pinned
   std::vector<int> sor_iters;
 };
@@ -146,6 +147,7 @@ int fmf_ctx_create(const fmf_params* prm, fmf_ctx** out) {
     rb.gw = allocf(c, fused::refine_floats(c->g, 0));
     rb.gx = allocf(c, fused::refine_floats(c->g, 1));
     rb.gz = allocf(c, fused::refine_floats(c->g, 2));
+    c->wsplit = (float2*)alloc(c, 6 * n);
   }
   {
     const long nb = (long)(prm->ni + 2) * (prm->nj + 2) * (prm->nk + 2) + 1;
@@ -339,7 +341,7 @@ static void seg_pre(fmf_ctx* c) {
   op::cal_arith_mean(s, g, phin0, P.rmul, P.rmug, c->rmun);
   // :532-541
   fused::weno5_both(s, g, dxinv, dyinv, dzinv, c->u, c->v, c->w, c->uo, c->vo, c->wo, c->adv, c->advo,
-                    P.precision == FMF_MIXED);
+                    P.precision == FMF_MIXED, c->wsplit);
   op::calphat(s, g, c->p, c->po, c->phat);
   op::cal_grad_prs(s, g, dxinv, dyinv, dzinv, c->phat, c->prs[0], c->prs[1], c->prs[2]);
   op::calsij(s, g, dxinv, dyinv, dzinv, c->u, c->v, c->w, c->sk);
@@ -527,7 +529,8 @@ int fmf_ctx_time_stage(fmf_ctx* c, int stage, int reps, float* ms) {
   auto run = [&]() {
     switch (stage) {
       case 0:
-        fused::weno5_both(s, g, dxinv, dyinv, dzinv, c->u, c->v, c->w, c->uo, c->vo, c->wo, c->adv, c->advo, mixed);
+        fused::weno5_both(s, g, dxinv, dyinv, dzinv, c->u, c->v, c->w, c->uo, c->vo, c->wo, c->adv, c->advo, mixed,
+                          c->wsplit);
         break;
       case 1:
         if (mixed)
