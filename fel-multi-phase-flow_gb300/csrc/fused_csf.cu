@@ -20,9 +20,11 @@
 // memory) and R = float (the mixed-precision step; each phi plane is converted once
 // into a shared-memory ring of three planes, everything after that is FP32 and the
 // three forces are widened to double on the store).
+#include <algorithm>
 #include <type_traits>
 
 #include "fused.cuh"
+#include "recip.cuh"
 
 namespace fmf {
 namespace fused {
@@ -40,7 +42,7 @@ constexpr bool kStaged = std::is_same<R, float>::value;
 
 template <class R>
 struct CsfP {
-  R dxi, dyi, dzi, gx, gy, gz, vs, st;
+  R dxi, dyi, dzi, gx, gy, gz, vs2, vs8, st;  // vs2 = 2 vs, vs8 = 8 vs
 };
 
 template <class R>
@@ -54,24 +56,14 @@ struct Smem {
   R Q[kStaged<R> ? 3 : 1][kStaged<R> ? QP : 1];  // staged phi planes, slot = plane % 3
 };
 
-// 1/sqrt(s) for s in the FP32 normal range: Newton-Raphson on f(y) = y^-2 - s,
-// y <- y (3 - s y^2)/2, seeded with the FP32 reciprocal square root (relative error
-// ~3e-7 after the rounding of s); the error squares per step, so two steps reach
-// FP64 rounding.  Eight FP64 operations instead of a square root and a division.
-__device__ __forceinline__ double rsqrt_newton(double s) {
-  double y = (double)rsqrtf((float)s);
-#pragma unroll
-  for (int it = 0; it < 2; ++it) y = y * fma(-0.5 * s * y, y, 1.5);
-  return y;
-}
 // N(v) = v/(|v| + vs).  Where |v| exceeds vs by more than 1e12 the relative
 // correction vs/|v| is below 1e-12 and 1/|v| is used; smaller |v| (including zero
-// gradients) takes the exact expression.  |v|^2 is below 1e6 dxinv^2 for phi in
-// [0, 1], inside the FP32 range.
+// gradients) takes the exact expression.  Callers pass v scaled by 1/c (a sum
+// instead of a mean) with vs scaled by 1/c: N(c w) = w/(|w| + vs/c).
 __device__ __forceinline__ void unit(double x, double y, double z, double vs, double* o) {
   const double s = x * x + y * y + z * z;
   const double big = vs * 1.0e12;
-  const double inv = (s > big * big && s < 1.0e30) ? rsqrt_newton(s) : 1.0 / (sqrt(s) + vs);
+  const double inv = s > big * big ? rsqrt_nr(s) : 1.0 / (sqrt(s) + vs);
   o[0] = x * inv;
   o[1] = y * inv;
   o[2] = z * inv;
@@ -139,19 +131,19 @@ __device__ void side_normals(const CsfP<R>& p, Smem<R>& S, int gk, int s) {
     const int ga = a, gb = b;          // same point in the G region (offset -1,-1)
     const int c0 = gb * GX + ga;
     R o[3];
-    // n13(i,j): mean of G(i, j-1) and G(i, j)
+    // n13(i,j): mean of G(i, j-1) and G(i, j) (the sum, with 2 vs)
     const int cm = (gb - 1) * GX + ga;
     if (gb >= 1) {
-      unit((S.G[gk][0][cm] + S.G[gk][0][c0]) * R(0.5), (S.G[gk][1][cm] + S.G[gk][1][c0]) * R(0.5),
-           (S.G[gk][2][cm] + S.G[gk][2][c0]) * R(0.5), p.vs, o);
+      unit(S.G[gk][0][cm] + S.G[gk][0][c0], S.G[gk][1][cm] + S.G[gk][1][c0], S.G[gk][2][cm] + S.G[gk][2][c0], p.vs2,
+           o);
       S.a13[s][0][e] = o[0];
       S.a13[s][1][e] = o[2];
     }
     // n23(i,j): mean of G(i-1, j) and G(i, j)
     if (ga >= 1) {
       const int cw = gb * GX + ga - 1;
-      unit((S.G[gk][0][cw] + S.G[gk][0][c0]) * R(0.5), (S.G[gk][1][cw] + S.G[gk][1][c0]) * R(0.5),
-           (S.G[gk][2][cw] + S.G[gk][2][c0]) * R(0.5), p.vs, o);
+      unit(S.G[gk][0][cw] + S.G[gk][0][c0], S.G[gk][1][cw] + S.G[gk][1][c0], S.G[gk][2][cw] + S.G[gk][2][c0], p.vs2,
+           o);
       S.a23[s][0][e] = o[1];
       S.a23[s][1][e] = o[2];
     }
@@ -166,16 +158,16 @@ __device__ void centre_normals(const CsfP<R>& p, Smem<R>& S, int gk, int gk1, in
   for (int e = threadIdx.x; e < NP; e += blockDim.x) {
     const int a = e % NX, b = e / NX;
     R o[3];
-    // npp at (I0+a, J0+b): H over (i-1..i, j-1..j) = G region (a..a+1, b..b+1)
+    // npp at (I0+a, J0+b): H over (i-1..i, j-1..j) = G region (a..a+1, b..b+1), the
+    // sum of the 8 vertex gradients with 8 vs
     const int h00 = b * GX + a, h10 = h00 + 1, h01 = h00 + GX, h11 = h01 + 1;
-    unit((S.H[0][h00] + S.H[0][h10] + S.H[0][h01] + S.H[0][h11]) * R(0.125),
-         (S.H[1][h00] + S.H[1][h10] + S.H[1][h01] + S.H[1][h11]) * R(0.125),
-         (S.H[2][h00] + S.H[2][h10] + S.H[2][h01] + S.H[2][h11]) * R(0.125), p.vs, o);
+    unit(S.H[0][h00] + S.H[0][h10] + S.H[0][h01] + S.H[0][h11], S.H[1][h00] + S.H[1][h10] + S.H[1][h01] + S.H[1][h11],
+         S.H[2][h00] + S.H[2][h10] + S.H[2][h01] + S.H[2][h11], p.vs8, o);
     S.pp[s][0][e] = o[0];
     S.pp[s][1][e] = o[1];
     S.pp[s][2][e] = o[2];
     // n12 at (I0-1+a, J0-1+b): H at the same point
-    unit(S.H[0][h00] * R(0.5), S.H[1][h00] * R(0.5), S.H[2][h00] * R(0.5), p.vs, o);
+    unit(S.H[0][h00], S.H[1][h00], S.H[2][h00], p.vs2, o);
     S.a12[s][0][e] = o[0];
     S.a12[s][1][e] = o[1];
   }
@@ -262,6 +254,39 @@ __global__ void __launch_bounds__(256) k_csf(Grid g, CsfP<R> p, int kchunk, cons
   }
 }
 
+// k planes per block.  A block of c planes costs about c + 1 plane passes (the
+// first plane's gradients and side normals are formed twice), and blocks run in
+// waves of (SMs x resident blocks per SM); the chunk minimises waves x (c + 1)
+// over 4 <= c <= nk (nk itself on small grids), so the last wave is not left
+// mostly empty.  Occupancy and SM count are queried once per kernel and device.
+int csf_chunk(const Grid& g, const void* fn, size_t smem) {
+  static thread_local const void* cached_fn = nullptr;
+  static thread_local int cached_dev = -1, cached_cap = 0;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (fn != cached_fn || dev != cached_dev) {
+    int sms = 0, per_sm = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, 256, smem);
+    cached_fn = fn;
+    cached_dev = dev;
+    cached_cap = std::max(1, sms * per_sm);
+  }
+  if (g.nk < 16) return g.nk;
+  const long tiles = (long)(g.ni / TX) * (g.nj / TY);
+  int best = 16;
+  long best_cost = -1;
+  for (int c = 4; c <= g.nk; ++c) {
+    const long blocks = tiles * ((g.nk + c - 1) / c);
+    const long cost = ((blocks + cached_cap - 1) / cached_cap) * (c + 1);
+    if (best_cost < 0 || cost < best_cost) {
+      best_cost = cost;
+      best = c;
+    }
+  }
+  return best;
+}
+
 template <class R>
 void launch_csf(cudaStream_t s, const Grid& g, double dxinv, double dyinv, double dzinv, double rhol, double rhog,
                 double sigma, const double* phi, double* fu, double* fv, double* fw, double* kap) {
@@ -272,11 +297,13 @@ void launch_csf(cudaStream_t s, const Grid& g, double dxinv, double dyinv, doubl
   p.gx = (R)(0.25 * dxinv);
   p.gy = (R)(0.25 * dyinv);
   p.gz = (R)(0.25 * dzinv);
-  p.vs = (R)(std::sqrt(dxinv * dxinv + dyinv * dyinv + dzinv * dzinv) * 1.0e-30);
+  const double vs = std::sqrt(dxinv * dxinv + dyinv * dyinv + dzinv * dzinv) * 1.0e-30;
+  p.vs2 = (R)(2.0 * vs);
+  p.vs8 = (R)(8.0 * vs);
   p.st = (R)(2.0 * sigma / (rhol + rhog));
-  const int kchunk = g.nk >= 64 ? 16 : (g.nk >= 16 ? 8 : g.nk);
   const size_t smem = sizeof(Smem<R>);
   cudaFuncSetAttribute(k_csf<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  const int kchunk = csf_chunk(g, (const void*)k_csf<R>, smem);
   dim3 gr((unsigned)(g.ni / TX), (unsigned)(g.nj / TY), (unsigned)((g.nk + kchunk - 1) / kchunk));
   k_csf<R><<<gr, 256, smem, s>>>(g, p, kchunk, phi, fu, fv, fw, kap);
   count_launch();

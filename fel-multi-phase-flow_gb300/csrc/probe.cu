@@ -5,7 +5,9 @@
 // so bench.py measures that rate live: 152*8 blocks of 256 threads, each thread
 // 8 independent multiply-add chains (enough independent work to fill every FP64
 // pipe), timed with CUDA events after a warm-up launch.  Reads no memory; writes
-// one value per thread so the chains are not removed.
+// one value per thread so the chains are not removed.  Also here: the error
+// checks of the division-free reciprocal and reciprocal square root (recip.cuh)
+// against CUDA's own 1.0 / x and 1.0 / sqrt(x).
 #include <cstring>
 
 #include "../../include/fmf_capi.h"
@@ -58,9 +60,9 @@ int measure(int iters, double* tflops) {
 
 // n positive normal doubles spread over exponents 2^-1000 .. 2^1000 with
 // pseudo-random mantissas (a 64-bit mix of the index); the largest relative error
-// of recip_nr against the IEEE quotient 1.0 / x, as ordered bits of a
-// non-negative double.
-__global__ void k_check_recip(long n, unsigned long long* worst) {
+// of recip_nr (which = 0) against the IEEE quotient 1.0 / x, or of rsqrt_nr
+// (which = 1) against 1.0 / sqrt(x), as ordered bits of a non-negative double.
+__global__ void k_check_recip(long n, int which, unsigned long long* worst) {
   unsigned long long m = 0;
   for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) {
     unsigned long long h = (unsigned long long)t * 0x9E3779B97F4A7C15ull;
@@ -69,21 +71,19 @@ __global__ void k_check_recip(long n, unsigned long long* worst) {
     h ^= h >> 29;
     const long long e = 1023 + (long long)(t % 2001) - 1000;
     const double x = __longlong_as_double((long long)((e << 52) | (h & 0xFFFFFFFFFFFFFull)));
-    const double q = 1.0 / x, r = fmf::recip_nr(x);
+    const double q = which ? 1.0 / sqrt(x) : 1.0 / x, r = which ? fmf::rsqrt_nr(x) : fmf::recip_nr(x);
     const double rel = fabs(r - q) / q;
     const unsigned long long b = (unsigned long long)__double_as_longlong(rel);
     m = b > m ? b : m;
   }
   atomicMax(worst, m);
 }
-}  // namespace
-
-extern "C" int fmf_check_reciprocal(long long n, double* max_rel_err) {
+int check_recip(long long n, int which, double* max_rel_err) {
   if (!max_rel_err || n <= 0) return FMF_ERR_ARG;
   unsigned long long* d = nullptr;
   if (cudaMalloc(&d, sizeof(unsigned long long)) != cudaSuccess) return FMF_ERR_NOMEM;
   cudaMemset(d, 0, sizeof(unsigned long long));
-  k_check_recip<<<152 * 4, 256>>>((long)n, d);
+  k_check_recip<<<152 * 4, 256>>>((long)n, which, d);
   fmf::count_launch();
   unsigned long long h = 0;
   const cudaError_t e = cudaMemcpy(&h, d, sizeof(h), cudaMemcpyDeviceToHost);
@@ -92,6 +92,10 @@ extern "C" int fmf_check_reciprocal(long long n, double* max_rel_err) {
   std::memcpy(max_rel_err, &h, sizeof(double));
   return FMF_OK;
 }
+}  // namespace
+
+extern "C" int fmf_check_reciprocal(long long n, double* max_rel_err) { return check_recip(n, 0, max_rel_err); }
+extern "C" int fmf_check_rsqrt(long long n, double* max_rel_err) { return check_recip(n, 1, max_rel_err); }
 
 extern "C" int fmf_measure_fma_rate(int fp64, double* tflops) {
   if (!tflops) return FMF_ERR_ARG;

@@ -396,6 +396,10 @@ int fmf_measure_fma_rate(int fp64, double* tflops);
  * Raphson from an approximate reciprocal) against the IEEE quotient 1.0 / x.
  * Verification support; no counterpart in the reference. */
 int fmf_check_reciprocal(long long n, double* max_rel_err);
+/* The same for the division-free reciprocal square root of the fused CSF kernel
+ * (Newton-Raphson from an approximate reciprocal square root) against
+ * 1.0 / sqrt(x). */
+int fmf_check_rsqrt(long long n, double* max_rel_err);
 
 /* ---- restart files (host code; no GPU needed) ---------------------------
  * One Fortran unformatted sequential record, as the reference writes it: u v w p

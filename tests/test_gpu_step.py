@@ -106,3 +106,15 @@ def test_division_free_reciprocal(fmf_lib):
     err = ctypes.c_double(-1.0)
     assert L.fmf_check_reciprocal(1 << 22, ctypes.byref(err)) == 0
     assert 0.0 <= err.value <= 2 * 2.0 ** -52, err.value
+
+
+def test_division_free_rsqrt(fmf_lib):
+    """The CSF kernel's Newton-Raphson reciprocal square root against
+    1.0 / sqrt(x) over 2^-1000 .. 2^1000: within two units in the last place."""
+    import ctypes
+
+    L = fmf_lib
+    L.fmf_check_rsqrt.argtypes = [ctypes.c_longlong, ctypes.POINTER(ctypes.c_double)]
+    err = ctypes.c_double(-1.0)
+    assert L.fmf_check_rsqrt(1 << 22, ctypes.byref(err)) == 0
+    assert 0.0 <= err.value <= 2 * 2.0 ** -52, err.value
