@@ -3,86 +3,100 @@
 // calfst).
 #include "adj.cuh"
 #include "ops.cuh"
+#include "recip.cuh"
 
 namespace fmf {
 namespace adj {
 
 namespace {
-// One side of weno5.h: r = w1 d1 + w2 d2 + w3 d3 with the product-form weights, and
-// its reverse sweep (la[0..4] += dr/d(a5, a3, a1, b1, b3) * lr).  The weights are
-// formed with one reciprocal of the denominator (iD), which the reverse sweep reuses:
-// an adjoint needs the derivative, not the forward's last bit.
-struct Side {
-  double d1, d2, d3, t[6], s1, s2, s3, P1, P2, P3, iD, w1, w3, r;
+// The forward derivative is fused_weno.cu's wdir: the five differences e taken
+// walking from the upwind end of the stencil, and R(e) = num / den with
+//   s_k/3 = (13/3) t1^2 + t2^2,  x = s2 s3, y = s1 s3, z = s1 s2,
+//   X = x^2, Y = y^2 + 1e-80/486, Z = z^2,
+//   num = X D1 + Y d2 + Z D3,  den = X/6 + Y + Z/2
+// (D1 = d1/6, D3 = d3/2 of weno5.h), out += |vel|/6 * di * R(e).  Walk holds the
+// forward quantities the reverse sweep reuses.
+struct Walk {
+  double t1a, t2a, t1b, t2b, t1c, t2c, s1, s2, s3, x, y, z, X, Y, Z, D1, d2, D3, iD, R;
 };
-__device__ __forceinline__ void side_fwd(double a5, double a3, double a1, double b1, double b3, Side& S) {
-  S.d1 = a5 * 2.0 - a3 * 7.0 + a1 * 11.0;
-  S.d2 = -a3 + a1 * 5.0 + b1 * 2.0;
-  S.d3 = a1 * 2.0 + b1 * 5.0 - b3;
-  S.t[0] = a5 - a3 * 2.0 + a1;
-  S.t[1] = a5 - a3 * 4.0 + a1 * 3.0;
-  S.t[2] = a3 - a1 * 2.0 + b1;
-  S.t[3] = a3 - b1;
-  S.t[4] = a1 - b1 * 2.0 + b3;
-  S.t[5] = a1 * 3.0 - b1 * 4.0 + b3;
-  S.s1 = S.t[0] * S.t[0] * 13.0 + S.t[1] * S.t[1] * 3.0;
-  S.s2 = S.t[2] * S.t[2] * 13.0 + S.t[3] * S.t[3] * 3.0;
-  S.s3 = S.t[4] * S.t[4] * 13.0 + S.t[5] * S.t[5] * 3.0;
-  S.P1 = S.s2 * S.s3;
-  S.P2 = S.s1 * S.s3;
-  S.P3 = S.s1 * S.s2;
-  const double m1 = S.P1 * S.P1, m2 = S.P2 * S.P2 * 6.0, m3 = S.P3 * S.P3 * 3.0;
-  S.iD = 1.0 / (m1 + m2 + m3 + 1.0e-80);
-  S.w1 = m1 * S.iD;
-  S.w3 = m3 * S.iD;
-  S.r = S.w1 * S.d1 + (1.0 - S.w1 - S.w3) * S.d2 + S.w3 * S.d3;
+__device__ __forceinline__ void walk_fwd(const double* __restrict__ q, long c, long st, Walk& W) {
+  const double* p = q + c - 3 * st;
+  const double q0 = p[0], q1 = p[st], q2 = p[2 * st], q3 = p[3 * st], q4 = p[4 * st], q5 = p[5 * st];
+  const double a5 = q1 - q0, a3 = q2 - q1, a1 = q3 - q2, b1 = q4 - q3, b3 = q5 - q4;
+  constexpr double c13 = 13.0 / 3.0;
+  W.t1a = fma(a3, -2.0, a5 + a1);
+  W.t2a = fma(a3, -4.0, fma(a1, 3.0, a5));
+  W.t1b = fma(a1, -2.0, a3 + b1);
+  W.t2b = a3 - b1;
+  W.t1c = fma(b1, -2.0, a1 + b3);
+  W.t2c = fma(b1, -4.0, fma(a1, 3.0, b3));
+  W.s1 = fma(W.t1a * c13, W.t1a, W.t2a * W.t2a);
+  W.s2 = fma(W.t1b * c13, W.t1b, W.t2b * W.t2b);
+  W.s3 = fma(W.t1c * c13, W.t1c, W.t2c * W.t2c);
+  W.x = W.s2 * W.s3;
+  W.y = W.s1 * W.s3;
+  W.z = W.s1 * W.s2;
+  W.X = W.x * W.x;
+  W.Y = fma(W.y, W.y, 1.0e-80 / 486.0);
+  W.Z = W.z * W.z;
+  W.D1 = fma(a1, 11.0 / 6.0, fma(a3, -7.0 / 6.0, a5 * (1.0 / 3.0)));
+  W.d2 = fma(b1, 2.0, fma(a1, 5.0, -a3));
+  W.D3 = fma(b1, 2.5, fma(b3, -0.5, a1));
+  const double num = fma(W.Z, W.D3, fma(W.Y, W.d2, W.X * W.D1));
+  W.iD = recip_nr(fma(W.X, 1.0 / 6.0, fma(W.Z, 0.5, W.Y)));
+  W.R = num * W.iD;
 }
-__device__ __forceinline__ void side_rev(const Side& S, double lr, double* la) {
-  const double w2 = 1.0 - S.w1 - S.w3;
-  const double ld1 = lr * S.w1, ld2 = lr * w2, ld3 = lr * S.w3;
-  const double lw1 = lr * (S.d1 - S.d2), lw3 = lr * (S.d3 - S.d2);
-  const double G = lw1 * S.w1 + lw3 * S.w3;
-  const double lm1 = (lw1 - G) * S.iD, lm2 = -G * S.iD, lm3 = (lw3 - G) * S.iD;
-  const double lP1 = 2.0 * S.P1 * lm1, lP2 = 12.0 * S.P2 * lm2, lP3 = 6.0 * S.P3 * lm3;
-  const double ls1 = lP2 * S.s3 + lP3 * S.s2, ls2 = lP1 * S.s3 + lP3 * S.s1, ls3 = lP1 * S.s2 + lP2 * S.s1;
-  const double lt0 = 26.0 * S.t[0] * ls1, lt1 = 6.0 * S.t[1] * ls1;
-  const double lt2 = 26.0 * S.t[2] * ls2, lt3 = 6.0 * S.t[3] * ls2;
-  const double lt4 = 26.0 * S.t[4] * ls3, lt5 = 6.0 * S.t[5] * ls3;
-  la[0] += 2.0 * ld1 + lt0 + lt1;
-  la[1] += -7.0 * ld1 - ld2 - 2.0 * lt0 - 4.0 * lt1 + lt2 + lt3;
-  la[2] += 11.0 * ld1 + 5.0 * ld2 + 2.0 * ld3 + lt0 + 3.0 * lt1 - 2.0 * lt2 + lt4 + 3.0 * lt5;
-  la[3] += 2.0 * ld2 + 5.0 * ld3 + lt2 - lt3 - 2.0 * lt4 - 4.0 * lt5;
-  la[4] += -ld3 + lt4 + lt5;
+// la[0..4] = lR dR/d(e) given g4 = 4 lR / den (lR the adjoint of R).  The factor
+// 4 stands for the two factors 2 of d(x^2) = 2x dx and d(t^2) = 2t dt, so the
+// smoothness-indicator terms need no constants; the terms through D1, d2, D3
+// divide it out in their coefficients.
+__device__ __forceinline__ void walk_rev(const Walk& W, double g4, double* la) {
+  constexpr double c13 = 13.0 / 3.0;
+  const double lD1 = g4 * W.X, ld2 = g4 * W.Y, lD3 = g4 * W.Z;  // 4 lR dR/d(D1, d2, D3)
+  const double lX = g4 * fma(W.R, -1.0 / 6.0, W.D1), lY = g4 * (W.d2 - W.R), lZ = g4 * fma(W.R, -0.5, W.D3);
+  const double lx = W.x * lX, ly = W.y * lY, lz = W.z * lZ;
+  const double S1 = fma(ly, W.s3, lz * W.s2), S2 = fma(lx, W.s3, lz * W.s1), S3 = fma(lx, W.s2, ly * W.s1);
+  const double lt1a = W.t1a * (c13 * S1), lt2a = W.t2a * S1;
+  const double lt1b = W.t1b * (c13 * S2), lt2b = W.t2b * S2;
+  const double lt1c = W.t1c * (c13 * S3), lt2c = W.t2c * S3;
+  la[0] = fma(lD1, 1.0 / 12.0, lt1a + lt2a);
+  la[1] = fma(lD1, -7.0 / 24.0, fma(ld2, -0.25, fma(lt1a, -2.0, fma(lt2a, -4.0, lt1b + lt2b))));
+  la[2] = fma(lD1, 11.0 / 24.0,
+              fma(ld2, 1.25, fma(lD3, 0.25, fma(lt2a, 3.0, fma(lt1b, -2.0, fma(lt2c, 3.0, lt1a + lt1c))))));
+  la[3] = fma(ld2, 0.5, fma(lD3, 0.625, fma(lt1c, -2.0, fma(lt2c, -4.0, lt1b - lt2b))));
+  la[4] = fma(lD3, -0.125, lt1c + lt2c);
 }
-// adjoint of  out += weno5_line(q, c, S, vel) * di  given lout: lD[0..5] = the
+// adjoint of  out += wdir(q, c, S, 4 vel, di/24)  given lout: lD[0..5] = the
 // adjoints of the six differences (dm5, dm3, dm1, dp1, dp3, dp5); returns lvel
 __device__ double wline_T(const double* __restrict__ q, long c, long S, double vel, double lout, double di,
                           double* lD) {
   for (int m = 0; m < 6; ++m) lD[m] = 0.0;
   const double lr = lout * di;
   if (lr == 0.0) return 0.0;
-  const double m3 = q[c - 3 * S], m2 = q[c - 2 * S], m1 = q[c - S], z0 = q[c], p1 = q[c + S], p2 = q[c + 2 * S],
-               p3 = q[c + 3 * S];
-  const double dm5 = -m3 + m2, dm3 = -m2 + m1, dm1 = -m1 + z0, dp1 = -z0 + p1, dp3 = -p1 + p2, dp5 = -p2 + p3;
-  // the upwind side (the other one carries the weight 0 in weno5.h), its inputs
-  // mirrored by selects so that one inlined copy serves both signs of vel
-  const bool neg = vel < 0.0;
-  Side A;
-  side_fwd(neg ? dp5 : dm5, neg ? dp3 : dm3, neg ? dp1 : dm1, neg ? dm1 : dp1, neg ? dm3 : dp3, A);
-  if (vel == 0.0) {  // both sides enter d(out)/d(vel); neither enters d(out)/d(q)
-    Side B;
-    side_fwd(dp5, dp3, dp1, dm1, dm3, B);
-    return lr * (A.r + B.r) / 12.0;
+  Walk A;
+  if (vel == 0.0) {
+    // both sides enter d(out)/d(vel) of weno5.h, (R_minus + R_plus)/12, where the
+    // walk from the plus end gives -R_plus; neither enters d(out)/d(q)
+    Walk B;
+    walk_fwd(q, c, S, A);
+    walk_fwd(q, c, -S, B);
+    return lr * (A.R - B.R) * (1.0 / 12.0);
   }
-  double la[5] = {0, 0, 0, 0, 0};
-  side_rev(A, lr * 2.0 * vel / 12.0, la);
-  lD[0] = neg ? 0.0 : la[0];
-  lD[1] = neg ? la[4] : la[1];
-  lD[2] = neg ? la[3] : la[2];
-  lD[3] = neg ? la[2] : la[3];
-  lD[4] = neg ? la[1] : la[4];
-  lD[5] = neg ? la[0] : 0.0;
-  return lr * 2.0 * A.r / 12.0;
+  const bool pos = vel > 0.0;
+  walk_fwd(q, c, pos ? S : -S, A);
+  // out = |vel|/6 di R, so lR = lr |vel| / 6 and g4 = 4 lR / den
+  double la[5];
+  walk_rev(A, (lr * fabs(vel)) * (2.0 / 3.0) * A.iD, la);
+  // walk differences: (dm5, dm3, dm1, dp1, dp3) for vel > 0, -(dp5, dp3, dp1, dm1,
+  // dm3) for vel < 0
+  lD[0] = pos ? la[0] : 0.0;
+  lD[1] = pos ? la[1] : -la[4];
+  lD[2] = pos ? la[2] : -la[3];
+  lD[3] = pos ? la[3] : -la[2];
+  lD[4] = pos ? la[4] : -la[1];
+  lD[5] = pos ? 0.0 : -la[0];
+  // d(out)/d(vel) = sign(vel) di R / 6
+  return lr * (pos ? A.R : -A.R) * (1.0 / 6.0);
 }
 
 // Offsets (relative to the cell) of the four velocity points that form the
@@ -278,9 +292,15 @@ void csf_T(cudaStream_t s, const Grid& g, double dxi, double dyi, double dzi, do
       // dN/dv = I/a - v v^T/(a^2 m) with m = |v|, a = m + vs:
       // lv = (l - v (v.l)/(m a)) / a, the factor formed as ((v.l)/m)/a, which stays
       // finite for any m > 0
+      // (division-free reciprocals where s2 is a normal number; subnormal and zero
+      // s2 take the library functions)
       const double s2 = r[0] * r[0] + r[1] * r[1] + r[2] * r[2];
       double ia, t = 0.0;
-      if (s2 > 0.0) {
+      if (s2 >= 0x1p-1000) {
+        const double im = rsqrt_nr(s2);
+        ia = recip_nr(s2 * im + vs);
+        t = ((r[0] * lx + r[1] * ly + r[2] * lz) * im) * ia;
+      } else if (s2 > 0.0) {
         const double im = rsqrt(s2);
         ia = 1.0 / (s2 * im + vs);
         t = ((r[0] * lx + r[1] * ly + r[2] * lz) * im) * ia;
