@@ -374,9 +374,10 @@ __device__ __forceinline__ double wall_col_T(const Grid& G, double* __restrict__
 // one thread per (column, wall, component) owning rows -2..2 (or nj-3..nj+3) of a
 // source column and its images: gathers them, applies the wall transpose, clears
 // the images;
-// [nbW, nbW + nb1): rows 3..nj-4 of the x-source columns (8 lanes per (j, k,
-// component), with the z and corner images where k has one); the rest: rows
-// 3..nj-4 of the columns with a z image only.  Each point has one owner.
+// [nbW, nbW + nb1): rows 3..nj-4 of the x-source columns, one thread per (j, k,
+// component) for its six slots, with the z and corner images where k has one; the
+// rest: rows 3..nj-4 of the columns with a z image only, one thread per (i, j,
+// component).  Each point has one owner.
 __global__ void __launch_bounds__(256) k_refresh_T(Grid G, int normal, double uwall, const double* __restrict__ wc,
                                                    const double* __restrict__ uk, const double* __restrict__ wk,
                                                    double* __restrict__ lu, double* __restrict__ lv,
@@ -410,50 +411,70 @@ __global__ void __launch_bounds__(256) k_refresh_T(Grid G, int normal, double uw
     }
     return;
   }
+  // Parts 1 and 2 take the six halo slots of a row (or column) in one thread: each
+  // slot's source and image are points no other slot touches, so every load is
+  // issued before any store (one memory round trip per thread).
   if (b < nbW + nb1) {
-    const long t = (long)(b - nbW) * 256 + threadIdx.x;
-    const int m = (int)(t & 7);
-    const long task = t >> 3;
+    const long task = (long)(b - nbW) * 256 + threadIdx.x;
     const int nj2 = NJ - 6;  // rows 3..nj-4
-    if (m >= 6 || task >= 3L * nj2 * (NK + 6)) return;
+    if (task >= 3L * nj2 * (NK + 6)) return;
     const int cmp = (int)(task / ((long)nj2 * (NK + 6)));
     const int rem = (int)(task % ((long)nj2 * (NK + 6)));
     const int j = 3 + rem % nj2, k = -2 + rem / nj2;
     const int sx = cmp == 0 ? shu : 0, sz = cmp == 2 ? shw : 0;
     if (halo_src(k, NK, sz) != k) return;  // a z destination: gathered by its source
-    const int d = halo_dest(m, NI, sx);
-    if (d == kNoHalo) return;
-    const int is = halo_src(d, NI, sx), kz = halo_image(k, NK, sz);
+    const int kz = halo_image(k, NK, sz);
     double* a = cmp == 0 ? lu : (cmp == 1 ? lv : lw);
-    const long c = G.at(is, j, k), e = G.at(d, j, k);
-    double v = a[c] + a[e];
-    a[e] = 0.0;
-    if (kz != kNoHalo) {
-      const long f = G.at(is, j, kz), h = G.at(d, j, kz);
-      v += a[f] + a[h];
-      a[f] = 0.0;
-      a[h] = 0.0;
+    double v[6];
+#pragma unroll
+    for (int m = 0; m < 6; ++m) {
+      const int d = halo_dest(m, NI, sx);
+      v[m] = d == kNoHalo ? 0.0 : a[G.at(halo_src(d, NI, sx), j, k)] + a[G.at(d, j, k)];
     }
-    a[c] = v;
+    if (kz != kNoHalo) {
+#pragma unroll
+      for (int m = 0; m < 6; ++m) {
+        const int d = halo_dest(m, NI, sx);
+        if (d != kNoHalo) v[m] += a[G.at(halo_src(d, NI, sx), j, kz)] + a[G.at(d, j, kz)];
+      }
+    }
+#pragma unroll
+    for (int m = 0; m < 6; ++m) {
+      const int d = halo_dest(m, NI, sx);
+      if (d == kNoHalo) continue;
+      const int is = halo_src(d, NI, sx);
+      a[G.at(d, j, k)] = 0.0;
+      if (kz != kNoHalo) {
+        a[G.at(is, j, kz)] = 0.0;
+        a[G.at(d, j, kz)] = 0.0;
+      }
+      a[G.at(is, j, k)] = v[m];
+    }
     return;
   }
   const long t = (long)(b - nbW - nb1) * 256 + threadIdx.x;
   const int nj2 = NJ - 6;
   const int i = 1 + (int)(t % (NI + 1));
-  long r = t / (NI + 1);
-  const int m = (int)(r % 6);
-  r /= 6;
+  const long r = t / (NI + 1);
   const int j = 3 + (int)(r % nj2);
   const int cmp = (int)(r / nj2);
   if (cmp >= 3) return;
   const int sx = cmp == 0 ? shu : 0, sz = cmp == 2 ? shw : 0;
   if (halo_src(i, NI, sx) != i || halo_image(i, NI, sx) != kNoHalo) return;  // x ghost, or done with its x image
-  const int d = halo_dest(m, NK, sz);
-  if (d == kNoHalo) return;
   double* a = cmp == 0 ? lu : (cmp == 1 ? lv : lw);
-  const long c = G.at(i, j, halo_src(d, NK, sz)), e = G.at(i, j, d);
-  a[c] += a[e];
-  a[e] = 0.0;
+  double v[6];
+#pragma unroll
+  for (int m = 0; m < 6; ++m) {
+    const int d = halo_dest(m, NK, sz);
+    v[m] = d == kNoHalo ? 0.0 : a[G.at(i, j, halo_src(d, NK, sz))] + a[G.at(i, j, d)];
+  }
+#pragma unroll
+  for (int m = 0; m < 6; ++m) {
+    const int d = halo_dest(m, NK, sz);
+    if (d == kNoHalo) continue;
+    a[G.at(i, j, halo_src(d, NK, sz))] = v[m];
+    a[G.at(i, j, d)] = 0.0;
+  }
 }
 void wall_T(cudaStream_t s, const Grid& g, double uwall, const double* wc, const double* uk, const double* wk,
             double* lu, double* lv, double* lw, double* lwc) {
@@ -475,8 +496,8 @@ void halo_z_T(cudaStream_t s, const Grid& g, int normal, double* lu, double* lv,
 void wall_halo_T(cudaStream_t s, const Grid& g, int normal, double uwall, const double* wc, const double* u,
                  const double* w, double* lu, double* lv, double* lw, double* lwc) {
   if (refresh_one_pass(g.ni, g.nj, g.nk)) {
-    const long tw = 6L * (g.ni + 6) * (g.nk + 6), t1 = 24L * (g.nj - 6) * (g.nk + 6),
-               t2 = 18L * (g.ni + 1) * (g.nj - 6);
+    const long tw = 6L * (g.ni + 6) * (g.nk + 6), t1 = 3L * (g.nj - 6) * (g.nk + 6),
+               t2 = 3L * (g.ni + 1) * (g.nj - 6);
     const int nbW = (int)((tw + 255) / 256), nb1 = (int)((t1 + 255) / 256), nb2 = (int)((t2 + 255) / 256);
     k_refresh_T<<<nbW + nb1 + nb2, 256, 0, s>>>(g, normal, uwall, wc, u, w, lu, lv, lw, lwc, nbW, nb1);
     count_launch();
