@@ -376,8 +376,9 @@ __global__ void __launch_bounds__(256) k_halo_x8(Grid g, int normal, double* __r
 // column's interior rows with that column's coefficients.  So the threads write
 // their points in any order.  Blocks [0, nbW): the wall rows of every column, one
 // thread per (column, wall); [nbW, nbW + nbX): the other rows of the x-ghost
-// columns, 8 lanes per (j, k, component); the rest: the other rows of the z-ghost
-// planes over the columns that are not x destinations.
+// columns, one thread per (j, k, component) for its six ghost slots; the rest: the
+// other rows of the z-ghost planes over the columns that are not x destinations,
+// one thread per (i, j, component).  A thread reads all its sources before writing.
 __global__ void __launch_bounds__(256) k_refresh(Grid g, int normal, double uwall, const double* __restrict__ wc,
                                                  double* __restrict__ uk, double* __restrict__ vk,
                                                  double* __restrict__ wk, int nbW, int nbX) {
@@ -440,35 +441,48 @@ __global__ void __launch_bounds__(256) k_refresh(Grid g, int normal, double uwal
     return;
   }
   if (b < nbW + nbX) {
-    const long t = (long)(b - nbW) * 256 + threadIdx.x;
-    const int m = (int)(t & 7);
-    const long task = t >> 3;
-    if (m >= 6 || task >= 3L * NJ * (NK + 6)) return;
+    const long task = (long)(b - nbW) * 256 + threadIdx.x;
+    if (task >= 3L * NJ * (NK + 6)) return;
     const int cmp = (int)(task / ((long)NJ * (NK + 6)));
     const int rem = (int)(task % ((long)NJ * (NK + 6)));
     const int j = 1 + rem % NJ, k = -2 + rem / NJ;
     if (cmp == 1 && j == NJ) return;  // a wall row of v
     const int sx = cmp == 0 ? shu : 0, sz = cmp == 2 ? shw : 0;
-    const int d = halo_dest(m, NI, sx);
-    if (d == kNoHalo) return;
+    const int ks = halo_src(k, NK, sz);
     double* a = cmp == 0 ? uk : (cmp == 1 ? vk : wk);
-    a[g.at(d, j, k)] = a[g.at(halo_src(d, NI, sx), j, halo_src(k, NK, sz))];
+    double v[6];
+#pragma unroll
+    for (int m = 0; m < 6; ++m) {
+      const int d = halo_dest(m, NI, sx);
+      v[m] = d == kNoHalo ? 0.0 : a[g.at(halo_src(d, NI, sx), j, ks)];
+    }
+#pragma unroll
+    for (int m = 0; m < 6; ++m) {
+      const int d = halo_dest(m, NI, sx);
+      if (d != kNoHalo) a[g.at(d, j, k)] = v[m];
+    }
     return;
   }
   const long t = (long)(b - nbW - nbX) * 256 + threadIdx.x;
   const int i = 1 + (int)(t % (NI + 1));
-  long r = t / (NI + 1);
-  const int m = (int)(r % 6);
-  r /= 6;
+  const long r = t / (NI + 1);
   const int j = 1 + (int)(r % NJ);
   const int cmp = (int)(r / NJ);
   if (cmp >= 3 || (cmp == 1 && j == NJ)) return;
   const int sx = cmp == 0 ? shu : 0, sz = cmp == 2 ? shw : 0;
   if (halo_src(i, NI, sx) != i) return;  // an x-ghost column: done above
-  const int d = halo_dest(m, NK, sz);
-  if (d == kNoHalo) return;
   double* a = cmp == 0 ? uk : (cmp == 1 ? vk : wk);
-  a[g.at(i, j, d)] = a[g.at(i, j, halo_src(d, NK, sz))];
+  double v[6];
+#pragma unroll
+  for (int m = 0; m < 6; ++m) {
+    const int d = halo_dest(m, NK, sz);
+    v[m] = d == kNoHalo ? 0.0 : a[g.at(i, j, halo_src(d, NK, sz))];
+  }
+#pragma unroll
+  for (int m = 0; m < 6; ++m) {
+    const int d = halo_dest(m, NK, sz);
+    if (d != kNoHalo) a[g.at(i, j, d)] = v[m];
+  }
 }
 // --- mixed precision: FP32 sweeps on the correction d = un - u ---------------------
 // During the solve un = u + d holds at every point, halos and wall ghosts included:
@@ -822,7 +836,7 @@ void wall_coef(cudaStream_t s, const Grid& g, double dy, const double* l1, const
 void wall_halo(cudaStream_t s, const Grid& g, int normal, double uwall, const double* wallc, double* un, double* vn,
                double* wn) {
   if (refresh_one_pass(g.ni, g.nj, g.nk)) {
-    const long tw = 2L * (g.ni + 6) * (g.nk + 6), tx = 24L * g.nj * (g.nk + 6), tz = 18L * (g.ni + 1) * g.nj;
+    const long tw = 2L * (g.ni + 6) * (g.nk + 6), tx = 3L * g.nj * (g.nk + 6), tz = 3L * (g.ni + 1) * g.nj;
     const int nbW = (int)((tw + 255) / 256), nbX = (int)((tx + 255) / 256), nbZ = (int)((tz + 255) / 256);
     k_refresh<<<nbW + nbX + nbZ, 256, 0, s>>>(g, normal, uwall, wallc, un, vn, wn, nbW, nbX);
     count_launch();
