@@ -18,6 +18,8 @@
 // refinement: the residual of the first sweep is formed in FP64 at u, then the
 // sweeps run in FP32 on the correction d = un - u (FP32 storage and arithmetic),
 // and un = u + d is formed in FP64 at the end.
+#include <cstdlib>
+
 #include "fused.cuh"
 #include "refresh.cuh"
 
@@ -242,7 +244,7 @@ __global__ void __launch_bounds__(256) k_wall(Grid g, double uwall, const double
   if (!side) {
     const long c = g.at(i, 1, k);
     const double u1 = uk[c], v1 = vk[c], v2 = vk[c + Y], w1 = wk[c];
-    const double u0 = c1 * (-uwall) + c2 * u1;
+    const double u0 = fma(c2, u1, c1 * (-uwall));  // one contraction, the same in k_refresh
     const double um1 = 2.0 * u0 - u1;
     uk[c - Y] = u0;
     uk[c - 2 * Y] = um1;
@@ -259,7 +261,7 @@ __global__ void __launch_bounds__(256) k_wall(Grid g, double uwall, const double
     const long c = g.at(i, NJ, k);
     const double u1 = uk[c], w1 = wk[c];
     const double vm1 = vk[c - Y], vm2 = vk[c - 2 * Y], vm3 = vk[c - 3 * Y];
-    const double u0 = c1 * uwall + c2 * u1;
+    const double u0 = fma(c2, u1, c1 * uwall);
     const double up2 = 2.0 * u0 - u1;
     uk[c + Y] = u0;
     uk[c + 2 * Y] = up2;
@@ -418,7 +420,7 @@ __global__ void __launch_bounds__(256) k_refresh(Grid g, int normal, double uwal
     const double c1 = wc[ou], c2 = wc[ou + 1];
     const long c = g.at(i, jw, k);
     const long t1 = side ? Y : -Y;
-    const double u0 = c1 * (side ? uwall : -uwall) + c2 * u1;
+    const double u0 = fma(c2, u1, c1 * (side ? uwall : -uwall));  // as k_wall
     const double um = 2.0 * u0 - u1;
     uk[c + t1] = u0;
     uk[c + 2 * t1] = um;
@@ -715,6 +717,128 @@ __global__ void __launch_bounds__(256) k_halo_z_d(Grid g, int normal, const floa
     }
   }
 }
+// k_wall_d, k_halo_x_d and k_halo_z_d in one pass (ni, nj, nk >= 8), composed as
+// k_refresh composes their FP64 counterparts, with the per-point constants added
+// in the same order (wall extrapolation of the source column, then + the x
+// constant of the source plane's row, then + the z constant of the final column's
+// row), so the result is bit for bit that of the three kernels.  Blocks [0, nbW):
+// the wall rows of every column, one thread per (column, wall); [nbW, nbW + nbX):
+// the other rows of the x-ghost columns, one thread per (j, k, component);
+// the rest: the other rows of the z-ghost planes of the columns that are not x
+// destinations, one thread per (i, j, component).
+__device__ __forceinline__ int gslot(int d, int N, int sh) { return d <= 0 ? d + 2 : d - N + 2 - sh; }
+__global__ void __launch_bounds__(256) k_refresh_d(Grid g, int normal, const float* __restrict__ gw,
+                                                   const float* __restrict__ gx, const float* __restrict__ gz,
+                                                   float* __restrict__ du, float* __restrict__ dv,
+                                                   float* __restrict__ dw, int nbW, int nbX) {
+  const int shu = !(normal & 1), shw = !(normal & 4);
+  const int NI = g.ni, NJ = g.nj, NK = g.nk;
+  // constant slots: x (per (k, j)): u 0, shifted u 6, v 12, w 18; z (per (j, i)): u 0,
+  // v 6, w 12, shifted w 18
+  auto xb = [&](int cmp) { return cmp == 0 ? (shu ? 6 : 0) : 6 * cmp + 6; };
+  auto zb = [&](int cmp) { return cmp == 2 ? (shw ? 18 : 12) : 6 * cmp; };
+  auto GX = [&](int j, int k, int slot) { return __ldg(gx + ((long)(k + 2) * (NJ + 6) + (j + 2)) * kGH + slot); };
+  auto GZ = [&](int i, int j, int slot) { return __ldg(gz + ((long)(j + 2) * (NI + 6) + (i + 2)) * kGH + slot); };
+  const int b = (int)blockIdx.x;
+  if (b < nbW) {
+    const long t = (long)b * 256 + threadIdx.x;
+    const int W = NI + 6;
+    if (t >= 2L * W * (NK + 6)) return;
+    const int i = (int)(t % W) - 2;
+    const int kk = (int)(t / W);
+    const int side = kk >= NK + 6 ? 1 : 0;
+    const int k = kk - side * (NK + 6) - 2;
+    const int jw = side ? NJ : 1, tj = side ? 1 : -1;
+    // value of ghost row j of this column from the source column's value v
+    auto compose = [&](float v, int cmp, int is, int ks, int j) {
+      if (is != i) v = v + GX(j, ks, xb(cmp) + gslot(i, NI, cmp == 0 ? shu : 0));
+      if (ks != k) v = v + GZ(i, j, zb(cmp) + gslot(k, NK, cmp == 2 ? shw : 0));
+      return v;
+    };
+    // u and w: q(g1) = c2 q1 + G1, q(g2) = 2 q(g1) - q1 + G2, q(g3) = 2 q(g2) - q(g1) + G3
+#pragma unroll
+    for (int cmp = 0; cmp < 3; cmp += 2) {
+      const int is = halo_src(i, NI, cmp == 0 ? shu : 0), ks = halo_src(k, NK, cmp == 2 ? shw : 0);
+      const float4* G4 = reinterpret_cast<const float4*>(gw + wall_slot(g, side, ks, is) * kGW);
+      const float4 a = __ldg(G4), e = __ldg(G4 + 2);
+      float* q = cmp == 0 ? du : dw;
+      const float q1 = q[g.at(is, jw, ks)];
+      const float c2 = a.x;
+      const float h1 = cmp == 0 ? a.y : e.x, h2 = cmp == 0 ? a.z : e.y, h3 = cmp == 0 ? a.w : e.z;
+      const float g1 = c2 * q1 + h1, g2 = 2.f * g1 - q1 + h2, g3 = 2.f * g2 - g1 + h3;
+      q[g.at(i, jw + tj, k)] = compose(g1, cmp, is, ks, jw + tj);
+      q[g.at(i, jw + 2 * tj, k)] = compose(g2, cmp, is, ks, jw + 2 * tj);
+      q[g.at(i, jw + 3 * tj, k)] = compose(g3, cmp, is, ks, jw + 3 * tj);
+    }
+    {
+      const int is = halo_src(i, NI, 0), ks = halo_src(k, NK, 0);
+      const float4 bb = __ldg(reinterpret_cast<const float4*>(gw + wall_slot(g, side, ks, is) * kGW) + 1);
+      const long c = g.at(is, jw, ks);
+      const long Y = g.sy;
+      if (!side) {  // v(0), v(-1), v(-2)
+        const float v1 = dv[c], v2 = dv[c + Y];
+        dv[g.at(i, 0, k)] = compose(bb.x, 1, is, ks, 0);
+        dv[g.at(i, -1, k)] = compose(-v1 + bb.y, 1, is, ks, -1);
+        dv[g.at(i, -2, k)] = compose(-v2 + bb.z, 1, is, ks, -2);
+      } else {  // v(nj), v(nj+1..nj+3)
+        const float v1 = dv[c - Y], v2 = dv[c - 2 * Y], v3 = dv[c - 3 * Y];
+        dv[g.at(i, NJ, k)] = compose(bb.x, 1, is, ks, NJ);
+        dv[g.at(i, NJ + 1, k)] = compose(-v1 + bb.y, 1, is, ks, NJ + 1);
+        dv[g.at(i, NJ + 2, k)] = compose(-v2 + bb.z, 1, is, ks, NJ + 2);
+        dv[g.at(i, NJ + 3, k)] = compose(-v3 + bb.w, 1, is, ks, NJ + 3);
+      }
+    }
+    return;
+  }
+  if (b < nbW + nbX) {
+    const long task = (long)(b - nbW) * 256 + threadIdx.x;
+    if (task >= 3L * NJ * (NK + 6)) return;
+    const int cmp = (int)(task / ((long)NJ * (NK + 6)));
+    const int rem = (int)(task % ((long)NJ * (NK + 6)));
+    const int j = 1 + rem % NJ, k = -2 + rem / NJ;
+    if (cmp == 1 && j == NJ) return;  // a wall row of v
+    const int sx = cmp == 0 ? shu : 0, sz = cmp == 2 ? shw : 0;
+    const int ks = halo_src(k, NK, sz);
+    float* a = cmp == 0 ? du : (cmp == 1 ? dv : dw);
+    float v[6];
+#pragma unroll
+    for (int m = 0; m < 6; ++m) {
+      const int d = halo_dest(m, NI, sx);
+      if (d == kNoHalo) {
+        v[m] = 0.f;
+        continue;
+      }
+      v[m] = a[g.at(halo_src(d, NI, sx), j, ks)] + GX(j, ks, xb(cmp) + gslot(d, NI, sx));
+      if (ks != k) v[m] = v[m] + GZ(d, j, zb(cmp) + gslot(k, NK, sz));
+    }
+#pragma unroll
+    for (int m = 0; m < 6; ++m) {
+      const int d = halo_dest(m, NI, sx);
+      if (d != kNoHalo) a[g.at(d, j, k)] = v[m];
+    }
+    return;
+  }
+  const long t = (long)(b - nbW - nbX) * 256 + threadIdx.x;
+  const int i = 1 + (int)(t % (NI + 1));
+  const long r = t / (NI + 1);
+  const int j = 1 + (int)(r % NJ);
+  const int cmp = (int)(r / NJ);
+  if (cmp >= 3 || (cmp == 1 && j == NJ)) return;
+  const int sx = cmp == 0 ? shu : 0, sz = cmp == 2 ? shw : 0;
+  if (halo_src(i, NI, sx) != i) return;  // an x-ghost column: done above
+  float* a = cmp == 0 ? du : (cmp == 1 ? dv : dw);
+  float v[6];
+#pragma unroll
+  for (int m = 0; m < 6; ++m) {
+    const int d = halo_dest(m, NK, sz);
+    v[m] = d == kNoHalo ? 0.f : a[g.at(i, j, halo_src(d, NK, sz))] + GZ(i, j, zb(cmp) + gslot(d, NK, sz));
+  }
+#pragma unroll
+  for (int m = 0; m < 6; ++m) {
+    const int d = halo_dest(m, NK, sz);
+    if (d != kNoHalo) a[g.at(i, j, d)] = v[m];
+  }
+}
 __global__ void k_to_float(long n, const double* __restrict__ a, float* __restrict__ b) {
   for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x)
     b[t] = (float)a[t];
@@ -742,6 +866,14 @@ __global__ void k_sum_parts2(const double* part, long n, double* out) {
     __syncthreads();
   }
   if (threadIdx.x == 0) out[0] = sh[0];
+}
+
+// The one-pass refresh kernels where the grid allows them, unless FMF_REFRESH_ORDERED
+// is set in the environment (then the ordered plane kernels, which give the same
+// values: the tests compare the two).
+bool one_pass_refresh(const Grid& g) {
+  static const bool ordered = std::getenv("FMF_REFRESH_ORDERED") != nullptr;
+  return !ordered && refresh_one_pass(g.ni, g.nj, g.nk);
 }
 
 VP make_vp(double dxinv, double dyinv, double dzinv, double dt, int harmonic) {
@@ -835,7 +967,7 @@ void wall_coef(cudaStream_t s, const Grid& g, double dy, const double* l1, const
 
 void wall_halo(cudaStream_t s, const Grid& g, int normal, double uwall, const double* wallc, double* un, double* vn,
                double* wn) {
-  if (refresh_one_pass(g.ni, g.nj, g.nk)) {
+  if (one_pass_refresh(g)) {
     const long tw = 2L * (g.ni + 6) * (g.nk + 6), tx = 3L * g.nj * (g.nk + 6), tz = 3L * (g.ni + 1) * g.nj;
     const int nbW = (int)((tw + 255) / 256), nbX = (int)((tx + 255) / 256), nbZ = (int)((tz + 255) / 256);
     k_refresh<<<nbW + nbX + nbZ, 256, 0, s>>>(g, normal, uwall, wallc, un, vn, wn, nbW, nbX);
@@ -914,6 +1046,13 @@ void sor_iteration_refine(cudaStream_t s, const Grid& g, double dxinv, double dy
 #undef FMF_PAIR
       },
       [&](int normal) {
+        if (one_pass_refresh(g)) {
+          const long tw = 2L * (g.ni + 6) * (g.nk + 6), tx = 3L * g.nj * (g.nk + 6), tz = 3L * (g.ni + 1) * g.nj;
+          const int nbW = (int)((tw + 255) / 256), nbX = (int)((tx + 255) / 256), nbZ = (int)((tz + 255) / 256);
+          k_refresh_d<<<nbW + nbX + nbZ, 256, 0, s>>>(g, normal, rb.gw, rb.gx, rb.gz, du, dv, dw, nbW, nbX);
+          count_launch();
+          return;
+        }
         k_wall_d<<<wall_grid(g), kB, 0, s>>>(g, rb.gw, du, dv, dw);
         k_halo_x_d<<<xh_grid(g), kB, 0, s>>>(g, normal, rb.gx, du, dv, dw);
         k_halo_z_d<<<zh_grid(g), kB, 0, s>>>(g, normal, rb.gz, du, dv, dw);
