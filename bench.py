@@ -187,10 +187,11 @@ def mixed_case(name, steps, warmup, stream):
     return out
 
 
-def adjoint_cost(K, stream, every):
-    """Adjoint/forward wall-clock ratio of the K-step rollout on the 128x64x64 Couette
-    workload (per-wall-cell angle 75 +- 5 deg), checkpoints every `every` steps (16 for
-    K = 200 as the workload states, about sqrt(K); 0: ceil(sqrt(K))):
+def adjoint_cost(K, stream, every, workload="couette128"):
+    """Adjoint/forward wall-clock ratio of the K-step rollout on a workload (default
+    the 128x64x64 Couette workload, per-wall-cell angle 75 +- 5 deg), checkpoints
+    every `every` steps (16 for K = 200 as the workload states, about sqrt(K);
+    0: ceil(sqrt(K))):
     fmf_adj_rollout (J and all gradients) against fmf_adj_forward (J) with the same
     solver settings (viscous solve to the reference's 1e-3, transposed solve to
     1e-6), and against the graph-replayed production step (fmf_ctx_step)."""
@@ -200,7 +201,7 @@ def adjoint_cost(K, stream, every):
     from fmf import config as C
     from fmf.adjoint import Adjoint
 
-    cfg = C.get("couette128")
+    cfg = C.get(workload)
     st0 = C.raw_state(cfg)
     walls = [w.copy() for w in C.wall_arrays(cfg)]
     every = every if every > 0 else int(math.ceil(math.sqrt(K)))
@@ -230,7 +231,7 @@ def adjoint_cost(K, stream, every):
     S.sync()
     t_ctx = time.perf_counter() - t0
     S.close()
-    return {"workload": f"couette128 {cfg.ni}x{cfg.nj}x{cfg.nk}", "K": K, "checkpoint_every": every,
+    return {"workload": f"{workload} {cfg.ni}x{cfg.nj}x{cfg.nk}", "K": K, "checkpoint_every": every,
             "objective": "find_interface_positions_lower after K steps", "J": J,
             "parameters": "theta0, zeta, l1, l2 (wall planes), initial phi",
             "forward_s": t_fwd, "rollout_s": t_adj, "adjoint_over_forward": t_adj / t_fwd,
@@ -249,11 +250,14 @@ def main():
     ap.add_argument("--workload", default=WORKLOAD)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--adjoint-steps", type=int, default=200,
-                    help="K of the adjoint-cost measurement on 128x64x64 (0: skip)")
+                    help="K of the adjoint-cost measurement (0: skip)")
     ap.add_argument("--mixed-workload", default="droplet512",
                     help="second FP64-vs-mixed measurement (the sessile-drop workload; '' to skip)")
     ap.add_argument("--adjoint-every", type=int, default=16,
                     help="checkpoint interval of the adjoint rollout (0: ceil(sqrt(K)))")
+    ap.add_argument("--adjoint-workload", default="couette128",
+                    help="workload of the adjoint-cost measurement (droplet256 with --adjoint-steps 500 "
+                         "--adjoint-every 0: the 256x128x128 sessile drop, K = 500, ceil(sqrt(K)) = 23)")
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed", "adjoint"], help="--profile only")
     ap.add_argument("--profile", action="store_true",
                     help="no timing: start-up pass, --warmup steps, then --steps steps (for ncu launch lists)")
@@ -426,7 +430,7 @@ def main():
         mixed_droplet = mixed_case(args.mixed_workload, 5, 3, stream)
     adjoint = None
     if rank == 0 and args.adjoint_steps > 0:
-        adjoint = adjoint_cost(args.adjoint_steps, stream, args.adjoint_every)
+        adjoint = adjoint_cost(args.adjoint_steps, stream, args.adjoint_every, args.adjoint_workload)
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         v, dt = cpu_baseline_sample(cfg, 1)
