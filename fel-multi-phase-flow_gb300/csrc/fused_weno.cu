@@ -4,12 +4,12 @@
 // weno5.h forms both one-sided reconstructions and multiplies the unused one by
 // vel-|vel| = 0 (or vel+|vel| = 0); here only the upwind side is evaluated, which
 // gives the same value and halves the FP64 work, in a rearranged form of the same
-// quotient (wdir) that needs about two thirds of the remaining FP64 operations.  The grid has one thread per
-// interior cell (x fastest, 32 x 4 block, one k plane per grid z).
+// quotient (wdir) that needs about two thirds of the remaining FP64 operations.
+// The grid has one thread per interior cell (x fastest, 32 x 4 block, one k plane
+// per grid z).
 #include "../../include/fmf_capi.h"
 #include "fused.cuh"
 #include "recip.cuh"
-#include "weno5_core.cuh"
 
 namespace fmf {
 namespace fused {
