@@ -16,6 +16,7 @@
 // interior row gets exactly one writer (solphi_mthinc1.f:121-130 zeroes first;
 // faces nobody donates through hold the zero written by k_classify's owner).
 #include "fused.cuh"
+#include "recip.cuh"
 
 namespace fmf {
 namespace fused {
@@ -23,6 +24,7 @@ namespace fused {
 namespace {
 struct MC {
   double gp1, gp2, lim, eps_trunc, bet, dt, dxi, dyi, dzi;
+  double lim2lo, lim2hi;  // lim^2 (1 -/+ 1e-12)
 };
 
 __device__ __forceinline__ double avg8(const double* __restrict__ p, long c, long X, long Y, long Z) {
@@ -34,21 +36,17 @@ __device__ __forceinline__ double avg8(const double* __restrict__ p, long c, lon
 __device__ __forceinline__ double ex(double x) { return exp(x); }
 __device__ __forceinline__ float ex(float x) { return expf(fminf(x, 80.0f)); }
 
-// sum over the 8 Gauss points of w/(1+exp(-2 bet (x_t + d))); optionally the sum of s(1-s)
-template <class R>
-__device__ __forceinline__ R sig8(const R* a, R w, R m2b, R d, R* sd) {
-  R s = 0, q = 0;
-#pragma unroll
-  for (int t = 0; t < 8; ++t) {
-    const R e = ex(m2b * (a[t] + d));
-    const R r = (R)1 / ((R)1 + e);
-    s += r;
-    if (sd) q += e * r * r;  // s(1-s) with 1-s = e/(1+e), exact in relative terms for any a
-  }
-  if (sd) *sd = q;
-  return w * s;
+// 1/(1+e) for e >= 0: the division-free reciprocal in double (an overflowed e gives
+// exactly 0, as the quotient does; NaN stays NaN), the quotient in float
+__device__ __forceinline__ double inv1p(double e) {
+  const double a = 1.0 + e;
+  return (__double2hiint(a) == 0x7ff00000 && __double2loint(a) == 0) ? 0.0 : recip_nr(a);
 }
-// The same sums with exp(m2b (a_t + d)) factorised: a_t = x + y + z over the Gauss
+__device__ __forceinline__ float inv1p(float e) { return 1.0f / (1.0f + e); }
+
+// The sum over the 8 Gauss points t of w/(1+exp(m2b (a_t + d))) (m2b = -2 bet) and,
+// optionally, the sum of s(1-s) (1-s = e/(1+e), exact in relative terms for any
+// a_t), with exp(m2b (a_t + d)) factorised: a_t = x + y + z over the Gauss
 // offsets of the three axes, so exp(m2b a_t) = X Y Z of per-axis factors (E_t,
 // gexp8) and only exp(m2b d) changes with d.  Every factor is bounded by the
 // normal's unit length times the Gauss offsets; where exp(m2b d) overflows or
@@ -60,14 +58,14 @@ __device__ __forceinline__ R sig8f(const R* E, R w, R ed, R* sd) {
 #pragma unroll
   for (int t = 0; t < 8; ++t) {
     const R e = E[t] * ed;
-    const R r = (R)1 / ((R)1 + e);
+    const R r = inv1p(e);
     s += r;
     if (sd) q += e * r * r;
   }
   if (sd) *sd = q;
   return w * s;
 }
-// E_t in gauss8's order (x fastest): factors X1 X2, Y1 Y2, Z1 Z2
+// E_t over the 8 Gauss points, x fastest, then y, then z: factors X1 X2, Y1 Y2, Z1 Z2
 template <class R>
 __device__ __forceinline__ void gexp8(R* E, R X1, R X2, R Y1, R Y2, R Z1, R Z2) {
   const R a = X1 * Y1, b = X2 * Y1, c = X1 * Y2, d = X2 * Y2;
@@ -80,19 +78,6 @@ __device__ __forceinline__ void gexp8(R* E, R X1, R X2, R Y1, R Y2, R Z1, R Z2) 
   E[6] = c * Z2;
   E[7] = d * Z2;
 }
-template <class R>
-__device__ __forceinline__ void gauss8(R* a, R rnx, R rny, R rnz, R x1g, R x2g, R y1g, R y2g, R z1g, R z2g) {
-  const R x1 = rnx * x1g, x2 = rnx * x2g, y1 = rny * y1g, y2 = rny * y2g, z1 = rnz * z1g, z2 = rnz * z2g;
-  a[0] = x1 + y1 + z1;
-  a[1] = x2 + y1 + z1;
-  a[2] = x1 + y2 + z1;
-  a[3] = x2 + y2 + z1;
-  a[4] = x1 + y1 + z2;
-  a[5] = x2 + y1 + z2;
-  a[6] = x1 + y2 + z2;
-  a[7] = x2 + y2 + z2;
-}
-
 __global__ void __launch_bounds__(256) k_classify(Grid g, MC m, const double* __restrict__ phi,
                                                   const double* __restrict__ gx, const double* __restrict__ gy,
                                                   const double* __restrict__ gz, const double* __restrict__ u,
@@ -107,10 +92,12 @@ __global__ void __launch_bounds__(256) k_classify(Grid g, MC m, const double* __
   const long X = 1, Y = g.sy, Z = g.sz;
   const long c = g.at(i, j, k);
   const double rnx = avg8(gx, c, X, Y, Z), rny = avg8(gy, c, X, Y, Z), rnz = avg8(gz, c, X, Y, Z);
-  const double q00 = sqrt(rnx * rnx + rny * rny + rnz * rnz);
+  const double q2 = rnx * rnx + rny * rny + rnz * rnz;
   const double uw = __ldg(u + c - X), ue = __ldg(u + c), vs = __ldg(v + c - Y), vn = __ldg(v + c),
                wb = __ldg(w + c - Z), wt = __ldg(w + c);
-  const bool band = !(q00 <= m.lim);
+  // the band test sqrt(q2) <= lim of the reference: decided on q2 against lim^2
+  // where q2 is clearly on one side, with the square root only within 1e-12 of it
+  const bool band = q2 < m.lim2lo ? false : (q2 > m.lim2hi ? true : !(sqrt(q2) <= m.lim));
   if (band) {
     const int slot = atomicAdd(count, 1);
     list[slot] = (int)c;
@@ -175,7 +162,7 @@ __global__ void __launch_bounds__(128) k_band(Grid g, MC m, const double* __rest
       const R f = sig8f<R>(E, (R)0.125, ex(m2b * ddd), &sd) - ph;
       // df = 0.5 bet sum 0.125/cosh^2 = 0.5 bet * 0.125 * 4 * sum s(1-s)
       const R df = (R)0.25 * bet * sd;
-      step = f * df / (df * df + reg);
+      step = sizeof(R) == 8 ? (R)((double)(f * df) * recip_nr((double)(df * df + reg))) : f * df / (df * df + reg);
       const R dn = ddd - step;
       // once d no longer changes, every remaining iteration recomputes the same
       // f, df and step: stopping here is the ten-step result bit for bit.  In
@@ -224,6 +211,8 @@ void mthinc_fluxes(cudaStream_t s, const Grid& g, double dxinv, double dyinv, do
   const double dcellinv = 1.0 / std::sqrt((dx * dx + dy * dy + dz * dz) / 3.0);
   const double ch = std::cosh(-bet * 1.5);
   m.lim = bet / (2.0 * (ch * ch)) * dcellinv;
+  m.lim2lo = m.lim * m.lim * (1.0 - 1.0e-12);
+  m.lim2hi = m.lim * m.lim * (1.0 + 1.0e-12);
   m.eps_trunc = 0.5 * (std::tanh(-bet * 2.5) + 1.0);
   m.bet = bet;
   m.dt = dt;

@@ -21,6 +21,7 @@
 #include <cstdlib>
 
 #include "fused.cuh"
+#include "recip.cuh"
 #include "refresh.cuh"
 
 namespace fmf {
@@ -66,8 +67,8 @@ __global__ void __launch_bounds__(256) k_edges(Grid g, VP p, const double* __res
 
 // cal_srcu.f:53-137 fused with the update factors: src is formed in registers and
 // only A = 0.5/(rho00*D), B = src/D are stored.  With T = 1/(rho00/dt + a_p/2)
-// these are A = T/2 and B = (rho00*(explicit terms) - prs + vis/2)*T: one division
-// per component.
+// these are A = T/2 and B = (rho00*(explicit terms) - prs + vis/2)*T: one
+// reciprocal per component (recip_nr: Newton-Raphson, no division).
 struct SrcIn {
   const double *u, *v, *w, *rho, *rhon, *adv[3], *advo[3], *prs[3], *vis[3], *fst[3], *fstn[3];
   double grvb, grvp;
@@ -113,7 +114,7 @@ __global__ void __launch_bounds__(256) k_src_ab(Grid g, VP p, SrcIn in, const do
     const double r = (r0 + __ldg(in.rho + c + X) + n0 + __ldg(in.rhon + c + X)) * 0.25;
     const double ap = p.dz2 * __ldg(exz + c - Z) + p.dy2 * __ldg(exy + c - Y) + p.dx2 * __ldg(mu + c) * 2.0 +
                       p.dx2 * __ldg(mu + c + X) * 2.0 + p.dy2 * __ldg(exy + c) + p.dz2 * __ldg(exz + c);
-    const double T = 1.0 / (r * p.dtinv + ap * 0.5);
+    const double T = recip_nr(r * p.dtinv + ap * 0.5);
     const double vn = REFINE ? visn_at<0, double>(g, p, c, mu, exy, exz, eyz, in.u, in.v, in.w) : 0.0;
     store(0, 0.5 * T, rsrc(0, in.u, r, in.grvb) * T, vn, in.u);
   }
@@ -121,7 +122,7 @@ __global__ void __launch_bounds__(256) k_src_ab(Grid g, VP p, SrcIn in, const do
     const double r = (r0 + __ldg(in.rho + c + Y) + n0 + __ldg(in.rhon + c + Y)) * 0.25;
     const double ap = p.dz2 * __ldg(eyz + c - Z) + p.dy2 * __ldg(mu + c) * 2.0 + p.dx2 * __ldg(exy + c - X) +
                       p.dx2 * __ldg(exy + c) + p.dy2 * __ldg(mu + c + Y) * 2.0 + p.dz2 * __ldg(eyz + c);
-    const double T = 1.0 / (r * p.dtinv + ap * 0.5);
+    const double T = recip_nr(r * p.dtinv + ap * 0.5);
     const double vn = REFINE ? visn_at<1, double>(g, p, c, mu, exy, exz, eyz, in.u, in.v, in.w) : 0.0;
     store(1, 0.5 * T, rsrc(1, in.v, r, in.grvp) * T, vn, in.v);
   }
@@ -129,7 +130,7 @@ __global__ void __launch_bounds__(256) k_src_ab(Grid g, VP p, SrcIn in, const do
     const double r = (r0 + __ldg(in.rho + c + Z) + n0 + __ldg(in.rhon + c + Z)) * 0.25;
     const double ap = p.dz2 * __ldg(mu + c) * 2.0 + p.dy2 * __ldg(eyz + c - Y) + p.dx2 * __ldg(exz + c - X) +
                       p.dx2 * __ldg(exz + c) + p.dy2 * __ldg(eyz + c) + p.dz2 * __ldg(mu + c + Z) * 2.0;
-    const double T = 1.0 / (r * p.dtinv + ap * 0.5);
+    const double T = recip_nr(r * p.dtinv + ap * 0.5);
     const double vn = REFINE ? visn_at<2, double>(g, p, c, mu, exy, exz, eyz, in.u, in.v, in.w) : 0.0;
     store(2, 0.5 * T, rsrc(2, in.w, r, 0.0) * T, vn, in.w);
   }
