@@ -72,9 +72,11 @@ __device__ double wline_T(const double* __restrict__ q, long c, long S, double v
                           double* lD) {
   for (int m = 0; m < 6; ++m) lD[m] = 0.0;
   const double lr = lout * di;
-  if (lr == 0.0) return 0.0;
+  // zero and sign tested on the bits (no FP64-pipe comparison)
+  if ((__double_as_longlong(lr) << 1) == 0) return 0.0;
+  const long long vb = __double_as_longlong(vel);
   Walk A;
-  if (vel == 0.0) {
+  if ((vb << 1) == 0) {
     // both sides enter d(out)/d(vel) of weno5.h, (R_minus + R_plus)/12, where the
     // walk from the plus end gives -R_plus; neither enters d(out)/d(q)
     Walk B;
@@ -82,7 +84,7 @@ __device__ double wline_T(const double* __restrict__ q, long c, long S, double v
     walk_fwd(q, c, -S, B);
     return lr * (A.R - B.R) * (1.0 / 12.0);
   }
-  const bool pos = vel > 0.0;
+  const bool pos = vb > 0;
   walk_fwd(q, c, pos ? S : -S, A);
   // out = |vel|/6 di R, so lR = lr |vel| / 6 and g4 = 4 lR / den
   double la[5];

@@ -33,8 +33,11 @@ namespace {
 //    the same value with fewer FP64 operations.
 // kx = dxi / 24.
 __device__ __forceinline__ double wdir(const double* __restrict__ q, long c, long S, double vsum, double kx) {
-  if (vsum == 0.0) return 0.0;
-  const long st = vsum > 0.0 ? S : -S;
+  // zero and sign tested on the bits (a double comparison would take an FP64-pipe
+  // slot): +-0 return 0; a positive sign bit walks from c - 3S
+  const long long vb = __double_as_longlong(vsum);
+  if ((vb << 1) == 0) return 0.0;
+  const long st = vb > 0 ? S : -S;
   const double* p = q + c - 3 * st;
   const double q0 = __ldg(p), q1 = __ldg(p + st), q2 = __ldg(p + 2 * st), q3 = __ldg(p + 3 * st),
                q4 = __ldg(p + 4 * st), q5 = __ldg(p + 5 * st);

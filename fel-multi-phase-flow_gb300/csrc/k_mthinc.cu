@@ -3,6 +3,7 @@
 // Arithmetic follows the reference operation by operation (this file is compiled
 // with -fmad=false so no multiply-add is fused), so results differ from the host
 // original only through the device exp/cosh/tanh.
+#include "recip.cuh"
 #include "ops.cuh"
 
 namespace fmf {
@@ -181,12 +182,17 @@ void solphi_mthinc3(cudaStream_t s, const Grid& g, double dxinv, double dyinv, d
                     double* phin, double* sums) {
   const Grid G = g;
   const MthincConst M = mthinc_const(dxinv, dyinv, dzinv, bet);
+  // the band test sqrt(q2) <= lim decided on q2 against lim^2 where q2 is clearly on
+  // one side, with the square root only within 1e-12 of it
+  const double lim = M.eps_mthinc * M.dcellinv;
+  const double lim2lo = lim * lim * (1.0 - 1.0e-12), lim2hi = lim * lim * (1.0 + 1.0e-12);
   range3(s, 0, g.ni + 1, 0, g.nj + 1, 0, g.nk + 1, [=] __device__(int i, int j, int k) {
     const long X = 1, Y = G.sy, Z = G.sz;
     const long c = G.at(i, j, k);
     const double rnx = avg8(phix, c, X, Y, Z), rny = avg8(phiy, c, X, Y, Z), rnz = avg8(phiz, c, X, Y, Z);
-    const double q00 = sqrt(rnx * rnx + rny * rny + rnz * rnz);
-    if (q00 <= M.eps_mthinc * M.dcellinv) {
+    const double q2 = rnx * rnx + rny * rny + rnz * rnz;
+    const bool outside = q2 < lim2lo ? true : (q2 > lim2hi ? false : sqrt(q2) <= lim);
+    if (outside) {
       double p = phin[c];
       if (p <= M.eps_trunc) p = 0.0;
       if (1.0 - p <= M.eps_trunc) p = 1.0;
@@ -209,7 +215,8 @@ void solphi_mthinc3(cudaStream_t s, const Grid& g, double dxinv, double dyinv, d
       sums);
   range3(s, 1, g.ni, 1, g.nj, 1, g.nk, [=] __device__(int i, int j, int k) {
     const long c = G.at(i, j, k);
-    const double offset = (sums[0] - sums[1]) / (sums[2] + 1.0e-99);
+    // (sums[2] >= 0: the reciprocal by Newton-Raphson, no division per cell)
+    const double offset = (sums[0] - sums[1]) * recip_nr(sums[2] + 1.0e-99);
     double p = phin[c];
     p = p + offset * (p * p) * (1.0 - p);
     p = fmin(p, 1.0);

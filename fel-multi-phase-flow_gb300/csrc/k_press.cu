@@ -8,6 +8,7 @@
 #include <map>
 #include <vector>
 
+#include "recip.cuh"
 #include "ops.cuh"
 
 namespace fmf {
@@ -225,7 +226,7 @@ __global__ void __launch_bounds__(128) k_tdma(Grid g, double dx2r, double dz2r, 
   for (int j = 1; j <= NJ; ++j) {
     const double ap = ap_f[j + 2] + dx2r * (2.0 - c1x) + dz2r * (2.0 - c1z);
     const double d00 = -ap + as_f[j + 2] * a_prev;
-    const double apinv = -d00 / (d00 * d00 + 1.0e-99);
+    const double apinv = -d00 * recip_nr(fma(d00, d00, 1.0e-99));  // Newton-Raphson, no division
     const double a = apinv * an_f[j + 2];
     const long o = base + (long)NI * (j - 1);
     br = apinv * (-pr[o] + as_f[j + 2] * br);
