@@ -57,6 +57,12 @@ void sor_iteration(cudaStream_t s, const Grid& g, double dxinv, double dyinv, do
                    double* un, double* vn, double* wn, double* part, double* errsum);
 long sor_parts(const Grid& g);
 
+// The pressure Poisson solve (solp_fft_tdma1-3) on the half spectrum of the real
+// divergence: div -> dp interior.  pr, pi: (ni/2+1) nj nk doubles each (the spectrum
+// after the forward transform and the Thomas solve).
+void pressure_half(cudaStream_t s, const Grid& g, double rho, double dxinv, double dzinv, const double* as_f,
+                   const double* an_f, const double* ap_f, const double* div, double* pr, double* pi, double* dp);
+
 // Mixed-precision viscous solve (one step of iterative refinement).  Buffers:
 struct RefineBufs {
   float* d[3];  // corrections d = un - u, v, w (n floats each)

@@ -434,9 +434,7 @@ static void seg_post(fmf_ctx* c) {
   // :625-646
   fused::wall_halo(s, g, 7, P.uwall, c->wallc, c->un, c->vn, c->wn);
   op::caldiv(s, g, dxinv, dyinv, dzinv, dt, c->un, c->vn, c->wn, c->div, nullptr);
-  op::fft_forward_planes(s, g, c->div, c->pr, c->pi);
-  op::tdma_modes(s, g, P.rhog, dxinv, dzinv, c->as_f, c->an_f, c->ap_f, c->pr, c->pi);
-  op::fft_inverse_planes(s, g, c->pr, c->pi, c->dp);
+  fused::pressure_half(s, g, P.rhog, dxinv, dzinv, c->as_f, c->an_f, c->ap_f, c->div, c->pr, c->pi, c->dp);
   op::bnd_avzero(s, g, c->dp);
   op::bnd_neumann(s, g, c->dp);
   op::bnd_periodic(s, g, c->dp);
@@ -540,9 +538,7 @@ int fmf_ctx_time_stage(fmf_ctx* c, int stage, int reps, float* ms) {
                                c->un, c->vn, c->wn, c->sorpart, c->red + 8);
         break;
       case 2:
-        op::fft_forward_planes(s, g, c->div, c->pr, c->pi);
-        op::tdma_modes(s, g, P.rhog, dxinv, dzinv, c->as_f, c->an_f, c->ap_f, c->pr, c->pi);
-        op::fft_inverse_planes(s, g, c->pr, c->pi, c->dp);
+        fused::pressure_half(s, g, P.rhog, dxinv, dzinv, c->as_f, c->an_f, c->ap_f, c->div, c->pr, c->pi, c->dp);
         break;
       case 3:
         fused::mthinc_fluxes(s, g, dxinv, dyinv, dzinv, P.dt, P.bet_mthinc, c->phi + n, c->phix, c->phiy,
