@@ -469,9 +469,7 @@ int record_step(fmf_adj* a) {
   // :625-661
   fused::wall_halo(s, g, 7, P.uwall, a->wallc, a->un[0], a->un[1], a->un[2]);
   op::caldiv(s, g, dxi, dyi, dzi, dt, a->un[0], a->un[1], a->un[2], a->div, nullptr);
-  op::fft_forward_planes(s, g, a->div, a->pr, a->pi);
-  op::tdma_modes(s, g, P.rhog, dxi, dzi, a->as_f, a->an_f, a->ap_f, a->pr, a->pi);
-  op::fft_inverse_planes(s, g, a->pr, a->pi, a->dp);
+  fused::pressure_half(s, g, P.rhog, dxi, dzi, a->as_f, a->an_f, a->ap_f, a->div, a->pr, a->pi, a->dp);
   op::bnd_avzero(s, g, a->dp);
   op::bnd_neumann(s, g, a->dp);
   op::bnd_periodic(s, g, a->dp);
@@ -551,9 +549,7 @@ void reverse_step(fmf_adj* a, const double* st) {
   adj::periodic_T(s, g, a->ldp);
   adj::neumann_T(s, g, a->ldp);
   adj::avzero_T(s, g, a->ldp);
-  op::fft_forward_planes(s, g, a->ldp, a->pr, a->pi);
-  op::tdma_modes(s, g, P.rhog, dxi, dzi, a->as_f, a->an_f, a->ap_f, a->pr, a->pi);
-  op::fft_inverse_planes(s, g, a->pr, a->pi, a->ldiv);
+  fused::pressure_half(s, g, P.rhog, dxi, dzi, a->as_f, a->an_f, a->ap_f, a->ldp, a->pr, a->pi, a->ldiv);
   adj::caldiv_T(s, g, dxi, dyi, dzi, dt, a->ldiv, a->lun[0], a->lun[1], a->lun[2]);
   check_stage(a, "poisson");
   adj::wall_halo_T(s, g, 7, P.uwall, a->wallc, a->ustar[0], a->ustar[2], a->lun[0], a->lun[1], a->lun[2], a->lwc);
