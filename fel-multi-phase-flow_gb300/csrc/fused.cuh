@@ -15,6 +15,11 @@ void weno5_both(cudaStream_t s, const Grid& g, double dxi, double dyi, double dz
                 const double* v, const double* w, const double* uo, const double* vo, const double* wo,
                 double* const* adv, double* const* advo, bool fp32 = false, float2* split = nullptr);
 
+// cal_grad_p2a (the vertex gradients of q at (i+1/2, j+1/2, k+1/2), i, j, k in
+// -2..n+2) in fewer FP64 operations than the reference's order
+void vertex_gradient(cudaStream_t s, const Grid& g, double dxinv, double dyinv, double dzinv, const double* q,
+                     double* qx, double* qy, double* qz);
+
 // solphi_mthinc1 for the faces solphi_mthinc2 reads (every face of rows 1..n in
 // the two directions normal to it, faces 0..n along it); list/count: device scratch
 // of >= (ni+2)(nj+2)(nk+2) ints and one int.  newton (optional, 2 (ni+2)(nj+2)(nk+2)

@@ -198,7 +198,37 @@ __global__ void __launch_bounds__(128) k_band(Grid g, MC m, const double* __rest
     if (wt > 0.0) side(wt, m.dzi, 2, false, fz + c);
   }
 }
+// cal_grad_p2a.f:46-60 for the fused step: the vertex gradient at (i+1/2, j+1/2,
+// k+1/2), i, j, k in -2..n+2, from the 8 surrounding points.  Per (i, j) corner the
+// sum s and difference d of the two k planes; with ta = s(+,+) - s(0,0) and
+// tb = s(+,0) - s(0,+) the x sum is ta + tb, the y sum ta - tb and the z sum the
+// four differences: 18 FP64 operations per point instead of the reference's 27.
+__global__ void __launch_bounds__(256) k_vertex_grad(Grid g, double cx, double cy, double cz,
+                                                     const double* __restrict__ q, double* __restrict__ qx,
+                                                     double* __restrict__ qy, double* __restrict__ qz) {
+  const int i = -2 + (int)(blockIdx.x * blockDim.x + threadIdx.x);
+  const int j = -2 + (int)(blockIdx.y * blockDim.y + threadIdx.y);
+  const int k = -2 + (int)blockIdx.z;
+  if (i > g.ni + 2 || j > g.nj + 2) return;
+  const long X = 1, Y = g.sy, Z = g.sz;
+  const long c = g.at(i, j, k);
+  const double q000 = __ldg(q + c), qp00 = __ldg(q + c + X), q0p0 = __ldg(q + c + Y), qpp0 = __ldg(q + c + X + Y),
+               q00p = __ldg(q + c + Z), qp0p = __ldg(q + c + X + Z), q0pp = __ldg(q + c + Y + Z),
+               qppp = __ldg(q + c + X + Y + Z);
+  const double s00 = q000 + q00p, sp0 = qp00 + qp0p, s0p = q0p0 + q0pp, spp = qpp0 + qppp;
+  const double ta = spp - s00, tb = sp0 - s0p;
+  qx[c] = (ta + tb) * cx;
+  qy[c] = (ta - tb) * cy;
+  qz[c] = ((q00p - q000) + (qp0p - qp00) + ((q0pp - q0p0) + (qppp - qpp0))) * cz;
+}
 }  // namespace
+
+void vertex_gradient(cudaStream_t s, const Grid& g, double dxinv, double dyinv, double dzinv, const double* q,
+                     double* qx, double* qy, double* qz) {
+  const dim3 b(32, 8, 1), gr((unsigned)((g.ni + 5 + 31) / 32), (unsigned)((g.nj + 5 + 7) / 8), (unsigned)(g.nk + 5));
+  k_vertex_grad<<<gr, b, 0, s>>>(g, 0.25 * dxinv, 0.25 * dyinv, 0.25 * dzinv, q, qx, qy, qz);
+  count_launch();
+}
 
 void mthinc_fluxes(cudaStream_t s, const Grid& g, double dxinv, double dyinv, double dzinv, double dt, double bet,
                    const double* phi, const double* gx, const double* gy, const double* gz, const double* u,

@@ -317,14 +317,14 @@ static void seg_pre(fmf_ctx* c) {
   double* phin0 = c->phin;
   double* phin1 = c->phin + n;
   // :491-503 transport
-  op::cal_grad_p2a(s, g, dxinv, dyinv, dzinv, phi1, c->phix, c->phiy, c->phiz);
+  fused::vertex_gradient(s, g, dxinv, dyinv, dzinv, phi1, c->phix, c->phiy, c->phiz);
   {
     const long nb = (long)(g.ni + 2) * (g.nj + 2) * (g.nk + 2);
     fused::mthinc_fluxes(s, g, dxinv, dyinv, dzinv, dt, P.bet_mthinc, phi1, c->phix, c->phiy, c->phiz, c->u, c->v,
                          c->w, c->flx, c->fly, c->flz, c->band, c->band + nb, P.precision == FMF_MIXED);
   }
   op::solphi_mthinc2(s, g, dxinv, dyinv, dzinv, dt, c->u, c->v, c->w, c->flx, c->fly, c->flz, phi1, phin1);
-  op::cal_grad_p2a(s, g, dxinv, dyinv, dzinv, phin1, c->phix, c->phiy, c->phiz);
+  fused::vertex_gradient(s, g, dxinv, dyinv, dzinv, phin1, c->phix, c->phiy, c->phiz);
   op::solphi_mthinc3(s, g, dxinv, dyinv, dzinv, P.bet_mthinc, c->phix, c->phiy, c->phiz, phi1, phin1, c->red);
   op::gnbc(s, g, c->u, c->w, P.uwall, c->theta0, P.sigma, c->zeta, c->theta);
   op::bnd_contact_angle(s, g, phin1, c->theta, P.dx, P.dy, P.dz);
@@ -396,10 +396,10 @@ static void csf_dropin(fmf_ctx* c, const double* phi1, const double* phin1) {
     op::fill(s, n, c->sfstn[q], 0.0);
   }
   static const int offs[4][3] = {{1, 1, 1}, {0, 0, 1}, {0, 1, 0}, {1, 0, 0}};
-  op::cal_grad_p2a(s, g, dxinv, dyinv, dzinv, phi1, c->phix, c->phiy, c->phiz);
+  fused::vertex_gradient(s, g, dxinv, dyinv, dzinv, phi1, c->phix, c->phiy, c->phiz);
   for (int q = 0; q < 4; ++q)
     op::calrn(s, g, dxinv, dyinv, dzinv, offs[q][0], offs[q][1], offs[q][2], c->phix, c->phiy, c->phiz, c->rn[q]);
-  op::cal_grad_p2a(s, g, dxinv, dyinv, dzinv, phin1, c->phix, c->phiy, c->phiz);
+  fused::vertex_gradient(s, g, dxinv, dyinv, dzinv, phin1, c->phix, c->phiy, c->phiz);
   for (int q = 0; q < 4; ++q)
     op::calrn(s, g, dxinv, dyinv, dzinv, offs[q][0], offs[q][1], offs[q][2], c->phix, c->phiy, c->phiz, c->rnn[q]);
   op::calrkap(s, g, dxinv, dyinv, dzinv, c->rn[0], c->rn[1], c->rn[2], c->rn[3], c->rkap);
