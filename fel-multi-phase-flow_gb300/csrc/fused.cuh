@@ -39,6 +39,11 @@ void csf_force(cudaStream_t s, const Grid& g, double dxinv, double dyinv, double
                double sigma, const double* phi, double* fu, double* fv, double* fw, bool fp32 = false,
                double* kap = nullptr);
 
+// The explicit viscous term (calsij, cal_arith_tau, cal_div_tensor) at the interior
+// u, v, w points into vis[0..2]; tau: 6 n doubles of workspace
+void explicit_viscous(cudaStream_t s, const Grid& g, double dxinv, double dyinv, double dzinv, const double* u,
+                      const double* v, const double* w, const double* mu, double* tau, double* const* vis);
+
 // Viscous solve.  src_visc_prep: edge viscosities E[0..2] (xy, xz, yz edges, i,j,k in
 // 0..n), per-component A/B (AB[0..5] = Au Bu Av Bv Aw Bw) with the momentum
 // right-hand side of cal_srcu formed in registers, and the Navier-slip wall

@@ -136,6 +136,57 @@ __global__ void __launch_bounds__(256) k_src_ab(Grid g, VP p, SrcIn in, const do
   }
 }
 
+// The explicit viscous term 2 div(mu S) of main.f90:538-541 (calsij, cal_arith_tau,
+// cal_div_tensor) for the interior u, v, w points, which are all the step reads.
+// k_stress forms the six stresses over i, j, k in 0..n+1 (the points the interior
+// divergence reads) straight from u, v, w and mu: tau_ii = 2 mu S_ii and, on the
+// edges, tau_ij = 2 (mean of 4 mu) S_ij with S_ij = (du_i/dx_j + du_j/dx_i)/2,
+// the factors 2, 1/2 and 1/4 folded into the constants; the strain never goes
+// through memory.  k_div_stress takes its divergence on the interior.
+__global__ void __launch_bounds__(256) k_stress(Grid g, double dxi, double dyi, double dzi,
+                                                const double* __restrict__ u, const double* __restrict__ v,
+                                                const double* __restrict__ w, const double* __restrict__ mu,
+                                                double* __restrict__ tau) {
+  const int i = (int)(blockIdx.x * blockDim.x + threadIdx.x);
+  const int j = (int)(blockIdx.y * blockDim.y + threadIdx.y);
+  const int k = (int)blockIdx.z;
+  if (i > g.ni + 1 || j > g.nj + 1) return;
+  const long X = 1, Y = g.sy, Z = g.sz, n = g.n;
+  const long c = g.at(i, j, k);
+  const double m0 = __ldg(mu + c), mx = __ldg(mu + c + X), my = __ldg(mu + c + Y), mz = __ldg(mu + c + Z);
+  const double u0 = __ldg(u + c), v0 = __ldg(v + c), w0 = __ldg(w + c);
+  const double hx = 0.25 * dxi, hy = 0.25 * dyi, hz = 0.25 * dzi;
+  tau[c] = (u0 - __ldg(u + c - X)) * m0 * (2.0 * dxi);
+  tau[c + n] = (v0 - __ldg(v + c - Y)) * m0 * (2.0 * dyi);
+  tau[c + 2 * n] = (w0 - __ldg(w + c - Z)) * m0 * (2.0 * dzi);
+  tau[c + 3 * n] = ((__ldg(u + c + Y) - u0) * hy + (__ldg(v + c + X) - v0) * hx) *
+                   ((m0 + mx) + (my + __ldg(mu + c + X + Y)));
+  tau[c + 4 * n] = ((__ldg(u + c + Z) - u0) * hz + (__ldg(w + c + X) - w0) * hx) *
+                   ((m0 + mx) + (mz + __ldg(mu + c + X + Z)));
+  tau[c + 5 * n] = ((__ldg(v + c + Z) - v0) * hz + (__ldg(w + c + Y) - w0) * hy) *
+                   ((m0 + my) + (mz + __ldg(mu + c + Y + Z)));
+}
+__global__ void __launch_bounds__(256) k_div_stress(Grid g, double dxi, double dyi, double dzi,
+                                                    const double* __restrict__ t, double* __restrict__ vu,
+                                                    double* __restrict__ vv, double* __restrict__ vw) {
+  const int i = 1 + (int)(blockIdx.x * blockDim.x + threadIdx.x);
+  const int j = 1 + (int)(blockIdx.y * blockDim.y + threadIdx.y);
+  const int k = 1 + (int)blockIdx.z;
+  if (i > g.ni || j > g.nj) return;
+  const long X = 1, Y = g.sy, Z = g.sz, n = g.n;
+  const long c = g.at(i, j, k);
+  const double* t1 = t;
+  const double* t2 = t + n;
+  const double* t3 = t + 2 * n;
+  const double* t4 = t + 3 * n;
+  const double* t5 = t + 4 * n;
+  const double* t6 = t + 5 * n;
+  const double a4 = __ldg(t4 + c), a5 = __ldg(t5 + c), a6 = __ldg(t6 + c);
+  vu[c] = (__ldg(t1 + c + X) - __ldg(t1 + c)) * dxi + (a4 - __ldg(t4 + c - Y)) * dyi + (a5 - __ldg(t5 + c - Z)) * dzi;
+  vv[c] = (a4 - __ldg(t4 + c - X)) * dxi + (__ldg(t2 + c + Y) - __ldg(t2 + c)) * dyi + (a6 - __ldg(t6 + c - Z)) * dzi;
+  vw[c] = (a5 - __ldg(t5 + c - X)) * dxi + (a6 - __ldg(t6 + c - Y)) * dyi + (__ldg(t3 + c + Z) - __ldg(t3 + c)) * dzi;
+}
+
 // One colour pair of one component.  Thread (a, b, kk) covers, for the pair whose
 // first colour has parities (pi,pj,pk), the point (pi+2a, pj+2b, pk+2kk) and the
 // point of the second colour (all parities flipped) at (pi'+2a, pj'+2b, pk'+2kk).
@@ -964,6 +1015,15 @@ void wall_coef(cudaStream_t s, const Grid& g, double dy, const double* l1, const
                double* wallc) {
   k_wall_coef<<<wall_grid(g), kB, 0, s>>>(g, dy, l1, l2, phi, wallc);
   count_launch();
+}
+
+void explicit_viscous(cudaStream_t s, const Grid& g, double dxinv, double dyinv, double dzinv, const double* u,
+                      const double* v, const double* w, const double* mu, double* tau, double* const* vis) {
+  k_stress<<<dim3((g.ni + 2 + 31) / 32, (g.nj + 2 + 7) / 8, g.nk + 2), kB, 0, s>>>(g, dxinv, dyinv, dzinv, u, v, w,
+                                                                               mu, tau);
+  k_div_stress<<<dim3((g.ni + 31) / 32, (g.nj + 7) / 8, g.nk), kB, 0, s>>>(g, dxinv, dyinv, dzinv, tau, vis[0],
+                                                                         vis[1], vis[2]);
+  count_launch(2);
 }
 
 void wall_halo(cudaStream_t s, const Grid& g, int normal, double uwall, const double* wallc, double* un, double* vn,

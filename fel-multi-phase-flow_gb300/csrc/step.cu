@@ -52,7 +52,7 @@ struct fmf_ctx {
   double *theta0, *zeta, *l1, *l2, *theta;
   // work
   double *phix, *phiy, *phiz, *flx, *fly, *flz, *rho, *rhon, *rmu, *rmun;
-  double *adv[3], *advo[3], *phat, *prs[3], *sk, *tau, *vis[3];
+  double *adv[3], *advo[3], *phat, *prs[3], *tau, *vis[3];
   double *rn[4], *rnn[4], *rkap, *rkapn, *fst[3], *fstn[3], *sfst[3], *sfstn[3], *src[3];
   double *edge[3], *ab[6], *wallc, *sorpart;  // fused viscous solve (fused_visc.cu)
   double *dp, *div, *pr, *pi;
@@ -116,7 +116,6 @@ int fmf_ctx_create(const fmf_params* prm, fmf_ctx** out) {
     c->sfstn[q] = alloc(c, n);
     c->src[q] = alloc(c, n);
   }
-  c->sk = alloc(c, 6 * n);
   c->tau = alloc(c, 6 * n);
   for (int q = 0; q < 4; ++q) {
     c->rn[q] = alloc(c, 3 * n);
@@ -344,9 +343,7 @@ static void seg_pre(fmf_ctx* c) {
                     P.precision == FMF_MIXED, c->wsplit);
   op::calphat(s, g, c->p, c->po, c->phat);
   op::cal_grad_prs(s, g, dxinv, dyinv, dzinv, c->phat, c->prs[0], c->prs[1], c->prs[2]);
-  op::calsij(s, g, dxinv, dyinv, dzinv, c->u, c->v, c->w, c->sk);
-  op::cal_tau(s, g, c->sk, c->rmu, c->tau, false);
-  op::cal_div_tensor(s, g, dxinv, dyinv, dzinv, c->tau, c->vis[0], c->vis[1], c->vis[2]);
+  fused::explicit_viscous(s, g, dxinv, dyinv, dzinv, c->u, c->v, c->w, c->rmu, c->tau, c->vis);
   // :545-570 surface tension
   if (fused::csf_supported(g)) {
     const bool f32 = P.precision == FMF_MIXED;
