@@ -73,6 +73,10 @@ long sor_parts(const Grid& g);
 void pressure_half(cudaStream_t s, const Grid& g, double rho, double dxinv, double dzinv, const double* as_f,
                    const double* an_f, const double* ap_f, const double* div, double* pr, double* pi, double* dp);
 
+// corunp_explicit: un, vn, wn += dt/rho grad(dp) at the interior, pn = phat + dp
+void project(cudaStream_t s, const Grid& g, double rho, double dxinv, double dyinv, double dzinv, double dt,
+             const double* dp, const double* phat, double* un, double* vn, double* wn, double* pn);
+
 // Mixed-precision viscous solve (one step of iterative refinement).  Buffers:
 struct RefineBufs {
   float* d[3];  // corrections d = un - u, v, w (n floats each)

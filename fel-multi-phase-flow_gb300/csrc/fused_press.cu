@@ -164,6 +164,24 @@ __global__ void __launch_bounds__(128) k_tdma_half(Grid g, double dx2r, double d
     pi[o] = xi;
   }
 }
+
+// corunp_explicit.f:26-75 with the constant dt dxinv / rho formed once on the host
+// (the reference divides by rho at every point)
+__global__ void __launch_bounds__(256) k_project(Grid g, double cx, double cy, double cz,
+                                                 const double* __restrict__ dp, const double* __restrict__ phat,
+                                                 double* __restrict__ un, double* __restrict__ vn,
+                                                 double* __restrict__ wn, double* __restrict__ pn) {
+  const int i = 1 + (int)(blockIdx.x * blockDim.x + threadIdx.x);
+  const int j = 1 + (int)(blockIdx.y * blockDim.y + threadIdx.y);
+  const int k = 1 + (int)blockIdx.z;
+  if (i > g.ni || j > g.nj) return;
+  const long c = g.at(i, j, k);
+  const double d0 = __ldg(dp + c);
+  un[c] = fma(d0 - __ldg(dp + c + 1), cx, un[c]);
+  if (j <= g.nj - 1) vn[c] = fma(d0 - __ldg(dp + c + g.sy), cy, vn[c]);
+  wn[c] = fma(d0 - __ldg(dp + c + g.sz), cz, wn[c]);
+  pn[c] = __ldg(phat + c) + d0;
+}
 }  // namespace
 
 void pressure_half(cudaStream_t s, const Grid& g, double rho, double dxinv, double dzinv, const double* as_f,
@@ -187,6 +205,13 @@ void pressure_half(cudaStream_t s, const Grid& g, double rho, double dxinv, doub
   k_fft_z_half<<<gz, 256, smz, s>>>(g, pr, pi, tr, ti, twz, +1.0, 1.0);
   k_rfft_x_inv<<<rows / kRows, 256, sizeof(double) * kRows * (2 * H + 2 * M), s>>>(g, tr, ti, dp, twM, twN);
   count_launch(5);
+}
+
+void project(cudaStream_t s, const Grid& g, double rho, double dxinv, double dyinv, double dzinv, double dt,
+             const double* dp, const double* phat, double* un, double* vn, double* wn, double* pn) {
+  k_project<<<dim3((g.ni + 31) / 32, (g.nj + 7) / 8, g.nk), dim3(32, 8), 0, s>>>(
+      g, dt * dxinv / rho, dt * dyinv / rho, dt * dzinv / rho, dp, phat, un, vn, wn, pn);
+  count_launch();
 }
 
 }  // namespace fused

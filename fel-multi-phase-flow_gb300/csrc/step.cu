@@ -436,7 +436,7 @@ static void seg_post(fmf_ctx* c) {
   op::bnd_neumann(s, g, c->dp);
   op::bnd_periodic(s, g, c->dp);
   // :648-661
-  op::corunp_explicit(s, g, P.rhog, dxinv, dyinv, dzinv, dt, c->dp, c->phat, c->un, c->vn, c->wn, c->pn);
+  fused::project(s, g, P.rhog, dxinv, dyinv, dzinv, dt, c->dp, c->phat, c->un, c->vn, c->wn, c->pn);
   fused::wall_halo(s, g, 7, P.uwall, c->wallc, c->un, c->vn, c->wn);
   op::bnd_avzero(s, g, c->pn);
   op::bnd_neumann(s, g, c->pn);
