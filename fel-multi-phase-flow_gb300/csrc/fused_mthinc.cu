@@ -25,6 +25,7 @@ namespace {
 struct MC {
   double gp1, gp2, lim, eps_trunc, bet, dt, dxi, dyi, dzi;
   double lim2lo, lim2hi;  // lim^2 (1 -/+ 1e-12)
+  double dtdx, dtdy, dtdz;  // dt dxinv etc.
 };
 
 __device__ __forceinline__ double avg8(const double* __restrict__ p, long c, long X, long Y, long Z) {
@@ -96,8 +97,12 @@ __global__ void __launch_bounds__(256) k_classify(Grid g, MC m, const double* __
   const double uw = __ldg(u + c - X), ue = __ldg(u + c), vs = __ldg(v + c - Y), vn = __ldg(v + c),
                wb = __ldg(w + c - Z), wt = __ldg(w + c);
   // the band test sqrt(q2) <= lim of the reference: decided on q2 against lim^2
-  // where q2 is clearly on one side, with the square root only within 1e-12 of it
-  const bool band = q2 < m.lim2lo ? false : (q2 > m.lim2hi ? true : !(sqrt(q2) <= m.lim));
+  // where q2 is clearly on one side (compared as bit patterns: all three are
+  // non-negative), with the square root only within 1e-12 of it
+  const long long qb = __double_as_longlong(q2);
+  const bool band = qb < __double_as_longlong(m.lim2lo)
+                        ? false
+                        : (qb > __double_as_longlong(m.lim2hi) ? true : !(sqrt(q2) <= m.lim));
   if (band) {
     const int slot = atomicAdd(count, 1);
     list[slot] = (int)c;
@@ -111,19 +116,25 @@ __global__ void __launch_bounds__(256) k_classify(Grid g, MC m, const double* __
   // owned faces: east/north/top when the velocity there is >= 0 (this cell donates or
   // the flux is zero), west/south/bottom when < 0; band cells leave the donated
   // faces to k_band but still zero the owned faces they do not donate through.
-  if (ue >= 0.0) fx[c] = band ? 0.0 : ue * phi00 * m.dt * m.dxi;
-  if (uw < 0.0) fx[c - X] = band ? 0.0 : uw * phi00 * m.dt * m.dxi;
-  if (vn >= 0.0) fy[c] = band ? 0.0 : vn * phi00 * m.dt * m.dyi;
-  if (vs < 0.0) fy[c - Y] = band ? 0.0 : vs * phi00 * m.dt * m.dyi;
-  if (wt >= 0.0) fz[c] = band ? 0.0 : wt * phi00 * m.dt * m.dzi;
-  if (wb < 0.0) fz[c - Z] = band ? 0.0 : wb * phi00 * m.dt * m.dzi;
+  // Signs are read from the bits: nonneg(v) is v >= 0 (so true for -0 as well; it
+  // differs from the comparison only for NaN).  Fluxes are v phi dt/dx with dt/dx
+  // formed once.
+  auto nonneg = [](double v) { return __double_as_longlong(v) >= 0 || (__double_as_longlong(v) << 1) == 0; };
+  const double pdx = phi00 * m.dtdx, pdy = phi00 * m.dtdy, pdz = phi00 * m.dtdz;
+  const bool e_ = nonneg(ue), w_ = nonneg(uw), n_ = nonneg(vn), s_ = nonneg(vs), t_ = nonneg(wt), b_ = nonneg(wb);
+  if (e_) fx[c] = band ? 0.0 : ue * pdx;
+  if (!w_) fx[c - X] = band ? 0.0 : uw * pdx;
+  if (n_) fy[c] = band ? 0.0 : vn * pdy;
+  if (!s_) fy[c - Y] = band ? 0.0 : vs * pdy;
+  if (t_) fz[c] = band ? 0.0 : wt * pdz;
+  if (!b_) fz[c - Z] = band ? 0.0 : wb * pdz;
   // west/south/bottom faces of the first cells with no in-range donor stay zero
-  if (i == 0 && uw >= 0.0) fx[c - X] = 0.0;
-  if (j == 0 && vs >= 0.0) fy[c - Y] = 0.0;
-  if (k == 0 && wb >= 0.0) fz[c - Z] = 0.0;
-  if (i == g.ni + 1 && ue < 0.0) fx[c] = 0.0;
-  if (j == g.nj + 1 && vn < 0.0) fy[c] = 0.0;
-  if (k == g.nk + 1 && wt < 0.0) fz[c] = 0.0;
+  if (i == 0 && w_) fx[c - X] = 0.0;
+  if (j == 0 && s_) fy[c - Y] = 0.0;
+  if (k == 0 && b_) fz[c - Z] = 0.0;
+  if (i == g.ni + 1 && !e_) fx[c] = 0.0;
+  if (j == g.nj + 1 && !n_) fy[c] = 0.0;
+  if (k == g.nk + 1 && !t_) fz[c] = 0.0;
 }
 
 // R = double: the FP64 step.  R = float: the mixed-precision step (normal, band
@@ -249,6 +260,9 @@ void mthinc_fluxes(cudaStream_t s, const Grid& g, double dxinv, double dyinv, do
   m.dxi = dxinv;
   m.dyi = dyinv;
   m.dzi = dzinv;
+  m.dtdx = dt * dxinv;
+  m.dtdy = dt * dyinv;
+  m.dtdz = dt * dzinv;
   FMF_CUDA(cudaMemsetAsync(count, 0, sizeof(int), s));
   dim3 b(32, 8, 1);
   dim3 gr((unsigned)((g.ni + 2 + 31) / 32), (unsigned)((g.nj + 2 + 7) / 8), (unsigned)(g.nk + 2));
