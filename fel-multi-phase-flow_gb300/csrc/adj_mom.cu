@@ -2,6 +2,7 @@
 // the CSF surface-tension force (cal_grad_p2a, calrn x4, calrkap, cal_grad_p2uvw,
 // calfst).
 #include "adj.cuh"
+#include "fused.cuh"
 #include "ops.cuh"
 #include "recip.cuh"
 
@@ -212,7 +213,7 @@ void csf_T(cudaStream_t s, const Grid& g, double dxi, double dyi, double dzi, do
   double* lgq = work + 39 * n;   // adjoint of the face gradient (3n)
   static const int offs[4][3] = {{1, 1, 1}, {0, 0, 1}, {0, 1, 0}, {1, 0, 0}};
   // forward recompute
-  op::cal_grad_p2a(s, g, dxi, dyi, dzi, phi, Gv, Gv + n, Gv + 2 * n);
+  fused::vertex_gradient(s, g, dxi, dyi, dzi, phi, Gv, Gv + n, Gv + 2 * n);
   if (!kap_rec) {
     for (int q = 0; q < 4; ++q)
       op::calrn(s, g, dxi, dyi, dzi, offs[q][0], offs[q][1], offs[q][2], Gv, Gv + n, Gv + 2 * n, rn + 3 * n * q);

@@ -379,7 +379,7 @@ int record_step(fmf_adj* a) {
   double** S = a->S;
   double *phi0 = S[SPHI0], *phi1 = S[SPHI1], *phn0 = S[SPHIN0], *phn1 = S[SPHIN1];
   // :491-503
-  op::cal_grad_p2a(s, g, dxi, dyi, dzi, phi1, a->gx1[0], a->gx1[1], a->gx1[2]);
+  fused::vertex_gradient(s, g, dxi, dyi, dzi, phi1, a->gx1[0], a->gx1[1], a->gx1[2]);
   {
     const long nb = (long)(g.ni + 2) * (g.nj + 2) * (g.nk + 2);
     fused::mthinc_fluxes(s, g, dxi, dyi, dzi, dt, P.bet_mthinc, phi1, a->gx1[0], a->gx1[1], a->gx1[2], S[SU],
@@ -387,7 +387,7 @@ int record_step(fmf_adj* a) {
   }
   op::solphi_mthinc2(s, g, dxi, dyi, dzi, dt, S[SU], S[SV], S[SW], a->fl[0], a->fl[1], a->fl[2], phi1, phn1);
   dcopy(a, phn1, a->pa, n);
-  op::cal_grad_p2a(s, g, dxi, dyi, dzi, phn1, a->gxn[0], a->gxn[1], a->gxn[2]);
+  fused::vertex_gradient(s, g, dxi, dyi, dzi, phn1, a->gxn[0], a->gxn[1], a->gxn[2]);
   adj::mthinc3_record(s, g, dxi, dyi, dzi, P.bet_mthinc, a->gxn[0], a->gxn[1], a->gxn[2], a->pa, a->pb, a->pass);
   op::solphi_mthinc3(s, g, dxi, dyi, dzi, P.bet_mthinc, a->gxn[0], a->gxn[1], a->gxn[2], phi1, phn1, a->sums);
   dcopy(a, phn1, a->pc, n);
@@ -408,9 +408,7 @@ int record_step(fmf_adj* a) {
   fused::weno5_both(s, g, dxi, dyi, dzi, S[SU], S[SV], S[SW], S[SUO], S[SVO], S[SWO], a->adv, a->advo, false);
   op::calphat(s, g, S[SP], S[SPO], a->phat);
   op::cal_grad_prs(s, g, dxi, dyi, dzi, a->phat, a->prs[0], a->prs[1], a->prs[2]);
-  op::calsij(s, g, dxi, dyi, dzi, S[SU], S[SV], S[SW], a->sk);
-  op::cal_tau(s, g, a->sk, a->rmu, a->tau, false);
-  op::cal_div_tensor(s, g, dxi, dyi, dzi, a->tau, a->vis[0], a->vis[1], a->vis[2]);
+  fused::explicit_viscous(s, g, dxi, dyi, dzi, S[SU], S[SV], S[SW], a->rmu, a->tau, a->vis, a->sk);
   // :545-573 (the fused kernel where the grid tiles; csf_T differentiates the same
   // sequence of reference subroutines either way)
   if (fused::csf_supported(g)) {
@@ -473,7 +471,7 @@ int record_step(fmf_adj* a) {
   op::bnd_avzero(s, g, a->dp);
   op::bnd_neumann(s, g, a->dp);
   op::bnd_periodic(s, g, a->dp);
-  op::corunp_explicit(s, g, P.rhog, dxi, dyi, dzi, dt, a->dp, a->phat, a->un[0], a->un[1], a->un[2], a->pn);
+  fused::project(s, g, P.rhog, dxi, dyi, dzi, dt, a->dp, a->phat, a->un[0], a->un[1], a->un[2], a->pn);
   for (int q = 0; q < 3; ++q) dcopy(a, a->un[q], a->un2[q], n);
   fused::wall_halo(s, g, 7, P.uwall, a->wallc, a->un[0], a->un[1], a->un[2]);
   op::bnd_avzero(s, g, a->pn);

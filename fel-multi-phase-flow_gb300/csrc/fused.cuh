@@ -40,9 +40,11 @@ void csf_force(cudaStream_t s, const Grid& g, double dxinv, double dyinv, double
                double* kap = nullptr);
 
 // The explicit viscous term (calsij, cal_arith_tau, cal_div_tensor) at the interior
-// u, v, w points into vis[0..2]; tau: 6 n doubles of workspace
+// u, v, w points into vis[0..2]; tau: 6 n doubles of workspace; sk (optional, 6 n):
+// the strain components at the points 0..n+1 the interior divergence reads
 void explicit_viscous(cudaStream_t s, const Grid& g, double dxinv, double dyinv, double dzinv, const double* u,
-                      const double* v, const double* w, const double* mu, double* tau, double* const* vis);
+                      const double* v, const double* w, const double* mu, double* tau, double* const* vis,
+                      double* sk = nullptr);
 
 // Viscous solve.  src_visc_prep: edge viscosities E[0..2] (xy, xz, yz edges, i,j,k in
 // 0..n), per-component A/B (AB[0..5] = Au Bu Av Bv Aw Bw) with the momentum

@@ -143,10 +143,12 @@ __global__ void __launch_bounds__(256) k_src_ab(Grid g, VP p, SrcIn in, const do
 // edges, tau_ij = 2 (mean of 4 mu) S_ij with S_ij = (du_i/dx_j + du_j/dx_i)/2,
 // the factors 2, 1/2 and 1/4 folded into the constants; the strain never goes
 // through memory.  k_div_stress takes its divergence on the interior.
+// (sk, optional: the six strain components of calsij.f:28-139 at the same points,
+// kept by the adjoint's record of the step)
 __global__ void __launch_bounds__(256) k_stress(Grid g, double dxi, double dyi, double dzi,
                                                 const double* __restrict__ u, const double* __restrict__ v,
                                                 const double* __restrict__ w, const double* __restrict__ mu,
-                                                double* __restrict__ tau) {
+                                                double* __restrict__ tau, double* __restrict__ sk) {
   const int i = (int)(blockIdx.x * blockDim.x + threadIdx.x);
   const int j = (int)(blockIdx.y * blockDim.y + threadIdx.y);
   const int k = (int)blockIdx.z;
@@ -165,6 +167,14 @@ __global__ void __launch_bounds__(256) k_stress(Grid g, double dxi, double dyi, 
                    ((m0 + mx) + (mz + __ldg(mu + c + X + Z)));
   tau[c + 5 * n] = ((__ldg(v + c + Z) - v0) * hz + (__ldg(w + c + Y) - w0) * hy) *
                    ((m0 + my) + (mz + __ldg(mu + c + Y + Z)));
+  if (sk) {
+    sk[c] = (u0 - __ldg(u + c - X)) * dxi;
+    sk[c + n] = (v0 - __ldg(v + c - Y)) * dyi;
+    sk[c + 2 * n] = (w0 - __ldg(w + c - Z)) * dzi;
+    sk[c + 3 * n] = ((__ldg(u + c + Y) - u0) * dyi + (__ldg(v + c + X) - v0) * dxi) * 0.5;
+    sk[c + 4 * n] = ((__ldg(u + c + Z) - u0) * dzi + (__ldg(w + c + X) - w0) * dxi) * 0.5;
+    sk[c + 5 * n] = ((__ldg(v + c + Z) - v0) * dzi + (__ldg(w + c + Y) - w0) * dyi) * 0.5;
+  }
 }
 __global__ void __launch_bounds__(256) k_div_stress(Grid g, double dxi, double dyi, double dzi,
                                                     const double* __restrict__ t, double* __restrict__ vu,
@@ -1018,9 +1028,10 @@ void wall_coef(cudaStream_t s, const Grid& g, double dy, const double* l1, const
 }
 
 void explicit_viscous(cudaStream_t s, const Grid& g, double dxinv, double dyinv, double dzinv, const double* u,
-                      const double* v, const double* w, const double* mu, double* tau, double* const* vis) {
+                      const double* v, const double* w, const double* mu, double* tau, double* const* vis,
+                      double* sk) {
   k_stress<<<dim3((g.ni + 2 + 31) / 32, (g.nj + 2 + 7) / 8, g.nk + 2), kB, 0, s>>>(g, dxinv, dyinv, dzinv, u, v, w,
-                                                                               mu, tau);
+                                                                               mu, tau, sk);
   k_div_stress<<<dim3((g.ni + 31) / 32, (g.nj + 7) / 8, g.nk), kB, 0, s>>>(g, dxinv, dyinv, dzinv, tau, vis[0],
                                                                          vis[1], vis[2]);
   count_launch(2);
