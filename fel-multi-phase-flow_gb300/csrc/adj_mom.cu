@@ -290,7 +290,10 @@ void csf_T(cudaStream_t s, const Grid& g, double dxi, double dyi, double dzi, do
 #pragma unroll
       for (int q3 = 0; q3 < 3; ++q3) {
         const double* p = Gv + q3 * n + b;
-        r[q3] = (p[0] + p[Xf] + p[Yf] + p[Xf + Yf] + p[Zf] + p[Xf + Zf] + p[Yf + Zf] + p[Xf + Yf + Zf]) * 0.125;
+        // family 0 averages 8 vertex gradients; families 1-3 (one offset only) the
+        // two along that offset, each four times in the 8-term mean
+        r[q3] = f == 0 ? (p[0] + p[Xf] + p[Yf] + p[Xf + Yf] + p[Zf] + p[Xf + Zf] + p[Yf + Zf] + p[Xf + Yf + Zf]) * 0.125
+                       : (p[0] + p[Xf + Yf + Zf]) * 0.5;
       }
       // dN/dv = I/a - v v^T/(a^2 m) with m = |v|, a = m + vs:
       // lv = (l - v (v.l)/(m a)) / a, the factor formed as ((v.l)/m)/a, which stays
