@@ -57,9 +57,10 @@ __device__ __forceinline__ void walk_rev(const Walk& W, double g4, double* la) {
   const double lX = g4 * fma(W.R, -1.0 / 6.0, W.D1), lY = g4 * (W.d2 - W.R), lZ = g4 * fma(W.R, -0.5, W.D3);
   const double lx = W.x * lX, ly = W.y * lY, lz = W.z * lZ;
   const double S1 = fma(ly, W.s3, lz * W.s2), S2 = fma(lx, W.s3, lz * W.s1), S3 = fma(lx, W.s2, ly * W.s1);
-  const double lt1a = W.t1a * (c13 * S1), lt2a = W.t2a * S1;
-  const double lt1b = W.t1b * (c13 * S2), lt2b = W.t2b * S2;
-  const double lt1c = W.t1c * (c13 * S3), lt2c = W.t2c * S3;
+  // (t1 c13) is the forward's own product in s = fma(t1 c13, t1, t2^2)
+  const double lt1a = (W.t1a * c13) * S1, lt2a = W.t2a * S1;
+  const double lt1b = (W.t1b * c13) * S2, lt2b = W.t2b * S2;
+  const double lt1c = (W.t1c * c13) * S3, lt2c = W.t2c * S3;
   la[0] = fma(lD1, 1.0 / 12.0, lt1a + lt2a);
   la[1] = fma(lD1, -7.0 / 24.0, fma(ld2, -0.25, fma(lt1a, -2.0, fma(lt2a, -4.0, lt1b + lt2b))));
   la[2] = fma(lD1, 11.0 / 24.0,

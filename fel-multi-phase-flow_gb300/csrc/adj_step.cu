@@ -16,6 +16,8 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <cstdint>
+#include <functional>
 #include <map>
 #include <string>
 #include <thread>
@@ -123,6 +125,8 @@ struct fmf_adj {
   adj::GraphCache graphs;      // transposed viscous iterations, one per record slot
   adj::GraphCache fgraphs;     // forward viscous iterations, one per record slot
   adj::GraphCache rgraphs;     // replays of the last forward viscous cycle, one per record slot
+  adj::GraphCache pgraphs;     // the parts before and after the viscous solve of steps not recorded
+  bool rec_warm = false;       // a step has run on this handle (scratch sized for capture)
   double* host_norm = nullptr;  // pinned
   fmf_adj* worker = nullptr;    // recomputes the next segment while this handle reverses one
 };
@@ -369,8 +373,30 @@ void csf_fwd(fmf_adj* a, const double* phi, double* const* f) {
   op::sum_fst(s, g, G, G + n, G + 2 * n, f[0], f[1], f[2]);
 }
 
+// Runs one part of a step: eagerly, or, for a step whose record is not kept
+// (graphs), as a CUDA graph captured at the handle's first such call with the
+// current buffers (keyed by them) and replayed afterwards.  The handle's first step
+// runs eagerly, which sizes the scratch buffers the captured kernels use.
+void run_part(fmf_adj* a, bool graphs, int id, const std::function<void()>& body) {
+  if (!graphs || !a->rec_warm) {
+    body();
+    return;
+  }
+  long long per_launch = 0;
+  const cudaGraphExec_t exec = adj::cached_graph(
+      a->s, &a->pgraphs,
+      {(const void*)(intptr_t)(id + 1), a->gx1[0], a->adv[0], a->E[0], a->ustar[0], a->kap, a->S[0], a->un[0]}, body,
+      &per_launch);
+  if (!exec) {
+    body();
+    return;
+  }
+  FMF_CUDA(cudaGraphLaunch(exec, a->s));
+  count_launch((int)per_launch);
+}
+
 // one FP64 step on a->S (main.f90:473-697), recording the intermediates
-int record_step(fmf_adj* a) {
+int record_step(fmf_adj* a, bool graphs) {
   const fmf_params& P = a->prm;
   const Grid& g = a->g;
   cudaStream_t s = a->s;
@@ -378,58 +404,62 @@ int record_step(fmf_adj* a) {
   const double dxi = 1.0 / P.dx, dyi = 1.0 / P.dy, dzi = 1.0 / P.dz, dt = P.dt;
   double** S = a->S;
   double *phi0 = S[SPHI0], *phi1 = S[SPHI1], *phn0 = S[SPHIN0], *phn1 = S[SPHIN1];
-  // :491-503
-  fused::vertex_gradient(s, g, dxi, dyi, dzi, phi1, a->gx1[0], a->gx1[1], a->gx1[2]);
-  {
-    const long nb = (long)(g.ni + 2) * (g.nj + 2) * (g.nk + 2);
-    fused::mthinc_fluxes(s, g, dxi, dyi, dzi, dt, P.bet_mthinc, phi1, a->gx1[0], a->gx1[1], a->gx1[2], S[SU],
-                         S[SV], S[SW], a->fl[0], a->fl[1], a->fl[2], a->band, a->band + nb, false, a->newton);
-  }
-  op::solphi_mthinc2(s, g, dxi, dyi, dzi, dt, S[SU], S[SV], S[SW], a->fl[0], a->fl[1], a->fl[2], phi1, phn1);
-  dcopy(a, phn1, a->pa, n);
-  fused::vertex_gradient(s, g, dxi, dyi, dzi, phn1, a->gxn[0], a->gxn[1], a->gxn[2]);
-  adj::mthinc3_record(s, g, dxi, dyi, dzi, P.bet_mthinc, a->gxn[0], a->gxn[1], a->gxn[2], a->pa, a->pb, a->pass);
-  op::solphi_mthinc3(s, g, dxi, dyi, dzi, P.bet_mthinc, a->gxn[0], a->gxn[1], a->gxn[2], phi1, phn1, a->sums);
-  dcopy(a, phn1, a->pc, n);
-  op::gnbc(s, g, S[SU], S[SW], P.uwall, a->theta0, P.sigma, a->zeta, a->theta);
-  op::bnd_contact_angle(s, g, phn1, a->theta, P.dx, P.dy, P.dz);
-  op::bnd_periodic(s, g, phn1);
-  dcopy(a, phn1, a->phn1f, n);
-  // :509-517
-  op::summation(s, g, phn0, phn1);
-  op::bnd_neumann(s, g, phn0);
-  op::bnd_contact_angle(s, g, phi0, a->theta, P.dx, P.dy, P.dz);
-  op::bnd_periodic(s, g, phn0);
-  // :526-541
-  op::cal_arith_mean(s, g, phi0, P.rhol, P.rhog, a->rho);
-  op::cal_arith_mean(s, g, phn0, P.rhol, P.rhog, a->rhon);
-  op::cal_arith_mean(s, g, phi0, P.rmul, P.rmug, a->rmu);
-  op::cal_arith_mean(s, g, phn0, P.rmul, P.rmug, a->rmun);
-  fused::weno5_both(s, g, dxi, dyi, dzi, S[SU], S[SV], S[SW], S[SUO], S[SVO], S[SWO], a->adv, a->advo, false);
-  op::calphat(s, g, S[SP], S[SPO], a->phat);
-  op::cal_grad_prs(s, g, dxi, dyi, dzi, a->phat, a->prs[0], a->prs[1], a->prs[2]);
-  fused::explicit_viscous(s, g, dxi, dyi, dzi, S[SU], S[SV], S[SW], a->rmu, a->tau, a->vis, a->sk);
-  // :545-573 (the fused kernel where the grid tiles; csf_T differentiates the same
-  // sequence of reference subroutines either way)
-  if (fused::csf_supported(g)) {
-    fused::csf_force(s, g, dxi, dyi, dzi, P.rhol, P.rhog, P.sigma, phi1, a->sfst[0], a->sfst[1], a->sfst[2], false,
-                     a->kap);
-    fused::csf_force(s, g, dxi, dyi, dzi, P.rhol, P.rhog, P.sigma, phn1, a->sfstn[0], a->sfstn[1], a->sfstn[2],
-                     false, a->kapn);
-  } else {
-    csf_fwd(a, phi1, a->sfst);
-    csf_fwd(a, phn1, a->sfstn);
-  }
-  // :579-623
-  const double* advp[3] = {a->adv[0], a->adv[1], a->adv[2]};
-  const double* advop[3] = {a->advo[0], a->advo[1], a->advo[2]};
-  const double* prsp[3] = {a->prs[0], a->prs[1], a->prs[2]};
-  const double* visp[3] = {a->vis[0], a->vis[1], a->vis[2]};
-  const double* fstp[3] = {a->sfst[0], a->sfst[1], a->sfst[2]};
-  const double* fstnp[3] = {a->sfstn[0], a->sfstn[1], a->sfstn[2]};
-  fused::src_visc_prep(s, g, dxi, dyi, dzi, dt, P.harmonic, P.grvb, P.grvp, S[SU], S[SV], S[SW], advp, advop, prsp,
-                       visp, fstp, fstnp, a->rmun, a->rho, a->rhon, a->E, a->AB, a->l1, a->l2, phi1, P.dy, a->wallc);
-  for (int q = 0; q < 3; ++q) dcopy(a, S[SU + q], a->un[q], n);
+  // the step before the viscous solve
+  auto pre = [&]() {
+    // :491-503
+    fused::vertex_gradient(s, g, dxi, dyi, dzi, phi1, a->gx1[0], a->gx1[1], a->gx1[2]);
+    {
+      const long nb = (long)(g.ni + 2) * (g.nj + 2) * (g.nk + 2);
+      fused::mthinc_fluxes(s, g, dxi, dyi, dzi, dt, P.bet_mthinc, phi1, a->gx1[0], a->gx1[1], a->gx1[2], S[SU],
+                           S[SV], S[SW], a->fl[0], a->fl[1], a->fl[2], a->band, a->band + nb, false, a->newton);
+    }
+    op::solphi_mthinc2(s, g, dxi, dyi, dzi, dt, S[SU], S[SV], S[SW], a->fl[0], a->fl[1], a->fl[2], phi1, phn1);
+    dcopy(a, phn1, a->pa, n);
+    fused::vertex_gradient(s, g, dxi, dyi, dzi, phn1, a->gxn[0], a->gxn[1], a->gxn[2]);
+    adj::mthinc3_record(s, g, dxi, dyi, dzi, P.bet_mthinc, a->gxn[0], a->gxn[1], a->gxn[2], a->pa, a->pb, a->pass);
+    op::solphi_mthinc3(s, g, dxi, dyi, dzi, P.bet_mthinc, a->gxn[0], a->gxn[1], a->gxn[2], phi1, phn1, a->sums);
+    dcopy(a, phn1, a->pc, n);
+    op::gnbc(s, g, S[SU], S[SW], P.uwall, a->theta0, P.sigma, a->zeta, a->theta);
+    op::bnd_contact_angle(s, g, phn1, a->theta, P.dx, P.dy, P.dz);
+    op::bnd_periodic(s, g, phn1);
+    dcopy(a, phn1, a->phn1f, n);
+    // :509-517
+    op::summation(s, g, phn0, phn1);
+    op::bnd_neumann(s, g, phn0);
+    op::bnd_contact_angle(s, g, phi0, a->theta, P.dx, P.dy, P.dz);
+    op::bnd_periodic(s, g, phn0);
+    // :526-541
+    op::cal_arith_mean(s, g, phi0, P.rhol, P.rhog, a->rho);
+    op::cal_arith_mean(s, g, phn0, P.rhol, P.rhog, a->rhon);
+    op::cal_arith_mean(s, g, phi0, P.rmul, P.rmug, a->rmu);
+    op::cal_arith_mean(s, g, phn0, P.rmul, P.rmug, a->rmun);
+    fused::weno5_both(s, g, dxi, dyi, dzi, S[SU], S[SV], S[SW], S[SUO], S[SVO], S[SWO], a->adv, a->advo, false);
+    op::calphat(s, g, S[SP], S[SPO], a->phat);
+    op::cal_grad_prs(s, g, dxi, dyi, dzi, a->phat, a->prs[0], a->prs[1], a->prs[2]);
+    fused::explicit_viscous(s, g, dxi, dyi, dzi, S[SU], S[SV], S[SW], a->rmu, a->tau, a->vis, a->sk);
+    // :545-573 (the fused kernel where the grid tiles; csf_T differentiates the same
+    // sequence of reference subroutines either way)
+    if (fused::csf_supported(g)) {
+      fused::csf_force(s, g, dxi, dyi, dzi, P.rhol, P.rhog, P.sigma, phi1, a->sfst[0], a->sfst[1], a->sfst[2], false,
+                       a->kap);
+      fused::csf_force(s, g, dxi, dyi, dzi, P.rhol, P.rhog, P.sigma, phn1, a->sfstn[0], a->sfstn[1], a->sfstn[2],
+                       false, a->kapn);
+    } else {
+      csf_fwd(a, phi1, a->sfst);
+      csf_fwd(a, phn1, a->sfstn);
+    }
+    // :579-623
+    const double* advp[3] = {a->adv[0], a->adv[1], a->adv[2]};
+    const double* advop[3] = {a->advo[0], a->advo[1], a->advo[2]};
+    const double* prsp[3] = {a->prs[0], a->prs[1], a->prs[2]};
+    const double* visp[3] = {a->vis[0], a->vis[1], a->vis[2]};
+    const double* fstp[3] = {a->sfst[0], a->sfst[1], a->sfst[2]};
+    const double* fstnp[3] = {a->sfstn[0], a->sfstn[1], a->sfstn[2]};
+    fused::src_visc_prep(s, g, dxi, dyi, dzi, dt, P.harmonic, P.grvb, P.grvp, S[SU], S[SV], S[SW], advp, advop, prsp,
+                         visp, fstp, fstnp, a->rmun, a->rho, a->rhon, a->E, a->AB, a->l1, a->l2, phi1, P.dy, a->wallc);
+    for (int q = 0; q < 3; ++q) dcopy(a, S[SU + q], a->un[q], n);
+  };
+  run_part(a, graphs, 0, pre);
   // one outer iteration (12 colour-pair sweeps and their refreshes), replayed as a
   // CUDA graph per record slot
   auto iteration = [&]() {
@@ -463,29 +493,34 @@ int record_step(fmf_adj* a) {
     if (err / err0 <= a->sor_tol) break;
   }
   a->sor_total += lp + 1;
-  for (int q = 0; q < 3; ++q) dcopy(a, a->un[q], a->ustar[q], n);
-  // :625-661
-  fused::wall_halo(s, g, 7, P.uwall, a->wallc, a->un[0], a->un[1], a->un[2]);
-  op::caldiv(s, g, dxi, dyi, dzi, dt, a->un[0], a->un[1], a->un[2], a->div, nullptr);
-  fused::pressure_half(s, g, P.rhog, dxi, dzi, a->as_f, a->an_f, a->ap_f, a->div, a->pr, a->pi, a->dp);
-  op::bnd_avzero(s, g, a->dp);
-  op::bnd_neumann(s, g, a->dp);
-  op::bnd_periodic(s, g, a->dp);
-  fused::project(s, g, P.rhog, dxi, dyi, dzi, dt, a->dp, a->phat, a->un[0], a->un[1], a->un[2], a->pn);
-  for (int q = 0; q < 3; ++q) dcopy(a, a->un[q], a->un2[q], n);
-  fused::wall_halo(s, g, 7, P.uwall, a->wallc, a->un[0], a->un[1], a->un[2]);
-  op::bnd_avzero(s, g, a->pn);
-  op::bnd_neumann(s, g, a->pn);
-  op::bnd_periodic(s, g, a->pn);
-  // :686-697 rotation (copies: the record keeps the step's inputs in the arrays above)
-  for (int q = 0; q < 3; ++q) {
-    dcopy(a, S[SU + q], S[SUO + q], n);
-    dcopy(a, a->un[q], S[SU + q], n);
-  }
-  dcopy(a, S[SP], S[SPO], n);
-  dcopy(a, a->pn, S[SP], n);
-  dcopy(a, phn0, phi0, n);
-  dcopy(a, phn1, phi1, n);
+  // the step after the viscous solve
+  auto post = [&]() {
+    for (int q = 0; q < 3; ++q) dcopy(a, a->un[q], a->ustar[q], n);
+    // :625-661
+    fused::wall_halo(s, g, 7, P.uwall, a->wallc, a->un[0], a->un[1], a->un[2]);
+    op::caldiv(s, g, dxi, dyi, dzi, dt, a->un[0], a->un[1], a->un[2], a->div, nullptr);
+    fused::pressure_half(s, g, P.rhog, dxi, dzi, a->as_f, a->an_f, a->ap_f, a->div, a->pr, a->pi, a->dp);
+    op::bnd_avzero(s, g, a->dp);
+    op::bnd_neumann(s, g, a->dp);
+    op::bnd_periodic(s, g, a->dp);
+    fused::project(s, g, P.rhog, dxi, dyi, dzi, dt, a->dp, a->phat, a->un[0], a->un[1], a->un[2], a->pn);
+    for (int q = 0; q < 3; ++q) dcopy(a, a->un[q], a->un2[q], n);
+    fused::wall_halo(s, g, 7, P.uwall, a->wallc, a->un[0], a->un[1], a->un[2]);
+    op::bnd_avzero(s, g, a->pn);
+    op::bnd_neumann(s, g, a->pn);
+    op::bnd_periodic(s, g, a->pn);
+    // :686-697 rotation (copies: the record keeps the step's inputs in the arrays above)
+    for (int q = 0; q < 3; ++q) {
+      dcopy(a, S[SU + q], S[SUO + q], n);
+      dcopy(a, a->un[q], S[SU + q], n);
+    }
+    dcopy(a, S[SP], S[SPO], n);
+    dcopy(a, a->pn, S[SP], n);
+    dcopy(a, phn0, phi0, n);
+    dcopy(a, phn1, phi1, n);
+  };
+  run_part(a, graphs, 1, post);
+  a->rec_warm = true;
   FMF_CUDA(cudaGetLastError());
   return get_status();
 }
@@ -838,6 +873,7 @@ int fmf_adj_destroy(fmf_adj* a) {
   for (void* p : a->rec_blocks) cudaFree(p);
   for (auto& e : a->graphs) cudaGraphExecDestroy(e.second.first);
   for (auto& e : a->fgraphs) cudaGraphExecDestroy(e.second.first);
+  for (auto& e : a->pgraphs) cudaGraphExecDestroy(e.second.first);
   for (auto& e : a->rgraphs) cudaGraphExecDestroy(e.second.first);
   if (a->host_norm) cudaFreeHost(a->host_norm);
   for (void* p : a->allocs) cudaFree(p);
@@ -863,7 +899,7 @@ int fmf_adj_forward(fmf_adj* a, int K, const double* const* state0, const double
   upload_inputs(a, state0, theta0, zeta, l1, l2);
   init_bc_fwd(a);
   a->sor_total = 0;
-  for (int t = 0; t < K && !get_status(); ++t) record_step(a);
+  for (int t = 0; t < K && !get_status(); ++t) record_step(a, true);
   *J = objective(a, a->S[SPHI0], nullptr);
   if (state_out)
     for (int f = 0; f < NSTATE; ++f)
@@ -955,11 +991,12 @@ int fmf_adj_rollout(fmf_adj* a, int K, int every, const double* const* state0, c
   const int tlast = (nck - 1) * every;
   for (int t = 0; t < K && !get_status(); ++t) {
     if (t % every == 0) save_state(a, a->ckpt[t / every]);
-    if (slots && t >= tlast) {
+    const bool kept = slots && t >= tlast;
+    if (kept) {
       set_rec(a, a->recs[t - tlast]);
       save_state(a, a->recs[t - tlast].state);
     }
-    record_step(a);
+    record_step(a, !kept);
   }
   if (get_status()) return take_status();
   *J = objective(a, a->S[SPHI0], a->lS[SPHI0]);
@@ -983,7 +1020,7 @@ int fmf_adj_rollout(fmf_adj* a, int K, int every, const double* const* state0, c
           for (int t = u0; t < u0 + every && !get_status(); ++t) {
             set_rec(w, w->recs[t - u0]);
             save_state(w, w->recs[t - u0].state);
-            record_step(w);
+            record_step(w, false);
           }
           FMF_CUDA(cudaStreamSynchronize(w->s));
           t_rec = std::chrono::duration<double>(clk::now() - ta).count();
@@ -1006,7 +1043,7 @@ int fmf_adj_rollout(fmf_adj* a, int K, int every, const double* const* state0, c
         for (int t = t0; t < t1; ++t) {
           set_rec(a, a->recs[t - t0]);
           save_state(a, a->recs[t - t0].state);
-          record_step(a);
+          record_step(a, false);
         }
       }
       a->t_phase[1] += lap(tp);
@@ -1020,12 +1057,12 @@ int fmf_adj_rollout(fmf_adj* a, int K, int every, const double* const* state0, c
       set_rec(a, a->recs[0]);
       for (int t = t0; t < t1; ++t) {
         save_state(a, a->seg[t - t0]);
-        if (t + 1 < t1) record_step(a);
+        if (t + 1 < t1) record_step(a, false);
       }
       a->t_phase[1] += lap(tp);
       for (int t = t1 - 1; t >= t0 && !get_status(); --t) {
         load_state(a, a->seg[t - t0]);
-        record_step(a);
+        record_step(a, false);
         a->t_phase[1] += lap(tp);
         reverse_step(a, a->seg[t - t0]);
         a->t_phase[2] += lap(tp);
