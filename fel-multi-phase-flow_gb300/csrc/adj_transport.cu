@@ -7,6 +7,7 @@
 // flux through its 8-point Gauss sum by hand (with respect to n, d and the swept
 // fraction vd).  Bulk cells: flux = u phi00 dt/dx with phi00 snapped (zero
 // derivative) inside eps_trunc of 0 or 1.
+#include "recip.cuh"
 #include "adj.cuh"
 #include "ops.cuh"
 
@@ -110,8 +111,8 @@ __device__ __forceinline__ GSums gsums(const double* eX, const double* eY, const
       for (int i = 0; i < 2; ++i) {
         const double e = eX[i] * eY[j] * eZ[k] * ed;
         double r = 0.0, ds = 0.0;
-        if (e < INFINITY) {
-          r = 1.0 / (1.0 + e);
+        if (e < INFINITY) {  // 1 + e >= 1: the Newton-Raphson reciprocal, no division
+          r = recip_nr(1.0 + e);
           ds = -(e * r) * r;
         }
         G.s += r;
