@@ -31,10 +31,10 @@ sys.path.insert(0, os.path.join(REPO, "oracle"))
 WORKLOAD = "couette256"
 # Per interior cell of one k_weno2 launch, from the ncu capture summarised in
 # profiles/k_weno2_couette256.md (4,194,304 cells): DRAM bytes read + written
-# (228.9 MB + 173.4 MB), and the executed FP64 instructions (DADD 955.7 M, DMUL
+# (228.2 MB + 173.3 MB), and the executed FP64 instructions (DADD 955.7 M, DMUL
 # 1219.5 M, DFMA 1885.8 M thread instructions); scaled to the workload by its cell
 # count
-WENO_TRAFFIC_PER_CELL = (228.919040e6 + 173.449216e6) / 4194304
+WENO_TRAFFIC_PER_CELL = (228.228864e6 + 173.254144e6) / 4194304
 WENO_FP64_INST_PER_CELL = (955711488 + 1219493888 + 1885798400) / 4194304
 WENO_FP64_FLOPS_PER_CELL = (955711488 + 1219493888 + 2 * 1885798400) / 4194304
 METRIC = "cell-updates/s/step plain FP64 vs mixed at stated error; adjoint/forward cost"
