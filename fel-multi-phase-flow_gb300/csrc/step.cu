@@ -8,6 +8,7 @@
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
+#include <functional>
 #include <map>
 #include <vector>
 
@@ -42,6 +43,8 @@ struct fmf_ctx {
   Grid g;
   cudaStream_t s = nullptr;
   bool own_stream = false;
+  cudaStream_t cs = nullptr;                        // copies overlapping the step (fmf_ctx_step_host)
+  cudaEvent_t ev_in = nullptr, ev_in2 = nullptr, ev_pre = nullptr;  // inputs up (two parts); first segment done
   std::vector<void*> allocs;
   long long bytes = 0;
   // state
@@ -181,6 +184,13 @@ int fmf_ctx_create(const fmf_params* prm, fmf_ctx** out) {
 int fmf_ctx_destroy(fmf_ctx* c) {
   if (!c) return 0;
   if (c->s) cudaStreamSynchronize(c->s);
+  if (c->cs) {
+    cudaStreamSynchronize(c->cs);
+    cudaStreamDestroy(c->cs);
+  }
+  if (c->ev_in) cudaEventDestroy(c->ev_in);
+  if (c->ev_in2) cudaEventDestroy(c->ev_in2);
+  if (c->ev_pre) cudaEventDestroy(c->ev_pre);
   for (auto& e : c->cache) cudaGraphExecDestroy(e.second.exec);
   scratch_set_destroy(c->scr);
   for (void* p : c->allocs) cudaFree(p);
@@ -338,6 +348,18 @@ static void seg_pre(fmf_ctx* c) {
   op::cal_arith_mean(s, g, phin0, P.rhol, P.rhog, c->rhon);
   op::cal_arith_mean(s, g, phi0, P.rmul, P.rmug, c->rmu);
   op::cal_arith_mean(s, g, phin0, P.rmul, P.rmug, c->rmun);
+}
+
+// The rest of the step before the viscous solve: reads uo, vo, wo, p, po (the
+// first part reads u, v, w and phi only).
+static void seg_pre2(fmf_ctx* c) {
+  const fmf_params& P = c->prm;
+  const Grid& g = c->g;
+  cudaStream_t s = c->s;
+  const long n = g.n;
+  const double dxinv = 1.0 / P.dx, dyinv = 1.0 / P.dy, dzinv = 1.0 / P.dz, dt = P.dt;
+  double* phi1 = c->phi + n;
+  double* phin1 = c->phin + n;
   // :532-541
   fused::weno5_both(s, g, dxinv, dyinv, dzinv, c->u, c->v, c->w, c->uo, c->vo, c->wo, c->adv, c->advo,
                     P.precision == FMF_MIXED, c->wsplit);
@@ -476,9 +498,15 @@ static void run_segment(fmf_ctx* c, int id, void (*fn)(fmf_ctx*)) {
   count_launch((int)it->second.launches);
 }
 
-static int step_once(fmf_ctx* c) {
+// One step; after_pre (optional) runs on the host right after the first segment is
+// enqueued (phin is final from there on), before_pre2 (optional) before the second.
+static int step_once(fmf_ctx* c, const std::function<void()>& after_pre = {},
+                     const std::function<void()>& before_pre2 = {}) {
   const Grid& g = c->g;
   run_segment(c, 0, seg_pre);
+  if (after_pre) after_pre();
+  if (before_pre2) before_pre2();
+  run_segment(c, 3, seg_pre2);
   double err = 0.0, err0 = 0.0;
   int lp;
   for (lp = 0; lp <= 20; ++lp) {
@@ -563,6 +591,62 @@ int fmf_ctx_time_stage(fmf_ctx* c, int stage, int reps, float* ms) {
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   return take_status();
+}
+
+// One step from host buffers to host buffers (fmf_capi.h).  The step's first
+// segment reads u, v, w and phi only: those go up first, uo, vo, wo, p, po follow
+// on a second stream while it runs (phin is not an input: the step writes it
+// before reading it).  After the pointer rotation the result's uo, vo, wo, po are
+// this step's inputs u, v, w, p (their buffers are only read during the step) and
+// its phi and phin both hold phin, final once the first segment has run: those
+// eight fields go back on the second stream while the rest of the step runs; u,
+// v, w, p follow the step.
+int fmf_ctx_step_host(fmf_ctx* c, const double* const* in, double* const* out) {
+  if (!c || !in || !out) return FMF_ERR_ARG;
+  ScratchScope scope(c->scr);
+  if (!c->cs) {
+    if (!FMF_CUDA(cudaStreamCreateWithFlags(&c->cs, cudaStreamNonBlocking)) ||
+        !FMF_CUDA(cudaEventCreateWithFlags(&c->ev_in, cudaEventDisableTiming)) ||
+        !FMF_CUDA(cudaEventCreateWithFlags(&c->ev_in2, cudaEventDisableTiming)) ||
+        !FMF_CUDA(cudaEventCreateWithFlags(&c->ev_pre, cudaEventDisableTiming)))
+      return take_status();
+  }
+  const long n = c->g.n;
+  const size_t b = sizeof(double) * n;
+  auto h2d = [&](int f, cudaStream_t st) {
+    FMF_CUDA(cudaMemcpyAsync(field_ptr(c, f), in[f], b, cudaMemcpyHostToDevice, st));
+  };
+  auto d2h = [&](int f, const double* src, cudaStream_t st) {
+    FMF_CUDA(cudaMemcpyAsync(out[f], src, b, cudaMemcpyDeviceToHost, st));
+  };
+  for (int f : {0, 1, 2, 8, 9}) h2d(f, c->s);  // u, v, w, phi
+  FMF_CUDA(cudaEventRecord(c->ev_in, c->s));
+  FMF_CUDA(cudaStreamWaitEvent(c->cs, c->ev_in, 0));
+  for (int f : {3, 4, 5, 6, 7}) h2d(f, c->cs);  // uo, vo, wo, p, po
+  FMF_CUDA(cudaEventRecord(c->ev_in2, c->cs));
+  // the result's uo, vo, wo, po: this step's u, v, w, p
+  d2h(3, c->u, c->cs);
+  d2h(4, c->v, c->cs);
+  d2h(5, c->w, c->cs);
+  d2h(7, c->p, c->cs);
+  c->sor_iters.clear();
+  const bool gr = c->graphs;
+  if (!c->warm) c->graphs = false;
+  double* phin = c->phin;
+  const int st = step_once(
+      c,
+      [&]() {
+        FMF_CUDA(cudaEventRecord(c->ev_pre, c->s));
+        FMF_CUDA(cudaStreamWaitEvent(c->cs, c->ev_pre, 0));
+        for (int f = 8; f < 12; ++f) d2h(f, phin + (f % 2) * n, c->cs);
+      },
+      [&]() { FMF_CUDA(cudaStreamWaitEvent(c->s, c->ev_in2, 0)); });
+  c->graphs = gr;
+  c->warm = true;
+  for (int f : {0, 1, 2, 6}) d2h(f, field_ptr(c, f), c->s);
+  FMF_CUDA(cudaStreamSynchronize(c->s));
+  FMF_CUDA(cudaStreamSynchronize(c->cs));
+  return st ? st : take_status();
 }
 
 int fmf_ctx_step(fmf_ctx* c, int nsteps) {

@@ -61,6 +61,7 @@ def load(path: str | None = None):
     L.fmf_ctx_set_walls.argtypes = [vp, vp, vp, vp, vp]
     L.fmf_ctx_upload.argtypes = [vp, ctypes.POINTER(vp)]
     L.fmf_ctx_download.argtypes = [vp, ctypes.POINTER(vp)]
+    L.fmf_ctx_step_host.argtypes = [vp, ctypes.POINTER(vp), ctypes.POINTER(vp)]
     L.fmf_ctx_sor_iterations.argtypes = [vp, ctypes.POINTER(ctypes.c_int), ip]
     L.fmf_ctx_sor_iterations.restype = ip
     L.fmf_ctx_state_device_ptr.argtypes = [vp, ip, ctypes.POINTER(vp)]
@@ -148,6 +149,11 @@ class Stepper:
 
     def step(self, n: int = 1):
         check(lib().fmf_ctx_step(self.h, int(n)), "step")
+
+    def step_host(self, st_in: np.ndarray, st_out: np.ndarray):
+        """One step from host state st_in to host state st_out (fmf_ctx_step_host;
+        synchronous, the early result fields copied back while the step runs)."""
+        check(lib().fmf_ctx_step_host(self.h, _ptr_array(list(st_in)), _ptr_array(list(st_out))), "step_host")
 
     def sync(self):
         check(lib().fmf_ctx_synchronize(self.h), "synchronize")

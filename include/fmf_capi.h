@@ -375,6 +375,14 @@ int fmf_ctx_upload(fmf_ctx* ctx, const double* const* state);   /* host -> devic
 int fmf_ctx_download(fmf_ctx* ctx, double* const* state);       /* device -> host, async */
 int fmf_ctx_init_bc(fmf_ctx* ctx);                  /* start-up boundary pass, main.f90:322-366 */
 int fmf_ctx_step(fmf_ctx* ctx, int nsteps);         /* enqueue nsteps full time steps */
+/* One step from host buffers to host buffers: in[12] -> out[12] (the state layout
+ * of fmf_ctx_upload; pinned host memory lets the copies overlap the step).  The
+ * same result as fmf_ctx_upload + fmf_ctx_step(ctx, 1) + fmf_ctx_download: uo, vo,
+ * wo, p, po go up while the step's first part runs (phin is not read: the step
+ * writes it first), and the result fields that are final early (uo, vo, wo, po,
+ * phi, phin) come back while the rest runs.  Returns after the result is in out.
+ * No counterpart in the reference: the drop-in form of its time-step loop body. */
+int fmf_ctx_step_host(fmf_ctx* ctx, const double* const* in, double* const* out);
 int fmf_ctx_synchronize(fmf_ctx* ctx);
 int fmf_ctx_set_stream(fmf_ctx* ctx, void* cuda_stream);
 /* per-step SOR iteration counts of the last fmf_ctx_step call (up to cap entries) */

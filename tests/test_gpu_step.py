@@ -118,3 +118,26 @@ def test_division_free_rsqrt(fmf_lib):
     err = ctypes.c_double(-1.0)
     assert L.fmf_check_rsqrt(1 << 22, ctypes.byref(err)) == 0
     assert 0.0 <= err.value <= 2 * 2.0 ** -52, err.value
+
+
+def test_step_host_matches_upload_step_download(fmf_lib):
+    """fmf_ctx_step_host (copies overlapping the step) gives bit for bit the state of
+    upload + step + download, step after step."""
+    import torch
+
+    cfg = C.get("couette32")
+    a = capi.Stepper(cfg)
+    st = a.initial_state()
+    b = capi.Stepper(cfg)
+    pin = torch.empty((12,) + cfg.shape, dtype=torch.float64, pin_memory=True).numpy()
+    pin[:] = st
+    ref = st.copy()
+    for _ in range(3):
+        b.step_host(pin, pin)
+        a.upload(ref)
+        a.step(1)
+        a.download(ref)
+        a.sync()
+        assert np.array_equal(pin, ref)
+    a.close()
+    b.close()
