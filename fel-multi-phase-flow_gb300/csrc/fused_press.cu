@@ -19,6 +19,7 @@
 // Half the FFT and Thomas work of the full-spectrum drop-in path (op::fft_*,
 // op::tdma_modes), which keeps the reference's full spectra for the C-ABI.
 // Spectrum layout: (kx, j, kz) at kx + H ((j-1) + nj kz), H = ni/2 + 1.
+#include "../../include/fmf_capi.h"
 #include "fft.cuh"
 #include "fused.cuh"
 #include "recip.cuh"
@@ -193,8 +194,16 @@ void pressure_half(cudaStream_t s, const Grid& g, double rho, double dxinv, doub
   const int M = g.ni / 2, H = M + 1;
   const double2 *twM = op::fft_twiddles(M), *twN = op::fft_twiddles(g.ni), *twz = op::fft_twiddles(g.nk);
   const int rows = g.nj * g.nk;  // a multiple of kRows for power-of-two nj, nk >= 4
-  k_rfft_x_fwd<<<rows / kRows, 256, sizeof(double) * kRows * 2 * M, s>>>(g, div, tr, ti, twM, twN);
+  const size_t smf = sizeof(double) * kRows * 2 * M, smi = sizeof(double) * kRows * (2 * H + 2 * M);
   const size_t smz = sizeof(double) * 2 * g.nk * kTileZ;
+  // shared memory per block: 227 KB at most on this GPU (ni up to 1024, nk up to 512)
+  if (smi > 232448 || smz > 232448) {
+    set_status(FMF_ERR_ARG);
+    return;
+  }
+  cudaFuncSetAttribute(k_rfft_x_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smf);
+  cudaFuncSetAttribute(k_rfft_x_inv, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smi);
+  k_rfft_x_fwd<<<rows / kRows, 256, smf, s>>>(g, div, tr, ti, twM, twN);
   cudaFuncSetAttribute(k_fft_z_half, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smz);
   const dim3 gz((unsigned)((H + kTileZ - 1) / kTileZ), (unsigned)g.nj);
   k_fft_z_half<<<gz, 256, smz, s>>>(g, tr, ti, pr, pi, twz, -1.0, 1.0 / ((double)g.ni * (double)g.nk));
@@ -203,7 +212,7 @@ void pressure_half(cudaStream_t s, const Grid& g, double rho, double dxinv, doub
   k_tdma_half<<<dim3((unsigned)((H + 127) / 128), (unsigned)g.nk), 128, 0, s>>>(
       g, dx2r, dz2r, pi_ * 2.0 / (double)g.ni, pi_ * 2.0 / (double)g.nk, as_f, an_f, ap_f, pr, pi, at);
   k_fft_z_half<<<gz, 256, smz, s>>>(g, pr, pi, tr, ti, twz, +1.0, 1.0);
-  k_rfft_x_inv<<<rows / kRows, 256, sizeof(double) * kRows * (2 * H + 2 * M), s>>>(g, tr, ti, dp, twM, twN);
+  k_rfft_x_inv<<<rows / kRows, 256, smi, s>>>(g, tr, ti, dp, twM, twN);
   count_launch(5);
 }
 
