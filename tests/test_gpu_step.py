@@ -120,15 +120,17 @@ def test_division_free_rsqrt(fmf_lib):
     assert 0.0 <= err.value <= 2 * 2.0 ** -52, err.value
 
 
-def test_step_host_matches_upload_step_download(fmf_lib):
-    """fmf_ctx_step_host (copies overlapping the step) gives bit for bit the state of
-    upload + step + download, step after step."""
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_step_host_matches_upload_step_download(fmf_lib, prec):
+    """fmf_ctx_step_host (copies overlapping the step, phin not uploaded) gives bit for
+    bit the state of upload + step + download, step after step, in both precisions."""
     import torch
 
     cfg = C.get("couette32")
-    a = capi.Stepper(cfg)
+    p = capi.FMF_FP64 if prec == "fp64" else capi.FMF_MIXED
+    a = capi.Stepper(cfg, precision=p)
     st = a.initial_state()
-    b = capi.Stepper(cfg)
+    b = capi.Stepper(cfg, precision=p)
     pin = torch.empty((12,) + cfg.shape, dtype=torch.float64, pin_memory=True).numpy()
     pin[:] = st
     ref = st.copy()
