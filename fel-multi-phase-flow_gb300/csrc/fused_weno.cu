@@ -66,9 +66,8 @@ __device__ __forceinline__ double wdir(const double* __restrict__ q, long c, lon
 
 // FP32 variant for the mixed-precision step.
 //
-// Inputs: the six velocity fields as float pairs (hi, lo), hi = (float)q and
-// lo = (float)(q - hi), written once per step by k_split6 (q - hi is exact in
-// double, so hi + lo holds q to about 2^-48).  A difference is formed as
+// Inputs: the six velocity fields as float pairs (hi, lo) written once per step by
+// k_split6 (split_pair: hi + lo holds q to about 2^-48).  A difference is formed as
 // (hi1 - hi0) + (lo1 - lo0): accurate to float precision relative to the
 // difference itself, as a double difference rounded to float would be, but
 // on the FP32 pipe (converting each double where a stencil reads it put about
@@ -84,17 +83,31 @@ __device__ __forceinline__ double wdir(const double* __restrict__ q, long c, lon
 // indicators are 0 (data exactly linear in float: the quotient is then d2, the
 // reference's limit); the upper keeps eps * d2 finite.  Differences below 2^-100
 // (a flat stencil) give 0.
+// The pair (hi, lo) of q from its bits, without FP64-pipe instructions: hi is q's
+// significand cut to float's 24 bits (toward zero), lo the 29 bits below them as
+// a float (rounded to 24 of them), so hi + lo = q to about 2^-48 of q.  Magnitudes
+// below 2^-126 give (0, 0); above float's range (and inf, NaN) the float
+// conversion of q and lo = 0.
+__device__ __forceinline__ float2 split_pair(double q) {
+  const long long b = __double_as_longlong(q);
+  const int hb = (int)(b >> 32);
+  const unsigned lb = (unsigned)b;
+  const int e = (hb >> 20) & 0x7ff;
+  const unsigned sg = (unsigned)hb & 0x80000000u;
+  if (e < 897) return make_float2(__uint_as_float(sg), __uint_as_float(sg));
+  if (e > 1150) return make_float2((float)q, 0.0f);
+  const float hi = __uint_as_float(sg | ((unsigned)(e - 896) << 23) | (((unsigned)hb & 0xfffffu) << 3) | (lb >> 29));
+  // q - hi = (low 29 bits) 2^(e - 1075), same sign as q; below 2^-126 of scale: 0
+  float lo = e >= 949 ? (float)(lb & 0x1fffffffu) * __uint_as_float((unsigned)(e - 948) << 23) : 0.0f;
+  return make_float2(hi, sg ? -lo : lo);
+}
 __global__ void k_split6(long n, const double* __restrict__ u, const double* __restrict__ v,
                          const double* __restrict__ w, const double* __restrict__ uo, const double* __restrict__ vo,
                          const double* __restrict__ wo, float2* __restrict__ out) {
   const double* src[6] = {u, v, w, uo, vo, wo};
   for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) {
 #pragma unroll
-    for (int f = 0; f < 6; ++f) {
-      const double q = __ldg(src[f] + t);
-      const float hi = (float)q;
-      out[f * n + t] = make_float2(hi, (float)(q - (double)hi));
-    }
+    for (int f = 0; f < 6; ++f) out[f * n + t] = split_pair(__ldg(src[f] + t));
   }
 }
 
