@@ -127,6 +127,21 @@ struct fmf_adj {
   adj::GraphCache rgraphs;     // replays of the last forward viscous cycle, one per record slot
   adj::GraphCache pgraphs;     // the parts before and after the viscous solve of steps not recorded
   bool rec_warm = false;       // a step has run on this handle (scratch sized for capture)
+  // The state continues from this handle's previous record_step (cont): that step's
+  // advection of (u, v, w) is this step's of (uo, vo, wo), and its surface tension
+  // (and curvatures) of phin(1) this step's of phi(1); where they were written
+  bool cont = false;
+  bool no_carry = false;  // FMF_STEP_CACHE=0 at creation: recompute both levels every step
+  double *prev_adv[3] = {nullptr, nullptr, nullptr}, *prev_sfstn[3] = {nullptr, nullptr, nullptr};
+  double* prev_kapn = nullptr;
+  // The reverse counterpart: the transposed advection and surface tension are linear
+  // in the adjoint they receive, and step t's (uo, vo, wo) and phi(1) are step t-1's
+  // (u, v, w) and phin(1).  reverse_step(t) leaves the adjoints of step t's advo and
+  // sfst in lcarry (6n doubles: ladvo, then lsfst) instead of transposing them;
+  // reverse_step(t-1) adds them to its adv and sfstn adjoints before their
+  // transposes (carry_in).
+  double* lcarry = nullptr;
+  bool carry_in = false;
   double* host_norm = nullptr;  // pinned
   fmf_adj* worker = nullptr;    // recomputes the next segment while this handle reverses one
 };
@@ -147,6 +162,16 @@ struct Scope {
   ~Scope() { scratch_set_use(nullptr); }
 };
 void zero(fmf_adj* a, double* p, long n) { FMF_CUDA(cudaMemsetAsync(p, 0, sizeof(double) * n, a->s)); }
+// dst[q] += src[q], q = 0..2, n points each
+void add3(cudaStream_t s, long n, double* const* src, double* const* dst) {
+  const double *s0 = src[0], *s1 = src[1], *s2 = src[2];
+  double *d0 = dst[0], *d1 = dst[1], *d2 = dst[2];
+  flat(s, n, [=] __device__(long t) {
+    d0[t] += s0[t];
+    d1[t] += s1[t];
+    d2[t] += s2[t];
+  });
+}
 
 // the record fields of a point at slot r
 void set_rec(fmf_adj* a, const fmf_adj::Rec& r) {
@@ -329,6 +354,7 @@ double objective(fmf_adj* a, const double* phi0, double* lphi) {
 namespace {
 // main.f90:322-366 on the working state, keeping what its adjoint reads
 void init_bc_fwd(fmf_adj* a) {
+  a->cont = false;
   const fmf_params& P = a->prm;
   const Grid& g = a->g;
   cudaStream_t s = a->s;
@@ -385,8 +411,9 @@ void run_part(fmf_adj* a, bool graphs, int id, const std::function<void()>& body
   long long per_launch = 0;
   const cudaGraphExec_t exec = adj::cached_graph(
       a->s, &a->pgraphs,
-      {(const void*)(intptr_t)(id + 1), a->gx1[0], a->adv[0], a->E[0], a->ustar[0], a->kap, a->S[0], a->un[0]}, body,
-      &per_launch);
+      {(const void*)(intptr_t)(id + 1 + (a->cont ? 100 : 0)), a->gx1[0], a->adv[0], a->E[0], a->ustar[0], a->kap,
+       a->S[0], a->un[0], a->prev_adv[0], a->prev_sfstn[0], a->prev_kapn},
+      body, &per_launch);
   if (!exec) {
     body();
     return;
@@ -404,8 +431,19 @@ int record_step(fmf_adj* a, bool graphs) {
   const double dxi = 1.0 / P.dx, dyi = 1.0 / P.dy, dzi = 1.0 / P.dz, dt = P.dt;
   double** S = a->S;
   double *phi0 = S[SPHI0], *phi1 = S[SPHI1], *phn0 = S[SPHIN0], *phn1 = S[SPHIN1];
+  const bool carry = a->cont;
+  const bool csf_fused = fused::csf_supported(g);
   // the step before the viscous solve
   auto pre = [&]() {
+    if (carry) {
+      // the previous step's terms, copied before this step overwrites them where
+      // both steps use the same record slot
+      for (int q = 0; q < 3; ++q) {
+        dcopy(a, a->prev_adv[q], a->advo[q], n);
+        dcopy(a, a->prev_sfstn[q], a->sfst[q], n);
+      }
+      if (csf_fused) dcopy(a, a->prev_kapn, a->kap, 3 * n);
+    }
     // :491-503
     fused::vertex_gradient(s, g, dxi, dyi, dzi, phi1, a->gx1[0], a->gx1[1], a->gx1[2]);
     {
@@ -433,19 +471,23 @@ int record_step(fmf_adj* a, bool graphs) {
     op::cal_arith_mean(s, g, phn0, P.rhol, P.rhog, a->rhon);
     op::cal_arith_mean(s, g, phi0, P.rmul, P.rmug, a->rmu);
     op::cal_arith_mean(s, g, phn0, P.rmul, P.rmug, a->rmun);
-    fused::weno5_both(s, g, dxi, dyi, dzi, S[SU], S[SV], S[SW], S[SUO], S[SVO], S[SWO], a->adv, a->advo, false);
+    if (carry)
+      fused::weno5_one(s, g, dxi, dyi, dzi, S[SU], S[SV], S[SW], a->adv, false);
+    else
+      fused::weno5_both(s, g, dxi, dyi, dzi, S[SU], S[SV], S[SW], S[SUO], S[SVO], S[SWO], a->adv, a->advo, false);
     op::calphat(s, g, S[SP], S[SPO], a->phat);
     op::cal_grad_prs(s, g, dxi, dyi, dzi, a->phat, a->prs[0], a->prs[1], a->prs[2]);
     fused::explicit_viscous(s, g, dxi, dyi, dzi, S[SU], S[SV], S[SW], a->rmu, a->tau, a->vis, a->sk);
     // :545-573 (the fused kernel where the grid tiles; csf_T differentiates the same
     // sequence of reference subroutines either way)
-    if (fused::csf_supported(g)) {
-      fused::csf_force(s, g, dxi, dyi, dzi, P.rhol, P.rhog, P.sigma, phi1, a->sfst[0], a->sfst[1], a->sfst[2], false,
-                       a->kap);
+    if (csf_fused) {
+      if (!carry)
+        fused::csf_force(s, g, dxi, dyi, dzi, P.rhol, P.rhog, P.sigma, phi1, a->sfst[0], a->sfst[1], a->sfst[2],
+                         false, a->kap);
       fused::csf_force(s, g, dxi, dyi, dzi, P.rhol, P.rhog, P.sigma, phn1, a->sfstn[0], a->sfstn[1], a->sfstn[2],
                        false, a->kapn);
     } else {
-      csf_fwd(a, phi1, a->sfst);
+      if (!carry) csf_fwd(a, phi1, a->sfst);
       csf_fwd(a, phn1, a->sfstn);
     }
     // :579-623
@@ -522,6 +564,12 @@ int record_step(fmf_adj* a, bool graphs) {
   run_part(a, graphs, 1, post);
   a->rec_warm = true;
   FMF_CUDA(cudaGetLastError());
+  for (int q = 0; q < 3; ++q) {
+    a->prev_adv[q] = a->adv[q];
+    a->prev_sfstn[q] = a->sfstn[q];
+  }
+  a->prev_kapn = a->kapn;
+  a->cont = get_status() == 0 && !a->no_carry;
   return get_status();
 }
 
@@ -529,14 +577,17 @@ void save_state(fmf_adj* a, double* dst) {
   for (int f = 0; f < NSTATE; ++f) dcopy(a, a->S[f], dst + (long)f * a->g.n, a->g.n);
 }
 void load_state(fmf_adj* a, const double* src) {
+  a->cont = false;
   for (int f = 0; f < NSTATE; ++f) dcopy(a, src + (long)f * a->g.n, a->S[f], a->g.n);
 }
 
 // Reverse of one step.  On entry lS holds the adjoint of the state after the step;
 // on exit the adjoint of the state before it.  The record of the step (record_step
 // run from that start state) must be current; the step-start state itself is passed
-// in st (NSTATE fields).
-void reverse_step(fmf_adj* a, const double* st) {
+// in st (NSTATE fields).  defer: the next reverse_step is that of the previous step
+// of the same rollout, which then transposes this step's (uo, vo, wo) advection and
+// phi(1) surface tension together with its own (u, v, w) and phin(1) ones.
+void reverse_step(fmf_adj* a, const double* st, bool defer) {
   const fmf_params& P = a->prm;
   const Grid& g = a->g;
   cudaStream_t s = a->s;
@@ -656,12 +707,19 @@ void reverse_step(fmf_adj* a, const double* st) {
   check_stage(a, "src");
   }
   // :545-573 surface tension of phi(1) and phin(1)
+  double* const cadv[3] = {a->lcarry, a->lcarry + n, a->lcarry + 2 * n};
+  double* const cfst[3] = {a->lcarry + 3 * n, a->lcarry + 4 * n, a->lcarry + 5 * n};
   {
-    const double* lf[3] = {a->lsfst[0], a->lsfst[1], a->lsfst[2]};
     // the curvatures recorded by the fused forward kernel where the grid tiles
     const bool rec = fused::csf_supported(g);
-    adj::csf_T(s, g, dxi, dyi, dzi, P.rhol, P.rhog, P.sigma, ST(SPHI1), lf, lS[SPHI1], a->work + 3 * n + 1024,
-               rec ? a->kap : nullptr);
+    if (defer) {
+      for (int q = 0; q < 3; ++q) dcopy(a, a->lsfst[q], cfst[q], n);
+    } else {
+      const double* lf[3] = {a->lsfst[0], a->lsfst[1], a->lsfst[2]};
+      adj::csf_T(s, g, dxi, dyi, dzi, P.rhol, P.rhog, P.sigma, ST(SPHI1), lf, lS[SPHI1], a->work + 3 * n + 1024,
+                 rec ? a->kap : nullptr);
+    }
+    if (a->carry_in) add3(s, n, cfst, a->lsfstn);
     const double* lfn[3] = {a->lsfstn[0], a->lsfstn[1], a->lsfstn[2]};
     adj::csf_T(s, g, dxi, dyi, dzi, P.rhol, P.rhog, P.sigma, a->phn1f, lfn, a->lphn1, a->work + 3 * n + 1024,
                rec ? a->kapn : nullptr);
@@ -684,12 +742,18 @@ void reverse_step(fmf_adj* a, const double* st) {
     });
   }
   {
+    if (a->carry_in) add3(s, n, cadv, a->ladv);
     const double* la[3] = {a->ladv[0], a->ladv[1], a->ladv[2]};
     adj::weno_T(s, g, dxi, dyi, dzi, ST(SU), ST(SV), ST(SW), la, lS[SU], lS[SV], lS[SW], a->work + 3 * n + 1024);
-    const double* lao[3] = {a->ladvo[0], a->ladvo[1], a->ladvo[2]};
-    adj::weno_T(s, g, dxi, dyi, dzi, ST(SUO), ST(SVO), ST(SWO), lao, lS[SUO], lS[SVO], lS[SWO],
-                a->work + 3 * n + 1024);
+    if (defer) {
+      for (int q = 0; q < 3; ++q) dcopy(a, a->ladvo[q], cadv[q], n);
+    } else {
+      const double* lao[3] = {a->ladvo[0], a->ladvo[1], a->ladvo[2]};
+      adj::weno_T(s, g, dxi, dyi, dzi, ST(SUO), ST(SVO), ST(SWO), lao, lS[SUO], lS[SVO], lS[SWO],
+                  a->work + 3 * n + 1024);
+    }
   }
+  a->carry_in = defer;
   check_stage(a, "weno");
   // :526-529 mixture properties (phi0 after its contact-angle ghosts, phin0)
   adj::mean_T(s, g, P.rhol, P.rhog, a->lrho, lS[SPHI0]);
@@ -760,6 +824,7 @@ void reverse_init_bc(fmf_adj* a) {
 void upload_inputs(fmf_adj* a, const double* const* st, const double* th, const double* ze, const double* l1,
                    const double* l2) {
   const size_t b = sizeof(double) * a->g.n;
+  a->cont = false;
   for (int f = 0; f < NSTATE; ++f) FMF_CUDA(cudaMemcpyAsync(a->S[f], st[f], b, cudaMemcpyHostToDevice, a->s));
   FMF_CUDA(cudaMemcpyAsync(a->theta0, th, b, cudaMemcpyHostToDevice, a->s));
   FMF_CUDA(cudaMemcpyAsync(a->zeta, ze, b, cudaMemcpyHostToDevice, a->s));
@@ -776,6 +841,7 @@ int fmf_adj_create(const fmf_params* prm, fmf_adj** out) {
   if (!p2(prm->ni) || !p2(prm->nj) || !p2(prm->nk) || prm->ni < 16) return FMF_ERR_ARG;
   fmf_adj* a = new fmf_adj();
   a->prm = *prm;
+  if (const char* e = std::getenv("FMF_STEP_CACHE")) a->no_carry = std::atoi(e) == 0;
   a->g = Grid(prm->ni, prm->nj, prm->nk);
   a->scr = scratch_set_create();
   // the highest stream priority: the reverse steps are the critical path when a
@@ -825,6 +891,7 @@ int fmf_adj_create(const fmf_params* prm, fmf_adj** out) {
   a->sorpart = dalloc(a, fused::sor_parts(a->g));
   a->csfwork = dalloc(a, 21 * n);
   a->work = dalloc(a, 3 * n + 1024 + 63 * n);  // SOR adjoint, then CSF (42n) or WENO5 (63n) adjoints
+  a->lcarry = dalloc(a, 6 * n);
   FMF_CUDA(cudaMallocHost(&a->host_norm, sizeof(double) * 2));
   grow_recs(a, 1);  // the record of the current step
   if (a->recs.empty()) {
@@ -1004,6 +1071,7 @@ int fmf_adj_rollout(fmf_adj* a, int K, int every, const double* const* state0, c
     if (f != SPHI0) zero(a, a->lS[f], n);
   a->t_phase[0] += lap(tp);
   // reverse, segment by segment
+  a->carry_in = false;
   for (int c = nck - 1; c >= 0 && !get_status(); --c) {
     const int t0 = c * every, t1 = std::min(K, t0 + every);
     if (w) {
@@ -1028,7 +1096,7 @@ int fmf_adj_rollout(fmf_adj* a, int K, int every, const double* const* state0, c
       }
       for (int t = t1 - 1; t >= t0 && !get_status(); --t) {
         set_rec(a, a->recs[t - t0]);
-        reverse_step(a, a->recs[t - t0].state);
+        reverse_step(a, a->recs[t - t0].state, t > 0 && !a->no_carry);
       }
       a->t_phase[2] += lap(tp);
       if (th.joinable()) {
@@ -1049,7 +1117,7 @@ int fmf_adj_rollout(fmf_adj* a, int K, int every, const double* const* state0, c
       a->t_phase[1] += lap(tp);
       for (int t = t1 - 1; t >= t0 && !get_status(); --t) {
         set_rec(a, a->recs[t - t0]);
-        reverse_step(a, a->recs[t - t0].state);
+        reverse_step(a, a->recs[t - t0].state, t > 0 && !a->no_carry);
       }
       a->t_phase[2] += lap(tp);
     } else {
@@ -1064,7 +1132,7 @@ int fmf_adj_rollout(fmf_adj* a, int K, int every, const double* const* state0, c
         load_state(a, a->seg[t - t0]);
         record_step(a, false);
         a->t_phase[1] += lap(tp);
-        reverse_step(a, a->seg[t - t0]);
+        reverse_step(a, a->seg[t - t0], t > 0 && !a->no_carry);
         a->t_phase[2] += lap(tp);
       }
     }

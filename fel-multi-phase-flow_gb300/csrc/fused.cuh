@@ -14,6 +14,9 @@ namespace fused {
 void weno5_both(cudaStream_t s, const Grid& g, double dxi, double dyi, double dzi, const double* u,
                 const double* v, const double* w, const double* uo, const double* vo, const double* wo,
                 double* const* adv, double* const* advo, bool fp32 = false, float2* split = nullptr);
+// cal_advu_weno5 of (u, v, w) alone into adv (fp32: split pairs of 3 fields, 3 n float2)
+void weno5_one(cudaStream_t s, const Grid& g, double dxi, double dyi, double dzi, const double* u, const double* v,
+               const double* w, double* const* adv, bool fp32 = false, float2* split = nullptr);
 
 // cal_grad_p2a (the vertex gradients of q at (i+1/2, j+1/2, k+1/2), i, j, k in
 // -2..n+2) in fewer FP64 operations than the reference's order

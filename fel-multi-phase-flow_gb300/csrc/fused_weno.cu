@@ -1,5 +1,7 @@
-// fused_weno.cu -- WENO5 advection of both velocity levels in one kernel (the two
-// cal_advu_weno5 calls of main.f90:532-533), compiled with multiply-add contraction.
+// fused_weno.cu -- WENO5 advection (the two cal_advu_weno5 calls of main.f90:532-533:
+// both velocity levels in one kernel, or the (u, v, w) level alone where the step
+// reuses the previous step's result for (uo, vo, wo)), compiled with multiply-add
+// contraction.
 //
 // weno5.h forms both one-sided reconstructions and multiplies the unused one by
 // vel-|vel| = 0 (or vel+|vel| = 0); here only the upwind side is evaluated, which
@@ -7,6 +9,8 @@
 // quotient (wdir) that needs about two thirds of the remaining FP64 operations.
 // The grid has one thread per interior cell (x fastest, 32 x 4 block, one k plane
 // per grid z).
+#include <cstring>
+
 #include "../../include/fmf_capi.h"
 #include "fused.cuh"
 #include "recip.cuh"
@@ -67,7 +71,7 @@ __device__ __forceinline__ double wdir(const double* __restrict__ q, long c, lon
 // FP32 variant for the mixed-precision step.
 //
 // Inputs: the six velocity fields as float pairs (hi, lo) written once per step by
-// k_split6 (split_pair: hi + lo holds q to about 2^-48).  A difference is formed as
+// k_split (split_pair: hi + lo holds q to about 2^-48).  A difference is formed as
 // (hi1 - hi0) + (lo1 - lo0): accurate to float precision relative to the
 // difference itself, as a double difference rounded to float would be, but
 // on the FP32 pipe (converting each double where a stencil reads it put about
@@ -85,9 +89,10 @@ __device__ __forceinline__ double wdir(const double* __restrict__ q, long c, lon
 // (a flat stencil) give 0.
 // The pair (hi, lo) of q from its bits, without FP64-pipe instructions: hi is q's
 // significand cut to float's 24 bits (toward zero), lo the 29 bits below them as
-// a float (rounded to 24 of them), so hi + lo = q to about 2^-48 of q.  Magnitudes
-// below 2^-126 give (0, 0); above float's range (and inf, NaN) the float
-// conversion of q and lo = 0.
+// a float (rounded to 24 of them), so hi + lo = q to about 2^-48 of q while lo is
+// a normal float (|q| above about 2^-97; below that lo is subnormal and the pair
+// holds q to 2^-149 absolute).  Magnitudes below 2^-126 give (0, 0); above
+// float's range (and inf, NaN) the float conversion of q and lo = 0.
 __device__ __forceinline__ float2 split_pair(double q) {
   const long long b = __double_as_longlong(q);
   const int hb = (int)(b >> 32);
@@ -97,17 +102,23 @@ __device__ __forceinline__ float2 split_pair(double q) {
   if (e < 897) return make_float2(__uint_as_float(sg), __uint_as_float(sg));
   if (e > 1150) return make_float2((float)q, 0.0f);
   const float hi = __uint_as_float(sg | ((unsigned)(e - 896) << 23) | (((unsigned)hb & 0xfffffu) << 3) | (lb >> 29));
-  // q - hi = (low 29 bits) 2^(e - 1075), same sign as q; below 2^-126 of scale: 0
-  float lo = e >= 949 ? (float)(lb & 0x1fffffffu) * __uint_as_float((unsigned)(e - 948) << 23) : 0.0f;
+  // q - hi = (low 29 bits) 2^(e - 1075), same sign as q.  The power of two is a
+  // normal float for e >= 949; below that it is applied as 2^-64 2^(e - 1011), both
+  // normal, so lo keeps its bits until the product itself leaves float's range
+  const float L = (float)(lb & 0x1fffffffu);
+  float lo = e >= 949 ? L * __uint_as_float((unsigned)(e - 948) << 23)
+                      : (L * 0x1p-64f) * __uint_as_float((unsigned)(e - 884) << 23);
   return make_float2(hi, sg ? -lo : lo);
 }
-__global__ void k_split6(long n, const double* __restrict__ u, const double* __restrict__ v,
-                         const double* __restrict__ w, const double* __restrict__ uo, const double* __restrict__ vo,
-                         const double* __restrict__ wo, float2* __restrict__ out) {
-  const double* src[6] = {u, v, w, uo, vo, wo};
+struct SplitSrc {
+  const double* f[6];
+};
+// the split pairs of nf (3 or 6) fields, field f at out[f n ..]
+template <int NF>
+__global__ void k_split(long n, SplitSrc src, float2* __restrict__ out) {
   for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) {
 #pragma unroll
-    for (int f = 0; f < 6; ++f) out[f * n + t] = split_pair(__ldg(src[f] + t));
+    for (int f = 0; f < NF; ++f) out[f * n + t] = split_pair(__ldg(src.f[f] + t));
   }
 }
 
@@ -158,8 +169,8 @@ __device__ __forceinline__ float wdir_f32(const float2* __restrict__ q, long c, 
   const float den = fmaf(X, 1.0f / 6.0f, fmaf(Z, 0.5f, Y));
   return (fabsf(vsum) * kx) * (__fdividef(num, den) * s);
 }
-// V[f] = the split pair arrays of u, v, w (f = 0..2) and uo, vo, wo (3..5)
-__global__ void __launch_bounds__(128) k_weno2_f32(Grid g, float kx, float ky, float kz,
+// sp: the split pair arrays of u, v, w (then uo, vo, wo for the second level)
+__global__ void __launch_bounds__(128) k_weno2_f32(Grid g, int nlev, float kx, float ky, float kz,
                                                    const float2* __restrict__ sp, double* __restrict__ au,
                                                    double* __restrict__ av, double* __restrict__ aw,
                                                    double* __restrict__ auo, double* __restrict__ avo,
@@ -171,7 +182,7 @@ __global__ void __launch_bounds__(128) k_weno2_f32(Grid g, float kx, float ky, f
   const long X = 1, Y = g.sy, Z = g.sz;
   const long c = g.at(i, j, k);
 #pragma unroll 1
-  for (int lev = 0; lev < 2; ++lev) {
+  for (int lev = 0; lev < nlev; ++lev) {
     const float2* U = sp + (long)(3 * lev) * g.n;
     const float2* V = U + g.n;
     const float2* W = V + g.n;
@@ -195,7 +206,8 @@ __global__ void __launch_bounds__(128) k_weno2_f32(Grid g, float kx, float ky, f
   }
 }
 
-__global__ void __launch_bounds__(128) k_weno2(Grid g, double dxi, double dyi, double dzi, const double* __restrict__ u,
+__global__ void __launch_bounds__(128) k_weno2(Grid g, int nlev, double dxi, double dyi, double dzi,
+                                               const double* __restrict__ u,
                                                const double* __restrict__ v, const double* __restrict__ w,
                                                const double* __restrict__ uo, const double* __restrict__ vo,
                                                const double* __restrict__ wo, double* __restrict__ au,
@@ -210,7 +222,7 @@ __global__ void __launch_bounds__(128) k_weno2(Grid g, double dxi, double dyi, d
   const long c = g.at(i, j, k);
   const double kx = dxi * (1.0 / 24.0), ky = dyi * (1.0 / 24.0), kz = dzi * (1.0 / 24.0);
 #pragma unroll 1
-  for (int lev = 0; lev < 2; ++lev) {
+  for (int lev = 0; lev < nlev; ++lev) {
     const double* U = lev ? uo : u;
     const double* V = lev ? vo : v;
     const double* W = lev ? wo : w;
@@ -237,29 +249,84 @@ __global__ void __launch_bounds__(128) k_weno2(Grid g, double dxi, double dyi, d
 }
 }  // namespace
 
-// Both levels; only interior cells are written (the fused step never reads the
-// halo of the advection terms, which cal_advu_weno5.f:44-52 sets to zero).  The
-// FP32 variant first writes the split pairs of the six fields into `split`
-// (6 n float2).
-void weno5_both(cudaStream_t s, const Grid& g, double dxi, double dyi, double dzi, const double* u,
-                const double* v, const double* w, const double* uo, const double* vo, const double* wo,
-                double* const* adv, double* const* advo, bool fp32, float2* split) {
+// One level (nlev = 1: u, v, w into adv) or both (nlev = 2: uo, vo, wo into advo as
+// well); only interior cells are written (the fused step never reads the halo of
+// the advection terms, which cal_advu_weno5.f:44-52 sets to zero).  The FP32
+// variant first writes the split pairs of the 3 nlev fields into `split`.
+static void weno5_levels(cudaStream_t s, const Grid& g, int nlev, double dxi, double dyi, double dzi,
+                         const double* u, const double* v, const double* w, const double* uo, const double* vo,
+                         const double* wo, double* const* adv, double* const* advo, bool fp32, float2* split) {
   dim3 b(32, 4, 1);
   dim3 gr((unsigned)((g.ni + 31) / 32), (unsigned)((g.nj + 3) / 4), (unsigned)g.nk);
+  double* const ao[3] = {advo ? advo[0] : nullptr, advo ? advo[1] : nullptr, advo ? advo[2] : nullptr};
   if (fp32) {
     if (!split) {
       set_status(FMF_ERR_ARG);
       return;
     }
-    k_split6<<<152 * 8, 256, 0, s>>>(g.n, u, v, w, uo, vo, wo, split);
-    k_weno2_f32<<<gr, b, 0, s>>>(g, (float)(dxi / 24.0), (float)(dyi / 24.0), (float)(dzi / 24.0), split, adv[0],
-                                 adv[1], adv[2], advo[0], advo[1], advo[2]);
+    const SplitSrc src{{u, v, w, uo, vo, wo}};
+    if (nlev == 2)
+      k_split<6><<<152 * 8, 256, 0, s>>>(g.n, src, split);
+    else
+      k_split<3><<<152 * 8, 256, 0, s>>>(g.n, src, split);
+    k_weno2_f32<<<gr, b, 0, s>>>(g, nlev, (float)(dxi / 24.0), (float)(dyi / 24.0), (float)(dzi / 24.0), split,
+                                 adv[0], adv[1], adv[2], ao[0], ao[1], ao[2]);
     count_launch(2);
     return;
   }
-  k_weno2<<<gr, b, 0, s>>>(g, dxi, dyi, dzi, u, v, w, uo, vo, wo, adv[0], adv[1], adv[2], advo[0], advo[1], advo[2]);
+  k_weno2<<<gr, b, 0, s>>>(g, nlev, dxi, dyi, dzi, u, v, w, uo, vo, wo, adv[0], adv[1], adv[2], ao[0], ao[1], ao[2]);
   count_launch();
+}
+
+void weno5_both(cudaStream_t s, const Grid& g, double dxi, double dyi, double dzi, const double* u,
+                const double* v, const double* w, const double* uo, const double* vo, const double* wo,
+                double* const* adv, double* const* advo, bool fp32, float2* split) {
+  weno5_levels(s, g, 2, dxi, dyi, dzi, u, v, w, uo, vo, wo, adv, advo, fp32, split);
+}
+
+void weno5_one(cudaStream_t s, const Grid& g, double dxi, double dyi, double dzi, const double* u, const double* v,
+               const double* w, double* const* adv, bool fp32, float2* split) {
+  weno5_levels(s, g, 1, dxi, dyi, dzi, u, v, w, nullptr, nullptr, nullptr, adv, nullptr, fp32, split);
+}
+
+// n doubles of both signs spread over magnitudes 2^-96 .. 2^127 with pseudo-random
+// significands; the largest |(hi + lo) - q| / |q| of their split pairs, as the
+// ordered bits of a non-negative double
+__global__ void k_check_split(long n, unsigned long long* worst) {
+  unsigned long long m = 0;
+  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) {
+    unsigned long long h = (unsigned long long)t * 0x9E3779B97F4A7C15ull;
+    h ^= h >> 31;
+    h *= 0xBF58476D1CE4E5B9ull;
+    h ^= h >> 29;
+    const long long e = 1023 - 96 + (long long)(t % 223);
+    const long long sg = (t & 1) ? (1ll << 63) : 0;
+    const double q = __longlong_as_double((long long)(sg | (e << 52) | (long long)(h & 0xFFFFFFFFFFFFFull)));
+    const float2 p = split_pair(q);
+    const double rel = fabs(((double)p.x + (double)p.y) - q) / fabs(q);
+    const unsigned long long b = (unsigned long long)__double_as_longlong(rel);
+    m = b > m ? b : m;
+  }
+  atomicMax(worst, m);
 }
 
 }  // namespace fused
 }  // namespace fmf
+
+// The split pairs of the mixed-precision WENO5 against the doubles they split:
+// largest relative error of hi + lo over n values of 2^-96 .. 2^127 (both signs).
+// Verification support; no counterpart in the reference.
+extern "C" int fmf_check_split_pair(long long n, double* max_rel_err) {
+  if (!max_rel_err || n <= 0) return FMF_ERR_ARG;
+  unsigned long long* d = nullptr;
+  if (cudaMalloc(&d, sizeof(unsigned long long)) != cudaSuccess) return FMF_ERR_NOMEM;
+  cudaMemset(d, 0, sizeof(unsigned long long));
+  fmf::fused::k_check_split<<<152 * 4, 256>>>((long)n, d);
+  fmf::count_launch();
+  unsigned long long h = 0;
+  const cudaError_t e = cudaMemcpy(&h, d, sizeof(h), cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  if (e != cudaSuccess || cudaGetLastError() != cudaSuccess) return FMF_ERR_CUDA;
+  std::memcpy(max_rel_err, &h, sizeof(double));
+  return FMF_OK;
+}

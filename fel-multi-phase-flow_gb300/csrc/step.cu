@@ -5,11 +5,25 @@
 // reference are absent (one rank), and the only host<->device traffic per step is
 // the 8-byte SOR residual read once per outer iteration (the stop test of
 // solu_sor4.f:291-293).
+//
+// Work carried from one step to the next.  After the rotation (:686-697), (uo, vo,
+// wo) of step n+1 is bit for bit (u, v, w) of step n (nothing writes u, v, w after
+// the step reads them), and phi slice 1 of step n+1 is phin slice 1 of step n,
+// untouched since that step's surface tension read it (:695-697 copies it, and
+// :509-516 of the next step writes slice 0 only).  So the advection of (uo, vo, wo)
+// (:533) is the previous step's advection of (u, v, w) (:532), and the surface
+// tension of phi(1) (:547-566) the previous step's of phin(1): the step swaps
+// those buffers instead of recomputing them, and computes one WENO5 level and one
+// CSF force.  The carried terms are valid while the state continues from this
+// context's previous step (`cont`); uploading, the start-up pass, the host-buffer
+// step, new walls or a request for a state pointer clear it (FMF_STEP_CACHE=0 in
+// the environment at creation turns the reuse off).
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
 #include <functional>
 #include <map>
+#include <utility>
 #include <vector>
 
 #include "../../include/fmf_capi.h"
@@ -21,10 +35,10 @@ using namespace fmf;
 
 struct GraphKey {
   int seg;
-  const double* p[14];
+  const double* p[16];
   bool operator<(const GraphKey& o) const {
     if (seg != o.seg) return seg < o.seg;
-    for (int t = 0; t < 14; ++t)
+    for (int t = 0; t < 16; ++t)
       if (p[t] != o.p[t]) return p[t] < o.p[t];
     return false;
   }
@@ -37,6 +51,8 @@ struct GraphEntry {
 struct fmf_ctx {
   bool graphs = true;  // replay captured CUDA graphs (FMF_GRAPHS=0 disables)
   bool warm = false;   // the first step runs eagerly (allocates scratch, twiddle tables)
+  bool reuse = true;   // carry advo and sfst over from the previous step (FMF_STEP_CACHE=0 disables)
+  bool cont = false;   // the state continues from this context's previous step
   void* scr = nullptr; // this context's scratch set
   std::map<GraphKey, GraphEntry> cache;
   fmf_params prm;
@@ -94,6 +110,7 @@ int fmf_ctx_create(const fmf_params* prm, fmf_ctx** out) {
   fmf_ctx* c = new fmf_ctx();
   c->prm = *prm;
   if (const char* e = std::getenv("FMF_GRAPHS")) c->graphs = std::atoi(e) != 0;
+  if (const char* e = std::getenv("FMF_STEP_CACHE")) c->reuse = std::atoi(e) != 0;
   c->scr = scratch_set_create();
   c->g = Grid(prm->ni, prm->nj, prm->nk);
   if (!FMF_CUDA(cudaStreamCreateWithFlags(&c->s, cudaStreamNonBlocking))) {
@@ -217,6 +234,7 @@ int fmf_ctx_set_stream(fmf_ctx* c, void* st) {
 int fmf_ctx_set_walls(fmf_ctx* c, const double* th, const double* ze, const double* l1, const double* l2) {
   if (!c || !th || !ze || !l1 || !l2) return FMF_ERR_ARG;
   const size_t b = sizeof(double) * c->g.n;
+  c->cont = false;
   FMF_CUDA(cudaMemcpyAsync(c->theta0, th, b, cudaMemcpyHostToDevice, c->s));
   FMF_CUDA(cudaMemcpyAsync(c->zeta, ze, b, cudaMemcpyHostToDevice, c->s));
   FMF_CUDA(cudaMemcpyAsync(c->l1, l1, b, cudaMemcpyHostToDevice, c->s));
@@ -252,6 +270,7 @@ static double* field_ptr(fmf_ctx* c, int f) {
 int fmf_ctx_upload(fmf_ctx* c, const double* const* st) {
   if (!c || !st) return FMF_ERR_ARG;
   const size_t b = sizeof(double) * c->g.n;
+  c->cont = false;
   for (int f = 0; f < 12; ++f) FMF_CUDA(cudaMemcpyAsync(field_ptr(c, f), st[f], b, cudaMemcpyHostToDevice, c->s));
   return take_status();
 }
@@ -263,6 +282,7 @@ int fmf_ctx_download(fmf_ctx* c, double* const* st) {
 }
 int fmf_ctx_state_device_ptr(fmf_ctx* c, int f, void** out) {
   if (!c || !out || f < 0 || f > 11) return FMF_ERR_ARG;
+  c->cont = false;  // the caller may write through the pointer before the next step
   *out = field_ptr(c, f);
   return 0;
 }
@@ -282,6 +302,7 @@ int fmf_ctx_sor_iterations(fmf_ctx* c, int* out, int cap) {
 // main.f90:322-366 (start-up boundary pass) on the uploaded state
 int fmf_ctx_init_bc(fmf_ctx* c) {
   if (!c) return FMF_ERR_ARG;
+  c->cont = false;
   ScratchScope scope(c->scr);
   const fmf_params& P = c->prm;
   const Grid& g = c->g;
@@ -313,7 +334,7 @@ int fmf_ctx_init_bc(fmf_ctx* c) {
 // seg_post: main.f90:625-697 (pressure solve, projection, boundary conditions, rotation
 // of phin into phi).  The pointer rotation of u/uo/un, p/po/pn and phi/phin is done
 // on the host between steps.
-static void csf_dropin(fmf_ctx* c, const double* phi1, const double* phin1);
+static void csf_one(fmf_ctx* c, const double* phi, double* const* f);
 
 static void seg_pre(fmf_ctx* c) {
   const fmf_params& P = c->prm;
@@ -360,22 +381,19 @@ static void seg_pre2(fmf_ctx* c) {
   const double dxinv = 1.0 / P.dx, dyinv = 1.0 / P.dy, dzinv = 1.0 / P.dz, dt = P.dt;
   double* phi1 = c->phi + n;
   double* phin1 = c->phin + n;
-  // :532-541
-  fused::weno5_both(s, g, dxinv, dyinv, dzinv, c->u, c->v, c->w, c->uo, c->vo, c->wo, c->adv, c->advo,
-                    P.precision == FMF_MIXED, c->wsplit);
+  // :532-541 (advo carried over from the previous step where the state continues)
+  if (c->cont)
+    fused::weno5_one(s, g, dxinv, dyinv, dzinv, c->u, c->v, c->w, c->adv, c->mixed, c->wsplit);
+  else
+    fused::weno5_both(s, g, dxinv, dyinv, dzinv, c->u, c->v, c->w, c->uo, c->vo, c->wo, c->adv, c->advo, c->mixed,
+                      c->wsplit);
   op::calphat(s, g, c->p, c->po, c->phat);
   op::cal_grad_prs(s, g, dxinv, dyinv, dzinv, c->phat, c->prs[0], c->prs[1], c->prs[2]);
   fused::explicit_viscous(s, g, dxinv, dyinv, dzinv, c->u, c->v, c->w, c->rmu, c->tau, c->vis);
-  // :545-570 surface tension
-  if (fused::csf_supported(g)) {
-    const bool f32 = P.precision == FMF_MIXED;
-    fused::csf_force(s, g, dxinv, dyinv, dzinv, P.rhol, P.rhog, P.sigma, phi1, c->sfst[0], c->sfst[1], c->sfst[2],
-                     f32);
-    fused::csf_force(s, g, dxinv, dyinv, dzinv, P.rhol, P.rhog, P.sigma, phin1, c->sfstn[0], c->sfstn[1],
-                     c->sfstn[2], f32);
-  } else {
-    csf_dropin(c, phi1, phin1);
-  }
+  // :545-570 surface tension (sfst carried over from the previous step's sfstn where
+  // the state continues)
+  if (!c->cont) csf_one(c, phi1, c->sfst);
+  csf_one(c, phin1, c->sfstn);
   // :579-603 (cal_av of rho/rhon at :571-573 feeds nothing downstream)
   const double* advp[3] = {c->adv[0], c->adv[1], c->adv[2]};
   const double* advop[3] = {c->advo[0], c->advo[1], c->advo[2]};
@@ -402,34 +420,28 @@ static void seg_pre2(fmf_ctx* c) {
   op::copy(s, n, c->w, c->wn);
 }
 
-// The surface-tension block as the reference's sequence of subroutines (grids the
-// fused kernel does not tile: ni not a multiple of 32 or nj not a multiple of 8).
-static void csf_dropin(fmf_ctx* c, const double* phi1, const double* phin1) {
+// The surface tension of one field (the force on the u, v, w points): the fused
+// kernel, or the reference's sequence of subroutines on grids it does not tile (ni
+// not a multiple of 32 or nj not a multiple of 8).
+static void csf_one(fmf_ctx* c, const double* phi, double* const* f) {
   const fmf_params& P = c->prm;
   const Grid& g = c->g;
   cudaStream_t s = c->s;
   const long n = g.n;
   const double dxinv = 1.0 / P.dx, dyinv = 1.0 / P.dy, dzinv = 1.0 / P.dz;
-  for (int q = 0; q < 3; ++q) {
-    op::fill(s, n, c->sfst[q], 0.0);
-    op::fill(s, n, c->sfstn[q], 0.0);
+  if (fused::csf_supported(g)) {
+    fused::csf_force(s, g, dxinv, dyinv, dzinv, P.rhol, P.rhog, P.sigma, phi, f[0], f[1], f[2], c->mixed);
+    return;
   }
+  for (int q = 0; q < 3; ++q) op::fill(s, n, f[q], 0.0);
   static const int offs[4][3] = {{1, 1, 1}, {0, 0, 1}, {0, 1, 0}, {1, 0, 0}};
-  fused::vertex_gradient(s, g, dxinv, dyinv, dzinv, phi1, c->phix, c->phiy, c->phiz);
+  fused::vertex_gradient(s, g, dxinv, dyinv, dzinv, phi, c->phix, c->phiy, c->phiz);
   for (int q = 0; q < 4; ++q)
     op::calrn(s, g, dxinv, dyinv, dzinv, offs[q][0], offs[q][1], offs[q][2], c->phix, c->phiy, c->phiz, c->rn[q]);
-  fused::vertex_gradient(s, g, dxinv, dyinv, dzinv, phin1, c->phix, c->phiy, c->phiz);
-  for (int q = 0; q < 4; ++q)
-    op::calrn(s, g, dxinv, dyinv, dzinv, offs[q][0], offs[q][1], offs[q][2], c->phix, c->phiy, c->phiz, c->rnn[q]);
   op::calrkap(s, g, dxinv, dyinv, dzinv, c->rn[0], c->rn[1], c->rn[2], c->rn[3], c->rkap);
-  op::calrkap(s, g, dxinv, dyinv, dzinv, c->rnn[0], c->rnn[1], c->rnn[2], c->rnn[3], c->rkapn);
-  op::cal_grad_prs(s, g, dxinv, dyinv, dzinv, phi1, c->phix, c->phiy, c->phiz);
+  op::cal_grad_prs(s, g, dxinv, dyinv, dzinv, phi, c->phix, c->phiy, c->phiz);
   op::calfst(s, g, P.rhol, P.rhog, P.sigma, c->phix, c->phiy, c->phiz, c->rkap, c->fst[0], c->fst[1], c->fst[2]);
-  op::cal_grad_prs(s, g, dxinv, dyinv, dzinv, phin1, c->phix, c->phiy, c->phiz);
-  op::calfst(s, g, P.rhol, P.rhog, P.sigma, c->phix, c->phiy, c->phiz, c->rkapn, c->fstn[0], c->fstn[1],
-             c->fstn[2]);
-  op::sum_fst(s, g, c->fst[0], c->fst[1], c->fst[2], c->sfst[0], c->sfst[1], c->sfst[2]);
-  op::sum_fst(s, g, c->fstn[0], c->fstn[1], c->fstn[2], c->sfstn[0], c->sfstn[1], c->sfstn[2]);
+  op::sum_fst(s, g, c->fst[0], c->fst[1], c->fst[2], f[0], f[1], f[2]);
 }
 
 static void seg_iter(fmf_ctx* c) {
@@ -476,7 +488,9 @@ static void run_segment(fmf_ctx* c, int id, void (*fn)(fmf_ctx*)) {
     fn(c);
     return;
   }
-  GraphKey key{id, {c->u, c->v, c->w, c->uo, c->vo, c->wo, c->un, c->vn, c->wn, c->p, c->po, c->pn, c->phi, c->phin}};
+  GraphKey key{id + (c->cont ? 100 : 0),
+               {c->u, c->v, c->w, c->uo, c->vo, c->wo, c->un, c->vn, c->wn, c->p, c->po, c->pn, c->phi, c->phin,
+                c->adv[0], c->sfst[0]}};
   auto it = c->cache.find(key);
   if (it == c->cache.end()) {
     const long long l0 = launches();
@@ -530,18 +544,25 @@ static int step_once(fmf_ctx* c, const std::function<void()>& after_pre = {},
   t = c->wo; c->wo = c->w; c->w = c->wn; c->wn = t;
   t = c->po; c->po = c->p; c->p = c->pn; c->pn = t;
   t = c->phi; c->phi = c->phin; c->phin = t;
+  // the next step's advo and sfst: this step's adv and sfstn
+  for (int q = 0; q < 3; ++q) {
+    std::swap(c->adv[q], c->advo[q]);
+    std::swap(c->sfst[q], c->sfstn[q]);
+  }
   FMF_CUDA(cudaGetLastError());
+  c->cont = c->reuse && get_status() == 0;
   return get_status();
 }
 
 // Times one stage of the step on the context's stream with CUDA events, reps
 // launches after one warm-up launch, on the current state (the state is not
-// advanced: stages write only work arrays).  Stage 0: WENO5 advection of (u,v,w);
-// 1: one outer SOR iteration on copies of the velocity; 2: pressure FFT+TDMA+inverse;
-// 3: MTHINC fluxes.  *ms = mean milliseconds per launch of the stage (stage 0 covers
-// both advection levels, u and uo).
+// advanced: stages write only work arrays).  Stage 0: WENO5 advection of both
+// levels, (u,v,w) and (uo,vo,wo); 1: one outer SOR iteration on copies of the
+// velocity; 2: pressure FFT+TDMA+inverse; 3: MTHINC fluxes; 4: WENO5 advection of
+// (u,v,w) alone (what a step that continues from the previous one runs).  *ms =
+// mean milliseconds per launch of the stage.
 int fmf_ctx_time_stage(fmf_ctx* c, int stage, int reps, float* ms) {
-  if (!c || !ms || reps <= 0 || stage < 0 || stage > 3) return FMF_ERR_ARG;
+  if (!c || !ms || reps <= 0 || stage < 0 || stage > 4) return FMF_ERR_ARG;
   ScratchScope scope(c->scr);
   const fmf_params& P = c->prm;
   const Grid& g = c->g;
@@ -569,6 +590,9 @@ int fmf_ctx_time_stage(fmf_ctx* c, int stage, int reps, float* ms) {
         fused::mthinc_fluxes(s, g, dxinv, dyinv, dzinv, P.dt, P.bet_mthinc, c->phi + n, c->phix, c->phiy,
                              c->phiz, c->u, c->v, c->w, c->flx, c->fly, c->flz, c->band,
                              c->band + (long)(g.ni + 2) * (g.nj + 2) * (g.nk + 2), mixed);
+        break;
+      case 4:  // writes adv only: the carried advo stays valid
+        fused::weno5_one(s, g, dxinv, dyinv, dzinv, c->u, c->v, c->w, c->adv, mixed, c->wsplit);
         break;
     }
   };
@@ -619,6 +643,7 @@ int fmf_ctx_step_host(fmf_ctx* c, const double* const* in, double* const* out) {
   auto d2h = [&](int f, const double* src, cudaStream_t st) {
     FMF_CUDA(cudaMemcpyAsync(out[f], src, b, cudaMemcpyDeviceToHost, st));
   };
+  c->cont = false;  // the inputs are the caller's, not this context's last step
   for (int f : {0, 1, 2, 8, 9}) h2d(f, c->s);  // u, v, w, phi
   FMF_CUDA(cudaEventRecord(c->ev_in, c->s));
   FMF_CUDA(cudaStreamWaitEvent(c->cs, c->ev_in, 0));

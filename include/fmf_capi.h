@@ -387,13 +387,21 @@ int fmf_ctx_synchronize(fmf_ctx* ctx);
 int fmf_ctx_set_stream(fmf_ctx* ctx, void* cuda_stream);
 /* per-step SOR iteration counts of the last fmf_ctx_step call (up to cap entries) */
 int fmf_ctx_sor_iterations(fmf_ctx* ctx, int* out, int cap);
-/* device pointers of the state fields (for zero-copy consumers) */
+/* device pointers of the state fields (for zero-copy consumers).  A step that
+ * continues from the context's previous step reuses that step's advection of
+ * (u, v, w) as its advection of (uo, vo, wo) and its surface tension of phin(1) as
+ * that of phi(1); this call, fmf_ctx_upload, fmf_ctx_init_bc, fmf_ctx_set_walls
+ * and fmf_ctx_step_host end that.  A caller that writes a state field through the
+ * pointer must do so before its next fmf_ctx_step, or call this function again
+ * after writing. */
 int fmf_ctx_state_device_ptr(fmf_ctx* ctx, int field, void** out);
 /* bytes of device memory held by the context */
 long long fmf_ctx_device_bytes(fmf_ctx* ctx);
 /* CUDA-event time of one stage of the step on the context stream (mean ms per
- * launch over reps): 0 WENO5 advection, 1 one outer SOR iteration, 2 pressure
- * FFT+TDMA, 3 MTHINC fluxes.  Measurement support; no counterpart in the reference. */
+ * launch over reps): 0 WENO5 advection of both velocity levels, 1 one outer SOR
+ * iteration, 2 pressure FFT+TDMA, 3 MTHINC fluxes, 4 WENO5 advection of (u, v, w)
+ * alone (the level a continuing step computes).  Measurement support; no
+ * counterpart in the reference. */
 int fmf_ctx_time_stage(fmf_ctx* ctx, int stage, int reps, float* ms);
 /* FMA throughput of this GPU in TFLOP/s (fp64=1: double, 0: float), from a
  * register-only kernel timed with CUDA events; the FP64 roofline denominator.
@@ -408,6 +416,11 @@ int fmf_check_reciprocal(long long n, double* max_rel_err);
  * (Newton-Raphson from an approximate reciprocal square root) against
  * 1.0 / sqrt(x). */
 int fmf_check_rsqrt(long long n, double* max_rel_err);
+/* Largest relative error of the (hi, lo) float pairs the mixed-precision WENO5
+ * splits each double into (hi + lo against the double), over n values of both
+ * signs spread over 2^-96 .. 2^127.  Verification support; no counterpart in the
+ * reference. */
+int fmf_check_split_pair(long long n, double* max_rel_err);
 
 /* ---- restart files (host code; no GPU needed) ---------------------------
  * One Fortran unformatted sequential record, as the reference writes it: u v w p

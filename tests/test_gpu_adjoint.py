@@ -165,3 +165,26 @@ def test_torch_autograd_function(setup):
     assert abs(out.item() - J) <= 1e-15 * max(abs(J), 1e-300)
     for t, g in zip(ts + [phi], grads):
         assert np.abs(t.grad.numpy() - g).max() <= 1e-10 * max(np.abs(g).max(), 1e-300)
+
+
+def test_carried_terms_in_forward_and_reverse(setup, monkeypatch):
+    """The adjoint's forward steps take the previous step's advection of (u, v, w)
+    and surface tension of phin(1) for (uo, vo, wo) and phi(1), as the product step
+    does.  A handle that recomputes both every step (FMF_STEP_CACHE=0) gives the
+    same J bit for bit and the same gradients up to the order of the reverse's
+    atomic additions."""
+    from fmf.adjoint import Adjoint
+
+    cfg, adj, st0, walls, J, grads = setup
+    monkeypatch.setenv("FMF_STEP_CACHE", "0")
+    b = Adjoint(cfg, sor_tol=SOR_TOL, sor_max=300, adj_tol=1e-13, adj_max=400)
+    monkeypatch.delenv("FMF_STEP_CACHE")
+    try:
+        assert b.forward(K, st0, walls) == adj.forward(K, st0, walls)
+        Jb, gb = b.rollout(K, st0, walls, every=3)
+    finally:
+        b.close()
+    assert Jb == J
+    for a_, b_ in zip(grads, gb):
+        scale = max(np.abs(a_).max(), 1e-300)
+        assert np.abs(a_ - b_).max() <= 1e-10 * scale

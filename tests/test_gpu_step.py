@@ -143,3 +143,53 @@ def test_step_host_matches_upload_step_download(fmf_lib, prec):
         assert np.array_equal(pin, ref)
     a.close()
     b.close()
+
+
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+@pytest.mark.parametrize("grid", ["fused_csf", "dropin_csf"])
+def test_carried_terms_bitwise(fmf_lib, monkeypatch, prec, grid):
+    """A step that continues from the previous one takes that step's advection of
+    (u, v, w) as its advection of (uo, vo, wo) and its surface tension of phin(1)
+    as that of phi(1) (main.f90:686-697 makes them the same fields).  Ten steps
+    that way give bit for bit the state of ten steps that recompute both terms
+    (FMF_STEP_CACHE=0), including across an upload that restarts the carry.  Two
+    grids: one the fused CSF kernel tiles (64x32x32, density and viscosity ratio
+    10) and one it does not (16x16x16: the drop-in CSF chain)."""
+    if grid == "fused_csf":
+        cfg = C.get("couette256", ni=64, nj=32, nk=32)
+    else:
+        cfg = C.get("couette32", ni=16, nj=16, nk=16, rhol=4.0, rmul=0.2)
+    p = capi.FMF_FP64 if prec == "fp64" else capi.FMF_MIXED
+    a = capi.Stepper(cfg, precision=p)
+    st0 = a.initial_state()
+    monkeypatch.setenv("FMF_STEP_CACHE", "0")
+    b = capi.Stepper(cfg, precision=p)
+    monkeypatch.delenv("FMF_STEP_CACHE")
+    b.upload(st0)
+    a.step(6)
+    b.step(6)
+    sa, sb = a.get_state(), b.get_state()
+    assert np.array_equal(sa, sb)
+    assert a.sor_iterations() == b.sor_iterations()
+    # an upload of the same state ends the carry; the next step recomputes both
+    a.upload(sa)
+    a.step(4)
+    b.step(4)
+    sa, sb = a.get_state(), b.get_state()
+    for f in range(12):
+        assert np.array_equal(sa[f], sb[f]), C.STATE_FIELDS[f]
+    a.close()
+    b.close()
+
+
+def test_split_pair_precision(fmf_lib):
+    """The (hi, lo) float pairs of the mixed WENO5 hold each double to about 2^-48
+    of itself over 2^-96 .. 2^127, small magnitudes included (where the low part
+    needs a two-factor scale to stay a normal float)."""
+    import ctypes
+
+    L = fmf_lib
+    L.fmf_check_split_pair.argtypes = [ctypes.c_longlong, ctypes.POINTER(ctypes.c_double)]
+    err = ctypes.c_double(-1.0)
+    assert L.fmf_check_split_pair(1 << 22, ctypes.byref(err)) == 0
+    assert 0.0 <= err.value <= 2.0 ** -47, err.value
