@@ -712,6 +712,8 @@ void reverse_step(fmf_adj* a, const double* st, bool defer) {
   {
     // the curvatures recorded by the fused forward kernel where the grid tiles
     const bool rec = fused::csf_supported(g);
+    // the next step's carried adjoint is consumed before this step's replaces it
+    if (a->carry_in) add3(s, n, cfst, a->lsfstn);
     if (defer) {
       for (int q = 0; q < 3; ++q) dcopy(a, a->lsfst[q], cfst[q], n);
     } else {
@@ -719,7 +721,6 @@ void reverse_step(fmf_adj* a, const double* st, bool defer) {
       adj::csf_T(s, g, dxi, dyi, dzi, P.rhol, P.rhog, P.sigma, ST(SPHI1), lf, lS[SPHI1], a->work + 3 * n + 1024,
                  rec ? a->kap : nullptr);
     }
-    if (a->carry_in) add3(s, n, cfst, a->lsfstn);
     const double* lfn[3] = {a->lsfstn[0], a->lsfstn[1], a->lsfstn[2]};
     adj::csf_T(s, g, dxi, dyi, dzi, P.rhol, P.rhog, P.sigma, a->phn1f, lfn, a->lphn1, a->work + 3 * n + 1024,
                rec ? a->kapn : nullptr);

@@ -1145,7 +1145,7 @@ void orc_cal_coef_solp_fft(const int* nj, const double* as_p, const double* an_p
 // The oracle's own FFT (the reference calls the vendored Numerical Recipes fourn.f,
 // whose arithmetic is the DFT X_m = sum_n x_n exp(sign*2*pi*i*m*n/N); this is an
 // independent radix-2 decimation-in-time restatement of that DFT, pinned against
-// numpy.fft in tests/test_oracle_fft.py).
+// numpy.fft in tests/test_oracle_pins.py).
 namespace {
 void fft1d(double* re, double* im, int n, int sign) {
   for (int i = 1, j = 0; i < n; ++i) {

@@ -31,7 +31,7 @@ def build(force: bool = False) -> str:
     os.makedirs(BUILD, exist_ok=True)
     if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < max(
             os.path.getmtime(SRC), os.path.getmtime(os.path.join(HERE, "fmf_oracle.h"))):
-        cmd = ["g++", "-O2", "-fopenmp", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared",
+        cmd = ["g++", "-O3", "-fopenmp", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared",
                "-std=c++17", "-o", LIB + ".tmp", SRC]
         subprocess.run(cmd, check=True)
         os.replace(LIB + ".tmp", LIB)
