@@ -1,23 +1,30 @@
 """Benchmark: cell-updates/s of the full FP64 time step on one GB300.
 
-Workload (the 256x128x128 case the metric is quoted on): two-phase Couette flow
-with contact lines, density and viscosity ratio 10, perturbed x-stripe
-interface, 60 deg walls, dt=2e-5 -- in reference axis order (ni, nj_wall, nk) =
-(256, 128, 128).  One "step" is one full time step (main.f90:473-697).
-value = interior cells x timed steps / device time (CUDA events on the
-library's stream, device-resident state).  e2e = the same through the C-ABI with
-host buffers (fmf_ctx_step_host): every step uploads the state's 10 input fields
-from pinned host memory, steps, and returns the 12 result fields to host memory.
+Workload: the 512x256x256 sessile drop (density ratio 1000, viscosity ratio 100,
+60/120 deg checkerboard lower wall, dt = 1e-5) in reference axis order (ni,
+nj_wall, nk) = (512, 256, 256), the largest single-GPU configuration the metric is
+quoted on.  One "step" is one full time step (main.f90:473-697).  value = interior
+cells x timed steps / device time (CUDA events on the library's stream,
+device-resident state, inputs larger than L2).  e2e = the same through the C-ABI
+with host buffers (fmf_ctx_step_host every step: the state's 10 input fields up
+from pinned host memory, the 12 result fields back), over the same steps.
+
+Beside the headline: the mixed-precision step on the same workload (value,
+speed-up, per-field error against the FP64 step after the timed steps and over the
+workload's 500 steps), the 256x128x128 Couette case in both precisions, the
+adjoint/forward cost of the 128x64x64 rollout (K = 200, checkpoints every 16), and
+the CPU baseline.
 
 `--impl reference` times the CPU restatement of the reference's algorithm
 (oracle/, the reference Fortran cannot be built here: no Fortran compiler) on
-the host cores, same workload and metric.
+the host cores, same workload, metric and config.
 """
 from __future__ import annotations
 
 import argparse
 import ctypes
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -28,17 +35,32 @@ REPO = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.join(REPO, "fel-multi-phase-flow_gb300"))
 sys.path.insert(0, os.path.join(REPO, "oracle"))
 
-WORKLOAD = "couette256"
-# Per interior cell of one k_weno2 launch, from the ncu capture summarised in
-# profiles/k_weno2_couette256.md (4,194,304 cells): DRAM bytes read + written
-# (228.2 MB + 173.3 MB), and the executed FP64 instructions (DADD 955.7 M, DMUL
-# 1219.5 M, DFMA 1885.8 M thread instructions); scaled to the workload by its cell
-# count
-WENO_TRAFFIC_PER_CELL = (228.228864e6 + 173.254144e6) / 4194304
-WENO_FP64_INST_PER_CELL = (955711488 + 1219493888 + 1885798400) / 4194304
-WENO_FP64_FLOPS_PER_CELL = (955711488 + 1219493888 + 2 * 1885798400) / 4194304
+WORKLOAD = "droplet512"
 METRIC = "cell-updates/s/step plain FP64 vs mixed at stated error; adjoint/forward cost"
 UNIT = "cell-updates/s"
+
+# The dominant kernel's counters per interior cell of one launch (k_weno2, one
+# velocity level: the advection of (u, v, w); the (uo, vo, wo) level is carried
+# over from the previous step).  DRAM bytes read + written from the ncu capture of
+# one one-level launch at 256x128x128 (113.5 MB + 68.7 MB over 4,194,304 cells;
+# python bench.py --profile --workload couette256 --warmup 2 --steps 1 under
+# ncu --set full -k regex:k_weno2 -s 1 -c 1 --clock-control none).  FP64
+# instructions (DADD + DMUL + DFMA thread instructions; flops count an FMA twice):
+# half of a two-level launch's (955.7 M + 1219.5 M + 1885.8 M at 256x128x128),
+# both levels running the same loop body.
+WENO_CAPTURE = ("ncu --set full of one one-level k_weno2 launch, couette256 256x128x128 (DRAM bytes); "
+                "FP64 instruction counts: half of a two-level launch's at the same size")
+WENO_TRAFFIC_PER_CELL = (113.540352e6 + 68.679168e6) / 4194304
+WENO_FP64_INST_PER_CELL = (955711488 + 1219493888 + 1885798400) / 2 / 4194304
+WENO_FP64_FLOPS_PER_CELL = (955711488 + 1219493888 + 2 * 1885798400) / 2 / 4194304
+# weno5.h's own formula (both one-sided reconstructions) per cell and level
+WENO_REFERENCE_FLOPS_PER_CELL = 1383.0
+
+# Algorithmic bytes of one cell-update: 83 words outside the viscous solve and 21
+# words per outer iteration of it (each stage's external arrays read once and
+# written once, FP64)
+B_CELL_FIXED = 664
+B_CELL_PER_SOR = 168
 
 
 def _peaks():
@@ -47,6 +69,13 @@ def _peaks():
             return json.load(f), "measured"
     except Exception:
         return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+def config_dict(cfg, world: int) -> dict:
+    """The workload description both arms print (identical keys and values)."""
+    return {"workload": f"{cfg.name} {cfg.ni}x{cfg.nj}x{cfg.nk} (ni,nj_wall,nk)", "precision": "fp64",
+            "l2": "inputs larger than L2 (each field of the state is " f"{8 * math.prod(cfg.shape) / 1e6:.0f} MB)",
+            "parallelism": "replicas" if world > 1 else "single"}
 
 
 class Clocks:
@@ -99,17 +128,27 @@ class Clocks:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def cpu_baseline_sample(cfg, steps=1):
-    """The oracle (C++/OpenMP restatement, all host threads) on a bounded sample."""
+def _oracle_env():
+    """All host threads, bound close, for the oracle's OpenMP loops (read when its
+    library loads)."""
+    os.environ.setdefault("OMP_NUM_THREADS", str(os.cpu_count() or 1))
+    os.environ.setdefault("OMP_PROC_BIND", "close")
+    return int(os.environ["OMP_NUM_THREADS"])
+
+
+def cpu_baseline_sample(cfg, warmup=1, steps=2):
+    """The oracle (C++/OpenMP restatement, all host threads) on a bounded sample:
+    `steps` full steps after `warmup`, from the workload's initial state."""
+    cores = _oracle_env()
     import oracle
-    from fmf import config as C
     s = oracle.Solver(cfg)
     st = s.initial_state()
-    s.step(st, 1)  # warm
+    s.step(st, warmup)
     t0 = time.perf_counter()
     s.step(st, steps)
     dt = time.perf_counter() - t0
-    return cfg.cells * steps / dt, dt
+    s.close()
+    return cfg.cells * steps / dt, dt, cores
 
 
 def run_reference(args):
@@ -117,7 +156,8 @@ def run_reference(args):
     if rank != 0:
         return
     from fmf import config as C
-    cfg = C.get(WORKLOAD)
+    cfg = C.get(args.workload)
+    cores = _oracle_env()
     import oracle
     s = oracle.Solver(cfg)
     st = s.initial_state()
@@ -125,42 +165,45 @@ def run_reference(args):
     t0 = time.perf_counter()
     s.step(st, args.steps)
     dt = time.perf_counter() - t0
+    s.close()
     v = cfg.cells * args.steps / dt
-    cores = os.cpu_count()
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic",
-            "config": {"workload": f"{WORKLOAD} 256x128x128 (ni,nj_wall,nk)", "precision": "fp64"},
+            "data": "synthetic", "config": config_dict(cfg, args.gpus),
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
-                             "sample": f"{args.steps} full steps of {WORKLOAD} after {args.warmup} warm-up "
-                                       "steps; the reference Fortran cannot be built here (no Fortran "
-                                       "compiler), so its C++/OpenMP restatement oracle/fmf_oracle.cpp runs"},
+                             "sample": f"{args.steps} full steps of {cfg.name} after {args.warmup} warm-up "
+                                       "steps, OMP_PROC_BIND=close; the reference Fortran cannot be built here (no "
+                                       "Fortran compiler), so its C++/OpenMP restatement oracle/fmf_oracle.cpp "
+                                       "(g++ -O3 -fopenmp -ffp-contract=off) runs"},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
 
-def mixed_case(name, steps, warmup, stream):
-    """FP64 and mixed-precision steps on one workload: CUDA-event time per step of
-    each (inputs resident, steps after `warmup`), and the per-field error of the mixed
-    state against the FP64 state after the same warmup + steps from the same initial
-    state."""
+def _rel(a, b, cfg):
+    from fmf import config as C
+    x, y = C.interior(a), C.interior(b)
     import numpy as np
+    return float(np.abs(x - y).max() / max(np.abs(y).max(), 1e-300))
+
+
+FIELDS = {"phi": 9, "u": 0, "v": 1, "w": 2, "p": 6}
+
+
+def mixed_case(cfg, st0, steps, warmup, stream, fp64_ms=None):
+    """The mixed-precision step against the FP64 step on one workload: CUDA-event
+    time per step of each (state resident, `steps` after `warmup`), and the
+    per-field error of the mixed state against the FP64 state after warmup + steps
+    from the same initial state."""
     import torch
 
     from fmf import capi
-    from fmf import config as C
 
-    cfg = C.get(name)
-    out = {"workload": f"{name} {cfg.ni}x{cfg.nj}x{cfg.nk}", "steps": steps, "warmup": warmup}
+    out = {"workload": f"{cfg.name} {cfg.ni}x{cfg.nj}x{cfg.nk}", "steps": steps, "warmup": warmup}
     states = {}
-    st = None
     for prec, key in ((capi.FMF_FP64, "fp64"), (capi.FMF_MIXED, "mixed")):
         g = capi.Stepper(cfg, precision=prec, stream=stream.cuda_stream)
-        if st is None:
-            st = g.initial_state()  # after the start-up boundary pass; the mixed run starts from it too
-        else:
-            g.upload(st)
+        g.upload(st0)
         g.step(warmup)
         g.sync()
         e0 = torch.cuda.Event(enable_timing=True)
@@ -172,19 +215,49 @@ def mixed_case(name, steps, warmup, stream):
         out[key + "_ms_per_step"] = e0.elapsed_time(e1) / steps
         states[key] = g.get_state()
         g.close()
+    if fp64_ms is not None:
+        out["fp64_ms_per_step"] = fp64_ms
     ref, mix = states["fp64"], states["mixed"]
-
-    def rel(f):
-        a, b = C.interior(mix[f]), C.interior(ref[f])
-        return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))
-
     out["value_fp64"] = cfg.cells / (out["fp64_ms_per_step"] * 1e-3)
     out["value_mixed"] = cfg.cells / (out["mixed_ms_per_step"] * 1e-3)
     out["unit"] = UNIT
     out["speedup_vs_fp64"] = out["fp64_ms_per_step"] / out["mixed_ms_per_step"]
     out["steps_compared"] = warmup + steps
-    out["max_rel_err_vs_fp64"] = {"phi": rel(9), "u": rel(0), "v": rel(1), "w": rel(2), "p": rel(6)}
+    out["max_rel_err_vs_fp64"] = {k: _rel(mix[f], ref[f], cfg) for k, f in FIELDS.items()}
     return out
+
+
+def mixed_horizon(cfg, st0, steps, every, stream):
+    """FP64 and mixed steps side by side from the same initial state over `steps`
+    steps: the largest relative error of each field (interior, against the FP64
+    field's largest magnitude) at every `every`-th step."""
+    import numpy as np
+
+    from fmf import capi
+
+    ref = capi.Stepper(cfg, stream=stream.cuda_stream)
+    ref.upload(st0)
+    mix = capi.Stepper(cfg, precision=capi.FMF_MIXED, stream=stream.cuda_stream)
+    mix.upload(st0)
+    worst = {k: 0.0 for k in FIELDS}
+    table = []
+    done = 0
+    t0 = time.perf_counter()
+    while done < steps:
+        n = min(every, steps - done)
+        ref.step(n)
+        mix.step(n)
+        done += n
+        a, b = mix.get_state(), ref.get_state()
+        finite = bool(np.isfinite(a).all() and np.isfinite(b).all())
+        errs = {k: _rel(a[f], b[f], cfg) for k, f in FIELDS.items()}
+        for k in FIELDS:
+            worst[k] = max(worst[k], errs[k])
+        table.append({"step": done, "finite": finite, **{k: errs[k] for k in FIELDS}})
+    ref.close()
+    mix.close()
+    return {"workload": f"{cfg.name} {cfg.ni}x{cfg.nj}x{cfg.nk}", "steps_compared": steps, "every": every,
+            "max_rel_err_vs_fp64": worst, "per_check": table, "seconds": time.perf_counter() - t0}
 
 
 def adjoint_cost(K, stream, every, workload="couette128"):
@@ -195,8 +268,6 @@ def adjoint_cost(K, stream, every, workload="couette128"):
     fmf_adj_rollout (J and all gradients) against fmf_adj_forward (J) with the same
     solver settings (viscous solve to the reference's 1e-3, transposed solve to
     1e-6), and against the graph-replayed production step (fmf_ctx_step)."""
-    import math
-
     from fmf import capi
     from fmf import config as C
     from fmf.adjoint import Adjoint
@@ -241,6 +312,36 @@ def adjoint_cost(K, stream, every, workload="couette128"):
             "tolerances": {"sor": 1e-3, "adjoint": 1e-6}}
 
 
+def profile(args):
+    """No timing: start-up pass, --warmup steps, then --steps steps (for ncu)."""
+    from fmf import build as fbuild
+    from fmf import capi
+    from fmf import config as C
+    fbuild.build()
+    if args.precision == "adjoint":
+        # --steps K of the adjoint rollout on the workload (for ncu launch lists)
+        from fmf.adjoint import Adjoint
+        cfg = C.get(args.workload)
+        A = Adjoint(cfg, sor_tol=1e-3, sor_max=21, adj_tol=1e-6, adj_max=200)
+        st0 = C.raw_state(cfg)
+        walls = C.wall_arrays(cfg)
+        A.rollout(max(1, args.warmup), st0, walls)
+        J, _ = A.rollout(args.steps, st0, walls)
+        print(json.dumps({"profile": args.workload, "adjoint_steps": args.steps, "J": J,
+                          "iterations": A.iterations()}))
+        A.close()
+        return
+    prec = capi.FMF_MIXED if args.precision == "mixed" else capi.FMF_FP64
+    g = capi.Stepper(C.get(args.workload), precision=prec)
+    g.initial_state()
+    g.step(args.warmup)
+    g.sync()
+    g.step(args.steps)
+    g.sync()
+    print(json.dumps({"profile": args.workload, "sor_iterations": g.sor_iterations()}))
+    g.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -249,15 +350,16 @@ def main():
     ap.add_argument("--impl", default="fmf", choices=["fmf", "reference"])
     ap.add_argument("--workload", default=WORKLOAD)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--mixed-horizon", type=int, default=500,
+                    help="steps of the side-by-side FP64/mixed error check on the workload (0: skip)")
+    ap.add_argument("--second-workload", default="couette256",
+                    help="FP64 and mixed step times on a second workload ('' to skip)")
     ap.add_argument("--adjoint-steps", type=int, default=200,
                     help="K of the adjoint-cost measurement (0: skip)")
-    ap.add_argument("--mixed-workload", default="droplet512",
-                    help="second FP64-vs-mixed measurement (the sessile-drop workload; '' to skip)")
     ap.add_argument("--adjoint-every", type=int, default=16,
                     help="checkpoint interval of the adjoint rollout (0: ceil(sqrt(K)))")
     ap.add_argument("--adjoint-workload", default="couette128",
-                    help="workload of the adjoint-cost measurement (droplet256 with --adjoint-steps 500 "
-                         "--adjoint-every 0: the 256x128x128 sessile drop, K = 500, ceil(sqrt(K)) = 23)")
+                    help="workload of the adjoint-cost measurement")
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed", "adjoint"], help="--profile only")
     ap.add_argument("--profile", action="store_true",
                     help="no timing: start-up pass, --warmup steps, then --steps steps (for ncu launch lists)")
@@ -266,32 +368,7 @@ def main():
         run_reference(args)
         return
     if args.profile:
-        from fmf import build as fbuild
-        from fmf import capi
-        from fmf import config as C
-        fbuild.build()
-        if args.precision == "adjoint":
-            # --steps K of the adjoint rollout on the workload (for ncu launch lists)
-            from fmf.adjoint import Adjoint
-            cfg = C.get(args.workload)
-            A = Adjoint(cfg, sor_tol=1e-3, sor_max=21, adj_tol=1e-6, adj_max=200)
-            st0 = C.raw_state(cfg)
-            walls = C.wall_arrays(cfg)
-            A.rollout(max(1, args.warmup), st0, walls)
-            J, _ = A.rollout(args.steps, st0, walls)
-            print(json.dumps({"profile": args.workload, "adjoint_steps": args.steps, "J": J,
-                              "iterations": A.iterations()}))
-            A.close()
-            return
-        prec = capi.FMF_MIXED if args.precision == "mixed" else capi.FMF_FP64
-        g = capi.Stepper(C.get(args.workload), precision=prec)
-        g.initial_state()
-        g.step(args.warmup)
-        g.sync()
-        g.step(args.steps)
-        g.sync()
-        print(json.dumps({"profile": args.workload, "sor_iterations": g.sor_iterations()}))
-        g.close()
+        profile(args)
         return
 
     import numpy as np
@@ -300,7 +377,6 @@ def main():
     from fmf import build as fbuild
     from fmf import capi
     from fmf import config as C
-
     from fmf import replicas
 
     rank, world = replicas.world()
@@ -322,6 +398,7 @@ def main():
         torch.cuda.synchronize()
         replicas.barrier()
 
+    # ---- headline: FP64 steps, state resident -------------------------------
     clocks = Clocks()
     barrier()
     clocks.start()
@@ -339,36 +416,40 @@ def main():
     iters = g.sor_iterations()
     ms = replicas.max_over_ranks(ms)
     value = replicas.throughput(cfg.cells, args.steps, ms * 1e-3)
+    n_sor = float(np.mean(iters)) if iters else 0.0
 
-    # e2e: host buffers through the C-ABI, every step uploads the 10 input fields of
-    # the state from pinned host memory (phin is written by the step before it is
-    # read) and returns the 12 result fields to it (fmf_ctx_step_host: part of the
-    # upload and the result fields that are final early overlap the step)
+    # ---- e2e: host buffers through the C-ABI, the same number of steps -------
+    # every step uploads the 10 input fields of the state from pinned host memory
+    # (phin is written by the step before it is read) and returns the 12 result
+    # fields to it (fmf_ctx_step_host: part of the upload and the result fields that
+    # are final early overlap the step); the host buffer carries the state from step
+    # to step, as a caller's time loop does
     pinned = torch.empty((12,) + cfg.shape, dtype=torch.float64, pin_memory=True)
     host = pinned.numpy()
     host[:] = g.get_state()
-    bytes_field = cfg.shape[0] * cfg.shape[1] * cfg.shape[2] * 8
-    e2e_steps = max(1, min(args.steps, 5))
+    bytes_field = math.prod(cfg.shape) * 8
     g.step_host(host, host)  # the host-buffer path's own first call (copy stream, events)
     barrier()
     t0 = time.perf_counter()
-    for _ in range(e2e_steps):
+    for _ in range(args.steps):
         g.step_host(host, host)
     e2e_dt = replicas.max_over_ranks(time.perf_counter() - t0)
-    e2e_value = replicas.throughput(cfg.cells, e2e_steps, e2e_dt)
+    e2e_value = replicas.throughput(cfg.cells, args.steps, e2e_dt)
+    del pinned, host
 
-    # Dominant kernel: WENO5 advection of both velocity levels (k_weno2, stage 0),
-    # FP64-pipe bound.  The FP64 roofline counts executed FP64 instructions (ncu
-    # DADD + DMUL + DFMA per cell, WENO_FP64_INST_PER_CELL) against the FP64 pipe's
+    # ---- rooflines ------------------------------------------------------------
+    # Dominant kernel: WENO5 advection of (u, v, w) (k_weno2, one level: stage 4),
+    # FP64-pipe bound.  Executed FP64 instructions per second (ncu DADD + DMUL +
+    # DFMA per cell of one launch, WENO_FP64_INST_PER_CELL) against the FP64 pipe's
     # instruction rate, half the FMA-chain flop rate fmf_measure_fma_rate measures
-    # live (an FMA is one instruction and two flops).  Also reported: the executed
-    # flops (FMA = 2) and the rate of the reference formula's flops (weno5.h, both
-    # one-sided reconstructions: 2766 per cell for the two calls), which exceeds
-    # the peak because the kernel evaluates the upwind side only, in fewer
-    # operations.  Algorithmic bytes 12 words per cell (6 fields in, 6 out); HBM
-    # peak from MEASURED_PEAKS.json.
+    # live (an FMA is one instruction and two flops).  Also reported: executed flops
+    # and the rate of weno5.h's own formula (both one-sided reconstructions), which
+    # exceeds the FMA peak because the kernel evaluates the upwind side only, in
+    # fewer operations; and the kernel against HBM (6 words per cell algorithmic).
     ms_stage = ctypes.c_float()
-    capi.check(L.fmf_ctx_time_stage(g.h, 0, 5, ctypes.byref(ms_stage)), "time_stage")
+    capi.check(L.fmf_ctx_time_stage(g.h, 4, 5, ctypes.byref(ms_stage)), "time_stage")
+    ms_stage2 = ctypes.c_float()
+    capi.check(L.fmf_ctx_time_stage(g.h, 0, 3, ctypes.byref(ms_stage2)), "time_stage")
     peaks, peak_kind = _peaks()
     fp64 = ctypes.c_double()
     L.fmf_measure_fma_rate.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_double)]
@@ -376,82 +457,69 @@ def main():
     t_weno = ms_stage.value * 1e-3
     inst_rate = WENO_FP64_INST_PER_CELL * cfg.cells / t_weno / 1e12
     inst_peak = fp64.value / 2.0
-    gbs = 12 * 8 * cfg.cells / t_weno / 1e9
+    gbs = 6 * 8 * cfg.cells / t_weno / 1e9
     roofline = {"bound": "fp64", "achieved": inst_rate, "peak": inst_peak, "unit": "T FP64 instructions/s",
                 "frac": inst_rate / inst_peak,
                 "traffic": WENO_TRAFFIC_PER_CELL * cfg.cells,
-                "kernel": "k_weno2 (both cal_advu_weno5 calls of the step)", "kernel_ms": ms_stage.value,
+                "kernel": "k_weno2, one level (the step's cal_advu_weno5 of u, v, w)", "kernel_ms": ms_stage.value,
+                "kernel_ms_both_levels": ms_stage2.value,
                 "fp64_inst_per_cell": WENO_FP64_INST_PER_CELL,
+                "counters_source": WENO_CAPTURE + ", scaled to the workload by its cell count",
                 "executed_tflops": WENO_FP64_FLOPS_PER_CELL * cfg.cells / t_weno / 1e12,
-                "reference_formula_tflops": 2766.0 * cfg.cells / t_weno / 1e12,
+                "reference_formula_tflops": WENO_REFERENCE_FLOPS_PER_CELL * cfg.cells / t_weno / 1e12,
                 "fma_peak_tflops": fp64.value,
                 "peak_source": "FP64 FMA chains measured live (fmf_measure_fma_rate), one instruction per FMA; "
-                               "HBM peak " + peak_kind,
+                               "HBM peak " + peak_kind + " (MEASURED_PEAKS.json hbm_gbs)",
                 "hbm": {"achieved": gbs, "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": gbs / peaks["hbm_gbs"]}}
-    # Mixed precision (FP32 WENO5 / MTHINC Newton+fluxes / SOR sweeps, FP64 pressure,
-    # projection, divergence, volume sums and state): throughput on the same workload,
-    # and the error of phi, u, v, w, p against the FP64 step after the same steps
-    # from the same initial state.
-    gm = capi.Stepper(cfg, precision=capi.FMF_MIXED, stream=stream.cuda_stream)
-    gm.upload(st)
-    gm.step(args.warmup)
-    gm.sync()
-    barrier()
-    e0.record(stream)
-    gm.step(args.steps)
-    e1.record(stream)
-    e1.synchronize()
-    ms_mixed = replicas.max_over_ranks(e0.elapsed_time(e1))
-    n_err = args.warmup + args.steps
-    g.upload(st)
-    g.step(n_err)
-    ref = g.get_state()
-    gm.upload(st)
-    gm.step(n_err)
-    mix = gm.get_state()
-    ms_stage_m = ctypes.c_float()
-    capi.check(L.fmf_ctx_time_stage(gm.h, 0, 5, ctypes.byref(ms_stage_m)), "time_stage mixed")
-    gm.close()
+    b_cell = B_CELL_FIXED + B_CELL_PER_SOR * n_sor
+    step_gbs = b_cell * cfg.cells / (ms / args.steps * 1e-3) / 1e9
+    step_roofline = {"bytes_per_cell": b_cell, "formula": "664 + 168 * mean viscous iterations",
+                     "sor_iterations_mean": n_sor, "achieved": step_gbs, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                     "frac": step_gbs / peaks["hbm_gbs"],
+                     "note": "the FP64 step is bound by the FP64 pipe (its largest kernels issue FP64 instructions "
+                             "near the pipe's rate), not by HBM"}
 
-    def rel(f):
-        a, b = C.interior(mix[f]), C.interior(ref[f])
-        return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))
-
-    mixed = {"value": replicas.throughput(cfg.cells, args.steps, ms_mixed * 1e-3), "unit": UNIT,
-             "ms_per_step": ms_mixed / args.steps, "speedup_vs_fp64": ms / ms_mixed,
-             "steps_compared": n_err,
-             "max_rel_err_vs_fp64": {"phi": rel(9), "u": rel(0), "v": rel(1), "w": rel(2), "p": rel(6)},
-             "weno5_ms": ms_stage_m.value,
-             "precision": "fp32: WENO5, MTHINC Newton + Gauss-point fluxes, CSF normals and curvature, viscous "
-                          "sweeps on FP32 corrections (FP64 residual, one refinement step); fp64: state, "
-                          "pressure FFT+TDMA, projection, divergence, volume sums"}
-    mixed_droplet = None
-    if rank == 0 and args.mixed_workload:
+    # ---- mixed precision on the same workload -----------------------------------
+    mixed = None
+    horizon = None
+    second = None
+    if rank == 0:
         g.close()
-        mixed_droplet = mixed_case(args.mixed_workload, 5, 3, stream)
+        mixed = mixed_case(cfg, st, args.steps, args.warmup, stream, fp64_ms=ms / args.steps)
+        mixed["precision"] = ("fp32: WENO5, MTHINC Newton + Gauss-point fluxes, CSF normals and curvature, viscous "
+                              "sweeps on FP32 corrections (FP64 residual, one refinement step); fp64: state, "
+                              "pressure FFT+TDMA, projection, divergence, volume sums")
+        if args.mixed_horizon > 0:
+            horizon = mixed_horizon(cfg, st, args.mixed_horizon, 100, stream)
+        del st
+        if args.second_workload:
+            cfg2 = C.get(args.second_workload)
+            g2 = capi.Stepper(cfg2, stream=stream.cuda_stream)
+            st2 = g2.initial_state()
+            g2.close()
+            second = mixed_case(cfg2, st2, args.steps, args.warmup, stream)
     adjoint = None
     if rank == 0 and args.adjoint_steps > 0:
         adjoint = adjoint_cost(args.adjoint_steps, stream, args.adjoint_every, args.adjoint_workload)
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
-        v, dt = cpu_baseline_sample(cfg, 1)
-        cpu = {"value": v, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
-               "sample": f"1 full step of {args.workload} after 1 warm-up step ({dt:.1f} s), oracle/fmf_oracle.cpp "
-                         "C++/OpenMP restatement, all host threads"}
+        v, dt, cores = cpu_baseline_sample(cfg, 1, 2)
+        cpu = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+               "sample": f"2 full steps of {cfg.name} after 1 warm-up step ({dt:.1f} s), oracle/fmf_oracle.cpp "
+                         "C++/OpenMP restatement (g++ -O3), all host threads, OMP_PROC_BIND=close"}
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-                "config": {"workload": f"{args.workload} {cfg.ni}x{cfg.nj}x{cfg.nk} (ni,nj_wall,nk)",
-                           "precision": "fp64", "l2": "inputs larger than L2 (state + work arrays ~GBs/step)",
-                           "sor_iterations_mean": float(np.mean(iters)) if iters else None,
-                           "parallelism": "replicas" if world > 1 else "single"},
+                "config": config_dict(cfg, world),
                 "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 10 * bytes_field,
-                        "d2h_bytes_per_step": 12 * bytes_field},
-                "gpu_launches": int(launches), "clocks": clk, "roofline": roofline, "cpu_baseline": cpu,
-                "mixed": mixed, "mixed_droplet": mixed_droplet, "adjoint": adjoint}
+                        "d2h_bytes_per_step": 12 * bytes_field, "steps": args.steps},
+                "gpu_launches": int(launches), "clocks": clk, "roofline": roofline, "step_roofline": step_roofline,
+                "cpu_baseline": cpu, "mixed": mixed, "mixed_horizon": horizon, "second_workload": second,
+                "adjoint": adjoint}
         print(json.dumps(line), flush=True)
-    g.close()
+    else:
+        g.close()
 
 
 if __name__ == "__main__":

@@ -17,6 +17,10 @@ void weno5_both(cudaStream_t s, const Grid& g, double dxi, double dyi, double dz
 // cal_advu_weno5 of (u, v, w) alone into adv (fp32: split pairs of 3 fields, 3 n float2)
 void weno5_one(cudaStream_t s, const Grid& g, double dxi, double dyi, double dzi, const double* u, const double* v,
                const double* w, double* const* adv, bool fp32 = false, float2* split = nullptr);
+// both levels, the second (uo, vo, wo into advo) skipped on the device where *keep != 0
+void weno5_keep(cudaStream_t s, const Grid& g, double dxi, double dyi, double dzi, const double* u, const double* v,
+                const double* w, const double* uo, const double* vo, const double* wo, double* const* adv,
+                double* const* advo, const int* keep, bool fp32 = false, float2* split = nullptr);
 
 // cal_grad_p2a (the vertex gradients of q at (i+1/2, j+1/2, k+1/2), i, j, k in
 // -2..n+2) in fewer FP64 operations than the reference's order
@@ -38,9 +42,10 @@ void mthinc_fluxes(cudaStream_t s, const Grid& g, double dxinv, double dyinv, do
 // and nj % 8 == 0 (csf_supported).  fp32: normals and curvature in FP32.  kap
 // (optional, 3 arrays of n): the curvatures at the interior u, v, w points.
 bool csf_supported(const Grid& g);
+// skip (optional): a device int; where it is nonzero the kernel writes nothing
 void csf_force(cudaStream_t s, const Grid& g, double dxinv, double dyinv, double dzinv, double rhol, double rhog,
                double sigma, const double* phi, double* fu, double* fv, double* fw, bool fp32 = false,
-               double* kap = nullptr);
+               double* kap = nullptr, const int* skip = nullptr);
 
 // The explicit viscous term (calsij, cal_arith_tau, cal_div_tensor) at the interior
 // u, v, w points into vis[0..2]; tau: 6 n doubles of workspace; sk (optional, 6 n):

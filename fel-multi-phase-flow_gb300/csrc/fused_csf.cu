@@ -185,7 +185,9 @@ __device__ void centre_normals(const CsfP<R>& p, Smem<R>& S, int gk, int gk1, in
 template <class R>
 __global__ void __launch_bounds__(256) k_csf(Grid g, CsfP<R> p, int kchunk, const double* __restrict__ phi,
                                              double* __restrict__ fu, double* __restrict__ fv,
-                                             double* __restrict__ fw, double* __restrict__ kap) {
+                                             double* __restrict__ fw, double* __restrict__ kap,
+                                             const int* __restrict__ skip) {
+  if (skip && *skip) return;  // the whole block leaves before any barrier
   extern __shared__ double smraw[];
   Smem<R>& S = *reinterpret_cast<Smem<R>*>(smraw);
   const int I0 = 1 + blockIdx.x * TX, J0 = 1 + blockIdx.y * TY;
@@ -298,7 +300,7 @@ int csf_chunk(const Grid& g, const void* fn, size_t smem) {
 
 template <class R>
 void launch_csf(cudaStream_t s, const Grid& g, double dxinv, double dyinv, double dzinv, double rhol, double rhog,
-                double sigma, const double* phi, double* fu, double* fv, double* fw, double* kap) {
+                double sigma, const double* phi, double* fu, double* fv, double* fw, double* kap, const int* skip) {
   CsfP<R> p;
   p.dxi = (R)dxinv;
   p.dyi = (R)dyinv;
@@ -317,7 +319,7 @@ void launch_csf(cudaStream_t s, const Grid& g, double dxinv, double dyinv, doubl
   cudaFuncSetAttribute(k_csf<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   const int kchunk = csf_chunk(g, (const void*)k_csf<R>, smem);
   dim3 gr((unsigned)(g.ni / TX), (unsigned)(g.nj / TY), (unsigned)((g.nk + kchunk - 1) / kchunk));
-  k_csf<R><<<gr, 256, smem, s>>>(g, p, kchunk, phi, fu, fv, fw, kap);
+  k_csf<R><<<gr, 256, smem, s>>>(g, p, kchunk, phi, fu, fv, fw, kap, skip);
   count_launch();
 }
 }  // namespace
@@ -325,11 +327,12 @@ void launch_csf(cudaStream_t s, const Grid& g, double dxinv, double dyinv, doubl
 bool csf_supported(const Grid& g) { return g.ni % TX == 0 && g.nj % TY == 0; }
 
 void csf_force(cudaStream_t s, const Grid& g, double dxinv, double dyinv, double dzinv, double rhol, double rhog,
-               double sigma, const double* phi, double* fu, double* fv, double* fw, bool fp32, double* kap) {
+               double sigma, const double* phi, double* fu, double* fv, double* fw, bool fp32, double* kap,
+               const int* skip) {
   if (fp32)
-    launch_csf<float>(s, g, dxinv, dyinv, dzinv, rhol, rhog, sigma, phi, fu, fv, fw, kap);
+    launch_csf<float>(s, g, dxinv, dyinv, dzinv, rhol, rhog, sigma, phi, fu, fv, fw, kap, skip);
   else
-    launch_csf<double>(s, g, dxinv, dyinv, dzinv, rhol, rhog, sigma, phi, fu, fv, fw, kap);
+    launch_csf<double>(s, g, dxinv, dyinv, dzinv, rhol, rhog, sigma, phi, fu, fv, fw, kap, skip);
 }
 
 }  // namespace fused

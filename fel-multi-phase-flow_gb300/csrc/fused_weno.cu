@@ -113,12 +113,15 @@ __device__ __forceinline__ float2 split_pair(double q) {
 struct SplitSrc {
   const double* f[6];
 };
-// the split pairs of nf (3 or 6) fields, field f at out[f n ..]
+// the split pairs of NF (3 or 6) fields, field f at out[f n ..]; the last three of
+// six are skipped where *keep != 0 (their level's advection is carried over)
 template <int NF>
-__global__ void k_split(long n, SplitSrc src, float2* __restrict__ out) {
+__global__ void k_split(long n, SplitSrc src, float2* __restrict__ out, const int* __restrict__ keep) {
+  const int nf = (NF == 6 && keep && *keep) ? 3 : NF;
   for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) {
 #pragma unroll
-    for (int f = 0; f < NF; ++f) out[f * n + t] = split_pair(__ldg(src.f[f] + t));
+    for (int f = 0; f < NF; ++f)
+      if (f < nf) out[f * n + t] = split_pair(__ldg(src.f[f] + t));
   }
 }
 
@@ -169,8 +172,10 @@ __device__ __forceinline__ float wdir_f32(const float2* __restrict__ q, long c, 
   const float den = fmaf(X, 1.0f / 6.0f, fmaf(Z, 0.5f, Y));
   return (fabsf(vsum) * kx) * (__fdividef(num, den) * s);
 }
-// sp: the split pair arrays of u, v, w (then uo, vo, wo for the second level)
-__global__ void __launch_bounds__(128) k_weno2_f32(Grid g, int nlev, float kx, float ky, float kz,
+// sp: the split pair arrays of u, v, w (then uo, vo, wo for the second level); the
+// second level is skipped where *keep != 0
+__global__ void __launch_bounds__(128) k_weno2_f32(Grid g, int nlev, const int* __restrict__ keep, float kx,
+                                                   float ky, float kz,
                                                    const float2* __restrict__ sp, double* __restrict__ au,
                                                    double* __restrict__ av, double* __restrict__ aw,
                                                    double* __restrict__ auo, double* __restrict__ avo,
@@ -183,6 +188,7 @@ __global__ void __launch_bounds__(128) k_weno2_f32(Grid g, int nlev, float kx, f
   const long c = g.at(i, j, k);
 #pragma unroll 1
   for (int lev = 0; lev < nlev; ++lev) {
+    if (lev == 1 && keep && *keep) break;
     const float2* U = sp + (long)(3 * lev) * g.n;
     const float2* V = U + g.n;
     const float2* W = V + g.n;
@@ -206,7 +212,8 @@ __global__ void __launch_bounds__(128) k_weno2_f32(Grid g, int nlev, float kx, f
   }
 }
 
-__global__ void __launch_bounds__(128) k_weno2(Grid g, int nlev, double dxi, double dyi, double dzi,
+__global__ void __launch_bounds__(128) k_weno2(Grid g, int nlev, const int* __restrict__ keep, double dxi,
+                                               double dyi, double dzi,
                                                const double* __restrict__ u,
                                                const double* __restrict__ v, const double* __restrict__ w,
                                                const double* __restrict__ uo, const double* __restrict__ vo,
@@ -223,6 +230,7 @@ __global__ void __launch_bounds__(128) k_weno2(Grid g, int nlev, double dxi, dou
   const double kx = dxi * (1.0 / 24.0), ky = dyi * (1.0 / 24.0), kz = dzi * (1.0 / 24.0);
 #pragma unroll 1
   for (int lev = 0; lev < nlev; ++lev) {
+    if (lev == 1 && keep && *keep) break;
     const double* U = lev ? uo : u;
     const double* V = lev ? vo : v;
     const double* W = lev ? wo : w;
@@ -255,7 +263,8 @@ __global__ void __launch_bounds__(128) k_weno2(Grid g, int nlev, double dxi, dou
 // variant first writes the split pairs of the 3 nlev fields into `split`.
 static void weno5_levels(cudaStream_t s, const Grid& g, int nlev, double dxi, double dyi, double dzi,
                          const double* u, const double* v, const double* w, const double* uo, const double* vo,
-                         const double* wo, double* const* adv, double* const* advo, bool fp32, float2* split) {
+                         const double* wo, double* const* adv, double* const* advo, bool fp32, float2* split,
+                         const int* keep = nullptr) {
   dim3 b(32, 4, 1);
   dim3 gr((unsigned)((g.ni + 31) / 32), (unsigned)((g.nj + 3) / 4), (unsigned)g.nk);
   double* const ao[3] = {advo ? advo[0] : nullptr, advo ? advo[1] : nullptr, advo ? advo[2] : nullptr};
@@ -266,15 +275,16 @@ static void weno5_levels(cudaStream_t s, const Grid& g, int nlev, double dxi, do
     }
     const SplitSrc src{{u, v, w, uo, vo, wo}};
     if (nlev == 2)
-      k_split<6><<<152 * 8, 256, 0, s>>>(g.n, src, split);
+      k_split<6><<<152 * 8, 256, 0, s>>>(g.n, src, split, keep);
     else
-      k_split<3><<<152 * 8, 256, 0, s>>>(g.n, src, split);
-    k_weno2_f32<<<gr, b, 0, s>>>(g, nlev, (float)(dxi / 24.0), (float)(dyi / 24.0), (float)(dzi / 24.0), split,
-                                 adv[0], adv[1], adv[2], ao[0], ao[1], ao[2]);
+      k_split<3><<<152 * 8, 256, 0, s>>>(g.n, src, split, nullptr);
+    k_weno2_f32<<<gr, b, 0, s>>>(g, nlev, keep, (float)(dxi / 24.0), (float)(dyi / 24.0), (float)(dzi / 24.0),
+                                 split, adv[0], adv[1], adv[2], ao[0], ao[1], ao[2]);
     count_launch(2);
     return;
   }
-  k_weno2<<<gr, b, 0, s>>>(g, nlev, dxi, dyi, dzi, u, v, w, uo, vo, wo, adv[0], adv[1], adv[2], ao[0], ao[1], ao[2]);
+  k_weno2<<<gr, b, 0, s>>>(g, nlev, keep, dxi, dyi, dzi, u, v, w, uo, vo, wo, adv[0], adv[1], adv[2], ao[0], ao[1],
+                           ao[2]);
   count_launch();
 }
 
@@ -287,6 +297,12 @@ void weno5_both(cudaStream_t s, const Grid& g, double dxi, double dyi, double dz
 void weno5_one(cudaStream_t s, const Grid& g, double dxi, double dyi, double dzi, const double* u, const double* v,
                const double* w, double* const* adv, bool fp32, float2* split) {
   weno5_levels(s, g, 1, dxi, dyi, dzi, u, v, w, nullptr, nullptr, nullptr, adv, nullptr, fp32, split);
+}
+
+void weno5_keep(cudaStream_t s, const Grid& g, double dxi, double dyi, double dzi, const double* u, const double* v,
+                const double* w, const double* uo, const double* vo, const double* wo, double* const* adv,
+                double* const* advo, const int* keep, bool fp32, float2* split) {
+  weno5_levels(s, g, 2, dxi, dyi, dzi, u, v, w, uo, vo, wo, adv, advo, fp32, split, keep);
 }
 
 // n doubles of both signs spread over magnitudes 2^-96 .. 2^127 with pseudo-random

@@ -15,9 +15,14 @@
 // tension of phi(1) (:547-566) the previous step's of phin(1): the step swaps
 // those buffers instead of recomputing them, and computes one WENO5 level and one
 // CSF force.  The carried terms are valid while the state continues from this
-// context's previous step (`cont`); uploading, the start-up pass, the host-buffer
-// step, new walls or a request for a state pointer clear it (FMF_STEP_CACHE=0 in
-// the environment at creation turns the reuse off).
+// context's previous step (`cont`); uploading, the start-up pass, new walls or a
+// request for a state pointer clear it (FMF_STEP_CACHE=0 in the environment at
+// creation turns the reuse off).  The host-buffer step uploads the caller's state:
+// there the uploaded uo, vo, wo and phi(1) are compared bit for bit with the
+// device's copies, and the kernels of the two carried terms read the outcome from
+// device flags (no host synchronisation): equal inputs (a caller that passes back
+// the previous step's result) keep the carried terms, any other inputs recompute
+// them.
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
@@ -53,6 +58,8 @@ struct fmf_ctx {
   bool warm = false;   // the first step runs eagerly (allocates scratch, twiddle tables)
   bool reuse = true;   // carry advo and sfst over from the previous step (FMF_STEP_CACHE=0 disables)
   bool cont = false;   // the state continues from this context's previous step
+  bool verify = false; // this step decides on the device whether the carried terms hold (same[])
+  int* same = nullptr; // device: [0] uploaded uo, vo, wo equal the carried ones; [1] phi(1) likewise
   void* scr = nullptr; // this context's scratch set
   std::map<GraphKey, GraphEntry> cache;
   fmf_params prm;
@@ -86,6 +93,38 @@ struct fmf_ctx {
 };
 
 namespace {
+// *same = 0 where any of the nf field pairs a[f], b[f] (n doubles each) differ in a bit
+struct Pairs3 {
+  const double* a[3];
+  const double* b[3];
+};
+__global__ void k_same(long n, int nf, Pairs3 p, int* same) {
+  bool eq = true;
+  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x)
+    for (int f = 0; f < nf; ++f)
+      eq = eq && __double_as_longlong(p.a[f][t]) == __double_as_longlong(p.b[f][t]);
+  if (__syncthreads_and(eq) == 0 && threadIdx.x == 0) *same = 0;
+}
+// b[f] = a[f] unless *same (then they are equal already)
+__global__ void k_copy_unless(long n, int nf, Pairs3 p, const int* same) {
+  if (*same) return;
+  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x)
+    for (int f = 0; f < nf; ++f) const_cast<double*>(p.b[f])[t] = p.a[f][t];
+}
+// staged copies of nf fields (src) against their destinations (dst): same[0] = 1 if
+// every bit agrees, else 0 and the destinations take the staged values
+void verify_upload(cudaStream_t s, long n, int nf, const double* const* src, double* const* dst, int* same) {
+  Pairs3 p{};
+  for (int f = 0; f < nf; ++f) {
+    p.a[f] = src[f];
+    p.b[f] = dst[f];
+  }
+  FMF_CUDA(cudaMemsetAsync(same, 0xff, sizeof(int), s));
+  k_same<<<152 * 8, 256, 0, s>>>(n, nf, p, same);
+  k_copy_unless<<<152 * 8, 256, 0, s>>>(n, nf, p, same);
+  count_launch(2);
+}
+
 double* alloc(fmf_ctx* c, long n) {
   void* p = nullptr;
   if (!FMF_CUDA(cudaMalloc(&p, sizeof(double) * n))) {
@@ -153,6 +192,7 @@ int fmf_ctx_create(const fmf_params* prm, fmf_ctx** out) {
   c->an_f = alloc(c, prm->nj + 6);
   c->ap_f = alloc(c, prm->nj + 6);
   c->red = alloc(c, 64);
+  c->same = (int*)alloc(c, 1);
   c->mixed = prm->precision == FMF_MIXED;
   if (c->mixed) {
     fused::RefineBufs& rb = c->rb;
@@ -382,7 +422,10 @@ static void seg_pre2(fmf_ctx* c) {
   double* phi1 = c->phi + n;
   double* phin1 = c->phin + n;
   // :532-541 (advo carried over from the previous step where the state continues)
-  if (c->cont)
+  if (c->verify)
+    fused::weno5_keep(s, g, dxinv, dyinv, dzinv, c->u, c->v, c->w, c->uo, c->vo, c->wo, c->adv, c->advo, c->same,
+                      c->mixed, c->wsplit);
+  else if (c->cont)
     fused::weno5_one(s, g, dxinv, dyinv, dzinv, c->u, c->v, c->w, c->adv, c->mixed, c->wsplit);
   else
     fused::weno5_both(s, g, dxinv, dyinv, dzinv, c->u, c->v, c->w, c->uo, c->vo, c->wo, c->adv, c->advo, c->mixed,
@@ -392,7 +435,11 @@ static void seg_pre2(fmf_ctx* c) {
   fused::explicit_viscous(s, g, dxinv, dyinv, dzinv, c->u, c->v, c->w, c->rmu, c->tau, c->vis);
   // :545-570 surface tension (sfst carried over from the previous step's sfstn where
   // the state continues)
-  if (!c->cont) csf_one(c, phi1, c->sfst);
+  if (c->verify && fused::csf_supported(g))
+    fused::csf_force(s, g, dxinv, dyinv, dzinv, P.rhol, P.rhog, P.sigma, phi1, c->sfst[0], c->sfst[1], c->sfst[2],
+                     c->mixed, nullptr, c->same + 1);
+  else if (!c->cont || c->verify)
+    csf_one(c, phi1, c->sfst);
   csf_one(c, phin1, c->sfstn);
   // :579-603 (cal_av of rho/rhon at :571-573 feeds nothing downstream)
   const double* advp[3] = {c->adv[0], c->adv[1], c->adv[2]};
@@ -488,7 +535,7 @@ static void run_segment(fmf_ctx* c, int id, void (*fn)(fmf_ctx*)) {
     fn(c);
     return;
   }
-  GraphKey key{id + (c->cont ? 100 : 0),
+  GraphKey key{id + (c->cont ? 100 : 0) + (c->verify ? 200 : 0),
                {c->u, c->v, c->w, c->uo, c->vo, c->wo, c->un, c->vn, c->wn, c->p, c->po, c->pn, c->phi, c->phin,
                 c->adv[0], c->sfst[0]}};
   auto it = c->cache.find(key);
@@ -643,11 +690,34 @@ int fmf_ctx_step_host(fmf_ctx* c, const double* const* in, double* const* out) {
   auto d2h = [&](int f, const double* src, cudaStream_t st) {
     FMF_CUDA(cudaMemcpyAsync(out[f], src, b, cudaMemcpyDeviceToHost, st));
   };
-  c->cont = false;  // the inputs are the caller's, not this context's last step
-  for (int f : {0, 1, 2, 8, 9}) h2d(f, c->s);  // u, v, w, phi
+  // Where this context's last step produced the device state, its carried advection
+  // of (uo, vo, wo) and surface tension of phi(1) hold if the caller passes those
+  // fields back unchanged: they go up into free work arrays (div; un, vn, wn, written
+  // by the step only after its first two parts) and are compared with the device's
+  // copies there.
+  c->verify = c->cont;
+  c->cont = false;
+  for (int f : {0, 1, 2, 8}) h2d(f, c->s);  // u, v, w, phi(0)
+  if (c->verify) {
+    FMF_CUDA(cudaMemcpyAsync(c->div, in[9], b, cudaMemcpyHostToDevice, c->s));
+    const double* src[1] = {c->div};
+    double* dst[1] = {field_ptr(c, 9)};
+    verify_upload(c->s, n, 1, src, dst, c->same + 1);
+  } else {
+    h2d(9, c->s);
+  }
   FMF_CUDA(cudaEventRecord(c->ev_in, c->s));
   FMF_CUDA(cudaStreamWaitEvent(c->cs, c->ev_in, 0));
-  for (int f : {3, 4, 5, 6, 7}) h2d(f, c->cs);  // uo, vo, wo, p, po
+  if (c->verify) {
+    double* st[3] = {c->un, c->vn, c->wn};
+    for (int f = 0; f < 3; ++f) FMF_CUDA(cudaMemcpyAsync(st[f], in[3 + f], b, cudaMemcpyHostToDevice, c->cs));
+    const double* src[3] = {c->un, c->vn, c->wn};
+    double* dst[3] = {c->uo, c->vo, c->wo};
+    verify_upload(c->cs, n, 3, src, dst, c->same);
+  } else {
+    for (int f : {3, 4, 5}) h2d(f, c->cs);  // uo, vo, wo
+  }
+  for (int f : {6, 7}) h2d(f, c->cs);  // p, po
   FMF_CUDA(cudaEventRecord(c->ev_in2, c->cs));
   // the result's uo, vo, wo, po: this step's u, v, w, p
   d2h(3, c->u, c->cs);
@@ -666,6 +736,7 @@ int fmf_ctx_step_host(fmf_ctx* c, const double* const* in, double* const* out) {
         for (int f = 8; f < 12; ++f) d2h(f, phin + (f % 2) * n, c->cs);
       },
       [&]() { FMF_CUDA(cudaStreamWaitEvent(c->s, c->ev_in2, 0)); });
+  c->verify = false;
   c->graphs = gr;
   c->warm = true;
   for (int f : {0, 1, 2, 6}) d2h(f, field_ptr(c, f), c->s);

@@ -123,7 +123,8 @@ def test_division_free_rsqrt(fmf_lib):
 @pytest.mark.parametrize("prec", ["fp64", "mixed"])
 def test_step_host_matches_upload_step_download(fmf_lib, prec):
     """fmf_ctx_step_host (copies overlapping the step, phin not uploaded) gives bit for
-    bit the state of upload + step + download, step after step, in both precisions."""
+    bit the state of upload + step + download, step after step, in both precisions,
+    whether the caller passes back the previous result or a changed state."""
     import torch
 
     cfg = C.get("couette32")
@@ -134,13 +135,22 @@ def test_step_host_matches_upload_step_download(fmf_lib, prec):
     pin = torch.empty((12,) + cfg.shape, dtype=torch.float64, pin_memory=True).numpy()
     pin[:] = st
     ref = st.copy()
-    for _ in range(3):
+    # from the second call on the inputs are the previous result: the carried
+    # advection of (uo, vo, wo) and surface tension of phi(1) are kept after the
+    # device compares them; calls 3 and 4 pass a changed uo and phi(1), which the
+    # compare must catch (the terms are then recomputed)
+    for it in range(5):
+        if it == 2:
+            pin[3, 5, 6, 7] += 1e-3
+        if it == 3:
+            pin[9, 6, 7, 8] -= 1e-3
+        ref[:] = pin
         b.step_host(pin, pin)
         a.upload(ref)
         a.step(1)
         a.download(ref)
         a.sync()
-        assert np.array_equal(pin, ref)
+        assert np.array_equal(pin, ref), it
     a.close()
     b.close()
 
