@@ -50,6 +50,9 @@ bool uniform_dy(const double* a, int ID, int nj, double* out) {
 }
 int g_last_sor_iters = 0;
 double g_last_sor_ratio = 0.0;
+double g_last_solp[2] = {0.0, 0.0};  // err, err0 of the last solp_fft_tdma4_ monitor
+double g_sor_tol = 1.0e-3;           // solu_sor4.f:291 stop rule, fmf_set_sor
+int g_sor_max = 21;                  // solu_sor4.f:130 do lp=0,20
 }  // namespace
 
 // Every array argument is resolved (evaluated as a macro argument) before the
@@ -103,6 +106,18 @@ int fmf_device_synchronize(void) {
 long long fmf_kernel_launches(void) { return launches(); }
 int fmf_last_sor_iterations(void) { return g_last_sor_iters; }
 double fmf_last_sor_ratio(void) { return g_last_sor_ratio; }
+int fmf_last_solp_residual(double* err, double* err0) {
+  if (!err || !err0) return FMF_ERR_ARG;
+  *err = g_last_solp[0];
+  *err0 = g_last_solp[1];
+  return FMF_OK;
+}
+int fmf_set_sor(double tol, int max_iter) {
+  if (!(tol > 0.0) || max_iter < 1 || max_iter > 100000) return FMF_ERR_ARG;
+  g_sor_tol = tol;
+  g_sor_max = max_iter;
+  return FMF_OK;
+}
 
 // ---------------------------------------------------------------- C1
 void cal_grad_p2a_(int* ID, int* svall, int* ni, int* nj, int* nk, double* dxinv, double* dyinv_array,
@@ -385,7 +400,7 @@ void solu_sor4_(int* ipara, int* ID, int* nID, int* ndiv, int* ni, int* nj, int*
   if (!call.ok || !es) return;
   double err = 0.0, err0 = 0.0;
   int lp;
-  for (lp = 0; lp <= 20; ++lp) {
+  for (lp = 0; lp < g_sor_max; ++lp) {
     op::sor_iteration(s, g, *dt, dr, drn, c, src, du, dv, dw, *uwall, *dy, dl1, dl2, dphi, es);
     double e = 0.0;
     FMF_CUDA(cudaMemcpyAsync(&e, es, sizeof(double), cudaMemcpyDeviceToHost, s));
@@ -396,10 +411,13 @@ void solu_sor4_(int* ipara, int* ID, int* nID, int* ndiv, int* ni, int* nj, int*
     }
     err = std::sqrt(e / (double)g.cells()) + 1.0e-99;
     if (lp == 0) err0 = err;
-    if (err / err0 <= 1.0e-3) break;
+    if (err / err0 <= g_sor_tol) break;
   }
-  g_last_sor_iters = (lp <= 20 ? lp : 20) + 1;
+  g_last_sor_iters = (lp < g_sor_max ? lp : g_sor_max - 1) + 1;
   g_last_sor_ratio = err0 > 0.0 ? err / err0 : 0.0;
+  // the loop ended without meeting the stop rule (solu_sor4.f:130,291-293): the
+  // reference carries on with the last iterate; reported, not fatal
+  if (lp == g_sor_max && !get_status()) set_status(FMF_ERR_ITER_CAP);
   if (*ID == 0 && *imon_t > 0 && (*nstep % *imon_t) == 0)
     std::printf("Err_solu %10d%10d%20.10E%20.10E%20.10E\n", *nstep, lp, err / err0, err, err0);
   call.finish();
@@ -525,6 +543,8 @@ void solp_fft_tdma4_(int* ipara, int* ID, int* ndiv, int* ni, int* nj, int* nk, 
   FMF_CUDA(cudaStreamSynchronize(s));
   const double N = (double)g.cells();
   const double err = std::sqrt(h[0] / N) + 1.0e-99, err0 = std::sqrt(h[1] / N) + 1.0e-99;
+  g_last_solp[0] = err;
+  g_last_solp[1] = err0;
   if (*ID == 0) std::printf("Err_solp %10d%20.10E%20.10E%20.10E\n", *nstep, err / err0, err, err0);
   call.finish();
 }

@@ -148,8 +148,11 @@ void dataou_(int* ipara, int* ID, int* ni, int* nj, int* nk, int* nbub, int* nst
     std::snprintf(fname, sizeof(fname), "x%07d", *nstep);
   double* f[8] = {u, v, w, p, uo, vo, wo, po};
   if (mode() == FMF_RESIDENT) {
-    for (double* q : f) sync_to_host(q, 0);  // arrays the library never saw: nothing to do
-    sync_to_host(phi, 0);
+    // every device mirror inside each array (none for arrays the library never
+    // saw; phi's slices may have been registered one by one)
+    const size_t b = sizeof(double) * (size_t)(*ni + 6) * (*nj + 6) * (*nk + 6);
+    for (double* q : f) sync_range_to_host(q, b);
+    sync_range_to_host(phi, b * (size_t)(*nbub + 1));
   }
   const int st = fmf_write_checkpoint(fname, *ni, *nj, *nk, *nbub, *nstep, *time, f, phi);
   if (st) set_status(st);
@@ -171,8 +174,9 @@ void datain_(int* ipara, int* ID, int* ni, int* nj, int* nk, int* nbub, int* nst
     return;
   }
   if (mode() == FMF_RESIDENT) {
-    for (double* q : f) sync_to_device(q, 0);
-    sync_to_device(phi, 0);
+    const size_t b = sizeof(double) * (size_t)(*ni + 6) * (*nj + 6) * (*nk + 6);
+    for (double* q : f) sync_range_to_device(q, b);
+    sync_range_to_device(phi, b * (size_t)(*nbub + 1));
   }
   std::printf(" input %s\n", fname);
 }

@@ -183,6 +183,28 @@ int sync_to_device(const void* host, size_t bytes_or_0) {
   FMF_CUDA(cudaStreamSynchronize(stream()));
   return get_status();
 }
+// Every mirror that overlaps [host, host + bytes), for the overlapping part: an
+// array whose pieces were registered separately (3-D slices of a 4-D array passed
+// to different calls) is synchronised whole.
+static int sync_range(const void* host, size_t bytes, bool to_host) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  const uintptr_t a = (uintptr_t)host, b = a + bytes;
+  auto it = g_reg.upper_bound(a);
+  if (it != g_reg.begin() && std::prev(it)->second.end > a) --it;
+  for (; it != g_reg.end() && it->first < b; ++it) {
+    const uintptr_t lo = std::max(a, it->first), hi = std::min(b, it->second.end);
+    if (lo >= hi) continue;
+    char* d = it->second.dev + (lo - it->first);
+    if (to_host)
+      FMF_CUDA(cudaMemcpyAsync((void*)lo, d, hi - lo, cudaMemcpyDeviceToHost, stream()));
+    else
+      FMF_CUDA(cudaMemcpyAsync(d, (const void*)lo, hi - lo, cudaMemcpyHostToDevice, stream()));
+  }
+  FMF_CUDA(cudaStreamSynchronize(stream()));
+  return get_status();
+}
+int sync_range_to_host(const void* host, size_t bytes) { return sync_range(host, bytes, true); }
+int sync_range_to_device(const void* host, size_t bytes) { return sync_range(host, bytes, false); }
 int sync_all_to_host() {
   std::lock_guard<std::mutex> lk(g_mu);
   for (auto& e : g_reg)

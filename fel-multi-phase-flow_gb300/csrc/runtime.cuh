@@ -15,6 +15,9 @@ void set_mode(int m);
 void* mirror(const void* host, size_t bytes, bool* fresh, std::vector<uintptr_t>* protect);
 int sync_to_host(const void* host, size_t bytes_or_0);
 int sync_to_device(const void* host, size_t bytes_or_0);
+// every mirror overlapping [host, host + bytes), for the overlapping bytes
+int sync_range_to_host(const void* host, size_t bytes);
+int sync_range_to_device(const void* host, size_t bytes);
 int sync_all_to_host();
 int forget(const void* host);
 int reset_registry();

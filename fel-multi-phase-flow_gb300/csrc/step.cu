@@ -90,6 +90,9 @@ struct fmf_ctx {
   float2* wsplit = nullptr;  // mixed: split pairs of u, v, w, uo, vo, wo for the FP32 WENO5 (6 n)
   double* host_err = nullptr;  // pinned
   std::vector<int> sor_iters;
+  double sor_tol = 1.0e-3;  // solu_sor4.f:291 stop rule (fmf_ctx_set_sor)
+  int sor_max = 21;         // solu_sor4.f:130 do lp=0,20
+  int capped = 0;           // steps of the last call whose viscous solve hit sor_max
 };
 
 namespace {
@@ -570,7 +573,7 @@ static int step_once(fmf_ctx* c, const std::function<void()>& after_pre = {},
   run_segment(c, 3, seg_pre2);
   double err = 0.0, err0 = 0.0;
   int lp;
-  for (lp = 0; lp <= 20; ++lp) {
+  for (lp = 0; lp < c->sor_max; ++lp) {
     run_segment(c, 1, seg_iter);
     FMF_CUDA(cudaStreamSynchronize(c->s));
     const double e = c->host_err[0];
@@ -580,9 +583,10 @@ static int step_once(fmf_ctx* c, const std::function<void()>& after_pre = {},
     }
     err = std::sqrt(e / (double)g.cells()) + 1.0e-99;
     if (lp == 0) err0 = err;
-    if (err / err0 <= 1.0e-3) break;
+    if (err / err0 <= c->sor_tol) break;
   }
-  c->sor_iters.push_back((lp <= 20 ? lp : 20) + 1);
+  c->sor_iters.push_back((lp < c->sor_max ? lp : c->sor_max - 1) + 1);
+  if (lp == c->sor_max) ++c->capped;  // reported after the call; the step carries on
   run_segment(c, 2, seg_post);
   // :686-697 rotation by pointer
   double* t;
@@ -725,6 +729,7 @@ int fmf_ctx_step_host(fmf_ctx* c, const double* const* in, double* const* out) {
   d2h(5, c->w, c->cs);
   d2h(7, c->p, c->cs);
   c->sor_iters.clear();
+  c->capped = 0;
   const bool gr = c->graphs;
   if (!c->warm) c->graphs = false;
   double* phin = c->phin;
@@ -742,13 +747,15 @@ int fmf_ctx_step_host(fmf_ctx* c, const double* const* in, double* const* out) {
   for (int f : {0, 1, 2, 6}) d2h(f, field_ptr(c, f), c->s);
   FMF_CUDA(cudaStreamSynchronize(c->s));
   FMF_CUDA(cudaStreamSynchronize(c->cs));
-  return st ? st : take_status();
+  const int st2 = st ? st : take_status();
+  return st2 ? st2 : (c->capped ? FMF_ERR_ITER_CAP : FMF_OK);
 }
 
 int fmf_ctx_step(fmf_ctx* c, int nsteps) {
   if (!c || nsteps < 0) return FMF_ERR_ARG;
   ScratchScope scope(c->scr);
   c->sor_iters.clear();
+  c->capped = 0;
   for (int t = 0; t < nsteps; ++t) {
     const bool g = c->graphs;
     if (!c->warm) c->graphs = false;  // first step eager: scratch and tables get allocated here
@@ -757,7 +764,15 @@ int fmf_ctx_step(fmf_ctx* c, int nsteps) {
     c->warm = true;
     if (st) break;
   }
-  return take_status();
+  const int st = take_status();
+  return st ? st : (c->capped ? FMF_ERR_ITER_CAP : FMF_OK);
+}
+
+int fmf_ctx_set_sor(fmf_ctx* c, double tol, int max_iter) {
+  if (!c || !(tol > 0.0) || max_iter < 1 || max_iter > 100000) return FMF_ERR_ARG;
+  c->sor_tol = tol;
+  c->sor_max = max_iter;
+  return FMF_OK;
 }
 
 }  // extern "C"

@@ -9,6 +9,7 @@ from __future__ import annotations
 
 import ctypes
 import os
+import warnings
 
 import numpy as np
 
@@ -19,6 +20,12 @@ _lib = None
 
 FMF_FP64, FMF_MIXED = 0, 1
 FMF_RESIDENT, FMF_COHERENT = 0, 1
+FMF_ERR_ITER_CAP = 4
+
+
+class SorCapWarning(UserWarning):
+    """A viscous solve ended at its iteration cap without meeting its stop rule (the
+    step carried on with the last iterate, as the reference's does)."""
 
 
 class FmfError(RuntimeError):
@@ -57,6 +64,12 @@ def load(path: str | None = None):
         getattr(L, name).restype = ip
     L.fmf_ctx_step.argtypes = [vp, ip]
     L.fmf_ctx_step.restype = ip
+    L.fmf_ctx_set_sor.argtypes = [vp, dp, ip]
+    L.fmf_ctx_set_sor.restype = ip
+    L.fmf_set_sor.argtypes = [dp, ip]
+    L.fmf_set_sor.restype = ip
+    L.fmf_last_solp_residual.argtypes = [ctypes.POINTER(dp), ctypes.POINTER(dp)]
+    L.fmf_last_solp_residual.restype = ip
     L.fmf_ctx_set_stream.argtypes = [vp, vp]
     L.fmf_ctx_set_walls.argtypes = [vp, vp, vp, vp, vp]
     L.fmf_ctx_upload.argtypes = [vp, ctypes.POINTER(vp)]
@@ -84,7 +97,11 @@ def lib():
 
 
 def check(code: int, what: str = "") -> None:
-    if code:
+    """Raise FmfError for a nonzero status; the iteration-cap status (not fatal:
+    the step carried on) is a SorCapWarning instead."""
+    if code == FMF_ERR_ITER_CAP:
+        warnings.warn(f"{what}: {lib().fmf_error_string(code).decode()}", SorCapWarning, stacklevel=2)
+    elif code:
         msg = lib().fmf_error_string(code).decode()
         raise FmfError(f"{what}: {msg} ({code})")
 
@@ -149,6 +166,10 @@ class Stepper:
 
     def step(self, n: int = 1):
         check(lib().fmf_ctx_step(self.h, int(n)), "step")
+
+    def set_sor(self, tol: float = 1e-3, max_iter: int = 21):
+        """The viscous solve's stop rule (default: the reference's)."""
+        check(lib().fmf_ctx_set_sor(self.h, float(tol), int(max_iter)), "set_sor")
 
     def step_host(self, st_in: np.ndarray, st_out: np.ndarray):
         """One step from host state st_in to host state st_out (fmf_ctx_step_host;

@@ -308,6 +308,14 @@ int fmf_format_fortran_e(char* buf, int bufsize, double x, int w, int d);
  * srcs/solu_sor4.f:298-305 and srcs/solp_fft_tdma4.f:84-93). */
 int fmf_last_sor_iterations(void);      /* lp+1 of the last solu_sor4_ call */
 double fmf_last_sor_ratio(void);        /* err/err0 of the last solu_sor4_ call */
+/* err and err0 (RMS Poisson residual and RMS div) of the last solp_fft_tdma4_
+ * call that computed them (srcs/solp_fft_tdma4.f:84-93) */
+int fmf_last_solp_residual(double* err, double* err0);
+/* Stop rule of solu_sor4_: err/err0 <= tol within max_iter outer iterations (the
+ * reference's 1e-3 and 21, srcs/solu_sor4.f:130,291 -- the defaults).  A call that
+ * ends without meeting it leaves FMF_ERR_ITER_CAP in fmf_last_error() and keeps
+ * the last iterate, as the reference does.  No counterpart in the reference. */
+int fmf_set_sor(double tol, int max_iter);
 double fmf_interface_lower(int ni, int nj, int nk, const double* phi_host, double dx,
                            double xl);
 
@@ -319,7 +327,7 @@ double fmf_interface_lower(int ni, int nj, int nk, const double* phi_host, doubl
  * the work is enqueued on `stream` (NULL: the legacy default stream) and no
  * cudaMalloc/cudaFree or allocating library routine is called.  Its scratch is a
  * 512 KiB array compiled into the library, so ceil(nj/8)*nk must not exceed
- * 65536 (FMF_ERR_ARG otherwise, nothing launched).  All calls on a GPU share
+ * 65536 and nk must not exceed 65535 (FMF_ERR_ARG otherwise, nothing launched).  All calls on a GPU share
  * that array: calls that overlap in time on one GPU race.  The first call on
  * each device looks up the array's address; make it before any stream capture.
  * Returns FMF_OK or an FMF_ERR_* code. */
@@ -374,7 +382,13 @@ int fmf_ctx_set_walls(fmf_ctx* ctx, const double* theta0, const double* zeta, co
 int fmf_ctx_upload(fmf_ctx* ctx, const double* const* state);   /* host -> device, async */
 int fmf_ctx_download(fmf_ctx* ctx, double* const* state);       /* device -> host, async */
 int fmf_ctx_init_bc(fmf_ctx* ctx);                  /* start-up boundary pass, main.f90:322-366 */
-int fmf_ctx_step(fmf_ctx* ctx, int nsteps);         /* enqueue nsteps full time steps */
+/* nsteps full time steps; returns FMF_ERR_ITER_CAP (after all nsteps) where a
+ * step's viscous solve ended without meeting its stop rule -- the step carries on
+ * with the last iterate, as the reference's does -- unless a worse error occurred */
+int fmf_ctx_step(fmf_ctx* ctx, int nsteps);
+/* the viscous solve's stop rule err/err0 <= tol within max_iter outer iterations
+ * (default: the reference's 1e-3 and 21, srcs/solu_sor4.f:130,291) */
+int fmf_ctx_set_sor(fmf_ctx* ctx, double tol, int max_iter);
 /* One step from host buffers to host buffers: in[12] -> out[12] (the state layout
  * of fmf_ctx_upload; pinned host memory lets the copies overlap the step).  The
  * same result as fmf_ctx_upload + fmf_ctx_step(ctx, 1) + fmf_ctx_download: uo, vo,

@@ -1,6 +1,7 @@
 """Restart files (dataou.f / datain.f): the record layout gfortran gives an
 unformatted sequential write, read back by the library and written by an
-independent numpy encoder.  Host code only: no GPU needed."""
+independent numpy encoder (host code, no GPU needed); and, on the GPU, the
+drop-ins dataou_/datain_ with device-resident arrays."""
 import ctypes
 import os
 
@@ -99,3 +100,64 @@ def test_size_mismatch_is_an_error(lib, tmp_path):
                                    ph.ctypes.data) != 0
     assert lib.fmf_read_checkpoint(os.path.join(str(tmp_path), "missing").encode(), NI, NJ, NK, NBUB,
                                    ctypes.byref(ns), ctypes.byref(t), _ptrs(big), ph.ctypes.data) != 0
+
+
+@pytest.mark.gpu
+def test_dataou_datain_resident(fmf_lib, tmp_path, monkeypatch):
+    """dataou_ / datain_ with the device copies authoritative (FMF_RESIDENT,
+    dataou.f:26-39, datain.f): arrays whose device mirror is newer than the host
+    (a drop-in call wrote them; phi's two slices registered one by one, as the
+    reference passes phi(...,l) slices) are copied back before the file is written,
+    and the file is byte for byte the one fmf_write_checkpoint writes from the
+    expected values; datain_ re-uploads what it read, which the next resident call
+    then sees on the device."""
+    from fmf import capi
+    from fmf import config as C
+
+    L = fmf_lib
+    L.fmf_write_checkpoint.argtypes = [ctypes.c_char_p] + [ctypes.c_int] * 5 + [ctypes.c_double, ctypes.c_void_p,
+                                                                                ctypes.c_void_p]
+    monkeypatch.chdir(tmp_path)
+    cfg = C.Config("restart", NI, NJ, NK, 2.0, 1.0, 1.0, dt=1e-3, steps=1)
+    I = lambda x: ctypes.byref(ctypes.c_int(x))
+    vp = lambda a: ctypes.c_void_p(a.ctypes.data)
+    L.fmf_reset()
+    L.fmf_set_mode(capi.FMF_RESIDENT)
+    try:
+        f, phi = _fields(5)
+        host = [a.copy() for a in f]
+        hphi = phi.copy()
+        for a in host:
+            L.bnd_periodic_(I(NI), I(NJ), I(NK), vp(a))
+        for sl in range(NBUB + 1):
+            L.bnd_periodic_(I(NI), I(NJ), I(NK), vp(hphi[sl]))
+        assert L.fmf_last_error() == 0
+        # resident: the host arrays still hold the values before the calls
+        assert all(np.array_equal(a, b) for a, b in zip(host, f)) and np.array_equal(hphi, phi)
+        want = [a.copy() for a in f]
+        wphi = phi.copy()
+        for a in want + [wphi[0], wphi[1]]:
+            C.periodic(a, cfg)
+        t = ctypes.byref(ctypes.c_double(0.125))
+        L.dataou_(I(0), I(0), I(NI), I(NJ), I(NK), I(NBUB), I(9), t, *[vp(a) for a in host], vp(hphi))
+        assert L.fmf_last_error() == 0
+        assert L.fmf_write_checkpoint(b"expected", NI, NJ, NK, NBUB, 9, 0.125, _ptrs(want), wphi.ctypes.data) == 0
+        assert open("x0000009", "rb").read() == open("expected", "rb").read()
+        # datain_: a different state in x.inp goes to the host arrays and their mirrors
+        g, gphi = _fields(6)
+        assert L.fmf_write_checkpoint(b"x.inp", NI, NJ, NK, NBUB, 3, 2.5, _ptrs(g), gphi.ctypes.data) == 0
+        ns, tt = ctypes.c_int(0), ctypes.c_double(0.0)
+        L.datain_(I(0), I(0), I(NI), I(NJ), I(NK), I(NBUB), ctypes.byref(ns), ctypes.byref(tt),
+                  *[vp(a) for a in host], vp(hphi))
+        assert L.fmf_last_error() == 0
+        assert ns.value == 3 and tt.value == 2.5
+        assert all(np.array_equal(a, b) for a, b in zip(host, g)) and np.array_equal(hphi, gphi)
+        # the device copies hold the new values: a resident copy reads them there
+        for src, ref in ((host[0], g[0]), (hphi[1], gphi[1])):
+            dst = np.zeros_like(ref)
+            L.cpy_(I(NI), I(NJ), I(NK), vp(src), vp(dst))
+            assert L.fmf_sync_to_host(vp(dst)) == 0
+            assert np.array_equal(dst, ref)
+    finally:
+        L.fmf_reset()
+        L.fmf_set_mode(capi.FMF_RESIDENT)

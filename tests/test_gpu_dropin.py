@@ -323,3 +323,120 @@ def test_cal_av_and_errors(orc, L):
     q[10, 10, 10] = np.nan
     L.cal_av_(I(0), I(1), I(NI), I(NJ), I(NK), ctypes.c_void_p(q.ctypes.data), ctypes.byref(av))
     assert L.fmf_last_error() == 3
+
+
+def test_solp_fft_tdma4_monitor(orc, L):
+    """The Err_solp monitor (solp_fft_tdma4.f:28-95): RMS of the 7-point Poisson
+    residual of dp against div, and RMS of div, as the oracle computes them; on a
+    step that is not a monitor step nothing is computed."""
+    div = np.zeros(SH)
+    d = RNG.normal(size=(NK, NJ, NI))
+    div[3:-3, 3:-3, 3:-3] = d - d.mean()
+    dp = field(0.01)
+    rho, dxi, dyi, dzi = 1.0, 1 / CFG.dx, 1 / CFG.dy, 1 / CFG.dz
+    eo, e0o = ctypes.c_double(), ctypes.c_double()
+    I, D, P = orc.I, orc.D, orc.P
+    orc.lib().orc_solp_fft_tdma4_v(I(NI), I(NJ), I(NK), D(rho), D(dxi), D(dyi), D(dzi), P(div), P(dp),
+                                   ctypes.byref(eo), ctypes.byref(e0o))
+    vp = lambda a: ctypes.c_void_p(a.ctypes.data)
+    L.solp_fft_tdma4_(I(0), I(0), I(1), I(NI), I(NJ), I(NK), I(10), I(5), D(rho), D(dxi), D(dyi), D(dzi), vp(div),
+                      vp(dp))
+    assert L.fmf_last_error() == 0
+    eg, e0g = ctypes.c_double(), ctypes.c_double()
+    assert L.fmf_last_solp_residual(ctypes.byref(eg), ctypes.byref(e0g)) == 0
+    assert abs(eg.value - eo.value) <= 1e-12 * eo.value, (eg.value, eo.value)
+    assert abs(e0g.value - e0o.value) <= 1e-12 * e0o.value, (e0g.value, e0o.value)
+    # nstep not a multiple of imon_t: the monitor is skipped, its last values stay
+    L.solp_fft_tdma4_(I(0), I(0), I(1), I(NI), I(NJ), I(NK), I(11), I(5), D(rho), D(dxi), D(dyi), D(dzi),
+                      vp(field()), vp(dp))
+    eg2, e0g2 = ctypes.c_double(), ctypes.c_double()
+    L.fmf_last_solp_residual(ctypes.byref(eg2), ctypes.byref(e0g2))
+    assert (eg2.value, e0g2.value) == (eg.value, e0g.value)
+
+
+def test_trans_r2w_w2r(orc, L):
+    """trans_r2w / trans_w2r on one rank (trans_r2w.f:23-38): the spectra's storage
+    is shared, so both are copies; w2r after r2w returns the input bit for bit."""
+    n = NI * NJ * NK
+    svall = [NI, NJ, NK]
+    r = RNG.normal(size=n)
+    args = [("i", 0), ("i", 0), ("i", 1), ("ia", svall), ("i", 0), ("none", None), ("none", None), ("a", r),
+            ("a", np.zeros(n))]
+    o, g = both(orc, L, "trans_r2w", args, [1])
+    check(o, g, 0.0)
+    args = [("i", 0), ("i", 0), ("i", 1), ("ia", svall), ("i", 0), ("none", None), ("none", None), ("a", g[0]),
+            ("a", np.zeros(n))]
+    o2, g2 = both(orc, L, "trans_w2r", args, [1])
+    check(o2, g2, 0.0)
+    assert np.array_equal(g2[0], r)
+
+
+def test_cal_grad_p2uvw(orc, L):
+    """Face gradients of q at the u, v, w points (cal_grad_p2uvw.f:25-44)."""
+    args = [("i", 0), ("i", NJ)] + dims() + [("d", 1 / CFG.dx), ("a", DYA), ("d", 1 / CFG.dz), ("a", field())] + \
+        [("a", np.zeros(SH))] * 3
+    o, g = both(orc, L, "cal_grad_p2uvw", args, [2, 3, 4])
+    check(o, g, EXACT)
+
+
+def test_cpy_init_q(orc, L):
+    """cpy (q2 = q1 over the whole array) and init_q (three arrays to zero)."""
+    o, g = both(orc, L, "cpy", dims() + [("a", field()), ("a", field())], [0, 1])
+    check(o, g, 0.0)
+    assert np.array_equal(g[0], g[1])
+    o, g = both(orc, L, "init_q", dims() + [("a", field()), ("a", field()), ("a", field())], [0, 1, 2])
+    for a, b in zip(o, g):
+        assert not a.any() and not b.any()
+
+
+def test_bnd_comm_one_rank(orc, L):
+    """bnd_comm (bnd_comm.f:18) exchanges nothing on one rank: the field is unchanged;
+    a multi-rank call (ipara = 1) is reported as unsupported."""
+    q = field()
+    args = [("i", 0), ("ia", NID)] + dims() + [("i", 0), ("none", None), ("none", None), ("a", q)]
+    o, g = both(orc, L, "bnd_comm", args, [0])
+    assert np.array_equal(o[0], q) and np.array_equal(g[0], q)
+    I = orc.I
+    L.bnd_comm_(I(1), orc.IA(NID), I(NI), I(NJ), I(NK), I(0), None, None, ctypes.c_void_p(q.ctypes.data))
+    assert L.fmf_last_error() == 6
+
+
+def test_solu_sor4_iteration_cap(orc, L):
+    """A stop rule the solve cannot meet: after max_iter outer iterations solu_sor4_
+    keeps the last iterate, as the reference does (solu_sor4.f:130,291-293), and
+    reports FMF_ERR_ITER_CAP; the iterate equals the oracle's after as many
+    iterations."""
+    phi = phi_field().clip(0, 1)
+    rho = 1.0 + 9.0 * (1 - phi)
+    rmu = 0.05 + 0.45 * (1 - phi)
+    I, D, P = orc.I, orc.D, orc.P
+    coef = [np.zeros(SH) for _ in range(45)]
+    parr = (ctypes.POINTER(ctypes.c_double) * 45)(*[P(c) for c in coef])
+    orc.lib().orc_cal_arith_coef_vis_v(I(NI), I(NJ), I(NK), D(1 / CFG.dx), D(1 / CFG.dy), D(1 / CFG.dz), P(rmu),
+                                       parr, ctypes.c_int(0))
+    srcs = [field(0.1) for _ in range(3)]
+    u, v, w = field(0.5), field(0.2), field(0.3)
+    th0, ze, l1, l2 = C.wall_arrays(C.get("couette32", ni=NI, nj=NJ, nk=NK))
+    uo, vo, wo = u.copy(), v.copy(), w.copy()
+    ug, vg, wg = u.copy(), v.copy(), w.copy()
+    rho2 = rho * 1.01
+    orc.lib().orc_set_sor.argtypes = [ctypes.c_double, ctypes.c_int]
+    L.fmf_set_sor.argtypes = [ctypes.c_double, ctypes.c_int]
+    # 1e-300: below what even an exactly converged sweep reaches (err carries +1e-99)
+    orc.lib().orc_set_sor(1e-300, 21)
+    assert L.fmf_set_sor(1e-300, 21) == 0
+    try:
+        err = ctypes.c_double()
+        nit = orc.lib().orc_solu_sor4_v(orc.IA(NID), I(NI), I(NJ), I(NK), D(1e-3), P(rho), P(rho2), parr,
+                                        P(srcs[0]), P(srcs[1]), P(srcs[2]), P(uo), P(vo), P(wo), D(-1.0),
+                                        D(CFG.dy), P(l1), P(l2), P(phi), ctypes.byref(err))
+        vp = lambda a: ctypes.c_void_p(a.ctypes.data)
+        L.solu_sor4_(I(0), I(0), orc.IA(NID), I(1), I(NI), I(NJ), I(NK), None, None, None, I(1), I(0), D(1e-3),
+                     vp(rho), vp(rho2), *[vp(c) for c in coef], vp(srcs[0]), vp(srcs[1]), vp(srcs[2]), vp(ug),
+                     vp(vg), vp(wg), D(-1.0), D(CFG.dy), vp(l1), vp(l2), vp(phi))
+        assert L.fmf_last_error() == 4
+        assert nit == 21 and L.fmf_last_sor_iterations() == 21
+        check([uo, vo, wo], [ug, vg, wg], 1e-13)
+    finally:
+        orc.lib().orc_set_sor(1e-3, 21)
+        L.fmf_set_sor(1e-3, 21)

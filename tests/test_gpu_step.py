@@ -28,18 +28,22 @@ def _compare(orc, cfg, steps, tol=TOL):
     for name, f in FIELDS.items():
         assert relerr(st_g[f], st_o[f]) <= 1e-13, ("init", name)
     g.upload(st_o)
+    gpu_iters = []
     for n in range(steps):
         s.step(st_o, 1)
         g.step(1)
+        gpu_iters += g.sor_iterations()
     out = g.get_state()
     errs = {name: relerr(C.interior(out[f]), C.interior(st_o[f])) for name, f in FIELDS.items()}
     full = {name: relerr(out[f], st_o[f]) for name, f in FIELDS.items()}
     g.close()
+    assert gpu_iters == s.sor_iters, (gpu_iters, s.sor_iters)
     return errs, full, s.sor_iters
 
 
-@pytest.mark.parametrize("steps", [1, 10])
+@pytest.mark.parametrize("steps", [1, 100])
 def test_step_parity_couette32(orc, fmf_lib, steps):
+    """The 32x32x16 Couette workload after 1 step and after its full 100 steps."""
     cfg = C.get("couette32")
     errs, full, _ = _compare(orc, cfg, steps)
     for name in FIELDS:
@@ -69,12 +73,67 @@ def test_sor_iterations_match(orc, fmf_lib):
     g.close()
 
 
-def test_step_parity_couette256_two_steps(orc, fmf_lib):
-    """The 256x128x128 workload (density and viscosity ratio 10, perturbed interface)."""
+def test_step_parity_couette256_ten_steps(orc, fmf_lib):
+    """The 256x128x128 workload (density and viscosity ratio 10, perturbed interface)
+    for 10 steps, with equal viscous iteration counts."""
     cfg = C.get("couette256")
-    errs, full, iters = _compare(orc, cfg, 2)
+    errs, full, iters = _compare(orc, cfg, 10)
     for name in FIELDS:
         assert full[name] <= TOL, (name, full)
+
+
+def test_step_parity_droplet(orc, fmf_lib):
+    """The sessile drop of the 512x256x256 and 256x128x128 workloads at 64x32x32
+    (density ratio 1000, viscosity ratio 100, resting walls, 60/120 deg checkerboard
+    lower wall in 0.125 squares) for 20 steps: the GNBC on mixed angles and the large
+    density jumps of the momentum factors and the projection against the oracle."""
+    cfg = C.get("droplet256", ni=64, nj=32, nk=32, checker_cells=4)
+    s = orc.Solver(cfg)
+    st_o = s.initial_state()
+    g = capi.Stepper(cfg)
+    g.upload(st_o)
+    s.step(st_o, 20)
+    g.step(20)
+    out = g.get_state()
+    assert g.sor_iterations() == s.sor_iters[-20:]
+    for name, f in FIELDS.items():
+        assert relerr(out[f], st_o[f]) <= TOL, (name, relerr(out[f], st_o[f]))
+    g.close()
+    s.close()
+
+
+def test_iteration_cap_fused_step(orc, fmf_lib):
+    """A viscous stop rule the solve cannot meet: each step runs max_iter outer
+    iterations, carries on with the last iterate (solu_sor4.f:130,291-293) and the
+    call reports FMF_ERR_ITER_CAP (a warning in the binding); the state matches the
+    oracle run with the same stop rule."""
+    import ctypes
+
+    cfg = C.get("couette32")
+    s = orc.Solver(cfg)
+    st_o = s.initial_state()
+    g = capi.Stepper(cfg)
+    g.upload(st_o)
+    g.set_sor(1e-300, 6)
+    L = orc.lib()
+    L.orc_set_sor.argtypes = [ctypes.c_double, ctypes.c_int]
+    L.orc_set_sor(1e-300, 6)
+    try:
+        s.step(st_o, 3)
+    finally:
+        L.orc_set_sor(1e-3, 21)
+    assert capi.lib().fmf_ctx_step(g.h, 3) == capi.FMF_ERR_ITER_CAP
+    assert g.sor_iterations() == [6, 6, 6]
+    out = g.get_state()
+    for name, f in FIELDS.items():
+        assert relerr(out[f], st_o[f]) <= TOL, (name, relerr(out[f], st_o[f]))
+    with pytest.warns(capi.SorCapWarning):
+        g.step(1)
+    g.set_sor(1e-3, 21)
+    g.step(1)
+    assert g.sor_iterations()[0] < 21
+    g.close()
+    s.close()
 
 
 def test_invariants_full_size(fmf_lib):

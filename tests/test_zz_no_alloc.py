@@ -18,7 +18,6 @@ from fmf import config as C
 
 pytestmark = pytest.mark.gpu
 
-EXACT = 1e-14  # same reduction tree as cal_av_, so the two agree to round-off
 
 
 def _cal_av_reference(L, q, ni, nj, nk):
@@ -51,7 +50,8 @@ def test_noalloc_mean_matches_cal_av_twice(fmf_lib):
         torch.cuda.synchronize()
         assert rc == 0
         got = float(av_dev.item())
-        assert abs(got - want) <= EXACT * max(abs(want), np.abs(q).max()), (call, got, want)
+        # the same reduction kernels, grid and division as cal_av_: bit for bit
+        assert got == want, (call, got, want)
 
 
 def test_noalloc_rejects_oversized_grid(fmf_lib):
@@ -64,4 +64,8 @@ def test_noalloc_rejects_oversized_grid(fmf_lib):
     q_dev = torch.zeros(8, dtype=torch.float64, device="cuda")
     # ceil(4096/8) * 256 = 131072 partial sums > 65536: refused before any launch
     rc = L.fmf_cal_av_noalloc(16, 4096, 256, q_dev.data_ptr(), av_dev.data_ptr(), None)
+    assert rc == 2
+    # 65536 k planes: within the partial-sum array (ceil(8/8) * 65536) but past the
+    # launch's 65535 block rows, also refused before any launch
+    rc = L.fmf_cal_av_noalloc(16, 8, 65536, q_dev.data_ptr(), av_dev.data_ptr(), None)
     assert rc == 2
