@@ -12,8 +12,10 @@ from pinned host memory, the 12 result fields back), over the same steps.
 Beside the headline: the mixed-precision step on the same workload (value,
 speed-up, per-field error against the FP64 step after the timed steps and over the
 workload's 500 steps), the 256x128x128 Couette case in both precisions, the
-adjoint/forward cost of the 128x64x64 rollout (K = 200, checkpoints every 16), and
-the CPU baseline.
+adjoint/forward cost of the 128x64x64 rollout (K = 200, checkpoints every 16), the
+adjoint with a mixed-precision forward on the 256x128x128 sessile drop (K = 500,
+ceil(sqrt(K)) checkpoints: gradient error against the FP64 adjoint, device bytes,
+cost), and the CPU baseline.
 
 `--impl reference` times the CPU restatement of the reference's algorithm
 (oracle/, the reference Fortran cannot be built here: no Fortran compiler) on
@@ -312,6 +314,79 @@ def adjoint_cost(K, stream, every, workload="couette128"):
             "tolerances": {"sor": 1e-3, "adjoint": 1e-6}}
 
 
+def adjoint_mixed(K, stream, workload="droplet256", every=0):
+    """The adjoint of the K-step rollout with a mixed-precision forward (FP32 WENO5,
+    MTHINC, CSF and viscous corrections in the forward and recomputed steps; FP64
+    reverse) on the sessile drop at 256x128x128, checkpoints every ceil(sqrt(K))
+    steps: the relative error of each gradient against the FP64 adjoint's (largest
+    |difference| over the largest |FP64 gradient|, and the same over the L2 norm),
+    the device bytes each handle holds (own accounting, and the device memory in use
+    after the rollout less that before the handle), and the rollout time against the
+    handle's own forward and against the graph-replayed product step of the same
+    precision.  The FP64 adjoint runs first and is closed before the mixed one
+    (their record slots do not fit together)."""
+    import numpy as np
+    import torch
+
+    from fmf import capi
+    from fmf import config as C
+    from fmf.adjoint import Adjoint
+
+    cfg = C.get(workload)
+    st0 = C.raw_state(cfg)
+    walls = [w.copy() for w in C.wall_arrays(cfg)]
+    every = every if every > 0 else int(math.ceil(math.sqrt(K)))
+    runs = {}
+    grads = {}
+    for prec, key in ((capi.FMF_FP64, "fp64"), (capi.FMF_MIXED, "mixed")):
+        torch.cuda.synchronize()
+        free0, _ = torch.cuda.mem_get_info()
+        A = Adjoint(cfg, sor_tol=1e-3, sor_max=21, adj_tol=1e-6, adj_max=200, precision=prec)
+        A.forward(2, st0, walls)
+        A.rollout(min(K, 2 * every), st0, walls, every=every)  # allocates checkpoints and record slots
+        t0 = time.perf_counter()
+        J = A.forward(K, st0, walls)
+        t_fwd = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        Ja, g = A.rollout(K, st0, walls, every=every)
+        t_adj = time.perf_counter() - t0
+        torch.cuda.synchronize()
+        free1, _ = torch.cuda.mem_get_info()
+        ph = A.phase_seconds()
+        its = A.iterations()
+        dev_bytes = A.device_bytes()
+        A.close()
+        S = capi.Stepper(cfg, precision=prec, stream=stream.cuda_stream)
+        S.upload(st0)
+        S.init_bc()
+        S.step(2)
+        S.sync()
+        S.upload(st0)
+        S.init_bc()
+        S.sync()
+        t0 = time.perf_counter()
+        S.step(K)
+        S.sync()
+        t_ctx = time.perf_counter() - t0
+        S.close()
+        runs[key] = {"J": J, "forward_s": t_fwd, "rollout_s": t_adj, "graph_forward_s": t_ctx,
+                     "adjoint_over_forward": t_adj / t_fwd, "adjoint_over_graph_forward": t_adj / t_ctx,
+                     "phases_s": {"forward": ph[0], "recompute": ph[1], "reverse": ph[2]},
+                     "handle_device_bytes": dev_bytes, "device_bytes_in_use_delta": int(free0 - free1),
+                     "viscous_iterations": {"forward_all": its[0], "transposed": its[1]}}
+        grads[key] = g
+    names = ("theta0", "zeta", "l1", "l2", "phi")
+    err = {n: {"max": float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300)),
+               "l2": float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))}
+           for n, a, b in zip(names, grads["mixed"], grads["fp64"])}
+    return {"workload": f"{workload} {cfg.ni}x{cfg.nj}x{cfg.nk}", "K": K, "checkpoint_every": every,
+            "objective": "find_interface_positions_lower after K steps",
+            "gradient_rel_err_mixed_vs_fp64": err,
+            "J_rel_err_mixed_vs_fp64": abs(runs["mixed"]["J"] - runs["fp64"]["J"]) / max(abs(runs["fp64"]["J"]),
+                                                                                          1e-300),
+            "mixed": runs["mixed"], "fp64": runs["fp64"], "tolerances": {"sor": 1e-3, "adjoint": 1e-6}}
+
+
 def profile(args):
     """No timing: start-up pass, --warmup steps, then --steps steps (for ncu)."""
     from fmf import build as fbuild
@@ -360,6 +435,8 @@ def main():
                     help="checkpoint interval of the adjoint rollout (0: ceil(sqrt(K)))")
     ap.add_argument("--adjoint-workload", default="couette128",
                     help="workload of the adjoint-cost measurement")
+    ap.add_argument("--adjoint-mixed-steps", type=int, default=500,
+                    help="K of the mixed-forward adjoint on the 256x128x128 sessile drop (0: skip)")
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed", "adjoint"], help="--profile only")
     ap.add_argument("--profile", action="store_true",
                     help="no timing: start-up pass, --warmup steps, then --steps steps (for ncu launch lists)")
@@ -501,6 +578,9 @@ def main():
     adjoint = None
     if rank == 0 and args.adjoint_steps > 0:
         adjoint = adjoint_cost(args.adjoint_steps, stream, args.adjoint_every, args.adjoint_workload)
+    adjoint_m = None
+    if rank == 0 and args.adjoint_mixed_steps > 0:
+        adjoint_m = adjoint_mixed(args.adjoint_mixed_steps, stream)
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         v, dt, cores = cpu_baseline_sample(cfg, 1, 2)
@@ -516,7 +596,7 @@ def main():
                         "d2h_bytes_per_step": 12 * bytes_field, "steps": args.steps},
                 "gpu_launches": int(launches), "clocks": clk, "roofline": roofline, "step_roofline": step_roofline,
                 "cpu_baseline": cpu, "mixed": mixed, "mixed_horizon": horizon, "second_workload": second,
-                "adjoint": adjoint}
+                "adjoint": adjoint, "adjoint_mixed_forward": adjoint_m}
         print(json.dumps(line), flush=True)
     else:
         g.close()

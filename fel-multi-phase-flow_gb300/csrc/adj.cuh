@@ -201,12 +201,11 @@ void mthinc3_T(cudaStream_t s, const Grid& g, const double* pb, const double* pa
 // work: >= 63n doubles (per-line adjoints of the differences and velocities)
 void weno_T(cudaStream_t s, const Grid& g, double dxi, double dyi, double dzi, const double* u, const double* v,
             const double* w, const double* const* ladv, double* lu, double* lv, double* lw, double* work);
-// CSF force of one field: lf (3 arrays) -> lphi; work: >= 42n doubles
-// kap: the curvatures the forward pass recorded at the interior u, v, w points
-// (fused csf_force), or nullptr to recompute them (calrn x4 + calrkap)
+// CSF force of one field: lf (3 arrays) -> lphi; work: >= 42n doubles.  The
+// normals and curvature are formed again from phi, normals of gradients at the
+// rounding level taken as constants (the noise floor in adj_mom.cu)
 void csf_T(cudaStream_t s, const Grid& g, double dxi, double dyi, double dzi, double rhol, double rhog,
-           double sigma, const double* phi, const double* const* lf, double* lphi, double* work,
-           const double* kap = nullptr);
+           double sigma, const double* phi, const double* const* lf, double* lphi, double* work);
 
 // ---- viscous solve -------------------------------------------------------------
 struct SrcArgs {

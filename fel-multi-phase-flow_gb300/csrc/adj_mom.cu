@@ -200,8 +200,7 @@ void weno_T(cudaStream_t s, const Grid& g, double dxi, double dyi, double dzi, c
 
 // ---- CSF --------------------------------------------------------------------------
 void csf_T(cudaStream_t s, const Grid& g, double dxi, double dyi, double dzi, double rhol, double rhog,
-           double sigma, const double* phi, const double* const* lf, double* lphi, double* work,
-           const double* kap_rec) {
+           double sigma, const double* phi, const double* const* lf, double* lphi, double* work) {
   const Grid G = g;
   const long n = g.n;
   double* Gv = work;             // vertex gradient (3n)
@@ -212,16 +211,55 @@ void csf_T(cudaStream_t s, const Grid& g, double dxi, double dyi, double dzi, do
   double* lv = work + 24 * n;    // per normal family: adjoint of its 8-point mean (12n)
   double* lkap = work + 36 * n;  // adjoint of the curvature (3n)
   double* lgq = work + 39 * n;   // adjoint of the face gradient (3n)
-  static const int offs[4][3] = {{1, 1, 1}, {0, 0, 1}, {0, 1, 0}, {1, 0, 0}};
-  // forward recompute
+  // Noise floor.  The normals N(v) = v/(|v| + vs) take vs = 1e-30 |grad| (calrn.f),
+  // so where phi is flat to within rounding (the far tails of the interface
+  // profile, phi = 1 - a few ulps) they are unit vectors of rounding noise with
+  // O(1/dx) curvature.  The force there is ~0, but the exact linearisation of
+  // those normals is O(1) and as random as the noise: it differs between any two
+  // trajectories, and a central difference of any resolvable step does not see it
+  // (the force is even in the step there).  So normals whose mean gradient is
+  // below tau = 1e-6 |(dxi, dyi, dzi)| -- phi varying by under 1e-6 per cell, far
+  // below the interface band's >= 1e-2 per cell and far above rounding -- are
+  // taken as the constant 0: the curvature the transpose uses is formed from the
+  // others (equal to the step's wherever the normals are resolved), and those
+  // normals pass no adjoint to the vertex gradients.
+  const double tau = 1.0e-6 * std::sqrt(dxi * dxi + dyi * dyi + dzi * dzi);
+  const double vs = std::sqrt(dxi * dxi + dyi * dyi + dzi * dzi) * 1.0e-30;
+  // forward recompute: vertex gradients, normals (calrn.f:45-87 with the floor),
+  // curvature (calrkap.f) and face gradients
   fused::vertex_gradient(s, g, dxi, dyi, dzi, phi, Gv, Gv + n, Gv + 2 * n);
-  if (!kap_rec) {
-    for (int q = 0; q < 4; ++q)
-      op::calrn(s, g, dxi, dyi, dzi, offs[q][0], offs[q][1], offs[q][2], Gv, Gv + n, Gv + 2 * n, rn + 3 * n * q);
-    op::calrkap(s, g, dxi, dyi, dzi, rn, rn + 3 * n, rn + 6 * n, rn + 9 * n, kap);
-  } else {
-    kap = (double*)kap_rec;  // read only; valid where the force adjoints can be non-zero
-  }
+  range3(s, -2, g.ni + 3, -2, g.nj + 3, -2, g.nk + 3, [=] __device__(int i, int j, int k) {
+    const long X = 1, Y = G.sy, Z = G.sz;
+    const long c = G.at(i, j, k);
+#pragma unroll
+    for (int f = 0; f < 4; ++f) {
+      const int ip = f == 0 || f == 3, jp = f == 0 || f == 2, kp = f == 0 || f == 1;
+      double* out = rn + 3 * n * f + c;
+      if (i < -2 + ip || j < -2 + jp || k < -2 + kp) {  // calrn does not write o
+        out[0] = out[n] = out[2 * n] = 0.0;
+        continue;
+      }
+      const long Xf = ip ? X : 0, Yf = jp ? Y : 0, Zf = kp ? Z : 0;
+      const long b = c - Xf - Yf - Zf;
+      double r[3];
+#pragma unroll
+      for (int q3 = 0; q3 < 3; ++q3) {
+        const double* p = Gv + q3 * n + b;
+        r[q3] = f == 0 ? (p[0] + p[Xf] + p[Yf] + p[Xf + Yf] + p[Zf] + p[Xf + Zf] + p[Yf + Zf] + p[Xf + Yf + Zf]) * 0.125
+                       : (p[0] + p[Xf + Yf + Zf]) * 0.5;
+      }
+      const double s2 = r[0] * r[0] + r[1] * r[1] + r[2] * r[2];
+      if (s2 <= tau * tau) {
+        out[0] = out[n] = out[2 * n] = 0.0;
+        continue;
+      }
+      const double d = sqrt(s2) + vs;
+      out[0] = r[0] / d;
+      out[n] = r[1] / d;
+      out[2 * n] = r[2] / d;
+    }
+  });
+  op::calrkap(s, g, dxi, dyi, dzi, rn, rn + 3 * n, rn + 6 * n, rn + 9 * n, kap);
   op::cal_grad_prs(s, g, dxi, dyi, dzi, phi, gq, gq + n, gq + 2 * n);
   // calfst: f_c = -st kap_c g_c
   const double st = 2.0 * sigma / (rhol + rhog);
@@ -241,7 +279,6 @@ void csf_T(cudaStream_t s, const Grid& g, double dxi, double dyi, double dzi, do
   // offset is 0), written by calrn for o_i in [-2 + ip, ni+3] (same in j, k).
   // calrkap writes the u curvature where k >= -1, j >= -1, i <= ni+2, the v one where
   // k >= -1, j <= nj+2, i >= -1, the w one where k <= nk+2, j >= -1, i >= -1.
-  const double vs = std::sqrt(dxi * dxi + dyi * dyi + dzi * dzi) * 1.0e-30;
   // pass 1, per normal point o and family: the normal's adjoint gathered from the
   // curvatures that read it, then lv = (dN/dv)^T lrn
   range3(s, -2, g.ni + 3, -2, g.nj + 3, -2, g.nk + 3, [=] __device__(int i, int j, int k) {
@@ -302,6 +339,10 @@ void csf_T(cudaStream_t s, const Grid& g, double dxi, double dyi, double dzi, do
       // (division-free reciprocals where s2 is a normal number; subnormal and zero
       // s2 take the library functions)
       const double s2 = r[0] * r[0] + r[1] * r[1] + r[2] * r[2];
+      if (s2 <= tau * tau) {  // below the noise floor: a constant normal
+        out[0] = out[n] = out[2 * n] = 0.0;
+        continue;
+      }
       double ia, t = 0.0;
       if (s2 >= 0x1p-1000) {
         const double im = rsqrt_nr(s2);

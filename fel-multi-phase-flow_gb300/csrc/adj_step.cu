@@ -76,6 +76,13 @@ struct StageTimer {
 struct fmf_adj {
   fmf_params prm;
   Grid g;
+  // precision FMF_MIXED: the forward (and recomputed) steps run the mixed-precision
+  // kernels of the product step (FP32 WENO5, MTHINC Newton and fluxes, CSF, viscous
+  // corrections); the record keeps what they produced and the reverse is FP64
+  bool mixed = false;
+  fused::RefineBufs rb{};    // FP32 buffers of the mixed viscous solve
+  float2* wsplit = nullptr;  // split pairs of the velocity fields for the FP32 WENO5
+  long long bytes = 0;       // device bytes this handle allocated
   cudaStream_t s = nullptr;
   void* scr = nullptr;
   std::vector<void*> allocs;
@@ -96,7 +103,6 @@ struct fmf_adj {
   double* csfwork;  // forward CSF chain (drop-in): G(3n) rn(12n) kap(3n) g(3n) f(3n)
   int* band;        // MTHINC band-cell list and its length
   double* newton;   // per band-list entry: Newton offset, last Newton step
-  double *kap, *kapn;  // curvatures of phi and phin at the u, v, w points (fused CSF)
   // adjoints
   double* lS[NSTATE];  // adjoint of the step-start state (in/out of reverse_step)
   double *lgx[3], *lfl[3], *lrn, *ltheta, *lphn0, *lphn1, *lrho, *lrhon, *lrmu, *lrmun;
@@ -115,7 +121,7 @@ struct fmf_adj {
   struct Rec {
     double *gx1[3], *fl[3], *pb, *pass, *pc, *theta, *phn1f, *rho, *rhon, *rmu, *rmun;
     double *adv[3], *advo[3], *prs[3], *vis[3], *sfst[3], *sfstn[3], *sk, *E[3], *AB[6], *ustar[3], *un2[3];
-    double *wallc, *sums, *state, *newton, *kap, *kapn;
+    double *wallc, *sums, *state, *newton;
     int* band;
   };
   std::vector<Rec> recs;
@@ -129,11 +135,10 @@ struct fmf_adj {
   bool rec_warm = false;       // a step has run on this handle (scratch sized for capture)
   // The state continues from this handle's previous record_step (cont): that step's
   // advection of (u, v, w) is this step's of (uo, vo, wo), and its surface tension
-  // (and curvatures) of phin(1) this step's of phi(1); where they were written
+  // of phin(1) this step's of phi(1); where they were written
   bool cont = false;
   bool no_carry = false;  // FMF_STEP_CACHE=0 at creation: recompute both levels every step
   double *prev_adv[3] = {nullptr, nullptr, nullptr}, *prev_sfstn[3] = {nullptr, nullptr, nullptr};
-  double* prev_kapn = nullptr;
   // The reverse counterpart: the transposed advection and surface tension are linear
   // in the adjoint they receive, and step t's (uo, vo, wo) and phi(1) are step t-1's
   // (u, v, w) and phin(1).  reverse_step(t) leaves the adjoints of step t's advo and
@@ -155,8 +160,10 @@ double* dalloc(fmf_adj* a, long n) {
   }
   FMF_CUDA(cudaMemsetAsync(p, 0, sizeof(double) * n, a->s));
   a->allocs.push_back(p);
+  a->bytes += (long long)sizeof(double) * n;
   return (double*)p;
 }
+float* falloc(fmf_adj* a, long n) { return (float*)dalloc(a, (n + 1) / 2); }
 struct Scope {
   explicit Scope(void* set) { scratch_set_use(set); }
   ~Scope() { scratch_set_use(nullptr); }
@@ -203,13 +210,11 @@ void set_rec(fmf_adj* a, const fmf_adj::Rec& r) {
   a->sums = r.sums;
   a->band = r.band;
   a->newton = r.newton;
-  a->kap = r.kap;
-  a->kapn = r.kapn;
 }
 long nwall(const Grid& g) { return 4L * (g.nk + 6) * (g.ni + 6); }
 long nband_d(const Grid& g) { return ((long)(g.ni + 2) * (g.nj + 2) * (g.nk + 2) + 2) / 2 + 1; }
 long nband(const Grid& g) { return (long)(g.ni + 2) * (g.nj + 2) * (g.nk + 2); }
-long slot_doubles(const Grid& g) { return 72 * g.n + nwall(g) + 8 + 2 * nband(g) + nband_d(g) + 16; }
+long slot_doubles(const Grid& g) { return 66 * g.n + nwall(g) + 8 + 2 * nband(g) + nband_d(g) + 16; }
 // carve one slot out of a block of slot_doubles(g) doubles
 fmf_adj::Rec carve(const Grid& g, double* p) {
   const long n = g.n;
@@ -247,8 +252,6 @@ fmf_adj::Rec carve(const Grid& g, double* p) {
   r.wallc = take(nwall(g));
   r.sums = take(8);
   r.newton = take(2 * nband(g));
-  r.kap = take(3 * g.n);
-  r.kapn = take(3 * g.n);
   r.band = (int*)take(nband_d(g));
   return r;
 }
@@ -262,6 +265,7 @@ void grow_recs(fmf_adj* a, int want) {
     void* p = nullptr;
     if (!FMF_CUDA(cudaMalloc(&p, bytes))) break;
     FMF_CUDA(cudaMemsetAsync(p, 0, bytes, a->s));
+    a->bytes += (long long)bytes;
     a->rec_blocks.push_back(p);
     a->recs.push_back(carve(a->g, (double*)p));
   }
@@ -411,8 +415,8 @@ void run_part(fmf_adj* a, bool graphs, int id, const std::function<void()>& body
   long long per_launch = 0;
   const cudaGraphExec_t exec = adj::cached_graph(
       a->s, &a->pgraphs,
-      {(const void*)(intptr_t)(id + 1 + (a->cont ? 100 : 0)), a->gx1[0], a->adv[0], a->E[0], a->ustar[0], a->kap,
-       a->S[0], a->un[0], a->prev_adv[0], a->prev_sfstn[0], a->prev_kapn},
+      {(const void*)(intptr_t)(id + 1 + (a->cont ? 100 : 0)), a->gx1[0], a->adv[0], a->E[0], a->ustar[0],
+       a->S[0], a->un[0], a->prev_adv[0], a->prev_sfstn[0]},
       body, &per_launch);
   if (!exec) {
     body();
@@ -442,14 +446,13 @@ int record_step(fmf_adj* a, bool graphs) {
         dcopy(a, a->prev_adv[q], a->advo[q], n);
         dcopy(a, a->prev_sfstn[q], a->sfst[q], n);
       }
-      if (csf_fused) dcopy(a, a->prev_kapn, a->kap, 3 * n);
     }
     // :491-503
     fused::vertex_gradient(s, g, dxi, dyi, dzi, phi1, a->gx1[0], a->gx1[1], a->gx1[2]);
     {
       const long nb = (long)(g.ni + 2) * (g.nj + 2) * (g.nk + 2);
       fused::mthinc_fluxes(s, g, dxi, dyi, dzi, dt, P.bet_mthinc, phi1, a->gx1[0], a->gx1[1], a->gx1[2], S[SU],
-                           S[SV], S[SW], a->fl[0], a->fl[1], a->fl[2], a->band, a->band + nb, false, a->newton);
+                           S[SV], S[SW], a->fl[0], a->fl[1], a->fl[2], a->band, a->band + nb, a->mixed, a->newton);
     }
     op::solphi_mthinc2(s, g, dxi, dyi, dzi, dt, S[SU], S[SV], S[SW], a->fl[0], a->fl[1], a->fl[2], phi1, phn1);
     dcopy(a, phn1, a->pa, n);
@@ -472,9 +475,10 @@ int record_step(fmf_adj* a, bool graphs) {
     op::cal_arith_mean(s, g, phi0, P.rmul, P.rmug, a->rmu);
     op::cal_arith_mean(s, g, phn0, P.rmul, P.rmug, a->rmun);
     if (carry)
-      fused::weno5_one(s, g, dxi, dyi, dzi, S[SU], S[SV], S[SW], a->adv, false);
+      fused::weno5_one(s, g, dxi, dyi, dzi, S[SU], S[SV], S[SW], a->adv, a->mixed, a->wsplit);
     else
-      fused::weno5_both(s, g, dxi, dyi, dzi, S[SU], S[SV], S[SW], S[SUO], S[SVO], S[SWO], a->adv, a->advo, false);
+      fused::weno5_both(s, g, dxi, dyi, dzi, S[SU], S[SV], S[SW], S[SUO], S[SVO], S[SWO], a->adv, a->advo, a->mixed,
+                        a->wsplit);
     op::calphat(s, g, S[SP], S[SPO], a->phat);
     op::cal_grad_prs(s, g, dxi, dyi, dzi, a->phat, a->prs[0], a->prs[1], a->prs[2]);
     fused::explicit_viscous(s, g, dxi, dyi, dzi, S[SU], S[SV], S[SW], a->rmu, a->tau, a->vis, a->sk);
@@ -483,9 +487,9 @@ int record_step(fmf_adj* a, bool graphs) {
     if (csf_fused) {
       if (!carry)
         fused::csf_force(s, g, dxi, dyi, dzi, P.rhol, P.rhog, P.sigma, phi1, a->sfst[0], a->sfst[1], a->sfst[2],
-                         false, a->kap);
+                         a->mixed);
       fused::csf_force(s, g, dxi, dyi, dzi, P.rhol, P.rhog, P.sigma, phn1, a->sfstn[0], a->sfstn[1], a->sfstn[2],
-                       false, a->kapn);
+                       a->mixed);
     } else {
       if (!carry) csf_fwd(a, phi1, a->sfst);
       csf_fwd(a, phn1, a->sfstn);
@@ -497,16 +501,28 @@ int record_step(fmf_adj* a, bool graphs) {
     const double* visp[3] = {a->vis[0], a->vis[1], a->vis[2]};
     const double* fstp[3] = {a->sfst[0], a->sfst[1], a->sfst[2]};
     const double* fstnp[3] = {a->sfstn[0], a->sfstn[1], a->sfstn[2]};
+    // the FP64 factors A, B the reverse differentiates (the viscous solve's fixed
+    // point is un* = A visn(un*) + B in either precision)
     fused::src_visc_prep(s, g, dxi, dyi, dzi, dt, P.harmonic, P.grvb, P.grvp, S[SU], S[SV], S[SW], advp, advop, prsp,
                          visp, fstp, fstnp, a->rmun, a->rho, a->rhon, a->E, a->AB, a->l1, a->l2, phi1, P.dy, a->wallc);
-    for (int q = 0; q < 3; ++q) dcopy(a, S[SU + q], a->un[q], n);
+    if (a->mixed)
+      // the mixed solve's FP64 first-sweep residual, FP32 factors and wall/halo
+      // constants; un = u through zero corrections
+      fused::refine_prep(s, g, dxi, dyi, dzi, dt, P.harmonic, P.grvb, P.grvp, S[SU], S[SV], S[SW], advp, advop, prsp,
+                         visp, fstp, fstnp, a->rmun, a->rho, a->rhon, a->E, a->l1, a->l2, phi1, P.dy, P.uwall,
+                         a->wallc, a->rb);
+    else
+      for (int q = 0; q < 3; ++q) dcopy(a, S[SU + q], a->un[q], n);
   };
   run_part(a, graphs, 0, pre);
   // one outer iteration (12 colour-pair sweeps and their refreshes), replayed as a
   // CUDA graph per record slot
   auto iteration = [&]() {
-    fused::sor_iteration(s, g, dxi, dyi, dzi, P.harmonic, a->rmun, a->E, a->AB, P.uwall, a->wallc, a->un[0],
-                         a->un[1], a->un[2], a->sorpart, a->red + 4);
+    if (a->mixed)
+      fused::sor_iteration_refine(s, g, dxi, dyi, dzi, a->rb, a->sorpart, a->red + 4);
+    else
+      fused::sor_iteration(s, g, dxi, dyi, dzi, P.harmonic, a->rmun, a->E, a->AB, P.uwall, a->wallc, a->un[0],
+                           a->un[1], a->un[2], a->sorpart, a->red + 4);
   };
   long long per_launch = 0;
   const cudaGraphExec_t exec =
@@ -537,6 +553,7 @@ int record_step(fmf_adj* a, bool graphs) {
   a->sor_total += lp + 1;
   // the step after the viscous solve
   auto post = [&]() {
+    if (a->mixed) fused::refine_finish(s, g, S[SU], S[SV], S[SW], a->rb, a->un[0], a->un[1], a->un[2]);
     for (int q = 0; q < 3; ++q) dcopy(a, a->un[q], a->ustar[q], n);
     // :625-661
     fused::wall_halo(s, g, 7, P.uwall, a->wallc, a->un[0], a->un[1], a->un[2]);
@@ -568,7 +585,6 @@ int record_step(fmf_adj* a, bool graphs) {
     a->prev_adv[q] = a->adv[q];
     a->prev_sfstn[q] = a->sfstn[q];
   }
-  a->prev_kapn = a->kapn;
   a->cont = get_status() == 0 && !a->no_carry;
   return get_status();
 }
@@ -710,20 +726,16 @@ void reverse_step(fmf_adj* a, const double* st, bool defer) {
   double* const cadv[3] = {a->lcarry, a->lcarry + n, a->lcarry + 2 * n};
   double* const cfst[3] = {a->lcarry + 3 * n, a->lcarry + 4 * n, a->lcarry + 5 * n};
   {
-    // the curvatures recorded by the fused forward kernel where the grid tiles
-    const bool rec = fused::csf_supported(g);
     // the next step's carried adjoint is consumed before this step's replaces it
     if (a->carry_in) add3(s, n, cfst, a->lsfstn);
     if (defer) {
       for (int q = 0; q < 3; ++q) dcopy(a, a->lsfst[q], cfst[q], n);
     } else {
       const double* lf[3] = {a->lsfst[0], a->lsfst[1], a->lsfst[2]};
-      adj::csf_T(s, g, dxi, dyi, dzi, P.rhol, P.rhog, P.sigma, ST(SPHI1), lf, lS[SPHI1], a->work + 3 * n + 1024,
-                 rec ? a->kap : nullptr);
+      adj::csf_T(s, g, dxi, dyi, dzi, P.rhol, P.rhog, P.sigma, ST(SPHI1), lf, lS[SPHI1], a->work + 3 * n + 1024);
     }
     const double* lfn[3] = {a->lsfstn[0], a->lsfstn[1], a->lsfstn[2]};
-    adj::csf_T(s, g, dxi, dyi, dzi, P.rhol, P.rhog, P.sigma, a->phn1f, lfn, a->lphn1, a->work + 3 * n + 1024,
-               rec ? a->kapn : nullptr);
+    adj::csf_T(s, g, dxi, dyi, dzi, P.rhol, P.rhog, P.sigma, a->phn1f, lfn, a->lphn1, a->work + 3 * n + 1024);
   }
   check_stage(a, "csf");
   // :536-541 explicit viscous term, pressure gradient, advection
@@ -840,8 +852,10 @@ int fmf_adj_create(const fmf_params* prm, fmf_adj** out) {
   if (!prm || !out) return FMF_ERR_ARG;
   auto p2 = [](int v) { return v >= 4 && (v & (v - 1)) == 0; };
   if (!p2(prm->ni) || !p2(prm->nj) || !p2(prm->nk) || prm->ni < 16) return FMF_ERR_ARG;
+  if (prm->precision != FMF_FP64 && prm->precision != FMF_MIXED) return FMF_ERR_ARG;
   fmf_adj* a = new fmf_adj();
   a->prm = *prm;
+  a->mixed = prm->precision == FMF_MIXED;
   if (const char* e = std::getenv("FMF_STEP_CACHE")) a->no_carry = std::atoi(e) == 0;
   a->g = Grid(prm->ni, prm->nj, prm->nk);
   a->scr = scratch_set_create();
@@ -893,6 +907,20 @@ int fmf_adj_create(const fmf_params* prm, fmf_adj** out) {
   a->csfwork = dalloc(a, 21 * n);
   a->work = dalloc(a, 3 * n + 1024 + 63 * n);  // SOR adjoint, then CSF (42n) or WENO5 (63n) adjoints
   a->lcarry = dalloc(a, 6 * n);
+  if (a->mixed) {
+    fused::RefineBufs& rb = a->rb;
+    for (int q = 0; q < 3; ++q) {
+      rb.d[q] = falloc(a, n);
+      rb.a[q] = falloc(a, n);
+      rb.r[q] = falloc(a, n);
+      rb.e[q] = falloc(a, n);
+    }
+    rb.mu = falloc(a, n);
+    rb.gw = falloc(a, fused::refine_floats(a->g, 0));
+    rb.gx = falloc(a, fused::refine_floats(a->g, 1));
+    rb.gz = falloc(a, fused::refine_floats(a->g, 2));
+    a->wsplit = (float2*)dalloc(a, 6 * n);
+  }
   FMF_CUDA(cudaMallocHost(&a->host_norm, sizeof(double) * 2));
   grow_recs(a, 1);  // the record of the current step
   if (a->recs.empty()) {
@@ -1029,6 +1057,7 @@ int fmf_adj_rollout(fmf_adj* a, int K, int every, const double* const* state0, c
     void* p = nullptr;
     if (!FMF_CUDA(cudaMalloc(&p, sizeof(double) * NSTATE * n))) return take_status();
     a->ckpt.push_back((double*)p);
+    a->bytes += (long long)sizeof(double) * NSTATE * n;
   }
   grow_recs(a, every);
   const bool slots = (int)a->recs.size() >= every;
@@ -1036,6 +1065,7 @@ int fmf_adj_rollout(fmf_adj* a, int K, int every, const double* const* state0, c
     void* p = nullptr;
     if (!FMF_CUDA(cudaMalloc(&p, sizeof(double) * NSTATE * n))) return take_status();
     a->seg.push_back((double*)p);
+    a->bytes += (long long)sizeof(double) * NSTATE * n;
   }
   upload_inputs(a, state0, theta0, zeta, l1, l2);
   for (double* p : {a->gtheta0, a->gzeta, a->gl1, a->gl2}) zero(a, p, n);
@@ -1162,6 +1192,11 @@ int fmf_adj_iterations(fmf_adj* a, int* sor_total, int* adjoint_total) {
   if (sor_total) *sor_total = a->sor_total;
   if (adjoint_total) *adjoint_total = a->adj_total;
   return 0;
+}
+
+long long fmf_adj_device_bytes(fmf_adj* a) {
+  if (!a) return 0;
+  return a->bytes + (a->worker ? a->worker->bytes : 0);
 }
 
 int fmf_adj_phase_seconds(fmf_adj* a, double* seconds3) {

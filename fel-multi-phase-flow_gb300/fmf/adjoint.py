@@ -32,6 +32,8 @@ def _bind():
     L.fmf_adj_rollout.argtypes = [vp, ip, ip, vp, vp, vp, vp, vp, ctypes.POINTER(dp), vp, vp, vp, vp, vp]
     L.fmf_adj_iterations.argtypes = [vp, ctypes.POINTER(ip), ctypes.POINTER(ip)]
     L.fmf_adj_phase_seconds.argtypes = [vp, ctypes.POINTER(dp)]
+    L.fmf_adj_device_bytes.argtypes = [vp]
+    L.fmf_adj_device_bytes.restype = ctypes.c_longlong
     _bound = True
 
 
@@ -39,10 +41,12 @@ class Adjoint:
     """One GPU adjoint context for a configuration."""
 
     def __init__(self, cfg: fcfg.Config, sor_tol: float = 1e-3, sor_max: int = 21, adj_tol: float = 1e-12,
-                 adj_max: int = 200):
+                 adj_max: int = 200, precision: int = 0):
+        """precision: 0 (FMF_FP64) or 1 (FMF_MIXED: the forward and recomputed steps
+        run the mixed-precision step; the reverse stays FP64)."""
         _bind()
         self.cfg = cfg
-        self._prm = params(cfg)
+        self._prm = params(cfg, precision)
         h = ctypes.c_void_p()
         check(lib().fmf_adj_create(ctypes.byref(self._prm), ctypes.byref(h)), "fmf_adj_create")
         self.h = h
@@ -89,6 +93,10 @@ class Adjoint:
         out = (ctypes.c_double * 3)()
         check(lib().fmf_adj_phase_seconds(self.h, out), "phase_seconds")
         return tuple(out)
+
+    def device_bytes(self) -> int:
+        """Device bytes the handle (and its recomputing second handle) holds."""
+        return int(lib().fmf_adj_device_bytes(self.h))
 
 
 def rollout_function(adj: Adjoint, K: int, state0: np.ndarray, every: int = 0):

@@ -460,9 +460,11 @@ void datain_(int* ipara, int* ID, int* ni, int* nj, int* nk, int* nbub, int* nst
  * (find_interface_positions_lower.f90:15-32): J = -mean over k of the first
  * phi(i,1,k) > 0.5 > phi(i+1,1,k) crossing of phi slice 0 after K steps, taken from
  * a state to which the start-up boundary pass (main.f90:322-366) is applied first.
- * The forward pass is the FP64 step (as fmf_ctx_step with precision FMF_FP64) with
- * the viscous solve run to sor_tol; the reverse pass recomputes each step from
- * checkpoints taken every `every` steps (0: ceil(sqrt(K))). */
+ * The forward pass is the step of fmf_ctx_step in the handle's precision
+ * (prm->precision: FMF_FP64, or FMF_MIXED for the mixed-precision forward) with
+ * the viscous solve run to sor_tol; the reverse pass, in FP64, recomputes each step
+ * from checkpoints taken every `every` steps (0: ceil(sqrt(K))) and differentiates
+ * the FP64 step's operations at the states that forward produced. */
 typedef struct fmf_adj fmf_adj;
 int fmf_adj_create(const fmf_params* prm, fmf_adj** out);
 int fmf_adj_destroy(fmf_adj* adj);
@@ -480,6 +482,9 @@ int fmf_adj_rollout(fmf_adj* adj, int K, int every, const double* const* state0,
                     double* g_zeta, double* g_l1, double* g_l2, double* g_phi);
 /* viscous-solve iterations of the last call: forward (all recomputations) and transposed */
 int fmf_adj_iterations(fmf_adj* adj, int* sor_total, int* adjoint_total);
+/* device bytes the handle holds (work arrays, record slots, checkpoints, and those
+ * of the second handle that recomputes segments beside the reverse) */
+long long fmf_adj_device_bytes(fmf_adj* adj);
 /* wall-clock seconds of the last fmf_adj_rollout: forward pass, segment
  * recomputation, reverse steps */
 int fmf_adj_phase_seconds(fmf_adj* adj, double* seconds3);
