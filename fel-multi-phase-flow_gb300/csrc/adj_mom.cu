@@ -253,10 +253,11 @@ void csf_T(cudaStream_t s, const Grid& g, double dxi, double dyi, double dzi, do
         out[0] = out[n] = out[2 * n] = 0.0;
         continue;
       }
-      const double d = sqrt(s2) + vs;
-      out[0] = r[0] / d;
-      out[n] = r[1] / d;
-      out[2 * n] = r[2] / d;
+      // v/(|v| + vs) by Newton-Raphson reciprocals (s2 is a normal number here)
+      const double ia = recip_nr(s2 * rsqrt_nr(s2) + vs);
+      out[0] = r[0] * ia;
+      out[n] = r[1] * ia;
+      out[2 * n] = r[2] * ia;
     }
   });
   op::calrkap(s, g, dxi, dyi, dzi, rn, rn + 3 * n, rn + 6 * n, rn + 9 * n, kap);

@@ -155,3 +155,139 @@ def test_poisson_residual_roundoff(orc):
     lib.orc_solp_fft_tdma4_v(I(cfg.ni), I(cfg.nj), I(cfg.nk), D(rho), D(1 / cfg.dx), D(1 / cfg.dy), D(1 / cfg.dz),
                              P(div), P(dp), e, e0)
     assert e[0] / e0[0] < 1e-12
+
+
+def _grads_p2a(orc, cfg, phi):
+    I, D, P = orc.I, orc.D, orc.P
+    g = [np.zeros(cfg.shape) for _ in range(3)]
+    dya = np.full(cfg.nj + 6, 1.0 / cfg.dy)
+    orc.lib().orc_cal_grad_p2a(I(0), I(cfg.nj), I(cfg.ni), I(cfg.nj), I(cfg.nk), D(1 / cfg.dx), P(dya),
+                               D(1 / cfg.dz), P(phi), *[P(a) for a in g])
+    return g
+
+
+def test_mthinc_planar_interface_flux(orc):
+    """solphi_mthinc1.f:56-282 on a planar interface normal to x (phi a function of x
+    only) advected at a constant u > 0.  The vertex gradients have no y or z part,
+    so the unit normal is (s, 0, 0), s = +-1, and the 8 Gauss points of the
+    reconstruction H(t) = 1/(1 + exp(-2 beta t)), t = n.x + d, fall on 2 along x:
+    the offset d solves (H(s x1 + d) + H(s x2 + d))/2 = phi_cell with x1,2 = -+1/(2
+    sqrt 3) (found here by bisection, independently of the oracle's Newton
+    iteration), and the flux through the east face is c (H(s g1 + d) + H(s g2 + d))/2
+    with c = u dt/dx and g1,2 the 2-point Gauss nodes of [1/2 - c, 1/2].  Outside the
+    band (mean gradient <= eps dcellinv) it is c phi with phi snapped to 0/1 within
+    eps_trunc of them."""
+    cfg = C.Config("planar", 32, 8, 8, 1.0, 0.25, 0.25, dt=1e-3, steps=1)
+    sh = cfg.shape
+    bet, u0 = 2.0, 0.4
+    dt = 0.2 * cfg.dx / u0
+    c = u0 * dt / cfg.dx
+    xc = (np.arange(-2, cfg.ni + 4) - 0.5) * cfg.dx
+    prof = 0.5 * (1.0 + np.tanh((xc - 0.503) / (1.5 * cfg.dx)))
+    phi = np.broadcast_to(prof[None, None, :], sh).copy()
+    gx, gy, gz = _grads_p2a(orc, cfg, phi)
+    # rounding-level y, z parts (the reference sums differences in its own order)
+    assert np.abs(gy).max() <= 1e-12 * np.abs(gx).max() and np.abs(gz).max() <= 1e-12 * np.abs(gx).max()
+    u = np.full(sh, u0)
+    v = np.zeros(sh)
+    w = np.zeros(sh)
+    fl = [np.zeros(sh) for _ in range(3)]
+    I, D, P = orc.I, orc.D, orc.P
+    orc.lib().orc_solphi_mthinc1(I(cfg.ni), I(cfg.nj), I(cfg.nk), D(1 / cfg.dx), D(1 / cfg.dy), D(1 / cfg.dz),
+                                 D(dt), D(bet), P(phi), P(gx), P(gy), P(gz), P(u), P(v), P(w), *[P(a) for a in fl])
+    H = lambda t: 1.0 / (1.0 + np.exp(-2.0 * bet * t))
+    gp = 0.5 / np.sqrt(3.0)
+    dx, dy, dz = cfg.dx, cfg.dy, cfg.dz
+    dcellinv = 1.0 / np.sqrt((dx * dx + dy * dy + dz * dz) / 3.0)
+    eps = bet / (2.0 * np.cosh(-bet * 1.5) ** 2)
+    eps_trunc = 0.5 * (np.tanh(-bet * 2.5) + 1.0)
+    k0, j0 = 4 + 2, 3 + 2
+    nband = 0
+    for i in range(0, cfg.ni + 2):
+        ix = i + 2
+        # mean of the 8 vertex gradients around the cell (all equal in y and z)
+        rn = 0.5 * (gx[k0, j0, ix - 1] + gx[k0, j0, ix])
+        p0 = phi[k0, j0, ix]
+        got = fl[0][k0, j0, ix]
+        if abs(rn) <= eps * dcellinv:
+            ph = 0.0 if p0 <= eps_trunc else (1.0 if 1.0 - p0 <= eps_trunc else p0)
+            want = u0 * ph * dt / dx
+        else:
+            nband += 1
+            s = np.sign(rn)
+            lo, hi = -50.0, 50.0
+            for _ in range(200):
+                mid = 0.5 * (lo + hi)
+                if 0.5 * (H(-s * gp + mid) + H(s * gp + mid)) < p0:
+                    lo = mid
+                else:
+                    hi = mid
+            d = 0.5 * (lo + hi)
+            a, b = 0.5 - c, 0.5
+            g1, g2 = 0.5 * (a + b) - (b - a) * gp, 0.5 * (a + b) + (b - a) * gp
+            want = 0.5 * c * (H(s * g1 + d) + H(s * g2 + d))
+        assert abs(got - want) <= 1e-12 * max(abs(want), 1e-3), (i, got, want)
+    assert nband >= 4
+
+
+def test_gnbc_known_answers(orc):
+    """gnbc.f90:24-97: with the fluid at rest on resting walls the dynamic angle is
+    the static one, up to the law's regularisation (|u_cl| = sqrt(0 + 1e-12)); with
+    a uniform x-velocity U it is acos(cos theta0 -+ zeta sqrt(U^2 + 1e-12)/sigma),
+    the sign flipped for i <= ni/2, clamped to [-1, 1]."""
+    cfg = C.get("couette32", ni=16, nj=8, nk=8, theta_lo=60.0, theta_hi=110.0)
+    th0, ze, l1, l2 = C.wall_arrays(cfg)
+    sh = cfg.shape
+    sigma, zeta = 0.7, ze[3, 3, 3]
+    I, D, P = orc.I, orc.D, orc.P
+    ii = np.arange(-2, cfg.ni + 4)
+    for U in (0.0, 0.35, 30.0):  # at rest, a moderate speed, a speed that saturates the clamp
+        u = np.full(sh, U)
+        w = np.zeros(sh)
+        theta = np.zeros(sh)
+        orc.lib().orc_gnbc(orc.IA([-1] * 6), I(cfg.ni), I(cfg.nj), I(cfg.nk), P(u), P(w), D(0.0), P(th0),
+                           D(sigma), P(ze), P(theta))
+        for jw, sgn_wall in ((1, 1.0), (cfg.nj, 1.0)):
+            ucl = np.sqrt(U * U + 1e-12) * sgn_wall * np.where(ii <= cfg.ni // 2, -1.0, 1.0)
+            cos_t = np.clip(np.cos(np.radians(th0[:, jw + 2, :])) - zeta * ucl[None, :] / sigma, -1.0, 1.0)
+            want = np.degrees(np.arccos(cos_t))
+            np.testing.assert_allclose(theta[:, jw + 2, :], want, rtol=0, atol=1e-10)
+        if U == 0.0:
+            np.testing.assert_allclose(theta[:, 3, :], th0[:, 3, :], rtol=0, atol=1e-4)
+
+
+@pytest.mark.parametrize("N", [32, 64])
+def test_csf_curvature_of_a_sphere(orc, N):
+    """calrn.f + calrkap.f on a resolved sphere of radius R = 0.25 (phi = 1 inside,
+    a tanh profile of width 1.5 cells): the curvature at the u points, weighted by
+    the face gradient |phi(i+1) - phi(i)| that multiplies it in calfst.f, is the
+    sphere's -2/R (normals point into the phi = 1 fluid) to within the
+    discretisation error, and that error falls as the grid is refined."""
+    cfg = C.Config("sphere", N, N, N, 1.0, 1.0, 1.0, dt=1e-3, steps=1)
+    sh = cfg.shape
+    x = (np.arange(-2, N + 4) - 0.5) / N
+    Z, Y, X = np.meshgrid(x, x, x, indexing="ij")
+    R = 0.25
+    r = np.sqrt((X - 0.501) ** 2 + (Y - 0.497) ** 2 + (Z - 0.5) ** 2)
+    phi = 0.5 * (1.0 + np.tanh((R - r) / (1.5 / N)))
+    gx, gy, gz = _grads_p2a(orc, cfg, phi)
+    I, D, P = orc.I, orc.D, orc.P
+    dxi = float(N)
+    rns = []
+    for ip, jp, kp in ((1, 1, 1), (0, 0, 1), (0, 1, 0), (1, 0, 0)):
+        rn = np.zeros((3,) + sh)
+        orc.lib().orc_calrn(I(N), I(N), I(N), D(dxi), D(dxi), D(dxi), I(ip), I(jp), I(kp), P(gx), P(gy), P(gz), P(rn))
+        rns.append(rn)
+    kap = np.zeros((3,) + sh)
+    orc.lib().orc_calrkap(I(N), I(N), I(N), D(dxi), D(dxi), D(dxi), *[P(a) for a in rns], P(kap))
+    ku = C.interior(kap[0])
+    wgt = np.abs(C.interior(np.roll(phi, -1, axis=2) - phi))
+    mean = float((ku * wgt).sum() / wgt.sum())
+    err = abs(mean * R / 2.0 + 1.0)
+    test_csf_curvature_of_a_sphere.errs[N] = err
+    assert err <= 0.05, (N, mean, -2.0 / R)
+    if 32 in test_csf_curvature_of_a_sphere.errs and 64 in test_csf_curvature_of_a_sphere.errs:
+        assert test_csf_curvature_of_a_sphere.errs[64] < test_csf_curvature_of_a_sphere.errs[32]
+
+
+test_csf_curvature_of_a_sphere.errs = {}
