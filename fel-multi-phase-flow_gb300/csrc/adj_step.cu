@@ -612,29 +612,34 @@ void reverse_step(fmf_adj* a, const double* st, bool defer) {
   auto ST = [&](int f) { return st + (long)f * n; };
   double** lS = a->lS;
   a->stimer.mark(s, "begin");
-  // :686-697 rotation: u' = un, uo' = u, p' = pn, po' = p, phi' = phin' = phin
-  for (int q = 0; q < 3; ++q) {
-    dcopy(a, lS[SU + q], a->lun[q], n);
-    dcopy(a, lS[SUO + q], lS[SU + q], n);
-    zero(a, lS[SUO + q], n);
-  }
-  dcopy(a, lS[SP], a->lpn, n);
-  dcopy(a, lS[SPO], lS[SP], n);
-  zero(a, lS[SPO], n);
-  dcopy(a, lS[SPHI0], a->lphn0, n);
-  dcopy(a, lS[SPHI1], a->lphn1, n);
-  {  // phin' is the same phin: its adjoint adds
-    double *p0 = a->lphn0, *p1 = a->lphn1;
-    const double *q0 = lS[SPHIN0], *q1 = lS[SPHIN1];
+  // :686-697 rotation: u' = un, uo' = u, p' = pn, po' = p, phi' = phin' = phin (phin'
+  // is the same phin: its adjoint adds); one pass over the 12 adjoint fields
+  {
+    double *lu = lS[SU], *lv = lS[SV], *lw = lS[SW], *luo = lS[SUO], *lvo = lS[SVO], *lwo = lS[SWO];
+    double *lp = lS[SP], *lpo = lS[SPO], *lf0 = lS[SPHI0], *lf1 = lS[SPHI1], *ln0 = lS[SPHIN0],
+           *ln1 = lS[SPHIN1];
+    double *o0 = a->lun[0], *o1 = a->lun[1], *o2 = a->lun[2], *opn = a->lpn, *oh0 = a->lphn0, *oh1 = a->lphn1;
     flat(s, n, [=] __device__(long t) {
-      p0[t] += q0[t];
-      p1[t] += q1[t];
+      o0[t] = lu[t];
+      o1[t] = lv[t];
+      o2[t] = lw[t];
+      lu[t] = luo[t];
+      lv[t] = lvo[t];
+      lw[t] = lwo[t];
+      luo[t] = 0.0;
+      lvo[t] = 0.0;
+      lwo[t] = 0.0;
+      opn[t] = lp[t];
+      lp[t] = lpo[t];
+      lpo[t] = 0.0;
+      oh0[t] = lf0[t] + ln0[t];
+      oh1[t] = lf1[t] + ln1[t];
+      lf0[t] = 0.0;
+      lf1[t] = 0.0;
+      ln0[t] = 0.0;
+      ln1[t] = 0.0;
     });
   }
-  zero(a, lS[SPHI0], n);
-  zero(a, lS[SPHI1], n);
-  zero(a, lS[SPHIN0], n);
-  zero(a, lS[SPHIN1], n);
   // clear the intermediate adjoints
   zero(a, a->lblock, a->lblock_n);
   // :655-661 pn boundary conditions, wall/halo of un
