@@ -232,7 +232,10 @@ def mixed_case(cfg, st0, steps, warmup, stream, fp64_ms=None):
 def mixed_horizon(cfg, st0, steps, every, stream):
     """FP64 and mixed steps side by side from the same initial state over `steps`
     steps: the largest relative error of each field (interior, against the FP64
-    field's largest magnitude) at every `every`-th step."""
+    field's largest magnitude) at every `every`-th step, and there the next mixed
+    viscous solve re-formed in FP64 (fmf_ctx_check_sor: one FP64 outer iteration
+    from its result over the FP64 solve's first-iteration change, which the
+    reference's rule wants at or below 1e-3)."""
     import numpy as np
 
     from fmf import capi
@@ -242,6 +245,7 @@ def mixed_horizon(cfg, st0, steps, every, stream):
     mix = capi.Stepper(cfg, precision=capi.FMF_MIXED, stream=stream.cuda_stream)
     mix.upload(st0)
     worst = {k: 0.0 for k in FIELDS}
+    worst_rule = 0.0
     table = []
     done = 0
     t0 = time.perf_counter()
@@ -255,11 +259,19 @@ def mixed_horizon(cfg, st0, steps, every, stream):
         errs = {k: _rel(a[f], b[f], cfg) for k, f in FIELDS.items()}
         for k in FIELDS:
             worst[k] = max(worst[k], errs[k])
-        table.append({"step": done, "finite": finite, **{k: errs[k] for k in FIELDS}})
+        # the next mixed viscous solve against the FP64 stop rule (the state is left
+        # as it was)
+        chk = mix.check_sor()
+        worst_rule = max(worst_rule, chk["fp64_ratio"])
+        table.append({"step": done, "finite": finite, **{k: errs[k] for k in FIELDS},
+                      "viscous_solve_fp64_rule": {k: chk[k] for k in ("iterations", "own_ratio", "fp64_ratio",
+                                                                       "fp64_ratio_of_fp64_solve",
+                                                                       "rel_diff_vs_fp64_solve")}})
     ref.close()
     mix.close()
     return {"workload": f"{cfg.name} {cfg.ni}x{cfg.nj}x{cfg.nk}", "steps_compared": steps, "every": every,
-            "max_rel_err_vs_fp64": worst, "per_check": table, "seconds": time.perf_counter() - t0}
+            "max_rel_err_vs_fp64": worst, "viscous_solve_max_fp64_ratio": worst_rule, "sor_tol": 1e-3,
+            "per_check": table, "seconds": time.perf_counter() - t0}
 
 
 def adjoint_cost(K, stream, every, workload="couette128"):

@@ -15,9 +15,17 @@
 #include <utility>
 #include <vector>
 
+#include "../../include/fmf_capi.h"
 #include "fmf_common.cuh"
 
 namespace fmf {
+// The product time step's state and walls (step.cu), for the forward steps of a
+// rollout whose intermediates no reverse step reads.
+double* ctx_field(fmf_ctx* c, int f);
+void ctx_load_device(fmf_ctx* c, const double* const* state, const double* th, const double* ze,
+                     const double* l1, const double* l2);
+long ctx_sor_total(fmf_ctx* c);
+
 namespace adj {
 
 // Forward-mode number with N partial derivatives, for local Jacobians of small

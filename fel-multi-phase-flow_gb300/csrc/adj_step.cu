@@ -149,6 +149,13 @@ struct fmf_adj {
   bool carry_in = false;
   double* host_norm = nullptr;  // pinned
   fmf_adj* worker = nullptr;    // recomputes the next segment while this handle reverses one
+  // The product step (graph-replayed, pointer rotation, no record copies) for the
+  // forward steps whose intermediates no reverse step reads: the rollout's steps
+  // before its last segment and every step of fmf_adj_forward.  It runs the same
+  // kernels in the same order as record_step, so the states are the same bits.
+  // FMF_ADJ_RECORD_ALL set at creation: record_step for every step instead.
+  fmf_ctx* plain = nullptr;
+  bool record_all = false;
 };
 
 namespace {
@@ -165,8 +172,9 @@ double* dalloc(fmf_adj* a, long n) {
 }
 float* falloc(fmf_adj* a, long n) { return (float*)dalloc(a, (n + 1) / 2); }
 struct Scope {
-  explicit Scope(void* set) { scratch_set_use(set); }
-  ~Scope() { scratch_set_use(nullptr); }
+  explicit Scope(void* set) : prev(scratch_set_use(set)) {}
+  ~Scope() { scratch_set_use(prev); }
+  void* prev;
 };
 void zero(fmf_adj* a, double* p, long n) { FMF_CUDA(cudaMemsetAsync(p, 0, sizeof(double) * n, a->s)); }
 // dst[q] += src[q], q = 0..2, n points each
@@ -597,6 +605,49 @@ void load_state(fmf_adj* a, const double* src) {
   for (int f = 0; f < NSTATE; ++f) dcopy(a, src + (long)f * a->g.n, a->S[f], a->g.n);
 }
 
+// The product step for forward steps whose record no reverse step reads, created on
+// first use on this handle's stream (nullptr: record_step runs them).
+fmf_ctx* plain_ctx(fmf_adj* a) {
+  if (a->record_all || get_status()) return nullptr;
+  if (!a->plain) {
+    fmf_ctx* c = nullptr;
+    if (fmf_ctx_create(&a->prm, &c) != 0) return nullptr;
+    if (fmf_ctx_set_stream(c, a->s) != 0) {
+      fmf_ctx_destroy(c);
+      return nullptr;
+    }
+    a->plain = c;
+    a->bytes += fmf_ctx_device_bytes(c);
+  }
+  fmf_ctx_set_sor(a->plain, a->sor_tol, a->sor_max);
+  return a->plain;
+}
+
+// Steps [t, t1) of a forward pass from a->S on the product step, the state copied
+// back into a->S after them; with every > 0 the state at each multiple of `every`
+// is saved into its checkpoint first.
+void plain_steps(fmf_adj* a, fmf_ctx* c, int t, int t1, int every) {
+  const long n = a->g.n;
+  ctx_load_device(c, a->S, a->theta0, a->zeta, a->l1, a->l2);
+  while (t < t1 && !get_status()) {
+    int m = t1 - t;
+    if (every > 0) {
+      if (t % every == 0)
+        for (int f = 0; f < NSTATE; ++f) dcopy(a, ctx_field(c, f), a->ckpt[t / every] + (long)f * n, n);
+      m = std::min(m, every - t % every);
+    }
+    const int st = fmf_ctx_step(c, m);  // its iteration cap is no error here, as in record_step
+    if (st != FMF_OK && st != FMF_ERR_ITER_CAP) {
+      set_status(st);
+      break;
+    }
+    a->sor_total += (int)ctx_sor_total(c);
+    t += m;
+  }
+  for (int f = 0; f < NSTATE; ++f) dcopy(a, ctx_field(c, f), a->S[f], n);
+  a->cont = false;
+}
+
 // Reverse of one step.  On entry lS holds the adjoint of the state after the step;
 // on exit the adjoint of the state before it.  The record of the step (record_step
 // run from that start state) must be current; the step-start state itself is passed
@@ -862,6 +913,7 @@ int fmf_adj_create(const fmf_params* prm, fmf_adj** out) {
   a->prm = *prm;
   a->mixed = prm->precision == FMF_MIXED;
   if (const char* e = std::getenv("FMF_STEP_CACHE")) a->no_carry = std::atoi(e) == 0;
+  a->record_all = std::getenv("FMF_ADJ_RECORD_ALL") != nullptr;
   a->g = Grid(prm->ni, prm->nj, prm->nk);
   a->scr = scratch_set_create();
   // the highest stream priority: the reverse steps are the critical path when a
@@ -969,6 +1021,7 @@ int fmf_adj_destroy(fmf_adj* a) {
   if (!a) return 0;
   if (a->worker) fmf_adj_destroy(a->worker);
   if (a->s) cudaStreamSynchronize(a->s);
+  if (a->plain) fmf_ctx_destroy(a->plain);
   for (double* p : a->ckpt) cudaFree(p);
   for (double* p : a->seg) cudaFree(p);
   for (void* p : a->rec_blocks) cudaFree(p);
@@ -1000,7 +1053,10 @@ int fmf_adj_forward(fmf_adj* a, int K, const double* const* state0, const double
   upload_inputs(a, state0, theta0, zeta, l1, l2);
   init_bc_fwd(a);
   a->sor_total = 0;
-  for (int t = 0; t < K && !get_status(); ++t) record_step(a, true);
+  if (fmf_ctx* c = plain_ctx(a))
+    plain_steps(a, c, 0, K, 0);
+  else
+    for (int t = 0; t < K && !get_status(); ++t) record_step(a, true);
   *J = objective(a, a->S[SPHI0], nullptr);
   if (state_out)
     for (int f = 0; f < NSTATE; ++f)
@@ -1090,9 +1146,17 @@ int fmf_adj_rollout(fmf_adj* a, int K, int every, const double* const* state0, c
   };
   for (double& t : a->t_phase) t = 0.0;
   clk::time_point tp = clk::now();
-  // the last segment is recorded into its slots on the way (it is reversed first)
+  // the last segment is recorded into its slots on the way (it is reversed first);
+  // the steps before it (all steps where no slots fit) need no record
   const int tlast = (nck - 1) * every;
-  for (int t = 0; t < K && !get_status(); ++t) {
+  const int tplain = slots ? tlast : K;
+  int t = 0;
+  if (tplain > 0)
+    if (fmf_ctx* pc = plain_ctx(a)) {
+      plain_steps(a, pc, 0, tplain, every);
+      t = tplain;
+    }
+  for (; t < K && !get_status(); ++t) {
     if (t % every == 0) save_state(a, a->ckpt[t / every]);
     const bool kept = slots && t >= tlast;
     if (kept) {

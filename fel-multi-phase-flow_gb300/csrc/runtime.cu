@@ -68,7 +68,11 @@ void scratch_set_destroy(void* p) {
     if (sl.p) cudaFree(sl.p);
   delete s;
 }
-void scratch_set_use(void* p) { g_set = (ScratchSet*)p; }
+void* scratch_set_use(void* p) {
+  ScratchSet* old = g_set;
+  g_set = (ScratchSet*)p;
+  return old;
+}
 void* scratch(size_t bytes, int slot) {
   Slot& s = (g_set ? g_set : &g_global_set)->slots[slot];
   if (s.bytes >= bytes) return s.p;

@@ -23,7 +23,9 @@ int forget(const void* host);
 int reset_registry();
 void* scratch_set_create();
 void scratch_set_destroy(void* set);
-void scratch_set_use(void* set);  // nullptr: the library-wide set
+// Makes `set` this thread's scratch set (nullptr: the library-wide set) and returns
+// the one it replaces, so that nested scopes restore their caller's.
+void* scratch_set_use(void* set);
 
 // The array arguments of one drop-in call.  arr() returns the device copy of a
 // host array: in resident mode the registry mirror (uploaded when first seen),

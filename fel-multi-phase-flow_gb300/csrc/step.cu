@@ -128,6 +128,34 @@ void verify_upload(cudaStream_t s, long n, int nf, const double* const* src, dou
   count_launch(2);
 }
 
+// acc[0] += sum over interior points of |a - b|^2, acc[1] += |b - c|^2 (three
+// components each); one thread per (i, j) of a k-plane
+struct Vel3 {
+  const double* q[3];
+};
+__global__ void __launch_bounds__(256) k_diff2(Grid g, Vel3 a, Vel3 b, Vel3 c, double* acc) {
+  const int i = 1 + (int)(blockIdx.x * blockDim.x + threadIdx.x);
+  const int j = 1 + (int)(blockIdx.y * blockDim.y + threadIdx.y);
+  const int k = 1 + (int)blockIdx.z;
+  double s0 = 0.0, s1 = 0.0;
+  if (i <= g.ni && j <= g.nj) {
+    const long x = g.at(i, j, k);
+    for (int f = 0; f < 3; ++f) {
+      const double d0 = a.q[f][x] - b.q[f][x], d1 = b.q[f][x] - c.q[f][x];
+      s0 = fma(d0, d0, s0);
+      s1 = fma(d1, d1, s1);
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    s0 += __shfl_down_sync(0xffffffffu, s0, o);
+    s1 += __shfl_down_sync(0xffffffffu, s1, o);
+  }
+  if ((threadIdx.x & 31) == 0 && (s0 != 0.0 || s1 != 0.0)) {
+    atomicAdd(acc, s0);
+    atomicAdd(acc + 1, s1);
+  }
+}
+
 double* alloc(fmf_ctx* c, long n) {
   void* p = nullptr;
   if (!FMF_CUDA(cudaMalloc(&p, sizeof(double) * n))) {
@@ -287,8 +315,9 @@ int fmf_ctx_set_walls(fmf_ctx* c, const double* th, const double* ze, const doub
 
 // Routes fmf::scratch to the context's own scratch set while the context works.
 struct ScratchScope {
-  explicit ScratchScope(void* set) { scratch_set_use(set); }
-  ~ScratchScope() { scratch_set_use(nullptr); }
+  explicit ScratchScope(void* set) : prev(scratch_set_use(set)) {}
+  ~ScratchScope() { scratch_set_use(prev); }
+  void* prev;
 };
 
 static double* field_ptr(fmf_ctx* c, int f) {
@@ -668,6 +697,98 @@ int fmf_ctx_time_stage(fmf_ctx* c, int stage, int reps, float* ms) {
   return take_status();
 }
 
+// The next step's viscous solve against the FP64 stop rule (fmf_capi.h), on the
+// current state: the step up to its solve and the solve as fmf_ctx_step runs them
+// (eagerly), then FP64 outer iterations of solu_sor4 on copies of the velocity.
+int fmf_ctx_check_sor(fmf_ctx* c, double* out) {
+  if (!c || !out) return FMF_ERR_ARG;
+  ScratchScope scope(c->scr);
+  const fmf_params& P = c->prm;
+  const Grid& g = c->g;
+  cudaStream_t s = c->s;
+  const long n = g.n;
+  const double dxinv = 1.0 / P.dx, dyinv = 1.0 / P.dy, dzinv = 1.0 / P.dz;
+  double* q = (double*)scratch(sizeof(double) * (10 * n + 2), 15);
+  if (!q) return take_status();
+  // phi and phin (written by the step's first part: phin, and the contact-angle
+  // ghosts of phi(0)) are put back at the end; both advection levels and both
+  // surface-tension forces are computed here and again by the next step
+  double* keep_phi = q + 6 * n;
+  op::copy(s, 2 * n, c->phi, keep_phi);
+  op::copy(s, 2 * n, c->phin, keep_phi + 2 * n);
+  c->cont = false;
+  seg_pre(c);
+  seg_pre2(c);
+  auto rms = [&](double e) { return std::sqrt(e / (double)g.cells()) + 1.0e-99; };
+  auto read_err = [&]() {
+    FMF_CUDA(cudaStreamSynchronize(s));
+    const double e = c->host_err[0];
+    if (!std::isfinite(e)) set_status(FMF_ERR_NONFINITE);
+    return rms(e);
+  };
+  // the context's own solve (FP32 correction sweeps in the mixed precision)
+  double err0 = 0.0, err = 0.0;
+  int lp;
+  for (lp = 0; lp < c->sor_max && !get_status(); ++lp) {
+    seg_iter(c);
+    err = read_err();
+    if (lp == 0) err0 = err;
+    if (err / err0 <= c->sor_tol) break;
+  }
+  out[0] = (double)std::min(lp + 1, c->sor_max);
+  out[1] = err / err0;
+  if (c->mixed) {
+    fused::refine_finish(s, g, c->u, c->v, c->w, c->rb, c->un, c->vn, c->wn);
+    // the FP64 factors of the same system
+    const double* advp[3] = {c->adv[0], c->adv[1], c->adv[2]};
+    const double* advop[3] = {c->advo[0], c->advo[1], c->advo[2]};
+    const double* prsp[3] = {c->prs[0], c->prs[1], c->prs[2]};
+    const double* visp[3] = {c->vis[0], c->vis[1], c->vis[2]};
+    const double* fstp[3] = {c->sfst[0], c->sfst[1], c->sfst[2]};
+    const double* fstnp[3] = {c->sfstn[0], c->sfstn[1], c->sfstn[2]};
+    fused::src_visc_prep(s, g, dxinv, dyinv, dzinv, P.dt, P.harmonic, P.grvb, P.grvp, c->u, c->v, c->w, advp, advop,
+                         prsp, visp, fstp, fstnp, c->rmun, c->rho, c->rhon, c->edge, c->ab, c->l1, c->l2,
+                         c->phi + n, P.dy, c->wallc);
+  }
+  double *q64[3] = {q, q + n, q + 2 * n}, *qx[3] = {q + 3 * n, q + 4 * n, q + 5 * n};
+  double* acc = q + 10 * n;
+  const double* uvw[3] = {c->u, c->v, c->w};
+  const double* unp[3] = {c->un, c->vn, c->wn};
+  auto iter64 = [&](double* const* v) {
+    fused::sor_iteration(s, g, dxinv, dyinv, dzinv, P.harmonic, c->rmun, c->edge, c->ab, P.uwall, c->wallc, v[0],
+                         v[1], v[2], c->sorpart, c->red + 8);
+    FMF_CUDA(cudaMemcpyAsync(c->host_err, c->red + 8, sizeof(double), cudaMemcpyDeviceToHost, s));
+    return read_err();
+  };
+  auto copy3 = [&](const double* const* a, double* const* b) {
+    for (int f = 0; f < 3; ++f) op::copy(s, n, a[f], b[f]);
+  };
+  // the FP64 solve from un = u to the same rule
+  copy3(uvw, q64);
+  double e0 = 0.0;
+  for (int l = 0; l < c->sor_max && !get_status(); ++l) {
+    const double e = iter64(q64);
+    if (l == 0) e0 = e;
+    if (e / e0 <= c->sor_tol) break;
+  }
+  // one more FP64 iteration from each result
+  copy3(unp, qx);
+  out[2] = iter64(qx) / e0;
+  copy3(q64, qx);
+  out[3] = iter64(qx) / e0;
+  FMF_CUDA(cudaMemsetAsync(acc, 0, 2 * sizeof(double), s));
+  k_diff2<<<dim3((g.ni + 31) / 32, (g.nj + 7) / 8, g.nk), dim3(32, 8), 0, s>>>(
+      g, Vel3{{c->un, c->vn, c->wn}}, Vel3{{q64[0], q64[1], q64[2]}}, Vel3{{c->u, c->v, c->w}}, acc);
+  count_launch();
+  double h[2] = {0.0, 0.0};
+  FMF_CUDA(cudaMemcpyAsync(h, acc, sizeof(h), cudaMemcpyDeviceToHost, s));
+  op::copy(s, 2 * n, keep_phi, c->phi);
+  op::copy(s, 2 * n, keep_phi + 2 * n, c->phin);
+  FMF_CUDA(cudaStreamSynchronize(s));
+  out[4] = std::sqrt(h[0]) / (std::sqrt(h[1]) + 1.0e-300);
+  return take_status();
+}
+
 // One step from host buffers to host buffers (fmf_capi.h).  The step's first
 // segment reads u, v, w and phi only: those go up first, uo, vo, wo, p, po follow
 // on a second stream while it runs (phin is not an input: the step writes it
@@ -776,3 +897,26 @@ int fmf_ctx_set_sor(fmf_ctx* c, double tol, int max_iter) {
 }
 
 }  // extern "C"
+
+namespace fmf {
+// For the adjoint's forward pass: the context's current array of state field f
+// (fmf_ctx_upload's order) without ending the carry, and a state and walls loaded
+// from device arrays on the context's stream (the carry ends).
+double* ctx_field(fmf_ctx* c, int f) { return field_ptr(c, f); }
+void ctx_load_device(fmf_ctx* c, const double* const* state, const double* th, const double* ze,
+                     const double* l1, const double* l2) {
+  const size_t b = sizeof(double) * c->g.n;
+  c->cont = false;
+  for (int f = 0; f < 12; ++f)
+    FMF_CUDA(cudaMemcpyAsync(field_ptr(c, f), state[f], b, cudaMemcpyDeviceToDevice, c->s));
+  const double* src[4] = {th, ze, l1, l2};
+  double* dst[4] = {c->theta0, c->zeta, c->l1, c->l2};
+  for (int q = 0; q < 4; ++q) FMF_CUDA(cudaMemcpyAsync(dst[q], src[q], b, cudaMemcpyDeviceToDevice, c->s));
+}
+// the viscous-solve iteration counts of the last fmf_ctx_step call, summed
+long ctx_sor_total(fmf_ctx* c) {
+  long t = 0;
+  for (int k : c->sor_iters) t += k;
+  return t;
+}
+}  // namespace fmf

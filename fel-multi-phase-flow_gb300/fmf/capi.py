@@ -66,6 +66,8 @@ def load(path: str | None = None):
     L.fmf_ctx_step.restype = ip
     L.fmf_ctx_set_sor.argtypes = [vp, dp, ip]
     L.fmf_ctx_set_sor.restype = ip
+    L.fmf_ctx_check_sor.argtypes = [vp, ctypes.POINTER(ctypes.c_double)]
+    L.fmf_ctx_check_sor.restype = ip
     L.fmf_set_sor.argtypes = [dp, ip]
     L.fmf_set_sor.restype = ip
     L.fmf_last_solp_residual.argtypes = [ctypes.POINTER(dp), ctypes.POINTER(dp)]
@@ -170,6 +172,17 @@ class Stepper:
     def set_sor(self, tol: float = 1e-3, max_iter: int = 21):
         """The viscous solve's stop rule (default: the reference's)."""
         check(lib().fmf_ctx_set_sor(self.h, float(tol), int(max_iter)), "set_sor")
+
+    def check_sor(self) -> dict:
+        """The next step's viscous solve against the FP64 stop rule, on the current
+        state (not advanced): its outer iterations, the ratio its own rule stopped
+        on, the FP64 ratio of one more FP64 iteration from its result and from an
+        FP64 solve's result, and its result's distance from the FP64 solve's
+        relative to the step's velocity change (fmf_ctx_check_sor)."""
+        out = (ctypes.c_double * 5)()
+        check(lib().fmf_ctx_check_sor(self.h, out), "check_sor")
+        return {"iterations": int(out[0]), "own_ratio": out[1], "fp64_ratio": out[2],
+                "fp64_ratio_of_fp64_solve": out[3], "rel_diff_vs_fp64_solve": out[4]}
 
     def step_host(self, st_in: np.ndarray, st_out: np.ndarray):
         """One step from host state st_in to host state st_out (fmf_ctx_step_host;

@@ -417,6 +417,19 @@ long long fmf_ctx_device_bytes(fmf_ctx* ctx);
  * alone (the level a continuing step computes).  Measurement support; no
  * counterpart in the reference. */
 int fmf_ctx_time_stage(fmf_ctx* ctx, int stage, int reps, float* ms);
+/* The next step's viscous solve (srcs/solu_sor4.f) measured against the FP64 stop
+ * rule, on the current state, which is left as it was (the next step recomputes
+ * the carried advection and surface tension).  Runs the step up to the solve and the
+ * solve in the context's precision, then FP64 outer iterations on copies:
+ *   out[0] outer iterations of the context's solve;
+ *   out[1] err/err0 at its last iteration (in FMF_MIXED: of the FP32 correction);
+ *   out[2] the RMS change of one FP64 outer iteration from the solve's result over
+ *          the FP64 first-iteration change from un = u (the FP64 solve's err0);
+ *   out[3] the same from the result of an FP64 solve run to the same rule;
+ *   out[4] RMS(un - un_fp64) / RMS(un_fp64 - u) over the interior.
+ * In FMF_FP64, out[2] = out[3] and out[4] = 0.  Measurement support; no
+ * counterpart in the reference. */
+int fmf_ctx_check_sor(fmf_ctx* ctx, double* out);
 /* FMA throughput of this GPU in TFLOP/s (fp64=1: double, 0: float), from a
  * register-only kernel timed with CUDA events; the FP64 roofline denominator.
  * Measurement support; no counterpart in the reference. */
