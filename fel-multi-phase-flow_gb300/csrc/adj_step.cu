@@ -156,6 +156,13 @@ struct fmf_adj {
   // FMF_ADJ_RECORD_ALL set at creation: record_step for every step instead.
   fmf_ctx* plain = nullptr;
   bool record_all = false;
+  // The transposed viscous solve of reverse step t starts from that of step t+1:
+  // lam = lout + fb, fb the feedback term G^T lam of the previous solve (3n), whose
+  // norm fb_norm (0: none yet, a cold start) also scales the stop rule.
+  // FMF_ADJ_WARM=0 at creation: every solve starts cold.
+  double* fb = nullptr;
+  double fb_norm = 0.0;
+  bool warm = true;
 };
 
 namespace {
@@ -731,7 +738,8 @@ void reverse_step(fmf_adj* a, const double* st, bool defer) {
   const double* lout[3] = {a->lun[0], a->lun[1], a->lun[2]};
   a->adj_total += adj::sor_T(s, g, dxi, dyi, dzi, a->rmun, a->E, a->AB, P.uwall, a->wallc, a->ustar, a->snaps,
                              lout, a->lam, a->lAB, a->lrmun, a->lE, a->lwc, a->adj_tol, a->adj_max, a->work,
-                             a->host_norm, &a->graphs);
+                             a->host_norm, &a->graphs, a->fb, &a->fb_norm);
+  if (!a->warm) a->fb_norm = 0.0;
   check_stage(a, "sor");
   // :579-603 momentum factors, edge viscosities, slip coefficients
   {
@@ -914,6 +922,7 @@ int fmf_adj_create(const fmf_params* prm, fmf_adj** out) {
   a->mixed = prm->precision == FMF_MIXED;
   if (const char* e = std::getenv("FMF_STEP_CACHE")) a->no_carry = std::atoi(e) == 0;
   a->record_all = std::getenv("FMF_ADJ_RECORD_ALL") != nullptr;
+  if (const char* e = std::getenv("FMF_ADJ_WARM")) a->warm = std::atoi(e) != 0;
   a->g = Grid(prm->ni, prm->nj, prm->nk);
   a->scr = scratch_set_create();
   // the highest stream priority: the reverse steps are the critical path when a
@@ -963,6 +972,7 @@ int fmf_adj_create(const fmf_params* prm, fmf_adj** out) {
   a->sorpart = dalloc(a, fused::sor_parts(a->g));
   a->csfwork = dalloc(a, 21 * n);
   a->work = dalloc(a, 3 * n + 1024 + 63 * n);  // SOR adjoint, then CSF (42n) or WENO5 (63n) adjoints
+  a->fb = dalloc(a, 3 * n);
   a->lcarry = dalloc(a, 6 * n);
   if (a->mixed) {
     fused::RefineBufs& rb = a->rb;
@@ -1172,6 +1182,7 @@ int fmf_adj_rollout(fmf_adj* a, int K, int every, const double* const* state0, c
   a->t_phase[0] += lap(tp);
   // reverse, segment by segment
   a->carry_in = false;
+  a->fb_norm = 0.0;
   for (int c = nck - 1; c >= 0 && !get_status(); --c) {
     const int t0 = c * every, t1 = std::min(K, t0 + every);
     if (w) {

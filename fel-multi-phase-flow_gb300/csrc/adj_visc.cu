@@ -194,37 +194,65 @@ __global__ void k_copy3(long n, Arr3 a, double* __restrict__ b) {
     b[t + 2 * n] = a.a[2][t];
   }
 }
-// l += lout; part[block] = sum of (l - prev)^2
-__global__ void k_add_diff3(long n, Arr3 l, CArr3 o, const double* __restrict__ prev, double* part) {
-  __shared__ double sh[256];
-  double acc = 0.0;
+// l holds G^T l_old: fb = l (the feedback term), l += lout; part[block] = sum of
+// (l - prev)^2, part[512 + block] = sum of fb^2 (gridDim.x <= 512)
+__global__ void k_add_diff3(long n, Arr3 l, CArr3 o, const double* __restrict__ prev, double* part,
+                            double* __restrict__ fb) {
+  __shared__ double sh[2][256];
+  double acc = 0.0, acf = 0.0;
   for (long t = blockIdx.x * 256L + threadIdx.x; t < n; t += (long)gridDim.x * 256) {
     for (int c = 0; c < 3; ++c) {
-      const double v = l.a[c][t] + o.a[c][t];
+      const double f = l.a[c][t];
+      fb[t + c * n] = f;
+      acf += f * f;
+      const double v = f + o.a[c][t];
       l.a[c][t] = v;
       const double d = v - prev[t + c * n];
       acc += d * d;
     }
   }
-  sh[threadIdx.x] = acc;
+  sh[0][threadIdx.x] = acc;
+  sh[1][threadIdx.x] = acf;
   __syncthreads();
   for (int st = 128; st > 0; st >>= 1) {
-    if ((int)threadIdx.x < st) sh[threadIdx.x] += sh[threadIdx.x + st];
+    if ((int)threadIdx.x < st) {
+      sh[0][threadIdx.x] += sh[0][threadIdx.x + st];
+      sh[1][threadIdx.x] += sh[1][threadIdx.x + st];
+    }
     __syncthreads();
   }
-  if (threadIdx.x == 0) part[blockIdx.x] = sh[0];
+  if (threadIdx.x == 0) {
+    part[blockIdx.x] = sh[0][0];
+    part[512 + blockIdx.x] = sh[1][0];
+  }
 }
+// l = lout + fb (the warm start)
+__global__ void k_warm3(long n, Arr3 l, CArr3 o, const double* __restrict__ fb) {
+  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x)
+    for (int c = 0; c < 3; ++c) l.a[c][t] = o.a[c][t] + fb[t + c * n];
+}
+// out[0] = sum of part[0..n), out[1] = sum of part[512..512+n)
 __global__ void k_sum_small(const double* part, int n, double* out) {
-  __shared__ double sh[256];
-  double acc = 0.0;
-  for (int t = threadIdx.x; t < n; t += 256) acc += part[t];
-  sh[threadIdx.x] = acc;
+  __shared__ double sh[2][256];
+  double acc = 0.0, acf = 0.0;
+  for (int t = threadIdx.x; t < n; t += 256) {
+    acc += part[t];
+    acf += part[512 + t];
+  }
+  sh[0][threadIdx.x] = acc;
+  sh[1][threadIdx.x] = acf;
   __syncthreads();
   for (int st = 128; st > 0; st >>= 1) {
-    if ((int)threadIdx.x < st) sh[threadIdx.x] += sh[threadIdx.x + st];
+    if ((int)threadIdx.x < st) {
+      sh[0][threadIdx.x] += sh[0][threadIdx.x + st];
+      sh[1][threadIdx.x] += sh[1][threadIdx.x + st];
+    }
     __syncthreads();
   }
-  if (threadIdx.x == 0) out[0] = sh[0];
+  if (threadIdx.x == 0) {
+    out[0] = sh[0][0];
+    out[1] = sh[1][0];
+  }
 }
 }  // namespace
 
@@ -366,16 +394,26 @@ cudaGraphExec_t cached_graph(cudaStream_t s, GraphCache* cache, const std::vecto
 int sor_T(cudaStream_t s, const Grid& g, double dxi, double dyi, double dzi, const double* mu, double* const* E,
           double* const* AB, double uwall, const double* wallc, const double* const* ustar, const double* snaps,
           const double* const* lout, double* const* lam, double* const* lAB, double* lmu, double* const* lE,
-          double* lwc, double tol, int maxit, double* work, double* host_norm, GraphCache* cache) {
+          double* lwc, double tol, int maxit, double* work, double* host_norm, GraphCache* cache, double* fb,
+          double* fb_norm) {
   const VPa p = make_vpa(dxi, dyi, dzi);
   const long n = g.n;
   const CArr4 cf{{mu, E[0], E[1], E[2]}};
   const dim3 grd = pgrid(g), blk(32, 8);
-  double* prev = work;              // 3n
-  double* part = work + 3 * n;      // 512
-  double* nrm = work + 3 * n + 512; // 1 double
-  // l = lout
-  for (int c = 0; c < 3; ++c) FMF_CUDA(cudaMemcpyAsync(lam[c], lout[c], sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+  double* prev = work;               // 3n
+  double* part = work + 3 * n;       // 1024
+  double* nrm = work + 3 * n + 1024; // 2 doubles
+  const Arr3 L3{{lam[0], lam[1], lam[2]}};
+  const CArr3 O3{{lout[0], lout[1], lout[2]}};
+  // l = lout, or lout plus the previous solve's feedback term
+  const bool warm = *fb_norm > 0.0;
+  if (warm) {
+    k_warm3<<<608, 256, 0, s>>>(n, L3, O3, fb);
+    count_launch();
+  } else {
+    for (int c = 0; c < 3; ++c)
+      FMF_CUDA(cudaMemcpyAsync(lam[c], lout[c], sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+  }
   auto backward_cycle = [&](bool grad) {
     const Arr3 L{{lam[0], lam[1], lam[2]}};
     for (int comp = 2; comp >= 0; --comp)
@@ -398,14 +436,13 @@ int sor_T(cudaStream_t s, const Grid& g, double dxi, double dyi, double dzi, con
         count_launch();
       }
   };
-  // one iteration l <- lout + G^T l and |l_new - l_old|^2 into nrm: 51 kernels,
-  // replayed as a CUDA graph (one per set of buffers)
-  const Arr3 L3{{lam[0], lam[1], lam[2]}};
-  const CArr3 O3{{lout[0], lout[1], lout[2]}};
+  // one iteration l <- lout + G^T l, |l_new - l_old|^2 and |G^T l|^2 into nrm and
+  // the feedback term G^T l into fb: 51 kernels, replayed as a CUDA graph (one per
+  // set of buffers)
   auto iteration = [&]() {
     k_copy3<<<608, 256, 0, s>>>(n, L3, prev);
     backward_cycle(false);
-    k_add_diff3<<<512, 256, 0, s>>>(n, L3, O3, prev, part);
+    k_add_diff3<<<512, 256, 0, s>>>(n, L3, O3, prev, part, fb);
     k_sum_small<<<1, 256, 0, s>>>(part, 512, nrm);
     count_launch(3);
   };
@@ -413,10 +450,13 @@ int sor_T(cudaStream_t s, const Grid& g, double dxi, double dyi, double dzi, con
   cudaGraphExec_t exec =
       cache ? cached_graph(s, cache,
                            {lam[0], lam[1], lam[2], lout[0], lout[1], lout[2], mu, E[0], E[1], E[2], AB[0], AB[2],
-                            AB[4], wallc, ustar[0], ustar[2], work},
+                            AB[4], wallc, ustar[0], ustar[2], work, fb},
                            iteration, &per_launch)
             : nullptr;
-  double n0 = -1.0;
+  // The stop rule's scale: the change of the first iteration from l = lout (the
+  // size of the feedback term G^T lout); from a warm start, the previous solve's
+  // feedback norm, the same quantity one step later.
+  double n0 = warm ? *fb_norm : -1.0;
   int it = 0;
   for (it = 0; it < maxit; ++it) {
     if (exec) {
@@ -425,13 +465,14 @@ int sor_T(cudaStream_t s, const Grid& g, double dxi, double dyi, double dzi, con
     } else {
       iteration();
     }
-    FMF_CUDA(cudaMemcpyAsync(host_norm, nrm, sizeof(double), cudaMemcpyDeviceToHost, s));
+    FMF_CUDA(cudaMemcpyAsync(host_norm, nrm, 2 * sizeof(double), cudaMemcpyDeviceToHost, s));
     FMF_CUDA(cudaStreamSynchronize(s));
     const double d = std::sqrt(host_norm[0]);
-    if (!std::isfinite(d)) {
+    if (!std::isfinite(d) || !std::isfinite(host_norm[1])) {
       set_status(FMF_ERR_NONFINITE);
       break;
     }
+    *fb_norm = std::sqrt(host_norm[1]);
     if (n0 < 0.0) n0 = d;
     if (!(d > tol * (n0 + 1e-300))) break;
   }
