@@ -93,7 +93,27 @@ struct fmf_ctx {
   double sor_tol = 1.0e-3;  // solu_sor4.f:291 stop rule (fmf_ctx_set_sor)
   int sor_max = 21;         // solu_sor4.f:130 do lp=0,20
   int capped = 0;           // steps of the last call whose viscous solve hit sor_max
+  // The stop rule on the device, for graph-replayed steps: a CUDA graph whose WHILE
+  // conditional node runs outer iterations until k_sor_ctl ends it, so no step
+  // waits for the host.  Each solve's iteration count goes to sorlog, read back
+  // after the call's steps.  FMF_DEVICE_LOOP=0 at creation: the host applies the
+  // rule after every iteration.
+  bool dev_loop = true;
+  struct SorLoop* loop = nullptr;  // device
+  int* sorlog = nullptr;           // device, kSorLog entries
+  int pending = 0;                 // solves logged on the device since the last read
+  long long per_iter = 0;          // kernels of one outer iteration (the loop body)
 };
+
+// The device side of the stop rule (solu_sor4.f:130,291-293 as step_once applies
+// it on the host): err = sqrt(e / cells) + 1e-99 after each outer iteration,
+// err0 = that of the first, stop at err/err0 <= tol or after maxit iterations.
+struct SorLoop {
+  double tol, cells, err0, pad;
+  int maxit, it, nlog, flags;
+};
+constexpr int kSorLog = 4096;
+constexpr int kLogCapped = 1 << 20, kLogNonfinite = 1 << 21;
 
 namespace {
 // *same = 0 where any of the nf field pairs a[f], b[f] (n doubles each) differ in a bit
@@ -126,6 +146,45 @@ void verify_upload(cudaStream_t s, long n, int nf, const double* const* src, dou
   k_same<<<152 * 8, 256, 0, s>>>(n, nf, p, same);
   k_copy_unless<<<152 * 8, 256, 0, s>>>(n, nf, p, same);
   count_launch(2);
+}
+
+__global__ void k_sor_rule(SorLoop* L, double tol, int maxit, double cells) {
+  L->tol = tol;
+  L->maxit = maxit;
+  L->cells = cells;
+}
+__global__ void k_sor_log_reset(SorLoop* L) {
+  L->nlog = 0;
+  L->flags = 0;
+}
+__global__ void k_sor_begin(SorLoop* L) { L->it = 0; }
+// After one outer iteration (its residual sum at *esum): the rule, the log entry of
+// a finished solve (iterations, capped and non-finite bits), and the condition of
+// the WHILE node (0 ends the loop).  The iteration count is bounded by maxit, itself
+// clamped to the 100000 fmf_ctx_set_sor allows, whatever the loop state holds.
+__global__ void k_sor_ctl(cudaGraphConditionalHandle h, const double* esum, SorLoop* L, int* log) {
+  const double e = *esum;
+  const int mx = min(max(L->maxit, 1), 100000);
+  const int it = L->it + 1;
+  L->it = it;
+  int entry = it;
+  bool done = it >= mx || it < 1;
+  if (!isfinite(e)) {
+    entry |= kLogNonfinite;
+    done = true;
+  } else {
+    const double err = sqrt(e / L->cells) + 1.0e-99;
+    if (it == 1) L->err0 = err;
+    if (err / L->err0 <= L->tol)
+      done = true;
+    else if (done)
+      entry |= kLogCapped;
+  }
+  if (done) {
+    if (L->nlog < kSorLog) log[L->nlog] = entry;
+    L->nlog += 1;
+  }
+  cudaGraphSetConditional(h, done ? 0u : 1u);
 }
 
 // acc[0] += sum over interior points of |a - b|^2, acc[1] += |b - c|^2 (three
@@ -244,6 +303,14 @@ int fmf_ctx_create(const fmf_params* prm, fmf_ctx** out) {
     c->band = (int*)alloc(c, (nb + 1) / 2);
   }
   FMF_CUDA(cudaMallocHost(&c->host_err, sizeof(double) * 8));
+  if (const char* e = std::getenv("FMF_DEVICE_LOOP")) c->dev_loop = std::atoi(e) != 0;
+  c->loop = (SorLoop*)alloc(c, (sizeof(SorLoop) + 7) / 8);
+  c->sorlog = (int*)alloc(c, kSorLog / 2);
+  if (c->loop) {
+    k_sor_rule<<<1, 1, 0, c->s>>>(c->loop, c->sor_tol, c->sor_max, (double)c->g.cells());
+    k_sor_log_reset<<<1, 1, 0, c->s>>>(c->loop);
+    count_launch(2);
+  }
   if (get_status()) {
     fmf_ctx_destroy(c);
     return take_status();
@@ -449,6 +516,8 @@ static void seg_pre2(fmf_ctx* c) {
   const fmf_params& P = c->prm;
   const Grid& g = c->g;
   cudaStream_t s = c->s;
+  k_sor_begin<<<1, 1, 0, s>>>(c->loop);  // the device stop rule's iteration count
+  count_launch();
   const long n = g.n;
   const double dxinv = 1.0 / P.dx, dyinv = 1.0 / P.dy, dzinv = 1.0 / P.dz, dt = P.dt;
   double* phi1 = c->phi + n;
@@ -523,7 +592,8 @@ static void csf_one(fmf_ctx* c, const double* phi, double* const* f) {
   op::sum_fst(s, g, c->fst[0], c->fst[1], c->fst[2], f[0], f[1], f[2]);
 }
 
-static void seg_iter(fmf_ctx* c) {
+// one outer iteration of the viscous solve; its residual sum lands in red[8]
+static void iter_kernels(fmf_ctx* c) {
   const fmf_params& P = c->prm;
   const double dxinv = 1.0 / P.dx, dyinv = 1.0 / P.dy, dzinv = 1.0 / P.dz;
   if (c->mixed)
@@ -531,7 +601,87 @@ static void seg_iter(fmf_ctx* c) {
   else
     fused::sor_iteration(c->s, c->g, dxinv, dyinv, dzinv, P.harmonic, c->rmun, c->edge, c->ab, P.uwall, c->wallc,
                          c->un, c->vn, c->wn, c->sorpart, c->red + 8);
+}
+// the same, with the residual sum copied to the host (the host applies the rule)
+static void seg_iter(fmf_ctx* c) {
+  iter_kernels(c);
   FMF_CUDA(cudaMemcpyAsync(c->host_err, c->red + 8, sizeof(double), cudaMemcpyDeviceToHost, c->s));
+}
+
+// The whole viscous solve as one executable graph: a WHILE conditional node whose
+// body is one outer iteration followed by k_sor_ctl, which applies the stop rule
+// and ends the loop; captured once per set of rotating buffers.  nullptr (and the
+// host-side rule from then on) where the runtime builds no such graph.
+static cudaGraphExec_t solve_exec(fmf_ctx* c) {
+  GraphKey key{4, {c->u, c->v, c->w, c->uo, c->vo, c->wo, c->un, c->vn, c->wn, c->p, c->po, c->pn, c->phi, c->phin,
+                   c->adv[0], c->sfst[0]}};
+  auto it = c->cache.find(key);
+  if (it != c->cache.end()) return it->second.exec;
+  cudaGraph_t g = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  cudaGraphConditionalHandle h;
+  cudaGraphNodeParams cp{};
+  cudaGraphNode_t node;
+  bool ok = cudaGraphCreate(&g, 0) == cudaSuccess &&
+            cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault) == cudaSuccess;
+  if (ok) {
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = h;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    ok = cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &cp) == cudaSuccess;
+  }
+  if (ok) {
+    cudaGraph_t body = cp.conditional.phGraph_out[0];
+    const long long l0 = launches();
+    ok = cudaStreamBeginCaptureToGraph(c->s, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed) ==
+         cudaSuccess;
+    if (ok) {
+      iter_kernels(c);
+      k_sor_ctl<<<1, 1, 0, c->s>>>(h, c->red + 8, c->loop, c->sorlog);
+      count_launch();
+      cudaGraph_t captured = nullptr;
+      ok = cudaStreamEndCapture(c->s, &captured) == cudaSuccess;
+    }
+    const long long nl = launches() - l0;
+    count_launch((int)-nl);  // counted per iteration when the log is read
+    c->per_iter = nl;
+    if (ok) ok = cudaGraphInstantiate(&exec, g, 0) == cudaSuccess;
+  }
+  if (g) cudaGraphDestroy(g);
+  if (!ok) {
+    cudaGetLastError();  // the host-side rule runs the same iterations
+    if (exec) cudaGraphExecDestroy(exec);
+    c->dev_loop = false;
+    return nullptr;
+  }
+  c->cache.emplace(key, GraphEntry{exec, 0});
+  return exec;
+}
+
+// The solves the device logged since the last read: their iteration counts into
+// sor_iters, the capped ones into capped, a non-finite residual into the status,
+// and their kernels into the launch count.
+static void read_sor_log(fmf_ctx* c) {
+  if (!c->pending) return;
+  SorLoop h{};
+  std::vector<int> lg((size_t)std::min(c->pending, kSorLog));
+  FMF_CUDA(cudaMemcpyAsync(&h, c->loop, sizeof(SorLoop), cudaMemcpyDeviceToHost, c->s));
+  FMF_CUDA(cudaMemcpyAsync(lg.data(), c->sorlog, sizeof(int) * lg.size(), cudaMemcpyDeviceToHost, c->s));
+  k_sor_log_reset<<<1, 1, 0, c->s>>>(c->loop);
+  count_launch();
+  FMF_CUDA(cudaStreamSynchronize(c->s));
+  if (h.nlog != c->pending) set_status(FMF_ERR_CUDA);  // a solve that did not finish
+  long long its = 0;
+  for (int e : lg) {
+    const int n = e & (kLogCapped - 1);
+    c->sor_iters.push_back(n);
+    its += n;
+    if (e & kLogCapped) ++c->capped;
+    if (e & kLogNonfinite) set_status(FMF_ERR_NONFINITE);
+  }
+  count_launch((int)(its * c->per_iter));
+  c->pending = 0;
 }
 
 static void seg_post(fmf_ctx* c) {
@@ -600,22 +750,29 @@ static int step_once(fmf_ctx* c, const std::function<void()>& after_pre = {},
   if (after_pre) after_pre();
   if (before_pre2) before_pre2();
   run_segment(c, 3, seg_pre2);
-  double err = 0.0, err0 = 0.0;
-  int lp;
-  for (lp = 0; lp < c->sor_max; ++lp) {
-    run_segment(c, 1, seg_iter);
-    FMF_CUDA(cudaStreamSynchronize(c->s));
-    const double e = c->host_err[0];
-    if (!std::isfinite(e)) {
-      set_status(FMF_ERR_NONFINITE);
-      break;
+  const cudaGraphExec_t sx = c->graphs && c->dev_loop ? solve_exec(c) : nullptr;
+  if (sx) {
+    // the rule on the device; the counts are read after the call's steps
+    FMF_CUDA(cudaGraphLaunch(sx, c->s));
+    ++c->pending;
+  } else {
+    double err = 0.0, err0 = 0.0;
+    int lp;
+    for (lp = 0; lp < c->sor_max; ++lp) {
+      run_segment(c, 1, seg_iter);
+      FMF_CUDA(cudaStreamSynchronize(c->s));
+      const double e = c->host_err[0];
+      if (!std::isfinite(e)) {
+        set_status(FMF_ERR_NONFINITE);
+        break;
+      }
+      err = std::sqrt(e / (double)g.cells()) + 1.0e-99;
+      if (lp == 0) err0 = err;
+      if (err / err0 <= c->sor_tol) break;
     }
-    err = std::sqrt(e / (double)g.cells()) + 1.0e-99;
-    if (lp == 0) err0 = err;
-    if (err / err0 <= c->sor_tol) break;
+    c->sor_iters.push_back((lp < c->sor_max ? lp : c->sor_max - 1) + 1);
+    if (lp == c->sor_max) ++c->capped;  // reported after the call; the step carries on
   }
-  c->sor_iters.push_back((lp < c->sor_max ? lp : c->sor_max - 1) + 1);
-  if (lp == c->sor_max) ++c->capped;  // reported after the call; the step carries on
   run_segment(c, 2, seg_post);
   // :686-697 rotation by pointer
   double* t;
@@ -866,6 +1023,7 @@ int fmf_ctx_step_host(fmf_ctx* c, const double* const* in, double* const* out) {
   c->graphs = gr;
   c->warm = true;
   for (int f : {0, 1, 2, 6}) d2h(f, field_ptr(c, f), c->s);
+  read_sor_log(c);
   FMF_CUDA(cudaStreamSynchronize(c->s));
   FMF_CUDA(cudaStreamSynchronize(c->cs));
   const int st2 = st ? st : take_status();
@@ -884,7 +1042,9 @@ int fmf_ctx_step(fmf_ctx* c, int nsteps) {
     c->graphs = g;
     c->warm = true;
     if (st) break;
+    if (c->pending >= kSorLog) read_sor_log(c);
   }
+  read_sor_log(c);
   const int st = take_status();
   return st ? st : (c->capped ? FMF_ERR_ITER_CAP : FMF_OK);
 }
@@ -893,7 +1053,9 @@ int fmf_ctx_set_sor(fmf_ctx* c, double tol, int max_iter) {
   if (!c || !(tol > 0.0) || max_iter < 1 || max_iter > 100000) return FMF_ERR_ARG;
   c->sor_tol = tol;
   c->sor_max = max_iter;
-  return FMF_OK;
+  k_sor_rule<<<1, 1, 0, c->s>>>(c->loop, tol, max_iter, (double)c->g.cells());
+  count_launch();
+  return take_status();
 }
 
 }  // extern "C"

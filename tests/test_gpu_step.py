@@ -262,3 +262,39 @@ def test_split_pair_precision(fmf_lib):
     err = ctypes.c_double(-1.0)
     assert L.fmf_check_split_pair(1 << 22, ctypes.byref(err)) == 0
     assert 0.0 <= err.value <= 2.0 ** -47, err.value
+
+
+@pytest.mark.parametrize("precision", [capi.FMF_FP64, capi.FMF_MIXED])
+def test_device_stop_rule_matches_host(fmf_lib, monkeypatch, precision):
+    """Graph-replayed steps run the viscous solve's stop rule on the device (a WHILE
+    conditional node; no host round trip per outer iteration).  Against a context
+    whose host applies the rule after every iteration (FMF_DEVICE_LOOP=0 at
+    creation): the same state bit for bit and the same iteration counts after 12
+    steps in one call, then after a stop rule the solve cannot meet (the cap) and
+    back."""
+    cfg = C.get("couette256", ni=64, nj=32, nk=32)
+    g0 = capi.Stepper(cfg)
+    st0 = g0.initial_state()
+    g0.close()
+    res = {}
+    for mode in ("0", "1"):
+        monkeypatch.setenv("FMF_DEVICE_LOOP", mode)
+        S = capi.Stepper(cfg, precision=precision)
+        monkeypatch.delenv("FMF_DEVICE_LOOP")
+        try:
+            S.upload(st0)
+            S.step(12)
+            its = list(S.sor_iterations())
+            S.set_sor(1e-300, 5)
+            assert capi.lib().fmf_ctx_step(S.h, 3) == capi.FMF_ERR_ITER_CAP
+            its += list(S.sor_iterations())
+            S.set_sor(1e-3, 21)
+            S.step(2)
+            its += list(S.sor_iterations())
+            res[mode] = (S.get_state(), its)
+        finally:
+            S.close()
+    (a, ia), (b, ib) = res["0"], res["1"]
+    assert ia == ib
+    assert ia[12:15] == [5, 5, 5] and all(1 <= k < 21 for k in ia[:12] + ia[15:])
+    assert np.array_equal(a, b)
