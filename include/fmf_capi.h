@@ -384,7 +384,10 @@ int fmf_ctx_download(fmf_ctx* ctx, double* const* state);       /* device -> hos
 int fmf_ctx_init_bc(fmf_ctx* ctx);                  /* start-up boundary pass, main.f90:322-366 */
 /* nsteps full time steps; returns FMF_ERR_ITER_CAP (after all nsteps) where a
  * step's viscous solve ended without meeting its stop rule -- the step carries on
- * with the last iterate, as the reference's does -- unless a worse error occurred */
+ * with the last iterate, as the reference's does -- unless a worse error occurred.
+ * The stop rule runs on the device, so the steps are enqueued without waiting for
+ * the host; a residual that is not finite is reported (FMF_ERR_NONFINITE) after
+ * the call's steps. */
 int fmf_ctx_step(fmf_ctx* ctx, int nsteps);
 /* the viscous solve's stop rule err/err0 <= tol within max_iter outer iterations
  * (default: the reference's 1e-3 and 21, srcs/solu_sor4.f:130,291) */
@@ -482,7 +485,10 @@ typedef struct fmf_adj fmf_adj;
 int fmf_adj_create(const fmf_params* prm, fmf_adj** out);
 int fmf_adj_destroy(fmf_adj* adj);
 /* viscous-solve stop rule err/err0 <= sor_tol within sor_max iterations (the
- * reference: 1e-3, 21) and the transposed solve's relative tolerance / cap */
+ * reference: 1e-3, 21) and the transposed solve's tolerance / cap: a reverse step's
+ * transposed solve starts from the previous reverse step's solution and stops when
+ * its change falls to adj_tol times the size of its feedback term (the first
+ * reverse step of a rollout: of its first change) */
 int fmf_adj_set_solver(fmf_adj* adj, double sor_tol, int sor_max, double adj_tol, int adj_max);
 /* forward only: J after K steps; state_out (12 host fields) may be NULL */
 int fmf_adj_forward(fmf_adj* adj, int K, const double* const* state0, const double* theta0,
