@@ -206,9 +206,12 @@ void mthinc3_T(cudaStream_t s, const Grid& g, const double* pb, const double* pa
                double* lphin, double* lphi, double* scal);
 
 // ---- momentum ------------------------------------------------------------------
-// work: >= 63n doubles (per-line adjoints of the differences and velocities)
+// work: >= 63n doubles (per-line adjoints of the differences and velocities);
+// split (3n float2, or nullptr): the reverse of the forward's FP32 kernel, in FP32
+// on the split pairs of u, v, w written there first (a mixed-precision forward)
 void weno_T(cudaStream_t s, const Grid& g, double dxi, double dyi, double dzi, const double* u, const double* v,
-            const double* w, const double* const* ladv, double* lu, double* lv, double* lw, double* work);
+            const double* w, const double* const* ladv, double* lu, double* lv, double* lw, double* work,
+            float2* split = nullptr);
 // CSF force of one field: lf (3 arrays) -> lphi; work: >= 42n doubles.  The
 // normals and curvature are formed again from phi, normals of gradients at the
 // rounding level taken as constants (the noise floor in adj_mom.cu)

@@ -103,6 +103,111 @@ __device__ double wline_T(const double* __restrict__ q, long c, long S, double v
   return lr * (pos ? A.R : -A.R) * (1.0 / 6.0);
 }
 
+// FP32 counterpart for handles whose forward runs the mixed-precision step
+// (fused_weno.cu's k_weno2_f32): the same reverse sweep in float on the split pairs
+// (hi, lo) of the velocity fields, a difference formed as (hi1 - hi0) + (lo1 -
+// lo0), with the forward kernel's scaling -- the five differences divided by their
+// largest magnitude s and the additive 1e-80/486 taken as 1e-80/486/s^8, clamped
+// to [2^-126, 2^100] (the same PTX approximations of log2 and exp2).  R is
+// homogeneous of degree 1 in the differences, so dR/de is the scaled quotient's
+// derivative and R = s R'.  A stencil flatter than 2^-100 gives R = 0, as forward.
+__device__ __forceinline__ float lg2_apx(float x) {
+  float r;
+  asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+__device__ __forceinline__ float ex2_apx(float x) {
+  float r;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+struct WalkF {
+  float t1a, t2a, t1b, t2b, t1c, t2c, s1, s2, s3, x, y, z, X, Y, Z, D1, d2, D3, iD, R, sc;
+};
+// false where the stencil is flat (R = 0 and no derivative)
+__device__ __forceinline__ bool walk_fwd_f32(const float2* __restrict__ q, long c, long st, WalkF& W) {
+  const float2* p = q + c - 3 * st;
+  const float2 q0 = __ldg(p), q1 = __ldg(p + st), q2 = __ldg(p + 2 * st), q3 = __ldg(p + 3 * st),
+               q4 = __ldg(p + 4 * st), q5 = __ldg(p + 5 * st);
+  float a5 = (q1.x - q0.x) + (q1.y - q0.y), a3 = (q2.x - q1.x) + (q2.y - q1.y), a1 = (q3.x - q2.x) + (q3.y - q2.y),
+        b1 = (q4.x - q3.x) + (q4.y - q3.y), b3 = (q5.x - q4.x) + (q5.y - q4.y);
+  const float s = fmaxf(fmaxf(fmaxf(fabsf(a5), fabsf(a3)), fmaxf(fabsf(a1), fabsf(b1))), fabsf(b3));
+  W.R = 0.0f;
+  W.sc = s;
+  if (s < 0x1p-100f) return false;
+  const float is = __fdividef(1.0f, s);
+  a5 *= is;
+  a3 *= is;
+  a1 *= is;
+  b1 *= is;
+  b3 *= is;
+  constexpr float c13 = 13.0f / 3.0f;
+  W.t1a = fmaf(a3, -2.0f, a5 + a1);
+  W.t2a = fmaf(a3, -4.0f, fmaf(a1, 3.0f, a5));
+  W.t1b = fmaf(a1, -2.0f, a3 + b1);
+  W.t2b = a3 - b1;
+  W.t1c = fmaf(b1, -2.0f, a1 + b3);
+  W.t2c = fmaf(b1, -4.0f, fmaf(a1, 3.0f, b3));
+  W.s1 = fmaf(W.t1a * c13, W.t1a, W.t2a * W.t2a);
+  W.s2 = fmaf(W.t1b * c13, W.t1b, W.t2b * W.t2b);
+  W.s3 = fmaf(W.t1c * c13, W.t1c, W.t2c * W.t2c);
+  // log2(1e-80 / 486) = -274.679
+  const float eps = ex2_apx(fminf(fmaxf(-274.679f - 8.0f * lg2_apx(s), -126.0f), 100.0f));
+  W.x = W.s2 * W.s3;
+  W.y = W.s1 * W.s3;
+  W.z = W.s1 * W.s2;
+  W.X = W.x * W.x;
+  W.Y = fmaf(W.y, W.y, eps);
+  W.Z = W.z * W.z;
+  W.D1 = fmaf(a1, 11.0f / 6.0f, fmaf(a3, -7.0f / 6.0f, a5 * (1.0f / 3.0f)));
+  W.d2 = fmaf(b1, 2.0f, fmaf(a1, 5.0f, -a3));
+  W.D3 = fmaf(b1, 2.5f, fmaf(b3, -0.5f, a1));
+  const float num = fmaf(W.Z, W.D3, fmaf(W.Y, W.d2, W.X * W.D1));
+  W.iD = __fdividef(1.0f, fmaf(W.X, 1.0f / 6.0f, fmaf(W.Z, 0.5f, W.Y)));
+  W.R = num * W.iD;
+  return true;
+}
+__device__ __forceinline__ void walk_rev_f32(const WalkF& W, float g4, float* la) {
+  constexpr float c13 = 13.0f / 3.0f;
+  const float lD1 = g4 * W.X, ld2 = g4 * W.Y, lD3 = g4 * W.Z;
+  const float lX = g4 * fmaf(W.R, -1.0f / 6.0f, W.D1), lY = g4 * (W.d2 - W.R), lZ = g4 * fmaf(W.R, -0.5f, W.D3);
+  const float lx = W.x * lX, ly = W.y * lY, lz = W.z * lZ;
+  const float S1 = fmaf(ly, W.s3, lz * W.s2), S2 = fmaf(lx, W.s3, lz * W.s1), S3 = fmaf(lx, W.s2, ly * W.s1);
+  const float lt1a = (W.t1a * c13) * S1, lt2a = W.t2a * S1;
+  const float lt1b = (W.t1b * c13) * S2, lt2b = W.t2b * S2;
+  const float lt1c = (W.t1c * c13) * S3, lt2c = W.t2c * S3;
+  la[0] = fmaf(lD1, 1.0f / 12.0f, lt1a + lt2a);
+  la[1] = fmaf(lD1, -7.0f / 24.0f, fmaf(ld2, -0.25f, fmaf(lt1a, -2.0f, fmaf(lt2a, -4.0f, lt1b + lt2b))));
+  la[2] = fmaf(lD1, 11.0f / 24.0f,
+               fmaf(ld2, 1.25f, fmaf(lD3, 0.25f, fmaf(lt2a, 3.0f, fmaf(lt1b, -2.0f, fmaf(lt2c, 3.0f, lt1a + lt1c))))));
+  la[3] = fmaf(ld2, 0.5f, fmaf(lD3, 0.625f, fmaf(lt1c, -2.0f, fmaf(lt2c, -4.0f, lt1b - lt2b))));
+  la[4] = fmaf(lD3, -0.125f, lt1c + lt2c);
+}
+// the adjoint of  out += |vsum| di/24 R  (vsum = 4 vel) given lr = lout di: lD =
+// the adjoints of the six differences; returns the adjoint of vel
+__device__ float wline_T_f32(const float2* __restrict__ q, long c, long S, float vsum, float lr, float* lD) {
+  for (int m = 0; m < 6; ++m) lD[m] = 0.0f;
+  if (lr == 0.0f) return 0.0f;
+  WalkF A;
+  if (vsum == 0.0f) {
+    WalkF B;
+    walk_fwd_f32(q, c, S, A);
+    walk_fwd_f32(q, c, -S, B);
+    return lr * (A.R * A.sc - B.R * B.sc) * (1.0f / 12.0f);
+  }
+  const bool pos = vsum > 0.0f;
+  if (!walk_fwd_f32(q, c, pos ? S : -S, A)) return 0.0f;
+  float la[5];
+  walk_rev_f32(A, (lr * fabsf(vsum)) * (1.0f / 6.0f) * A.iD, la);
+  lD[0] = pos ? la[0] : 0.0f;
+  lD[1] = pos ? la[1] : -la[4];
+  lD[2] = pos ? la[2] : -la[3];
+  lD[3] = pos ? la[3] : -la[2];
+  lD[4] = pos ? la[4] : -la[1];
+  lD[5] = pos ? 0.0f : -la[0];
+  return lr * (pos ? A.R : -A.R) * A.sc * (1.0f / 6.0f);
+}
+
 // Offsets (relative to the cell) of the four velocity points that form the
 // advecting velocity of line (component q, direction d); the line reads component d.
 __constant__ signed char kVelOff[9][4][3] = {
@@ -141,6 +246,33 @@ __global__ void __launch_bounds__(256) k_weno_T1(Grid g, double dxi, double dyi,
 #pragma unroll
   for (int m = 0; m < 6; ++m) D[(long)(line * 6 + m) * n + c] = lD[m];
   V[(long)line * n + c] = lvel;
+}
+// Pass 1 in FP32 (handles with a mixed-precision forward): sp holds the split pairs
+// of u, v, w (3 n float2); the advecting velocity is formed as the forward FP32
+// kernel forms it (vsum = (a + b) + (c + d) of the pairs' high parts).  The
+// adjoints are stored as double for pass 2.
+__global__ void __launch_bounds__(256) k_weno_T1_f32(Grid g, float dxi, float dyi, float dzi,
+                                                     const float2* __restrict__ sp, const double* __restrict__ la0,
+                                                     const double* __restrict__ la1, const double* __restrict__ la2,
+                                                     double* __restrict__ D, double* __restrict__ V) {
+  const int i = 1 + (int)(blockIdx.x * blockDim.x + threadIdx.x);
+  const int j = 1 + (int)(blockIdx.y * blockDim.y + threadIdx.y);
+  const int line = (int)blockIdx.z % 9, k = 1 + (int)blockIdx.z / 9;
+  if (i > g.ni || j > g.nj) return;
+  const int q = line / 3, d = line % 3;
+  const long X = 1, Y = g.sy, Z = g.sz, n = g.n;
+  const long c = g.at(i, j, k);
+  const float2* vq = sp + (long)d * n;
+  const signed char(*o)[3] = kVelOff[line];
+  auto h = [&](int t) { return __ldg(&vq[c + o[t][0] * X + o[t][1] * Y + o[t][2] * Z].x); };
+  const float vsum = (h(0) + h(1)) + (h(2) + h(3));
+  const float L = (float)(q == 0 ? la0 : (q == 1 ? la1 : la2))[c];
+  float lD[6];
+  const float lvel = wline_T_f32(sp + (long)q * n, c, d == 0 ? X : (d == 1 ? Y : Z), vsum,
+                                 L * (d == 0 ? dxi : (d == 1 ? dyi : dzi)), lD);
+#pragma unroll
+  for (int m = 0; m < 6; ++m) D[(long)(line * 6 + m) * n + c] = (double)lD[m];
+  V[(long)line * n + c] = (double)lvel;
 }
 // Pass 2: every point gathers what the lines of the cells around it owe it.
 __global__ void __launch_bounds__(256) k_weno_T2(Grid g, const double* __restrict__ D,
@@ -189,11 +321,17 @@ __global__ void __launch_bounds__(256) k_weno_T2(Grid g, const double* __restric
 }  // namespace
 
 void weno_T(cudaStream_t s, const Grid& g, double dxi, double dyi, double dzi, const double* u, const double* v,
-            const double* w, const double* const* ladv, double* lu, double* lv, double* lw, double* work) {
+            const double* w, const double* const* ladv, double* lu, double* lv, double* lw, double* work,
+            float2* split) {
   double* D = work;
   double* V = work + 54 * g.n;
-  k_weno_T1<<<dim3((g.ni + 31) / 32, (g.nj + 7) / 8, 9 * g.nk), dim3(32, 8), 0, s>>>(g, dxi, dyi, dzi, u, v, w, ladv[0],
-                                                                               ladv[1], ladv[2], D, V);
+  const dim3 grd((g.ni + 31) / 32, (g.nj + 7) / 8, 9 * g.nk), blk(32, 8);
+  if (split) {
+    fused::split3(s, g, u, v, w, split);
+    k_weno_T1_f32<<<grd, blk, 0, s>>>(g, (float)dxi, (float)dyi, (float)dzi, split, ladv[0], ladv[1], ladv[2], D, V);
+  } else {
+    k_weno_T1<<<grd, blk, 0, s>>>(g, dxi, dyi, dzi, u, v, w, ladv[0], ladv[1], ladv[2], D, V);
+  }
   k_weno_T2<<<dim3((g.ni + 6 + 31) / 32, (g.nj + 6 + 7) / 8, g.nk + 6), dim3(32, 8), 0, s>>>(g, D, V, lu, lv, lw);
   count_launch(2);
 }

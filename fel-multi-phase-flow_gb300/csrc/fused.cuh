@@ -17,6 +17,9 @@ void weno5_both(cudaStream_t s, const Grid& g, double dxi, double dyi, double dz
 // cal_advu_weno5 of (u, v, w) alone into adv (fp32: split pairs of 3 fields, 3 n float2)
 void weno5_one(cudaStream_t s, const Grid& g, double dxi, double dyi, double dzi, const double* u, const double* v,
                const double* w, double* const* adv, bool fp32 = false, float2* split = nullptr);
+// the split pairs (hi, lo) of three fields (field f at out[f n ..]; hi + lo = q to
+// about 2^-48), as the FP32 WENO5 reads them
+void split3(cudaStream_t s, const Grid& g, const double* a, const double* b, const double* c, float2* out);
 // both levels, the second (uo, vo, wo into advo) skipped on the device where *keep != 0
 void weno5_keep(cudaStream_t s, const Grid& g, double dxi, double dyi, double dzi, const double* u, const double* v,
                 const double* w, const double* uo, const double* vo, const double* wo, double* const* adv,

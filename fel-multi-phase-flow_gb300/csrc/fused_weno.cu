@@ -298,6 +298,11 @@ void weno5_one(cudaStream_t s, const Grid& g, double dxi, double dyi, double dzi
                const double* w, double* const* adv, bool fp32, float2* split) {
   weno5_levels(s, g, 1, dxi, dyi, dzi, u, v, w, nullptr, nullptr, nullptr, adv, nullptr, fp32, split);
 }
+void split3(cudaStream_t s, const Grid& g, const double* a, const double* b, const double* c, float2* out) {
+  const SplitSrc src{{a, b, c, nullptr, nullptr, nullptr}};
+  k_split<3><<<152 * 8, 256, 0, s>>>(g.n, src, out, nullptr);
+  count_launch();
+}
 
 void weno5_keep(cudaStream_t s, const Grid& g, double dxi, double dyi, double dzi, const double* u, const double* v,
                 const double* w, const double* uo, const double* vo, const double* wo, double* const* adv,
