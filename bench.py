@@ -292,8 +292,9 @@ def adjoint_cost(K, stream, every, workload="couette128"):
     every = every if every > 0 else int(math.ceil(math.sqrt(K)))
     A = Adjoint(cfg, sor_tol=1e-3, sor_max=21, adj_tol=1e-6, adj_max=200)
     A.forward(2, st0, walls)
-    # allocates the checkpoint and record slots (two segments: the recomputing worker's too)
-    A.rollout(min(K, 2 * every), st0, walls, every=every)
+    # allocates the checkpoint and record slots; three segments capture the graphs of
+    # both slot banks of both handles (the recomputing worker's too)
+    A.rollout(min(K, 3 * every), st0, walls, every=every)
     t0 = time.perf_counter()
     J = A.forward(K, st0, walls)
     t_fwd = time.perf_counter() - t0
@@ -357,7 +358,9 @@ def adjoint_mixed(K, stream, workload="droplet256", every=0):
         free0, _ = torch.cuda.mem_get_info()
         A = Adjoint(cfg, sor_tol=1e-3, sor_max=21, adj_tol=1e-6, adj_max=200, precision=prec)
         A.forward(2, st0, walls)
-        A.rollout(min(K, 2 * every), st0, walls, every=every)  # allocates checkpoints and record slots
+        # allocates checkpoints and record slots; three segments capture the graphs of
+        # both slot banks of both handles
+        A.rollout(min(K, 3 * every), st0, walls, every=every)
         t0 = time.perf_counter()
         J = A.forward(K, st0, walls)
         t_fwd = time.perf_counter() - t0
@@ -407,11 +410,13 @@ def profile(args):
     from fmf import capi
     from fmf import config as C
     fbuild.build()
-    if args.precision == "adjoint":
-        # --steps K of the adjoint rollout on the workload (for ncu launch lists)
+    if args.precision in ("adjoint", "adjoint_mixed"):
+        # --steps K of the adjoint rollout on the workload (for ncu launch lists);
+        # adjoint_mixed: with the mixed-precision forward
         from fmf.adjoint import Adjoint
         cfg = C.get(args.workload)
-        A = Adjoint(cfg, sor_tol=1e-3, sor_max=21, adj_tol=1e-6, adj_max=200)
+        A = Adjoint(cfg, sor_tol=1e-3, sor_max=21, adj_tol=1e-6, adj_max=200,
+                    precision=capi.FMF_MIXED if args.precision == "adjoint_mixed" else capi.FMF_FP64)
         st0 = C.raw_state(cfg)
         walls = C.wall_arrays(cfg)
         A.rollout(max(1, args.warmup), st0, walls)
@@ -451,7 +456,7 @@ def main():
                     help="workload of the adjoint-cost measurement")
     ap.add_argument("--adjoint-mixed-steps", type=int, default=500,
                     help="K of the mixed-forward adjoint on the 256x128x128 sessile drop (0: skip)")
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed", "adjoint"], help="--profile only")
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed", "adjoint", "adjoint_mixed"], help="--profile only")
     ap.add_argument("--profile", action="store_true",
                     help="no timing: start-up pass, --warmup steps, then --steps steps (for ncu launch lists)")
     args = ap.parse_args()
