@@ -292,9 +292,8 @@ def adjoint_cost(K, stream, every, workload="couette128"):
     every = every if every > 0 else int(math.ceil(math.sqrt(K)))
     A = Adjoint(cfg, sor_tol=1e-3, sor_max=21, adj_tol=1e-6, adj_max=200)
     A.forward(2, st0, walls)
-    # allocates the checkpoint and record slots; three segments capture the graphs of
-    # both slot banks of both handles (the recomputing worker's too)
-    A.rollout(min(K, 3 * every), st0, walls, every=every)
+    # allocates the checkpoint and record slots (two segments: the recomputing worker's too)
+    A.rollout(min(K, 2 * every), st0, walls, every=every)
     t0 = time.perf_counter()
     J = A.forward(K, st0, walls)
     t_fwd = time.perf_counter() - t0
@@ -358,9 +357,7 @@ def adjoint_mixed(K, stream, workload="droplet256", every=0):
         free0, _ = torch.cuda.mem_get_info()
         A = Adjoint(cfg, sor_tol=1e-3, sor_max=21, adj_tol=1e-6, adj_max=200, precision=prec)
         A.forward(2, st0, walls)
-        # allocates checkpoints and record slots; three segments capture the graphs of
-        # both slot banks of both handles
-        A.rollout(min(K, 3 * every), st0, walls, every=every)
+        A.rollout(min(K, 2 * every), st0, walls, every=every)  # allocates checkpoints and record slots
         t0 = time.perf_counter()
         J = A.forward(K, st0, walls)
         t_fwd = time.perf_counter() - t0

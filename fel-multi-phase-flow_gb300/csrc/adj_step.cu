@@ -1180,7 +1180,7 @@ int fmf_adj_rollout(fmf_adj* a, int K, int every, const double* const* state0, c
       set_rec(a, a->recs[t - tlast]);
       save_state(a, a->recs[t - tlast].state);
     }
-    record_step(a, true);
+    record_step(a, !kept);
   }
   if (get_status()) return take_status();
   *J = objective(a, a->S[SPHI0], a->lS[SPHI0]);
@@ -1206,7 +1206,7 @@ int fmf_adj_rollout(fmf_adj* a, int K, int every, const double* const* state0, c
           for (int t = u0; t < u0 + every && !get_status(); ++t) {
             set_rec(w, w->recs[t - u0]);
             save_state(w, w->recs[t - u0].state);
-            record_step(w, true);
+            record_step(w, false);
           }
           FMF_CUDA(cudaStreamSynchronize(w->s));
           t_rec = std::chrono::duration<double>(clk::now() - ta).count();
