@@ -756,6 +756,7 @@ static int step_once(fmf_ctx* c, const std::function<void()>& after_pre = {},
     FMF_CUDA(cudaGraphLaunch(sx, c->s));
     ++c->pending;
   } else {
+    read_sor_log(c);  // counts of earlier device-side solves first, in step order
     double err = 0.0, err0 = 0.0;
     int lp;
     for (lp = 0; lp < c->sor_max; ++lp) {
