@@ -488,10 +488,7 @@ int record_step(fmf_adj* a, bool graphs) {
     op::bnd_contact_angle(s, g, phi0, a->theta, P.dx, P.dy, P.dz);
     op::bnd_periodic(s, g, phn0);
     // :526-541
-    op::cal_arith_mean(s, g, phi0, P.rhol, P.rhog, a->rho);
-    op::cal_arith_mean(s, g, phn0, P.rhol, P.rhog, a->rhon);
-    op::cal_arith_mean(s, g, phi0, P.rmul, P.rmug, a->rmu);
-    op::cal_arith_mean(s, g, phn0, P.rmul, P.rmug, a->rmun);
+    op::mixture_means(s, g, phi0, phn0, P.rhol, P.rhog, P.rmul, P.rmug, a->rho, a->rhon, a->rmu, a->rmun);
     if (carry)
       fused::weno5_one(s, g, dxi, dyi, dzi, S[SU], S[SV], S[SW], a->adv, a->mixed, a->wsplit);
     else

@@ -43,6 +43,10 @@ void cal_advu_weno5(cudaStream_t s, const Grid& g, double dxinv, double dyinv, d
 
 // C6 glue
 void cal_arith_mean(cudaStream_t s, const Grid& g, const double* phi, double ql, double qg, double* q);
+// rho, rhon, rmu, rmun = cal_arith_mean of (rhol, rhog) and (rmul, rmug) over phi0
+// and phin0 in one pass (main.f90:526-529; the same values as the four calls)
+void mixture_means(cudaStream_t s, const Grid& g, const double* phi0, const double* phin0, double rhol, double rhog,
+                   double rmul, double rmug, double* rho, double* rhon, double* rmu, double* rmun);
 void cal_harm_mean(cudaStream_t s, const Grid& g, const double* phi, double ql, double qg, double* q);
 void calphat(cudaStream_t s, const Grid& g, const double* p, const double* po, double* phat);
 void cal_grad_prs(cudaStream_t s, const Grid& g, double dxinv, double dyinv, double dzinv,

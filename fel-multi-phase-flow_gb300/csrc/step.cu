@@ -2,9 +2,11 @@
 //
 // fmf_ctx_step runs main.f90:473-697 on the GPU with every field resident in HBM:
 // the state rotation of :686-697 is a pointer rotation, the MPI calls of the
-// reference are absent (one rank), and the only host<->device traffic per step is
-// the 8-byte SOR residual read once per outer iteration (the stop test of
-// solu_sor4.f:291-293).
+// reference are absent (one rank), and the stop test of solu_sor4.f:291-293 runs
+// on the device in graph-replayed steps (a conditional loop in the solve's graph;
+// the iteration counts are read once per call), so a call enqueues its steps
+// without host round trips (an eager step reads the 8-byte residual after each
+// outer iteration instead).
 //
 // Work carried from one step to the next.  After the rotation (:686-697), (uo, vo,
 // wo) of step n+1 is bit for bit (u, v, w) of step n (nothing writes u, v, w after
@@ -504,10 +506,7 @@ static void seg_pre(fmf_ctx* c) {
   op::bnd_contact_angle(s, g, phi0, c->theta, P.dx, P.dy, P.dz);  // gnbc result unchanged since :498
   op::bnd_periodic(s, g, phin0);
   // :526-529
-  op::cal_arith_mean(s, g, phi0, P.rhol, P.rhog, c->rho);
-  op::cal_arith_mean(s, g, phin0, P.rhol, P.rhog, c->rhon);
-  op::cal_arith_mean(s, g, phi0, P.rmul, P.rmug, c->rmu);
-  op::cal_arith_mean(s, g, phin0, P.rmul, P.rmug, c->rmun);
+  op::mixture_means(s, g, phi0, phin0, P.rhol, P.rhog, P.rmul, P.rmug, c->rho, c->rhon, c->rmu, c->rmun);
 }
 
 // The rest of the step before the viscous solve: reads uo, vo, wo, p, po (the
