@@ -69,7 +69,8 @@ struct fmf_ctx {
   cudaStream_t s = nullptr;
   bool own_stream = false;
   cudaStream_t cs = nullptr;                        // copies overlapping the step (fmf_ctx_step_host)
-  cudaEvent_t ev_in = nullptr, ev_in2 = nullptr, ev_pre = nullptr;  // inputs up (two parts); first segment done
+  // inputs up (u, v, w; phi(0); the rest); first part of the step done
+  cudaEvent_t ev_in = nullptr, ev_in_phi0 = nullptr, ev_in2 = nullptr, ev_pre = nullptr;
   std::vector<void*> allocs;
   long long bytes = 0;
   // state
@@ -346,6 +347,7 @@ int fmf_ctx_destroy(fmf_ctx* c) {
     cudaStreamDestroy(c->cs);
   }
   if (c->ev_in) cudaEventDestroy(c->ev_in);
+  if (c->ev_in_phi0) cudaEventDestroy(c->ev_in_phi0);
   if (c->ev_in2) cudaEventDestroy(c->ev_in2);
   if (c->ev_pre) cudaEventDestroy(c->ev_pre);
   for (auto& e : c->cache) cudaGraphExecDestroy(e.second.exec);
@@ -477,18 +479,25 @@ int fmf_ctx_init_bc(fmf_ctx* c) {
 // on the host between steps.
 static void csf_one(fmf_ctx* c, const double* phi, double* const* f);
 
-static void seg_pre(fmf_ctx* c) {
+// The first part in three pieces, so that the host-buffer step can start it while
+// inputs are still on their way: (a) reads phi(1) only, (b) u, v, w as well, (c)
+// phi(0) as well.  phin is final after (b).
+static void seg_pre_a(fmf_ctx* c) {
+  const fmf_params& P = c->prm;
+  const double dxinv = 1.0 / P.dx, dyinv = 1.0 / P.dy, dzinv = 1.0 / P.dz;
+  // :491 (the vertex gradients of phi(1))
+  fused::vertex_gradient(c->s, c->g, dxinv, dyinv, dzinv, c->phi + c->g.n, c->phix, c->phiy, c->phiz);
+}
+static void seg_pre_b(fmf_ctx* c) {
   const fmf_params& P = c->prm;
   const Grid& g = c->g;
   cudaStream_t s = c->s;
   const long n = g.n;
   const double dxinv = 1.0 / P.dx, dyinv = 1.0 / P.dy, dzinv = 1.0 / P.dz, dt = P.dt;
-  double* phi0 = c->phi;
   double* phi1 = c->phi + n;
   double* phin0 = c->phin;
   double* phin1 = c->phin + n;
   // :491-503 transport
-  fused::vertex_gradient(s, g, dxinv, dyinv, dzinv, phi1, c->phix, c->phiy, c->phiz);
   {
     const long nb = (long)(g.ni + 2) * (g.nj + 2) * (g.nk + 2);
     fused::mthinc_fluxes(s, g, dxinv, dyinv, dzinv, dt, P.bet_mthinc, phi1, c->phix, c->phiy, c->phiz, c->u, c->v,
@@ -500,13 +509,24 @@ static void seg_pre(fmf_ctx* c) {
   op::gnbc(s, g, c->u, c->w, P.uwall, c->theta0, P.sigma, c->zeta, c->theta);
   op::bnd_contact_angle(s, g, phin1, c->theta, P.dx, P.dy, P.dz);
   op::bnd_periodic(s, g, phin1);
-  // :509-517
+  // :509-517 on phin (the contact-angle pass on phi(0) of :515, independent of
+  // these, follows in part c)
   op::summation(s, g, phin0, phin1);
   op::bnd_neumann(s, g, phin0);
-  op::bnd_contact_angle(s, g, phi0, c->theta, P.dx, P.dy, P.dz);  // gnbc result unchanged since :498
   op::bnd_periodic(s, g, phin0);
+}
+static void seg_pre_c(fmf_ctx* c) {
+  const fmf_params& P = c->prm;
+  const Grid& g = c->g;
+  double* phi0 = c->phi;
+  op::bnd_contact_angle(c->s, g, phi0, c->theta, P.dx, P.dy, P.dz);  // gnbc result unchanged since :498
   // :526-529
-  op::mixture_means(s, g, phi0, phin0, P.rhol, P.rhog, P.rmul, P.rmug, c->rho, c->rhon, c->rmu, c->rmun);
+  op::mixture_means(c->s, g, phi0, c->phin, P.rhol, P.rhog, P.rmul, P.rmug, c->rho, c->rhon, c->rmu, c->rmun);
+}
+static void seg_pre(fmf_ctx* c) {
+  seg_pre_a(c);
+  seg_pre_b(c);
+  seg_pre_c(c);
 }
 
 // The rest of the step before the viscous solve: reads uo, vo, wo, p, po (the
@@ -740,14 +760,25 @@ static void run_segment(fmf_ctx* c, int id, void (*fn)(fmf_ctx*)) {
   count_launch((int)it->second.launches);
 }
 
-// One step; after_pre (optional) runs on the host right after the first segment is
-// enqueued (phin is final from there on), before_pre2 (optional) before the second.
-static int step_once(fmf_ctx* c, const std::function<void()>& after_pre = {},
-                     const std::function<void()>& before_pre2 = {}) {
+// One step.  The optional host callbacks run between its parts (fmf_ctx_step_host:
+// waits for inputs, copies of results final early): before_b once part a is
+// enqueued, after_b once part b is (phin is final from there on), before_c, and
+// before_pre2 ahead of the second segment.
+struct StepHooks {
+  std::function<void()> before_b, after_b, before_c, before_pre2;
+};
+static int step_once(fmf_ctx* c, const StepHooks* hk = nullptr) {
   const Grid& g = c->g;
-  run_segment(c, 0, seg_pre);
-  if (after_pre) after_pre();
-  if (before_pre2) before_pre2();
+  auto hook = [&](const std::function<void()> StepHooks::*f) {
+    if (hk && hk->*f) (hk->*f)();
+  };
+  run_segment(c, 0, seg_pre_a);
+  hook(&StepHooks::before_b);
+  run_segment(c, 5, seg_pre_b);
+  hook(&StepHooks::after_b);
+  hook(&StepHooks::before_c);
+  run_segment(c, 6, seg_pre_c);
+  hook(&StepHooks::before_pre2);
   run_segment(c, 3, seg_pre2);
   const cudaGraphExec_t sx = c->graphs && c->dev_loop ? solve_exec(c) : nullptr;
   if (sx) {
@@ -946,20 +977,23 @@ int fmf_ctx_check_sor(fmf_ctx* c, double* out) {
   return take_status();
 }
 
-// One step from host buffers to host buffers (fmf_capi.h).  The step's first
-// segment reads u, v, w and phi only: those go up first, uo, vo, wo, p, po follow
-// on a second stream while it runs (phin is not an input: the step writes it
-// before reading it).  After the pointer rotation the result's uo, vo, wo, po are
-// this step's inputs u, v, w, p (their buffers are only read during the step) and
-// its phi and phin both hold phin, final once the first segment has run: those
-// eight fields go back on the second stream while the rest of the step runs; u,
-// v, w, p follow the step.
+// One step from host buffers to host buffers (fmf_capi.h).  The copies run on a
+// second stream beside the step: the step's first part starts once phi(1) is up
+// (its vertex gradients), goes on once u, v, w are (transport and the volume fix),
+// and once phi(0) is (its contact-angle pass, the mixture properties); uo, vo, wo,
+// p, po follow while that runs (phin is not an input: the step writes it before
+// reading it).  After the pointer rotation the result's uo, vo, wo, po are this
+// step's inputs u, v, w, p (their buffers are only read during the step) and its
+// phi and phin both hold phin, final once the first part has run: those eight
+// fields go back on the second stream while the rest of the step runs; u, v, w, p
+// follow the step.
 int fmf_ctx_step_host(fmf_ctx* c, const double* const* in, double* const* out) {
   if (!c || !in || !out) return FMF_ERR_ARG;
   ScratchScope scope(c->scr);
   if (!c->cs) {
     if (!FMF_CUDA(cudaStreamCreateWithFlags(&c->cs, cudaStreamNonBlocking)) ||
         !FMF_CUDA(cudaEventCreateWithFlags(&c->ev_in, cudaEventDisableTiming)) ||
+        !FMF_CUDA(cudaEventCreateWithFlags(&c->ev_in_phi0, cudaEventDisableTiming)) ||
         !FMF_CUDA(cudaEventCreateWithFlags(&c->ev_in2, cudaEventDisableTiming)) ||
         !FMF_CUDA(cudaEventCreateWithFlags(&c->ev_pre, cudaEventDisableTiming)))
       return take_status();
@@ -979,7 +1013,7 @@ int fmf_ctx_step_host(fmf_ctx* c, const double* const* in, double* const* out) {
   // copies there.
   c->verify = c->cont;
   c->cont = false;
-  for (int f : {0, 1, 2, 8}) h2d(f, c->s);  // u, v, w, phi(0)
+  // the step's stream: phi(1)
   if (c->verify) {
     FMF_CUDA(cudaMemcpyAsync(c->div, in[9], b, cudaMemcpyHostToDevice, c->s));
     const double* src[1] = {c->div};
@@ -988,8 +1022,11 @@ int fmf_ctx_step_host(fmf_ctx* c, const double* const* in, double* const* out) {
   } else {
     h2d(9, c->s);
   }
-  FMF_CUDA(cudaEventRecord(c->ev_in, c->s));
-  FMF_CUDA(cudaStreamWaitEvent(c->cs, c->ev_in, 0));
+  // the copy stream: u, v, w, then phi(0), then uo, vo, wo, p, po
+  for (int f : {0, 1, 2}) h2d(f, c->cs);
+  FMF_CUDA(cudaEventRecord(c->ev_in, c->cs));
+  h2d(8, c->cs);
+  FMF_CUDA(cudaEventRecord(c->ev_in_phi0, c->cs));
   if (c->verify) {
     double* st[3] = {c->un, c->vn, c->wn};
     for (int f = 0; f < 3; ++f) FMF_CUDA(cudaMemcpyAsync(st[f], in[3 + f], b, cudaMemcpyHostToDevice, c->cs));
@@ -1011,14 +1048,16 @@ int fmf_ctx_step_host(fmf_ctx* c, const double* const* in, double* const* out) {
   const bool gr = c->graphs;
   if (!c->warm) c->graphs = false;
   double* phin = c->phin;
-  const int st = step_once(
-      c,
-      [&]() {
-        FMF_CUDA(cudaEventRecord(c->ev_pre, c->s));
-        FMF_CUDA(cudaStreamWaitEvent(c->cs, c->ev_pre, 0));
-        for (int f = 8; f < 12; ++f) d2h(f, phin + (f % 2) * n, c->cs);
-      },
-      [&]() { FMF_CUDA(cudaStreamWaitEvent(c->s, c->ev_in2, 0)); });
+  StepHooks hk;
+  hk.before_b = [&]() { FMF_CUDA(cudaStreamWaitEvent(c->s, c->ev_in, 0)); };
+  hk.after_b = [&]() {
+    FMF_CUDA(cudaEventRecord(c->ev_pre, c->s));
+    FMF_CUDA(cudaStreamWaitEvent(c->cs, c->ev_pre, 0));
+    for (int f = 8; f < 12; ++f) d2h(f, phin + (f % 2) * n, c->cs);
+  };
+  hk.before_c = [&]() { FMF_CUDA(cudaStreamWaitEvent(c->s, c->ev_in_phi0, 0)); };
+  hk.before_pre2 = [&]() { FMF_CUDA(cudaStreamWaitEvent(c->s, c->ev_in2, 0)); };
+  const int st = step_once(c, &hk);
   c->verify = false;
   c->graphs = gr;
   c->warm = true;
