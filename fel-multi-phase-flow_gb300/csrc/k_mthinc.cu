@@ -177,6 +177,28 @@ void solphi_mthinc2(cudaStream_t s, const Grid& g, double dxinv, double dyinv, d
 }
 
 // solphi_mthinc3.f:84-209
+namespace {
+// solphi_mthinc3.f:138-160: phin += offset phin^2 (1 - phin), clipped, over the
+// interior; the offset (sums[2] >= 0: the Newton-Raphson reciprocal, no division)
+// formed once per block
+__global__ void __launch_bounds__(256) k_mthinc3_offset(Grid g, const double* __restrict__ sums,
+                                                        double* __restrict__ phin) {
+  __shared__ double off;
+  if (threadIdx.x == 0 && threadIdx.y == 0) off = (sums[0] - sums[1]) * recip_nr(sums[2] + 1.0e-99);
+  __syncthreads();
+  const int i = 1 + (int)(blockIdx.x * blockDim.x + threadIdx.x);
+  const int j = 1 + (int)(blockIdx.y * blockDim.y + threadIdx.y);
+  const int k = 1 + (int)blockIdx.z;
+  if (i > g.ni || j > g.nj) return;
+  const long c = g.at(i, j, k);
+  const double offset = off;
+  double p = phin[c];
+  p = p + offset * (p * p) * (1.0 - p);
+  p = fmin(p, 1.0);
+  phin[c] = fmax(p, 0.0);
+}
+}  // namespace
+
 void solphi_mthinc3(cudaStream_t s, const Grid& g, double dxinv, double dyinv, double dzinv, double bet,
                     const double* phix, const double* phiy, const double* phiz, const double* phi,
                     double* phin, double* sums) {
@@ -186,22 +208,24 @@ void solphi_mthinc3(cudaStream_t s, const Grid& g, double dxinv, double dyinv, d
   // one side, with the square root only within 1e-12 of it
   const double lim = M.eps_mthinc * M.dcellinv;
   const double lim2lo = lim * lim * (1.0 - 1.0e-12), lim2hi = lim * lim * (1.0 + 1.0e-12);
+  // the snap of :61-112 over 0..n+1, and on the interior the clip of :113-120 of
+  // the snapped value (the two passes of the reference touch each point alone)
   range3(s, 0, g.ni + 1, 0, g.nj + 1, 0, g.nk + 1, [=] __device__(int i, int j, int k) {
     const long X = 1, Y = G.sy, Z = G.sz;
     const long c = G.at(i, j, k);
     const double rnx = avg8(phix, c, X, Y, Z), rny = avg8(phiy, c, X, Y, Z), rnz = avg8(phiz, c, X, Y, Z);
     const double q2 = rnx * rnx + rny * rny + rnz * rnz;
     const bool outside = q2 < lim2lo ? true : (q2 > lim2hi ? false : sqrt(q2) <= lim);
-    if (outside) {
+    const bool interior = i >= 1 && i <= G.ni && j >= 1 && j <= G.nj && k >= 1 && k <= G.nk;
+    if (outside || interior) {
       double p = phin[c];
-      if (p <= M.eps_trunc) p = 0.0;
-      if (1.0 - p <= M.eps_trunc) p = 1.0;
+      if (outside) {
+        if (p <= M.eps_trunc) p = 0.0;
+        if (1.0 - p <= M.eps_trunc) p = 1.0;
+      }
+      if (interior) p = fmax(fmin(p, 1.0), 0.0);
       phin[c] = p;
     }
-  });
-  range3(s, 1, g.ni, 1, g.nj, 1, g.nk, [=] __device__(int i, int j, int k) {
-    const long c = G.at(i, j, k);
-    phin[c] = fmax(fmin(phin[c], 1.0), 0.0);
   });
   reduce_interior<3>(
       s, g,
@@ -213,15 +237,8 @@ void solphi_mthinc3(cudaStream_t s, const Grid& g, double dxinv, double dyinv, d
         r[2] = p * p * (1.0 - p);
       },
       sums);
-  range3(s, 1, g.ni, 1, g.nj, 1, g.nk, [=] __device__(int i, int j, int k) {
-    const long c = G.at(i, j, k);
-    // (sums[2] >= 0: the reciprocal by Newton-Raphson, no division per cell)
-    const double offset = (sums[0] - sums[1]) * recip_nr(sums[2] + 1.0e-99);
-    double p = phin[c];
-    p = p + offset * (p * p) * (1.0 - p);
-    p = fmin(p, 1.0);
-    phin[c] = fmax(p, 0.0);
-  });
+  k_mthinc3_offset<<<dim3((g.ni + 31) / 32, (g.nj + 7) / 8, g.nk), dim3(32, 8), 0, s>>>(g, sums, phin);
+  count_launch();
 }
 
 // summation.f:222-264 (nbub=1): q0 = q1 over the whole array, then clip the interior.
