@@ -610,7 +610,12 @@ def main():
                 "config": config_dict(cfg, world),
                 "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 10 * bytes_field,
                         "d2h_bytes_per_step": 12 * bytes_field, "steps": args.steps},
-                "gpu_launches": int(launches), "clocks": clk, "roofline": roofline, "step_roofline": step_roofline,
+                "gpu_launches": int(launches),
+                "gpu_launches_note": "this library's kernels in the timed steps (fmf_kernel_launches), including "
+                                     "the viscous-solve iterations run inside the CUDA graph's conditional loop "
+                                     "(the device-side stop rule), which an ncu launch list does not show "
+                                     "(FMF_DEVICE_LOOP=0 runs the same kernels from the host)",
+                "clocks": clk, "roofline": roofline, "step_roofline": step_roofline,
                 "cpu_baseline": cpu, "mixed": mixed, "mixed_horizon": horizon, "second_workload": second,
                 "adjoint": adjoint, "adjoint_mixed_forward": adjoint_m}
         print(json.dumps(line), flush=True)
