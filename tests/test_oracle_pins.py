@@ -291,3 +291,46 @@ def test_csf_curvature_of_a_sphere(orc, N):
 
 
 test_csf_curvature_of_a_sphere.errs = {}
+
+
+@pytest.mark.parametrize("axis", [0, 1, 2])
+@pytest.mark.parametrize("sign", [1.0, -1.0])
+def test_weno5_fifth_order_on_a_smooth_field(orc, axis, sign):
+    """weno5.h on a smooth monotone field q = sign * exp(x/2) along one axis (the
+    component of that axis, the others zero; every halo point filled with the exact
+    function): the advection term divided by the discrete advecting velocity of
+    cal_advu_weno5.f ((q(i-1) + 2 q(i) + q(i+1))/4) is the upwind-biased WENO5
+    derivative, which converges to dq/dx at fifth order where the field has no
+    critical point.  Checked on 16, 32 and 64 cells (each halving the error about
+    32-fold) on both upwind sides and every axis."""
+    errs = []
+    for n in (16, 32, 64):
+        dims = [8, 8, 8]
+        dims[axis] = n
+        ni, nj, nk = dims
+        h = 1.0 / n
+        sh = (nk + 6, nj + 6, ni + 6)
+        x = (np.arange(-2, n + 4, dtype=np.float64)) * h
+        f = sign * np.exp(0.5 * x)
+        bshape = [1, 1, 1]
+        bshape[2 - axis] = n + 6
+        fields = [np.zeros(sh) for _ in range(3)]
+        fields[axis] = np.broadcast_to(f.reshape(bshape), sh).copy()
+        out = [np.zeros(sh) for _ in range(3)]
+        d = [1.0, 1.0, 1.0]
+        d[axis] = 1.0 / h
+        orc.lib().orc_cal_advu_weno5(orc.I(ni), orc.I(nj), orc.I(nk), orc.D(d[0]), orc.D(d[1]), orc.D(d[2]),
+                                     *[orc.P(a) for a in fields], *[orc.P(a) for a in out])
+        line = [slice(3, 4)] * 3
+        line[2 - axis] = slice(3, n + 3)
+        adv = out[axis][tuple(line)].ravel()
+        fi = f[3:n + 3]
+        vel = ((f[2:n + 2] + fi) * 0.5 + (fi + f[4:n + 4]) * 0.5) * 0.5
+        exact = 0.5 * fi
+        errs.append(np.abs(adv / vel - exact).max())
+        for q in range(3):
+            if q != axis:
+                assert np.all(out[q] == 0.0)
+    orders = [np.log2(errs[t] / errs[t + 1]) for t in range(2)]
+    assert min(orders) >= 4.5, (errs, orders)
+    assert errs[-1] <= 1e-9, errs
