@@ -184,15 +184,16 @@ namespace {
 __global__ void __launch_bounds__(256) k_mthinc3_offset(Grid g, const double* __restrict__ sums,
                                                         double* __restrict__ phin) {
   __shared__ double off;
-  if (threadIdx.x == 0 && threadIdx.y == 0) off = (sums[0] - sums[1]) * recip_nr(sums[2] + 1.0e-99);
-  __syncthreads();
   const int i = 1 + (int)(blockIdx.x * blockDim.x + threadIdx.x);
   const int j = 1 + (int)(blockIdx.y * blockDim.y + threadIdx.y);
   const int k = 1 + (int)blockIdx.z;
-  if (i > g.ni || j > g.nj) return;
-  const long c = g.at(i, j, k);
+  const bool in = i <= g.ni && j <= g.nj;
+  const long c = in ? g.at(i, j, k) : 0;
+  double p = in ? phin[c] : 0.0;  // in flight while the offset is formed
+  if (threadIdx.x == 0 && threadIdx.y == 0) off = (sums[0] - sums[1]) * recip_nr(sums[2] + 1.0e-99);
+  __syncthreads();
+  if (!in) return;
   const double offset = off;
-  double p = phin[c];
   p = p + offset * (p * p) * (1.0 - p);
   p = fmin(p, 1.0);
   phin[c] = fmax(p, 0.0);
