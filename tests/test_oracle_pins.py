@@ -334,3 +334,75 @@ def test_weno5_fifth_order_on_a_smooth_field(orc, axis, sign):
     orders = [np.log2(errs[t] / errs[t + 1]) for t in range(2)]
     assert min(orders) >= 4.5, (errs, orders)
     assert errs[-1] <= 1e-9, errs
+
+
+def test_viscous_solve_fixed_point_is_the_staggered_stress_divergence(orc):
+    """cal_arith_coef_vis + solu_sor4, run to round-off (stop rule 1e-300, 200 outer
+    iterations), solve  q/dt - (0.5/rho) div(tau)_h(q) = src  for (u, v, w), with
+    div(tau)_h the staggered-grid stress divergence written here from its
+    definition: normal stresses 2 mu dq_i/dx_i at cell centres, shear stresses
+    mu_e (du_i/dx_j + du_j/dx_i) on the cell edges with mu_e the mean of the four
+    cells around the edge.  Smoothly varying viscosity, uniform density, unequal dx,
+    dy, dz; checked at every point whose stencil stays off the wall ghosts (x and
+    z periodic), to 1e-12 of the largest source."""
+    import ctypes
+
+    ni, nj, nk = 16, 16, 8
+    lx, ly, lz = 2.0, 1.0, 0.75
+    dx, dy, dz = lx / ni, ly / nj, lz / nk
+    dt, rho0 = 2e-3, 2.0
+    sh = (nk + 6, nj + 6, ni + 6)
+    k3, j3, i3 = np.meshgrid(np.arange(-2, nk + 4), np.arange(-2, nj + 4), np.arange(-2, ni + 4), indexing="ij")
+    xc, yc, zc = (i3 - 0.5) * dx, (j3 - 0.5) * dy, (k3 - 0.5) * dz
+    mu = 0.05 * (1.0 + 0.3 * np.sin(2 * np.pi * xc / lx) * np.cos(2 * np.pi * zc / lz) + 0.2 * yc)
+    rho = np.full(sh, rho0)
+    src = [np.sin(2 * np.pi * xc / lx + 0.3 * q) * np.cos(2 * np.pi * zc / lz) * (1.0 + yc) for q in range(3)]
+    u, v, w = np.zeros(sh), np.zeros(sh), np.zeros(sh)
+    l1, l2, phi = np.full(sh, 0.1), np.full(sh, 0.1), np.zeros(sh)
+    I, D, P = orc.I, orc.D, orc.P
+    coef = [np.zeros(sh) for _ in range(45)]
+    parr = (ctypes.POINTER(ctypes.c_double) * 45)(*[P(c) for c in coef])
+    L = orc.lib()
+    L.orc_cal_arith_coef_vis_v(I(ni), I(nj), I(nk), D(1 / dx), D(1 / dy), D(1 / dz), P(mu), parr, ctypes.c_int(0))
+    L.orc_set_sor.argtypes = [ctypes.c_double, ctypes.c_int]
+    L.orc_set_sor(1e-300, 200)
+    try:
+        err = ctypes.c_double()
+        L.orc_solu_sor4_v(orc.IA(orc.NID), I(ni), I(nj), I(nk), D(dt), P(rho), P(rho), parr, P(src[0]), P(src[1]),
+                          P(src[2]), P(u), P(v), P(w), D(0.0), D(dy), P(l1), P(l2), P(phi), ctypes.byref(err))
+    finally:
+        L.orc_set_sor(1e-3, 21)
+
+    def at(a, di=0, dj=0, dk=0):  # a[i+di, j+dj, k+dk] over i, j, k = 1..n (the interior block)
+        return a[3 + dk:3 + dk + nk, 3 + dj:3 + dj + nj, 3 + di:3 + di + ni]
+
+    m = lambda di=0, dj=0, dk=0: at(mu, di, dj, dk)
+    exy = lambda di=0, dj=0: (m(di, dj) + m(di + 1, dj) + m(di, dj + 1) + m(di + 1, dj + 1)) / 4
+    exz = lambda di=0, dk=0: (m(di, 0, dk) + m(di + 1, 0, dk) + m(di, 0, dk + 1) + m(di + 1, 0, dk + 1)) / 4
+    eyz = lambda dj=0, dk=0: (m(0, dj, dk) + m(0, dj + 1, dk) + m(0, dj, dk + 1) + m(0, dj + 1, dk + 1)) / 4
+    # shear stresses on the edges (i+1/2, j+1/2), (i+1/2, k+1/2), (j+1/2, k+1/2) of cell (i, j, k)
+    txy = lambda di=0, dj=0: exy(di, dj) * ((at(u, di, dj + 1) - at(u, di, dj)) / dy +
+                                            (at(v, di + 1, dj) - at(v, di, dj)) / dx)
+    txz = lambda di=0, dk=0: exz(di, dk) * ((at(u, di, 0, dk + 1) - at(u, di, 0, dk)) / dz +
+                                            (at(w, di + 1, 0, dk) - at(w, di, 0, dk)) / dx)
+    tyz = lambda dj=0, dk=0: eyz(dj, dk) * ((at(v, 0, dj, dk + 1) - at(v, 0, dj, dk)) / dz +
+                                            (at(w, 0, dj + 1, dk) - at(w, 0, dj, dk)) / dy)
+    # normal stresses at cell centres
+    txx = lambda di=0: 2 * m(di) * (at(u, di) - at(u, di - 1)) / dx
+    tyy = lambda dj=0: 2 * m(0, dj) * (at(v, 0, dj) - at(v, 0, dj - 1)) / dy
+    tzz = lambda dk=0: 2 * m(0, 0, dk) * (at(w, 0, 0, dk) - at(w, 0, 0, dk - 1)) / dz
+    div = [(txx(1) - txx(0)) / dx + (txy(0, 0) - txy(0, -1)) / dy + (txz(0, 0) - txz(0, -1)) / dz,
+           (txy(0, 0) - txy(-1, 0)) / dx + (tyy(1) - tyy(0)) / dy + (tyz(0, 0) - tyz(0, -1)) / dz,
+           (txz(0, 0) - txz(-1, 0)) / dx + (tyz(0, 0) - tyz(-1, 0)) / dy + (tzz(1) - tzz(0)) / dz]
+    scale = max(np.abs(at(s)).max() for s in src)
+    # points whose stencils stay off the wall ghosts (j = 0, nj + 1) and the walls'
+    # v, and off the x and z halos: bndu.f refreshes every component's halos
+    # shifted by one cell before the periodic copy of the swept one only, so the
+    # other components' halos differ between the sweeps that read them and the end
+    # of the solve
+    rows = {0: slice(1, nj - 1), 1: slice(1, nj - 2), 2: slice(1, nj - 1)}
+    for q, fld in enumerate((u, v, w)):
+        res = at(fld) / dt - 0.5 / rho0 * div[q] - at(src[q])
+        r = np.abs(res[1:nk - 1, rows[q], 1:ni - 1]).max()
+        assert r <= 1e-12 * scale, (q, r, scale)
+    assert np.abs(at(v)).max() > 0.0 and np.abs(at(w)).max() > 0.0  # the coupling is exercised
