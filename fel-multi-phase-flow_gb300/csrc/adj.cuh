@@ -249,15 +249,17 @@ cudaGraphExec_t cached_graph(cudaStream_t s, GraphCache* cache, const std::vecto
 // transposed fixed-point solve and gradient collection; lam: 3 output arrays (the
 // converged adjoint of un*, consumed by the gradient pass); lAB, lmu, lE, lwc
 // accumulate; work: >= 3n + 1026 doubles; host_norm: 2 pinned doubles; cache may
-// be null (no graphs).  fb (3n) receives the feedback term G^T lam of the solve and
-// *fb_norm its norm; where *fb_norm > 0 on entry, the solve starts from lout + fb
-// (the previous solve's, a warm start) and its stop rule's scale is *fb_norm.
+// be null (no graphs).  fb_out (3n) receives the feedback term G^T lam of the
+// solve and *fb_norm its norm.  Where *fb_norm > 0 on entry, fb holds the previous
+// solve's feedback term (and fb_prev, if not null, the one before): the solve
+// starts from lout + fb, or lout + 2 fb - fb_prev (a warm start extrapolated in
+// time), and its stop rule's scale is *fb_norm.  fb_out may be fb_prev's buffer.
 // Returns the iterations used.
 int sor_T(cudaStream_t s, const Grid& g, double dxi, double dyi, double dzi, const double* mu, double* const* E,
           double* const* AB, double uwall, const double* wallc, const double* const* ustar, const double* snaps,
           const double* const* lout, double* const* lam, double* const* lAB, double* lmu, double* const* lE,
           double* lwc, double tol, int maxit, double* work, double* host_norm, GraphCache* cache, double* fb,
-          double* fb_norm);
+          double* fb_norm, const double* fb_prev, double* fb_out);
 
 }  // namespace adj
 }  // namespace fmf

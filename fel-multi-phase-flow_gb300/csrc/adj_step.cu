@@ -160,7 +160,12 @@ struct fmf_adj {
   // lam = lout + fb, fb the feedback term G^T lam of the previous solve (3n), whose
   // norm fb_norm (0: none yet, a cold start) also scales the stop rule.
   // FMF_ADJ_WARM=0 at creation: every solve starts cold.
-  double* fb = nullptr;
+  // The last two solves' feedback terms (fb[fb_latest] the latest; fb_count of them
+  // valid): from two on, the start is extrapolated linearly in time, lout + 2 fb -
+  // fb_prev (FMF_ADJ_EXTRAP=0 at creation: lout + fb).
+  double* fb[2] = {nullptr, nullptr};
+  int fb_latest = 0, fb_count = 0;
+  bool extrap = true;
   double fb_norm = 0.0;
   bool warm = true;
   // With a mixed-precision forward the reverse of its FP32 WENO5 runs in FP32
@@ -738,8 +743,15 @@ void reverse_step(fmf_adj* a, const double* st, bool defer) {
   const double* lout[3] = {a->lun[0], a->lun[1], a->lun[2]};
   a->adj_total += adj::sor_T(s, g, dxi, dyi, dzi, a->rmun, a->E, a->AB, P.uwall, a->wallc, a->ustar, a->snaps,
                              lout, a->lam, a->lAB, a->lrmun, a->lE, a->lwc, a->adj_tol, a->adj_max, a->work,
-                             a->host_norm, &a->graphs, a->fb, &a->fb_norm);
-  if (!a->warm) a->fb_norm = 0.0;
+                             a->host_norm, &a->graphs, a->fb[a->fb_latest], &a->fb_norm,
+                             a->fb_count >= 2 && a->extrap ? a->fb[1 - a->fb_latest] : nullptr,
+                             a->fb[1 - a->fb_latest]);
+  a->fb_latest = 1 - a->fb_latest;
+  ++a->fb_count;
+  if (!a->warm) {
+    a->fb_norm = 0.0;
+    a->fb_count = 0;
+  }
   check_stage(a, "sor");
   // :579-603 momentum factors, edge viscosities, slip coefficients
   {
@@ -926,6 +938,7 @@ int fmf_adj_create(const fmf_params* prm, fmf_adj** out) {
   if (const char* e = std::getenv("FMF_STEP_CACHE")) a->no_carry = std::atoi(e) == 0;
   a->record_all = std::getenv("FMF_ADJ_RECORD_ALL") != nullptr;
   if (const char* e = std::getenv("FMF_ADJ_WARM")) a->warm = std::atoi(e) != 0;
+  if (const char* e = std::getenv("FMF_ADJ_EXTRAP")) a->extrap = std::atoi(e) != 0;
   if (const char* e = std::getenv("FMF_ADJ_F32_REVERSE")) a->f32_reverse = std::atoi(e) != 0;
   a->g = Grid(prm->ni, prm->nj, prm->nk);
   a->scr = scratch_set_create();
@@ -976,7 +989,8 @@ int fmf_adj_create(const fmf_params* prm, fmf_adj** out) {
   a->sorpart = dalloc(a, fused::sor_parts(a->g));
   a->csfwork = dalloc(a, 21 * n);
   a->work = dalloc(a, 3 * n + 1024 + 63 * n);  // SOR adjoint, then CSF (42n) or WENO5 (63n) adjoints
-  a->fb = dalloc(a, 3 * n);
+  a->fb[0] = dalloc(a, 3 * n);
+  a->fb[1] = dalloc(a, 3 * n);
   a->lcarry = dalloc(a, 6 * n);
   if (a->mixed) {
     fused::RefineBufs& rb = a->rb;
@@ -1187,6 +1201,7 @@ int fmf_adj_rollout(fmf_adj* a, int K, int every, const double* const* state0, c
   // reverse, segment by segment
   a->carry_in = false;
   a->fb_norm = 0.0;
+  a->fb_count = 0;
   for (int c = nck - 1; c >= 0 && !get_status(); --c) {
     const int t0 = c * every, t1 = std::min(K, t0 + every);
     if (w) {

@@ -226,10 +226,14 @@ __global__ void k_add_diff3(long n, Arr3 l, CArr3 o, const double* __restrict__ 
     part[512 + blockIdx.x] = sh[1][0];
   }
 }
-// l = lout + fb (the warm start)
-__global__ void k_warm3(long n, Arr3 l, CArr3 o, const double* __restrict__ fb) {
+// l = lout + fb (the warm start), or lout + 2 fb - fb2 (fb2 the feedback term one
+// solve earlier: linear extrapolation in time)
+__global__ void k_warm3(long n, Arr3 l, CArr3 o, const double* __restrict__ fb, const double* __restrict__ fb2) {
   for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x)
-    for (int c = 0; c < 3; ++c) l.a[c][t] = o.a[c][t] + fb[t + c * n];
+    for (int c = 0; c < 3; ++c) {
+      const double f = fb[t + c * n];
+      l.a[c][t] = o.a[c][t] + (fb2 ? f + (f - fb2[t + c * n]) : f);
+    }
 }
 // out[0] = sum of part[0..n), out[1] = sum of part[512..512+n)
 __global__ void k_sum_small(const double* part, int n, double* out) {
@@ -395,7 +399,7 @@ int sor_T(cudaStream_t s, const Grid& g, double dxi, double dyi, double dzi, con
           double* const* AB, double uwall, const double* wallc, const double* const* ustar, const double* snaps,
           const double* const* lout, double* const* lam, double* const* lAB, double* lmu, double* const* lE,
           double* lwc, double tol, int maxit, double* work, double* host_norm, GraphCache* cache, double* fb,
-          double* fb_norm) {
+          double* fb_norm, const double* fb_prev, double* fb_out) {
   const VPa p = make_vpa(dxi, dyi, dzi);
   const long n = g.n;
   const CArr4 cf{{mu, E[0], E[1], E[2]}};
@@ -408,7 +412,7 @@ int sor_T(cudaStream_t s, const Grid& g, double dxi, double dyi, double dzi, con
   // l = lout, or lout plus the previous solve's feedback term
   const bool warm = *fb_norm > 0.0;
   if (warm) {
-    k_warm3<<<608, 256, 0, s>>>(n, L3, O3, fb);
+    k_warm3<<<608, 256, 0, s>>>(n, L3, O3, fb, fb_prev);
     count_launch();
   } else {
     for (int c = 0; c < 3; ++c)
@@ -442,7 +446,7 @@ int sor_T(cudaStream_t s, const Grid& g, double dxi, double dyi, double dzi, con
   auto iteration = [&]() {
     k_copy3<<<608, 256, 0, s>>>(n, L3, prev);
     backward_cycle(false);
-    k_add_diff3<<<512, 256, 0, s>>>(n, L3, O3, prev, part, fb);
+    k_add_diff3<<<512, 256, 0, s>>>(n, L3, O3, prev, part, fb_out);
     k_sum_small<<<1, 256, 0, s>>>(part, 512, nrm);
     count_launch(3);
   };
@@ -450,7 +454,7 @@ int sor_T(cudaStream_t s, const Grid& g, double dxi, double dyi, double dzi, con
   cudaGraphExec_t exec =
       cache ? cached_graph(s, cache,
                            {lam[0], lam[1], lam[2], lout[0], lout[1], lout[2], mu, E[0], E[1], E[2], AB[0], AB[2],
-                            AB[4], wallc, ustar[0], ustar[2], work, fb},
+                            AB[4], wallc, ustar[0], ustar[2], work, fb_out},
                            iteration, &per_launch)
             : nullptr;
   // The stop rule's scale: the change of the first iteration from l = lout (the
