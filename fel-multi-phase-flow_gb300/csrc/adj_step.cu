@@ -148,6 +148,7 @@ struct fmf_adj {
   double* lcarry = nullptr;
   bool carry_in = false;
   double* host_norm = nullptr;  // pinned
+  double* tdma = nullptr;       // the pressure solve's Thomas factors (fused::tdma_coef)
   fmf_adj* worker = nullptr;    // recomputes the next segment while this handle reverses one
   // The product step (graph-replayed, pointer rotation, no record copies) for the
   // forward steps whose intermediates no reverse step reads: the rollout's steps
@@ -578,7 +579,7 @@ int record_step(fmf_adj* a, bool graphs) {
     // :625-661
     fused::wall_halo(s, g, 7, P.uwall, a->wallc, a->un[0], a->un[1], a->un[2]);
     op::caldiv(s, g, dxi, dyi, dzi, dt, a->un[0], a->un[1], a->un[2], a->div, nullptr);
-    fused::pressure_half(s, g, P.rhog, dxi, dzi, a->as_f, a->an_f, a->ap_f, a->div, a->pr, a->pi, a->dp);
+    fused::pressure_half(s, g, P.rhog, dxi, dzi, a->as_f, a->an_f, a->ap_f, a->div, a->pr, a->pi, a->dp, a->tdma);
     op::bnd_avzero(s, g, a->dp);
     op::bnd_neumann(s, g, a->dp);
     op::bnd_periodic(s, g, a->dp);
@@ -717,7 +718,8 @@ void reverse_step(fmf_adj* a, const double* st, bool defer) {
   adj::periodic_T(s, g, a->ldp);
   adj::neumann_T(s, g, a->ldp);
   adj::avzero_T(s, g, a->ldp);
-  fused::pressure_half(s, g, P.rhog, dxi, dzi, a->as_f, a->an_f, a->ap_f, a->ldp, a->pr, a->pi, a->ldiv);
+  fused::pressure_half(s, g, P.rhog, dxi, dzi, a->as_f, a->an_f, a->ap_f, a->ldp, a->pr, a->pi, a->ldiv,
+                       a->tdma);
   adj::caldiv_T(s, g, dxi, dyi, dzi, dt, a->ldiv, a->lun[0], a->lun[1], a->lun[2]);
   check_stage(a, "poisson");
   adj::wall_halo_T(s, g, 7, P.uwall, a->wallc, a->ustar[0], a->ustar[2], a->lun[0], a->lun[1], a->lun[2], a->lwc);
@@ -1040,6 +1042,10 @@ int fmf_adj_create(const fmf_params* prm, fmf_adj** out) {
   FMF_CUDA(cudaMemcpyAsync(a->as_f, as.data(), sizeof(double) * (NJ + 6), cudaMemcpyHostToDevice, a->s));
   FMF_CUDA(cudaMemcpyAsync(a->an_f, an.data(), sizeof(double) * (NJ + 6), cudaMemcpyHostToDevice, a->s));
   FMF_CUDA(cudaMemcpyAsync(a->ap_f, ap.data(), sizeof(double) * (NJ + 6), cudaMemcpyHostToDevice, a->s));
+  // the Thomas elimination factors of the pressure solve and its transpose
+  a->tdma = dalloc(a, fused::tdma_coef_doubles(a->g));
+  if (a->tdma)
+    fused::tdma_coef(a->s, a->g, prm->rhog, 1.0 / prm->dx, 1.0 / prm->dz, a->as_f, a->an_f, a->ap_f, a->tdma);
   FMF_CUDA(cudaStreamSynchronize(a->s));
   *out = a;
   return take_status();

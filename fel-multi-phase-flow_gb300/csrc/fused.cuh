@@ -83,8 +83,14 @@ long sor_parts(const Grid& g);
 // The pressure Poisson solve (solp_fft_tdma1-3) on the half spectrum of the real
 // divergence: div -> dp interior.  pr, pi: (ni/2+1) nj nk doubles each (the spectrum
 // after the forward transform and the Thomas solve).
+// coef (optional): the Thomas elimination factors of every mode (tdma_coef), formed
+// once for the grid and rho; without it each solve forms them again.
 void pressure_half(cudaStream_t s, const Grid& g, double rho, double dxinv, double dzinv, const double* as_f,
-                   const double* an_f, const double* ap_f, const double* div, double* pr, double* pi, double* dp);
+                   const double* an_f, const double* ap_f, const double* div, double* pr, double* pi, double* dp,
+                   const double* coef = nullptr);
+long tdma_coef_doubles(const Grid& g);
+void tdma_coef(cudaStream_t s, const Grid& g, double rho, double dxinv, double dzinv, const double* as_f,
+               const double* an_f, const double* ap_f, double* coef);
 
 // corunp_explicit: un, vn, wn += dt/rho grad(dp) at the interior, pn = phat + dp
 void project(cudaStream_t s, const Grid& g, double rho, double dxinv, double dyinv, double dzinv, double dt,

@@ -166,6 +166,60 @@ __global__ void __launch_bounds__(128) k_tdma_half(Grid g, double dx2r, double d
   }
 }
 
+// The matrix of every mode's system is fixed by the grid and rho_g, so its
+// elimination factors are formed once (k_tdma_coef: apinv and a of the forward
+// sweep above, by the same expressions) and the solves only apply them
+// (k_tdma_pre).  coef: [apinv | a], each (ni/2+1) nk nj doubles, index
+// (j-1) nmode + mode.
+__global__ void __launch_bounds__(128) k_tdma_coef(Grid g, double dx2r, double dz2r, double pi2_ni, double pi2_nk,
+                                                   const double* __restrict__ as_f, const double* __restrict__ an_f,
+                                                   const double* __restrict__ ap_f, double* __restrict__ coef) {
+  const int H = g.ni / 2 + 1, NJ = g.nj;
+  const int kx = blockIdx.x * blockDim.x + threadIdx.x;
+  const int kz = blockIdx.y;
+  if (kx >= H) return;
+  const double c1x = cos((double)kx * pi2_ni) * 2.0;
+  const double c1z = cos((double)kz * pi2_nk) * 2.0;
+  const long mode = kx + (long)H * kz, nmode = (long)H * g.nk, nh = nmode * NJ;
+  double a_prev = 0.0;
+  for (int j = 1; j <= NJ; ++j) {
+    const double ap = ap_f[j + 2] + dx2r * (2.0 - c1x) + dz2r * (2.0 - c1z);
+    const double d00 = -ap + as_f[j + 2] * a_prev;
+    const double apinv = -d00 * recip_nr(fma(d00, d00, 1.0e-99));
+    const double a = apinv * an_f[j + 2];
+    coef[(long)(j - 1) * nmode + mode] = apinv;
+    coef[nh + (long)(j - 1) * nmode + mode] = a;
+    a_prev = a;
+  }
+}
+__global__ void __launch_bounds__(128) k_tdma_pre(Grid g, const double* __restrict__ as_f,
+                                                  const double* __restrict__ coef, double* pr, double* pi) {
+  const int H = g.ni / 2 + 1, NJ = g.nj;
+  const int kx = blockIdx.x * blockDim.x + threadIdx.x;
+  const int kz = blockIdx.y;
+  if (kx >= H) return;
+  const long mode = kx + (long)H * kz, nmode = (long)H * g.nk, nh = nmode * NJ;
+  const long base = kx + (long)H * NJ * kz;
+  double br = 0.0, bi = 0.0;
+  for (int j = 1; j <= NJ; ++j) {
+    const double apinv = __ldg(coef + (long)(j - 1) * nmode + mode);
+    const long o = base + (long)H * (j - 1);
+    br = apinv * (-pr[o] + as_f[j + 2] * br);
+    bi = apinv * (-pi[o] + as_f[j + 2] * bi);
+    pr[o] = br;
+    pi[o] = bi;
+  }
+  double xr = br, xi = bi;
+  for (int j = NJ - 1; j >= 1; --j) {
+    const long o = base + (long)H * (j - 1);
+    const double a = __ldg(coef + nh + (long)(j - 1) * nmode + mode);
+    xr = pr[o] + a * xr;
+    xi = pi[o] + a * xi;
+    pr[o] = xr;
+    pi[o] = xi;
+  }
+}
+
 // corunp_explicit.f:26-75 with the constant dt dxinv / rho formed once on the host
 // (the reference divides by rho at every point)
 __global__ void __launch_bounds__(256) k_project(Grid g, double cx, double cy, double cz,
@@ -185,12 +239,25 @@ __global__ void __launch_bounds__(256) k_project(Grid g, double cx, double cy, d
 }
 }  // namespace
 
+long tdma_coef_doubles(const Grid& g) { return 2L * (g.ni / 2 + 1) * g.nj * g.nk; }
+
+void tdma_coef(cudaStream_t s, const Grid& g, double rho, double dxinv, double dzinv, const double* as_f,
+               const double* an_f, const double* ap_f, double* coef) {
+  const int H = g.ni / 2 + 1;
+  const double pi_ = 3.141592653589793238462643383279502884;
+  k_tdma_coef<<<dim3((unsigned)((H + 127) / 128), (unsigned)g.nk), 128, 0, s>>>(
+      g, dxinv * dxinv / rho, dzinv * dzinv / rho, pi_ * 2.0 / (double)g.ni, pi_ * 2.0 / (double)g.nk, as_f, an_f,
+      ap_f, coef);
+  count_launch();
+}
+
 void pressure_half(cudaStream_t s, const Grid& g, double rho, double dxinv, double dzinv, const double* as_f,
-                   const double* an_f, const double* ap_f, const double* div, double* pr, double* pi, double* dp) {
+                   const double* an_f, const double* ap_f, const double* div, double* pr, double* pi, double* dp,
+                   const double* coef) {
   const long nh = (long)(g.ni / 2 + 1) * g.nj * g.nk;
   double* tr = (double*)scratch(sizeof(double) * 2 * nh, 5);
   double* ti = tr + nh;
-  double* at = (double*)scratch(sizeof(double) * nh, 4);
+  double* at = coef ? nullptr : (double*)scratch(sizeof(double) * nh, 4);
   const int M = g.ni / 2, H = M + 1;
   const double2 *twM = op::fft_twiddles(M), *twN = op::fft_twiddles(g.ni), *twz = op::fft_twiddles(g.nk);
   const int rows = g.nj * g.nk;  // a multiple of kRows for power-of-two nj, nk >= 4
@@ -209,8 +276,11 @@ void pressure_half(cudaStream_t s, const Grid& g, double rho, double dxinv, doub
   k_fft_z_half<<<gz, 256, smz, s>>>(g, tr, ti, pr, pi, twz, -1.0, 1.0 / ((double)g.ni * (double)g.nk));
   const double pi_ = 3.141592653589793238462643383279502884;
   const double dx2r = dxinv * dxinv / rho, dz2r = dzinv * dzinv / rho;
-  k_tdma_half<<<dim3((unsigned)((H + 127) / 128), (unsigned)g.nk), 128, 0, s>>>(
-      g, dx2r, dz2r, pi_ * 2.0 / (double)g.ni, pi_ * 2.0 / (double)g.nk, as_f, an_f, ap_f, pr, pi, at);
+  if (coef)
+    k_tdma_pre<<<dim3((unsigned)((H + 127) / 128), (unsigned)g.nk), 128, 0, s>>>(g, as_f, coef, pr, pi);
+  else
+    k_tdma_half<<<dim3((unsigned)((H + 127) / 128), (unsigned)g.nk), 128, 0, s>>>(
+        g, dx2r, dz2r, pi_ * 2.0 / (double)g.ni, pi_ * 2.0 / (double)g.nk, as_f, an_f, ap_f, pr, pi, at);
   k_fft_z_half<<<gz, 256, smz, s>>>(g, pr, pi, tr, ti, twz, +1.0, 1.0);
   k_rfft_x_inv<<<rows / kRows, 256, smi, s>>>(g, tr, ti, dp, twM, twN);
   count_launch(5);

@@ -92,6 +92,7 @@ struct fmf_ctx {
   fused::RefineBufs rb{};    // FP32 buffers of the mixed-precision viscous solve
   float2* wsplit = nullptr;  // mixed: split pairs of u, v, w, uo, vo, wo for the FP32 WENO5 (6 n)
   double* host_err = nullptr;  // pinned
+  double* tdma = nullptr;       // the pressure solve's Thomas factors (fused::tdma_coef)
   std::vector<int> sor_iters;
   double sor_tol = 1.0e-3;  // solu_sor4.f:291 stop rule (fmf_ctx_set_sor)
   int sor_max = 21;         // solu_sor4.f:130 do lp=0,20
@@ -334,6 +335,9 @@ int fmf_ctx_create(const fmf_params* prm, fmf_ctx** out) {
   FMF_CUDA(cudaMemcpyAsync(c->as_f, as.data(), sizeof(double) * (NJ + 6), cudaMemcpyHostToDevice, c->s));
   FMF_CUDA(cudaMemcpyAsync(c->an_f, an.data(), sizeof(double) * (NJ + 6), cudaMemcpyHostToDevice, c->s));
   FMF_CUDA(cudaMemcpyAsync(c->ap_f, ap.data(), sizeof(double) * (NJ + 6), cudaMemcpyHostToDevice, c->s));
+  // the Thomas elimination factors of the pressure solve, fixed for the context
+  c->tdma = alloc(c, fused::tdma_coef_doubles(c->g));
+  if (c->tdma) fused::tdma_coef(c->s, c->g, prm->rhog, 1.0 / prm->dx, 1.0 / prm->dz, c->as_f, c->an_f, c->ap_f, c->tdma);
   FMF_CUDA(cudaStreamSynchronize(c->s));
   *out = c;
   return take_status();
@@ -713,7 +717,8 @@ static void seg_post(fmf_ctx* c) {
   // :625-646
   fused::wall_halo(s, g, 7, P.uwall, c->wallc, c->un, c->vn, c->wn);
   op::caldiv(s, g, dxinv, dyinv, dzinv, dt, c->un, c->vn, c->wn, c->div, nullptr);
-  fused::pressure_half(s, g, P.rhog, dxinv, dzinv, c->as_f, c->an_f, c->ap_f, c->div, c->pr, c->pi, c->dp);
+  fused::pressure_half(s, g, P.rhog, dxinv, dzinv, c->as_f, c->an_f, c->ap_f, c->div, c->pr, c->pi, c->dp,
+                        c->tdma);
   op::bnd_avzero(s, g, c->dp);
   op::bnd_neumann(s, g, c->dp);
   op::bnd_periodic(s, g, c->dp);
@@ -852,7 +857,8 @@ int fmf_ctx_time_stage(fmf_ctx* c, int stage, int reps, float* ms) {
                                c->un, c->vn, c->wn, c->sorpart, c->red + 8);
         break;
       case 2:
-        fused::pressure_half(s, g, P.rhog, dxinv, dzinv, c->as_f, c->an_f, c->ap_f, c->div, c->pr, c->pi, c->dp);
+        fused::pressure_half(s, g, P.rhog, dxinv, dzinv, c->as_f, c->an_f, c->ap_f, c->div, c->pr, c->pi, c->dp,
+                        c->tdma);
         break;
       case 3:
         fused::mthinc_fluxes(s, g, dxinv, dyinv, dzinv, P.dt, P.bet_mthinc, c->phi + n, c->phix, c->phiy,
