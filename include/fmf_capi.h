@@ -480,7 +480,9 @@ void datain_(int* ipara, int* ID, int* ni, int* nj, int* nk, int* nbub, int* nst
  * (prm->precision: FMF_FP64, or FMF_MIXED for the mixed-precision forward) with
  * the viscous solve run to sor_tol; the reverse pass, in FP64, recomputes each step
  * from checkpoints taken every `every` steps (0: ceil(sqrt(K))) and differentiates
- * the FP64 step's operations at the states that forward produced. */
+ * the FP64 step's operations at the states that forward produced.  In an FMF_MIXED
+ * handle the reverse of the WENO5 advection runs in FP32, as its forward does
+ * (environment FMF_ADJ_F32_REVERSE=0 at creation keeps it FP64). */
 typedef struct fmf_adj fmf_adj;
 int fmf_adj_create(const fmf_params* prm, fmf_adj** out);
 int fmf_adj_destroy(fmf_adj* adj);
