@@ -229,6 +229,48 @@ def mixed_case(cfg, st0, steps, warmup, stream, fp64_ms=None):
     return out
 
 
+def fp64e_case(cfg, st0, steps, warmup, stream, fp64_ms):
+    """The FP64-accurate step (FMF_FP64E: the FP64 step with its WENO5 in FP32-pair
+    arithmetic) on the workload: CUDA-event time per step (state resident, `steps`
+    after `warmup`), and against the FP64 step from the same initial state after
+    warmup + steps: each field's largest difference relative to the FP64 field's
+    largest magnitude, and whether every viscous solve took the same iterations."""
+    import torch
+
+    from fmf import capi
+
+    states, iters = {}, {}
+    out = {"workload": f"{cfg.name} {cfg.ni}x{cfg.nj}x{cfg.nk}", "steps": steps, "warmup": warmup}
+    for prec, key in ((capi.FMF_FP64E, "fp64e"), (capi.FMF_FP64, "fp64")):
+        g = capi.Stepper(cfg, precision=prec, stream=stream.cuda_stream)
+        g.upload(st0)
+        g.step(warmup)
+        its = g.sor_iterations()
+        g.sync()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        g.step(steps)
+        e1.record(stream)
+        e1.synchronize()
+        iters[key] = its + g.sor_iterations()
+        if key == "fp64e":
+            out["ms_per_step"] = e0.elapsed_time(e1) / steps
+        states[key] = g.get_state()
+        g.close()
+    out["fp64_ms_per_step"] = fp64_ms
+    out["value"] = cfg.cells / (out["ms_per_step"] * 1e-3)
+    out["unit"] = UNIT
+    out["speedup_vs_fp64"] = fp64_ms / out["ms_per_step"]
+    out["steps_compared"] = warmup + steps
+    out["max_rel_err_vs_fp64"] = {k: _rel(states["fp64e"][f], states["fp64"][f], cfg) for k, f in FIELDS.items()}
+    out["same_viscous_iterations"] = iters["fp64e"] == iters["fp64"]
+    out["precision"] = ("the FP64 step with its WENO5 advection in FP32-pair arithmetic (two floats per value, about "
+                        "49 significant bits) on the FP32 pipe; every other kernel FP64; parity with the oracle "
+                        "at the FP64 step's 1e-10 (tests/test_gpu_fp64e.py)")
+    return out
+
+
 def mixed_horizon(cfg, st0, steps, every, stream):
     """FP64 and mixed steps side by side from the same initial state over `steps`
     steps: the largest relative error of each field (interior, against the FP64
@@ -422,7 +464,7 @@ def profile(args):
                           "iterations": A.iterations()}))
         A.close()
         return
-    prec = capi.FMF_MIXED if args.precision == "mixed" else capi.FMF_FP64
+    prec = {"mixed": capi.FMF_MIXED, "fp64e": capi.FMF_FP64E}.get(args.precision, capi.FMF_FP64)
     g = capi.Stepper(C.get(args.workload), precision=prec)
     g.initial_state()
     g.step(args.warmup)
@@ -453,7 +495,10 @@ def main():
                     help="workload of the adjoint-cost measurement")
     ap.add_argument("--adjoint-mixed-steps", type=int, default=500,
                     help="K of the mixed-forward adjoint on the 256x128x128 sessile drop (0: skip)")
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed", "adjoint", "adjoint_mixed"], help="--profile only")
+    ap.add_argument("--fp64e", type=int, default=1,
+                    help="1: time the FP64-accurate FP32-pair WENO5 step (FMF_FP64E) on the workload too")
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed", "fp64e", "adjoint", "adjoint_mixed"],
+                    help="--profile only")
     ap.add_argument("--profile", action="store_true",
                     help="no timing: start-up pass, --warmup steps, then --steps steps (for ncu launch lists)")
     args = ap.parse_args()
@@ -576,6 +621,7 @@ def main():
     mixed = None
     horizon = None
     second = None
+    fp64e = None
     if rank == 0:
         g.close()
         mixed = mixed_case(cfg, st, args.steps, args.warmup, stream, fp64_ms=ms / args.steps)
@@ -584,6 +630,8 @@ def main():
                               "pressure FFT+TDMA, projection, divergence, volume sums")
         if args.mixed_horizon > 0:
             horizon = mixed_horizon(cfg, st, args.mixed_horizon, 100, stream)
+        if args.fp64e:
+            fp64e = fp64e_case(cfg, st, args.steps, args.warmup, stream, ms / args.steps)
         del st
         if args.second_workload:
             cfg2 = C.get(args.second_workload)
@@ -616,7 +664,8 @@ def main():
                                      "(the device-side stop rule), which an ncu launch list does not show "
                                      "(FMF_DEVICE_LOOP=0 runs the same kernels from the host)",
                 "clocks": clk, "roofline": roofline, "step_roofline": step_roofline,
-                "cpu_baseline": cpu, "mixed": mixed, "mixed_horizon": horizon, "second_workload": second,
+                "cpu_baseline": cpu, "mixed": mixed, "mixed_horizon": horizon, "fp64_pairs": fp64e,
+                "second_workload": second,
                 "adjoint": adjoint, "adjoint_mixed_forward": adjoint_m}
         print(json.dumps(line), flush=True)
     else:

@@ -5,6 +5,7 @@
 #include <vector>
 
 #include "../../include/fmf_capi.h"
+#include "fused.cuh"
 #include "ops.cuh"
 #include "runtime.cuh"
 
@@ -902,6 +903,24 @@ void fmf_dev_cal_advu_weno5(int ni, int nj, int nk, double dxinv, double dyinv, 
   }
   op::cal_advu_weno5(stream(), Grid(ni, nj, nk), dxinv, dyinv, dzinv, u, v, w, au, av, aw);
   FMF_CUDA(cudaGetLastError());
+}
+// The fused step's WENO5 of one velocity level (cal_advu_weno5.f:1-258 as the fused
+// step evaluates it) in the arithmetic of a context precision: FMF_FP64,
+// FMF_MIXED (FP32) or FMF_FP64E (FP32 pairs); interior cells of adv written.
+int fmf_dev_weno5_fused(int precision, int ni, int nj, int nk, double dxinv, double dyinv, double dzinv,
+                        const double* u, const double* v, const double* w, double* au, double* av, double* aw) {
+  if (!check_grid(ni, nj, nk)) return take_status();
+  if (!u || !v || !w || !au || !av || !aw || precision < FMF_FP64 || precision > FMF_FP64E) return FMF_ERR_ARG;
+  const Grid g(ni, nj, nk);
+  float2* split = nullptr;
+  if (precision != FMF_FP64) {
+    split = (float2*)scratch(sizeof(float2) * 3 * g.n, 6);
+    if (!split) return take_status();
+  }
+  double* adv[3] = {au, av, aw};
+  fused::weno5_one(stream(), g, dxinv, dyinv, dzinv, u, v, w, adv, precision, split);
+  FMF_CUDA(cudaGetLastError());
+  return take_status();
 }
 void fmf_dev_bnd_periodic(int ni, int nj, int nk, double* qk) {
   if (!check_grid(ni, nj, nk)) return;

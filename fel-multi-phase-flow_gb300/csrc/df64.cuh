@@ -1,0 +1,163 @@
+// df64.cuh -- FP32-pair ("double-float") arithmetic for the FP64-accurate step on
+// GB300's FP32 pipe.
+//
+// GB300 executes FP64 at 2 operations per clock per SM against 128 for FP32, so a
+// stencil that needs FP64 accuracy runs faster as a few FP32 operations per FP64
+// one.  A value is the unevaluated sum h + l of two floats (|l| <= ulp(h)/2 after
+// renormalisation), about 49 significant bits, with float's exponent range.  The
+// error-free transformations are the published ones:
+//  * two_sum: Knuth, TAOCP vol. 2, 4.2.2 (Theorem B): s + e = a + b exactly, six
+//    additions, no ordering condition;
+//  * fast_two_sum: Dekker 1971 ("A floating-point technique for extending the
+//    available precision"): s + e = a + b exactly when exponent(a) >= exponent(b);
+//  * two_prod: with a fused multiply-add, e = fma(a, b, -p) is the exact error of
+//    p = a * b (Ogita, Rump, Oishi 2005, "Accurate sum and dot product", Alg. 3.5);
+// and the pair operations built from them follow Hida, Li, Bailey 2001 ("Algorithms
+// for quad-double precision floating point arithmetic", the double-double "sloppy"
+// addition and the FMA product).  Every float operation goes through an explicitly
+// rounded intrinsic, so the compiler cannot contract a product into a following
+// addition and break an error-free transformation.
+//
+// The header is also compiled by a host C++ compiler (without multiply-add
+// contraction) to check the operations against long double on the CPU.
+#pragma once
+
+#include <cstdint>
+#include <cstring>
+
+#if defined(__CUDACC__)
+#define DF_FN __host__ __device__ __forceinline__
+#else
+#define DF_FN inline
+#endif
+
+namespace fmf {
+namespace df {
+
+struct D {
+  float h, l;
+};
+
+DF_FN float fadd(float a, float b) {
+#if defined(__CUDA_ARCH__)
+  return __fadd_rn(a, b);
+#else
+  return a + b;
+#endif
+}
+DF_FN float fsub(float a, float b) {
+#if defined(__CUDA_ARCH__)
+  return __fsub_rn(a, b);
+#else
+  return a - b;
+#endif
+}
+DF_FN float fmul(float a, float b) {
+#if defined(__CUDA_ARCH__)
+  return __fmul_rn(a, b);
+#else
+  return a * b;
+#endif
+}
+DF_FN float ffma(float a, float b, float c) {
+#if defined(__CUDA_ARCH__)
+  return __fmaf_rn(a, b, c);
+#else
+  return __builtin_fmaf(a, b, c);
+#endif
+}
+DF_FN uint32_t fbits(float a) {
+#if defined(__CUDA_ARCH__)
+  return __float_as_uint(a);
+#else
+  uint32_t u;
+  std::memcpy(&u, &a, 4);
+  return u;
+#endif
+}
+DF_FN float bitsf(uint32_t u) {
+#if defined(__CUDA_ARCH__)
+  return __uint_as_float(u);
+#else
+  float a;
+  std::memcpy(&a, &u, 4);
+  return a;
+#endif
+}
+// 2^k as a float, for -126 <= k <= 127
+DF_FN float pow2f(int k) { return bitsf((uint32_t)(k + 127) << 23); }
+// biased exponent field of a float (0: zero or subnormal)
+DF_FN int fexp(float a) { return (int)((fbits(a) >> 23) & 0xffu); }
+
+DF_FN D two_sum(float a, float b) {
+  const float s = fadd(a, b);
+  const float bb = fsub(s, a);
+  const float e = fadd(fsub(a, fsub(s, bb)), fsub(b, bb));
+  return {s, e};
+}
+DF_FN D fast_two_sum(float a, float b) {
+  const float s = fadd(a, b);
+  return {s, fsub(b, fsub(s, a))};
+}
+DF_FN D neg(D x) { return {-x.h, -x.l}; }
+// sloppy addition: absolute error about 2^-48 (|x| + |y|)
+DF_FN D add(D x, D y) {
+  const D s = two_sum(x.h, y.h);
+  return fast_two_sum(s.h, fadd(s.l, fadd(x.l, y.l)));
+}
+DF_FN D sub(D x, D y) { return add(x, neg(y)); }
+DF_FN D mul(D x, D y) {
+  const float p = fmul(x.h, y.h);
+  float e = ffma(x.h, y.h, -p);
+  e = ffma(x.h, y.l, e);
+  e = ffma(x.l, y.h, e);
+  return fast_two_sum(p, e);
+}
+// times a float (exact small integers such as 3, 7, 11 in the stencils)
+DF_FN D mulf(D x, float f) {
+  const float p = fmul(x.h, f);
+  float e = ffma(x.h, f, -p);
+  e = ffma(x.l, f, e);
+  return fast_two_sum(p, e);
+}
+DF_FN D sqr(D x) {
+  const float p = fmul(x.h, x.h);
+  float e = ffma(x.h, x.h, -p);
+  e = ffma(fadd(x.h, x.h), x.l, e);
+  return fast_two_sum(p, e);
+}
+// times a power of two (exact while both parts stay normal floats)
+DF_FN D scale(D x, float p2) { return {fmul(x.h, p2), fmul(x.l, p2)}; }
+
+// float reciprocal to about one ulp: the hardware approximation refined by one
+// Newton-Raphson step r + r (1 - d r) (on the host, the IEEE quotient)
+DF_FN float recipf(float d) {
+#if defined(__CUDA_ARCH__)
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(d));
+  const float e = ffma(-d, r, 1.0f);
+  return ffma(r, e, r);
+#else
+  return 1.0f / d;
+#endif
+}
+// n / d for a normal d: the float quotient q1 = n.h / d.h and one correction from
+// the pair residual n - q1 d, relative error about 2^-46
+DF_FN D div(D n, D d) {
+  const float r = recipf(d.h);
+  const float q1 = fmul(n.h, r);
+  const D p = mulf(d, q1);  // q1 d
+  // n - q1 d: n.h - p.h is exact (the two agree to a few ulps)
+  const float rem = fsub(fadd(fsub(n.h, p.h), n.l), p.l);
+  const float q2 = fmul(rem, r);
+  return fast_two_sum(q1, q2);
+}
+
+// A pair from a double, on the host (constants): h = (float)v, l = (float)(v - h)
+DF_FN D from_double_host(double v) {
+  const float h = (float)v;
+  return {h, (float)(v - (double)h)};
+}
+
+}  // namespace df
+}  // namespace fmf

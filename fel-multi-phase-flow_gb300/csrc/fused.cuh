@@ -9,21 +9,22 @@ namespace fmf {
 namespace fused {
 
 // cal_advu_weno5 of (u, v, w) into adv and of (uo, vo, wo) into advo, interior
-// cells.  fp32: FP32 arithmetic on the split pairs (hi, lo) of the six fields,
-// written into `split` (6 n float2) first.
+// cells.  prec 0: FP64; 1: FP32 arithmetic on the split pairs (hi, lo) of the six
+// fields, written into `split` (6 n float2) first; 2: FP32-pair arithmetic on the
+// same pairs (about 2^-42 of the stencil's values: the FP64-accurate step).
 void weno5_both(cudaStream_t s, const Grid& g, double dxi, double dyi, double dzi, const double* u,
                 const double* v, const double* w, const double* uo, const double* vo, const double* wo,
-                double* const* adv, double* const* advo, bool fp32 = false, float2* split = nullptr);
-// cal_advu_weno5 of (u, v, w) alone into adv (fp32: split pairs of 3 fields, 3 n float2)
+                double* const* adv, double* const* advo, int prec = 0, float2* split = nullptr);
+// cal_advu_weno5 of (u, v, w) alone into adv (prec 1, 2: split pairs of 3 fields, 3 n float2)
 void weno5_one(cudaStream_t s, const Grid& g, double dxi, double dyi, double dzi, const double* u, const double* v,
-               const double* w, double* const* adv, bool fp32 = false, float2* split = nullptr);
+               const double* w, double* const* adv, int prec = 0, float2* split = nullptr);
 // the split pairs (hi, lo) of three fields (field f at out[f n ..]; hi + lo = q to
 // about 2^-48), as the FP32 WENO5 reads them
 void split3(cudaStream_t s, const Grid& g, const double* a, const double* b, const double* c, float2* out);
 // both levels, the second (uo, vo, wo into advo) skipped on the device where *keep != 0
 void weno5_keep(cudaStream_t s, const Grid& g, double dxi, double dyi, double dzi, const double* u, const double* v,
                 const double* w, const double* uo, const double* vo, const double* wo, double* const* adv,
-                double* const* advo, const int* keep, bool fp32 = false, float2* split = nullptr);
+                double* const* advo, const int* keep, int prec = 0, float2* split = nullptr);
 
 // cal_grad_p2a (the vertex gradients of q at (i+1/2, j+1/2, k+1/2), i, j, k in
 // -2..n+2) in fewer FP64 operations than the reference's order

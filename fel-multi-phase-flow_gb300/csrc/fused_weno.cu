@@ -14,6 +14,7 @@
 #include "../../include/fmf_capi.h"
 #include "fused.cuh"
 #include "recip.cuh"
+#include "weno5_df.cuh"
 
 namespace fmf {
 namespace fused {
@@ -87,28 +88,11 @@ __device__ __forceinline__ double wdir(const double* __restrict__ q, long c, lon
 // indicators are 0 (data exactly linear in float: the quotient is then d2, the
 // reference's limit); the upper keeps eps * d2 finite.  Differences below 2^-100
 // (a flat stencil) give 0.
-// The pair (hi, lo) of q from its bits, without FP64-pipe instructions: hi is q's
-// significand cut to float's 24 bits (toward zero), lo the 29 bits below them as
-// a float (rounded to 24 of them), so hi + lo = q to about 2^-48 of q while lo is
-// a normal float (|q| above about 2^-97; below that lo is subnormal and the pair
-// holds q to 2^-149 absolute).  Magnitudes below 2^-126 give (0, 0); above
-// float's range (and inf, NaN) the float conversion of q and lo = 0.
+// The pair (hi, lo) of q from its bits, without FP64-pipe instructions (df::split_double:
+// hi + lo holds q to about 2^-48 of q)
 __device__ __forceinline__ float2 split_pair(double q) {
-  const long long b = __double_as_longlong(q);
-  const int hb = (int)(b >> 32);
-  const unsigned lb = (unsigned)b;
-  const int e = (hb >> 20) & 0x7ff;
-  const unsigned sg = (unsigned)hb & 0x80000000u;
-  if (e < 897) return make_float2(__uint_as_float(sg), __uint_as_float(sg));
-  if (e > 1150) return make_float2((float)q, 0.0f);
-  const float hi = __uint_as_float(sg | ((unsigned)(e - 896) << 23) | (((unsigned)hb & 0xfffffu) << 3) | (lb >> 29));
-  // q - hi = (low 29 bits) 2^(e - 1075), same sign as q.  The power of two is a
-  // normal float for e >= 949; below that it is applied as 2^-64 2^(e - 1011), both
-  // normal, so lo keeps its bits until the product itself leaves float's range
-  const float L = (float)(lb & 0x1fffffffu);
-  float lo = e >= 949 ? L * __uint_as_float((unsigned)(e - 948) << 23)
-                      : (L * 0x1p-64f) * __uint_as_float((unsigned)(e - 884) << 23);
-  return make_float2(hi, sg ? -lo : lo);
+  const df::D d = df::split_double(q);
+  return make_float2(d.h, d.l);
 }
 struct SplitSrc {
   const double* f[6];
@@ -212,6 +196,77 @@ __global__ void __launch_bounds__(128) k_weno2_f32(Grid g, int nlev, const int* 
   }
 }
 
+// A float as a double from its bits (no FP64-pipe conversion): normal floats and
+// zeros exactly by their fields; subnormals, infinities and NaN by the conversion
+__device__ __forceinline__ double f2d(float f) {
+  const unsigned b = __float_as_uint(f);
+  const unsigned e = (b >> 23) & 0xffu;
+  const unsigned long long sg = (unsigned long long)(b & 0x80000000u) << 32;
+  if ((b << 1) == 0) return __longlong_as_double((long long)sg);
+  if (e == 0 || e == 255) return (double)f;
+  return __longlong_as_double(
+      (long long)(sg | ((unsigned long long)(e + 896) << 52) | ((unsigned long long)(b & 0x7fffffu) << 29)));
+}
+// One direction of the FP64-accurate step's WENO5 (df::wdir_core) on the split
+// pairs of q; vsum as a pair
+__device__ __forceinline__ df::D wdir_df(const float2* __restrict__ q, long c, long S, df::D vsum, df::D kx) {
+  if (vsum.h == 0.0f) return {0.0f, 0.0f};
+  const long st = vsum.h > 0.0f ? S : -S;
+  const float2* p = q + c - 3 * st;
+  df::D w[6];
+#pragma unroll
+  for (int t = 0; t < 6; ++t) {
+    const float2 v = __ldg(p + t * st);
+    w[t] = {v.x, v.y};
+  }
+  return df::wdir_core(w, vsum, kx);
+}
+// The FP64-accurate step's WENO5 of one or both levels (as k_weno2) in FP32-pair
+// arithmetic: sp holds the split pairs of u, v, w (then uo, vo, wo); each velocity
+// sum and derivative is a pair, the three derivatives of a component are summed as
+// pairs and the sum is rounded to a double once.
+__global__ void __launch_bounds__(128) k_weno2_df(Grid g, int nlev, const int* __restrict__ keep, df::D kx,
+                                                  df::D ky, df::D kz, const float2* __restrict__ sp,
+                                                  double* __restrict__ au, double* __restrict__ av,
+                                                  double* __restrict__ aw, double* __restrict__ auo,
+                                                  double* __restrict__ avo, double* __restrict__ awo) {
+  using df::add;
+  const int i = 1 + (int)(blockIdx.x * blockDim.x + threadIdx.x);
+  const int j = 1 + (int)(blockIdx.y * blockDim.y + threadIdx.y);
+  const int k = 1 + (int)blockIdx.z;
+  if (i > g.ni || j > g.nj) return;
+  const long X = 1, Y = g.sy, Z = g.sz;
+  const long c = g.at(i, j, k);
+#pragma unroll 1
+  for (int lev = 0; lev < nlev; ++lev) {
+    if (lev == 1 && keep && *keep) break;
+    const float2* U = sp + (long)(3 * lev) * g.n;
+    const float2* V = U + g.n;
+    const float2* W = V + g.n;
+    auto h = [](const float2* a, long o) {
+      const float2 v = __ldg(a + o);
+      return df::D{v.x, v.y};
+    };
+    auto out = [](df::D a) { return f2d(a.h) + f2d(a.l); };
+    const df::D u0 = h(U, c), uxm = h(U, c - X), uxp = h(U, c + X);
+    const df::D v0 = h(V, c), vym = h(V, c - Y), vyp = h(V, c + Y);
+    const df::D w0 = h(W, c), wzm = h(W, c - Z), wzp = h(W, c + Z);
+    df::D a;
+    a = wdir_df(U, c, X, add(add(uxm, u0), add(u0, uxp)), kx);
+    a = add(a, wdir_df(U, c, Y, add(add(vym, h(V, c + X - Y)), add(v0, h(V, c + X))), ky));
+    a = add(a, wdir_df(U, c, Z, add(add(wzm, h(W, c + X - Z)), add(w0, h(W, c + X))), kz));
+    (lev ? auo : au)[c] = out(a);
+    a = wdir_df(V, c, X, add(add(uxm, h(U, c - X + Y)), add(u0, h(U, c + Y))), kx);
+    a = add(a, wdir_df(V, c, Y, add(add(vym, v0), add(v0, vyp)), ky));
+    a = add(a, wdir_df(V, c, Z, add(add(wzm, h(W, c + Y - Z)), add(w0, h(W, c + Y))), kz));
+    (lev ? avo : av)[c] = out(a);
+    a = wdir_df(W, c, X, add(add(uxm, h(U, c - X + Z)), add(u0, h(U, c + Z))), kx);
+    a = add(a, wdir_df(W, c, Y, add(add(vym, h(V, c - Y + Z)), add(v0, h(V, c + Z))), ky));
+    a = add(a, wdir_df(W, c, Z, add(add(wzm, w0), add(w0, wzp)), kz));
+    (lev ? awo : aw)[c] = out(a);
+  }
+}
+
 __global__ void __launch_bounds__(128) k_weno2(Grid g, int nlev, const int* __restrict__ keep, double dxi,
                                                double dyi, double dzi,
                                                const double* __restrict__ u,
@@ -259,16 +314,17 @@ __global__ void __launch_bounds__(128) k_weno2(Grid g, int nlev, const int* __re
 
 // One level (nlev = 1: u, v, w into adv) or both (nlev = 2: uo, vo, wo into advo as
 // well); only interior cells are written (the fused step never reads the halo of
-// the advection terms, which cal_advu_weno5.f:44-52 sets to zero).  The FP32
-// variant first writes the split pairs of the 3 nlev fields into `split`.
+// the advection terms, which cal_advu_weno5.f:44-52 sets to zero).  prec: 0 FP64,
+// 1 FP32, 2 FP32 pairs; the last two first write the split pairs of the 3 nlev
+// fields into `split`.
 static void weno5_levels(cudaStream_t s, const Grid& g, int nlev, double dxi, double dyi, double dzi,
                          const double* u, const double* v, const double* w, const double* uo, const double* vo,
-                         const double* wo, double* const* adv, double* const* advo, bool fp32, float2* split,
+                         const double* wo, double* const* adv, double* const* advo, int prec, float2* split,
                          const int* keep = nullptr) {
   dim3 b(32, 4, 1);
   dim3 gr((unsigned)((g.ni + 31) / 32), (unsigned)((g.nj + 3) / 4), (unsigned)g.nk);
   double* const ao[3] = {advo ? advo[0] : nullptr, advo ? advo[1] : nullptr, advo ? advo[2] : nullptr};
-  if (fp32) {
+  if (prec == 1 || prec == 2) {
     if (!split) {
       set_status(FMF_ERR_ARG);
       return;
@@ -278,9 +334,18 @@ static void weno5_levels(cudaStream_t s, const Grid& g, int nlev, double dxi, do
       k_split<6><<<152 * 8, 256, 0, s>>>(g.n, src, split, keep);
     else
       k_split<3><<<152 * 8, 256, 0, s>>>(g.n, src, split, nullptr);
-    k_weno2_f32<<<gr, b, 0, s>>>(g, nlev, keep, (float)(dxi / 24.0), (float)(dyi / 24.0), (float)(dzi / 24.0),
-                                 split, adv[0], adv[1], adv[2], ao[0], ao[1], ao[2]);
+    if (prec == 1)
+      k_weno2_f32<<<gr, b, 0, s>>>(g, nlev, keep, (float)(dxi / 24.0), (float)(dyi / 24.0), (float)(dzi / 24.0),
+                                   split, adv[0], adv[1], adv[2], ao[0], ao[1], ao[2]);
+    else
+      k_weno2_df<<<gr, b, 0, s>>>(g, nlev, keep, df::from_double_host(dxi / 24.0), df::from_double_host(dyi / 24.0),
+                                  df::from_double_host(dzi / 24.0), split, adv[0], adv[1], adv[2], ao[0], ao[1],
+                                  ao[2]);
     count_launch(2);
+    return;
+  }
+  if (prec != 0) {
+    set_status(FMF_ERR_ARG);
     return;
   }
   k_weno2<<<gr, b, 0, s>>>(g, nlev, keep, dxi, dyi, dzi, u, v, w, uo, vo, wo, adv[0], adv[1], adv[2], ao[0], ao[1],
@@ -290,13 +355,13 @@ static void weno5_levels(cudaStream_t s, const Grid& g, int nlev, double dxi, do
 
 void weno5_both(cudaStream_t s, const Grid& g, double dxi, double dyi, double dzi, const double* u,
                 const double* v, const double* w, const double* uo, const double* vo, const double* wo,
-                double* const* adv, double* const* advo, bool fp32, float2* split) {
-  weno5_levels(s, g, 2, dxi, dyi, dzi, u, v, w, uo, vo, wo, adv, advo, fp32, split);
+                double* const* adv, double* const* advo, int prec, float2* split) {
+  weno5_levels(s, g, 2, dxi, dyi, dzi, u, v, w, uo, vo, wo, adv, advo, prec, split);
 }
 
 void weno5_one(cudaStream_t s, const Grid& g, double dxi, double dyi, double dzi, const double* u, const double* v,
-               const double* w, double* const* adv, bool fp32, float2* split) {
-  weno5_levels(s, g, 1, dxi, dyi, dzi, u, v, w, nullptr, nullptr, nullptr, adv, nullptr, fp32, split);
+               const double* w, double* const* adv, int prec, float2* split) {
+  weno5_levels(s, g, 1, dxi, dyi, dzi, u, v, w, nullptr, nullptr, nullptr, adv, nullptr, prec, split);
 }
 void split3(cudaStream_t s, const Grid& g, const double* a, const double* b, const double* c, float2* out) {
   const SplitSrc src{{a, b, c, nullptr, nullptr, nullptr}};
@@ -306,8 +371,8 @@ void split3(cudaStream_t s, const Grid& g, const double* a, const double* b, con
 
 void weno5_keep(cudaStream_t s, const Grid& g, double dxi, double dyi, double dzi, const double* u, const double* v,
                 const double* w, const double* uo, const double* vo, const double* wo, double* const* adv,
-                double* const* advo, const int* keep, bool fp32, float2* split) {
-  weno5_levels(s, g, 2, dxi, dyi, dzi, u, v, w, uo, vo, wo, adv, advo, fp32, split, keep);
+                double* const* advo, const int* keep, int prec, float2* split) {
+  weno5_levels(s, g, 2, dxi, dyi, dzi, u, v, w, uo, vo, wo, adv, advo, prec, split, keep);
 }
 
 // n doubles of both signs spread over magnitudes 2^-96 .. 2^127 with pseudo-random

@@ -89,6 +89,7 @@ struct fmf_ctx {
   double* red;  // small reduction outputs
   int* band;    // MTHINC band-cell list, then its length
   bool mixed = false;        // precision == FMF_MIXED
+  int wprec = 0;             // WENO5 arithmetic: 0 FP64, 1 FP32 (FMF_MIXED), 2 FP32 pairs (FMF_FP64E)
   fused::RefineBufs rb{};    // FP32 buffers of the mixed-precision viscous solve
   float2* wsplit = nullptr;  // mixed: split pairs of u, v, w, uo, vo, wo for the FP32 WENO5 (6 n)
   double* host_err = nullptr;  // pinned
@@ -239,7 +240,8 @@ int fmf_ctx_create(const fmf_params* prm, fmf_ctx** out) {
   if (!prm || !out) return FMF_ERR_ARG;
   auto p2 = [](int n) { return n >= 4 && (n & (n - 1)) == 0; };
   if (!p2(prm->ni) || !p2(prm->nj) || !p2(prm->nk) || prm->ni < 16) return FMF_ERR_ARG;
-  if (prm->precision != FMF_FP64 && prm->precision != FMF_MIXED) return FMF_ERR_ARG;
+  if (prm->precision != FMF_FP64 && prm->precision != FMF_MIXED && prm->precision != FMF_FP64E)
+    return FMF_ERR_ARG;
   fmf_ctx* c = new fmf_ctx();
   c->prm = *prm;
   if (const char* e = std::getenv("FMF_GRAPHS")) c->graphs = std::atoi(e) != 0;
@@ -302,6 +304,8 @@ int fmf_ctx_create(const fmf_params* prm, fmf_ctx** out) {
     rb.gz = allocf(c, fused::refine_floats(c->g, 2));
     c->wsplit = (float2*)alloc(c, 6 * n);
   }
+  c->wprec = c->mixed ? 1 : prm->precision == FMF_FP64E ? 2 : 0;
+  if (c->wprec == 2) c->wsplit = (float2*)alloc(c, 6 * n);
   {
     const long nb = (long)(prm->ni + 2) * (prm->nj + 2) * (prm->nk + 2) + 1;
     c->band = (int*)alloc(c, (nb + 1) / 2);
@@ -548,11 +552,11 @@ static void seg_pre2(fmf_ctx* c) {
   // :532-541 (advo carried over from the previous step where the state continues)
   if (c->verify)
     fused::weno5_keep(s, g, dxinv, dyinv, dzinv, c->u, c->v, c->w, c->uo, c->vo, c->wo, c->adv, c->advo, c->same,
-                      c->mixed, c->wsplit);
+                      c->wprec, c->wsplit);
   else if (c->cont)
-    fused::weno5_one(s, g, dxinv, dyinv, dzinv, c->u, c->v, c->w, c->adv, c->mixed, c->wsplit);
+    fused::weno5_one(s, g, dxinv, dyinv, dzinv, c->u, c->v, c->w, c->adv, c->wprec, c->wsplit);
   else
-    fused::weno5_both(s, g, dxinv, dyinv, dzinv, c->u, c->v, c->w, c->uo, c->vo, c->wo, c->adv, c->advo, c->mixed,
+    fused::weno5_both(s, g, dxinv, dyinv, dzinv, c->u, c->v, c->w, c->uo, c->vo, c->wo, c->adv, c->advo, c->wprec,
                       c->wsplit);
   op::calphat(s, g, c->p, c->po, c->phat);
   op::cal_grad_prs(s, g, dxinv, dyinv, dzinv, c->phat, c->prs[0], c->prs[1], c->prs[2]);
@@ -846,8 +850,8 @@ int fmf_ctx_time_stage(fmf_ctx* c, int stage, int reps, float* ms) {
   auto run = [&]() {
     switch (stage) {
       case 0:
-        fused::weno5_both(s, g, dxinv, dyinv, dzinv, c->u, c->v, c->w, c->uo, c->vo, c->wo, c->adv, c->advo, mixed,
-                          c->wsplit);
+        fused::weno5_both(s, g, dxinv, dyinv, dzinv, c->u, c->v, c->w, c->uo, c->vo, c->wo, c->adv, c->advo,
+                          c->wprec, c->wsplit);
         break;
       case 1:
         if (mixed)
@@ -866,7 +870,7 @@ int fmf_ctx_time_stage(fmf_ctx* c, int stage, int reps, float* ms) {
                              c->band + (long)(g.ni + 2) * (g.nj + 2) * (g.nk + 2), mixed);
         break;
       case 4:  // writes adv only: the carried advo stays valid
-        fused::weno5_one(s, g, dxinv, dyinv, dzinv, c->u, c->v, c->w, c->adv, mixed, c->wsplit);
+        fused::weno5_one(s, g, dxinv, dyinv, dzinv, c->u, c->v, c->w, c->adv, c->wprec, c->wsplit);
         break;
     }
   };

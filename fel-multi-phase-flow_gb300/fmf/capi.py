@@ -18,7 +18,7 @@ from .build import LIB
 
 _lib = None
 
-FMF_FP64, FMF_MIXED = 0, 1
+FMF_FP64, FMF_MIXED, FMF_FP64E = 0, 1, 2
 FMF_RESIDENT, FMF_COHERENT = 0, 1
 FMF_ERR_ITER_CAP = 4
 
@@ -88,6 +88,8 @@ def load(path: str | None = None):
     L.fmf_interface_lower.restype = dp
     L.fmf_interface_lower.argtypes = [ip, ip, ip, vp, dp, dp]
     L.fmf_set_stream.argtypes = [vp]
+    L.fmf_dev_weno5_fused.argtypes = [ip, ip, ip, ip, dp, dp, dp, vp, vp, vp, vp, vp, vp]
+    L.fmf_dev_weno5_fused.restype = ip
     for name in ("fmf_sync_to_host", "fmf_sync_to_device", "fmf_forget"):
         getattr(L, name).argtypes = [vp]
     _lib = L

@@ -339,6 +339,11 @@ int fmf_cal_av_noalloc(int ni, int nj, int nk, const double* q, double* av, void
 void fmf_dev_cal_advu_weno5(int ni, int nj, int nk, double dxinv, double dyinv, double dzinv,
                             const double* u, const double* v, const double* w, double* adv_u,
                             double* adv_v, double* adv_w);
+/* the fused step's WENO5 of one velocity level in a context precision (FMF_FP64,
+ * FMF_MIXED: FP32, FMF_FP64E: FP32 pairs), interior cells; returns a status */
+int fmf_dev_weno5_fused(int precision, int ni, int nj, int nk, double dxinv, double dyinv,
+                        double dzinv, const double* u, const double* v, const double* w,
+                        double* adv_u, double* adv_v, double* adv_w);
 void fmf_dev_bnd_periodic(int ni, int nj, int nk, double* qk);
 /* Monitors on device arrays, results left in device memory (nothing is read back,
  * no host synchronisation):
@@ -368,9 +373,16 @@ typedef struct {
   double rhol, rhog, rmul, rmug;  /* phi=0 fluid (l) and phi=1 fluid (g) */
   double sigma, uwall, grvb, grvp, bet_mthinc;
   int harmonic;                   /* 0: cal_arith_coef_vis (as main.f90 calls it), 1: harmonic */
-  int precision;                  /* FMF_FP64 or FMF_MIXED */
+  int precision;                  /* FMF_FP64, FMF_MIXED or FMF_FP64E */
 } fmf_params;
-enum { FMF_FP64 = 0, FMF_MIXED = 1 };
+/* FMF_FP64: every operation in FP64.  FMF_MIXED: FP32 WENO5, MTHINC, CSF and viscous
+ * corrections (errors about 1e-6).  FMF_FP64E: the FP64 step with its WENO5
+ * advection in FP32-pair arithmetic (a value is the sum of two floats, about 49
+ * significant bits) on the FP32 pipe; the advection agrees with FP64's to about
+ * 4e-13 of |vel| dxi times the stencil's largest value, and the step with the
+ * oracle within the FP64 step's 1e-10.  Contexts only (fmf_adj_create takes
+ * FMF_FP64 and FMF_MIXED). */
+enum { FMF_FP64 = 0, FMF_MIXED = 1, FMF_FP64E = 2 };
 
 typedef struct fmf_ctx fmf_ctx;
 /* state order: u v w uo vo wo p po phi0 phi1 phin0 phin1, each (ni+6)(nj+6)(nk+6) doubles */
