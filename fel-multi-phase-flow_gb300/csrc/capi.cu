@@ -922,6 +922,20 @@ int fmf_dev_weno5_fused(int precision, int ni, int nj, int nk, double dxinv, dou
   FMF_CUDA(cudaGetLastError());
   return take_status();
 }
+// The fused step's CSF force of one volume-fraction field (main.f90:548-567 as the
+// fused step evaluates it: cal_grad_p2a, calrn x4, calrkap, cal_grad_p2uvw, calfst)
+// in the arithmetic of a context precision; interior u, v, w points of f written.
+// Needs ni % 32 == 0 and nj % 8 == 0.
+int fmf_dev_csf_fused(int precision, int ni, int nj, int nk, double dx, double dy, double dz, double rhol,
+                      double rhog, double sigma, const double* phi, double* fu, double* fv, double* fw) {
+  if (!check_grid(ni, nj, nk)) return take_status();
+  const Grid g(ni, nj, nk);
+  if (!phi || !fu || !fv || !fw || precision < FMF_FP64 || precision > FMF_FP64E || !fused::csf_supported(g))
+    return FMF_ERR_ARG;
+  fused::csf_force(stream(), g, 1.0 / dx, 1.0 / dy, 1.0 / dz, rhol, rhog, sigma, phi, fu, fv, fw, precision);
+  FMF_CUDA(cudaGetLastError());
+  return take_status();
+}
 void fmf_dev_bnd_periodic(int ni, int nj, int nk, double* qk) {
   if (!check_grid(ni, nj, nk)) return;
   if (!qk) {

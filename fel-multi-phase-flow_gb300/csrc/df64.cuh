@@ -153,11 +153,75 @@ DF_FN D div(D n, D d) {
   return fast_two_sum(q1, q2);
 }
 
+// 1/sqrt(s) for a normal positive s: the float estimate r (hardware approximation
+// and one Newton-Raphson step; on the host the IEEE value) corrected once with the
+// pair residual, r + r (1 - s r^2) / 2, relative error about 2^-46
+DF_FN float rsqrtf_(float s) {
+#if defined(__CUDA_ARCH__)
+  float r;
+  asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(s));
+  return fmul(r, ffma(fmul(-0.5f, s), fmul(r, r), 1.5f));
+#else
+  return 1.0f / __builtin_sqrtf(s);
+#endif
+}
+DF_FN D rsqrt(D s) {
+  const float r = rsqrtf_(s.h);
+  const float rr = fmul(r, r);
+  const D t = mul(s, D{rr, ffma(r, r, -rr)});  // s r^2 (r^2 exact as a pair)
+  const float e = fsub(fsub(1.0f, t.h), t.l);
+  return fast_two_sum(r, fmul(fmul(0.5f, r), e));
+}
+
+// The pair (h, l) of a double from its bits, without FP64 instructions: h is q's
+// significand cut to float's 24 bits (toward zero), l the 29 bits below them as a
+// float (rounded to 24), so h + l = q to about 2^-48 of q while l is a normal float
+// (|q| above about 2^-97; below that l is subnormal and the pair holds q to 2^-149
+// absolute).  Magnitudes below 2^-126 give (0, 0); above float's range (and inf,
+// NaN) the float conversion of q and l = 0.
+DF_FN D split_double(double q) {
+  uint64_t b;
+#if defined(__CUDA_ARCH__)
+  b = (uint64_t)__double_as_longlong(q);
+#else
+  std::memcpy(&b, &q, 8);
+#endif
+  const uint32_t hb = (uint32_t)(b >> 32);
+  const uint32_t lb = (uint32_t)b;
+  const int e = (int)((hb >> 20) & 0x7ffu);
+  const uint32_t sg = hb & 0x80000000u;
+  if (e < 897) return {bitsf(sg), bitsf(sg)};
+  if (e > 1150) return {(float)q, 0.0f};
+  const float hi = bitsf(sg | ((uint32_t)(e - 896) << 23) | ((hb & 0xfffffu) << 3) | (lb >> 29));
+  // q - hi = (low 29 bits) 2^(e - 1075), same sign as q.  The power of two is a
+  // normal float for e >= 949; below that it is applied as 2^-64 2^(e - 1011)
+  const float L = (float)(lb & 0x1fffffffu);
+  const float lo = e >= 949 ? fmul(L, bitsf((uint32_t)(e - 948) << 23))
+                            : fmul(fmul(L, 0x1p-64f), bitsf((uint32_t)(e - 884) << 23));
+  return {hi, sg ? -lo : lo};
+}
+
 // A pair from a double, on the host (constants): h = (float)v, l = (float)(v - h)
 DF_FN D from_double_host(double v) {
   const float h = (float)v;
   return {h, (float)(v - (double)h)};
 }
+
+#if defined(__CUDACC__)
+// A float as a double from its bits (no FP64-pipe conversion): normal floats and
+// zeros exactly by their fields; subnormals, infinities and NaN by the conversion
+__device__ __forceinline__ double f2d(float f) {
+  const unsigned b = __float_as_uint(f);
+  const unsigned e = (b >> 23) & 0xffu;
+  const unsigned long long sg = (unsigned long long)(b & 0x80000000u) << 32;
+  if ((b << 1) == 0) return __longlong_as_double((long long)sg);
+  if (e == 0 || e == 255) return (double)f;
+  return __longlong_as_double(
+      (long long)(sg | ((unsigned long long)(e + 896) << 52) | ((unsigned long long)(b & 0x7fffffu) << 29)));
+}
+// a pair rounded to a double (one FP64 addition)
+__device__ __forceinline__ double to_double(D a) { return f2d(a.h) + f2d(a.l); }
+#endif
 
 }  // namespace df
 }  // namespace fmf

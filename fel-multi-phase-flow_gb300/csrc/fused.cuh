@@ -43,12 +43,13 @@ void mthinc_fluxes(cudaStream_t s, const Grid& g, double dxinv, double dyinv, do
 
 // CSF force of one field on the interior u, v, w points (fu/fv/fw), replacing
 // cal_grad_p2a + calrn x4 + calrkap + cal_grad_p2uvw + calfst; needs ni % 32 == 0
-// and nj % 8 == 0 (csf_supported).  fp32: normals and curvature in FP32.  kap
+// and nj % 8 == 0 (csf_supported).  prec 0: FP64; 1: normals and curvature in
+// FP32; 2: in FP32 pairs (the FP64-accurate step).  kap
 // (optional, 3 arrays of n): the curvatures at the interior u, v, w points.
 bool csf_supported(const Grid& g);
 // skip (optional): a device int; where it is nonzero the kernel writes nothing
 void csf_force(cudaStream_t s, const Grid& g, double dxinv, double dyinv, double dzinv, double rhol, double rhog,
-               double sigma, const double* phi, double* fu, double* fv, double* fw, bool fp32 = false,
+               double sigma, const double* phi, double* fu, double* fv, double* fw, int prec = 0,
                double* kap = nullptr, const int* skip = nullptr);
 
 // The explicit viscous term (calsij, cal_arith_tau, cal_div_tensor) at the interior

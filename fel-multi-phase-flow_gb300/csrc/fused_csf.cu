@@ -16,13 +16,16 @@
 // shared memory; H(k+1) = G(k)+G(k+1) gives both n12(k+1) and, summed over the
 // four surrounding (i,j), npp(k+1).  Each normal is formed once per block.
 //
-// Two instantiations: R = double (the FP64 step; phi read straight from global
-// memory) and R = float (the mixed-precision step; each phi plane is converted once
+// Three instantiations: R = double (the FP64 step; phi read straight from global
+// memory), R = float (the mixed-precision step; each phi plane is converted once
 // into a shared-memory ring of three planes, everything after that is FP32 and the
-// three forces are widened to double on the store).
+// three forces are widened to double on the store) and R = Pr, an FP32 pair (the
+// FP64-accurate step FMF_FP64E: phi planes split into pairs in the same ring, the
+// arithmetic in FP32-pair operations on the FP32 pipe, the forces rounded to double).
 #include <algorithm>
 #include <type_traits>
 
+#include "df64.cuh"
 #include "fused.cuh"
 #include "recip.cuh"
 
@@ -37,8 +40,21 @@ constexpr int GP = GX * GY, NP = NX * NY;
 constexpr int QX = GX + 1, QY = GY + 1;  // staged phi plane: i in [I0-1, I0+TX+1], j in [J0-1, J0+TY+1]
 constexpr int QP = QX * QY;
 
+// FP32 pair (df64.cuh) with the arithmetic operators the kernel's template uses
+struct Pr {
+  df::D v;
+  Pr() = default;
+  __host__ __device__ Pr(df::D d) : v(d) {}
+  __host__ __device__ explicit Pr(double q) : v(df::split_double(q)) {}
+  __device__ explicit operator double() const { return df::to_double(v); }
+};
+__host__ __device__ __forceinline__ Pr operator+(Pr a, Pr b) { return df::add(a.v, b.v); }
+__host__ __device__ __forceinline__ Pr operator-(Pr a, Pr b) { return df::sub(a.v, b.v); }
+__host__ __device__ __forceinline__ Pr operator*(Pr a, Pr b) { return df::mul(a.v, b.v); }
+__host__ __device__ __forceinline__ Pr operator-(Pr a) { return df::neg(a.v); }
+
 template <class R>
-constexpr bool kStaged = std::is_same<R, float>::value;
+constexpr bool kStaged = !std::is_same<R, double>::value;
 
 template <class R>
 struct CsfP {
@@ -89,6 +105,34 @@ __device__ __forceinline__ void unit(float x, float y, float z, float vs, float*
   o[2] = z * inv;
 }
 
+// FP32 pairs.  Where |v| is below about 2^-50 the squares approach float's normal
+// range, so v and vs are scaled by 2^64 first (exact; N is unchanged); a sum of
+// squares below 2^-126 after that counts as 0 (|v| + vs = vs).
+__device__ __forceinline__ void unit(Pr x, Pr y, Pr z, Pr vs, Pr* o) {
+  using namespace df;
+  D X = x.v, Y = y.v, Z = z.v, V = vs.v;
+  D s = add(add(sqr(X), sqr(Y)), sqr(Z));
+  if (s.h < 0x1p-100f) {
+    const float c = 0x1p64f;
+    X = scale(X, c);
+    Y = scale(Y, c);
+    Z = scale(Z, c);
+    V = scale(V, c);
+    s = add(add(sqr(X), sqr(Y)), sqr(Z));
+  }
+  const float big = fmul(V.h, 1.0e12f);
+  D inv;
+  if (s.h > fmul(big, big))
+    inv = rsqrt(s);
+  else if (fexp(s.h) == 0)
+    inv = div(D{1.0f, 0.0f}, V);
+  else
+    inv = div(D{1.0f, 0.0f}, add(mul(s, rsqrt(s)), V));
+  o[0] = mul(X, inv);
+  o[1] = mul(Y, inv);
+  o[2] = mul(Z, inv);
+}
+
 // vertex gradient at (i+1/2, j+1/2, k+1/2), straight from phi in global memory
 __device__ void grad_plane(const Grid& g, const CsfP<double>& p, const double* __restrict__ phi, int I0, int J0,
                            int k, double (*G)[GP]) {
@@ -119,9 +163,19 @@ __device__ void grad_staged(const CsfP<R>& p, const R* Qa, const R* Qb, R (*G)[G
     const int c = b * QX + a;
     const R q000 = Qa[c], qp00 = Qa[c + 1], q0p0 = Qa[c + QX], qpp0 = Qa[c + QX + 1];
     const R q00p = Qb[c], qp0p = Qb[c + 1], q0pp = Qb[c + QX], qppp = Qb[c + QX + 1];
-    G[0][e] = (-q000 + qp00 - q0p0 + qpp0 - q00p + qp0p - q0pp + qppp) * p.gx;
-    G[1][e] = (-q000 - qp00 + q0p0 + qpp0 - q00p - qp0p + q0pp + qppp) * p.gy;
-    G[2][e] = (-q000 - qp00 - q0p0 - qpp0 + q00p + qp0p + q0pp + qppp) * p.gz;
+    if constexpr (std::is_same<R, Pr>::value) {
+      // the FP64 path's sums and differences of the two planes (15 pair additions)
+      const R s00 = q000 + q00p, sp0 = qp00 + qp0p, s0p = q0p0 + q0pp, spp = qpp0 + qppp;
+      const R d00 = q00p - q000, dp0 = qp0p - qp00, d0p = q0pp - q0p0, dpp = qppp - qpp0;
+      const R ta = spp - s00, tb = sp0 - s0p;
+      G[0][e] = (ta + tb) * p.gx;
+      G[1][e] = (ta - tb) * p.gy;
+      G[2][e] = ((d00 + dp0) + (d0p + dpp)) * p.gz;
+    } else {
+      G[0][e] = (-q000 + qp00 - q0p0 + qpp0 - q00p + qp0p - q0pp + qppp) * p.gx;
+      G[1][e] = (-q000 - qp00 + q0p0 + qpp0 - q00p - qp0p + q0pp + qppp) * p.gy;
+      G[2][e] = (-q000 - qp00 - q0p0 - qpp0 + q00p + qp0p + q0pp + qppp) * p.gz;
+    }
   }
 }
 // phi plane k (i in [I0-1, I0+TX+1], j in [J0-1, J0+TY+1]) into Q, converted to R
@@ -327,10 +381,12 @@ void launch_csf(cudaStream_t s, const Grid& g, double dxinv, double dyinv, doubl
 bool csf_supported(const Grid& g) { return g.ni % TX == 0 && g.nj % TY == 0; }
 
 void csf_force(cudaStream_t s, const Grid& g, double dxinv, double dyinv, double dzinv, double rhol, double rhog,
-               double sigma, const double* phi, double* fu, double* fv, double* fw, bool fp32, double* kap,
+               double sigma, const double* phi, double* fu, double* fv, double* fw, int prec, double* kap,
                const int* skip) {
-  if (fp32)
+  if (prec == 1)
     launch_csf<float>(s, g, dxinv, dyinv, dzinv, rhol, rhog, sigma, phi, fu, fv, fw, kap, skip);
+  else if (prec == 2)
+    launch_csf<Pr>(s, g, dxinv, dyinv, dzinv, rhol, rhog, sigma, phi, fu, fv, fw, kap, skip);
   else
     launch_csf<double>(s, g, dxinv, dyinv, dzinv, rhol, rhog, sigma, phi, fu, fv, fw, kap, skip);
 }

@@ -196,17 +196,6 @@ __global__ void __launch_bounds__(128) k_weno2_f32(Grid g, int nlev, const int* 
   }
 }
 
-// A float as a double from its bits (no FP64-pipe conversion): normal floats and
-// zeros exactly by their fields; subnormals, infinities and NaN by the conversion
-__device__ __forceinline__ double f2d(float f) {
-  const unsigned b = __float_as_uint(f);
-  const unsigned e = (b >> 23) & 0xffu;
-  const unsigned long long sg = (unsigned long long)(b & 0x80000000u) << 32;
-  if ((b << 1) == 0) return __longlong_as_double((long long)sg);
-  if (e == 0 || e == 255) return (double)f;
-  return __longlong_as_double(
-      (long long)(sg | ((unsigned long long)(e + 896) << 52) | ((unsigned long long)(b & 0x7fffffu) << 29)));
-}
 // One direction of the FP64-accurate step's WENO5 (df::wdir_core) on the split
 // pairs of q; vsum as a pair
 __device__ __forceinline__ df::D wdir_df(const float2* __restrict__ q, long c, long S, df::D vsum, df::D kx) {
@@ -247,7 +236,7 @@ __global__ void __launch_bounds__(128) k_weno2_df(Grid g, int nlev, const int* _
       const float2 v = __ldg(a + o);
       return df::D{v.x, v.y};
     };
-    auto out = [](df::D a) { return f2d(a.h) + f2d(a.l); };
+    auto out = [](df::D a) { return df::to_double(a); };
     const df::D u0 = h(U, c), uxm = h(U, c - X), uxp = h(U, c + X);
     const df::D v0 = h(V, c), vym = h(V, c - Y), vyp = h(V, c + Y);
     const df::D w0 = h(W, c), wzm = h(W, c - Z), wzp = h(W, c + Z);

@@ -565,7 +565,7 @@ static void seg_pre2(fmf_ctx* c) {
   // the state continues)
   if (c->verify && fused::csf_supported(g))
     fused::csf_force(s, g, dxinv, dyinv, dzinv, P.rhol, P.rhog, P.sigma, phi1, c->sfst[0], c->sfst[1], c->sfst[2],
-                     c->mixed, nullptr, c->same + 1);
+                     c->wprec, nullptr, c->same + 1);
   else if (!c->cont || c->verify)
     csf_one(c, phi1, c->sfst);
   csf_one(c, phin1, c->sfstn);
@@ -605,7 +605,7 @@ static void csf_one(fmf_ctx* c, const double* phi, double* const* f) {
   const long n = g.n;
   const double dxinv = 1.0 / P.dx, dyinv = 1.0 / P.dy, dzinv = 1.0 / P.dz;
   if (fused::csf_supported(g)) {
-    fused::csf_force(s, g, dxinv, dyinv, dzinv, P.rhol, P.rhog, P.sigma, phi, f[0], f[1], f[2], c->mixed);
+    fused::csf_force(s, g, dxinv, dyinv, dzinv, P.rhol, P.rhog, P.sigma, phi, f[0], f[1], f[2], c->wprec);
     return;
   }
   for (int q = 0; q < 3; ++q) op::fill(s, n, f[q], 0.0);

@@ -32,34 +32,6 @@
 namespace fmf {
 namespace df {
 
-// The pair (h, l) of a double from its bits, without FP64 instructions: h is q's
-// significand cut to float's 24 bits (toward zero), l the 29 bits below them as a
-// float (rounded to 24), so h + l = q to about 2^-48 of q while l is a normal float
-// (|q| above about 2^-97; below that l is subnormal and the pair holds q to 2^-149
-// absolute).  Magnitudes below 2^-126 give (0, 0); above float's range (and inf,
-// NaN) the float conversion of q and l = 0.
-DF_FN D split_double(double q) {
-  uint64_t b;
-#if defined(__CUDA_ARCH__)
-  b = (uint64_t)__double_as_longlong(q);
-#else
-  std::memcpy(&b, &q, 8);
-#endif
-  const uint32_t hb = (uint32_t)(b >> 32);
-  const uint32_t lb = (uint32_t)b;
-  const int e = (int)((hb >> 20) & 0x7ffu);
-  const uint32_t sg = hb & 0x80000000u;
-  if (e < 897) return {bitsf(sg), bitsf(sg)};
-  if (e > 1150) return {(float)q, 0.0f};
-  const float hi = bitsf(sg | ((uint32_t)(e - 896) << 23) | ((hb & 0xfffffu) << 3) | (lb >> 29));
-  // q - hi = (low 29 bits) 2^(e - 1075), same sign as q.  The power of two is a
-  // normal float for e >= 949; below that it is applied as 2^-64 2^(e - 1011)
-  const float L = (float)(lb & 0x1fffffffu);
-  const float lo = e >= 949 ? fmul(L, bitsf((uint32_t)(e - 948) << 23))
-                            : fmul(fmul(L, 0x1p-64f), bitsf((uint32_t)(e - 884) << 23));
-  return {hi, sg ? -lo : lo};
-}
-
 // b - a of two split pairs
 DF_FN D pair_diff(D b, D a) {
   const D s = two_sum(b.h, -a.h);

@@ -90,6 +90,8 @@ def load(path: str | None = None):
     L.fmf_set_stream.argtypes = [vp]
     L.fmf_dev_weno5_fused.argtypes = [ip, ip, ip, ip, dp, dp, dp, vp, vp, vp, vp, vp, vp]
     L.fmf_dev_weno5_fused.restype = ip
+    L.fmf_dev_csf_fused.argtypes = [ip, ip, ip, ip, dp, dp, dp, dp, dp, dp, vp, vp, vp, vp]
+    L.fmf_dev_csf_fused.restype = ip
     for name in ("fmf_sync_to_host", "fmf_sync_to_device", "fmf_forget"):
         getattr(L, name).argtypes = [vp]
     _lib = L

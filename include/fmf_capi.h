@@ -344,6 +344,11 @@ void fmf_dev_cal_advu_weno5(int ni, int nj, int nk, double dxinv, double dyinv, 
 int fmf_dev_weno5_fused(int precision, int ni, int nj, int nk, double dxinv, double dyinv,
                         double dzinv, const double* u, const double* v, const double* w,
                         double* adv_u, double* adv_v, double* adv_w);
+/* the fused step's CSF force of one phi field in a context precision, interior u, v,
+ * w points (ni % 32 == 0, nj % 8 == 0); returns a status */
+int fmf_dev_csf_fused(int precision, int ni, int nj, int nk, double dx, double dy, double dz,
+                      double rhol, double rhog, double sigma, const double* phi, double* fu,
+                      double* fv, double* fw);
 void fmf_dev_bnd_periodic(int ni, int nj, int nk, double* qk);
 /* Monitors on device arrays, results left in device memory (nothing is read back,
  * no host synchronisation):

@@ -93,3 +93,51 @@ def test_weno5_pairs_against_fp64(fmf_lib, scale):
         assert m > 0
         err = np.abs(got - ref).max() / m
         assert err <= 1e-12, (c, scale, err)
+
+
+@pytest.mark.parametrize("shape", [(64, 32, 32), (256, 128, 128)])
+def test_csf_pairs_against_fp64(fmf_lib, shape):
+    """fmf_dev_csf_fused in FP32 pairs against FP64: the force of a tanh-profiled
+    sphere (radius a quarter of the domain height, 1.5-cell width, as the sessile
+    drop's initial phi) and of a tilted planar front, whose far field carries
+    gradients down to the end of double's range.  Pairs hold phi to 2^-48, so a
+    vertex gradient g carries an error of about 2^-48 dxi, its normal 2^-48 dxi / g,
+    the curvature dxi times that, and the force C kappa (phi(i+1) - phi(i)) dxi,
+    with C = 2 sigma/(rho_l + rho_g) and a phi difference of about g dx, an error of
+    about 2^-48 C dxi^2 wherever the interface is: each component within 1e-12 of
+    C dxi^2 (the force of a grid-scale curvature on a unit jump), and the sphere's
+    within 1e-11 of its own largest force."""
+    import torch
+
+    ni, nj, nk = shape
+    dx = 1.0 / nj
+    rhol, rhog, sigma = 1000.0, 1.0, 1.0
+    scale = 2.0 * sigma / (rhol + rhog) / dx ** 2
+    pad = (nk + 6, nj + 6, ni + 6)
+    z, y, x = np.meshgrid(np.arange(pad[0]) - 2.5, np.arange(pad[1]) - 2.5, np.arange(pad[2]) - 2.5, indexing="ij")
+    X, Y, Z = x * dx, y * dx, z * dx
+    r = np.sqrt((X - ni * dx / 2) ** 2 + (Y - 0.1) ** 2 + (Z - nk * dx / 2) ** 2)
+    w = 1.5 * dx
+    phis = {"sphere": 0.5 * (1 - np.tanh((r - 0.25) / w)),
+            "front": 0.5 * (1 + np.tanh((0.3 * X + 0.9 * Y - 0.2 * Z - 0.4) / w))}
+    errs = {}
+    for name, phi in phis.items():
+        d = torch.from_numpy(np.ascontiguousarray(phi)).cuda()
+        outs = {}
+        for prec in (capi.FMF_FP64, capi.FMF_FP64E):
+            f = [torch.zeros(pad, dtype=torch.float64, device="cuda") for _ in range(3)]
+            torch.cuda.synchronize()
+            st = capi.lib().fmf_dev_csf_fused(prec, ni, nj, nk, dx, dx, dx, rhol, rhog, sigma, d.data_ptr(),
+                                              *[t.data_ptr() for t in f])
+            assert st == 0, st
+            assert capi.lib().fmf_device_synchronize() == 0
+            outs[prec] = [t.cpu().numpy() for t in f]
+        for c in range(3):
+            ref, got = outs[capi.FMF_FP64][c], outs[capi.FMF_FP64E][c]
+            assert np.isfinite(got).all()
+            e = np.abs(got - ref).max()
+            errs[(name, c)] = (e / scale, e / np.abs(ref).max())
+    for (name, c), (e_scale, e_own) in errs.items():
+        assert e_scale <= 1e-12, errs
+        if name == "sphere":
+            assert e_own <= 1e-11, errs
