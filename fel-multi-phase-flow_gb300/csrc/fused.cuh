@@ -68,7 +68,7 @@ void src_visc_prep(cudaStream_t s, const Grid& g, double dxinv, double dyinv, do
                    const double* const* adv, const double* const* advo, const double* const* prs,
                    const double* const* vis, const double* const* fst, const double* const* fstn, const double* mu,
                    const double* rho, const double* rhon, double* const* E, double* const* AB, const double* l1,
-                   const double* l2, const double* phi, double dy, double* wallc);
+                   const double* l2, const double* phi, double dy, double* wallc, bool pairs = false);
 // the Navier-slip coefficients wallc alone (as src_visc_prep computes them)
 void wall_coef(cudaStream_t s, const Grid& g, double dy, const double* l1, const double* l2, const double* phi,
                double* wallc);

@@ -20,6 +20,7 @@
 // and un = u + d is formed in FP64 at the end.
 #include <cstdlib>
 
+#include "df64.cuh"
 #include "fused.cuh"
 #include "recip.cuh"
 #include "refresh.cuh"
@@ -133,6 +134,60 @@ __global__ void __launch_bounds__(256) k_src_ab(Grid g, VP p, SrcIn in, const do
     const double T = recip_nr(r * p.dtinv + ap * 0.5);
     const double vn = REFINE ? visn_at<2, double>(g, p, c, mu, exy, exz, eyz, in.u, in.v, in.w) : 0.0;
     store(2, 0.5 * T, rsrc(2, in.w, r, 0.0) * T, vn, in.w);
+  }
+}
+
+// The FP64-accurate step (FMF_FP64E): k_src_ab's A and B in FP32-pair arithmetic
+// (each double read split into a pair, A and B rounded to doubles once).  The
+// momentum-factor denominator is grouped as dz2 (e(-Z) + e(0)) + dy2 (e(-Y) + e(0))
+// + 2 dx2 (mu(0) + mu(X)) (and likewise per component), the same sum.
+struct VPS {
+  df::D dtinv, dx2, dy2, dz2, dx2x2, dy2x2, dz2x2, grvb, grvp;
+};
+__global__ void __launch_bounds__(256) k_src_ab_e(Grid g, VPS p, SrcIn in, const double* __restrict__ mu,
+                                                  const double* __restrict__ exy, const double* __restrict__ exz,
+                                                  const double* __restrict__ eyz, ABOut out) {
+  using namespace df;
+  const int i = 1 + (int)(blockIdx.x * blockDim.x + threadIdx.x);
+  const int j = 1 + (int)(blockIdx.y * blockDim.y + threadIdx.y);
+  const int k = 1 + (int)blockIdx.z;
+  if (i > g.ni || j > g.nj) return;
+  const long X = 1, Y = g.sy, Z = g.sz;
+  const long c = g.at(i, j, k);
+  auto L = [&](const double* a, long o) { return split_double(__ldg(a + c + o)); };
+  const D r0n0 = add(L(in.rho, 0), L(in.rhon, 0)), mu0 = L(mu, 0);
+  // rho00 * src
+  auto rsrc = [&](int q, const double* vel, D r, D grav) {
+    D t = sub(mul(L(vel, 0), p.dtinv), mulf(L(in.adv[q], 0), 1.5f));
+    t = add(t, scale(add(add(L(in.advo[q], 0), L(in.fst[q], 0)), L(in.fstn[q], 0)), 0.5f));
+    t = add(t, grav);
+    return add(sub(mul(r, t), L(in.prs[q], 0)), scale(L(in.vis[q], 0), 0.5f));
+  };
+  auto store = [&](int q, D r, D ap, D rs) {
+    const D T = div(D{1.0f, 0.0f}, add(mul(r, p.dtinv), scale(ap, 0.5f)));
+    out.a[q][c] = to_double(scale(T, 0.5f));
+    out.b[q][c] = to_double(mul(rs, T));
+  };
+  {
+    const D r = scale(add(r0n0, add(L(in.rho, X), L(in.rhon, X))), 0.25f);
+    D ap = mul(p.dz2, add(L(exz, -Z), L(exz, 0)));
+    ap = add(ap, mul(p.dy2, add(L(exy, -Y), L(exy, 0))));
+    ap = add(ap, mul(p.dx2x2, add(mu0, L(mu, X))));
+    store(0, r, ap, rsrc(0, in.u, r, p.grvb));
+  }
+  if (j <= g.nj - 1) {
+    const D r = scale(add(r0n0, add(L(in.rho, Y), L(in.rhon, Y))), 0.25f);
+    D ap = mul(p.dz2, add(L(eyz, -Z), L(eyz, 0)));
+    ap = add(ap, mul(p.dy2x2, add(mu0, L(mu, Y))));
+    ap = add(ap, mul(p.dx2, add(L(exy, -X), L(exy, 0))));
+    store(1, r, ap, rsrc(1, in.v, r, p.grvp));
+  }
+  {
+    const D r = scale(add(r0n0, add(L(in.rho, Z), L(in.rhon, Z))), 0.25f);
+    D ap = mul(p.dz2x2, add(mu0, L(mu, Z)));
+    ap = add(ap, mul(p.dy2, add(L(eyz, -Y), L(eyz, 0))));
+    ap = add(ap, mul(p.dx2, add(L(exz, -X), L(exz, 0))));
+    store(2, r, ap, rsrc(2, in.w, r, D{0.0f, 0.0f}));
   }
 }
 
@@ -966,7 +1021,8 @@ void src_prep(cudaStream_t s, const Grid& g, const VP& p, const double* u, const
               const double* const* adv, const double* const* advo, const double* const* prs,
               const double* const* vis, const double* const* fst, const double* const* fstn, double grvb,
               double grvp, const double* mu, const double* rho, const double* rhon, double* const* E, F3 ef,
-              ABOut out, const double* l1, const double* l2, const double* phi, double dy, double* wallc) {
+              ABOut out, const double* l1, const double* l2, const double* phi, double dy, double* wallc,
+              bool pairs = false) {
   SrcIn in;
   in.u = u;
   in.v = v;
@@ -984,7 +1040,22 @@ void src_prep(cudaStream_t s, const Grid& g, const VP& p, const double* u, const
   in.grvb = grvb;
   in.grvp = grvp;
   k_edges<<<dim3((g.ni + 1 + 31) / 32, (g.nj + 1 + 7) / 8, g.nk + 1), kB, 0, s>>>(g, p, mu, E[0], E[1], E[2], ef);
-  k_src_ab<REFINE><<<dim3((g.ni + 31) / 32, (g.nj + 7) / 8, g.nk), kB, 0, s>>>(g, p, in, mu, E[0], E[1], E[2], out);
+  if (!REFINE && pairs) {
+    using df::split_double;
+    VPS ps;
+    ps.dtinv = split_double(p.dtinv);
+    ps.dx2 = split_double(p.dx2);
+    ps.dy2 = split_double(p.dy2);
+    ps.dz2 = split_double(p.dz2);
+    ps.dx2x2 = split_double(2.0 * p.dx2);
+    ps.dy2x2 = split_double(2.0 * p.dy2);
+    ps.dz2x2 = split_double(2.0 * p.dz2);
+    ps.grvb = split_double(grvb);
+    ps.grvp = split_double(grvp);
+    k_src_ab_e<<<dim3((g.ni + 31) / 32, (g.nj + 7) / 8, g.nk), kB, 0, s>>>(g, ps, in, mu, E[0], E[1], E[2], out);
+  } else {
+    k_src_ab<REFINE><<<dim3((g.ni + 31) / 32, (g.nj + 7) / 8, g.nk), kB, 0, s>>>(g, p, in, mu, E[0], E[1], E[2], out);
+  }
   k_wall_coef<<<wall_grid(g), kB, 0, s>>>(g, dy, l1, l2, phi, wallc);
   count_launch(3);
 }
@@ -1011,14 +1082,14 @@ void src_visc_prep(cudaStream_t s, const Grid& g, double dxinv, double dyinv, do
                    const double* const* adv, const double* const* advo, const double* const* prs,
                    const double* const* vis, const double* const* fst, const double* const* fstn, const double* mu,
                    const double* rho, const double* rhon, double* const* E, double* const* AB, const double* l1,
-                   const double* l2, const double* phi, double dy, double* wallc) {
+                   const double* l2, const double* phi, double dy, double* wallc, bool pairs) {
   ABOut out{};
   for (int q = 0; q < 3; ++q) {
     out.a[q] = AB[2 * q];
     out.b[q] = AB[2 * q + 1];
   }
   src_prep<false>(s, g, make_vp(dxinv, dyinv, dzinv, dt, harmonic), u, v, w, adv, advo, prs, vis, fst, fstn, grvb,
-                  grvp, mu, rho, rhon, E, F3{{nullptr, nullptr, nullptr}}, out, l1, l2, phi, dy, wallc);
+                  grvp, mu, rho, rhon, E, F3{{nullptr, nullptr, nullptr}}, out, l1, l2, phi, dy, wallc, pairs);
 }
 
 void wall_coef(cudaStream_t s, const Grid& g, double dy, const double* l1, const double* l2, const double* phi,

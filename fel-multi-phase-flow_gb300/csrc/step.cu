@@ -588,7 +588,7 @@ static void seg_pre2(fmf_ctx* c) {
   }
   fused::src_visc_prep(s, g, dxinv, dyinv, dzinv, dt, P.harmonic, P.grvb, P.grvp, c->u, c->v, c->w, advp, advop,
                        prsp, visp, fstp, fstnp, c->rmun, c->rho, c->rhon, c->edge, c->ab, c->l1, c->l2, phi1, P.dy,
-                       c->wallc);
+                       c->wallc, c->wprec == 2);
   // :605-607
   op::copy(s, n, c->u, c->un);
   op::copy(s, n, c->v, c->vn);
