@@ -177,8 +177,8 @@ DF_FN D rsqrt(D s) {
 // significand cut to float's 24 bits (toward zero), l the 29 bits below them as a
 // float (rounded to 24), so h + l = q to about 2^-48 of q while l is a normal float
 // (|q| above about 2^-97; below that l is subnormal and the pair holds q to 2^-149
-// absolute).  Magnitudes below 2^-126 give (0, 0); above float's range (and inf,
-// NaN) the float conversion of q and l = 0.
+// absolute).  Magnitudes below 2^-126 give (0, 0); above float's range +-inf (NaN
+// for NaN) and l = 0.
 DF_FN D split_double(double q) {
   uint64_t b;
 #if defined(__CUDA_ARCH__)
@@ -191,11 +191,21 @@ DF_FN D split_double(double q) {
   const int e = (int)((hb >> 20) & 0x7ffu);
   const uint32_t sg = hb & 0x80000000u;
   if (e < 897) return {bitsf(sg), bitsf(sg)};
-  if (e > 1150) return {(float)q, 0.0f};
+  // beyond float's range: +-inf, NaN stays NaN (by bits: a double-to-float
+  // conversion would take an FP64-pipe instruction on every call)
+  if (e > 1150)
+    return {bitsf(sg | (e == 2047 && ((hb & 0xfffffu) | lb) ? 0x7fc00000u : 0x7f800000u)), 0.0f};
   const float hi = bitsf(sg | ((uint32_t)(e - 896) << 23) | ((hb & 0xfffffu) << 3) | (lb >> 29));
   // q - hi = (low 29 bits) 2^(e - 1075), same sign as q.  The power of two is a
   // normal float for e >= 949; below that it is applied as 2^-64 2^(e - 1011)
-  const float L = (float)(lb & 0x1fffffffu);
+  // L = the 29 low bits as a float, rounded once, without an integer-to-float
+  // conversion (which GB300 issues on its FP64 pipe): the high 23 and low 6 bits
+  // are exact floats by the 2^23 offset (2^23 + x has x in its significand for
+  // x < 2^23), and one fused multiply-add joins them with a single rounding
+  const uint32_t m29 = lb & 0x1fffffffu;
+  const float fh = fsub(bitsf(0x4b000000u | (m29 >> 6)), 8388608.0f);
+  const float fl = fsub(bitsf(0x4b000000u | (m29 & 63u)), 8388608.0f);
+  const float L = ffma(fh, 64.0f, fl);
   const float lo = e >= 949 ? fmul(L, bitsf((uint32_t)(e - 948) << 23))
                             : fmul(fmul(L, 0x1p-64f), bitsf((uint32_t)(e - 884) << 23));
   return {hi, sg ? -lo : lo};
@@ -208,16 +218,22 @@ DF_FN D from_double_host(double v) {
 }
 
 #if defined(__CUDACC__)
-// A float as a double from its bits (no FP64-pipe conversion): normal floats and
-// zeros exactly by their fields; subnormals, infinities and NaN by the conversion
+// A float as a double from its bits, with integer operations only (a float-to-
+// double conversion takes an FP64-pipe instruction), exactly: normal floats by
+// their fields, a subnormal m 2^-149 normalised at its leading bit p
+// (m 2^-149 = 1.f 2^(p - 149)), zeros, infinities and NaN as such.
 __device__ __forceinline__ double f2d(float f) {
   const unsigned b = __float_as_uint(f);
-  const unsigned e = (b >> 23) & 0xffu;
+  const unsigned e = (b >> 23) & 0xffu, m = b & 0x7fffffu;
   const unsigned long long sg = (unsigned long long)(b & 0x80000000u) << 32;
-  if ((b << 1) == 0) return __longlong_as_double((long long)sg);
-  if (e == 0 || e == 255) return (double)f;
-  return __longlong_as_double(
-      (long long)(sg | ((unsigned long long)(e + 896) << 52) | ((unsigned long long)(b & 0x7fffffu) << 29)));
+  unsigned long long ed = e == 255 ? 2047ull : (unsigned long long)(e + 896);
+  unsigned long long md = (unsigned long long)m << 29;
+  if (e == 0) {
+    const int p = 31 - __clz((int)m);  // -1 for m = 0
+    ed = m ? (unsigned long long)(p + 874) : 0ull;
+    md = m ? (((unsigned long long)m << (52 - p)) & 0xfffffffffffffull) : 0ull;
+  }
+  return __longlong_as_double((long long)(sg | (ed << 52) | md));
 }
 // a pair rounded to a double (one FP64 addition)
 __device__ __forceinline__ double to_double(D a) { return f2d(a.h) + f2d(a.l); }

@@ -55,9 +55,10 @@ void csf_force(cudaStream_t s, const Grid& g, double dxinv, double dyinv, double
 // The explicit viscous term (calsij, cal_arith_tau, cal_div_tensor) at the interior
 // u, v, w points into vis[0..2]; tau: 6 n doubles of workspace; sk (optional, 6 n):
 // the strain components at the points 0..n+1 the interior divergence reads
+// (pairs: in FP32-pair arithmetic, the FP64-accurate step; not with sk)
 void explicit_viscous(cudaStream_t s, const Grid& g, double dxinv, double dyinv, double dzinv, const double* u,
                       const double* v, const double* w, const double* mu, double* tau, double* const* vis,
-                      double* sk = nullptr);
+                      double* sk = nullptr, bool pairs = false);
 
 // Viscous solve.  src_visc_prep: edge viscosities E[0..2] (xy, xz, yz edges, i,j,k in
 // 0..n), per-component A/B (AB[0..5] = Au Bu Av Bv Aw Bw) with the momentum
@@ -76,7 +77,9 @@ void wall_coef(cudaStream_t s, const Grid& g, double dy, const double* l1, const
 void wall_halo(cudaStream_t s, const Grid& g, int normal, double uwall, const double* wallc, double* un, double* vn,
                double* wn);
 // one outer iteration (u, v, w sweeps of 4 colour pairs each); errsum[0] = sum du^2;
-// part: sor_parts(g) doubles of scratch
+// part: sor_parts(g) doubles of scratch.  FP64 in the FP64-accurate step as well (a
+// point update reads 23 doubles for about 30 operations; measured in FP32 pairs the
+// splits cost more than the arithmetic saves)
 void sor_iteration(cudaStream_t s, const Grid& g, double dxinv, double dyinv, double dzinv, int harmonic,
                    const double* mu, double* const* E, double* const* AB, double uwall, const double* wallc,
                    double* un, double* vn, double* wn, double* part, double* errsum);

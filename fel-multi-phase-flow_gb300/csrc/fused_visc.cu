@@ -252,6 +252,55 @@ __global__ void __launch_bounds__(256) k_div_stress(Grid g, double dxi, double d
   vw[c] = (a5 - __ldg(t5 + c - X)) * dxi + (a6 - __ldg(t6 + c - Y)) * dyi + (__ldg(t3 + c + Z) - __ldg(t3 + c)) * dzi;
 }
 
+// The FP64-accurate step (FMF_FP64E): k_stress and k_div_stress in FP32-pair
+// arithmetic (each double read split into a pair, each output rounded to a double
+// once); the same sums in the same grouping.
+struct VPT {
+  df::D dxi2, dyi2, dzi2, hx, hy, hz, dxi, dyi, dzi;  // 2 dxi, ..., dxi/4, ..., dxi, ...
+};
+__global__ void __launch_bounds__(256) k_stress_e(Grid g, VPT p, const double* __restrict__ u,
+                                                  const double* __restrict__ v, const double* __restrict__ w,
+                                                  const double* __restrict__ mu, double* __restrict__ tau) {
+  using namespace df;
+  const int i = (int)(blockIdx.x * blockDim.x + threadIdx.x);
+  const int j = (int)(blockIdx.y * blockDim.y + threadIdx.y);
+  const int k = (int)blockIdx.z;
+  if (i > g.ni + 1 || j > g.nj + 1) return;
+  const long X = 1, Y = g.sy, Z = g.sz, n = g.n;
+  const long c = g.at(i, j, k);
+  auto L = [&](const double* a, long o) { return split_double(__ldg(a + c + o)); };
+  const D m0 = L(mu, 0), mx = L(mu, X), my = L(mu, Y), mz = L(mu, Z);
+  const D u0 = L(u, 0), v0 = L(v, 0), w0 = L(w, 0);
+  tau[c] = to_double(mul(mul(sub(u0, L(u, -X)), m0), p.dxi2));
+  tau[c + n] = to_double(mul(mul(sub(v0, L(v, -Y)), m0), p.dyi2));
+  tau[c + 2 * n] = to_double(mul(mul(sub(w0, L(w, -Z)), m0), p.dzi2));
+  tau[c + 3 * n] = to_double(mul(add(mul(sub(L(u, Y), u0), p.hy), mul(sub(L(v, X), v0), p.hx)),
+                                 add(add(m0, mx), add(my, L(mu, X + Y)))));
+  tau[c + 4 * n] = to_double(mul(add(mul(sub(L(u, Z), u0), p.hz), mul(sub(L(w, X), w0), p.hx)),
+                                 add(add(m0, mx), add(mz, L(mu, X + Z)))));
+  tau[c + 5 * n] = to_double(mul(add(mul(sub(L(v, Z), v0), p.hz), mul(sub(L(w, Y), w0), p.hy)),
+                                 add(add(m0, my), add(mz, L(mu, Y + Z)))));
+}
+__global__ void __launch_bounds__(256) k_div_stress_e(Grid g, VPT p, const double* __restrict__ t,
+                                                      double* __restrict__ vu, double* __restrict__ vv,
+                                                      double* __restrict__ vw) {
+  using namespace df;
+  const int i = 1 + (int)(blockIdx.x * blockDim.x + threadIdx.x);
+  const int j = 1 + (int)(blockIdx.y * blockDim.y + threadIdx.y);
+  const int k = 1 + (int)blockIdx.z;
+  if (i > g.ni || j > g.nj) return;
+  const long X = 1, Y = g.sy, Z = g.sz, n = g.n;
+  const long c = g.at(i, j, k);
+  auto L = [&](int q, long o) { return split_double(__ldg(t + q * n + c + o)); };
+  const D a4 = L(3, 0), a5 = L(4, 0), a6 = L(5, 0);
+  vu[c] = to_double(add(add(mul(sub(L(0, X), L(0, 0)), p.dxi), mul(sub(a4, L(3, -Y)), p.dyi)),
+                        mul(sub(a5, L(4, -Z)), p.dzi)));
+  vv[c] = to_double(add(add(mul(sub(a4, L(3, -X)), p.dxi), mul(sub(L(1, Y), L(1, 0)), p.dyi)),
+                        mul(sub(a6, L(5, -Z)), p.dzi)));
+  vw[c] = to_double(add(add(mul(sub(a5, L(4, -X)), p.dxi), mul(sub(a6, L(5, -Y)), p.dyi)),
+                        mul(sub(L(2, Z), L(2, 0)), p.dzi)));
+}
+
 // One colour pair of one component.  Thread (a, b, kk) covers, for the pair whose
 // first colour has parities (pi,pj,pk), the point (pi+2a, pj+2b, pk+2kk) and the
 // point of the second colour (all parities flipped) at (pi'+2a, pj'+2b, pk'+2kk).
@@ -1100,7 +1149,24 @@ void wall_coef(cudaStream_t s, const Grid& g, double dy, const double* l1, const
 
 void explicit_viscous(cudaStream_t s, const Grid& g, double dxinv, double dyinv, double dzinv, const double* u,
                       const double* v, const double* w, const double* mu, double* tau, double* const* vis,
-                      double* sk) {
+                      double* sk, bool pairs) {
+  if (pairs && !sk) {
+    using df::split_double;
+    VPT p;
+    p.dxi2 = split_double(2.0 * dxinv);
+    p.dyi2 = split_double(2.0 * dyinv);
+    p.dzi2 = split_double(2.0 * dzinv);
+    p.hx = split_double(0.25 * dxinv);
+    p.hy = split_double(0.25 * dyinv);
+    p.hz = split_double(0.25 * dzinv);
+    p.dxi = split_double(dxinv);
+    p.dyi = split_double(dyinv);
+    p.dzi = split_double(dzinv);
+    k_stress_e<<<dim3((g.ni + 2 + 31) / 32, (g.nj + 2 + 7) / 8, g.nk + 2), kB, 0, s>>>(g, p, u, v, w, mu, tau);
+    k_div_stress_e<<<dim3((g.ni + 31) / 32, (g.nj + 7) / 8, g.nk), kB, 0, s>>>(g, p, tau, vis[0], vis[1], vis[2]);
+    count_launch(2);
+    return;
+  }
   k_stress<<<dim3((g.ni + 2 + 31) / 32, (g.nj + 2 + 7) / 8, g.nk + 2), kB, 0, s>>>(g, dxinv, dyinv, dzinv, u, v, w,
                                                                                mu, tau, sk);
   k_div_stress<<<dim3((g.ni + 31) / 32, (g.nj + 7) / 8, g.nk), kB, 0, s>>>(g, dxinv, dyinv, dzinv, tau, vis[0],
