@@ -230,8 +230,8 @@ def mixed_case(cfg, st0, steps, warmup, stream, fp64_ms=None):
 
 
 def fp64e_case(cfg, st0, steps, warmup, stream, fp64_ms):
-    """The FP64-accurate step (FMF_FP64E: the FP64 step with its WENO5 in FP32-pair
-    arithmetic) on the workload: CUDA-event time per step (state resident, `steps`
+    """The FP64-accurate step (FMF_FP64E: the FP64 step with its FP64-pipe-bound
+    stencils in FP32-pair arithmetic) on the workload: CUDA-event time per step (state resident, `steps`
     after `warmup`), and against the FP64 step from the same initial state after
     warmup + steps: each field's largest difference relative to the FP64 field's
     largest magnitude, and whether every viscous solve took the same iterations."""
@@ -265,9 +265,10 @@ def fp64e_case(cfg, st0, steps, warmup, stream, fp64_ms):
     out["steps_compared"] = warmup + steps
     out["max_rel_err_vs_fp64"] = {k: _rel(states["fp64e"][f], states["fp64"][f], cfg) for k, f in FIELDS.items()}
     out["same_viscous_iterations"] = iters["fp64e"] == iters["fp64"]
-    out["precision"] = ("the FP64 step with its WENO5 advection in FP32-pair arithmetic (two floats per value, about "
-                        "49 significant bits) on the FP32 pipe; every other kernel FP64; parity with the oracle "
-                        "at the FP64 step's 1e-10 (tests/test_gpu_fp64e.py)")
+    out["precision"] = ("the FP64 step with its WENO5 advection, CSF force, viscous momentum factors and explicit "
+                        "viscous term in FP32-pair arithmetic (two floats per value, about 48 significant bits) on "
+                        "the FP32 pipe; state, viscous sweeps, pressure solve, projection and volume sums FP64; "
+                        "parity with the oracle at the FP64 step's 1e-10 (tests/test_gpu_fp64e.py)")
     return out
 
 
@@ -496,7 +497,7 @@ def main():
     ap.add_argument("--adjoint-mixed-steps", type=int, default=500,
                     help="K of the mixed-forward adjoint on the 256x128x128 sessile drop (0: skip)")
     ap.add_argument("--fp64e", type=int, default=1,
-                    help="1: time the FP64-accurate FP32-pair WENO5 step (FMF_FP64E) on the workload too")
+                    help="1: time the FP64-accurate step with FP32-pair stencils (FMF_FP64E) on the workload too")
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed", "fp64e", "adjoint", "adjoint_mixed"],
                     help="--profile only")
     ap.add_argument("--profile", action="store_true",

@@ -19,7 +19,8 @@
 // addition and break an error-free transformation.
 //
 // The header is also compiled by a host C++ compiler (without multiply-add
-// contraction) to check the operations against long double on the CPU.
+// contraction) to check the operations against long double on the CPU
+// (tests/test_df64_host.py).
 #pragma once
 
 #include <cstdint>
@@ -100,12 +101,14 @@ DF_FN D fast_two_sum(float a, float b) {
   return {s, fsub(b, fsub(s, a))};
 }
 DF_FN D neg(D x) { return {-x.h, -x.l}; }
-// sloppy addition: absolute error about 2^-48 (|x| + |y|)
+// sloppy addition: absolute error below 2^-46 (|x| + |y|)
 DF_FN D add(D x, D y) {
   const D s = two_sum(x.h, y.h);
   return fast_two_sum(s.h, fadd(s.l, fadd(x.l, y.l)));
 }
 DF_FN D sub(D x, D y) { return add(x, neg(y)); }
+// product (x.l y.l dropped): relative error below 2^-44 while the result and its
+// low part are normal floats
 DF_FN D mul(D x, D y) {
   const float p = fmul(x.h, y.h);
   float e = ffma(x.h, y.h, -p);
@@ -142,7 +145,7 @@ DF_FN float recipf(float d) {
 #endif
 }
 // n / d for a normal d: the float quotient q1 = n.h / d.h and one correction from
-// the pair residual n - q1 d, relative error about 2^-46
+// the pair residual n - q1 d, relative error below 2^-43
 DF_FN D div(D n, D d) {
   const float r = recipf(d.h);
   const float q1 = fmul(n.h, r);
@@ -155,7 +158,7 @@ DF_FN D div(D n, D d) {
 
 // 1/sqrt(s) for a normal positive s: the float estimate r (hardware approximation
 // and one Newton-Raphson step; on the host the IEEE value) corrected once with the
-// pair residual, r + r (1 - s r^2) / 2, relative error about 2^-46
+// pair residual, r + r (1 - s r^2) / 2, relative error below 2^-43
 DF_FN float rsqrtf_(float s) {
 #if defined(__CUDA_ARCH__)
   float r;
@@ -175,8 +178,8 @@ DF_FN D rsqrt(D s) {
 
 // The pair (h, l) of a double from its bits, without FP64 instructions: h is q's
 // significand cut to float's 24 bits (toward zero), l the 29 bits below them as a
-// float (rounded to 24), so h + l = q to about 2^-48 of q while l is a normal float
-// (|q| above about 2^-97; below that l is subnormal and the pair holds q to 2^-149
+// float (rounded to 24), so h + l = q to 2^-48 of q while l is a normal float
+// (|q| above about 2^-102; below that l is subnormal and adds up to 2^-150
 // absolute).  Magnitudes below 2^-126 give (0, 0); above float's range +-inf (NaN
 // for NaN) and l = 0.
 DF_FN D split_double(double q) {

@@ -381,12 +381,15 @@ typedef struct {
   int precision;                  /* FMF_FP64, FMF_MIXED or FMF_FP64E */
 } fmf_params;
 /* FMF_FP64: every operation in FP64.  FMF_MIXED: FP32 WENO5, MTHINC, CSF and viscous
- * corrections (errors about 1e-6).  FMF_FP64E: the FP64 step with its WENO5
- * advection in FP32-pair arithmetic (a value is the sum of two floats, about 49
- * significant bits) on the FP32 pipe; the advection agrees with FP64's to about
- * 4e-13 of |vel| dxi times the stencil's largest value, and the step with the
- * oracle within the FP64 step's 1e-10.  Contexts only (fmf_adj_create takes
- * FMF_FP64 and FMF_MIXED). */
+ * corrections (errors about 1e-6).  FMF_FP64E: the FP64 step with four of its
+ * FP64-pipe-bound stages in FP32-pair arithmetic (a value is the sum of two
+ * floats, about 48 significant bits) on the FP32 pipe: the WENO5 advection, the
+ * CSF force, the viscous solve's momentum factors (A, B) and the explicit viscous
+ * term; each stage reads doubles, splits them into pairs with integer operations
+ * and rounds its outputs to doubles once.  The state, the viscous sweeps, the
+ * pressure solve, the projection and the volume sums stay FP64, and the step
+ * agrees with the oracle within the FP64 step's 1e-10 with the same viscous
+ * iteration counts.  Contexts only (fmf_adj_create takes FMF_FP64 and FMF_MIXED). */
 enum { FMF_FP64 = 0, FMF_MIXED = 1, FMF_FP64E = 2 };
 
 typedef struct fmf_ctx fmf_ctx;

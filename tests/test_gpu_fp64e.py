@@ -1,5 +1,6 @@
 """The FP64-accurate step (precision FMF_FP64E: the FP64 step with its WENO5
-advection in FP32-pair arithmetic on GB300's FP32 pipe) against the oracle's
+advection, CSF force, viscous momentum factors and explicit viscous term in
+FP32-pair arithmetic on GB300's FP32 pipe) against the oracle's
 restatement of main.f90:473-697 at the FP64 step's bar: phi, u, v, w, p within a
 relative tolerance of 1e-10 (largest difference over the oracle field's largest
 magnitude) with identical viscous iteration counts per step; and its WENO5 kernel
