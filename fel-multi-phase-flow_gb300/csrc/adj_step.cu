@@ -502,7 +502,8 @@ int record_step(fmf_adj* a, bool graphs) {
                         a->wsplit);
     op::calphat(s, g, S[SP], S[SPO], a->phat);
     op::cal_grad_prs(s, g, dxi, dyi, dzi, a->phat, a->prs[0], a->prs[1], a->prs[2]);
-    fused::explicit_viscous(s, g, dxi, dyi, dzi, S[SU], S[SV], S[SW], a->rmu, a->tau, a->vis, a->sk);
+    // in FP32 pairs with a mixed-precision forward, as the product step forms it
+    fused::explicit_viscous(s, g, dxi, dyi, dzi, S[SU], S[SV], S[SW], a->rmu, a->tau, a->vis, a->sk, a->mixed);
     // :545-573 (the fused kernel where the grid tiles; csf_T differentiates the same
     // sequence of reference subroutines either way)
     if (csf_fused) {

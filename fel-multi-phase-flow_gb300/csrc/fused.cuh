@@ -55,7 +55,8 @@ void csf_force(cudaStream_t s, const Grid& g, double dxinv, double dyinv, double
 // The explicit viscous term (calsij, cal_arith_tau, cal_div_tensor) at the interior
 // u, v, w points into vis[0..2]; tau: 6 n doubles of workspace; sk (optional, 6 n):
 // the strain components at the points 0..n+1 the interior divergence reads
-// (pairs: in FP32-pair arithmetic, the FP64-accurate step; not with sk)
+// (pairs: the stresses and their divergence in FP32-pair arithmetic, the strain
+// still FP64; the FP64-accurate and the mixed-precision steps)
 void explicit_viscous(cudaStream_t s, const Grid& g, double dxinv, double dyinv, double dzinv, const double* u,
                       const double* v, const double* w, const double* mu, double* tau, double* const* vis,
                       double* sk = nullptr, bool pairs = false);
@@ -105,7 +106,7 @@ void project(cudaStream_t s, const Grid& g, double rho, double dxinv, double dyi
 struct RefineBufs {
   float* d[3];  // corrections d = un - u, v, w (n floats each)
   float* a[3];  // A per component (n)
-  float* r[3];  // R = A*visn(u) + B - u, formed in FP64 (n)
+  float* r[3];  // R = A*visn(u) + B - u, formed in FP64 (A, B in FP32 pairs) (n)
   float* mu;    // mu (n)
   float* e[3];  // edge viscosities (n)
   float* gw;    // wall constants, refine_floats(g, 0)

@@ -137,14 +137,20 @@ __global__ void __launch_bounds__(256) k_src_ab(Grid g, VP p, SrcIn in, const do
   }
 }
 
-// The FP64-accurate step (FMF_FP64E): k_src_ab's A and B in FP32-pair arithmetic
-// (each double read split into a pair, A and B rounded to doubles once).  The
-// momentum-factor denominator is grouped as dz2 (e(-Z) + e(0)) + dy2 (e(-Y) + e(0))
-// + 2 dx2 (mu(0) + mu(X)) (and likewise per component), the same sum.
+// k_src_ab with A and B in FP32-pair arithmetic (each double read split into a
+// pair, A and B rounded to doubles once).  The FP64-accurate step (FMF_FP64E, REFINE
+// false) stores them.  The mixed-precision step (REFINE true) forms the first-sweep
+// residual R = A visn(u) + B - u from them in FP64, as k_src_ab<true> does: the
+// viscous sum visn reads 20 doubles for about 25 operations, which splitting into
+// pairs makes dearer (measured), while its FP64 instructions overlap the pair
+// arithmetic of A and B on the FP32 pipe.  The momentum-factor denominator is
+// grouped as dz2 (e(-Z) + e(0)) + dy2 (e(-Y) + e(0)) + 2 dx2 (mu(0) + mu(X)) (and
+// likewise per component), the same sum.
 struct VPS {
   df::D dtinv, dx2, dy2, dz2, dx2x2, dy2x2, dz2x2, grvb, grvp;
 };
-__global__ void __launch_bounds__(256) k_src_ab_e(Grid g, VPS p, SrcIn in, const double* __restrict__ mu,
+template <bool REFINE>
+__global__ void __launch_bounds__(256) k_src_ab_e(Grid g, VPS p, VP pd, SrcIn in, const double* __restrict__ mu,
                                                   const double* __restrict__ exy, const double* __restrict__ exz,
                                                   const double* __restrict__ eyz, ABOut out) {
   using namespace df;
@@ -163,31 +169,42 @@ __global__ void __launch_bounds__(256) k_src_ab_e(Grid g, VPS p, SrcIn in, const
     t = add(t, grav);
     return add(sub(mul(r, t), L(in.prs[q], 0)), scale(L(in.vis[q], 0), 0.5f));
   };
-  auto store = [&](int q, D r, D ap, D rs) {
+  // A = T/2, B = rs T; REFINE: A and R = A visn + B - u (FP64) as floats
+  auto store = [&](int q, D r, D ap, D rs, double vn, const double* vel) {
     const D T = div(D{1.0f, 0.0f}, add(mul(r, p.dtinv), scale(ap, 0.5f)));
-    out.a[q][c] = to_double(scale(T, 0.5f));
-    out.b[q][c] = to_double(mul(rs, T));
+    const double A = to_double(scale(T, 0.5f)), B = to_double(mul(rs, T));
+    if (REFINE) {
+      out.af[q][c] = (float)A;
+      out.rf[q][c] = (float)(A * vn + B - __ldg(vel + c));
+    } else {
+      out.a[q][c] = A;
+      out.b[q][c] = B;
+    }
   };
+  const D zero{0.0f, 0.0f};
   {
     const D r = scale(add(r0n0, add(L(in.rho, X), L(in.rhon, X))), 0.25f);
     D ap = mul(p.dz2, add(L(exz, -Z), L(exz, 0)));
     ap = add(ap, mul(p.dy2, add(L(exy, -Y), L(exy, 0))));
     ap = add(ap, mul(p.dx2x2, add(mu0, L(mu, X))));
-    store(0, r, ap, rsrc(0, in.u, r, p.grvb));
+    const double vn = REFINE ? visn_at<0, double>(g, pd, c, mu, exy, exz, eyz, in.u, in.v, in.w) : 0.0;
+    store(0, r, ap, rsrc(0, in.u, r, p.grvb), vn, in.u);
   }
   if (j <= g.nj - 1) {
     const D r = scale(add(r0n0, add(L(in.rho, Y), L(in.rhon, Y))), 0.25f);
     D ap = mul(p.dz2, add(L(eyz, -Z), L(eyz, 0)));
     ap = add(ap, mul(p.dy2x2, add(mu0, L(mu, Y))));
     ap = add(ap, mul(p.dx2, add(L(exy, -X), L(exy, 0))));
-    store(1, r, ap, rsrc(1, in.v, r, p.grvp));
+    const double vn = REFINE ? visn_at<1, double>(g, pd, c, mu, exy, exz, eyz, in.u, in.v, in.w) : 0.0;
+    store(1, r, ap, rsrc(1, in.v, r, p.grvp), vn, in.v);
   }
   {
     const D r = scale(add(r0n0, add(L(in.rho, Z), L(in.rhon, Z))), 0.25f);
     D ap = mul(p.dz2x2, add(mu0, L(mu, Z)));
     ap = add(ap, mul(p.dy2, add(L(eyz, -Y), L(eyz, 0))));
     ap = add(ap, mul(p.dx2, add(L(exz, -X), L(exz, 0))));
-    store(2, r, ap, rsrc(2, in.w, r, D{0.0f, 0.0f}));
+    const double vn = REFINE ? visn_at<2, double>(g, pd, c, mu, exy, exz, eyz, in.u, in.v, in.w) : 0.0;
+    store(2, r, ap, rsrc(2, in.w, r, zero), vn, in.w);
   }
 }
 
@@ -255,12 +272,16 @@ __global__ void __launch_bounds__(256) k_div_stress(Grid g, double dxi, double d
 // The FP64-accurate step (FMF_FP64E): k_stress and k_div_stress in FP32-pair
 // arithmetic (each double read split into a pair, each output rounded to a double
 // once); the same sums in the same grouping.
+// With sk (the adjoint's record of a mixed-precision step) the strain components
+// are written as well, in FP64 as k_stress forms them.
 struct VPT {
   df::D dxi2, dyi2, dzi2, hx, hy, hz, dxi, dyi, dzi;  // 2 dxi, ..., dxi/4, ..., dxi, ...
+  double dxd, dyd, dzd;                               // dxi, dyi, dzi (the strain in FP64)
 };
 __global__ void __launch_bounds__(256) k_stress_e(Grid g, VPT p, const double* __restrict__ u,
                                                   const double* __restrict__ v, const double* __restrict__ w,
-                                                  const double* __restrict__ mu, double* __restrict__ tau) {
+                                                  const double* __restrict__ mu, double* __restrict__ tau,
+                                                  double* __restrict__ sk) {
   using namespace df;
   const int i = (int)(blockIdx.x * blockDim.x + threadIdx.x);
   const int j = (int)(blockIdx.y * blockDim.y + threadIdx.y);
@@ -280,6 +301,16 @@ __global__ void __launch_bounds__(256) k_stress_e(Grid g, VPT p, const double* _
                                  add(add(m0, mx), add(mz, L(mu, X + Z)))));
   tau[c + 5 * n] = to_double(mul(add(mul(sub(L(v, Z), v0), p.hz), mul(sub(L(w, Y), w0), p.hy)),
                                  add(add(m0, my), add(mz, L(mu, Y + Z)))));
+  if (sk) {
+    const double dxi = p.dxd, dyi = p.dyd, dzi = p.dzd;
+    const double ud = __ldg(u + c), vd = __ldg(v + c), wd = __ldg(w + c);
+    sk[c] = (ud - __ldg(u + c - X)) * dxi;
+    sk[c + n] = (vd - __ldg(v + c - Y)) * dyi;
+    sk[c + 2 * n] = (wd - __ldg(w + c - Z)) * dzi;
+    sk[c + 3 * n] = ((__ldg(u + c + Y) - ud) * dyi + (__ldg(v + c + X) - vd) * dxi) * 0.5;
+    sk[c + 4 * n] = ((__ldg(u + c + Z) - ud) * dzi + (__ldg(w + c + X) - wd) * dxi) * 0.5;
+    sk[c + 5 * n] = ((__ldg(v + c + Z) - vd) * dzi + (__ldg(w + c + Y) - wd) * dyi) * 0.5;
+  }
 }
 __global__ void __launch_bounds__(256) k_div_stress_e(Grid g, VPT p, const double* __restrict__ t,
                                                       double* __restrict__ vu, double* __restrict__ vv,
@@ -1089,7 +1120,7 @@ void src_prep(cudaStream_t s, const Grid& g, const VP& p, const double* u, const
   in.grvb = grvb;
   in.grvp = grvp;
   k_edges<<<dim3((g.ni + 1 + 31) / 32, (g.nj + 1 + 7) / 8, g.nk + 1), kB, 0, s>>>(g, p, mu, E[0], E[1], E[2], ef);
-  if (!REFINE && pairs) {
+  if (pairs) {
     using df::split_double;
     VPS ps;
     ps.dtinv = split_double(p.dtinv);
@@ -1101,7 +1132,8 @@ void src_prep(cudaStream_t s, const Grid& g, const VP& p, const double* u, const
     ps.dz2x2 = split_double(2.0 * p.dz2);
     ps.grvb = split_double(grvb);
     ps.grvp = split_double(grvp);
-    k_src_ab_e<<<dim3((g.ni + 31) / 32, (g.nj + 7) / 8, g.nk), kB, 0, s>>>(g, ps, in, mu, E[0], E[1], E[2], out);
+    k_src_ab_e<REFINE><<<dim3((g.ni + 31) / 32, (g.nj + 7) / 8, g.nk), kB, 0, s>>>(g, ps, p, in, mu, E[0], E[1],
+                                                                                 E[2], out);
   } else {
     k_src_ab<REFINE><<<dim3((g.ni + 31) / 32, (g.nj + 7) / 8, g.nk), kB, 0, s>>>(g, p, in, mu, E[0], E[1], E[2], out);
   }
@@ -1150,9 +1182,12 @@ void wall_coef(cudaStream_t s, const Grid& g, double dy, const double* l1, const
 void explicit_viscous(cudaStream_t s, const Grid& g, double dxinv, double dyinv, double dzinv, const double* u,
                       const double* v, const double* w, const double* mu, double* tau, double* const* vis,
                       double* sk, bool pairs) {
-  if (pairs && !sk) {
+  if (pairs) {
     using df::split_double;
     VPT p;
+    p.dxd = dxinv;
+    p.dyd = dyinv;
+    p.dzd = dzinv;
     p.dxi2 = split_double(2.0 * dxinv);
     p.dyi2 = split_double(2.0 * dyinv);
     p.dzi2 = split_double(2.0 * dzinv);
@@ -1162,7 +1197,8 @@ void explicit_viscous(cudaStream_t s, const Grid& g, double dxinv, double dyinv,
     p.dxi = split_double(dxinv);
     p.dyi = split_double(dyinv);
     p.dzi = split_double(dzinv);
-    k_stress_e<<<dim3((g.ni + 2 + 31) / 32, (g.nj + 2 + 7) / 8, g.nk + 2), kB, 0, s>>>(g, p, u, v, w, mu, tau);
+    k_stress_e<<<dim3((g.ni + 2 + 31) / 32, (g.nj + 2 + 7) / 8, g.nk + 2), kB, 0, s>>>(g, p, u, v, w, mu, tau,
+                                                                                                 sk);
     k_div_stress_e<<<dim3((g.ni + 31) / 32, (g.nj + 7) / 8, g.nk), kB, 0, s>>>(g, p, tau, vis[0], vis[1], vis[2]);
     count_launch(2);
     return;
@@ -1229,8 +1265,9 @@ void refine_prep(cudaStream_t s, const Grid& g, double dxinv, double dyinv, doub
     out.af[q] = rb.a[q];
     out.rf[q] = rb.r[q];
   }
+  // A and B in FP32 pairs, the residual in FP64 (k_src_ab_e<true>)
   src_prep<true>(s, g, make_vp(dxinv, dyinv, dzinv, dt, harmonic), u, v, w, adv, advo, prs, vis, fst, fstn, grvb,
-                 grvp, mu, rho, rhon, E, F3{{rb.e[0], rb.e[1], rb.e[2]}}, out, l1, l2, phi, dy, wallc);
+                 grvp, mu, rho, rhon, E, F3{{rb.e[0], rb.e[1], rb.e[2]}}, out, l1, l2, phi, dy, wallc, true);
   k_to_float<<<4 * 152, 256, 0, s>>>(g.n, mu, rb.mu);
   k_gamma_wall<<<wall_grid(g), kB, 0, s>>>(g, uwall, wallc, u, v, w, rb.gw);
   k_gamma_x<<<xh_grid(g), kB, 0, s>>>(g, u, v, w, rb.gx);

@@ -561,7 +561,7 @@ static void seg_pre2(fmf_ctx* c) {
   op::calphat(s, g, c->p, c->po, c->phat);
   op::cal_grad_prs(s, g, dxinv, dyinv, dzinv, c->phat, c->prs[0], c->prs[1], c->prs[2]);
   fused::explicit_viscous(s, g, dxinv, dyinv, dzinv, c->u, c->v, c->w, c->rmu, c->tau, c->vis, nullptr,
-                          c->wprec == 2);
+                          c->wprec != 0);
   // :545-570 surface tension (sfst carried over from the previous step's sfstn where
   // the state continues)
   if (c->verify && fused::csf_supported(g))
