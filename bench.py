@@ -368,6 +368,7 @@ def adjoint_cost(K, stream, every, workload="couette128"):
             "adjoint_over_graph_forward": t_adj / t_ctx, "graph_forward_s": t_ctx,
             "phases_s": {"forward": phases[0], "recompute": phases[1], "reverse": phases[2]},
             "viscous_iterations": {"forward_all": its[0], "transposed": its[1]},
+            "weno5_reverse": "FP32 pairs on the FP64 differences (FMF_ADJ_PAIR_REVERSE=0: FP64)",
             "tolerances": {"sor": 1e-3, "adjoint": 1e-6}}
 
 
@@ -427,6 +428,7 @@ def adjoint_mixed(K, stream, workload="droplet256", every=0):
         t_ctx = time.perf_counter() - t0
         S.close()
         runs[key] = {"J": J, "forward_s": t_fwd, "rollout_s": t_adj, "graph_forward_s": t_ctx,
+                     "weno5_reverse": "FP32 pairs on the FP64 differences" if key == "fp64" else "FP32",
                      "adjoint_over_forward": t_adj / t_fwd, "adjoint_over_graph_forward": t_adj / t_ctx,
                      "phases_s": {"forward": ph[0], "recompute": ph[1], "reverse": ph[2]},
                      "handle_device_bytes": dev_bytes, "device_bytes_in_use_delta": int(free0 - free1),
@@ -627,8 +629,9 @@ def main():
         g.close()
         mixed = mixed_case(cfg, st, args.steps, args.warmup, stream, fp64_ms=ms / args.steps)
         mixed["precision"] = ("fp32: WENO5, MTHINC Newton + Gauss-point fluxes, CSF normals and curvature, viscous "
-                              "sweeps on FP32 corrections (FP64 residual, one refinement step); fp64: state, "
-                              "pressure FFT+TDMA, projection, divergence, volume sums")
+                              "sweeps on FP32 corrections (one refinement step); fp32 pairs: explicit viscous term, "
+                              "momentum factors under the FP64 residual; fp64: state, residual, pressure FFT+TDMA, "
+                              "projection, divergence, volume sums")
         if args.mixed_horizon > 0:
             horizon = mixed_horizon(cfg, st, args.mixed_horizon, 100, stream)
         if args.fp64e:

@@ -207,11 +207,13 @@ void mthinc3_T(cudaStream_t s, const Grid& g, const double* pb, const double* pa
 
 // ---- momentum ------------------------------------------------------------------
 // work: >= 63n doubles (per-line adjoints of the differences and velocities);
-// split (3n float2, or nullptr): the reverse of the forward's FP32 kernel, in FP32
-// on the split pairs of u, v, w written there first (a mixed-precision forward)
+// pairs: the reverse of the FP64 forward in FP32-pair arithmetic (an FP64 forward);
+// else split (3n float2, or nullptr: FP64): the reverse of the forward's FP32
+// kernel, in FP32 on the split pairs of u, v, w written there first (a
+// mixed-precision forward)
 void weno_T(cudaStream_t s, const Grid& g, double dxi, double dyi, double dzi, const double* u, const double* v,
             const double* w, const double* const* ladv, double* lu, double* lv, double* lw, double* work,
-            float2* split = nullptr);
+            float2* split = nullptr, bool pairs = false);
 // CSF force of one field: lf (3 arrays) -> lphi; work: >= 42n doubles.  The
 // normals and curvature are formed again from phi, normals of gradients at the
 // rounding level taken as constants (the noise floor in adj_mom.cu)

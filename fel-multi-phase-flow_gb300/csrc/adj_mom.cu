@@ -5,6 +5,7 @@
 #include "fused.cuh"
 #include "ops.cuh"
 #include "recip.cuh"
+#include "weno5_df.cuh"
 
 namespace fmf {
 namespace adj {
@@ -208,6 +209,54 @@ __device__ float wline_T_f32(const float2* __restrict__ q, long c, long S, float
   return lr * (pos ? A.R : -A.R) * A.sc * (1.0f / 6.0f);
 }
 
+// FP32-pair counterpart for handles whose forward is the FP64 step: the walk's
+// five differences taken in FP64 (exact for neighbouring values, as the forward's)
+// and split into pairs, then R and dR/de in FP32-pair arithmetic
+// (weno5_df.cuh's wrev_core).  Each line then costs about 25 FP64 operations (the
+// advecting velocity, the differences, the rounding of the results, the products
+// with lR) instead of about 100.
+struct WalkP {
+  df::D R;     // the forward's R
+  df::D g[5];  // dR/d(a5, a3, a1, b1, b3)
+};
+__device__ __forceinline__ void walk_df(const double* __restrict__ q, long c, long st, bool grad, WalkP& W) {
+  const double* p = q + c - 3 * st;
+  const double q0 = __ldg(p), q1 = __ldg(p + st), q2 = __ldg(p + 2 * st), q3 = __ldg(p + 3 * st),
+               q4 = __ldg(p + 4 * st), q5 = __ldg(p + 5 * st);
+  using df::split_double;
+  df::wrev_core(split_double(q1 - q0), split_double(q2 - q1), split_double(q3 - q2), split_double(q4 - q3),
+                split_double(q5 - q4), grad, W.R, W.g);
+}
+// wline_T with the walks in FP32 pairs (FP64 handles): the same contract
+__device__ double wline_T_df(const double* __restrict__ q, long c, long S, double vel, double lout, double di,
+                             double* lD) {
+  for (int m = 0; m < 6; ++m) lD[m] = 0.0;
+  const double lr = lout * di;
+  if ((__double_as_longlong(lr) << 1) == 0) return 0.0;
+  const long long vb = __double_as_longlong(vel);
+  WalkP A;
+  if ((vb << 1) == 0) {
+    WalkP B;
+    walk_df(q, c, S, false, A);
+    walk_df(q, c, -S, false, B);
+    return lr * (df::to_double(A.R) - df::to_double(B.R)) * (1.0 / 12.0);
+  }
+  const bool pos = vb > 0;
+  walk_df(q, c, pos ? S : -S, true, A);
+  const double lR = (lr * __longlong_as_double(vb & 0x7fffffffffffffffLL)) * (1.0 / 6.0);
+  double la[5];
+#pragma unroll
+  for (int m = 0; m < 5; ++m) la[m] = lR * df::to_double(A.g[m]);
+  lD[0] = pos ? la[0] : 0.0;
+  lD[1] = pos ? la[1] : -la[4];
+  lD[2] = pos ? la[2] : -la[3];
+  lD[3] = pos ? la[3] : -la[2];
+  lD[4] = pos ? la[4] : -la[1];
+  lD[5] = pos ? 0.0 : -la[0];
+  const double R = df::to_double(A.R);
+  return lr * (pos ? R : -R) * (1.0 / 6.0);
+}
+
 // Offsets (relative to the cell) of the four velocity points that form the
 // advecting velocity of line (component q, direction d); the line reads component d.
 __constant__ signed char kVelOff[9][4][3] = {
@@ -274,6 +323,36 @@ __global__ void __launch_bounds__(256) k_weno_T1_f32(Grid g, float dxi, float dy
   for (int m = 0; m < 6; ++m) D[(long)(line * 6 + m) * n + c] = (double)lD[m];
   V[(long)line * n + c] = (double)lvel;
 }
+// Pass 1 in FP32 pairs (FP64 handles): the advecting velocity as k_weno_T1 forms
+// it, the walks through wline_T_df
+__global__ void __launch_bounds__(256) k_weno_T1_df(Grid g, double dxi, double dyi, double dzi,
+                                                    const double* __restrict__ u, const double* __restrict__ v,
+                                                    const double* __restrict__ w,
+                                                    const double* __restrict__ la0, const double* __restrict__ la1,
+                                                    const double* __restrict__ la2, double* __restrict__ D,
+                                                    double* __restrict__ V) {
+  const int i = 1 + (int)(blockIdx.x * blockDim.x + threadIdx.x);
+  const int j = 1 + (int)(blockIdx.y * blockDim.y + threadIdx.y);
+  const int line = (int)blockIdx.z % 9, k = 1 + (int)blockIdx.z / 9;
+  if (i > g.ni || j > g.nj) return;
+  const int q = line / 3, d = line % 3;
+  const long X = 1, Y = g.sy, Z = g.sz, n = g.n;
+  const long c = g.at(i, j, k);
+  const double* vq = d == 0 ? u : (d == 1 ? v : w);
+  const signed char(*o)[3] = kVelOff[line];
+  const double a = vq[c + o[0][0] * X + o[0][1] * Y + o[0][2] * Z];
+  const double b = vq[c + o[1][0] * X + o[1][1] * Y + o[1][2] * Z];
+  const double e = vq[c + o[2][0] * X + o[2][1] * Y + o[2][2] * Z];
+  const double f = vq[c + o[3][0] * X + o[3][1] * Y + o[3][2] * Z];
+  const double vel = ((a + b) * 0.5 + (e + f) * 0.5) * 0.5;
+  const double L = (q == 0 ? la0 : (q == 1 ? la1 : la2))[c];
+  double lD[6];
+  const double lvel = wline_T_df(q == 0 ? u : (q == 1 ? v : w), c, d == 0 ? X : (d == 1 ? Y : Z), vel, L,
+                                 d == 0 ? dxi : (d == 1 ? dyi : dzi), lD);
+#pragma unroll
+  for (int m = 0; m < 6; ++m) D[(long)(line * 6 + m) * n + c] = lD[m];
+  V[(long)line * n + c] = lvel;
+}
 // Pass 2: every point gathers what the lines of the cells around it owe it.
 __global__ void __launch_bounds__(256) k_weno_T2(Grid g, const double* __restrict__ D,
                                                  const double* __restrict__ V, double* __restrict__ lu,
@@ -322,11 +401,13 @@ __global__ void __launch_bounds__(256) k_weno_T2(Grid g, const double* __restric
 
 void weno_T(cudaStream_t s, const Grid& g, double dxi, double dyi, double dzi, const double* u, const double* v,
             const double* w, const double* const* ladv, double* lu, double* lv, double* lw, double* work,
-            float2* split) {
+            float2* split, bool pairs) {
   double* D = work;
   double* V = work + 54 * g.n;
   const dim3 grd((g.ni + 31) / 32, (g.nj + 7) / 8, 9 * g.nk), blk(32, 8);
-  if (split) {
+  if (pairs) {
+    k_weno_T1_df<<<grd, blk, 0, s>>>(g, dxi, dyi, dzi, u, v, w, ladv[0], ladv[1], ladv[2], D, V);
+  } else if (split) {
     fused::split3(s, g, u, v, w, split);
     k_weno_T1_f32<<<grd, blk, 0, s>>>(g, (float)dxi, (float)dyi, (float)dzi, split, ladv[0], ladv[1], ladv[2], D, V);
   } else {

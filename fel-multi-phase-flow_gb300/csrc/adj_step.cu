@@ -172,6 +172,9 @@ struct fmf_adj {
   // With a mixed-precision forward the reverse of its FP32 WENO5 runs in FP32
   // (FMF_ADJ_F32_REVERSE=0 at creation: FP64)
   bool f32_reverse = true;
+  // With an FP64 forward the WENO5 reverse runs in FP32-pair arithmetic
+  // (FMF_ADJ_PAIR_REVERSE=0 at creation: FP64)
+  bool pair_reverse = true;
 };
 
 namespace {
@@ -836,16 +839,18 @@ void reverse_step(fmf_adj* a, const double* st, bool defer) {
   {
     if (a->carry_in) add3(s, n, cadv, a->ladv);
     const double* la[3] = {a->ladv[0], a->ladv[1], a->ladv[2]};
-    // a mixed-precision forward (FP32 WENO5): its reverse in FP32 as well
+    // a mixed-precision forward (FP32 WENO5): its reverse in FP32 as well; an FP64
+    // forward: its reverse in FP32 pairs
     float2* wsp = a->mixed && a->f32_reverse ? a->wsplit : nullptr;
+    const bool wpairs = !a->mixed && a->pair_reverse;
     adj::weno_T(s, g, dxi, dyi, dzi, ST(SU), ST(SV), ST(SW), la, lS[SU], lS[SV], lS[SW], a->work + 3 * n + 1024,
-                wsp);
+                wsp, wpairs);
     if (defer) {
       for (int q = 0; q < 3; ++q) dcopy(a, a->ladvo[q], cadv[q], n);
     } else {
       const double* lao[3] = {a->ladvo[0], a->ladvo[1], a->ladvo[2]};
       adj::weno_T(s, g, dxi, dyi, dzi, ST(SUO), ST(SVO), ST(SWO), lao, lS[SUO], lS[SVO], lS[SWO],
-                  a->work + 3 * n + 1024, wsp);
+                  a->work + 3 * n + 1024, wsp, wpairs);
     }
   }
   a->carry_in = defer;
@@ -943,6 +948,7 @@ int fmf_adj_create(const fmf_params* prm, fmf_adj** out) {
   if (const char* e = std::getenv("FMF_ADJ_WARM")) a->warm = std::atoi(e) != 0;
   if (const char* e = std::getenv("FMF_ADJ_EXTRAP")) a->extrap = std::atoi(e) != 0;
   if (const char* e = std::getenv("FMF_ADJ_F32_REVERSE")) a->f32_reverse = std::atoi(e) != 0;
+  if (const char* e = std::getenv("FMF_ADJ_PAIR_REVERSE")) a->pair_reverse = std::atoi(e) != 0;
   a->g = Grid(prm->ni, prm->nj, prm->nk);
   a->scr = scratch_set_create();
   // the highest stream priority: the reverse steps are the critical path when a
