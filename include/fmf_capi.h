@@ -502,7 +502,9 @@ void datain_(int* ipara, int* ID, int* ni, int* nj, int* nk, int* nbub, int* nst
  * from checkpoints taken every `every` steps (0: ceil(sqrt(K))) and differentiates
  * the FP64 step's operations at the states that forward produced.  In an FMF_MIXED
  * handle the reverse of the WENO5 advection runs in FP32, as its forward does
- * (environment FMF_ADJ_F32_REVERSE=0 at creation keeps it FP64). */
+ * (environment FMF_ADJ_F32_REVERSE=0 at creation keeps it FP64); in an FMF_FP64
+ * handle it runs in FP32-pair arithmetic on FP64 differences, to about 1e-11 of
+ * the FP64 reverse (FMF_ADJ_PAIR_REVERSE=0 at creation keeps it FP64). */
 typedef struct fmf_adj fmf_adj;
 int fmf_adj_create(const fmf_params* prm, fmf_adj** out);
 int fmf_adj_destroy(fmf_adj* adj);
