@@ -213,7 +213,12 @@ __device__ __forceinline__ df::D wdir_df(const float2* __restrict__ q, long c, l
 // The FP64-accurate step's WENO5 of one or both levels (as k_weno2) in FP32-pair
 // arithmetic: sp holds the split pairs of u, v, w (then uo, vo, wo); each velocity
 // sum and derivative is a pair, the three derivatives of a component are summed as
-// pairs and the sum is rounded to a double once.
+// pairs and the sum is rounded to a double once.  The nine (component, direction)
+// derivatives of a level run as one loop that is not unrolled: fully inlined they
+// made a loop body whose instruction fetch stalled the warps (the leading stall
+// reason under ncu).  Line (q, d) advects component q along d with the velocity
+// sum (Vd(c - Sd) + Vd(c - Sd + Sq)) + (Vd(c) + Vd(c + Sq)), Vd the d component,
+// the same pairs in the same order as the unrolled form.
 __global__ void __launch_bounds__(128) k_weno2_df(Grid g, int nlev, const int* __restrict__ keep, df::D kx,
                                                   df::D ky, df::D kz, const float2* __restrict__ sp,
                                                   double* __restrict__ au, double* __restrict__ av,
@@ -236,23 +241,20 @@ __global__ void __launch_bounds__(128) k_weno2_df(Grid g, int nlev, const int* _
       const float2 v = __ldg(a + o);
       return df::D{v.x, v.y};
     };
-    auto out = [](df::D a) { return df::to_double(a); };
-    const df::D u0 = h(U, c), uxm = h(U, c - X), uxp = h(U, c + X);
-    const df::D v0 = h(V, c), vym = h(V, c - Y), vyp = h(V, c + Y);
-    const df::D w0 = h(W, c), wzm = h(W, c - Z), wzp = h(W, c + Z);
-    df::D a;
-    a = wdir_df(U, c, X, add(add(uxm, u0), add(u0, uxp)), kx);
-    a = add(a, wdir_df(U, c, Y, add(add(vym, h(V, c + X - Y)), add(v0, h(V, c + X))), ky));
-    a = add(a, wdir_df(U, c, Z, add(add(wzm, h(W, c + X - Z)), add(w0, h(W, c + X))), kz));
-    (lev ? auo : au)[c] = out(a);
-    a = wdir_df(V, c, X, add(add(uxm, h(U, c - X + Y)), add(u0, h(U, c + Y))), kx);
-    a = add(a, wdir_df(V, c, Y, add(add(vym, v0), add(v0, vyp)), ky));
-    a = add(a, wdir_df(V, c, Z, add(add(wzm, h(W, c + Y - Z)), add(w0, h(W, c + Y))), kz));
-    (lev ? avo : av)[c] = out(a);
-    a = wdir_df(W, c, X, add(add(uxm, h(U, c - X + Z)), add(u0, h(U, c + Z))), kx);
-    a = add(a, wdir_df(W, c, Y, add(add(vym, h(V, c - Y + Z)), add(v0, h(V, c + Z))), ky));
-    a = add(a, wdir_df(W, c, Z, add(add(wzm, w0), add(w0, wzp)), kz));
-    (lev ? awo : aw)[c] = out(a);
+    df::D a{0.0f, 0.0f};
+#pragma unroll 1
+    for (int line = 0; line < 9; ++line) {
+      const int q = line / 3, d = line - 3 * q;
+      const long Sq = q == 0 ? X : (q == 1 ? Y : Z), Sd = d == 0 ? X : (d == 1 ? Y : Z);
+      const float2* Fd = d == 0 ? U : (d == 1 ? V : W);
+      const df::D vsum = add(add(h(Fd, c - Sd), h(Fd, c - Sd + Sq)), add(h(Fd, c), h(Fd, c + Sq)));
+      const df::D t = wdir_df(q == 0 ? U : (q == 1 ? V : W), c, Sd, vsum, d == 0 ? kx : (d == 1 ? ky : kz));
+      a = d == 0 ? t : add(a, t);
+      if (d == 2) {
+        double* o = q == 0 ? (lev ? auo : au) : (q == 1 ? (lev ? avo : av) : (lev ? awo : aw));
+        o[c] = df::to_double(a);
+      }
+    }
   }
 }
 
