@@ -58,6 +58,17 @@ WENO_FP64_FLOPS_PER_CELL = (955711488 + 1219493888 + 2 * 1885798400) / 2 / 41943
 # weno5.h's own formula (both one-sided reconstructions) per cell and level
 WENO_REFERENCE_FLOPS_PER_CELL = 1383.0
 
+# The FP64-accurate step's WENO5 kernel (k_weno2_df, one level, FP32-pair
+# arithmetic): FP32 thread instructions (FADD + FMUL + FFMA) per interior cell from
+# the ncu capture of one one-level launch at 256x128x128 (13,157.6 per cycle over
+# 1,736,058 cycles, 4,194,304 cells; python bench.py --profile --precision fp64e
+# --workload couette256 --warmup 2 --steps 1 under ncu --set full -k
+# regex:k_weno2_df -s 1 -c 1 --clock-control none)
+PAIR_WENO_CAPTURE = ("ncu --set full of one one-level k_weno2_df launch, couette256 256x128x128: FADD + FMUL + "
+                     "FFMA thread instructions")
+PAIR_WENO_FP32_INST_PER_CELL = (10113.089172 + 1495.997566 + 1548.534517) * 1736057.75 / 4194304
+PAIR_WENO_TRAFFIC_PER_CELL = (113.535232e6 + 70.033408e6) / 4194304
+
 # Algorithmic bytes of one cell-update: 83 words outside the viscous solve and 21
 # words per outer iteration of it (each stage's external arrays read once and
 # written once, FP64)
@@ -256,6 +267,23 @@ def fp64e_case(cfg, st0, steps, warmup, stream, fp64_ms):
         iters[key] = its + g.sor_iterations()
         if key == "fp64e":
             out["ms_per_step"] = e0.elapsed_time(e1) / steps
+            # the dominant pair kernel, WENO5 of (u, v, w) (stage 4: the split of the
+            # three fields into pairs, then k_weno2_df), against the FP32 pipe
+            ms_stage = ctypes.c_float()
+            capi.check(capi.lib().fmf_ctx_time_stage(g.h, 4, 5, ctypes.byref(ms_stage)), "time_stage")
+            fp32 = ctypes.c_double()
+            capi.lib().fmf_measure_fma_rate.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_double)]
+            capi.check(capi.lib().fmf_measure_fma_rate(0, ctypes.byref(fp32)), "fma rate")
+            rate = PAIR_WENO_FP32_INST_PER_CELL * cfg.cells / (ms_stage.value * 1e-3) / 1e12
+            out["roofline"] = {"bound": "fp32", "achieved": rate, "peak": fp32.value / 2.0,
+                               "unit": "T FP32 instructions/s", "frac": rate / (fp32.value / 2.0),
+                               "traffic": PAIR_WENO_TRAFFIC_PER_CELL * cfg.cells,
+                               "kernel": "k_weno2_df, one level (with the split of u, v, w into pairs before it)",
+                               "kernel_ms": ms_stage.value,
+                               "fp32_inst_per_cell": PAIR_WENO_FP32_INST_PER_CELL,
+                               "counters_source": PAIR_WENO_CAPTURE + ", scaled to the workload by its cell count",
+                               "peak_source": "FP32 FMA chains measured live (fmf_measure_fma_rate), one "
+                                              "instruction per FMA"}
         states[key] = g.get_state()
         g.close()
     out["fp64_ms_per_step"] = fp64_ms
