@@ -256,6 +256,55 @@ def test_gnbc_known_answers(orc):
             np.testing.assert_allclose(theta[:, 3, :], th0[:, 3, :], rtol=0, atol=1e-4)
 
 
+def test_bnd_contact_angle_known_answers(orc):
+    """bnd_contact_angle.f90:25-85 on fields with closed-form ghosts, unequal
+    spacings and a different static angle in every wall cell:
+    * a field linear in i and k, q = q0 + a i + b j + c k: the wall normal
+      (sg sin(theta) dy/dx, cos(theta), sg sin(theta) dy/dz) (sg = +1 for
+      i >= ni/2, else -1) turns the centred x and z differences into the ghost
+      q(j=0) = q(j=1) - sg cot(theta) (a + c) (and q(nj+1) = q(nj) - ... at the upper
+      wall), and the two outer ghosts continue linearly;
+    * theta = 90 deg: every ghost is the first interior value, for any field;
+    * a field that varies in j only: the same, for any angle;
+    * the columns i = -2, ni+3 and planes k = -2, nk+3, which the reference's
+      stencil would read out of bounds, are left as they were (every call site
+      refills them with bnd_periodic)."""
+    ni, nj, nk = 16, 8, 8
+    dx, dy, dz = 0.1, 0.05, 0.2
+    sh = (nk + 6, nj + 6, ni + 6)
+    rng = np.random.default_rng(5)
+    kk, jj, ii = np.meshgrid(np.arange(-2, nk + 4), np.arange(-2, nj + 4), np.arange(-2, ni + 4), indexing="ij")
+    theta = rng.uniform(35.0, 145.0, sh)
+    sg = np.where(np.arange(-1, ni + 3) - ni // 2 >= 0, 1.0, -1.0)[None, :]
+    I, D, P = orc.I, orc.D, orc.P
+
+    def run(q, th):
+        q = np.ascontiguousarray(q.copy())
+        orc.lib().orc_bnd_contact_angle(orc.IA([-1] * 6), I(ni), I(nj), I(nk), P(q), P(th), D(dx), D(dy), D(dz))
+        return q
+
+    a, b, c = 0.3, 0.11, -0.7
+    q = 0.5 + a * ii + b * jj + c * kk
+    got = run(q, theta)
+    inner = (slice(1, nk + 5), slice(1, ni + 5))  # k, i in -1 .. n+2
+    for jw, ghosts in ((1, (0, -1, -2)), (nj, (nj + 1, nj + 2, nj + 3))):
+        cot = 1.0 / np.tan(np.radians(theta[:, jw + 2, :][inner]))
+        step = -sg * cot * (a + c)  # q(ghost 1) - q(wall row)
+        q1 = q[:, jw + 2, :][inner]
+        for m, jg in enumerate(ghosts, start=1):
+            np.testing.assert_allclose(got[:, jg + 2, :][inner], q1 + m * step, rtol=0, atol=1e-12)
+    # D2: the outermost columns and planes keep their values
+    for jg in (0, -1, -2, nj + 1, nj + 2, nj + 3):
+        assert np.array_equal(got[:, jg + 2, 0], q[:, jg + 2, 0]) and np.array_equal(got[:, jg + 2, -1], q[:, jg + 2, -1])
+        assert np.array_equal(got[0, jg + 2, :], q[0, jg + 2, :]) and np.array_equal(got[-1, jg + 2, :], q[-1, jg + 2, :])
+    # 90 degrees, any field; a field that varies in j only, any angle
+    for field, th in ((rng.standard_normal(sh), np.full(sh, 90.0)), (np.sin(0.7 * jj) + 0.0 * ii, theta)):
+        got = run(field, th)
+        for jw, ghosts in ((1, (0, -1, -2)), (nj, (nj + 1, nj + 2, nj + 3))):
+            for jg in ghosts:
+                np.testing.assert_allclose(got[:, jg + 2, :][inner], field[:, jw + 2, :][inner], rtol=0, atol=1e-13)
+
+
 @pytest.mark.parametrize("N", [32, 64])
 def test_csf_curvature_of_a_sphere(orc, N):
     """calrn.f + calrkap.f on a resolved sphere of radius R = 0.25 (phi = 1 inside,
