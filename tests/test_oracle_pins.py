@@ -305,6 +305,52 @@ def test_bnd_contact_angle_known_answers(orc):
                 np.testing.assert_allclose(got[:, jg + 2, :][inner], field[:, jw + 2, :][inner], rtol=0, atol=1e-13)
 
 
+def test_bndu_navier_slip_law(orc):
+    """bndu.f:29-97: at both walls the first ghost of u satisfies the discrete
+    Navier-slip law at the wall face, (u_ghost + u_wall_row)/2 - U = ls (du/dn)
+    with du/dn the one-cell difference into the fluid, U = -uwall at the lower and
+    +uwall at the upper wall, and ls = 1/(phi_bar/l1 + (1 - phi_bar)/l2), phi_bar
+    the mean of phi over the two cells beside the u point; w the same law with U = 0
+    (and the u point's slip length, as the reference has it); v vanishes on the wall
+    face and is odd about it; the outer ghosts of u and w continue linearly.
+    Checked on the interior columns (the x and z halos are refilled afterwards) with
+    random fields, phi in [0, 1] and l1 != l2."""
+    ni, nj, nk = 16, 8, 8
+    dy, uwall = 0.05, 0.8
+    sh = (nk + 6, nj + 6, ni + 6)
+    rng = np.random.default_rng(9)
+    u, v, w = (rng.standard_normal(sh) for _ in range(3))
+    phi = rng.uniform(0.0, 1.0, sh)
+    l1, l2 = rng.uniform(0.01, 0.2, sh), rng.uniform(0.3, 2.0, sh)
+    u0, v0, w0 = u.copy(), v.copy(), w.copy()
+    I, D, P = orc.I, orc.D, orc.P
+    orc.lib().orc_bndu(orc.IA([-1] * 6), I(ni), I(nj), I(nk), P(u), P(v), P(w), D(uwall), D(dy), P(l1), P(l2),
+                       P(phi))
+    K, Ii = slice(3, nk + 3), slice(3, ni + 3)  # k, i in 1 .. n
+    for jw, jg, sgn, U in ((1, 0, 1.0, -uwall), (nj, nj + 1, -1.0, uwall)):
+        pb = 0.5 * (phi[K, jw + 2, Ii] + phi[K, jw + 2, 4:ni + 4])
+        ls = 1.0 / (pb / l1[K, jw + 2, Ii] + (1.0 - pb) / l2[K, jw + 2, Ii])
+        for q, Uw in ((u, U), (w, 0.0)):
+            qw, qg = q[K, jw + 2, Ii], q[K, jg + 2, Ii]
+            lhs = 0.5 * (qg + qw) - Uw
+            rhs = ls * (qw - qg) / dy  # into the fluid: (wall row - ghost) / dy at either wall
+            np.testing.assert_allclose(lhs, rhs, rtol=0, atol=1e-12 * (1 + np.abs(rhs).max()))
+            # outer ghosts linear
+            step = qg - qw
+            for m in (2, 3):
+                jo = jw - sgn * m  # j = -1, -2 below, nj + 2, nj + 3 above
+                np.testing.assert_allclose(q[K, int(jo) + 2, Ii], qw + m * step, rtol=0, atol=1e-12)
+    # v: zero on the wall face, odd about it
+    assert np.all(v[K, 2, Ii] == 0.0) and np.all(v[K, nj + 2, Ii] == 0.0)
+    for m in (1, 2):
+        np.testing.assert_array_equal(v[K, 2 - m, Ii], -v0[K, 2 + m, Ii])
+    for m in (1, 2, 3):
+        np.testing.assert_array_equal(v[K, nj + 2 + m, Ii], -v0[K, nj + 2 - m, Ii])
+    # the interior is untouched
+    sl = (K, slice(3, nj + 2), Ii)
+    assert np.array_equal(u[sl], u0[sl]) and np.array_equal(w[sl], w0[sl]) and np.array_equal(v[sl], v0[sl])
+
+
 @pytest.mark.parametrize("N", [32, 64])
 def test_csf_curvature_of_a_sphere(orc, N):
     """calrn.f + calrkap.f on a resolved sphere of radius R = 0.25 (phi = 1 inside,
