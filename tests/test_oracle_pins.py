@@ -351,6 +351,62 @@ def test_bndu_navier_slip_law(orc):
     assert np.array_equal(u[sl], u0[sl]) and np.array_equal(w[sl], w0[sl]) and np.array_equal(v[sl], v0[sl])
 
 
+def test_explicit_viscous_term_known_answers(orc):
+    """calsij.f:28-139, cal_arith_tau.f:21-117 and cal_div_tensor.f:20-86 chained
+    (the explicit term div(2 mu S) of main.f90:538-541) on fields where the
+    staggered second-order differences are exact, with unequal spacings:
+    * constant mu, quadratic u, v, w: div(2 mu S) = mu (lap u + grad div u), a
+      constant per component (u: mu (2 Axx + 2 Ayy + 2 Azz + 2 Axx + Bxy + Cxz) for
+      u = ... + Axx x^2 + Axy x y + ..., v and w with coefficients B and C);
+    * linear mu, linear u, v, w (S constant): div(2 mu S) = 2 S grad mu, a constant
+      (the four-cell edge means of a linear mu are its values on the edges).
+    Checked at the interior u, v, w points to 1e-9 of the largest term."""
+    ni, nj, nk = 16, 8, 12
+    dx, dy, dz = 0.11, 0.07, 0.23
+    sh = (nk + 6, nj + 6, ni + 6)
+    kk, jj, ii = np.meshgrid(np.arange(-2, nk + 4), np.arange(-2, nj + 4), np.arange(-2, ni + 4), indexing="ij")
+    x, y, z = ii * dx, jj * dy, kk * dz
+    I, D, P = orc.I, orc.D, orc.P
+    inner = (slice(3, nk + 3), slice(3, nj + 3), slice(3, ni + 3))
+
+    def chain(u, v, w, mu):
+        sk = np.zeros((6,) + sh)
+        tau = np.zeros((6,) + sh)
+        out = [np.zeros(sh) for _ in range(3)]
+        orc.lib().orc_calsij(I(ni), I(nj), I(nk), D(1 / dx), D(1 / dy), D(1 / dz), P(u), P(v), P(w), P(sk))
+        orc.lib().orc_cal_arith_tau(I(ni), I(nj), I(nk), P(sk), P(mu), P(tau))
+        orc.lib().orc_cal_div_tensor(I(ni), I(nj), I(nk), D(1 / dx), D(1 / dy), D(1 / dz), P(tau), *[P(o) for o in out])
+        return out
+
+    rng = np.random.default_rng(13)
+    keys = ("xx", "yy", "zz", "xy", "xz", "yz", "x", "y", "z", "c")
+    A, B, C = ({k: rng.uniform(-1, 1) for k in keys} for _ in range(3))
+
+    def quad(c):
+        return (c["xx"] * x * x + c["yy"] * y * y + c["zz"] * z * z + c["xy"] * x * y + c["xz"] * x * z
+                + c["yz"] * y * z + c["x"] * x + c["y"] * y + c["z"] * z + c["c"])
+
+    mu0 = 0.37
+    got = chain(quad(A), quad(B), quad(C), np.full(sh, mu0))
+    want = (mu0 * (4 * A["xx"] + 2 * A["yy"] + 2 * A["zz"] + B["xy"] + C["xz"]),
+            mu0 * (2 * B["xx"] + 4 * B["yy"] + 2 * B["zz"] + A["xy"] + C["yz"]),
+            mu0 * (2 * C["xx"] + 2 * C["yy"] + 4 * C["zz"] + A["xz"] + B["yz"]))
+    for g, w_ in zip(got, want):
+        np.testing.assert_allclose(g[inner], w_, rtol=0, atol=1e-9 * max(abs(x) for x in want))
+
+    # linear mu and velocities
+    m = {"x": 0.3, "y": -0.2, "z": 0.45}
+    mu = 2.0 + m["x"] * x + m["y"] * y + m["z"] * z
+    lin = [{k: rng.uniform(-1, 1) for k in ("x", "y", "z", "c")} for _ in range(3)]
+    vel = [L["x"] * x + L["y"] * y + L["z"] * z + L["c"] for L in lin]
+    got = chain(*vel, mu)
+    grad = [[lin[a][b] for b in ("x", "y", "z")] for a in range(3)]  # grad[a][b] = d u_a / d x_b
+    gm = (m["x"], m["y"], m["z"])
+    want = [sum((grad[a][b] + grad[b][a]) * gm[b] for b in range(3)) for a in range(3)]
+    for g, w_ in zip(got, want):
+        np.testing.assert_allclose(g[inner], w_, rtol=0, atol=1e-9 * max(abs(x) for x in want))
+
+
 @pytest.mark.parametrize("N", [32, 64])
 def test_csf_curvature_of_a_sphere(orc, N):
     """calrn.f + calrkap.f on a resolved sphere of radius R = 0.25 (phi = 1 inside,
