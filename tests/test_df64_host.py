@@ -14,7 +14,10 @@ differences and dR/de) evaluated in long double, on stencils of six doubles in s
 regimes (smooth waves over 1e-12 .. 1e10, small variations on a large mean,
 constant and linear runs, jumps, noise, near-flat values): R within 1e-12 of the
 largest difference and the gradient within 1e-10 of its largest entry (measured
-1.3e-13 and 2.2e-11; the FP64 walk itself 3.6e-15 and 7.8e-13)."""
+1.3e-13 and 2.2e-11; the FP64 walk itself 3.6e-15 and 7.8e-13).  On the same
+stencils the forward pair core of the FP64-accurate step (wdir_core, which takes
+its differences between split values) within 1e-12 of the largest difference +
+4e-13 of the largest value + 2^-94 (measured at most 0.2 of that)."""
 import os
 import shutil
 import subprocess
@@ -53,6 +56,7 @@ def test_weno_reverse_core_against_long_double(tmp_path):
     out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout
     rows = [line.split() for line in out.split("\n") if line.strip()]
     assert len(rows) == 6, out
-    for name, r, g, r64, g64 in rows:
+    for name, r, g, r64, g64, fwd in rows:
         assert float(r) <= 1e-12, (name, out)
         assert float(g) <= 1e-10, (name, out)
+        assert float(fwd) <= 1.0, (name, out)

@@ -8,7 +8,8 @@
 // limit.  The differences are taken in double, as the device does.  Built by
 // tests/test_df64_host.py with g++ -O2 -ffp-contract=off; prints per regime
 // the worst error of R (over the largest |difference|) and of the gradient (over its
-// largest entry), of the pair core and then of the same walk in double.
+// largest entry), of the pair core and then of the same walk in double, and last
+// the worst error of the forward pair core wdir_core (see there).
 #include <cmath>
 #include <cstdio>
 #include <random>
@@ -89,7 +90,7 @@ int main() {
   std::uniform_real_distribution<double> U(-1.0, 1.0);
   const char* names[] = {"smooth", "offset", "linear", "jump", "noise", "tiny"};
   for (int regime = 0; regime < 6; ++regime) {
-    double worst_r = 0, worst_g = 0, worst_r64 = 0, worst_g64 = 0;
+    double worst_r = 0, worst_g = 0, worst_r64 = 0, worst_g64 = 0, worst_f = 0;
     for (int t = 0; t < 40000; ++t) {
       double q[6];
       const double mag = std::pow(10.0, std::uniform_int_distribution<int>(-12, 10)(rng));
@@ -125,6 +126,23 @@ int main() {
       for (int k = 0; k < 5; ++k)
         if (!std::isfinite((double)val(g[k]))) ge = 1e30;
       worst_g = std::fmax(worst_g, (double)(gmax > 0 ? ge / gmax : ge));
+      // the forward pair core (the FP64-accurate step's WENO5) on the split values
+      // themselves (vsum = 4 > 0: the walk from q[0], kx = 1, so it returns 4 R): its
+      // differences are taken between split values, each within 2^-48 of its double,
+      // and below 2^-99 it returns 0 (the FP64 walk: D2), so its error is taken over
+      // 1e-12 of the largest difference + 4e-13 of the largest value + 2^-94
+      {
+        D w[6];
+        LD qmax = 0;
+        for (int k = 0; k < 6; ++k) {
+          w[k] = fmf::df::split_double(q[k]);
+          qmax = std::fmax(qmax, std::fabs((LD)q[k]));
+        }
+        const D f = fmf::df::wdir_core(w, D{4.0f, 0.0f}, D{1.0f, 0.0f});
+        const LD scale = 1e-12L * emax + 4e-13L * qmax + std::ldexp((LD)1, -94);
+        if (scale > 0) worst_f = std::fmax(worst_f, (double)(std::fabs(val(f) / 4 - Rl) / scale));
+        if (!std::isfinite((double)val(f))) worst_f = 1e30;
+      }
       double R64, g64[5];
       walk_d(e, R64, g64);
       if (emax > 0) worst_r64 = std::fmax(worst_r64, (double)(std::fabs((LD)R64 - Rl) / emax));
@@ -132,7 +150,7 @@ int main() {
       for (int k = 0; k < 5; ++k) ge64 = std::fmax(ge64, std::fabs((LD)g64[k] - gl[k]));
       worst_g64 = std::fmax(worst_g64, (double)(gmax > 0 ? ge64 / gmax : ge64));
     }
-    std::printf("%s %.3g %.3g %.3g %.3g\n", names[regime], worst_r, worst_g, worst_r64, worst_g64);
+    std::printf("%s %.3g %.3g %.3g %.3g %.3g\n", names[regime], worst_r, worst_g, worst_r64, worst_g64, worst_f);
   }
   return 0;
 }
