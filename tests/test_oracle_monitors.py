@@ -1,7 +1,8 @@
 """Pins of the oracle's run-time monitors (no GPU): cal_vel.f, cal_center.f and
 find_interface_positions_upper.f90 against numpy restatements and known answers
 (a uniform velocity, a box of phi with a known centre, a blob carried across the
-periodic x boundary)."""
+periodic x boundary), and the adjoint's objective find_interface_positions_lower
+on wall rows whose contact-line positions are known exactly."""
 import ctypes
 
 import numpy as np
@@ -115,3 +116,29 @@ def test_interface_upper_matches_numpy(orc):
     # a short output buffer still gets the count
     assert orc.lib().orc_interface_upper(I(NI), I(NJ), I(NK), P(phi), D(0.1), D(0.2), D(1.6), P(xz),
                                          ctypes.c_int(1)) == n
+
+
+def test_interface_lower_known_positions(orc):
+    """find_interface_positions_lower.f90:15-32 (the adjoint's objective): on each
+    wall row k of phi slice 0 (j = 1) a profile falling linearly through 0.5 at a
+    chosen x0_k (cell centres at (i - 1/2) dx, clipped to [0, 1]) is found at x0_k
+    exactly by the linear interpolation between the first pair of cells that
+    brackets 0.5, less the reference's 0.75 xl shift; a row that never crosses
+    counts as 0; J = -(mean over the rows).  Rows of the other j and the other
+    slices do not enter."""
+    dx, xl = 0.125, NI * 0.125
+    rng = np.random.default_rng(21)
+    phi = rng.random(SH)  # noise everywhere but the wall row
+    x0 = 0.3 * xl + rng.uniform(-0.4, 0.4, NK) * dx * 3
+    xc = (np.arange(-2, NI + 4) - 0.5) * dx
+    want = []
+    for k in range(NK):
+        if k == 2:
+            phi[k + 3, 3, :] = 1.0  # no crossing on this row
+            want.append(0.0)
+            continue
+        slope = rng.uniform(0.1, 0.45) / dx  # the two bracketing cells stay inside [0, 1]
+        phi[k + 3, 3, :] = np.clip(0.5 - slope * (xc - x0[k]), 0.0, 1.0)
+        want.append(x0[k] - 0.75 * xl)
+    J = orc.lib().orc_interface_lower(orc.I(NI), orc.I(NJ), orc.I(NK), orc.P(phi), orc.D(dx), orc.D(xl))
+    assert abs(J - (-np.mean(want))) <= 1e-14, (J, -np.mean(want))
