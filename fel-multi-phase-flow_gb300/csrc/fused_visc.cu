@@ -141,9 +141,10 @@ __global__ void __launch_bounds__(256) k_src_ab(Grid g, VP p, SrcIn in, const do
 // pair, A and B rounded to doubles once).  The FP64-accurate step (FMF_FP64E, REFINE
 // false) stores them.  The mixed-precision step (REFINE true) forms the first-sweep
 // residual R = A visn(u) + B - u from them in FP64, as k_src_ab<true> does: the
-// viscous sum visn reads 20 doubles for about 25 operations, which splitting into
-// pairs makes dearer (measured), while its FP64 instructions overlap the pair
-// arithmetic of A and B on the FP32 pipe.  The momentum-factor denominator is
+// viscous sum visn reads 20 doubles for about 25 operations, and with it in pairs
+// as well the kernel measured 10.2 ms against 9.7 for k_src_ab<true> at
+// 512x256x256 (the splits cost more than the FP64 operations they replace); in
+// this form, 6.7 ms.  The momentum-factor denominator is
 // grouped as dz2 (e(-Z) + e(0)) + dy2 (e(-Y) + e(0)) + 2 dx2 (mu(0) + mu(X)) (and
 // likewise per component), the same sum.
 struct VPS {
@@ -269,9 +270,9 @@ __global__ void __launch_bounds__(256) k_div_stress(Grid g, double dxi, double d
   vw[c] = (a5 - __ldg(t5 + c - X)) * dxi + (a6 - __ldg(t6 + c - Y)) * dyi + (__ldg(t3 + c + Z) - __ldg(t3 + c)) * dzi;
 }
 
-// The FP64-accurate step (FMF_FP64E): k_stress and k_div_stress in FP32-pair
-// arithmetic (each double read split into a pair, each output rounded to a double
-// once); the same sums in the same grouping.
+// The FP64-accurate and mixed-precision steps: k_stress and k_div_stress in
+// FP32-pair arithmetic (each double read split into a pair, each output rounded to
+// a double once); the same sums in the same grouping.
 // With sk (the adjoint's record of a mixed-precision step) the strain components
 // are written as well, in FP64 as k_stress forms them.
 struct VPT {
