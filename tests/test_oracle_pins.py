@@ -122,7 +122,11 @@ def test_single_phase_slip_couette_is_steady(orc):
 
 
 def test_poisson_residual_roundoff(orc):
-    """solp_fft_tdma4: the FFT+TDMA solution satisfies the 7-point Poisson equation."""
+    """The FFT+TDMA solution (solp_fft_tdma1-3 with cal_coef_prs/cal_coef_solp_fft)
+    satisfies the 7-point Poisson equation: by the reference's own monitor
+    (solp_fft_tdma4), and by the operator written here in numpy (periodic in x and z,
+    closed wall faces at j = 1 and nj), to 1e-11 of the right-hand side (measured
+    8e-16; a periodic y operator misses by 0.57)."""
     cfg = C.Config("p", 32, 16, 16, 2.0, 1.0, 1.0, dt=1e-3, steps=1)
     lib = orc.lib()
     rng = np.random.default_rng(5)
@@ -155,6 +159,18 @@ def test_poisson_residual_roundoff(orc):
     lib.orc_solp_fft_tdma4_v(I(cfg.ni), I(cfg.nj), I(cfg.nk), D(rho), D(1 / cfg.dx), D(1 / cfg.dy), D(1 / cfg.dz),
                              P(div), P(dp), e, e0)
     assert e[0] / e0[0] < 1e-12
+    # the same equation written here: the 7-point operator over rho, periodic in x
+    # and z, the wall faces closed at j = 1 and j = nj (cal_coef_prs.f's fold), on the
+    # interior of dp, against the right-hand side
+    q = dp[3:-3, 3:-3, 3:-3]
+    lap = (np.roll(q, -1, 2) - 2 * q + np.roll(q, 1, 2)) / cfg.dx ** 2
+    lap += (np.roll(q, -1, 0) - 2 * q + np.roll(q, 1, 0)) / cfg.dz ** 2
+    up = np.zeros_like(q)
+    up[:, :-1, :] = q[:, 1:, :] - q[:, :-1, :]  # (j+1) - j, closed at j = nj
+    dn = np.zeros_like(q)
+    dn[:, 1:, :] = q[:, 1:, :] - q[:, :-1, :]  # j - (j-1), closed at j = 1
+    lap += (up - dn) / cfg.dy ** 2
+    assert np.abs(lap / rho - d).max() <= 1e-11 * np.abs(d).max()
 
 
 def _grads_p2a(orc, cfg, phi):
