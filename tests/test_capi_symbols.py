@@ -53,3 +53,13 @@ def test_load_fails_loudly_without_library(tmp_path):
             capi.load(str(tmp_path / "absent.so"))
     finally:
         capi._lib = saved
+
+
+def test_python_constants_match_the_header():
+    """The ctypes binding's precision, residency and status values are the header's."""
+    from fmf import capi
+    text = open(HDR).read()
+    vals = {m.group(1): int(m.group(2)) for m in re.finditer(r"\b(FMF_[A-Z0-9_]+)\s*=\s*(\d+)", text)}
+    for name in ("FMF_FP64", "FMF_MIXED", "FMF_FP64E", "FMF_RESIDENT", "FMF_COHERENT", "FMF_ERR_ITER_CAP"):
+        assert name in vals, name
+        assert getattr(capi, name) == vals[name], name
